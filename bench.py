@@ -1,0 +1,383 @@
+"""Benchmark: HDG diffusion-source time-to-solve on GB300.
+
+Workload (default, one GPU): 3D HDG diffusion-source on the unit cube, 40^3
+cubes x 6 tetrahedra = 384,000 tets, p = 3, manufactured u = prod sin(pi x),
+tau = 1, kappa = 1, Dirichlet from u. One step = the whole hot path with the
+mesh and fields resident on the device: element assembly + static
+condensation + Dirichlet + scatter into the trace system, the Krylov solve to
+the stated tolerance, and local recovery of Solution and Flux.
+
+value = elements per second of that step (elements / time-to-solve), device
+time from CUDA events on the library's stream. e2e = the same through the C
+ABI with host buffers: the field uploads (Tau, Dirichlet) and the downloads of
+Trace, Solution and Flux are inside the timed region.
+
+Inputs are far larger than L2 (element blocks ~15 GB, trace matrix ~4 GB), so
+no L2 flush is needed between steps.
+
+--impl reference times the CPU oracle (C++ restatement of HyperFox's path:
+per-element dense assembly + LU condensation, CSR scatter, GMRES(30)+Jacobi,
+recovery) on the host cores with all threads, on a bounded sample of the same
+workload (a sub-cube of the same element type and order).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "time-to-solve @1e-8 rel err, learned+mixed vs plain FP64 GPU; elements/s"
+
+CONFIGS = {
+    # name: dim, n (cubes per side), order
+    "cfg2": dict(dim=3, n=40, order=3, desc="3D HDG diffusion-source, unit cube 40^3x6 tets (384k), p=3"),
+    "cfg1": dict(dim=2, n=32, order=2, desc="2D HDG diffusion-source, unit square 32x32x2 tris (2048), p=2"),
+    "small3d": dict(dim=3, n=12, order=3, desc="3D HDG diffusion-source, 12^3x6 tets, p=3"),
+    "cfg5mesh": dict(dim=3, n=60, order=2, desc="3D HDG diffusion-source, 60^3x6 tets (1.296M), p=2"),
+}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_problem(cfg):
+    from hyperfox_gb300 import capi, meshgen
+    dim, n, p = cfg["dim"], cfg["n"], cfg["order"]
+    re = capi.refel(dim, p)
+    v, s = meshgen.square_simplices(n) if dim == 2 else meshgen.cube_simplices(n)
+    coords, cells = meshgen.high_order(v, s, re["nodes"])
+    return coords, cells
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("HFX_BENCH_GLOO") is None else "gloo")
+    return world, rank, local
+
+
+def barrier_max(world, value):
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    from hyperfox_gb300 import capi
+    torch.cuda.set_device(local)
+    cfg = CONFIGS[args.config]
+    dim, p = cfg["dim"], cfg["order"]
+    t0 = time.time()
+    coords, cells = make_problem(cfg)
+    ctx = capi.Context(local)
+    ctx.upload_mesh(dim, p, coords, cells)
+    t_setup = time.time() - t0
+    _, _, faces, _ = ctx.topology()
+    Nf = ctx.re["nNodesFace"]
+    # pinned host buffers for the per-step inputs and results (e2e)
+    pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    tau_h = pin((ctx.nFaces, Nf))
+    tau_h[:] = 1.0
+    dir_h = pin((ctx.nFaces, Nf))
+    dir_h[:] = np.prod(np.sin(np.pi * coords[faces]), axis=-1)
+    trace_h = pin(ctx.ndofs)
+    sol_h = pin((ctx.nCells, ctx.lenU))
+    flux_h = pin((ctx.nCells, ctx.lenQ))
+    ctx.set_tau(tau_h)
+    ctx.set_dirichlet(dir_h)
+    ctx.set_source(capi.SRC_SINPROD, param=dim * np.pi ** 2)
+    L = ctx.L
+    prec = capi.PREC_MIXED if args.precision == "mixed" else capi.PREC_FP64
+    opts = capi.solve_opts(precision=prec, rtol=args.rtol, precond=capi.PC_BLOCK_JACOBI, maxits=200000,
+                           inner_rtol=args.inner_rtol)
+    info = capi.SolveInfo()
+
+    def step_device():
+        ctx._chk(L.hfx_assemble(ctx.h), "assemble")
+        ctx._chk(L.hfx_solve(ctx.h, capi.ctypes.byref(opts), None, capi.ctypes.byref(info)), "solve")
+        ctx._chk(L.hfx_recover(ctx.h, None, None), "recover")
+
+    def step_e2e():
+        ctx.set_tau(tau_h)
+        ctx.set_dirichlet(dir_h)
+        ctx._chk(L.hfx_assemble(ctx.h), "assemble")
+        ctx._chk(L.hfx_solve(ctx.h, capi.ctypes.byref(opts), capi._p(trace_h), capi.ctypes.byref(info)), "solve")
+        ctx._chk(L.hfx_recover(ctx.h, capi._p(sol_h), capi._p(flux_h)), "recover")
+
+    # accuracy reference: plain FP64 CG to 1e-13 (untimed)
+    ctx.assemble()
+    ref_opts = capi.solve_opts(precision=capi.PREC_FP64, rtol=1e-13, precond=capi.PC_BLOCK_JACOBI, maxits=500000)
+    ref_info = capi.SolveInfo()
+    x_ref = np.zeros(ctx.ndofs)
+    ctx._chk(L.hfx_solve(ctx.h, capi.ctypes.byref(ref_opts), capi._p(x_ref), capi.ctypes.byref(ref_info)), "ref solve")
+    for _ in range(args.warmup):
+        step_device()
+    # device-resident timed region
+    barrier(world)
+    ctx._chk(L.hfx_synchronize(ctx.h), "sync")
+    clocks = ClockSampler(local)
+    clocks.start()
+    ctx._chk(L.hfx_profile_enable(ctx.h, 1), "profile")
+    ctx._chk(L.hfx_mark(ctx.h, 0), "mark")
+    for _ in range(args.steps):
+        step_device()
+    ctx._chk(L.hfx_mark(ctx.h, 1), "mark")
+    ms = capi.ctypes.c_double()
+    ctx._chk(L.hfx_elapsed_ms(ctx.h, 0, 1, capi.ctypes.byref(ms)), "elapsed")
+    clk = clocks.stop()
+    dev_ms = barrier_max(world, ms.value)
+    kt = {}
+    for name, kid in (("local", 0), ("scatter", 1), ("spmv64", 2), ("spmv32", 3), ("update", 4), ("recover", 5),
+                      ("other", 6)):
+        n_l, t_l = capi.ctypes.c_int(), capi.ctypes.c_double()
+        L.hfx_kernel_time(ctx.h, kid, capi.ctypes.byref(n_l), capi.ctypes.byref(t_l))
+        kt[name] = (n_l.value, t_l.value)
+    ctx._chk(L.hfx_profile_enable(ctx.h, 0), "profile")
+    iters, refinements = info.iterations, info.refinements
+    # accuracy of the last solve vs the FP64 reference
+    x = np.zeros(ctx.ndofs)
+    ctx._chk(L.hfx_solve(ctx.h, capi.ctypes.byref(opts), capi._p(x), capi.ctypes.byref(info)), "solve")
+    rel_err = float(np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref))
+    # e2e timed region (host buffers, copies inside)
+    barrier(world)
+    ctx._chk(L.hfx_synchronize(ctx.h), "sync")
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_e2e()
+    ctx._chk(L.hfx_synchronize(ctx.h), "sync")
+    e2e_s = barrier_max(world, time.perf_counter() - t0)
+    h2d = tau_h.nbytes + dir_h.nbytes
+    d2h = trace_h.nbytes + sol_h.nbytes + flux_h.nbytes
+    # plain FP64 GPU time-to-solve (same tolerance), for the learned+mixed vs plain comparison
+    plain = None
+    if args.precision == "mixed" and not args.no_plain:
+        fp_opts = capi.solve_opts(precision=capi.PREC_FP64, rtol=args.rtol, precond=capi.PC_BLOCK_JACOBI, maxits=500000)
+        fp_info = capi.SolveInfo()
+        ctx._chk(L.hfx_mark(ctx.h, 2), "mark")
+        for _ in range(max(1, args.plain_steps)):
+            ctx._chk(L.hfx_assemble(ctx.h), "assemble")
+            ctx._chk(L.hfx_solve(ctx.h, capi.ctypes.byref(fp_opts), None, capi.ctypes.byref(fp_info)), "solve")
+            ctx._chk(L.hfx_recover(ctx.h, None, None), "recover")
+        ctx._chk(L.hfx_mark(ctx.h, 3), "mark")
+        pms = capi.ctypes.c_double()
+        ctx._chk(L.hfx_elapsed_ms(ctx.h, 2, 3, capi.ctypes.byref(pms)), "elapsed")
+        plain = dict(time_to_solve_s=pms.value / 1e3 / max(1, args.plain_steps), iterations=fp_info.iterations)
+    E = ctx.nCells
+    step_s = dev_ms / 1e3 / args.steps
+    # roofline of the dominant kernel
+    hbm, peak_kind = peaks()
+    nnz, n = ctx.nnz, ctx.ndofs
+    nblocks = nnz // (Nf * Nf)
+    dom = max(("local", "spmv64", "spmv32", "update", "scatter", "recover"), key=lambda k: kt[k][1])
+    roof = None
+    if dom in ("spmv32", "spmv64"):
+        sv = 4 if dom == "spmv32" else 8
+        # values once, block columns + row pointers once, z and p_old gathered once, p_new and q written
+        alg = nnz * sv + nblocks * 4 + (ctx.nFaces + 1) * 8 + 4 * n * sv
+        launches = kt[dom][0]
+        avg_ms = kt[dom][1] / max(1, launches)
+        achieved = alg / (avg_ms / 1e3) / 1e9
+        roof = dict(bound="hbm", kernel="cg_spmv<%s>" % ("float" if sv == 4 else "double"),
+                    achieved=round(achieved, 1), peak=hbm, unit="GB/s", frac=round(achieved / hbm, 4),
+                    traffic=None, bytes_per_launch=int(alg), avg_launch_ms=round(avg_ms, 4), peak_source=peak_kind)
+    elif dom == "local":
+        LU, LQ, LL = ctx.lenU, ctx.lenQ, ctx.lenL
+        alg = E * ((ctx.re["nNodes"] * dim + ctx.re["nNodes"]) * 8 + (LL * LL + LL + (LU + LQ) * (LL + 1)) * 8)
+        avg_ms = kt["local"][1] / max(1, kt["local"][0])
+        achieved = alg / (avg_ms / 1e3) / 1e9
+        roof = dict(bound="hbm", kernel="local_condense_f64", achieved=round(achieved, 1), peak=hbm, unit="GB/s",
+                    frac=round(achieved / hbm, 4), traffic=None, bytes_per_launch=int(alg),
+                    avg_launch_ms=round(avg_ms, 4), peak_source=peak_kind,
+                    note="FP64-pipe bound on GB300; HBM fraction shown")
+    if args.traffic and roof is not None:
+        roof["traffic"] = args.traffic
+    res = {
+        "metric": METRIC,
+        "value": E / step_s,
+        "unit": "elements/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": step_s * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64+f32" if prec else "f64",
+        "data": "synthetic (seedless structured mesh, manufactured solution)",
+        "config": {"workload": cfg["desc"], "elements": E, "order": p, "trace_dofs": n, "csr_nnz": nnz,
+                   "precision": args.precision, "preconditioner": "block-Jacobi (per face)",
+                   "rtol": args.rtol, "l2_flush": "inputs > L2 (no flush needed)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "time_to_solve_s": step_s,
+        "assembly_elements_per_s": E / (kt["local"][1] / 1e3 / max(1, kt["local"][0])) if kt["local"][0] else None,
+        "krylov_iterations": iters,
+        "refinements": refinements,
+        "rel_err_vs_fp64": rel_err,
+        "fp64_reference_iterations": ref_info.iterations,
+        "plain_fp64": plain,
+        "kernel_ms": {k: dict(launches=v[0], total_ms=round(v[1], 3)) for k, v in kt.items()},
+        "roofline": roof,
+        "clocks": clk,
+        "e2e": {"value": E * args.steps / e2e_s, "unit": "elements/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(sum(v[0] for v in kt.values())),
+        "setup_s": t_setup,
+    }
+    if plain:
+        res["speedup_vs_plain_fp64"] = plain["time_to_solve_s"] / step_s
+    return res, ctx
+
+
+def cpu_sample(cfg_name, nthreads, budget_elems=None):
+    """Time the CPU oracle on a bounded sample: a sub-cube of the same workload."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import _oracle as O
+    from hyperfox_gb300 import meshgen
+    cfg = CONFIGS[cfg_name]
+    dim, p = cfg["dim"], cfg["order"]
+    n = {3: 12, 2: 32}[dim] if budget_elems is None else budget_elems
+    n = min(n, cfg["n"])
+    re = O.RefEl(dim, p)
+    v, s = meshgen.square_simplices(n) if dim == 2 else meshgen.cube_simplices(n)
+    coords, cells = meshgen.high_order(v, s, re.nodes)
+    P = O.Problem(dim, p, coords, cells)
+    g = np.prod(np.sin(np.pi * coords[P.faces]), axis=-1)
+    P.set_fields(np.ones(P.ndofs), src_mode=2, dirichlet=g.ravel())
+    t0 = time.perf_counter()
+    P.assemble(nthreads)
+    x, it = P.solve_gmres(1e-10, 200000, nthreads)
+    P.recover(x)
+    dt = time.perf_counter() - t0
+    return dict(value=P.nCells / dt, unit="elements/s", cores=nthreads, kind="port",
+                sample="%s sub-mesh n=%d (%d elements, %d trace DOFs): oracle assemble+condense+scatter, "
+                       "GMRES(30)+Jacobi to 1e-10 (%d its), recovery" % (cfg_name, n, P.nCells, P.ndofs, it),
+                seconds=dt)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="cfg2", choices=sorted(CONFIGS))
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--rtol", type=float, default=1e-10)
+    ap.add_argument("--inner-rtol", type=float, default=1e-4)
+    ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--traffic", type=float, default=None, help="ncu DRAM bytes per launch of the top kernel")
+    args = ap.parse_args()
+    world, rank, local = dist_init()
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        nthreads = os.cpu_count() or 1
+        vals = []
+        for i in range(args.warmup + args.steps):
+            r = cpu_sample(args.config, nthreads)
+            if i >= args.warmup:
+                vals.append(r["value"])
+        v = statistics.median(vals)
+        out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "elements/s", "n_gpus": world,
+               "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+               "config": {"workload": CONFIGS[args.config]["desc"]},
+               "cpu_baseline": dict(r, value=v),
+               "e2e": {"value": v, "unit": "elements/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(out))
+        return
+    res, ctx = run_ours(args, world, rank, local)
+    if rank == 0:
+        if not args.no_cpu:
+            try:
+                res["cpu_baseline"] = cpu_sample(args.config, os.cpu_count() or 1)
+            except Exception as e:  # the baseline is reported, not required
+                res["cpu_baseline"] = {"error": str(e)}
+        print(json.dumps(res))
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()

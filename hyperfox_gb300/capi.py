@@ -1,0 +1,343 @@
+"""ctypes binding of the C ABI (include/hfx_gb300.h) and a small host-side
+mirror of HyperFox's HDGSolver for Python callers, tests and the bench.
+
+The library is the in-tree ``_lib/libhfx_gb300.so``; loading fails loudly if
+it has not been built (there is no CPU fallback).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_lib", "libhfx_gb300.so")
+
+HFX_OK = 0
+HFX_ERR_ARG = 1
+HFX_ERR_STATE = 2
+HFX_ERR_CUDA = 3
+HFX_ERR_ALLOC = 4
+HFX_ERR_NOT_CONVERGED = 5
+HFX_ERR_BREAKDOWN = 6
+HFX_ERR_NAN = 7
+HFX_ERR_SINGULAR = 8
+HFX_ERR_UNSUPPORTED = 9
+
+KSP_CG, KSP_GMRES = 0, 1
+PC_NONE, PC_JACOBI, PC_BLOCK_JACOBI = 0, 1, 2
+PREC_FP64, PREC_MIXED = 0, 1
+SRC_NONE, SRC_VALUES, SRC_SINPROD = 0, 1, 2
+
+# Every symbol include/hfx_gb300.h declares.
+EXPORTED = [
+    "hfx_ctx_create", "hfx_ctx_destroy", "hfx_last_error", "hfx_version",
+    "hfx_refel_query", "hfx_refel_tables",
+    "hfx_mesh_upload", "hfx_mesh_sizes", "hfx_mesh_topology", "hfx_mesh_compute_topology",
+    "hfx_set_tau", "hfx_set_kappa", "hfx_set_source", "hfx_set_dirichlet", "hfx_set_time_scheme",
+    "hfx_ip_coords", "hfx_assemble", "hfx_get_condensed", "hfx_get_csr",
+    "hfx_solve_opts_default", "hfx_solve", "hfx_recover",
+    "hfx_la_create", "hfx_la_destroy", "hfx_la_allocate", "hfx_la_set_values", "hfx_la_set_rhs",
+    "hfx_la_zero_rows", "hfx_la_assemble", "hfx_la_clear", "hfx_la_solve", "hfx_la_nnz",
+]
+
+
+class HfxError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("hfx error %d: %s" % (code, msg))
+        self.code = code
+
+
+class RefElInfo(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ("dim", "order", "nNodes", "nFaces", "nNodesFace", "nIP", "nIPFace")]
+
+
+class SolveOpts(ctypes.Structure):
+    _fields_ = [("method", ctypes.c_int), ("precond", ctypes.c_int), ("precision", ctypes.c_int),
+                ("rtol", ctypes.c_double), ("maxits", ctypes.c_int), ("restart", ctypes.c_int),
+                ("inner_rtol", ctypes.c_double), ("use_initial_guess", ctypes.c_int)]
+
+
+class SolveInfo(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("iterations", ctypes.c_int), ("refinements", ctypes.c_int),
+                ("rel_residual", ctypes.c_double), ("solve_ms", ctypes.c_double)]
+
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load the CUDA library (raises if it is missing: no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError("libhfx_gb300.so is not built (run __graft_entry__.build()): %s" % path)
+    L = ctypes.CDLL(path)
+    vp, ip, dp = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    sig = {
+        "hfx_ctx_create": ([ip, ctypes.POINTER(vp)], ip),
+        "hfx_ctx_destroy": ([vp], ip),
+        "hfx_last_error": ([vp], ctypes.c_char_p),
+        "hfx_version": ([], ip),
+        "hfx_refel_query": ([ip, ip, ctypes.POINTER(RefElInfo)], ip),
+        "hfx_refel_tables": ([ip, ip] + [vp] * 10, ip),
+        "hfx_mesh_upload": ([vp, ip, ip, ip, vp, ip, vp, ip, vp, vp, vp, ip, vp], ip),
+        "hfx_mesh_sizes": ([vp, vp, vp, vp], ip),
+        "hfx_mesh_topology": ([vp] * 5, ip),
+        "hfx_mesh_compute_topology": ([ip, ip, ip, vp, vp, vp, vp, vp, vp, vp], ip),
+        "hfx_set_tau": ([vp, vp, ip], ip),
+        "hfx_set_kappa": ([vp, vp, ip, ip], ip),
+        "hfx_set_source": ([vp, ip, vp, dp], ip),
+        "hfx_set_dirichlet": ([vp, vp], ip),
+        "hfx_set_time_scheme": ([vp, dp, vp], ip),
+        "hfx_ip_coords": ([vp, vp], ip),
+        "hfx_assemble": ([vp], ip),
+        "hfx_get_condensed": ([vp] * 7, ip),
+        "hfx_get_csr": ([vp] * 5, ip),
+        "hfx_solve_opts_default": ([ctypes.POINTER(SolveOpts)], None),
+        "hfx_solve": ([vp, ctypes.POINTER(SolveOpts), vp, ctypes.POINTER(SolveInfo)], ip),
+        "hfx_recover": ([vp, vp, vp], ip),
+        "hfx_la_create": ([vp, ctypes.POINTER(vp)], ip),
+        "hfx_la_destroy": ([vp], ip),
+        "hfx_la_allocate": ([vp, ip], ip),
+        "hfx_la_set_values": ([vp, ip, vp, ip, vp, vp, ip], ip),
+        "hfx_la_set_rhs": ([vp, ip, vp, vp, ip], ip),
+        "hfx_la_zero_rows": ([vp, ip, vp], ip),
+        "hfx_la_assemble": ([vp], ip),
+        "hfx_la_clear": ([vp], ip),
+        "hfx_la_solve": ([vp, ctypes.POINTER(SolveOpts), vp, ctypes.POINTER(SolveInfo)], ip),
+        "hfx_la_nnz": ([vp, vp], ip),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def refel(dim, order):
+    """Reference-element tables from the library (host only, no GPU)."""
+    L = load()
+    info = RefElInfo()
+    rc = L.hfx_refel_query(dim, order, ctypes.byref(info))
+    if rc:
+        raise HfxError(rc, "refel_query(%d, %d)" % (dim, order))
+    N, F, Nf, nI, nIf = info.nNodes, info.nFaces, info.nNodesFace, info.nIP, info.nIPFace
+    t = dict(nodes=np.zeros((N, dim)), faceNodes=np.zeros((F, Nf), np.int32), ipX=np.zeros((nI, dim)),
+             ipW=np.zeros(nI), phi=np.zeros((nI, N)), dphi=np.zeros((nI, N, dim)),
+             fIpX=np.zeros((nIf, dim - 1)), fIpW=np.zeros(nIf), fPhi=np.zeros((nIf, Nf)),
+             fDphi=np.zeros((nIf, Nf, dim - 1)))
+    rc = L.hfx_refel_tables(dim, order, *[_p(t[k]) for k in ("nodes", "faceNodes", "ipX", "ipW", "phi", "dphi",
+                                                              "fIpX", "fIpW", "fPhi", "fDphi")])
+    if rc:
+        raise HfxError(rc, "refel_tables")
+    t.update(dim=dim, order=order, nNodes=N, nFaces=F, nNodesFace=Nf, nIP=nI, nIPFace=nIf)
+    return t
+
+
+def mesh_topology(dim, order, cells):
+    """Face topology by the MOAB creation-order rule (host only, no GPU)."""
+    L = load()
+    cells = np.ascontiguousarray(cells, np.int32)
+    nf, nb = ctypes.c_int(), ctypes.c_int()
+    rc = L.hfx_mesh_compute_topology(dim, order, cells.shape[0], _p(cells), ctypes.byref(nf), ctypes.byref(nb),
+                                     None, None, None, None)
+    if rc:
+        raise HfxError(rc, "mesh_compute_topology")
+    F = dim + 1
+    Nf = refel(dim, order)["nNodesFace"]
+    c2f = np.zeros((cells.shape[0], F), np.int32)
+    f2c = np.zeros((nf.value, 2), np.int32)
+    faces = np.zeros((nf.value, Nf), np.int32)
+    bnd = np.zeros(nb.value, np.int32)
+    rc = L.hfx_mesh_compute_topology(dim, order, cells.shape[0], _p(cells), ctypes.byref(nf), ctypes.byref(nb),
+                                     _p(c2f), _p(f2c), _p(faces), _p(bnd))
+    if rc:
+        raise HfxError(rc, "mesh_compute_topology")
+    return c2f, f2c, faces, bnd
+
+
+def solve_opts(**kw):
+    o = SolveOpts()
+    load().hfx_solve_opts_default(ctypes.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+class Context:
+    """One device context (one stream) holding one HDG problem."""
+
+    def __init__(self, device=0):
+        L = load()
+        h = ctypes.c_void_p()
+        rc = L.hfx_ctx_create(device, ctypes.byref(h))
+        if rc:
+            raise HfxError(rc, "ctx_create(device=%d)" % device)
+        self.h = h
+        self.L = L
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.hfx_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _chk(self, rc, what):
+        if rc:
+            raise HfxError(rc, "%s: %s" % (what, self.L.hfx_last_error(self.h).decode()))
+
+    # ---- mesh and fields
+    def upload_mesh(self, dim, order, coords, cells, topology=None):
+        coords = np.ascontiguousarray(coords, np.float64)
+        cells = np.ascontiguousarray(cells, np.int32)
+        self._keep = (coords, cells)
+        if topology is None:
+            rc = self.L.hfx_mesh_upload(self.h, dim, order, coords.shape[0], _p(coords), cells.shape[0], _p(cells),
+                                        0, None, None, None, 0, None)
+        else:
+            c2f, f2c, faces, bnd = [np.ascontiguousarray(a, np.int32) for a in topology]
+            rc = self.L.hfx_mesh_upload(self.h, dim, order, coords.shape[0], _p(coords), cells.shape[0], _p(cells),
+                                        faces.shape[0], _p(c2f), _p(f2c), _p(faces), bnd.size, _p(bnd))
+        self._chk(rc, "mesh_upload")
+        self.dim, self.order = dim, order
+        self.re = refel(dim, order)
+        self.nCells = cells.shape[0]
+        nf, nb, nnz = ctypes.c_int(), ctypes.c_int(), ctypes.c_int64()
+        self._chk(self.L.hfx_mesh_sizes(self.h, ctypes.byref(nf), ctypes.byref(nb), ctypes.byref(nnz)), "mesh_sizes")
+        self.nFaces, self.nBoundary, self.nnz = nf.value, nb.value, nnz.value
+        self.ndofs = self.nFaces * self.re["nNodesFace"]
+        self.lenU = self.re["nNodes"]
+        self.lenQ = dim * self.re["nNodes"]
+        self.lenL = self.re["nFaces"] * self.re["nNodesFace"]
+
+    def topology(self):
+        F, Nf = self.re["nFaces"], self.re["nNodesFace"]
+        c2f = np.zeros((self.nCells, F), np.int32)
+        f2c = np.zeros((self.nFaces, 2), np.int32)
+        faces = np.zeros((self.nFaces, Nf), np.int32)
+        bnd = np.zeros(self.nBoundary, np.int32)
+        self._chk(self.L.hfx_mesh_topology(self.h, _p(c2f), _p(f2c), _p(faces), _p(bnd)), "mesh_topology")
+        return c2f, f2c, faces, bnd
+
+    def set_tau(self, tau):
+        tau = np.ascontiguousarray(tau, np.float64)
+        nvals = tau.size // self.ndofs
+        self._chk(self.L.hfx_set_tau(self.h, _p(tau), nvals), "set_tau")
+
+    def set_kappa(self, kappa, layout=1):
+        if kappa is None:
+            self._chk(self.L.hfx_set_kappa(self.h, None, 0, 0), "set_kappa")
+            return
+        kappa = np.ascontiguousarray(kappa, np.float64)
+        rows = self.nCells * self.re["nNodes"] if layout == 1 else None
+        comps = kappa.size // rows if rows else kappa.shape[-1]
+        self._chk(self.L.hfx_set_kappa(self.h, _p(kappa), comps, layout), "set_kappa")
+
+    def set_source(self, mode, values=None, param=0.0):
+        v = None if values is None else np.ascontiguousarray(values, np.float64)
+        self._chk(self.L.hfx_set_source(self.h, mode, _p(v), float(param)), "set_source")
+
+    def set_dirichlet(self, values):
+        v = np.ascontiguousarray(values, np.float64)
+        self._chk(self.L.hfx_set_dirichlet(self.h, _p(v)), "set_dirichlet")
+
+    def set_time_scheme(self, dt, u_old=None):
+        v = None if u_old is None else np.ascontiguousarray(u_old, np.float64)
+        self._chk(self.L.hfx_set_time_scheme(self.h, float(dt), _p(v)), "set_time_scheme")
+
+    def ip_coords(self):
+        out = np.zeros((self.nCells, self.re["nIP"], self.dim))
+        self._chk(self.L.hfx_ip_coords(self.h, _p(out)), "ip_coords")
+        return out
+
+    # ---- hot path
+    def assemble(self):
+        self._chk(self.L.hfx_assemble(self.h), "assemble")
+
+    def condensed(self):
+        E, U, Q, Ll = self.nCells, self.lenU, self.lenQ, self.lenL
+        out = dict(S=np.zeros((E, Ll * Ll)), S0=np.zeros((E, Ll)), U=np.zeros((E, U * Ll)), Q=np.zeros((E, Q * Ll)),
+                   U0=np.zeros((E, U)), Q0=np.zeros((E, Q)))
+        self._chk(self.L.hfx_get_condensed(self.h, *[_p(out[k]) for k in ("S", "S0", "U", "Q", "U0", "Q0")]),
+                  "get_condensed")
+        return out
+
+    def csr(self):
+        rowptr = np.zeros(self.ndofs + 1, np.int64)
+        col = np.zeros(self.nnz, np.int32)
+        val = np.zeros(self.nnz)
+        rhs = np.zeros(self.ndofs)
+        self._chk(self.L.hfx_get_csr(self.h, _p(rowptr), _p(col), _p(val), _p(rhs)), "get_csr")
+        return rowptr, col, val, rhs
+
+    def solve(self, want_trace=True, **opts):
+        o = solve_opts(**opts)
+        info = SolveInfo()
+        trace = np.zeros(self.ndofs) if want_trace else None
+        rc = self.L.hfx_solve(self.h, ctypes.byref(o), _p(trace), ctypes.byref(info))
+        self._chk(rc, "solve")
+        return trace, info
+
+    def recover(self):
+        sol = np.zeros((self.nCells, self.lenU))
+        flux = np.zeros((self.nCells, self.lenQ))
+        self._chk(self.L.hfx_recover(self.h, _p(sol), _p(flux)), "recover")
+        return sol, flux
+
+
+class LinearSystem:
+    """hfx_la_* handle (LinAlgebraInterface drop-in on the device)."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+        h = ctypes.c_void_p()
+        ctx._chk(ctx.L.hfx_la_create(ctx.h, ctypes.byref(h)), "la_create")
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.ctx.L.hfx_la_destroy(self.h)
+            self.h = None
+
+    def allocate(self, n):
+        self.n = n
+        self.ctx._chk(self.ctx.L.hfx_la_allocate(self.h, n), "la_allocate")
+
+    def values(self, rows, cols, vals, insert=False):
+        r = np.ascontiguousarray(rows, np.int32)
+        c = np.ascontiguousarray(cols, np.int32)
+        v = np.ascontiguousarray(vals, np.float64)
+        self.ctx._chk(self.ctx.L.hfx_la_set_values(self.h, r.size, _p(r), c.size, _p(c), _p(v), int(insert)),
+                      "la_set_values")
+
+    def rhs(self, idx, vals, insert=False):
+        i = np.ascontiguousarray(idx, np.int32)
+        v = np.ascontiguousarray(vals, np.float64)
+        self.ctx._chk(self.ctx.L.hfx_la_set_rhs(self.h, i.size, _p(i), _p(v), int(insert)), "la_set_rhs")
+
+    def zero_rows(self, rows):
+        r = np.ascontiguousarray(rows, np.int32)
+        self.ctx._chk(self.ctx.L.hfx_la_zero_rows(self.h, r.size, _p(r)), "la_zero_rows")
+
+    def assemble(self):
+        self.ctx._chk(self.ctx.L.hfx_la_assemble(self.h), "la_assemble")
+
+    def clear(self):
+        self.ctx._chk(self.ctx.L.hfx_la_clear(self.h), "la_clear")
+
+    def solve(self, **opts):
+        kw = dict(method=KSP_GMRES, precond=PC_JACOBI)
+        kw.update(opts)
+        o = solve_opts(**kw)
+        info = SolveInfo()
+        x = np.zeros(self.n)
+        self.ctx._chk(self.ctx.L.hfx_la_solve(self.h, ctypes.byref(o), _p(x), ctypes.byref(info)), "la_solve")
+        return x, info

@@ -1,0 +1,825 @@
+// C ABI of the GB300 HDG hot path (declared in include/hfx_gb300.h).
+//
+// The context owns every device buffer and one CUDA stream. Host arrays are
+// copied in; results are copied out into caller buffers, as HyperFox writes
+// into Field::getValues()->data().
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/hfx_gb300.h"
+#include "hfx_device.h"
+#include "hfx_host.h"
+#include "krylov.h"
+#include "la_gmres.h"
+#include "timer.h"
+
+using namespace hfx;
+
+namespace {
+
+struct DevMem {
+  std::vector<void*> ptrs;
+  ~DevMem() { release(); }
+  void release() {
+    for (void* p : ptrs) cudaFree(p);
+    ptrs.clear();
+  }
+};
+
+// A field's device buffer, reallocated only when it must grow.
+struct FieldBuf {
+  double* p = nullptr;
+  size_t cap = 0;
+  ~FieldBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  cudaError_t set(const double* h, size_t n, cudaStream_t s) {
+    if (n > cap) {
+      cudaStreamSynchronize(s);
+      release();
+      cudaError_t e = cudaMalloc(&p, sizeof(double) * (n > 0 ? n : 1));
+      if (e != cudaSuccess) {
+        p = nullptr;
+        return e;
+      }
+      cap = n;
+    }
+    return n ? cudaMemcpyAsync(p, h, sizeof(double) * n, cudaMemcpyHostToDevice, s) : cudaSuccess;
+  }
+};
+
+}  // namespace
+
+struct hfx_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // mesh and tables
+  bool haveMesh = false;
+  int dim = 0, order = 0, nNodes = 0, nCells = 0;
+  RefEl re;
+  Topology topo;
+  BlockPattern bp;
+  std::vector<uint8_t> perm;
+  DevMem meshMem;
+  double* d_tab = nullptr;
+  int* d_itab = nullptr;
+  double* d_phi = nullptr;
+  double* d_coords = nullptr;
+  int* d_cells = nullptr;
+  int* d_cell2face = nullptr;
+  uint8_t* d_perm = nullptr;
+  int* d_face2cell = nullptr;
+  uint8_t* d_isBnd = nullptr;
+  int64_t* d_browptr = nullptr;
+  int* d_bcol = nullptr;
+  int* d_brow = nullptr;
+  int *d_src0 = nullptr, *d_src1 = nullptr;
+  uint8_t *d_loc0 = nullptr, *d_loc1 = nullptr;
+  // fields
+  FieldBuf tau, kappa, src, dir, uold;
+  int tauVals = 1;
+  int kc = 0, kLayout = 0;
+  int srcMode = 0;
+  double srcParam = 0.0;
+  double dt = 0.0;
+  // outputs
+  DevMem outMem;
+  double *d_S = nullptr, *d_S0 = nullptr, *d_U = nullptr, *d_Q = nullptr, *d_U0 = nullptr, *d_Q0 = nullptr;
+  double *d_val = nullptr, *d_rhs = nullptr, *d_trace = nullptr, *d_sol = nullptr, *d_flux = nullptr;
+  int* d_status = nullptr;
+  bool assembled = false, solved = false;
+  // solver workspace
+  DevMem wsMem;
+  TraceWorkspace ws{};
+  bool wsReady = false, wsMixed = false;
+  // timing
+  KernelTimer timer;
+  cudaEvent_t marks[8] = {};
+
+  int64_t nnz() const { return bp.rowptr.empty() ? 0 : bp.rowptr.back() * re.nNodesFace * re.nNodesFace; }
+  int64_t ndofs() const { return (int64_t)topo.nFaces * re.nNodesFace; }
+};
+
+struct hfx_la {
+  hfx_ctx* ctx;
+  LaSystem sys;
+};
+
+namespace {
+
+int set_err(hfx_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cuda_err(hfx_ctx* c, cudaError_t e, const char* where) {
+  return set_err(c, e == cudaErrorMemoryAllocation ? HFX_ERR_ALLOC : HFX_ERR_CUDA,
+                 std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+template <typename T>
+cudaError_t dalloc(DevMem& m, T** p, size_t count) {
+  void* ptr = nullptr;
+  cudaError_t e = cudaMalloc(&ptr, sizeof(T) * (count > 0 ? count : 1));
+  if (e != cudaSuccess) return e;
+  m.ptrs.push_back(ptr);
+  *p = (T*)ptr;
+  return cudaSuccess;
+}
+
+template <typename T>
+cudaError_t upload(DevMem& m, T** p, const T* host, size_t count, cudaStream_t s) {
+  cudaError_t e = dalloc(m, p, count);
+  if (e != cudaSuccess || count == 0) return e;
+  return cudaMemcpyAsync(*p, host, sizeof(T) * count, cudaMemcpyHostToDevice, s);
+}
+
+#define HFX_CUDA(c, call)                              \
+  do {                                                 \
+    cudaError_t e_ = (call);                           \
+    if (e_ != cudaSuccess) return cuda_err(c, e_, #call); \
+  } while (0)
+
+void free_outputs(hfx_ctx* c) {
+  cudaStreamSynchronize(c->stream);
+  c->outMem.release();
+  c->wsMem.release();
+  c->d_S = c->d_S0 = c->d_U = c->d_Q = c->d_U0 = c->d_Q0 = c->d_val = c->d_rhs = c->d_trace = nullptr;
+  c->d_sol = c->d_flux = nullptr;
+  c->d_status = nullptr;
+  c->wsReady = false;
+  c->assembled = c->solved = false;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hfx_version(void) { return 100; }
+
+int hfx_ctx_create(int device, hfx_ctx** out) {
+  if (!out) return HFX_ERR_ARG;
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) return HFX_ERR_CUDA;
+  if (device < 0 || device >= n) return HFX_ERR_ARG;
+  if ((e = cudaSetDevice(device)) != cudaSuccess) return HFX_ERR_CUDA;
+  std::unique_ptr<hfx_ctx> c(new hfx_ctx());
+  c->device = device;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return HFX_ERR_CUDA;
+  *out = c.release();
+  return HFX_OK;
+}
+
+int hfx_ctx_destroy(hfx_ctx* c) {
+  if (!c) return HFX_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  c->wsMem.release();
+  c->outMem.release();
+  c->tau.release();
+  c->kappa.release();
+  c->src.release();
+  c->dir.release();
+  c->uold.release();
+  c->meshMem.release();
+  c->timer.reset();
+  for (auto& e : c->marks)
+    if (e) cudaEventDestroy(e);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return HFX_OK;
+}
+
+const char* hfx_last_error(const hfx_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int hfx_refel_query(int dim, int order, hfx_refel_info* info) {
+  if (!info) return HFX_ERR_ARG;
+  RefEl r;
+  std::string err;
+  if (!build_refel(dim, order, &r, &err)) return HFX_ERR_ARG;
+  *info = {r.dim, r.order, r.nNodes, r.nFaces, r.nNodesFace, r.nIP, r.nIPFace};
+  return HFX_OK;
+}
+
+int hfx_refel_tables(int dim, int order, double* nodes, int* faceNodes, double* ipCoords, double* ipWeights,
+                     double* phi, double* dphi, double* fIpCoords, double* fIpWeights, double* fPhi,
+                     double* fDphi) {
+  RefEl r;
+  std::string err;
+  if (!build_refel(dim, order, &r, &err)) return HFX_ERR_ARG;
+  auto cp = [](double* dst, const std::vector<double>& v) {
+    if (dst) std::copy(v.begin(), v.end(), dst);
+  };
+  cp(nodes, r.nodes);
+  if (faceNodes) std::copy(r.faceNodes.begin(), r.faceNodes.end(), faceNodes);
+  cp(ipCoords, r.ipX);
+  cp(ipWeights, r.ipW);
+  cp(phi, r.phi);
+  cp(dphi, r.dphi);
+  cp(fIpCoords, r.fIpX);
+  cp(fIpWeights, r.fIpW);
+  cp(fPhi, r.fPhi);
+  cp(fDphi, r.fDphi);
+  return HFX_OK;
+}
+
+int hfx_mesh_upload(hfx_ctx* c, int dim, int order, int nNodes, const double* coords, int nCells, const int* cells,
+                    int nFaces, const int* cell2face, const int* face2cell, const int* faces, int nBoundary,
+                    const int* boundary) {
+  if (!c) return HFX_ERR_ARG;
+  if (!coords || !cells || nNodes <= 0 || nCells <= 0) return set_err(c, HFX_ERR_ARG, "mesh_upload: empty mesh");
+  cudaSetDevice(c->device);
+  std::string err;
+  RefEl re;
+  if (!build_refel(dim, order, &re, &err)) return set_err(c, HFX_ERR_ARG, err);
+  if (!local_condense_supported(dim, order))
+    return set_err(c, HFX_ERR_ARG, "mesh_upload: element (dim, order) not built (2D p<=5, 3D p<=3)");
+  const int N = re.nNodes, F = re.nFaces, Nf = re.nNodesFace;
+  for (int64_t i = 0; i < (int64_t)nCells * N; ++i)
+    if (cells[i] < 0 || cells[i] >= nNodes) return set_err(c, HFX_ERR_ARG, "mesh_upload: cell node index out of range");
+  Topology topo;
+  if (cell2face) {
+    if (!face2cell || !faces || nFaces <= 0 || (nBoundary > 0 && !boundary))
+      return set_err(c, HFX_ERR_ARG, "mesh_upload: incomplete topology");
+    topo.nFaces = nFaces;
+    topo.cell2face.assign(cell2face, cell2face + (int64_t)nCells * F);
+    topo.face2cell.assign(face2cell, face2cell + 2 * (int64_t)nFaces);
+    topo.faces.assign(faces, faces + (int64_t)nFaces * Nf);
+    if (nBoundary > 0) topo.boundary.assign(boundary, boundary + nBoundary);
+    for (int v : topo.cell2face)
+      if (v < 0 || v >= nFaces) return set_err(c, HFX_ERR_ARG, "mesh_upload: cell2face out of range");
+  } else if (!compute_topology(re, nCells, cells, &topo, &err)) {
+    return set_err(c, HFX_ERR_ARG, err);
+  }
+  std::vector<uint8_t> perm;
+  if (!compute_face_perm(re, nCells, cells, topo, &perm, &err)) return set_err(c, HFX_ERR_ARG, err);
+  BlockPattern bp;
+  if (!compute_block_pattern(re, nCells, topo, &bp, &err)) return set_err(c, HFX_ERR_ARG, err);
+  // release previous state
+  free_outputs(c);
+  c->meshMem.release();
+  c->re = std::move(re);
+  c->topo = std::move(topo);
+  c->bp = std::move(bp);
+  c->perm = std::move(perm);
+  c->dim = dim;
+  c->order = order;
+  c->nNodes = nNodes;
+  c->nCells = nCells;
+  cudaStream_t s = c->stream;
+  DevMem& m = c->meshMem;
+  // packed tables: phi, dphi, w, fphi, fdphi, fw
+  std::vector<double> tab;
+  tab.insert(tab.end(), c->re.phi.begin(), c->re.phi.end());
+  tab.insert(tab.end(), c->re.dphi.begin(), c->re.dphi.end());
+  tab.insert(tab.end(), c->re.ipW.begin(), c->re.ipW.end());
+  tab.insert(tab.end(), c->re.fPhi.begin(), c->re.fPhi.end());
+  tab.insert(tab.end(), c->re.fDphi.begin(), c->re.fDphi.end());
+  tab.insert(tab.end(), c->re.fIpW.begin(), c->re.fIpW.end());
+  std::vector<int> itab(c->re.faceNodes);
+  itab.insert(itab.end(), c->re.faceOpposite.begin(), c->re.faceOpposite.end());
+  std::vector<uint8_t> isBnd(c->topo.nFaces, 0);
+  for (int f : c->topo.boundary) isBnd[f] = 1;
+  HFX_CUDA(c, upload(m, &c->d_tab, tab.data(), tab.size(), s));
+  HFX_CUDA(c, upload(m, &c->d_itab, itab.data(), itab.size(), s));
+  HFX_CUDA(c, upload(m, &c->d_phi, c->re.phi.data(), c->re.phi.size(), s));
+  HFX_CUDA(c, upload(m, &c->d_coords, coords, (size_t)nNodes * dim, s));
+  HFX_CUDA(c, upload(m, &c->d_cells, cells, (size_t)nCells * N, s));
+  HFX_CUDA(c, upload(m, &c->d_cell2face, c->topo.cell2face.data(), c->topo.cell2face.size(), s));
+  HFX_CUDA(c, upload(m, &c->d_perm, c->perm.data(), c->perm.size(), s));
+  HFX_CUDA(c, upload(m, &c->d_face2cell, c->topo.face2cell.data(), c->topo.face2cell.size(), s));
+  HFX_CUDA(c, upload(m, &c->d_isBnd, isBnd.data(), isBnd.size(), s));
+  HFX_CUDA(c, upload(m, &c->d_browptr, c->bp.rowptr.data(), c->bp.rowptr.size(), s));
+  HFX_CUDA(c, upload(m, &c->d_bcol, c->bp.col.data(), c->bp.col.size(), s));
+  HFX_CUDA(c, upload(m, &c->d_src0, c->bp.src0.data(), c->bp.src0.size(), s));
+  HFX_CUDA(c, upload(m, &c->d_src1, c->bp.src1.data(), c->bp.src1.size(), s));
+  HFX_CUDA(c, upload(m, &c->d_loc0, c->bp.loc0.data(), c->bp.loc0.size(), s));
+  HFX_CUDA(c, upload(m, &c->d_loc1, c->bp.loc1.data(), c->bp.loc1.size(), s));
+  HFX_CUDA(c, dalloc(m, &c->d_brow, c->bp.col.size()));
+  HFX_CUDA(c, launch_block_rows(c->d_browptr, c->topo.nFaces, c->d_brow, s));
+  // default fields: tau = 1, Dirichlet = 0, kappa = identity, no source
+  std::vector<double> ones((size_t)c->topo.nFaces * Nf, 1.0), zeros((size_t)c->topo.nFaces * Nf, 0.0);
+  c->tauVals = 1;
+  HFX_CUDA(c, c->tau.set(ones.data(), ones.size(), s));
+  HFX_CUDA(c, c->dir.set(zeros.data(), zeros.size(), s));
+  c->kc = 0;
+  c->srcMode = 0;
+  c->dt = 0.0;
+  HFX_CUDA(c, cudaStreamSynchronize(s));
+  c->haveMesh = true;
+  return HFX_OK;
+}
+
+int hfx_mesh_compute_topology(int dim, int order, int nCells, const int* cells, int* nFaces, int* nBoundary,
+                              int* cell2face, int* face2cell, int* faces, int* boundary) {
+  if (!cells || nCells <= 0 || !nFaces || !nBoundary) return HFX_ERR_ARG;
+  RefEl re;
+  std::string err;
+  if (!build_refel(dim, order, &re, &err)) return HFX_ERR_ARG;
+  Topology t;
+  if (!compute_topology(re, nCells, cells, &t, &err)) return HFX_ERR_ARG;
+  *nFaces = t.nFaces;
+  *nBoundary = (int)t.boundary.size();
+  if (cell2face) std::copy(t.cell2face.begin(), t.cell2face.end(), cell2face);
+  if (face2cell) std::copy(t.face2cell.begin(), t.face2cell.end(), face2cell);
+  if (faces) std::copy(t.faces.begin(), t.faces.end(), faces);
+  if (boundary) std::copy(t.boundary.begin(), t.boundary.end(), boundary);
+  return HFX_OK;
+}
+
+int hfx_mesh_sizes(hfx_ctx* c, int* nFaces, int* nBoundary, int64_t* nnz) {
+  if (!c) return HFX_ERR_ARG;
+  if (!c->haveMesh) return set_err(c, HFX_ERR_STATE, "mesh_sizes: no mesh");
+  if (nFaces) *nFaces = c->topo.nFaces;
+  if (nBoundary) *nBoundary = (int)c->topo.boundary.size();
+  if (nnz) *nnz = c->nnz();
+  return HFX_OK;
+}
+
+int hfx_mesh_topology(hfx_ctx* c, int* cell2face, int* face2cell, int* faces, int* boundary) {
+  if (!c) return HFX_ERR_ARG;
+  if (!c->haveMesh) return set_err(c, HFX_ERR_STATE, "mesh_topology: no mesh");
+  if (cell2face) std::copy(c->topo.cell2face.begin(), c->topo.cell2face.end(), cell2face);
+  if (face2cell) std::copy(c->topo.face2cell.begin(), c->topo.face2cell.end(), face2cell);
+  if (faces) std::copy(c->topo.faces.begin(), c->topo.faces.end(), faces);
+  if (boundary) std::copy(c->topo.boundary.begin(), c->topo.boundary.end(), boundary);
+  return HFX_OK;
+}
+
+static int replace_field(hfx_ctx* c, FieldBuf* dst, const double* src, size_t n) {
+  HFX_CUDA(c, dst->set(src, n, c->stream));
+  c->assembled = false;
+  return HFX_OK;
+}
+
+int hfx_set_tau(hfx_ctx* c, const double* tau, int nVals) {
+  if (!c) return HFX_ERR_ARG;
+  if (!c->haveMesh) return set_err(c, HFX_ERR_STATE, "set_tau: upload a mesh first");
+  if (!tau || (nVals != 1 && nVals != 2)) return set_err(c, HFX_ERR_ARG, "set_tau: Tau needs 1 or 2 values per face node");
+  c->tauVals = nVals;
+  return replace_field(c, &c->tau, tau, (size_t)c->topo.nFaces * c->re.nNodesFace * nVals);
+}
+
+int hfx_set_kappa(hfx_ctx* c, const double* kappa, int comps, int layout) {
+  if (!c) return HFX_ERR_ARG;
+  if (!c->haveMesh) return set_err(c, HFX_ERR_STATE, "set_kappa: upload a mesh first");
+  if (comps == 0) {
+    c->kc = 0;
+    c->assembled = false;
+    return HFX_OK;
+  }
+  if (!kappa || (comps != 1 && comps != c->dim * c->dim) || (layout != 0 && layout != 1))
+    return set_err(c, HFX_ERR_ARG, "set_kappa: the diffusion tensor must be scalar or dim x dim");
+  c->kc = comps;
+  c->kLayout = layout;
+  size_t n = (layout == 0 ? (size_t)c->nNodes : (size_t)c->nCells * c->re.nNodes) * comps;
+  return replace_field(c, &c->kappa, kappa, n);
+}
+
+int hfx_set_source(hfx_ctx* c, int mode, const double* values, double param) {
+  if (!c) return HFX_ERR_ARG;
+  if (!c->haveMesh) return set_err(c, HFX_ERR_STATE, "set_source: upload a mesh first");
+  if (mode < HFX_SRC_NONE || mode > HFX_SRC_SINPROD) return set_err(c, HFX_ERR_ARG, "set_source: unknown mode");
+  c->srcMode = mode;
+  c->srcParam = param;
+  c->assembled = false;
+  if (mode == HFX_SRC_VALUES) {
+    if (!values) return set_err(c, HFX_ERR_ARG, "set_source: values required");
+    return replace_field(c, &c->src, values, (size_t)c->nCells * c->re.nIP);
+  }
+  return HFX_OK;
+}
+
+int hfx_set_dirichlet(hfx_ctx* c, const double* values) {
+  if (!c) return HFX_ERR_ARG;
+  if (!c->haveMesh) return set_err(c, HFX_ERR_STATE, "set_dirichlet: upload a mesh first");
+  if (!values) return set_err(c, HFX_ERR_ARG, "set_dirichlet: values required");
+  return replace_field(c, &c->dir, values, (size_t)c->topo.nFaces * c->re.nNodesFace);
+}
+
+int hfx_set_time_scheme(hfx_ctx* c, double dt, const double* uOld) {
+  if (!c) return HFX_ERR_ARG;
+  if (!c->haveMesh) return set_err(c, HFX_ERR_STATE, "set_time_scheme: upload a mesh first");
+  if (dt < 0.0 || (dt > 0.0 && !uOld)) return set_err(c, HFX_ERR_ARG, "set_time_scheme: dt >= 0 and the old Solution");
+  c->dt = dt;
+  c->assembled = false;
+  if (dt > 0.0) return replace_field(c, &c->uold, uOld, (size_t)c->nCells * c->re.nNodes);
+  return HFX_OK;
+}
+
+int hfx_ip_coords(hfx_ctx* c, double* out) {
+  if (!c || !out) return HFX_ERR_ARG;
+  if (!c->haveMesh) return set_err(c, HFX_ERR_STATE, "ip_coords: upload a mesh first");
+  size_t n = (size_t)c->nCells * c->re.nIP * c->dim;
+  double* d = nullptr;
+  DevMem tmp;
+  HFX_CUDA(c, dalloc(tmp, &d, n));
+  IpCoordParams p{c->nCells, c->re.nNodes, c->re.nIP, c->dim, c->d_coords, c->d_cells, c->d_phi, d};
+  HFX_CUDA(c, launch_ip_coords(p, c->stream));
+  HFX_CUDA(c, cudaMemcpyAsync(out, d, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+  HFX_CUDA(c, cudaStreamSynchronize(c->stream));
+  return HFX_OK;
+}
+
+static int ensure_outputs(hfx_ctx* c) {
+  if (c->d_S) return HFX_OK;
+  const int64_t E = c->nCells;
+  const int LU = c->re.nNodes, LQ = c->dim * c->re.nNodes, LL = c->re.nFaces * c->re.nNodesFace;
+  DevMem& m = c->outMem;
+  HFX_CUDA(c, dalloc(m, &c->d_S, (size_t)E * LL * LL));
+  HFX_CUDA(c, dalloc(m, &c->d_S0, (size_t)E * LL));
+  HFX_CUDA(c, dalloc(m, &c->d_U, (size_t)E * LU * LL));
+  HFX_CUDA(c, dalloc(m, &c->d_Q, (size_t)E * LQ * LL));
+  HFX_CUDA(c, dalloc(m, &c->d_U0, (size_t)E * LU));
+  HFX_CUDA(c, dalloc(m, &c->d_Q0, (size_t)E * LQ));
+  HFX_CUDA(c, dalloc(m, &c->d_val, (size_t)c->nnz()));
+  HFX_CUDA(c, dalloc(m, &c->d_rhs, (size_t)c->ndofs()));
+  HFX_CUDA(c, dalloc(m, &c->d_trace, (size_t)c->ndofs()));
+  HFX_CUDA(c, dalloc(m, &c->d_status, 1));
+  HFX_CUDA(c, dalloc(m, &c->d_sol, (size_t)E * LU));
+  HFX_CUDA(c, dalloc(m, &c->d_flux, (size_t)E * LQ));
+  HFX_CUDA(c, cudaMemsetAsync(c->d_trace, 0, sizeof(double) * c->ndofs(), c->stream));
+  return HFX_OK;
+}
+
+int hfx_assemble(hfx_ctx* c) {
+  if (!c) return HFX_ERR_ARG;
+  if (!c->haveMesh) return set_err(c, HFX_ERR_STATE, "assemble: upload a mesh first");
+  cudaSetDevice(c->device);
+  int rc = ensure_outputs(c);
+  if (rc) return rc;
+  cudaStream_t s = c->stream;
+  HFX_CUDA(c, cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
+  LocalParams p{};
+  p.nCells = c->nCells;
+  p.coords = c->d_coords;
+  p.cells = c->d_cells;
+  p.cell2face = c->d_cell2face;
+  p.perm = c->d_perm;
+  p.face2cell = c->d_face2cell;
+  p.isBoundary = c->d_isBnd;
+  p.tau = c->tau.p;
+  p.tauVals = c->tauVals;
+  p.kappa = c->kappa.p;
+  p.kc = c->kc;
+  p.kappaLayout = c->kLayout;
+  p.srcMode = c->srcMode;
+  p.src = c->src.p;
+  p.srcParam = c->srcParam;
+  p.dirichlet = c->dir.p;
+  p.dt = c->dt;
+  p.uOld = c->uold.p;
+  p.tab = c->d_tab;
+  p.itab = c->d_itab;
+  p.S = c->d_S;
+  p.S0 = c->d_S0;
+  p.U = c->d_U;
+  p.Q = c->d_Q;
+  p.U0 = c->d_U0;
+  p.Q0 = c->d_Q0;
+  p.status = c->d_status;
+  c->timer.begin(K_LOCAL, s);
+  HFX_CUDA(c, launch_local_condense(c->dim, c->order, p, s));
+  c->timer.end(K_LOCAL, s);
+  ScatterParams sp{};
+  sp.nFaces = c->topo.nFaces;
+  sp.NF = c->re.nNodesFace;
+  sp.LL = c->re.nFaces * c->re.nNodesFace;
+  sp.browptr = c->d_browptr;
+  sp.brow = c->d_brow;
+  sp.nBlocks = (int64_t)c->bp.col.size();
+  sp.src0 = c->d_src0;
+  sp.src1 = c->d_src1;
+  sp.loc0 = c->d_loc0;
+  sp.loc1 = c->d_loc1;
+  sp.perm = c->d_perm;
+  sp.S = c->d_S;
+  sp.S0 = c->d_S0;
+  sp.cell2face = c->d_cell2face;
+  sp.face2cell = c->d_face2cell;
+  sp.F = c->re.nFaces;
+  sp.val = c->d_val;
+  sp.rhs = c->d_rhs;
+  c->timer.begin(K_SCATTER, s);
+  HFX_CUDA(c, launch_scatter(sp, s));
+  c->timer.end(K_SCATTER, s);
+  int status = 0;
+  HFX_CUDA(c, cudaMemcpyAsync(&status, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  HFX_CUDA(c, cudaStreamSynchronize(s));
+  if (status != 0) return set_err(c, HFX_ERR_SINGULAR, "assemble: singular element block in condensation");
+  c->assembled = true;
+  c->solved = false;
+  return HFX_OK;
+}
+
+int hfx_get_condensed(hfx_ctx* c, double* S, double* S0, double* U, double* Q, double* U0, double* Q0) {
+  if (!c) return HFX_ERR_ARG;
+  if (!c->assembled) return set_err(c, HFX_ERR_STATE, "get_condensed: assemble first");
+  const int64_t E = c->nCells;
+  const int LU = c->re.nNodes, LQ = c->dim * c->re.nNodes, LL = c->re.nFaces * c->re.nNodesFace;
+  cudaStream_t s = c->stream;
+  auto cp = [&](double* h, const double* d, size_t n) {
+    return h ? cudaMemcpyAsync(h, d, sizeof(double) * n, cudaMemcpyDeviceToHost, s) : cudaSuccess;
+  };
+  HFX_CUDA(c, cp(S, c->d_S, (size_t)E * LL * LL));
+  HFX_CUDA(c, cp(S0, c->d_S0, (size_t)E * LL));
+  HFX_CUDA(c, cp(U, c->d_U, (size_t)E * LU * LL));
+  HFX_CUDA(c, cp(Q, c->d_Q, (size_t)E * LQ * LL));
+  HFX_CUDA(c, cp(U0, c->d_U0, (size_t)E * LU));
+  HFX_CUDA(c, cp(Q0, c->d_Q0, (size_t)E * LQ));
+  HFX_CUDA(c, cudaStreamSynchronize(s));
+  return HFX_OK;
+}
+
+int hfx_get_csr(hfx_ctx* c, int64_t* rowptr, int* col, double* val, double* rhs) {
+  if (!c) return HFX_ERR_ARG;
+  if (!c->assembled && (val || rhs)) return set_err(c, HFX_ERR_STATE, "get_csr: assemble first");
+  if (!c->haveMesh) return set_err(c, HFX_ERR_STATE, "get_csr: no mesh");
+  const int NF = c->re.nNodesFace;
+  const int nF = c->topo.nFaces;
+  if (rowptr || col) {
+    int64_t pos = 0;
+    if (rowptr) rowptr[0] = 0;
+    for (int f = 0; f < nF; ++f) {
+      int64_t b0 = c->bp.rowptr[f], nb = c->bp.rowptr[f + 1] - b0;
+      for (int a = 0; a < NF; ++a) {
+        if (col)
+          for (int64_t k = 0; k < nb; ++k)
+            for (int b = 0; b < NF; ++b) col[pos + k * NF + b] = c->bp.col[b0 + k] * NF + b;
+        pos += nb * NF;
+        if (rowptr) rowptr[(int64_t)f * NF + a + 1] = pos;
+      }
+    }
+  }
+  cudaStream_t s = c->stream;
+  if (val) HFX_CUDA(c, cudaMemcpyAsync(val, c->d_val, sizeof(double) * c->nnz(), cudaMemcpyDeviceToHost, s));
+  if (rhs) HFX_CUDA(c, cudaMemcpyAsync(rhs, c->d_rhs, sizeof(double) * c->ndofs(), cudaMemcpyDeviceToHost, s));
+  HFX_CUDA(c, cudaStreamSynchronize(s));
+  return HFX_OK;
+}
+
+void hfx_solve_opts_default(hfx_solve_opts* o) {
+  if (!o) return;
+  o->method = HFX_KSP_CG;
+  o->precond = HFX_PC_BLOCK_JACOBI;
+  o->precision = HFX_PREC_FP64;
+  o->rtol = 1e-10;
+  o->maxits = 20000;
+  o->restart = 30;
+  o->inner_rtol = 1e-4;
+  o->use_initial_guess = 0;
+}
+
+static int ensure_workspace(hfx_ctx* c, bool mixed) {
+  if (c->wsReady && (!mixed || c->wsMixed)) return HFX_OK;
+  const size_t n = (size_t)c->ndofs(), nnz = (size_t)c->nnz();
+  const int NF = c->re.nNodesFace;
+  DevMem& m = c->wsMem;
+  TraceWorkspace& w = c->ws;
+  if (!c->wsReady) {
+    HFX_CUDA(c, dalloc(m, &w.bS, n));
+    HFX_CUDA(c, dalloc(m, &w.r, n));
+    HFX_CUDA(c, dalloc(m, &w.z, n));
+    HFX_CUDA(c, dalloc(m, &w.p0, n));
+    HFX_CUDA(c, dalloc(m, &w.p1, n));
+    HFX_CUDA(c, dalloc(m, &w.q, n));
+    HFX_CUDA(c, dalloc(m, &w.pc64, (size_t)c->topo.nFaces * NF * NF));
+    HFX_CUDA(c, dalloc(m, &w.partials, trace_partials_needed()));
+    HFX_CUDA(c, dalloc(m, &w.state, 1));
+    HFX_CUDA(c, cudaMemsetAsync(w.p0, 0, sizeof(double) * n, c->stream));
+    HFX_CUDA(c, cudaMemsetAsync(w.p1, 0, sizeof(double) * n, c->stream));
+    c->wsReady = true;
+  }
+  if (mixed && !c->wsMixed) {
+    HFX_CUDA(c, dalloc(m, &w.val32, nnz));
+    HFX_CUDA(c, dalloc(m, &w.pc32, (size_t)c->topo.nFaces * NF * NF));
+    HFX_CUDA(c, dalloc(m, &w.r32, n));
+    HFX_CUDA(c, dalloc(m, &w.z32, n));
+    HFX_CUDA(c, dalloc(m, &w.p032, n));
+    HFX_CUDA(c, dalloc(m, &w.p132, n));
+    HFX_CUDA(c, dalloc(m, &w.q32, n));
+    HFX_CUDA(c, dalloc(m, &w.d32, n));
+    HFX_CUDA(c, dalloc(m, &w.rhs32, n));
+    HFX_CUDA(c, cudaMemsetAsync(w.p032, 0, sizeof(float) * n, c->stream));
+    HFX_CUDA(c, cudaMemsetAsync(w.p132, 0, sizeof(float) * n, c->stream));
+    c->wsMixed = true;
+  }
+  return HFX_OK;
+}
+
+int hfx_solve(hfx_ctx* c, const hfx_solve_opts* opts, double* trace, hfx_solve_info* info) {
+  if (!c) return HFX_ERR_ARG;
+  if (!c->assembled) return set_err(c, HFX_ERR_STATE, "solve: system must be assembled before solving");
+  hfx_solve_opts o;
+  if (opts) o = *opts;
+  else hfx_solve_opts_default(&o);
+  if (o.method != HFX_KSP_CG) return set_err(c, HFX_ERR_UNSUPPORTED, "solve: the trace system solve is CG (use hfx_la for GMRES)");
+  if (o.precond < HFX_PC_NONE || o.precond > HFX_PC_BLOCK_JACOBI || o.rtol <= 0.0 || o.maxits <= 0)
+    return set_err(c, HFX_ERR_ARG, "solve: bad options");
+  cudaSetDevice(c->device);
+  bool mixed = o.precision == HFX_PREC_MIXED;
+  int rc = ensure_workspace(c, mixed);
+  if (rc) return rc;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, c->stream);
+  TraceSolveArgs a{};
+  a.dim = c->dim;
+  a.A = TraceView{c->topo.nFaces, c->re.nNodesFace, c->d_browptr, c->d_bcol, c->d_isBnd};
+  a.val = c->d_val;
+  a.rhs = c->d_rhs;
+  a.x = c->d_trace;
+  a.precond = o.precond;
+  a.mixed = mixed;
+  a.rtol = o.rtol;
+  a.inner_rtol = o.inner_rtol > 0 ? o.inner_rtol : 1e-4;
+  a.maxits = o.maxits;
+  a.max_refinements = 50;
+  a.check_every = 25;
+  a.use_initial_guess = o.use_initial_guess;
+  a.ws = c->ws;
+  a.stream = c->stream;
+  a.timer = &c->timer;
+  TraceSolveResult res;
+  int st = trace_solve(a, &res);
+  cudaEventRecord(e1, c->stream);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (info) {
+    info->status = st;
+    info->iterations = res.iterations;
+    info->refinements = res.refinements;
+    info->rel_residual = res.rel_residual;
+    info->solve_ms = ms;
+  }
+  if (st == 3) return cuda_err(c, res.cudaErr, "solve");
+  if (trace) HFX_CUDA(c, cudaMemcpy(trace, c->d_trace, sizeof(double) * c->ndofs(), cudaMemcpyDeviceToHost));
+  c->solved = true;
+  if (st == HFX_ERR_NOT_CONVERGED) return set_err(c, st, "solve: not converged within maxits");
+  if (st == HFX_ERR_BREAKDOWN) return set_err(c, st, "solve: CG breakdown (non-positive curvature)");
+  if (st == HFX_ERR_NAN) return set_err(c, st, "solve: NaN or Inf in the Krylov iteration");
+  if (st != 0) return set_err(c, st, "solve: failed");
+  return HFX_OK;
+}
+
+int hfx_recover(hfx_ctx* c, double* solution, double* flux) {
+  if (!c) return HFX_ERR_ARG;
+  if (!c->solved) return set_err(c, HFX_ERR_STATE, "recover: solve first");
+  cudaSetDevice(c->device);
+  const int LU = c->re.nNodes, LQ = c->dim * c->re.nNodes, LL = c->re.nFaces * c->re.nNodesFace;
+  const int64_t E = c->nCells;
+  RecoverParams p{c->nCells, c->re.nFaces, c->re.nNodesFace, LU, LQ, LL, c->d_cell2face, c->d_perm,
+                  c->d_U, c->d_Q, c->d_U0, c->d_Q0, c->d_trace, c->d_sol, c->d_flux};
+  c->timer.begin(K_RECOVER, c->stream);
+  HFX_CUDA(c, launch_recover(p, c->stream));
+  c->timer.end(K_RECOVER, c->stream);
+  // NULL outputs keep Solution and Flux on the device only
+  if (solution) HFX_CUDA(c, cudaMemcpyAsync(solution, c->d_sol, sizeof(double) * E * LU, cudaMemcpyDeviceToHost, c->stream));
+  if (flux) HFX_CUDA(c, cudaMemcpyAsync(flux, c->d_flux, sizeof(double) * E * LQ, cudaMemcpyDeviceToHost, c->stream));
+  HFX_CUDA(c, cudaStreamSynchronize(c->stream));
+  return HFX_OK;
+}
+
+int hfx_profile_enable(hfx_ctx* c, int on) {
+  if (!c) return HFX_ERR_ARG;
+  cudaStreamSynchronize(c->stream);
+  c->timer.reset();
+  c->timer.enable(on != 0);
+  return HFX_OK;
+}
+
+int hfx_kernel_time(hfx_ctx* c, int kernel, int* launches, double* ms) {
+  if (!c || !launches || !ms || kernel < 0 || kernel >= K_COUNT) return HFX_ERR_ARG;
+  c->timer.read(kernel, launches, ms);
+  return HFX_OK;
+}
+
+int hfx_mark(hfx_ctx* c, int slot) {
+  if (!c || slot < 0 || slot >= 8) return HFX_ERR_ARG;
+  if (!c->marks[slot]) HFX_CUDA(c, cudaEventCreate(&c->marks[slot]));
+  HFX_CUDA(c, cudaEventRecord(c->marks[slot], c->stream));
+  return HFX_OK;
+}
+
+int hfx_elapsed_ms(hfx_ctx* c, int slot0, int slot1, double* ms) {
+  if (!c || !ms || slot0 < 0 || slot0 >= 8 || slot1 < 0 || slot1 >= 8 || !c->marks[slot0] || !c->marks[slot1])
+    return HFX_ERR_ARG;
+  HFX_CUDA(c, cudaEventSynchronize(c->marks[slot1]));
+  float x = 0.f;
+  HFX_CUDA(c, cudaEventElapsedTime(&x, c->marks[slot0], c->marks[slot1]));
+  *ms = x;
+  return HFX_OK;
+}
+
+int hfx_synchronize(hfx_ctx* c) {
+  if (!c) return HFX_ERR_ARG;
+  HFX_CUDA(c, cudaStreamSynchronize(c->stream));
+  return HFX_OK;
+}
+
+// ---- generic sparse system --------------------------------------------------
+int hfx_la_create(hfx_ctx* c, hfx_la** out) {
+  if (!c || !out) return HFX_ERR_ARG;
+  *out = new hfx_la{c, LaSystem()};
+  return HFX_OK;
+}
+
+int hfx_la_destroy(hfx_la* la) {
+  delete la;
+  return HFX_OK;
+}
+
+int hfx_la_allocate(hfx_la* la, int ndofs) {
+  if (!la) return HFX_ERR_ARG;
+  if (ndofs <= 0) return set_err(la->ctx, HFX_ERR_ARG, "la_allocate: ndofs must be positive");
+  la->sys.allocate(ndofs);
+  return HFX_OK;
+}
+
+int hfx_la_set_values(hfx_la* la, int nr, const int* rows, int nc, const int* cols, const double* vals, int insert) {
+  if (!la) return HFX_ERR_ARG;
+  if (!la->sys.allocated()) return set_err(la->ctx, HFX_ERR_STATE, "la_set_values: allocate first");
+  std::string err;
+  if (!la->sys.add_block(nr, rows, nc, cols, vals, insert != 0, &err)) return set_err(la->ctx, HFX_ERR_ARG, err);
+  return HFX_OK;
+}
+
+int hfx_la_set_rhs(hfx_la* la, int n, const int* idx, const double* vals, int insert) {
+  if (!la) return HFX_ERR_ARG;
+  if (!la->sys.allocated()) return set_err(la->ctx, HFX_ERR_STATE, "la_set_rhs: allocate first");
+  std::string err;
+  if (!la->sys.add_rhs(n, idx, vals, insert != 0, &err)) return set_err(la->ctx, HFX_ERR_ARG, err);
+  return HFX_OK;
+}
+
+int hfx_la_zero_rows(hfx_la* la, int n, const int* rows) {
+  if (!la) return HFX_ERR_ARG;
+  if (!la->sys.allocated()) return set_err(la->ctx, HFX_ERR_STATE, "la_zero_rows: allocate first");
+  std::string err;
+  if (!la->sys.zero_rows(n, rows, &err)) return set_err(la->ctx, HFX_ERR_ARG, err);
+  return HFX_OK;
+}
+
+int hfx_la_assemble(hfx_la* la) {
+  if (!la) return HFX_ERR_ARG;
+  if (!la->sys.allocated()) return set_err(la->ctx, HFX_ERR_STATE, "la_assemble: allocate first");
+  la->sys.assemble();
+  return HFX_OK;
+}
+
+int hfx_la_clear(hfx_la* la) {
+  if (!la) return HFX_ERR_ARG;
+  if (!la->sys.assembled()) return set_err(la->ctx, HFX_ERR_STATE, "la_clear: assemble at least once first");
+  la->sys.clear();
+  return HFX_OK;
+}
+
+int hfx_la_nnz(hfx_la* la, int64_t* nnz) {
+  if (!la || !nnz) return HFX_ERR_ARG;
+  *nnz = la->sys.nnz();
+  return HFX_OK;
+}
+
+int hfx_la_solve(hfx_la* la, const hfx_solve_opts* opts, double* x, hfx_solve_info* info) {
+  if (!la || !x) return HFX_ERR_ARG;
+  if (!la->sys.assembled()) return set_err(la->ctx, HFX_ERR_STATE, "la_solve: assemble before solving");
+  hfx_solve_opts o;
+  if (opts) o = *opts;
+  else {
+    hfx_solve_opts_default(&o);
+    o.method = HFX_KSP_GMRES;
+    o.precond = HFX_PC_JACOBI;
+  }
+  cudaSetDevice(la->ctx->device);
+  LaSolveResult r;
+  std::string err;
+  int st = la->sys.solve(o.rtol, o.maxits, o.restart > 0 ? o.restart : 30, o.precond == HFX_PC_NONE ? 0 : 1,
+                         la->ctx->stream, x, &r, &err);
+  if (info) {
+    info->status = st;
+    info->iterations = r.iterations;
+    info->refinements = 0;
+    info->rel_residual = r.rel_residual;
+    info->solve_ms = r.ms;
+  }
+  if (st != 0) return set_err(la->ctx, st, err);
+  return HFX_OK;
+}
+
+}  // extern "C"

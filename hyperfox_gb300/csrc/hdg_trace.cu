@@ -1,0 +1,153 @@
+// Trace-system scatter, local recovery and integration-point coordinates.
+//
+// Trace values are stored in scalar-CSR order over face-block rows: the Nf
+// scalar rows of face f are contiguous, each of length nb(f)*Nf where nb(f) is
+// the number of neighbour faces (sorted), and within a row the entry of
+// neighbour k, node b sits at k*Nf + b. This is exactly PETSc's AIJ layout of
+// the reference system (sorted columns, explicit zeros kept), so the scalar
+// column array is implied by the face-block columns and is never stored.
+#include "hfx_device.h"
+
+namespace hfx {
+namespace {
+
+// One thread per stored value: sum of the (one or two) element contributions,
+// first the lower cell then the upper one (the order HyperFox adds them in,
+// HDGSolver.cpp:605-625). With at most two addends the sum is exact-order
+// independent.
+__global__ void scatter_values(ScatterParams p, const int* brow, int64_t nBlocks) {
+  const int NF = p.NF, LL = p.LL, F = p.F;
+  const int64_t total = nBlocks * NF * NF;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t k = idx / (NF * NF);
+    int ab = (int)(idx % (NF * NF));
+    int a = ab / NF, b = ab % NF;
+    int f = brow[k];
+    int64_t b0 = p.browptr[f];
+    int64_t nb = p.browptr[f + 1] - b0;
+    double v = 0.0;
+    for (int s = 0; s < 2; ++s) {
+      int c = s == 0 ? p.src0[k] : p.src1[k];
+      if (c < 0) continue;
+      int loc = s == 0 ? p.loc0[k] : p.loc1[k];
+      int li = loc >> 4, lj = loc & 15;
+      // local node positions whose face-order positions are a (row) and b (col)
+      const uint8_t* pi = p.perm + ((int64_t)c * F + li) * NF;
+      const uint8_t* pj = p.perm + ((int64_t)c * F + lj) * NF;
+      int ja = 0, jb = 0;
+      for (int q = 0; q < NF; ++q) {
+        if (pi[q] == a) ja = q;
+        if (pj[q] == b) jb = q;
+      }
+      v += p.S[(int64_t)c * LL * LL + (li * NF + ja) + (int64_t)(lj * NF + jb) * LL];
+    }
+    p.val[b0 * NF * NF + (int64_t)a * nb * NF + (k - b0) * NF + b] = v;
+  }
+}
+
+__global__ void scatter_rhs(ScatterParams p) {
+  const int NF = p.NF, LL = p.LL, F = p.F;
+  const int64_t total = (int64_t)p.nFaces * NF;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int f = (int)(idx / NF), a = (int)(idx % NF);
+    double v = 0.0;
+    for (int s = 0; s < 2; ++s) {
+      int c = p.face2cell[2 * (int64_t)f + s];
+      if (c < 0) continue;
+      int li = 0;
+      for (int i = 0; i < F; ++i)
+        if (p.cell2face[(int64_t)c * F + i] == f) li = i;
+      const uint8_t* pi = p.perm + ((int64_t)c * F + li) * NF;
+      int ja = 0;
+      for (int q = 0; q < NF; ++q)
+        if (pi[q] == a) ja = q;
+      v += p.S0[(int64_t)c * LL + li * NF + ja];
+    }
+    p.rhs[idx] = v;
+  }
+}
+
+__global__ void block_rows(const int64_t* browptr, int nFaces, int* brow) {
+  for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nFaces; f += gridDim.x * blockDim.x)
+    for (int64_t k = browptr[f]; k < browptr[f + 1]; ++k) brow[k] = f;
+}
+
+// One CTA per element: thread r computes row r of [U; Q] * lambda + [U0; Q0]
+// (HDGSolver.cpp:741-775). Columns of U and Q are contiguous per element, so
+// consecutive threads read consecutive addresses.
+__global__ void recover_kernel(RecoverParams p) {
+  extern __shared__ double lam[];
+  const int F = p.F, NF = p.NF, LU = p.LU, LQ = p.LQ, LL = p.LL;
+  for (int64_t e = blockIdx.x; e < p.nCells; e += gridDim.x) {
+    for (int j = threadIdx.x; j < LL; j += blockDim.x) {
+      int i = j / NF;
+      int f = p.cell2face[e * F + i];
+      lam[j] = p.trace[(int64_t)f * NF + p.perm[(e * F + i) * NF + (j % NF)]];
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < LU + LQ; r += blockDim.x) {
+      double acc;
+      if (r < LU) {
+        const double* U = p.U + e * LU * LL;
+        acc = p.U0[e * LU + r];
+        for (int c = 0; c < LL; ++c) acc += U[r + (int64_t)c * LU] * lam[c];
+        p.sol[e * LU + r] = acc;
+      } else {
+        int rq = r - LU;
+        const double* Q = p.Q + e * LQ * LL;
+        acc = p.Q0[e * LQ + rq];
+        for (int c = 0; c < LL; ++c) acc += Q[rq + (int64_t)c * LQ] * lam[c];
+        p.flux[e * LQ + rq] = acc;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void ip_coords_kernel(IpCoordParams p) {
+  const int64_t total = (int64_t)p.nCells * p.NI * p.D;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t c = idx / (p.NI * p.D);
+    int q = (int)((idx / p.D) % p.NI), d = (int)(idx % p.D);
+    double acc = 0.0;
+    for (int i = 0; i < p.N; ++i) acc += p.phi[q * p.N + i] * p.coords[(int64_t)p.cells[c * p.N + i] * p.D + d];
+    p.out[idx] = acc;
+  }
+}
+
+unsigned grid_for(int64_t n, int threads) {
+  int64_t g = (n + threads - 1) / threads;
+  if (g > 152 * 64) g = 152 * 64;
+  return (unsigned)(g < 1 ? 1 : g);
+}
+
+}  // namespace
+
+cudaError_t launch_block_rows(const int64_t* browptr, int nFaces, int* brow, cudaStream_t s) {
+  block_rows<<<grid_for(nFaces, 256), 256, 0, s>>>(browptr, nFaces, brow);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter(const ScatterParams& p, cudaStream_t s) {
+  scatter_values<<<grid_for(p.nBlocks * p.NF * p.NF, 256), 256, 0, s>>>(p, p.brow, p.nBlocks);
+  scatter_rhs<<<grid_for((int64_t)p.nFaces * p.NF, 256), 256, 0, s>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_recover(const RecoverParams& p, cudaStream_t s) {
+  int threads = ((p.LU + p.LQ + 31) / 32) * 32;
+  if (threads > 256) threads = 256;
+  int64_t grid = p.nCells < 152 * 256 ? p.nCells : 152 * 256;
+  recover_kernel<<<(unsigned)(grid < 1 ? 1 : grid), threads, p.LL * sizeof(double), s>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ip_coords(const IpCoordParams& p, cudaStream_t s) {
+  ip_coords_kernel<<<grid_for((int64_t)p.nCells * p.NI * p.D, 256), 256, 0, s>>>(p);
+  return cudaGetLastError();
+}
+
+}  // namespace hfx

@@ -1,0 +1,101 @@
+// Device-side parameter blocks and launcher declarations (internal).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace hfx {
+
+// Compile-time sizes of a simplex HDG element of dimension D and order P.
+__host__ __device__ constexpr int simplex_nodes(int D, int P) {
+  return D == 1 ? P + 1 : (D == 2 ? (P + 1) * (P + 2) / 2 : (P + 1) * (P + 2) * (P + 3) / 6);
+}
+// Number of points of the order-2P rule HyperFox uses (TestCubature.cpp:41-44).
+__host__ __device__ constexpr int cubature_points(int D, int P) {
+  return D == 1 ? P + 1
+                : (D == 2 ? (P == 1 ? 3 : P == 2 ? 6 : P == 3 ? 12 : P == 4 ? 16 : 25)
+                          : (P == 1 ? 4 : P == 2 ? 14 : P == 3 ? 24 : P == 4 ? 46 : 81));
+}
+
+template <int D, int P>
+struct Dims {
+  static constexpr int N = simplex_nodes(D, P);
+  static constexpr int NF = simplex_nodes(D - 1, P);
+  static constexpr int F = D + 1;
+  static constexpr int NI = cubature_points(D, P);
+  static constexpr int NIF = cubature_points(D - 1, P);
+  static constexpr int LU = N;
+  static constexpr int LQ = D * N;
+  static constexpr int LL = F * NF;
+};
+
+// Everything the element kernel reads and writes (device pointers).
+struct LocalParams {
+  int nCells;
+  const double* coords;        // [nNodes][D]
+  const int* cells;            // [nCells][N]
+  const int* cell2face;        // [nCells][F]
+  const uint8_t* perm;         // [nCells][F][NF]
+  const int* face2cell;        // [nFaces][2]
+  const uint8_t* isBoundary;   // [nFaces]
+  const double* tau;           // [nFaces][NF][tauVals]
+  int tauVals;
+  const double* kappa;         // layout 0: [nNodes][kc], 1: [nCells][N][kc]
+  int kc, kappaLayout;
+  int srcMode;
+  const double* src;           // [nCells][NI]
+  double srcParam;
+  const double* dirichlet;     // [nFaces][NF]
+  double dt;
+  const double* uOld;          // [nCells][N]
+  const double* tab;           // phi, dphi, w, fphi, fdphi, fw
+  const int* itab;             // faceNodes[F*NF], faceOpposite[F]
+  double *S, *S0, *U, *Q, *U0, *Q0;
+  int* status;                 // first error: 1 = singular block
+};
+
+cudaError_t launch_local_condense(int dim, int order, const LocalParams& p, cudaStream_t s);
+bool local_condense_supported(int dim, int order);
+
+// Trace-system scatter (face-block rows, values in scalar-CSR order).
+struct ScatterParams {
+  int nFaces, NF, LL;
+  const int64_t* browptr;  // [nFaces+1]
+  const int* brow;         // [nBlocks] row face of every block
+  int64_t nBlocks;
+  const int* src0;         // [nBlocks]
+  const int* src1;
+  const uint8_t* loc0;
+  const uint8_t* loc1;
+  const uint8_t* perm;     // [nCells][F][NF]
+  const double* S;         // [nCells][LL*LL] column-major
+  const double* S0;        // [nCells][LL]
+  const int* cell2face;
+  const int* face2cell;
+  int F;
+  double* val;             // scalar-CSR ordered values
+  double* rhs;             // [nFaces*NF]
+};
+cudaError_t launch_scatter(const ScatterParams& p, cudaStream_t s);
+cudaError_t launch_block_rows(const int64_t* browptr, int nFaces, int* brow, cudaStream_t s);
+
+struct RecoverParams {
+  int nCells, F, NF, LU, LQ, LL;
+  const int* cell2face;
+  const uint8_t* perm;
+  const double *U, *Q, *U0, *Q0;
+  const double* trace;
+  double* sol;
+  double* flux;
+};
+cudaError_t launch_recover(const RecoverParams& p, cudaStream_t s);
+
+struct IpCoordParams {
+  int nCells, N, NI, D;
+  const double* coords;
+  const int* cells;
+  const double* phi;  // [NI][N]
+  double* out;        // [nCells][NI][D]
+};
+cudaError_t launch_ip_coords(const IpCoordParams& p, cudaStream_t s);
+
+}  // namespace hfx

@@ -1,0 +1,703 @@
+// Krylov solve of the condensed trace system on the device (replaces
+// PetscInterface::solve / KSPSolve, PetscInterface.cpp:222-247).
+//
+// HyperFox's trace system has identity rows for Dirichlet DOFs with their
+// columns left in place (HDGSolver.cpp:493-501), so it is not symmetric; its
+// interior block is symmetric negative definite. The solver works on the
+// equivalent SPD system
+//     A' = [ -A_II  0 ]   b' = [ -(b_I - A_ID g) ]
+//          [  0     I ]        [        g        ]
+// whose solution is the reference system's solution. The FP64 operator is
+// applied from the reference values on the fly (face-level masks), so no
+// second FP64 copy of the matrix is stored; the mixed-precision path keeps an
+// FP32 copy of A' for the inner solves and refines in FP64 against A'.
+//
+// CG per iteration is two kernels:
+//   K1: p = z + beta*p_old (computed on the fly for every gathered entry),
+//       q = A' p, partial p.q, and in the last block alpha = rz / p.q;
+//   K2: x += alpha p, r -= alpha q, z = M^{-1} r, partial r.z and r.r, and in
+//       the last block beta, the convergence test and the iteration count.
+// Reductions are deterministic: per-block partials in fixed order, summed by
+// the last block to finish (atomic ticket, no spin-waits). Once converged (or
+// broken down) every later kernel returns at entry, so the host may queue
+// many iterations between checks.
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "hfx_device.h"
+#include "krylov.h"
+
+namespace hfx {
+namespace {
+
+constexpr int kThreads = 256;
+
+template <typename T>
+__device__ __forceinline__ T fma_t(T a, T b, T c);
+template <>
+__device__ __forceinline__ double fma_t<double>(double a, double b, double c) { return fma(a, b, c); }
+template <>
+__device__ __forceinline__ float fma_t<float>(float a, float b, float c) { return fmaf(a, b, c); }
+
+// Block-sum then last-block-done total of one or two values; the block that
+// takes the last ticket writes the totals (fixed summation order).
+template <int NV>
+__device__ bool block_reduce_last(double (&v)[NV], double* partials, unsigned* ticket, double (&tot)[NV]) {
+  __shared__ double red[NV][kThreads / 32];
+  __shared__ bool amLast;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int k = 0; k < NV; ++k) {
+    double x = v[k];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) red[k][wid] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < NV; ++k) {
+      double s = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[k][w];
+      partials[(size_t)k * gridDim.x + blockIdx.x] = s;
+    }
+    __threadfence();
+    unsigned t = atomicAdd(ticket, 1u);
+    amLast = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!amLast) return false;
+  __threadfence();
+  // the last block sums all partials in block order
+  for (int k = 0; k < NV; ++k) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+      s += ((volatile double*)partials)[(size_t)k * gridDim.x + b];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) red[k][wid] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < NV; ++k) {
+      double s = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[k][w];
+      tot[k] = s;
+    }
+    *ticket = 0u;
+  }
+  return true;
+}
+
+template <int NF, int NBMAX>
+struct GroupCfg {
+  static constexpr int NPOS = NBMAX * NF;
+  static constexpr int GS = NPOS <= 16 ? 16 : 32;
+  static constexpr int KPL = (NPOS + GS - 1) / GS;
+};
+
+// y = A' x on face-block rows. MASKED: apply the reference values with the
+// Dirichlet elimination and the sign flip on the fly (FP64 path); otherwise
+// the values already hold A'.
+template <typename T, int NF, int NBMAX, bool MASKED>
+__device__ __forceinline__ void face_row_spmv(const T* __restrict__ val, int64_t b0, int nb,
+                                              const T (&xv)[GroupCfg<NF, NBMAX>::KPL], int lane,
+                                              T (&yrow)[NF]) {
+  using G = GroupCfg<NF, NBMAX>;
+  const int npos = nb * NF;
+  const T* base = val + b0 * NF * NF;
+#pragma unroll
+  for (int a = 0; a < NF; ++a) {
+    T acc = 0;
+#pragma unroll
+    for (int k = 0; k < G::KPL; ++k) {
+      int m = lane + k * G::GS;
+      if (m < npos) acc = fma_t<T>(base[(int64_t)a * npos + m], xv[k], acc);
+    }
+#pragma unroll
+    for (int o = G::GS / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G::GS);
+    yrow[a] = acc;
+  }
+}
+
+// K1 of CG (see the file comment).
+template <typename T, int NF, int NBMAX, bool MASKED>
+__global__ void __launch_bounds__(kThreads) cg_spmv(TraceView A, const T* __restrict__ val,
+                                                    const T* __restrict__ z, const T* __restrict__ pold,
+                                                    T* __restrict__ pnew, T* __restrict__ q, CgState* st,
+                                                    double* partials, int first) {
+  using G = GroupCfg<NF, NBMAX>;
+  if (st->done) return;
+  const T beta = first ? T(0) : (T)st->beta;
+  const int lane = threadIdx.x % G::GS;
+  const int gpb = kThreads / G::GS;
+  double pq = 0.0;
+  // warp-uniform loop: every lane of a warp takes the same trips (shuffles use
+  // the full mask); a group past the last face works on nothing
+  const int gInWarp = (threadIdx.x & 31) / G::GS;
+  for (int64_t fb = ((int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5)) * (32 / G::GS); fb < A.nFaces;
+       fb += (int64_t)gridDim.x * gpb) {
+    const int64_t f = fb + gInWarp;
+    const bool act = f < A.nFaces;
+    const int64_t b0 = act ? A.browptr[f] : 0;
+    const int nb = act ? (int)(A.browptr[f + 1] - b0) : 0;
+    const bool rowBnd = MASKED && act && A.isBnd[f];
+    T xv[G::KPL];
+#pragma unroll
+    for (int k = 0; k < G::KPL; ++k) {
+      int m = lane + k * G::GS;
+      T v = 0;
+      if (m < nb * NF) {
+        int g = A.bcol[b0 + m / NF];
+        int64_t j = (int64_t)g * NF + m % NF;
+        v = fma_t<T>(beta, pold[j], z[j]);
+        if (MASKED && (rowBnd || A.isBnd[g])) v = 0;  // eliminated columns
+      }
+      xv[k] = v;
+    }
+    T y[NF];
+    face_row_spmv<T, NF, NBMAX, MASKED>(val, b0, nb, xv, lane, y);
+    if (lane == 0 && act) {
+#pragma unroll
+      for (int a = 0; a < NF; ++a) {
+        int64_t i = f * NF + a;
+        T pi = fma_t<T>(beta, pold[i], z[i]);
+        T yi = MASKED ? (rowBnd ? pi : -y[a]) : y[a];
+        pnew[i] = pi;
+        q[i] = yi;
+        pq += (double)pi * (double)yi;
+      }
+    }
+  }
+  double v[1] = {pq}, tot[1];
+  if (block_reduce_last<1>(v, partials, &st->ticket, tot) && threadIdx.x == 0) {
+    double pAp = tot[0];
+    if (!(pAp > 0.0) || !isfinite(pAp)) {
+      st->status = isfinite(pAp) ? 6 : 7;  // HFX_ERR_BREAKDOWN / HFX_ERR_NAN
+      st->done = 1;
+    } else {
+      st->alpha = st->rz / pAp;
+    }
+  }
+}
+
+// K2 of CG. PC: 0 none, 1 Jacobi (pc = inverse diagonal), 2 block Jacobi
+// (pc = inverse face blocks, row-major NF x NF).
+template <typename T, int NF, int PC>
+__global__ void __launch_bounds__(kThreads) cg_update(int64_t nFaces, T* __restrict__ x, T* __restrict__ r,
+                                                      T* __restrict__ z, const T* __restrict__ p,
+                                                      const T* __restrict__ q, const T* __restrict__ pc,
+                                                      CgState* st, double* partials, double tol2) {
+  if (st->done) return;
+  const T alpha = (T)st->alpha;
+  double rz = 0.0, rr = 0.0;
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < nFaces; f += (int64_t)gridDim.x * blockDim.x) {
+    T rl[NF];
+#pragma unroll
+    for (int a = 0; a < NF; ++a) {
+      int64_t i = f * NF + a;
+      x[i] = fma_t<T>(alpha, p[i], x[i]);
+      rl[a] = fma_t<T>(-alpha, q[i], r[i]);
+      r[i] = rl[a];
+      rr += (double)rl[a] * (double)rl[a];
+    }
+#pragma unroll
+    for (int a = 0; a < NF; ++a) {
+      int64_t i = f * NF + a;
+      T zi;
+      if (PC == 0) zi = rl[a];
+      else if (PC == 1) zi = pc[i] * rl[a];
+      else {
+        zi = 0;
+        const T* B = pc + f * NF * NF + a * NF;
+#pragma unroll
+        for (int b = 0; b < NF; ++b) zi = fma_t<T>(B[b], rl[b], zi);
+      }
+      z[i] = zi;
+      rz += (double)rl[a] * (double)zi;
+    }
+  }
+  double v[2] = {rz, rr}, tot[2];
+  if (block_reduce_last<2>(v, partials, &st->ticket, tot) && threadIdx.x == 0) {
+    double rzn = tot[0];
+    st->iters += 1;
+    st->rr = tot[1];
+    if (!isfinite(rzn) || !isfinite(tot[1])) {
+      st->status = 7;
+      st->done = 1;
+    } else {
+      st->beta = rzn / st->rz;
+      st->rz = rzn;
+      if (tot[1] <= tol2) st->done = 1;
+      else if (st->iters >= st->maxits) {
+        st->status = 5;  // HFX_ERR_NOT_CONVERGED
+        st->done = 1;
+      }
+    }
+  }
+}
+
+// r = b' - A' x (FP64, masked reference values) and its norm; also z = M^{-1} r
+// and r.z to start CG. Writes the squared norms to st.
+template <int NF, int NBMAX, int PC>
+__global__ void __launch_bounds__(kThreads) cg_start(TraceView A, const double* __restrict__ val,
+                                                     const double* __restrict__ bS, const double* __restrict__ bref,
+                                                     const double* __restrict__ x, double* __restrict__ r,
+                                                     double* __restrict__ z, const double* __restrict__ pc, CgState* st,
+                                                     double* partials) {
+  using G = GroupCfg<NF, NBMAX>;
+  const int lane = threadIdx.x % G::GS;
+  const int gpb = kThreads / G::GS;
+  double rr = 0.0, rz = 0.0, bb = 0.0;
+  // warp-uniform loop: every lane of a warp takes the same trips (shuffles use
+  // the full mask); a group past the last face works on nothing
+  const int gInWarp = (threadIdx.x & 31) / G::GS;
+  for (int64_t fb = ((int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5)) * (32 / G::GS); fb < A.nFaces;
+       fb += (int64_t)gridDim.x * gpb) {
+    const int64_t f = fb + gInWarp;
+    const bool act = f < A.nFaces;
+    const int64_t b0 = act ? A.browptr[f] : 0;
+    const int nb = act ? (int)(A.browptr[f + 1] - b0) : 0;
+    const bool rowBnd = act && A.isBnd[f];
+    double xv[G::KPL];
+#pragma unroll
+    for (int k = 0; k < G::KPL; ++k) {
+      int m = lane + k * G::GS;
+      double v = 0;
+      if (m < nb * NF) {
+        int g = A.bcol[b0 + m / NF];
+        v = (rowBnd || A.isBnd[g]) ? 0.0 : x[(int64_t)g * NF + m % NF];
+      }
+      xv[k] = v;
+    }
+    double y[NF];
+    face_row_spmv<double, NF, NBMAX, true>(val, b0, nb, xv, lane, y);
+    if (lane == 0 && act) {
+      double rl[NF];
+      for (int a = 0; a < NF; ++a) {
+        int64_t i = f * NF + a;
+        double ax = rowBnd ? x[i] : -y[a];
+        rl[a] = bS[i] - ax;
+        r[i] = rl[a];
+        rr += rl[a] * rl[a];
+        bb += bref[i] * bref[i];
+      }
+      for (int a = 0; a < NF; ++a) {
+        int64_t i = f * NF + a;
+        double zi;
+        if (PC == 0) zi = rl[a];
+        else if (PC == 1) zi = pc[i] * rl[a];
+        else {
+          zi = 0;
+          for (int b = 0; b < NF; ++b) zi += pc[f * NF * NF + a * NF + b] * rl[b];
+        }
+        z[i] = zi;
+        rz += rl[a] * zi;
+      }
+    }
+  }
+  double v[3] = {rr, rz, bb}, tot[3];
+  if (block_reduce_last<3>(v, partials, &st->ticket, tot) && threadIdx.x == 0) {
+    st->rr = tot[0];
+    st->rz = tot[1];
+    st->bb = tot[2];
+  }
+}
+
+// Residual of the reference system: res = b - A x with the stored values as
+// they are (Dirichlet identity rows included); totals ||b-Ax||^2, ||b||^2.
+template <int NF, int NBMAX>
+__global__ void __launch_bounds__(kThreads) ref_residual(TraceView A, const double* __restrict__ val,
+                                                         const double* __restrict__ b, const double* __restrict__ x,
+                                                         CgState* st, double* partials) {
+  using G = GroupCfg<NF, NBMAX>;
+  const int lane = threadIdx.x % G::GS;
+  const int gpb = kThreads / G::GS;
+  double rr = 0.0, bb = 0.0;
+  // warp-uniform loop: every lane of a warp takes the same trips (shuffles use
+  // the full mask); a group past the last face works on nothing
+  const int gInWarp = (threadIdx.x & 31) / G::GS;
+  for (int64_t fb = ((int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5)) * (32 / G::GS); fb < A.nFaces;
+       fb += (int64_t)gridDim.x * gpb) {
+    const int64_t f = fb + gInWarp;
+    const bool act = f < A.nFaces;
+    const int64_t b0 = act ? A.browptr[f] : 0;
+    const int nb = act ? (int)(A.browptr[f + 1] - b0) : 0;
+    double xv[G::KPL];
+#pragma unroll
+    for (int k = 0; k < G::KPL; ++k) {
+      int m = lane + k * G::GS;
+      xv[k] = m < nb * NF ? x[(int64_t)A.bcol[b0 + m / NF] * NF + m % NF] : 0.0;
+    }
+    double y[NF];
+    face_row_spmv<double, NF, NBMAX, false>(val, b0, nb, xv, lane, y);
+    if (lane == 0 && act)
+      for (int a = 0; a < NF; ++a) {
+        double ri = b[f * NF + a] - y[a];
+        rr += ri * ri;
+        bb += b[f * NF + a] * b[f * NF + a];
+      }
+  }
+  double v[2] = {rr, bb}, tot[2];
+  if (block_reduce_last<2>(v, partials, &st->ticket, tot) && threadIdx.x == 0) {
+    st->res_rr = tot[0];
+    st->res_bb = tot[1];
+  }
+}
+
+// b' and the FP32 copy of A' (optional), one group per face row.
+template <int NF, int NBMAX>
+__global__ void __launch_bounds__(kThreads) prepare_system(TraceView A, const double* __restrict__ val,
+                                                           const double* __restrict__ b, double* __restrict__ bS,
+                                                           float* __restrict__ val32) {
+  using G = GroupCfg<NF, NBMAX>;
+  const int lane = threadIdx.x % G::GS;
+  const int gpb = kThreads / G::GS;
+  // warp-uniform loop: every lane of a warp takes the same trips (shuffles use
+  // the full mask); a group past the last face works on nothing
+  const int gInWarp = (threadIdx.x & 31) / G::GS;
+  for (int64_t fb = ((int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5)) * (32 / G::GS); fb < A.nFaces;
+       fb += (int64_t)gridDim.x * gpb) {
+    const int64_t f = fb + gInWarp;
+    const bool act = f < A.nFaces;
+    const int64_t b0 = act ? A.browptr[f] : 0;
+    const int nb = act ? (int)(A.browptr[f + 1] - b0) : 0;
+    const int npos = nb * NF;
+    const bool rowBnd = act && A.isBnd[f];
+    for (int a = 0; a < NF; ++a) {
+      // lifted Dirichlet values: sum over boundary columns of A_ij g_j
+      double lift = 0.0;
+      for (int m = lane; m < npos; m += G::GS) {
+        int g = A.bcol[b0 + m / NF];
+        int64_t j = (int64_t)g * NF + m % NF;
+        double v = val[b0 * NF * NF + (int64_t)a * npos + m];
+        if (!rowBnd && A.isBnd[g]) lift += v * b[j];
+        if (val32) {
+          float w;
+          if (rowBnd) w = (j == f * NF + a) ? 1.0f : 0.0f;
+          else w = A.isBnd[g] ? 0.0f : (float)(-v);
+          val32[b0 * NF * NF + (int64_t)a * npos + m] = w;
+        }
+      }
+      for (int o = G::GS / 2; o > 0; o >>= 1) lift += __shfl_xor_sync(0xffffffffu, lift, o, G::GS);
+      if (lane == 0 && act) {
+        int64_t i = f * NF + a;
+        bS[i] = rowBnd ? b[i] : -(b[i] - lift);
+      }
+    }
+  }
+}
+
+// Inverse diagonal / inverse diagonal face blocks of A' (FP64 and FP32 copies).
+template <int NF>
+__global__ void build_precond(TraceView A, const double* __restrict__ val, int pcType, double* pc64, float* pc32) {
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < A.nFaces; f += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b0 = A.browptr[f];
+    const int nb = (int)(A.browptr[f + 1] - b0);
+    int kd = 0;
+    for (int k = 0; k < nb; ++k)
+      if (A.bcol[b0 + k] == (int)f) kd = k;
+    double B[NF][2 * NF];
+    for (int a = 0; a < NF; ++a)
+      for (int b = 0; b < NF; ++b) {
+        double v = A.isBnd[f] ? (a == b ? 1.0 : 0.0) : -val[b0 * NF * NF + (int64_t)a * nb * NF + kd * NF + b];
+        B[a][b] = v;
+        B[a][NF + b] = (a == b) ? 1.0 : 0.0;
+      }
+    if (pcType == 1) {
+      for (int a = 0; a < NF; ++a) {
+        double d = B[a][a];
+        double v = d != 0.0 ? 1.0 / d : 1.0;
+        if (pc64) pc64[f * NF + a] = v;
+        if (pc32) pc32[f * NF + a] = (float)v;
+      }
+      continue;
+    }
+    // Gauss-Jordan (SPD block, no pivoting)
+    for (int k = 0; k < NF; ++k) {
+      double inv = 1.0 / B[k][k];
+      for (int j = 0; j < 2 * NF; ++j) B[k][j] *= inv;
+      for (int i = 0; i < NF; ++i) {
+        if (i == k) continue;
+        double l = B[i][k];
+        for (int j = 0; j < 2 * NF; ++j) B[i][j] -= l * B[k][j];
+      }
+    }
+    for (int a = 0; a < NF; ++a)
+      for (int b = 0; b < NF; ++b) {
+        if (pc64) pc64[f * NF * NF + a * NF + b] = B[a][NF + b];
+        if (pc32) pc32[f * NF * NF + a * NF + b] = (float)B[a][NF + b];
+      }
+  }
+}
+
+// FP32 <-> FP64 vector helpers for the refinement loop.
+__global__ void scale_to_f32(int64_t n, const double* __restrict__ src, double scale, float* __restrict__ dst) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = (float)(src[i] * scale);
+}
+__global__ void axpy_f32_to_f64(int64_t n, double a, const float* __restrict__ d, double* __restrict__ x) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] += a * (double)d[i];
+}
+// Start of an inner FP32 CG from d = 0: r = rhs, z = M^{-1} r, r.z, r.r.
+template <int NF, int PC>
+__global__ void __launch_bounds__(kThreads) cg_start_zero_f32(int64_t nFaces, const float* __restrict__ rhs,
+                                                              float* __restrict__ x, float* __restrict__ r,
+                                                              float* __restrict__ z, const float* __restrict__ pc,
+                                                              CgState* st, double* partials) {
+  double rr = 0.0, rz = 0.0;
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < nFaces; f += (int64_t)gridDim.x * blockDim.x) {
+    float rl[NF];
+    for (int a = 0; a < NF; ++a) {
+      int64_t i = f * NF + a;
+      rl[a] = rhs[i];
+      r[i] = rl[a];
+      x[i] = 0.0f;
+      rr += (double)rl[a] * rl[a];
+    }
+    for (int a = 0; a < NF; ++a) {
+      int64_t i = f * NF + a;
+      float zi;
+      if (PC == 0) zi = rl[a];
+      else if (PC == 1) zi = pc[i] * rl[a];
+      else {
+        zi = 0.0f;
+        for (int b = 0; b < NF; ++b) zi = fmaf(pc[f * NF * NF + a * NF + b], rl[b], zi);
+      }
+      z[i] = zi;
+      rz += (double)rl[a] * zi;
+    }
+  }
+  double v[2] = {rr, rz}, tot[2];
+  if (block_reduce_last<2>(v, partials, &st->ticket, tot) && threadIdx.x == 0) {
+    st->rr = tot[0];
+    st->rz = tot[1];
+    st->bb = tot[0];
+  }
+}
+
+template <int NF>
+__global__ void copy_dirichlet(TraceView A, const double* __restrict__ bS, double* __restrict__ x) {
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < A.nFaces; f += (int64_t)gridDim.x * blockDim.x)
+    if (A.isBnd[f])
+      for (int a = 0; a < NF; ++a) x[f * NF + a] = bS[f * NF + a];
+}
+
+template <typename KernelT>
+int grid_of(KernelT k, int threads) {
+  int dev = 0, nsm = 0, perSM = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k, threads, 0);
+  if (perSM < 1) perSM = 1;
+  return nsm * perSM;
+}
+
+// ------------------------------------------------------------------ driver
+template <int NF, int NBMAX>
+struct Driver {
+  static int run(const TraceSolveArgs& a, TraceSolveResult* out) {
+    cudaStream_t s = a.stream;
+    const TraceView& A = a.A;
+    const int64_t n = (int64_t)A.nFaces * NF;
+    const int pcT = a.precond;  // 0 none, 1 Jacobi, 2 block Jacobi
+    auto fail = [&](cudaError_t e) {
+      out->cudaErr = e;
+      return 3;
+    };
+    cudaError_t err;
+    const int gridF = grid_of(cg_spmv<double, NF, NBMAX, true>, kThreads);
+    const int gridU = grid_of(cg_update<double, NF, 2>, kThreads);
+    const int gridS = grid_of(prepare_system<NF, NBMAX>, kThreads);
+    double* partials = a.ws.partials;
+    CgState* st = a.ws.state;
+    CgState hst;
+    KernelTimer* tm = a.timer;
+    // 1. system b', FP32 values if needed, preconditioner
+    tm->begin(K_OTHER, s);
+    prepare_system<NF, NBMAX><<<gridS, kThreads, 0, s>>>(A, a.val, a.rhs, a.ws.bS,
+                                                           a.mixed ? a.ws.val32 : nullptr);
+    if (pcT > 0)
+      build_precond<NF><<<(unsigned)((A.nFaces + 127) / 128), 128, 0, s>>>(
+          A, a.val, pcT, a.ws.pc64, a.mixed ? a.ws.pc32 : nullptr);
+    tm->end(K_OTHER, s);
+    if ((err = cudaGetLastError()) != cudaSuccess) return fail(err);
+    double* x = a.x;
+    if (!a.use_initial_guess) {
+      // interior 0, Dirichlet rows g (b' holds g there)
+      cudaMemsetAsync(x, 0, sizeof(double) * n, s);
+    }
+    auto reset_state = [&](int maxits) {
+      CgState init{};
+      init.maxits = maxits;
+      return cudaMemcpyAsync(st, &init, sizeof(CgState), cudaMemcpyHostToDevice, s);
+    };
+    int totalIters = 0, refinements = 0, status = 0;
+    if (!a.mixed) {
+      if ((err = reset_state(a.maxits)) != cudaSuccess) return fail(err);
+      if (!a.use_initial_guess) {
+        // Dirichlet rows start exact: x_D = g
+        set_dirichlet_start(A, a.ws.bS, x, s);
+      }
+      tm->begin(K_OTHER, s);
+      launch_start(A, a, x, st, partials, pcT, gridF, s);
+      tm->end(K_OTHER, s);
+      if ((err = cudaMemcpyAsync(&hst, st, sizeof(CgState), cudaMemcpyDeviceToHost, s)) != cudaSuccess) return fail(err);
+      cudaStreamSynchronize(s);
+      double tol2 = a.rtol * a.rtol * hst.bb;
+      if (hst.rr <= tol2) {
+        // already converged
+      } else {
+        double *r = a.ws.r, *z = a.ws.z, *p0 = a.ws.p0, *p1 = a.ws.p1, *q = a.ws.q;
+        int it = 0;
+        while (true) {
+          for (int k = 0; k < a.check_every; ++k, ++it) {
+            double* pold = (it & 1) ? p1 : p0;
+            double* pnew = (it & 1) ? p0 : p1;
+            tm->begin(K_SPMV64, s);
+            cg_spmv<double, NF, NBMAX, true><<<gridF, kThreads, 0, s>>>(A, a.val, z, pold, pnew, q, st, partials, it == 0);
+            tm->end(K_SPMV64, s);
+            tm->begin(K_UPDATE, s);
+            launch_update<double>(A.nFaces, x, r, z, pnew, q, pcT == 2 ? a.ws.pc64 : (pcT == 1 ? a.ws.pc64 : nullptr),
+                                  st, partials, tol2, pcT, gridU, s);
+            tm->end(K_UPDATE, s);
+          }
+          if ((err = cudaGetLastError()) != cudaSuccess) return fail(err);
+          cudaMemcpyAsync(&hst, st, sizeof(CgState), cudaMemcpyDeviceToHost, s);
+          cudaStreamSynchronize(s);
+          if (hst.done) break;
+        }
+        status = hst.status;
+        totalIters = hst.iters;
+      }
+    } else {
+      // FP64 iterative refinement around FP32 CG on A'
+      float *r32 = a.ws.r32, *z32 = a.ws.z32, *p032 = a.ws.p032, *p132 = a.ws.p132, *q32 = a.ws.q32;
+      float *d32 = a.ws.d32, *rhs32 = a.ws.rhs32;
+      if (!a.use_initial_guess) set_dirichlet_start(A, a.ws.bS, x, s);
+      int innerLeft = a.maxits;
+      while (true) {
+        if ((err = reset_state(innerLeft)) != cudaSuccess) return fail(err);
+        tm->begin(K_OTHER, s);
+        launch_start(A, a, x, st, partials, 0, gridF, s);  // FP64 residual of A'
+        tm->end(K_OTHER, s);
+        cudaMemcpyAsync(&hst, st, sizeof(CgState), cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        if (refinements == 0) out->bb = hst.bb;
+        double bb = out->bb;
+        if (!(hst.rr <= a.rtol * a.rtol * bb) && !std::isfinite(hst.rr)) {
+          status = 7;
+          break;
+        }
+        if (hst.rr <= a.rtol * a.rtol * bb) break;
+        if (innerLeft <= 0 || refinements >= a.max_refinements) {
+          status = 5;
+          break;
+        }
+        double rn = std::sqrt(hst.rr);
+        scale_to_f32<<<gridU, kThreads, 0, s>>>(n, a.ws.r, 1.0 / rn, rhs32);
+        if ((err = reset_state(innerLeft)) != cudaSuccess) return fail(err);
+        launch_start_f32(A.nFaces, rhs32, d32, r32, z32, a.ws.pc32, st, partials, pcT, gridU, s);
+        cudaMemcpyAsync(&hst, st, sizeof(CgState), cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        // inner target relative to ||rhs32|| = 1, but no tighter than needed
+        double want = a.rtol * std::sqrt(bb) / rn;
+        double inner = a.inner_rtol > want ? a.inner_rtol : want;
+        double tol2 = inner * inner * hst.rr;
+        int it = 0;
+        while (true) {
+          for (int k = 0; k < a.check_every; ++k, ++it) {
+            float* pold = (it & 1) ? p132 : p032;
+            float* pnew = (it & 1) ? p032 : p132;
+            tm->begin(K_SPMV32, s);
+            cg_spmv<float, NF, NBMAX, false><<<gridF, kThreads, 0, s>>>(A, a.ws.val32, z32, pold, pnew, q32, st,
+                                                                        partials, it == 0);
+            tm->end(K_SPMV32, s);
+            tm->begin(K_UPDATE, s);
+            launch_update<float>(A.nFaces, d32, r32, z32, pnew, q32, a.ws.pc32, st, partials, tol2, pcT, gridU, s);
+            tm->end(K_UPDATE, s);
+          }
+          if ((err = cudaGetLastError()) != cudaSuccess) return fail(err);
+          cudaMemcpyAsync(&hst, st, sizeof(CgState), cudaMemcpyDeviceToHost, s);
+          cudaStreamSynchronize(s);
+          if (hst.done) break;
+        }
+        totalIters += hst.iters;
+        innerLeft -= hst.iters;
+        refinements += 1;
+        if (hst.status != 0 && hst.status != 5) {
+          status = hst.status;
+          break;
+        }
+        axpy_f32_to_f64<<<gridU, kThreads, 0, s>>>(n, rn, d32, x);
+      }
+    }
+    // final residual of the reference system
+    CgState init{};
+    cudaMemcpyAsync(st, &init, sizeof(CgState), cudaMemcpyHostToDevice, s);
+    tm->begin(K_OTHER, s);
+    ref_residual<NF, NBMAX><<<gridF, kThreads, 0, s>>>(A, a.val, a.rhs, x, st, partials);
+    tm->end(K_OTHER, s);
+    if ((err = cudaGetLastError()) != cudaSuccess) return fail(err);
+    cudaMemcpyAsync(&hst, st, sizeof(CgState), cudaMemcpyDeviceToHost, s);
+    if ((err = cudaStreamSynchronize(s)) != cudaSuccess) return fail(err);
+    out->iterations = totalIters;
+    out->refinements = refinements;
+    out->rel_residual = hst.res_bb > 0 ? std::sqrt(hst.res_rr / hst.res_bb) : std::sqrt(hst.res_rr);
+    return status;
+  }
+
+  static void set_dirichlet_start(const TraceView& A, const double* bS, double* x, cudaStream_t s) {
+    copy_dirichlet<NF><<<(unsigned)((A.nFaces + 255) / 256), 256, 0, s>>>(A, bS, x);
+  }
+  static void launch_start(const TraceView& A, const TraceSolveArgs& a, double* x, CgState* st, double* partials,
+                           int pcT, int grid, cudaStream_t s) {
+    const double* pc = a.ws.pc64;
+    switch (pcT) {
+      case 0: cg_start<NF, NBMAX, 0><<<grid, kThreads, 0, s>>>(A, a.val, a.ws.bS, a.rhs, x, a.ws.r, a.ws.z, pc, st, partials); break;
+      case 1: cg_start<NF, NBMAX, 1><<<grid, kThreads, 0, s>>>(A, a.val, a.ws.bS, a.rhs, x, a.ws.r, a.ws.z, pc, st, partials); break;
+      default: cg_start<NF, NBMAX, 2><<<grid, kThreads, 0, s>>>(A, a.val, a.ws.bS, a.rhs, x, a.ws.r, a.ws.z, pc, st, partials); break;
+    }
+  }
+  static void launch_start_f32(int64_t nFaces, const float* rhs, float* x, float* r, float* z, const float* pc,
+                               CgState* st, double* partials, int pcT, int grid, cudaStream_t s) {
+    switch (pcT) {
+      case 0: cg_start_zero_f32<NF, 0><<<grid, kThreads, 0, s>>>(nFaces, rhs, x, r, z, pc, st, partials); break;
+      case 1: cg_start_zero_f32<NF, 1><<<grid, kThreads, 0, s>>>(nFaces, rhs, x, r, z, pc, st, partials); break;
+      default: cg_start_zero_f32<NF, 2><<<grid, kThreads, 0, s>>>(nFaces, rhs, x, r, z, pc, st, partials); break;
+    }
+  }
+  template <typename T>
+  static void launch_update(int64_t nFaces, T* x, T* r, T* z, const T* p, const T* q, const T* pc, CgState* st,
+                            double* partials, double tol2, int pcT, int grid, cudaStream_t s) {
+    switch (pcT) {
+      case 0: cg_update<T, NF, 0><<<grid, kThreads, 0, s>>>(nFaces, x, r, z, p, q, pc, st, partials, tol2); break;
+      case 1: cg_update<T, NF, 1><<<grid, kThreads, 0, s>>>(nFaces, x, r, z, p, q, pc, st, partials, tol2); break;
+      default: cg_update<T, NF, 2><<<grid, kThreads, 0, s>>>(nFaces, x, r, z, p, q, pc, st, partials, tol2); break;
+    }
+  }
+};
+
+}  // namespace
+
+int trace_solve(const TraceSolveArgs& a, TraceSolveResult* out) {
+  const int NF = a.A.NF;
+  if (a.dim == 2) {
+    switch (NF) {
+      case 2: return Driver<2, 5>::run(a, out);
+      case 3: return Driver<3, 5>::run(a, out);
+      case 4: return Driver<4, 5>::run(a, out);
+      case 5: return Driver<5, 5>::run(a, out);
+      case 6: return Driver<6, 5>::run(a, out);
+    }
+  } else if (a.dim == 3) {
+    switch (NF) {
+      case 3: return Driver<3, 7>::run(a, out);
+      case 6: return Driver<6, 7>::run(a, out);
+      case 10: return Driver<10, 7>::run(a, out);
+    }
+  }
+  return 9;  // HFX_ERR_UNSUPPORTED
+}
+
+size_t trace_partials_needed() { return 3 * 152 * 32; }
+
+}  // namespace hfx

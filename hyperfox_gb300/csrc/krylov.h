@@ -1,0 +1,62 @@
+// Trace-system Krylov solver (internal interface).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "timer.h"
+
+namespace hfx {
+
+// Face-block view of the trace system: rows = faces, block columns = sorted
+// neighbour faces, values in scalar-CSR order (see hdg_trace.cu).
+struct TraceView {
+  int64_t nFaces;
+  int NF;
+  const int64_t* browptr;
+  const int* bcol;
+  const uint8_t* isBnd;  // Dirichlet (boundary) faces
+};
+
+// Device-resident solver scalars. Reductions finish in the last block, which
+// writes here; "done" makes every later kernel of the solve return at entry.
+struct CgState {
+  double rz, rr, bb, alpha, beta;
+  double res_rr, res_bb;
+  int iters, maxits, done, status;
+  unsigned ticket;
+  int pad;
+};
+
+struct TraceWorkspace {
+  double *bS, *r, *z, *p0, *p1, *q, *pc64;
+  float *val32, *pc32, *r32, *z32, *p032, *p132, *q32, *d32, *rhs32;
+  double* partials;
+  CgState* state;
+};
+
+struct TraceSolveArgs {
+  int dim;
+  TraceView A;
+  const double* val;  // reference values (scalar-CSR order)
+  const double* rhs;  // reference right-hand side
+  double* x;          // solution (in: initial guess if use_initial_guess)
+  int precond;        // 0 none, 1 Jacobi, 2 block Jacobi
+  int mixed;          // FP32 inner CG inside FP64 refinement
+  double rtol, inner_rtol;
+  int maxits, max_refinements, check_every, use_initial_guess;
+  TraceWorkspace ws;
+  cudaStream_t stream;
+  KernelTimer* timer;
+};
+
+struct TraceSolveResult {
+  int iterations = 0, refinements = 0;
+  double rel_residual = 0.0, bb = 0.0;
+  cudaError_t cudaErr = cudaSuccess;
+};
+
+// Returns an HFX status code (0 = converged).
+int trace_solve(const TraceSolveArgs& a, TraceSolveResult* out);
+size_t trace_partials_needed();
+
+}  // namespace hfx

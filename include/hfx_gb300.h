@@ -1,0 +1,199 @@
+/*
+ * hfx_gb300.h -- C ABI of the GB300 (sm_103a) HDG hot path.
+ *
+ * Drop-in for HyperFox's HDG element-local path and the trace solve behind it:
+ * every entry point below replaces one reference interface, cited as
+ * file:line of the HyperFox source tree. Plain pointers and sizes only; every
+ * function returns an int status (HFX_OK == 0) and never throws or aborts.
+ * The message of the last failure on a context is hfx_last_error(ctx).
+ *
+ * Host arrays are copied; device state is owned by the context. A context is
+ * used from one host thread at a time and runs its work on its own stream.
+ *
+ * Layouts (all follow HyperFox):
+ *   coords      [nNodes][dim]                        (Mesh nodes, Mesh.cpp:31-46)
+ *   cells       [nCells][nNodesPerCell]   int32      (vertices first)
+ *   cell2face   [nCells][nFacesPerCell]              (Mesh.cpp:404-425)
+ *   face2cell   [nFaces][2], -1 on the boundary      (Mesh.cpp:377-402)
+ *   faces       [nFaces][nNodesPerFace]              (Mesh.cpp:517-537)
+ *   Tau         [nFaces][nNodesPerFace][1 or 2]      (Face field, HDGSolver.cpp:276-304)
+ *   Dirichlet   [nFaces][nNodesPerFace]              (Face field, TestHDGLaplace.cpp:37-46)
+ *   Trace       [nFaces][nNodesPerFace]              (global DOF (face*Nf+node), HDGSolver.cpp:596)
+ *   Solution    [nCells][nNodesPerCell]              (Cell field, HDGSolver.cpp:768)
+ *   Flux        [nCells][nNodesPerCell][dim]         (Cell field, HDGSolver.cpp:769)
+ *   S,S0,U,Q,U0,Q0 per element, column-major         (HDGSolver.cpp:93-104,331-348)
+ */
+#ifndef HFX_GB300_H
+#define HFX_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HFX_OK 0
+#define HFX_ERR_ARG 1           /* bad argument (sizes, pointers, unsupported order) */
+#define HFX_ERR_STATE 2         /* call out of order (HyperFox throws ErrorHandle) */
+#define HFX_ERR_CUDA 3          /* CUDA runtime error */
+#define HFX_ERR_ALLOC 4         /* device allocation failed */
+#define HFX_ERR_NOT_CONVERGED 5 /* Krylov solve hit maxits */
+#define HFX_ERR_BREAKDOWN 6     /* Krylov breakdown (zero curvature) */
+#define HFX_ERR_NAN 7           /* NaN/Inf detected */
+#define HFX_ERR_SINGULAR 8      /* singular element block in condensation */
+#define HFX_ERR_UNSUPPORTED 9   /* feature not built */
+
+/* Krylov method / preconditioner / precision (PetscOpts.h:8-29 analogue). */
+#define HFX_KSP_CG 0        /* CG on the symmetric-eliminated trace system */
+#define HFX_KSP_GMRES 1     /* restarted GMRES, any nonsingular system */
+#define HFX_PC_NONE 0
+#define HFX_PC_JACOBI 1
+#define HFX_PC_BLOCK_JACOBI 2 /* one dense block per face (HDG trace systems) */
+#define HFX_PREC_FP64 0
+#define HFX_PREC_MIXED 1    /* FP32 inner Krylov inside FP64 iterative refinement */
+
+/* Source modes for hfx_set_source (Source::calcSource, Source.cpp:5-22). */
+#define HFX_SRC_NONE 0      /* no source (HDGLaplaceModel) */
+#define HFX_SRC_VALUES 1    /* caller gives f at every volume IP: [nCells][nIP] */
+#define HFX_SRC_SINPROD 2   /* f = param * prod_k sin(pi x_k)  (manufactured u = prod sin) */
+
+typedef struct hfx_ctx hfx_ctx;
+
+typedef struct {
+  int dim, order, nNodes, nFaces, nNodesFace, nIP, nIPFace;
+} hfx_refel_info;
+
+typedef struct {
+  int method;            /* HFX_KSP_* */
+  int precond;           /* HFX_PC_* */
+  int precision;         /* HFX_PREC_* */
+  double rtol;           /* ||b - A x|| <= rtol ||b|| (PetscOpts::rtol) */
+  int maxits;            /* total inner iterations allowed (PetscOpts::maxits) */
+  int restart;           /* GMRES restart length (PETSc default 30) */
+  double inner_rtol;     /* mixed precision: inner FP32 reduction per refinement step */
+  int use_initial_guess; /* start from the trace already on the device */
+} hfx_solve_opts;
+
+typedef struct {
+  int status;              /* HFX_OK or an error code */
+  int iterations;          /* Krylov iterations (inner, summed) */
+  int refinements;         /* FP64 refinement steps (mixed precision) */
+  double rel_residual;     /* final FP64 ||b-Ax||/||b|| of the reference system */
+  double solve_ms;         /* device time of the solve */
+} hfx_solve_info;
+
+/* ---- context ------------------------------------------------------------ */
+int hfx_ctx_create(int device, hfx_ctx** out);
+int hfx_ctx_destroy(hfx_ctx* ctx);
+const char* hfx_last_error(const hfx_ctx* ctx);
+int hfx_version(void);
+
+/* ---- reference element (host, no GPU needed) -----------------------------
+ * Replaces ReferenceElement(dim, ord, "simplex") (ReferenceElement.cpp:5-26):
+ * nodes (ReferenceElement.cpp:614-1150), face nodes (:136-202), cubature of
+ * order 2p (:102-106, Cubature.cpp:5-139), shape functions and derivatives at
+ * the integration points (:447-480). Sizes from hfx_refel_query.
+ *   nodes[N*dim] faceNodes[F*Nf] ipCoords[nIP*dim] ipWeights[nIP]
+ *   phi[nIP*N] dphi[nIP*N*dim]; face element: fIpCoords[nIPf*(dim-1)],
+ *   fIpWeights[nIPf], fPhi[nIPf*Nf], fDphi[nIPf*Nf*(dim-1)] (any may be NULL) */
+int hfx_refel_query(int dim, int order, hfx_refel_info* info);
+int hfx_refel_tables(int dim, int order, double* nodes, int* faceNodes, double* ipCoords,
+                     double* ipWeights, double* phi, double* dphi, double* fIpCoords,
+                     double* fIpWeights, double* fPhi, double* fDphi);
+
+/* ---- mesh ------------------------------------------------------------------
+ * Replaces Mesh::setMesh + Mesh::computeFaces (Mesh.cpp:31-46,183-537). When
+ * cell2face is NULL the face topology is computed on the host with the MOAB
+ * creation-order rule (cells in order, sides in MOAB canonical order); else
+ * the caller's topology (cell2face, face2cell, faces, boundary) is used. */
+int hfx_mesh_upload(hfx_ctx* ctx, int dim, int order, int nNodes, const double* coords, int nCells,
+                    const int* cells, int nFaces, const int* cell2face, const int* face2cell,
+                    const int* faces, int nBoundary, const int* boundary);
+int hfx_mesh_sizes(hfx_ctx* ctx, int* nFaces, int* nBoundary, int64_t* nnz);
+/* Host only, no context: the same MOAB-rule topology as hfx_mesh_upload
+ * computes. Call with NULL arrays for nFaces/nBoundary, then with arrays
+ * sized cell2face[nCells*F], face2cell[2*nFaces], faces[nFaces*Nf],
+ * boundary[nBoundary]. */
+int hfx_mesh_compute_topology(int dim, int order, int nCells, const int* cells, int* nFaces, int* nBoundary,
+                              int* cell2face, int* face2cell, int* faces, int* boundary);
+int hfx_mesh_topology(hfx_ctx* ctx, int* cell2face, int* face2cell, int* faces, int* boundary);
+
+/* ---- fields (the HDGSolver field map) --------------------------------------
+ * Tau: Face field, nVals 1 or 2 (double valued, side 0 = face2cell[0]).
+ * Kappa (DiffusionTensor, HDGDiffusionSource.cpp:60-79): comps 0 (identity),
+ * 1 (scalar) or dim*dim (column-major tensor); layout 0 = per mesh node
+ * [nNodes][comps], 1 = per cell node [nCells][N][comps].
+ * Dirichlet: Face field [nFaces][Nf] (only boundary faces are read).
+ * Time scheme: implicit Euler (Euler.cpp:18-34) when dt > 0, with the previous
+ * Solution [nCells][N]. */
+int hfx_set_tau(hfx_ctx* ctx, const double* tau, int nVals);
+int hfx_set_kappa(hfx_ctx* ctx, const double* kappa, int comps, int layout);
+int hfx_set_source(hfx_ctx* ctx, int mode, const double* values, double param);
+int hfx_set_dirichlet(hfx_ctx* ctx, const double* values);
+int hfx_set_time_scheme(hfx_ctx* ctx, double dt, const double* uOld);
+int hfx_ip_coords(hfx_ctx* ctx, double* out /* [nCells][nIP][dim] */);
+
+/* ---- assembly ----------------------------------------------------------------
+ * Replaces HDGSolver::assemble (HDGSolver.cpp:166-174): element Jacobians,
+ * normals, HDGBase + HDGDiffusion + Source operators, static condensation
+ * (:331-348), Dirichlet Set (:361-529) and the scatter into the trace CSR
+ * (:531-675). All on the device, FP64. */
+int hfx_assemble(hfx_ctx* ctx);
+/* Condensed element blocks, column-major per element (any pointer may be NULL). */
+int hfx_get_condensed(hfx_ctx* ctx, double* S, double* S0, double* U, double* Q, double* U0,
+                      double* Q0);
+/* Global trace system in PETSc AIJ form: sorted columns, explicit zeros kept. */
+int hfx_get_csr(hfx_ctx* ctx, int64_t* rowptr, int* col, double* val, double* rhs);
+
+/* ---- solve and recovery --------------------------------------------------------
+ * hfx_solve replaces LinAlgebraInterface::solve / PetscInterface::solve
+ * (PetscInterface.cpp:222-247) on the assembled trace system; trace may be NULL
+ * (the result stays on the device). hfx_recover replaces the recovery loop of
+ * HDGSolver::solve (HDGSolver.cpp:741-775); NULL outputs keep
+ * Solution and Flux on the device. */
+void hfx_solve_opts_default(hfx_solve_opts* opts);
+int hfx_solve(hfx_ctx* ctx, const hfx_solve_opts* opts, double* trace, hfx_solve_info* info);
+int hfx_recover(hfx_ctx* ctx, double* solution, double* flux);
+
+/* ---- timing on the context's stream (CUDA events; no profiler) ---------------
+ * hfx_profile_enable(ctx, 1) resets and starts per-kernel event timing;
+ * hfx_kernel_time reads launches and total device ms of one kernel class
+ * (HFX_K_*). hfx_mark records an event in one of 8 slots; hfx_elapsed_ms
+ * returns the device time between two marks. hfx_synchronize waits for the
+ * context's stream. These replace the std::chrono stage timers of the
+ * reference's tests (TestHDGDiffusionSource.cpp:238-251). */
+#define HFX_K_LOCAL 0
+#define HFX_K_SCATTER 1
+#define HFX_K_SPMV64 2
+#define HFX_K_SPMV32 3
+#define HFX_K_UPDATE 4
+#define HFX_K_RECOVER 5
+#define HFX_K_OTHER 6
+int hfx_profile_enable(hfx_ctx* ctx, int on);
+int hfx_kernel_time(hfx_ctx* ctx, int kernel, int* launches, double* ms);
+int hfx_mark(hfx_ctx* ctx, int slot);
+int hfx_elapsed_ms(hfx_ctx* ctx, int slot0, int slot1, double* ms);
+int hfx_synchronize(hfx_ctx* ctx);
+
+/* ---- generic sparse system (LinAlgebraInterface, LinAlgebraInterface.h:23-162) ----
+ * The state machine initialize -> configure -> allocate -> set/add -> assemble ->
+ * solve is kept by the host C++ wrapper; these entry points take values in the
+ * reference's row-major is.size() x js.size() block convention. */
+typedef struct hfx_la hfx_la;
+int hfx_la_create(hfx_ctx* ctx, hfx_la** out);
+int hfx_la_destroy(hfx_la* la);
+int hfx_la_allocate(hfx_la* la, int ndofs);
+int hfx_la_set_values(hfx_la* la, int nr, const int* rows, int nc, const int* cols,
+                      const double* vals, int insert);
+int hfx_la_set_rhs(hfx_la* la, int n, const int* idx, const double* vals, int insert);
+int hfx_la_zero_rows(hfx_la* la, int n, const int* rows);
+int hfx_la_assemble(hfx_la* la);
+int hfx_la_clear(hfx_la* la);
+int hfx_la_solve(hfx_la* la, const hfx_solve_opts* opts, double* x, hfx_solve_info* info);
+int hfx_la_nnz(hfx_la* la, int64_t* nnz);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HFX_GB300_H */

@@ -1,0 +1,202 @@
+"""ctypes bindings of the CPU oracle (oracle/hdg_oracle.cpp).
+
+Test infrastructure only: the oracle is the checker for the CUDA path, never
+the thing measured or shipped.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(ROOT, "oracle", "_build", "libhdg_oracle.so")
+SRC_PATH = os.path.join(ROOT, "oracle", "hdg_oracle.cpp")
+
+_lib = None
+
+
+def build():
+    os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
+    if (not os.path.exists(LIB_PATH)) or os.path.getmtime(LIB_PATH) < os.path.getmtime(SRC_PATH):
+        subprocess.check_call(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-pthread",
+                               SRC_PATH, "-o", LIB_PATH])
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        vp, ip, dp = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+        L.orc_last_error.restype = ctypes.c_char_p
+        L.orc_refel_sizes.argtypes = [ip, ip, vp]
+        L.orc_refel_tables.argtypes = [ip, ip] + [vp] * 6
+        L.orc_refel_eval.argtypes = [ip, ip, ip, vp, vp, vp]
+        L.orc_problem_create.restype = vp
+        L.orc_problem_create.argtypes = [ip, ip, ip, vp, ip, vp]
+        L.orc_problem_destroy.argtypes = [vp]
+        L.orc_problem_face_counts.argtypes = [vp, vp]
+        L.orc_problem_faces.argtypes = [vp] * 5
+        L.orc_problem_set_fields.argtypes = [vp, vp, ip, vp, ip, ip, vp, vp, dp, vp]
+        L.orc_problem_ip_coords.argtypes = [vp, vp]
+        L.orc_problem_local.argtypes = [vp, ip, ip, ip]
+        L.orc_problem_assemble.argtypes = [vp, ip]
+        L.orc_problem_local_matrix.argtypes = [vp, ip, vp, vp, vp]
+        L.orc_problem_condensed.argtypes = [vp] * 7
+        L.orc_problem_nnz.restype = ctypes.c_long
+        L.orc_problem_nnz.argtypes = [vp]
+        L.orc_problem_csr.argtypes = [vp] * 5
+        L.orc_problem_solve.argtypes = [vp, dp, ip, ip, vp]
+        L.orc_problem_recover.argtypes = [vp] * 4
+        L.orc_problem_timings.argtypes = [vp, vp]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def _check(rc):
+    if rc != 0:
+        raise RuntimeError("oracle: " + lib().orc_last_error().decode())
+
+
+class RefEl:
+    def __init__(self, dim, order):
+        L = lib()
+        s = np.zeros(5, dtype=np.int32)
+        _check(L.orc_refel_sizes(dim, order, _ptr(s)))
+        self.dim, self.order = dim, order
+        self.nNodes, self.nFaces, self.nNodesFace, self.nIP, self.nIPFace = (int(v) for v in s)
+        N, F, Nf, nI = self.nNodes, self.nFaces, self.nNodesFace, self.nIP
+        self.nodes = np.zeros((N, dim))
+        self.faceNodes = np.zeros((F, Nf), dtype=np.int32)
+        self.ipX = np.zeros((nI, dim))
+        self.ipW = np.zeros(nI)
+        self.phi = np.zeros((nI, N))
+        self.dphi = np.zeros((nI, N, dim))
+        _check(L.orc_refel_tables(dim, order, _ptr(self.nodes), _ptr(self.faceNodes), _ptr(self.ipX),
+                                  _ptr(self.ipW), _ptr(self.phi), _ptr(self.dphi)))
+
+    def eval(self, pts):
+        pts = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, self.dim)
+        phi = np.zeros((pts.shape[0], self.nNodes))
+        dphi = np.zeros((pts.shape[0], self.nNodes, self.dim))
+        _check(lib().orc_refel_eval(self.dim, self.order, pts.shape[0], _ptr(pts), _ptr(phi), _ptr(dphi)))
+        return phi, dphi
+
+
+class Problem:
+    """One HDG diffusion-source problem on the oracle."""
+
+    def __init__(self, dim, order, coords, cells):
+        L = lib()
+        self.dim, self.order = dim, order
+        self.coords = np.ascontiguousarray(coords, dtype=np.float64)
+        self.cells = np.ascontiguousarray(cells, dtype=np.int32)
+        self.h = L.orc_problem_create(dim, order, self.coords.shape[0], _ptr(self.coords),
+                                      self.cells.shape[0], _ptr(self.cells))
+        if not self.h:
+            raise RuntimeError("oracle: " + L.orc_last_error().decode())
+        self.re = RefEl(dim, order)
+        c = np.zeros(2, dtype=np.int32)
+        L.orc_problem_face_counts(self.h, _ptr(c))
+        self.nFaces, self.nBoundary = int(c[0]), int(c[1])
+        F, Nf = self.re.nFaces, self.re.nNodesFace
+        nC = self.cells.shape[0]
+        self.cell2face = np.zeros((nC, F), dtype=np.int32)
+        self.face2cell = np.zeros((self.nFaces, 2), dtype=np.int32)
+        self.faces = np.zeros((self.nFaces, Nf), dtype=np.int32)
+        self.boundary = np.zeros(self.nBoundary, dtype=np.int32)
+        L.orc_problem_faces(self.h, _ptr(self.cell2face), _ptr(self.face2cell), _ptr(self.faces),
+                            _ptr(self.boundary))
+        self.nCells = nC
+        self.lenU = self.re.nNodes
+        self.lenQ = dim * self.re.nNodes
+        self.lenL = F * Nf
+        self.ndofs = self.nFaces * Nf
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_problem_destroy(self.h)
+            self.h = None
+
+    def ip_coords(self):
+        out = np.zeros((self.nCells, self.re.nIP, self.dim))
+        lib().orc_problem_ip_coords(self.h, _ptr(out))
+        return out
+
+    def set_fields(self, tau, kappa=None, src_mode=0, src=None, dirichlet=None, dt=0.0, u_old=None):
+        tau = np.ascontiguousarray(tau, dtype=np.float64)
+        tau_vals = tau.size // (self.nFaces * self.re.nNodesFace)
+        kc = 0
+        if kappa is not None:
+            kappa = np.ascontiguousarray(kappa, dtype=np.float64)
+            kc = kappa.size // (self.nCells * self.re.nNodes)
+        src = None if src is None else np.ascontiguousarray(src, dtype=np.float64)
+        dirichlet = None if dirichlet is None else np.ascontiguousarray(dirichlet, dtype=np.float64)
+        u_old = None if u_old is None else np.ascontiguousarray(u_old, dtype=np.float64)
+        self._keep = (tau, kappa, src, dirichlet, u_old)
+        _check(lib().orc_problem_set_fields(self.h, _ptr(tau), tau_vals, _ptr(kappa), kc, src_mode,
+                                            _ptr(src), _ptr(dirichlet), float(dt), _ptr(u_old)))
+
+    def local(self, nthreads=1, first=0, count=0):
+        _check(lib().orc_problem_local(self.h, nthreads, first, count))
+
+    def assemble(self, nthreads=1):
+        _check(lib().orc_problem_assemble(self.h, nthreads))
+
+    def local_matrix(self, iel):
+        n = self.lenU + self.lenQ + self.lenL
+        A = np.zeros((n, n), order="F")
+        r = np.zeros(n)
+        f2c = np.zeros(self.lenL, dtype=np.int32)
+        _check(lib().orc_problem_local_matrix(self.h, iel, A.ctypes.data, _ptr(r), _ptr(f2c)))
+        return A, r, f2c
+
+    def condensed(self):
+        nC, U, Q, L_ = self.nCells, self.lenU, self.lenQ, self.lenL
+        S = np.zeros((nC, L_ * L_))
+        S0 = np.zeros((nC, L_))
+        Um = np.zeros((nC, U * L_))
+        Qm = np.zeros((nC, Q * L_))
+        U0 = np.zeros((nC, U))
+        Q0 = np.zeros((nC, Q))
+        lib().orc_problem_condensed(self.h, _ptr(S), _ptr(S0), _ptr(Um), _ptr(Qm), _ptr(U0), _ptr(Q0))
+        return dict(S=S, S0=S0, U=Um, Q=Qm, U0=U0, Q0=Q0)
+
+    def csr(self):
+        nnz = lib().orc_problem_nnz(self.h)
+        rowptr = np.zeros(self.ndofs + 1, dtype=np.int32)
+        col = np.zeros(nnz, dtype=np.int32)
+        val = np.zeros(nnz)
+        rhs = np.zeros(self.ndofs)
+        lib().orc_problem_csr(self.h, _ptr(rowptr), _ptr(col), _ptr(val), _ptr(rhs))
+        return rowptr, col, val, rhs
+
+    def solve_gmres(self, rtol=1e-12, maxit=20000, nthreads=1):
+        x = np.zeros(self.ndofs)
+        it = lib().orc_problem_solve(self.h, rtol, maxit, nthreads, _ptr(x))
+        return x, it
+
+    def solve_direct(self):
+        import scipy.sparse as sp
+        import scipy.sparse.linalg as spla
+        rowptr, col, val, rhs = self.csr()
+        A = sp.csr_matrix((val, col, rowptr), shape=(self.ndofs, self.ndofs))
+        return spla.spsolve(A.tocsc(), rhs)
+
+    def recover(self, trace):
+        trace = np.ascontiguousarray(trace, dtype=np.float64)
+        sol = np.zeros((self.nCells, self.lenU))
+        flux = np.zeros((self.nCells, self.lenQ))
+        _check(lib().orc_problem_recover(self.h, _ptr(trace), _ptr(sol), _ptr(flux)))
+        return sol, flux
+
+    def timings(self):
+        t = np.zeros(5)
+        lib().orc_problem_timings(self.h, _ptr(t))
+        return dict(local=t[0], dirichlet=t[1], scatter=t[2], solve=t[3], recover=t[4])
