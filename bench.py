@@ -41,6 +41,7 @@ CONFIGS = {
     "cfg2": dict(dim=3, n=40, order=3, desc="3D HDG diffusion-source, unit cube 40^3x6 tets (384k), p=3"),
     "cfg1": dict(dim=2, n=32, order=2, desc="2D HDG diffusion-source, unit square 32x32x2 tris (2048), p=2"),
     "small3d": dict(dim=3, n=12, order=3, desc="3D HDG diffusion-source, 12^3x6 tets, p=3"),
+    "mid3d": dict(dim=3, n=20, order=3, desc="3D HDG diffusion-source, 20^3x6 tets (48k), p=3"),
     "cfg5mesh": dict(dim=3, n=60, order=2, desc="3D HDG diffusion-source, 60^3x6 tets (1.296M), p=2"),
 }
 

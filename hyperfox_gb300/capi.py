@@ -23,7 +23,7 @@ HFX_ERR_NAN = 7
 HFX_ERR_SINGULAR = 8
 HFX_ERR_UNSUPPORTED = 9
 
-KSP_CG, KSP_GMRES = 0, 1
+KSP_CG, KSP_GMRES, KSP_AUTO = 0, 1, 2
 PC_NONE, PC_JACOBI, PC_BLOCK_JACOBI = 0, 1, 2
 PREC_FP64, PREC_MIXED = 0, 1
 SRC_NONE, SRC_VALUES, SRC_SINPROD = 0, 1, 2

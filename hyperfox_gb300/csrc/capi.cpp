@@ -89,6 +89,7 @@ struct hfx_ctx {
   FieldBuf tau, kappa, src, dir, uold;
   int tauVals = 1;
   int kc = 0, kLayout = 0;
+  bool kappaCellConstant = true;  // symmetric trace system (CG applies)
   int srcMode = 0;
   double srcParam = 0.0;
   double dt = 0.0;
@@ -102,6 +103,7 @@ struct hfx_ctx {
   DevMem wsMem;
   TraceWorkspace ws{};
   bool wsReady = false, wsMixed = false;
+  int wsRestart = 0;
   // timing
   KernelTimer timer;
   cudaEvent_t marks[8] = {};
@@ -158,6 +160,9 @@ void free_outputs(hfx_ctx* c) {
   c->d_sol = c->d_flux = nullptr;
   c->d_status = nullptr;
   c->wsReady = false;
+  c->wsMixed = false;
+  c->wsRestart = 0;
+  c->ws = TraceWorkspace{};
   c->assembled = c->solved = false;
 }
 
@@ -377,6 +382,7 @@ int hfx_set_kappa(hfx_ctx* c, const double* kappa, int comps, int layout) {
   if (!c->haveMesh) return set_err(c, HFX_ERR_STATE, "set_kappa: upload a mesh first");
   if (comps == 0) {
     c->kc = 0;
+    c->kappaCellConstant = true;
     c->assembled = false;
     return HFX_OK;
   }
@@ -384,6 +390,27 @@ int hfx_set_kappa(hfx_ctx* c, const double* kappa, int comps, int layout) {
     return set_err(c, HFX_ERR_ARG, "set_kappa: the diffusion tensor must be scalar or dim x dim");
   c->kc = comps;
   c->kLayout = layout;
+  // A tensor that varies inside a cell makes the trace system non-symmetric
+  // (only Suq/Slq carry it, HDGDiffusion.cpp:74-145): record it for the solver.
+  {
+    const int N = c->re.nNodes;
+    const int* cells = nullptr;
+    std::vector<int> hcells;
+    if (layout == 0) {
+      hcells.resize((size_t)c->nCells * N);
+      cudaMemcpy(hcells.data(), c->d_cells, sizeof(int) * hcells.size(), cudaMemcpyDeviceToHost);
+      cells = hcells.data();
+    }
+    bool cst = true;
+    for (int64_t e = 0; e < c->nCells && cst; ++e)
+      for (int i = 1; i < N && cst; ++i)
+        for (int k = 0; k < comps && cst; ++k) {
+          double a = layout == 0 ? kappa[(int64_t)cells[e * N] * comps + k] : kappa[(e * N) * comps + k];
+          double b = layout == 0 ? kappa[(int64_t)cells[e * N + i] * comps + k] : kappa[(e * N + i) * comps + k];
+          if (a != b) cst = false;
+        }
+    c->kappaCellConstant = cst;
+  }
   size_t n = (layout == 0 ? (size_t)c->nNodes : (size_t)c->nCells * c->re.nNodes) * comps;
   return replace_field(c, &c->kappa, kappa, n);
 }
@@ -490,6 +517,9 @@ int hfx_assemble(hfx_ctx* c) {
   p.U0 = c->d_U0;
   p.Q0 = c->d_Q0;
   p.status = c->d_status;
+  p.fp32 = 0;
+  p.rhsU = p.rhsQ = nullptr;
+  p.writeOps = 1;
   c->timer.begin(K_LOCAL, s);
   HFX_CUDA(c, launch_local_condense(c->dim, c->order, p, s));
   c->timer.end(K_LOCAL, s);
@@ -572,7 +602,7 @@ int hfx_get_csr(hfx_ctx* c, int64_t* rowptr, int* col, double* val, double* rhs)
 
 void hfx_solve_opts_default(hfx_solve_opts* o) {
   if (!o) return;
-  o->method = HFX_KSP_CG;
+  o->method = HFX_KSP_AUTO;
   o->precond = HFX_PC_BLOCK_JACOBI;
   o->precision = HFX_PREC_FP64;
   o->rtol = 1e-10;
@@ -582,12 +612,19 @@ void hfx_solve_opts_default(hfx_solve_opts* o) {
   o->use_initial_guess = 0;
 }
 
-static int ensure_workspace(hfx_ctx* c, bool mixed) {
-  if (c->wsReady && (!mixed || c->wsMixed)) return HFX_OK;
+static int ensure_workspace(hfx_ctx* c, bool mixed, int restart) {
   const size_t n = (size_t)c->ndofs(), nnz = (size_t)c->nnz();
   const int NF = c->re.nNodesFace;
   DevMem& m = c->wsMem;
   TraceWorkspace& w = c->ws;
+  if (restart > c->wsRestart) {
+    // GMRES bases grow on demand (restart+1 vectors per precision)
+    HFX_CUDA(c, dalloc(m, &w.V64, n * (restart + 1)));
+    HFX_CUDA(c, dalloc(m, &w.V32, n * (restart + 1)));
+    HFX_CUDA(c, dalloc(m, &w.hdev, (size_t)restart + 1));
+    c->wsRestart = restart;
+  }
+  if (c->wsReady && (!mixed || c->wsMixed)) return HFX_OK;
   if (!c->wsReady) {
     HFX_CUDA(c, dalloc(m, &w.bS, n));
     HFX_CUDA(c, dalloc(m, &w.r, n));
@@ -625,12 +662,18 @@ int hfx_solve(hfx_ctx* c, const hfx_solve_opts* opts, double* trace, hfx_solve_i
   hfx_solve_opts o;
   if (opts) o = *opts;
   else hfx_solve_opts_default(&o);
-  if (o.method != HFX_KSP_CG) return set_err(c, HFX_ERR_UNSUPPORTED, "solve: the trace system solve is CG (use hfx_la for GMRES)");
+  if (o.method < HFX_KSP_CG || o.method > HFX_KSP_AUTO) return set_err(c, HFX_ERR_ARG, "solve: unknown method");
   if (o.precond < HFX_PC_NONE || o.precond > HFX_PC_BLOCK_JACOBI || o.rtol <= 0.0 || o.maxits <= 0)
     return set_err(c, HFX_ERR_ARG, "solve: bad options");
+  int method = o.method;
+  if (method == HFX_KSP_AUTO) method = c->kappaCellConstant ? HFX_KSP_CG : HFX_KSP_GMRES;
+  if (method == HFX_KSP_CG && !c->kappaCellConstant)
+    return set_err(c, HFX_ERR_ARG,
+                   "solve: CG needs a symmetric trace system; the diffusion tensor varies inside cells (use GMRES)");
+  const int restart = o.restart > 0 ? o.restart : 30;
   cudaSetDevice(c->device);
   bool mixed = o.precision == HFX_PREC_MIXED;
-  int rc = ensure_workspace(c, mixed);
+  int rc = ensure_workspace(c, mixed, method == HFX_KSP_GMRES ? restart : 0);
   if (rc) return rc;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
@@ -653,8 +696,9 @@ int hfx_solve(hfx_ctx* c, const hfx_solve_opts* opts, double* trace, hfx_solve_i
   a.ws = c->ws;
   a.stream = c->stream;
   a.timer = &c->timer;
+  a.restart = restart;
   TraceSolveResult res;
-  int st = trace_solve(a, &res);
+  int st = method == HFX_KSP_CG ? trace_solve(a, &res) : trace_gmres(a, &res);
   cudaEventRecord(e1, c->stream);
   cudaEventSynchronize(e1);
   float ms = 0.f;

@@ -28,7 +28,7 @@
 namespace hfx {
 namespace {
 
-template <int D, int P, int TPE, int EPC>
+template <typename T_, int D, int P, int TPE, int EPC>
 struct Layout {
   using K = Dims<D, P>;
   static constexpr int N = K::N, NF = K::NF, F = K::F, NI = K::NI, NIF = K::NIF, LL = K::LL;
@@ -65,19 +65,21 @@ struct Layout {
   static constexpr int AR = XU + XU_SZ;             // A (N*N) + RHS N*(LL+1); Gauss-Jordan before
   static constexpr int AR_SZ = (N * N + N * (LL + 1) > 2 * N * N) ? N * N + N * (LL + 1) : 2 * N * N;
   static constexpr int Q0 = AR + AR_SZ;             // D*N
-  static constexpr int GROUP = (Q0 + D * N + 1) & ~1;
+  static constexpr int WQ = Q0 + D * N;             // D*N  M^{-1} r_q (residual mode)
+  static constexpr int GROUP = (WQ + D * N + 1) & ~1;
   static constexpr int TOTAL_DOUBLES = TAB + EPC * GROUP;
   // per-group ints
   static constexpr int IGROUP = N + 2 * F;          // pivots, face ids, boundary flags
 };
 
-template <int D, int P, int TPE, int EPC>
+template <typename T, int D, int P, int TPE, int EPC>
 __global__ void __launch_bounds__(TPE * EPC)
-    local_condense_f64(LocalParams p) {
-  using L = Layout<D, P, TPE, EPC>;
+    local_condense(LocalParams p) {
+  using L = Layout<T, D, P, TPE, EPC>;
   constexpr int N = L::N, NF = L::NF, F = L::F, NI = L::NI, NIF = L::NIF, LL = L::LL, DM = L::DM;
   constexpr int LU = N, LQ = D * N;
-  extern __shared__ double smem[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* smem = reinterpret_cast<T*>(smem_raw);
   __shared__ int sFaceNodes[F * NF];
   __shared__ int sOpp[F];
   __shared__ int sPos[F * N];  // position of element node i on face f, -1 if not on it
@@ -87,7 +89,7 @@ __global__ void __launch_bounds__(TPE * EPC)
   // ---- stage tables once per CTA
   {
     constexpr int nTab = L::T_FW + NIF;
-    for (int i = threadIdx.x; i < nTab; i += nthr) smem[i] = p.tab[i];
+    for (int i = threadIdx.x; i < nTab; i += nthr) smem[i] = (T)p.tab[i];
     for (int i = threadIdx.x; i < F * NF; i += nthr) sFaceNodes[i] = p.itab[i];
     for (int i = threadIdx.x; i < F; i += nthr) sOpp[i] = p.itab[F * NF + i];
     for (int i = threadIdx.x; i < F * N; i += nthr) sPos[i] = -1;
@@ -95,41 +97,43 @@ __global__ void __launch_bounds__(TPE * EPC)
     for (int i = threadIdx.x; i < F * NF; i += nthr) sPos[(i / NF) * N + sFaceNodes[i]] = i % NF;
     __syncthreads();
   }
-  const double* phi = smem + L::T_PHI;
-  const double* dphi = smem + L::T_DPHI;
-  const double* w = smem + L::T_W;
-  const double* fphi = smem + L::T_FPHI;
-  const double* fdphi = smem + L::T_FDPHI;
-  const double* fw = smem + L::T_FW;
+  const T* phi = smem + L::T_PHI;
+  const T* dphi = smem + L::T_DPHI;
+  const T* w = smem + L::T_W;
+  const T* fphi = smem + L::T_FPHI;
+  const T* fdphi = smem + L::T_FDPHI;
+  const T* fw = smem + L::T_FW;
 
   const int grp = threadIdx.x / TPE, t = threadIdx.x % TPE;
-  double* R = smem + L::TAB + grp * L::GROUP;
+  T* R = smem + L::TAB + grp * L::GROUP;
   int* I = sInt + grp * L::IGROUP;
-  double* X = R + L::X;
-  double* kapN = R + L::KAPN;
-  double* tauL = R + L::TAUL;
-  double* dV = R + L::DV;
-  double* fq = R + L::FQ;
-  double* fu = R + L::FU;
-  double* dSt = R + L::DST;
-  double* dSn = R + L::DSN;
-  double* dSkn = R + L::DSKN;
-  double* Mm = R + L::M;
-  double* Cm = R + L::C;
-  double* Km = R + L::KS;
-  double* Tm = R + L::T;
-  double* Em = R + L::E;
-  double* Hm = R + L::H;
-  double* G = R + L::BIG;                 // [NI][N][D] dV * J^{-1} grad phi
-  double* KG = G + NI * N * D;            // [NI][N][D] dV * kappa J^{-1} grad phi
-  double* Xl = R + L::BIG;                // [D][N][LL] (after G, KG die), later Q
-  double* Xu = R + L::XU;                 // [D][N][N]
-  double* invJ = R + L::XU;               // [NI][D][D] (before Xu)
-  double* kq = invJ + NI * D * D;         // [NI][D][D]
-  double* Am = R + L::AR;                 // [N][N] row-major
-  double* Rhs = Am + N * N;               // [N][LL+1] row-major: Schur RHS columns then fu
-  double* Aug = R + L::AR;                // Gauss-Jordan [N][2N] (before Am)
-  double* Q0s = R + L::Q0;
+  T* X = R + L::X;
+  T* kapN = R + L::KAPN;
+  T* tauL = R + L::TAUL;
+  T* dV = R + L::DV;
+  T* fq = R + L::FQ;
+  T* fu = R + L::FU;
+  T* dSt = R + L::DST;
+  T* dSn = R + L::DSN;
+  T* dSkn = R + L::DSKN;
+  T* Mm = R + L::M;
+  T* Cm = R + L::C;
+  T* Km = R + L::KS;
+  T* Tm = R + L::T;
+  T* Em = R + L::E;
+  T* Hm = R + L::H;
+  T* G = R + L::BIG;                 // [NI][N][D] dV * J^{-1} grad phi
+  T* KG = G + NI * N * D;            // [NI][N][D] dV * kappa J^{-1} grad phi
+  T* Xl = R + L::BIG;                // [D][N][LL] (after G, KG die), later Q
+  T* Xu = R + L::XU;                 // [D][N][N]
+  T* invJ = R + L::XU;               // [NI][D][D] (before Xu)
+  T* kq = invJ + NI * D * D;         // [NI][D][D]
+  T* Am = R + L::AR;                 // [N][N] row-major
+  T* Rhs = Am + N * N;               // [N][LL+1] row-major: Schur RHS columns then fu
+  T* Aug = R + L::AR;                // Gauss-Jordan [N][2N] (before Am)
+  T* Q0s = R + L::Q0;
+  T* Wq = R + L::WQ;
+  const bool rhsMode = p.rhsU != nullptr;
   int* piv = I;
   int* faceId = I + N;
   int* bnd = I + N + F;
@@ -144,7 +148,7 @@ __global__ void __launch_bounds__(TPE * EPC)
       for (int i = t; i < N * D; i += TPE) X[i] = p.coords[(int64_t)cell[i / D] * D + (i % D)];
       for (int i = t; i < N * D * D; i += TPE) {
         int n = i / (D * D), a = i % (D * D);
-        double v;
+        T v;
         if (p.kc == 0) v = (a % (D + 1) == 0) ? 1.0 : 0.0;
         else {
           int64_t base_k = p.kappaLayout == 0 ? (int64_t)cell[n] * p.kc : (e * N + n) * p.kc;
@@ -169,27 +173,27 @@ __global__ void __launch_bounds__(TPE * EPC)
     // ------------------------------------------------- volume geometry
     if (active) {
       for (int q = t; q < NI; q += TPE) {
-        double J[D][D];
+        T J[D][D];
         for (int r = 0; r < D; ++r)
           for (int s = 0; s < D; ++s) {
-            double acc = 0.0;
+            T acc = 0.0;
             for (int i = 0; i < N; ++i) acc += dphi[(q * N + i) * D + r] * X[i * D + s];
             J[r][s] = acc;
           }
-        double det, iv[D][D];
+        T det, iv[D][D];
         if (D == 2) {
           det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
-          double id = 1.0 / det;
+          T id = 1.0 / det;
           iv[0][0] = J[1][1] * id;
           iv[0][1] = -J[0][1] * id;
           iv[1][0] = -J[1][0] * id;
           iv[1][1] = J[0][0] * id;
         } else {
-          double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
-          double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
-          double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+          T c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+          T c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+          T c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
           det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
-          double id = 1.0 / det;
+          T id = 1.0 / det;
           iv[0][0] = c00 * id;
           iv[1][0] = c01 * id;
           iv[2][0] = c02 * id;
@@ -200,23 +204,23 @@ __global__ void __launch_bounds__(TPE * EPC)
           iv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
           iv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
         }
-        double dv = w[q] * det;
+        T dv = w[q] * det;
         dV[q] = dv;
         for (int a = 0; a < D; ++a)
           for (int b = 0; b < D; ++b) invJ[(q * D + a) * D + b] = iv[a][b];
         for (int a = 0; a < D * D; ++a) {
-          double acc = 0.0;
+          T acc = 0.0;
           for (int i = 0; i < N; ++i) acc += phi[q * N + i] * kapN[i * D * D + a];
           kq[q * D * D + a] = acc;  // column-major d x d (HDGDiffusion.cpp:52-57)
         }
-        double fval = 0.0;
+        T fval = 0.0;
         if (p.srcMode == 1) fval = p.src[e * NI + q];
         else if (p.srcMode == 2) {
           fval = p.srcParam;
           for (int k = 0; k < D; ++k) {
-            double xk = 0.0;
+            T xk = 0.0;
             for (int i = 0; i < N; ++i) xk += phi[q * N + i] * X[i * D + k];
-            fval *= sin(M_PI * xk);
+            fval *= sin(T(M_PI) * xk);
           }
         }
         fq[q] = fval * dv;
@@ -224,31 +228,31 @@ __global__ void __launch_bounds__(TPE * EPC)
       // face geometry
       for (int fk = t; fk < F * NIF; fk += TPE) {
         int f = fk / NIF, k = fk % NIF;
-        double Jf[D - 1][D];
+        T Jf[D - 1][D];
         for (int r = 0; r < DM; ++r)
           for (int s = 0; s < D; ++s) {
-            double acc = 0.0;
+            T acc = 0.0;
             for (int i = 0; i < NF; ++i) acc += fdphi[(k * NF + i) * DM + r] * X[sFaceNodes[f * NF + i] * D + s];
             Jf[r][s] = acc;
           }
-        double nv[D], ds;
+        T nv[D], ds;
         if (D == 2) {
           ds = sqrt(Jf[0][0] * Jf[0][0] + Jf[0][1] * Jf[0][1]);
           nv[0] = -Jf[0][1];
           nv[1] = Jf[0][0];
         } else {
-          double g00 = Jf[0][0] * Jf[0][0] + Jf[0][1] * Jf[0][1] + Jf[0][2] * Jf[0][2];
-          double g11 = Jf[1][0] * Jf[1][0] + Jf[1][1] * Jf[1][1] + Jf[1][2] * Jf[1][2];
-          double g01 = Jf[0][0] * Jf[1][0] + Jf[0][1] * Jf[1][1] + Jf[0][2] * Jf[1][2];
+          T g00 = Jf[0][0] * Jf[0][0] + Jf[0][1] * Jf[0][1] + Jf[0][2] * Jf[0][2];
+          T g11 = Jf[1][0] * Jf[1][0] + Jf[1][1] * Jf[1][1] + Jf[1][2] * Jf[1][2];
+          T g01 = Jf[0][0] * Jf[1][0] + Jf[0][1] * Jf[1][1] + Jf[0][2] * Jf[1][2];
           ds = sqrt(g00 * g11 - g01 * g01);
           nv[0] = Jf[0][1] * Jf[1][2] - Jf[0][2] * Jf[1][1];
           nv[1] = Jf[0][2] * Jf[1][0] - Jf[0][0] * Jf[1][2];
           nv[2] = Jf[0][0] * Jf[1][1] - Jf[0][1] * Jf[1][0];
         }
-        double nn = 0.0;
+        T nn = 0.0;
         for (int a = 0; a < D; ++a) nn += nv[a] * nv[a];
         nn = 1.0 / sqrt(nn);
-        double prod = 0.0;
+        T prod = 0.0;
         int v0 = sFaceNodes[f * NF], vn = sOpp[f];
         for (int a = 0; a < D; ++a) {
           nv[a] *= nn;
@@ -257,14 +261,14 @@ __global__ void __launch_bounds__(TPE * EPC)
         if (prod > 0)
           for (int a = 0; a < D; ++a) nv[a] = -nv[a];
         ds *= fw[k];
-        double tq = 0.0;
+        T tq = 0.0;
         for (int i = 0; i < NF; ++i) tq += fphi[k * NF + i] * tauL[f * NF + i];
         dSt[fk] = ds * tq;
         for (int a = 0; a < D; ++a) dSn[fk * D + a] = ds * nv[a];
         for (int a = 0; a < D; ++a) {
-          double acc = 0.0;  // (kappa n)_a with kappa interpolated on the face
+          T acc = 0.0;  // (kappa n)_a with kappa interpolated on the face
           for (int b = 0; b < D; ++b) {
-            double kab = 0.0;
+            T kab = 0.0;
             for (int i = 0; i < NF; ++i) kab += fphi[k * NF + i] * kapN[sFaceNodes[f * NF + i] * D * D + a + b * D];
             acc += kab * nv[b];
           }
@@ -277,22 +281,24 @@ __global__ void __launch_bounds__(TPE * EPC)
     if (active) {
       for (int qi = t; qi < NI * N; qi += TPE) {
         int q = qi / N, i = qi % N;
-        double g[D];
+        T g[D];
         for (int a = 0; a < D; ++a) {
-          double acc = 0.0;
+          T acc = 0.0;
           for (int b = 0; b < D; ++b) acc += invJ[(q * D + a) * D + b] * dphi[(q * N + i) * D + b];
           g[a] = acc * dV[q];
         }
         for (int a = 0; a < D; ++a) {
           G[qi * D + a] = g[a];
-          double acc = 0.0;
+          T acc = 0.0;
           for (int b = 0; b < D; ++b) acc += kq[q * D * D + a + b * D] * g[b];
           KG[qi * D + a] = acc;
         }
       }
       for (int i = t; i < N; i += TPE) {
-        double acc = 0.0;
-        for (int q = 0; q < NI; ++q) acc += phi[q * N + i] * fq[q];
+        T acc = 0.0;
+        if (rhsMode) acc = (T)p.rhsU[e * N + i];
+        else
+          for (int q = 0; q < NI; ++q) acc += phi[q * N + i] * fq[q];
         fu[i] = acc;
       }
     }
@@ -301,15 +307,15 @@ __global__ void __launch_bounds__(TPE * EPC)
     if (active) {
       for (int ij = t; ij < N * N; ij += TPE) {
         int i = ij / N, j = ij % N;
-        double m = 0.0;
+        T m = 0.0;
         for (int q = 0; q < NI; ++q) m += dV[q] * phi[q * N + i] * phi[q * N + j];
         Mm[ij] = m;
       }
       for (int dij = t; dij < D * N * N; dij += TPE) {
         int d = dij / (N * N), i = (dij / N) % N, j = dij % N;
-        double c = 0.0, k = 0.0;
+        T c = 0.0, k = 0.0;
         for (int q = 0; q < NI; ++q) {
-          double pj = phi[q * N + j];
+          T pj = phi[q * N + j];
           c += G[(q * N + i) * D + d] * pj;
           k += KG[(q * N + i) * D + d] * pj;
         }
@@ -318,10 +324,10 @@ __global__ void __launch_bounds__(TPE * EPC)
       }
       for (int fab = t; fab < F * NF * NF; fab += TPE) {
         int f = fab / (NF * NF), a = (fab / NF) % NF, b = fab % NF;
-        double tt = 0.0, ee[D], hh[D];
+        T tt = 0.0, ee[D], hh[D];
         for (int d = 0; d < D; ++d) ee[d] = hh[d] = 0.0;
         for (int k = 0; k < NIF; ++k) {
-          double ss = fphi[k * NF + a] * fphi[k * NF + b];
+          T ss = fphi[k * NF + a] * fphi[k * NF + b];
           int fk = f * NIF + k;
           tt += dSt[fk] * ss;
           for (int d = 0; d < D; ++d) {
@@ -345,13 +351,13 @@ __global__ void __launch_bounds__(TPE * EPC)
       }
     __syncthreads();
     for (int k = 0; k < N; ++k) {
-      double pinv = active ? 1.0 / Aug[k * 2 * N + k] : 0.0;
+      T pinv = active ? 1.0 / Aug[k * 2 * N + k] : 0.0;
       __syncthreads();
       if (active)
         for (int ij = t; ij < N * 2 * N; ij += TPE) {
           int i = ij / (2 * N), j = ij % (2 * N);
           if (i == k || j <= k) continue;  // column k of row i is the factor: keep it
-          double f = Aug[i * 2 * N + k] * pinv;
+          T f = Aug[i * 2 * N + k] * pinv;
           Aug[ij] -= f * Aug[k * 2 * N + j];
         }
       __syncthreads();
@@ -363,18 +369,27 @@ __global__ void __launch_bounds__(TPE * EPC)
     if (active)
       for (int ij = t; ij < N * N; ij += TPE) Mm[ij] = Aug[(ij / N) * 2 * N + N + (ij % N)];
     __syncthreads();
+    // residual mode: w_d = M^{-1} r_q,d (r_q node-major (i, d))
+    if (active)
+      for (int di = t; di < D * N; di += TPE) {
+        int d = di / N, i = di % N;
+        T acc = 0.0;
+        if (rhsMode)
+          for (int m = 0; m < N; ++m) acc += Mm[i * N + m] * (T)p.rhsQ[e * N * D + m * D + d];
+        Wq[di] = acc;
+      }
     // ---- Xu_d = M^{-1} C_d ; Xl_d(:, (f,b)) = -sum_a M^{-1}(:, fn(f,a)) E_fd(a,b)
     if (active) {
       for (int dij = t; dij < D * N * N; dij += TPE) {
         int d = dij / (N * N), i = (dij / N) % N, j = dij % N;
-        double acc = 0.0;
+        T acc = 0.0;
         for (int m = 0; m < N; ++m) acc += Mm[i * N + m] * Cm[(d * N + m) * N + j];
         Xu[dij] = acc;
       }
       for (int dic = t; dic < D * N * LL; dic += TPE) {
         int d = dic / (N * LL), i = (dic / LL) % N, c = dic % LL;
         int f = c / NF, b = c % NF;
-        double acc = 0.0;
+        T acc = 0.0;
         for (int a = 0; a < NF; ++a)
           acc += Mm[i * N + sFaceNodes[f * NF + a]] * Em[((f * D + d) * NF + a) * NF + b];
         Xl[dic] = -acc;
@@ -382,7 +397,7 @@ __global__ void __launch_bounds__(TPE * EPC)
       // Suq_d(i,j) = K_d(i,j) - sum_f H_fd(pos_f(i), pos_f(j)) (in place, entry-wise)
       for (int dij = t; dij < D * N * N; dij += TPE) {
         int d = dij / (N * N), i = (dij / N) % N, j = dij % N;
-        double acc = Km[dij];
+        T acc = Km[dij];
         for (int f = 0; f < F; ++f) {
           int a = sPos[f * N + i], b = sPos[f * N + j];
           if (a >= 0 && b >= 0) acc -= Hm[((f * D + d) * NF + a) * NF + b];
@@ -393,22 +408,22 @@ __global__ void __launch_bounds__(TPE * EPC)
     __syncthreads();
     // ---- A = dt*(Suu - Suq Xu) + M_mass ; Rhs = [dt*(Sul - Suq Xl) | fu']
     // (without a time scheme dt_eff = 1 and no mass term)
-    const double dts = p.dt > 0.0 ? p.dt : 1.0;
+    const T dts = p.dt > 0.0 ? p.dt : 1.0;
     if (active) {
       for (int ij = t; ij < N * N; ij += TPE) {
         int i = ij / N, j = ij % N;
-        double suu = 0.0;
+        T suu = 0.0;
         for (int f = 0; f < F; ++f) {
           int a = sPos[f * N + i], b = sPos[f * N + j];
           if (a >= 0 && b >= 0) suu += Tm[(f * NF + a) * NF + b];
         }
-        double acc = 0.0;
+        T acc = 0.0;
         for (int d = 0; d < D; ++d)
           for (int m = 0; m < N; ++m) acc += Km[(d * N + i) * N + m] * Xu[(d * N + m) * N + j];
-        double v = suu - acc;
+        T v = suu - acc;
         if (p.dt > 0.0) {
           // mass of the time scheme: M = sum_q dV phi phi (Mass.cpp:5-38)
-          double mm = 0.0;
+          T mm = 0.0;
           for (int q = 0; q < NI; ++q) mm += dV[q] * phi[q * N + i] * phi[q * N + j];
           v = dts * v + mm;
         }
@@ -416,21 +431,27 @@ __global__ void __launch_bounds__(TPE * EPC)
       }
       for (int ic = t; ic < N * (LL + 1); ic += TPE) {
         int i = ic / (LL + 1), c = ic % (LL + 1);
-        double v;
+        T v;
         if (c < LL) {
           int f = c / NF, b = c % NF;
           int a = sPos[f * N + i];
-          double sul = (a >= 0) ? -Tm[(f * NF + a) * NF + b] : 0.0;
-          double acc = 0.0;
+          T sul = (a >= 0) ? -Tm[(f * NF + a) * NF + b] : 0.0;
+          T acc = 0.0;
           for (int d = 0; d < D; ++d)
             for (int m = 0; m < N; ++m) acc += Km[(d * N + i) * N + m] * Xl[(d * N + m) * LL + c];
           v = dts * (sul - acc);
+        } else if (rhsMode) {
+          // r_u - dt Suq M^{-1} r_q (the residual already carries the time scheme)
+          T acc = 0.0;
+          for (int d = 0; d < D; ++d)
+            for (int m = 0; m < N; ++m) acc += Km[(d * N + i) * N + m] * Wq[d * N + m];
+          v = fu[i] - dts * acc;
         } else {
           v = dts * fu[i];
           if (p.dt > 0.0) {
-            double mu = 0.0;
+            T mu = 0.0;
             for (int j = 0; j < N; ++j) {
-              double mm = 0.0;
+              T mm = 0.0;
               for (int q = 0; q < NI; ++q) mm += dV[q] * phi[q * N + i] * phi[q * N + j];
               mu += mm * p.uOld[e * N + j];
             }
@@ -446,9 +467,9 @@ __global__ void __launch_bounds__(TPE * EPC)
     for (int k = 0; k < N; ++k) {
       if (active && t == 0) {
         int pr = k;
-        double best = fabs(Am[k * N + k]);
+        T best = fabs(Am[k * N + k]);
         for (int i = k + 1; i < N; ++i) {
-          double v = fabs(Am[i * N + k]);
+          T v = fabs(Am[i * N + k]);
           if (v > best) {
             best = v;
             pr = i;
@@ -461,12 +482,12 @@ __global__ void __launch_bounds__(TPE * EPC)
         int pr = piv[k];
         if (pr != k) {
           for (int j = t; j < N; j += TPE) {
-            double tmp = Am[k * N + j];
+            T tmp = Am[k * N + j];
             Am[k * N + j] = Am[pr * N + j];
             Am[pr * N + j] = tmp;
           }
           for (int j = t; j < LL + 1; j += TPE) {
-            double tmp = Rhs[k * (LL + 1) + j];
+            T tmp = Rhs[k * (LL + 1) + j];
             Rhs[k * (LL + 1) + j] = Rhs[pr * (LL + 1) + j];
             Rhs[pr * (LL + 1) + j] = tmp;
           }
@@ -474,14 +495,14 @@ __global__ void __launch_bounds__(TPE * EPC)
       }
       __syncthreads();
       if (active) {
-        double akk = Am[k * N + k];
+        T akk = Am[k * N + k];
         if (akk == 0.0) singular = true;
-        double inv = 1.0 / akk;
+        T inv = 1.0 / akk;
         int rows = N - k - 1;
         int cols = (N - k - 1) + (LL + 1);
         for (int rc = t; rc < rows * cols; rc += TPE) {
           int i = k + 1 + rc / cols, c = rc % cols;
-          double l = Am[i * N + k] * inv;
+          T l = Am[i * N + k] * inv;
           if (c < N - k - 1) {
             int j = k + 1 + c;
             Am[i * N + j] -= l * Am[k * N + j];
@@ -497,7 +518,7 @@ __global__ void __launch_bounds__(TPE * EPC)
     if (active)
       for (int c = t; c < LL + 1; c += TPE)
         for (int i = N - 1; i >= 0; --i) {
-          double s = Rhs[i * (LL + 1) + c];
+          T s = Rhs[i * (LL + 1) + c];
           for (int j = i + 1; j < N; ++j) s -= Am[i * N + j] * Rhs[j * (LL + 1) + c];
           Rhs[i * (LL + 1) + c] = s / Am[i * N + i];
         }
@@ -514,39 +535,39 @@ __global__ void __launch_bounds__(TPE * EPC)
     if (active) {
       for (int dic = t; dic < D * N * LL; dic += TPE) {
         int d = dic / (N * LL), i = (dic / LL) % N, c = dic % LL;
-        double acc = 0.0;
+        T acc = 0.0;
         for (int m = 0; m < N; ++m) acc += Xu[(d * N + i) * N + m] * Rhs[m * (LL + 1) + c];
         Xl[dic] = -acc - Xl[dic];
       }
       for (int di = t; di < D * N; di += TPE) {
         int d = di / N, i = di % N;
-        double acc = 0.0;
+        T acc = 0.0;
         for (int m = 0; m < N; ++m) acc += Xu[(d * N + i) * N + m] * Rhs[m * (LL + 1) + LL];
-        Q0s[di] = -acc;
+        Q0s[di] = Wq[di] - acc;
       }
     }
     __syncthreads();
     // ---- outputs: U, U0, Q, Q0 (column-major, HDGSolver.cpp:337-342)
     if (active) {
-      double* Ug = p.U + e * LU * LL;
-      for (int idx = t; idx < LU * LL; idx += TPE) {
+      T* Ug = (T*)p.U + e * LU * LL;
+      for (int idx = t; p.writeOps && idx < LU * LL; idx += TPE) {
         int i = idx % LU, c = idx / LU;
         Ug[idx] = Rhs[i * (LL + 1) + c];
       }
-      for (int i = t; i < LU; i += TPE) p.U0[e * LU + i] = Rhs[i * (LL + 1) + LL];
-      double* Qg = p.Q + e * LQ * LL;
-      for (int idx = t; idx < LQ * LL; idx += TPE) {
+      for (int i = t; i < LU; i += TPE) ((T*)p.U0)[e * LU + i] = Rhs[i * (LL + 1) + LL];
+      T* Qg = (T*)p.Q + e * LQ * LL;
+      for (int idx = t; p.writeOps && idx < LQ * LL; idx += TPE) {
         int r = idx % LQ, c = idx / LQ;
         int i = r / D, d = r % D;
         Qg[idx] = Xl[(d * N + i) * LL + c];
       }
-      for (int r = t; r < LQ; r += TPE) p.Q0[e * LQ + r] = Q0s[(r % D) * N + r / D];
+      for (int r = t; r < LQ; r += TPE) ((T*)p.Q0)[e * LQ + r] = Q0s[(r % D) * N + r / D];
       // S = Sll + Slu U + Slq Q ; S0 = -Slu U0 - Slq Q0, then the Dirichlet Set rows
-      double* Sg = p.S + e * LL * LL;
-      for (int idx = t; idx < LL * LL; idx += TPE) {
+      T* Sg = (T*)p.S + e * LL * LL;
+      for (int idx = t; p.writeOps && idx < LL * LL; idx += TPE) {
         int row = idx % LL, c = idx / LL;
         int f = row / NF, a = row % NF;
-        double v;
+        T v;
         if (bnd[f]) {
           v = (row == c) ? 1.0 : 0.0;
         } else {
@@ -561,9 +582,9 @@ __global__ void __launch_bounds__(TPE * EPC)
       }
       for (int row = t; row < LL; row += TPE) {
         int f = row / NF, a = row % NF;
-        double v;
+        T v;
         if (bnd[f]) {
-          v = p.dirichlet[(int64_t)faceId[f] * NF + a];
+          v = rhsMode ? T(0) : (T)p.dirichlet[(int64_t)faceId[f] * NF + a];
         } else {
           v = 0.0;
           for (int b = 0; b < NF; ++b) {
@@ -572,18 +593,18 @@ __global__ void __launch_bounds__(TPE * EPC)
             for (int d = 0; d < D; ++d) v += Hm[((f * D + d) * NF + a) * NF + b] * Q0s[d * N + nb];
           }
         }
-        p.S0[e * LL + row] = v;
+        ((T*)p.S0)[e * LL + row] = v;
       }
     }
     __syncthreads();
   }
 }
 
-template <int D, int P, int TPE, int EPC>
+template <typename T, int D, int P, int TPE, int EPC>
 cudaError_t launch_t(const LocalParams& p, cudaStream_t s) {
-  using L = Layout<D, P, TPE, EPC>;
-  size_t smem = (size_t)L::TOTAL_DOUBLES * sizeof(double);
-  auto kern = local_condense_f64<D, P, TPE, EPC>;
+  using L = Layout<T, D, P, TPE, EPC>;
+  size_t smem = (size_t)L::TOTAL_DOUBLES * sizeof(T);
+  auto kern = local_condense<T, D, P, TPE, EPC>;
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
   int dev = 0, nsm = 0, perSM = 0;
@@ -606,23 +627,28 @@ bool local_condense_supported(int dim, int order) {
   return (dim == 2 && order >= 1 && order <= 5) || (dim == 3 && order >= 1 && order <= 3);
 }
 
-cudaError_t launch_local_condense(int dim, int order, const LocalParams& p, cudaStream_t s) {
+template <typename T>
+cudaError_t launch_any(int dim, int order, const LocalParams& p, cudaStream_t s) {
   if (dim == 2) {
     switch (order) {
-      case 1: return launch_t<2, 1, 32, 8>(p, s);
-      case 2: return launch_t<2, 2, 32, 8>(p, s);
-      case 3: return launch_t<2, 3, 64, 4>(p, s);
-      case 4: return launch_t<2, 4, 64, 4>(p, s);
-      case 5: return launch_t<2, 5, 128, 2>(p, s);
+      case 1: return launch_t<T, 2, 1, 32, 8>(p, s);
+      case 2: return launch_t<T, 2, 2, 32, 8>(p, s);
+      case 3: return launch_t<T, 2, 3, 64, 4>(p, s);
+      case 4: return launch_t<T, 2, 4, 64, 4>(p, s);
+      case 5: return launch_t<T, 2, 5, 128, 2>(p, s);
     }
   } else if (dim == 3) {
     switch (order) {
-      case 1: return launch_t<3, 1, 64, 4>(p, s);
-      case 2: return launch_t<3, 2, 128, 2>(p, s);
-      case 3: return launch_t<3, 3, 256, 1>(p, s);
+      case 1: return launch_t<T, 3, 1, 64, 4>(p, s);
+      case 2: return launch_t<T, 3, 2, 128, 2>(p, s);
+      case 3: return launch_t<T, 3, 3, 256, 1>(p, s);
     }
   }
   return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_local_condense(int dim, int order, const LocalParams& p, cudaStream_t s) {
+  return p.fp32 ? launch_any<float>(dim, order, p, s) : launch_any<double>(dim, order, p, s);
 }
 
 }  // namespace hfx

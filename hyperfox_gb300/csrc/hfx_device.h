@@ -49,8 +49,15 @@ struct LocalParams {
   const double* uOld;          // [nCells][N]
   const double* tab;           // phi, dphi, w, fphi, fdphi, fw
   const int* itab;             // faceNodes[F*NF], faceOpposite[F]
-  double *S, *S0, *U, *Q, *U0, *Q0;
+  void *S, *S0, *U, *Q, *U0, *Q0;  // double (fp32 == 0) or float (fp32 == 1)
   int* status;                 // first error: 1 = singular block
+  int fp32;                    // element arithmetic in FP32 (mixed-precision path)
+  // Residual mode (mixed-precision corrections): when rhsU is set, the element
+  // right-hand side is (rhsU, rhsQ) = the FP64 residual rows instead of the
+  // source, S0 gets no Dirichlet values, and U0/Q0 are the corrections' local parts.
+  const double* rhsU;          // [nCells][N]
+  const double* rhsQ;          // [nCells][N*D]
+  int writeOps;                // write S, U, Q (else only S0, U0, Q0)
 };
 
 cudaError_t launch_local_condense(int dim, int order, const LocalParams& p, cudaStream_t s);

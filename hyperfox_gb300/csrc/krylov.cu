@@ -103,18 +103,28 @@ __device__ __forceinline__ void face_row_spmv(const T* __restrict__ val, int64_t
   using G = GroupCfg<NF, NBMAX>;
   const int npos = nb * NF;
   const T* base = val + b0 * NF * NF;
+  // issue every value load of the face first (NF*KPL independent loads per
+  // lane), then reduce all rows: memory latency overlaps instead of
+  // serialising row by row
+  T vv[NF][G::KPL];
+#pragma unroll
+  for (int a = 0; a < NF; ++a)
+#pragma unroll
+    for (int k = 0; k < G::KPL; ++k) {
+      int m = lane + k * G::GS;
+      vv[a][k] = (m < npos) ? __ldg(base + (int64_t)a * npos + m) : T(0);
+    }
 #pragma unroll
   for (int a = 0; a < NF; ++a) {
     T acc = 0;
 #pragma unroll
-    for (int k = 0; k < G::KPL; ++k) {
-      int m = lane + k * G::GS;
-      if (m < npos) acc = fma_t<T>(base[(int64_t)a * npos + m], xv[k], acc);
-    }
-#pragma unroll
-    for (int o = G::GS / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G::GS);
+    for (int k = 0; k < G::KPL; ++k) acc = fma_t<T>(vv[a][k], xv[k], acc);
     yrow[a] = acc;
   }
+#pragma unroll
+  for (int o = G::GS / 2; o > 0; o >>= 1)
+#pragma unroll
+    for (int a = 0; a < NF; ++a) yrow[a] += __shfl_xor_sync(0xffffffffu, yrow[a], o, G::GS);
 }
 
 // K1 of CG (see the file comment).
@@ -154,16 +164,17 @@ __global__ void __launch_bounds__(kThreads) cg_spmv(TraceView A, const T* __rest
     }
     T y[NF];
     face_row_spmv<T, NF, NBMAX, MASKED>(val, b0, nb, xv, lane, y);
-    if (lane == 0 && act) {
+    if (act && lane < NF) {
+      T ya = 0;
 #pragma unroll
-      for (int a = 0; a < NF; ++a) {
-        int64_t i = f * NF + a;
-        T pi = fma_t<T>(beta, pold[i], z[i]);
-        T yi = MASKED ? (rowBnd ? pi : -y[a]) : y[a];
-        pnew[i] = pi;
-        q[i] = yi;
-        pq += (double)pi * (double)yi;
-      }
+      for (int a = 0; a < NF; ++a)
+        if (a == lane) ya = y[a];
+      int64_t i = f * NF + lane;
+      T pi = fma_t<T>(beta, pold[i], z[i]);
+      T yi = MASKED ? (rowBnd ? pi : -ya) : ya;
+      pnew[i] = pi;
+      q[i] = yi;
+      pq += (double)pi * (double)yi;
     }
   }
   double v[1] = {pq}, tot[1];
@@ -505,6 +516,7 @@ struct Driver {
     };
     cudaError_t err;
     const int gridF = grid_of(cg_spmv<double, NF, NBMAX, true>, kThreads);
+    const int gridF32 = grid_of(cg_spmv<float, NF, NBMAX, false>, kThreads);
     const int gridU = grid_of(cg_update<double, NF, 2>, kThreads);
     const int gridS = grid_of(prepare_system<NF, NBMAX>, kThreads);
     double* partials = a.ws.partials;
@@ -608,7 +620,7 @@ struct Driver {
             float* pold = (it & 1) ? p132 : p032;
             float* pnew = (it & 1) ? p032 : p132;
             tm->begin(K_SPMV32, s);
-            cg_spmv<float, NF, NBMAX, false><<<gridF, kThreads, 0, s>>>(A, a.ws.val32, z32, pold, pnew, q32, st,
+            cg_spmv<float, NF, NBMAX, false><<<gridF32, kThreads, 0, s>>>(A, a.ws.val32, z32, pold, pnew, q32, st,
                                                                         partials, it == 0);
             tm->end(K_SPMV32, s);
             tm->begin(K_UPDATE, s);
@@ -698,6 +710,51 @@ int trace_solve(const TraceSolveArgs& a, TraceSolveResult* out) {
   return 9;  // HFX_ERR_UNSUPPORTED
 }
 
-size_t trace_partials_needed() { return 3 * 152 * 32; }
+size_t trace_partials_needed() { return 64 * 152 * 32; }
+
+template <int NF, int NBMAX>
+static void prepare_t(const TraceSolveArgs& a) {
+  cudaStream_t s = a.stream;
+  const int gridS = grid_of(prepare_system<NF, NBMAX>, kThreads);
+  a.timer->begin(K_OTHER, s);
+  prepare_system<NF, NBMAX><<<gridS, kThreads, 0, s>>>(a.A, a.val, a.rhs, a.ws.bS, a.mixed ? a.ws.val32 : nullptr);
+  if (a.precond > 0)
+    build_precond<NF><<<(unsigned)((a.A.nFaces + 127) / 128), 128, 0, s>>>(a.A, a.val, a.precond, a.ws.pc64,
+                                                                           a.mixed ? a.ws.pc32 : nullptr);
+  a.timer->end(K_OTHER, s);
+}
+
+template <int NF, int NBMAX>
+static void residual_t(const TraceSolveArgs& a, TraceSolveResult* out) {
+  cudaStream_t s = a.stream;
+  CgState init{}, hst;
+  cudaMemcpyAsync(a.ws.state, &init, sizeof(CgState), cudaMemcpyHostToDevice, s);
+  const int gridF = grid_of(ref_residual<NF, NBMAX>, kThreads);
+  a.timer->begin(K_OTHER, s);
+  ref_residual<NF, NBMAX><<<gridF, kThreads, 0, s>>>(a.A, a.val, a.rhs, a.x, a.ws.state, a.ws.partials);
+  a.timer->end(K_OTHER, s);
+  cudaMemcpyAsync(&hst, a.ws.state, sizeof(CgState), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  out->rel_residual = hst.res_bb > 0 ? std::sqrt(hst.res_rr / hst.res_bb) : std::sqrt(hst.res_rr);
+}
+
+#define HFX_DISPATCH_NF(fn, ...)                                            \
+  do {                                                                      \
+    const int NF_ = a.A.NF;                                                 \
+    if (a.dim == 2) {                                                       \
+      if (NF_ == 2) fn<2, 5>(__VA_ARGS__);                                  \
+      else if (NF_ == 3) fn<3, 5>(__VA_ARGS__);                             \
+      else if (NF_ == 4) fn<4, 5>(__VA_ARGS__);                             \
+      else if (NF_ == 5) fn<5, 5>(__VA_ARGS__);                             \
+      else if (NF_ == 6) fn<6, 5>(__VA_ARGS__);                             \
+    } else {                                                                \
+      if (NF_ == 3) fn<3, 7>(__VA_ARGS__);                                  \
+      else if (NF_ == 6) fn<6, 7>(__VA_ARGS__);                             \
+      else if (NF_ == 10) fn<10, 7>(__VA_ARGS__);                           \
+    }                                                                       \
+  } while (0)
+
+void trace_prepare(const TraceSolveArgs& a) { HFX_DISPATCH_NF(prepare_t, a); }
+void trace_ref_residual(const TraceSolveArgs& a, TraceSolveResult* out) { HFX_DISPATCH_NF(residual_t, a, out); }
 
 }  // namespace hfx

@@ -32,6 +32,10 @@ struct TraceWorkspace {
   float *val32, *pc32, *r32, *z32, *p032, *p132, *q32, *d32, *rhs32;
   double* partials;
   CgState* state;
+  // GMRES: Krylov bases (restart+1 vectors) and the small device vector of coefficients
+  double* V64;
+  float* V32;
+  double* hdev;
 };
 
 struct TraceSolveArgs {
@@ -44,6 +48,7 @@ struct TraceSolveArgs {
   int mixed;          // FP32 inner CG inside FP64 refinement
   double rtol, inner_rtol;
   int maxits, max_refinements, check_every, use_initial_guess;
+  int restart;        // GMRES restart length
   TraceWorkspace ws;
   cudaStream_t stream;
   KernelTimer* timer;
@@ -56,7 +61,12 @@ struct TraceSolveResult {
 };
 
 // Returns an HFX status code (0 = converged).
-int trace_solve(const TraceSolveArgs& a, TraceSolveResult* out);
+int trace_solve(const TraceSolveArgs& a, TraceSolveResult* out);   // CG (symmetric systems)
+int trace_gmres(const TraceSolveArgs& a, TraceSolveResult* out);   // GMRES (any system)
 size_t trace_partials_needed();
+// Shared pieces: b', the FP32 copy of A' (mixed) and the preconditioner; the
+// reference-system residual into out->rel_residual.
+void trace_prepare(const TraceSolveArgs& a);
+void trace_ref_residual(const TraceSolveArgs& a, TraceSolveResult* out);
 
 }  // namespace hfx

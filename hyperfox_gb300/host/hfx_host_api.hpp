@@ -1,0 +1,289 @@
+// C++ host API over the C ABI, mirroring HyperFox's own interfaces so that a
+// HyperFox user keeps the same calls:
+//   hfx::gpu::GpuLinAlgebraInterface  ~ LinAlgebraInterface / PetscInterface
+//                                       (LinAlgebraInterface.h:23-162, PetscInterface.cpp:33-265)
+//   hfx::gpu::GpuHDGSolver            ~ HDGSolver (HDGSolver.h:16-87) with the
+//                                       field map Solution/Flux/Trace/Tau/Dirichlet
+//   hfx::gpu::Mesh / Field / models   ~ the parts of Mesh, Field, HDGDiffusionSource,
+//                                       HDGLaplaceModel and DirichletModel the path reads
+// Errors throw ErrorHandle(class, method, message) exactly where HyperFox
+// throws (calls out of order, missing fields); device failures carry the
+// library's message.
+#pragma once
+#include <cmath>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "hfx_gb300.h"
+
+namespace hfx {
+namespace gpu {
+
+class ErrorHandle : public std::exception {
+ public:
+  ErrorHandle(std::string cls, std::string method, std::string msg)
+      : what_(cls + "::" + method + ": " + msg) {}
+  const char* what() const noexcept override { return what_.c_str(); }
+
+ private:
+  std::string what_;
+};
+
+// One device context shared by the objects of a thread.
+class Device {
+ public:
+  explicit Device(int device = 0) {
+    if (hfx_ctx_create(device, &ctx_) != HFX_OK) throw ErrorHandle("Device", "Device", "no CUDA device");
+  }
+  ~Device() { hfx_ctx_destroy(ctx_); }
+  Device(const Device&) = delete;
+  Device& operator=(const Device&) = delete;
+  hfx_ctx* ctx() const { return ctx_; }
+  void check(int rc, const char* cls, const char* method) const {
+    if (rc != HFX_OK) throw ErrorHandle(cls, method, hfx_last_error(ctx_));
+  }
+
+ private:
+  hfx_ctx* ctx_ = nullptr;
+};
+
+// ---------------------------------------------------------------- LinAlgebraInterface
+struct GpuSolverOpts {  // PetscOpts (PetscOpts.h:8-29) analogue
+  int method = HFX_KSP_GMRES;
+  int precond = HFX_PC_JACOBI;
+  int precision = HFX_PREC_FP64;
+  double rtol = 1e-6;
+  int maxits = 1000;
+  int restart = 30;
+};
+
+class GpuLinAlgebraInterface {
+ public:
+  explicit GpuLinAlgebraInterface(Device* dev, GpuSolverOpts opts = GpuSolverOpts()) : dev_(dev), opts_(opts) {}
+  ~GpuLinAlgebraInterface() { destroySystem(); }
+
+  void initialize() {
+    if (!initialized) {
+      dev_->check(hfx_la_create(dev_->ctx(), &la_), "GpuLinAlgebraInterface", "initialize");
+      initialized = true;
+    }
+  }
+  void configure() {
+    if (!initialized) throw ErrorHandle("GpuLinAlgebraInterface", "configure", "the object was not initialized before being configured.");
+    configured = true;
+  }
+  void allocate(int ndofs, const std::vector<int>* diag = nullptr, const std::vector<int>* off = nullptr) {
+    (void)diag;
+    (void)off;  // the device CSR is built from the values given, no preallocation needed
+    if (!(initialized && configured))
+      throw ErrorHandle("GpuLinAlgebraInterface", "allocate", "the object was not initialized and configured before being allocated.");
+    dev_->check(hfx_la_allocate(la_, ndofs), "GpuLinAlgebraInterface", "allocate");
+    nDOFs = ndofs;
+    allocated = true;
+  }
+  void addValMatrix(int i, int j, const double& v) { vals("addValMatrix", 1, &i, 1, &j, &v, 0); }
+  void addValsMatrix(std::vector<int>& is, std::vector<int>& js, const double* v) {
+    vals("addValsMatrix", (int)is.size(), is.data(), (int)js.size(), js.data(), v, 0);
+  }
+  void addValRHS(int i, const double& v) { rhs("addValRHS", 1, &i, &v, 0); }
+  void addValsRHS(std::vector<int>& is, const double* v) { rhs("addValsRHS", (int)is.size(), is.data(), v, 0); }
+  void setValMatrix(int i, int j, const double& v) { vals("setValMatrix", 1, &i, 1, &j, &v, 1); }
+  void setValsMatrix(std::vector<int>& is, std::vector<int>& js, const double* v) {
+    vals("setValsMatrix", (int)is.size(), is.data(), (int)js.size(), js.data(), v, 1);
+  }
+  void setValRHS(int i, const double& v) { rhs("setValRHS", 1, &i, &v, 1); }
+  void setValsRHS(std::vector<int>& is, const double* v) { rhs("setValsRHS", (int)is.size(), is.data(), v, 1); }
+  void zeroOutRows(std::vector<int>& is) {
+    if (!allocated) throw ErrorHandle("GpuLinAlgebraInterface", "zeroOutRows", "the matrix must be allocated before zeroing out rows.");
+    dev_->check(hfx_la_zero_rows(la_, (int)is.size(), is.data()), "GpuLinAlgebraInterface", "zeroOutRows");
+  }
+  void assemble() {
+    if (!allocated) throw ErrorHandle("GpuLinAlgebraInterface", "assemble", "the matrix should at least be allocated before assembling.");
+    dev_->check(hfx_la_assemble(la_), "GpuLinAlgebraInterface", "assemble");
+    assembled = true;
+  }
+  void assembleFlush() { assemble(); }
+  void solve(std::vector<double>* solution) {
+    if (!assembled) throw ErrorHandle("GpuLinAlgebraInterface", "solve", "the matrix needs to be assembled before solving.");
+    solution->resize(nDOFs);
+    hfx_solve_opts o;
+    hfx_solve_opts_default(&o);
+    o.method = opts_.method;
+    o.precond = opts_.precond;
+    o.precision = opts_.precision;
+    o.rtol = opts_.rtol;
+    o.maxits = opts_.maxits;
+    o.restart = opts_.restart;
+    hfx_solve_info info;
+    dev_->check(hfx_la_solve(la_, &o, solution->data(), &info), "GpuLinAlgebraInterface", "solve");
+    lastInfo = info;
+  }
+  void getSolutionOwnership(std::vector<int>* range) {
+    if (!assembled) throw ErrorHandle("GpuLinAlgebraInterface", "getRowOwnership", "the matrix needs to be assembled before querying ownership.");
+    range->resize(nDOFs);
+    for (int i = 0; i < nDOFs; ++i) (*range)[i] = i;
+  }
+  void clearSystem() {
+    if (!assembled) throw ErrorHandle("GpuLinAlgebraInterface", "clearSystem", "the matrix needs to be assembled at least once before clearing.");
+    dev_->check(hfx_la_clear(la_), "GpuLinAlgebraInterface", "clearSystem");
+  }
+  void destroySystem() {
+    if (la_) hfx_la_destroy(la_);
+    la_ = nullptr;
+    initialized = configured = allocated = assembled = false;
+  }
+  int getNumDofs() const { return nDOFs; }
+  hfx_solve_info lastInfo{};
+
+ private:
+  void vals(const char* m, int nr, const int* r, int nc, const int* cc, const double* v, int insert) {
+    if (!allocated) throw ErrorHandle("GpuLinAlgebraInterface", m, "the matrix must be allocated before adding values.");
+    dev_->check(hfx_la_set_values(la_, nr, r, nc, cc, v, insert), "GpuLinAlgebraInterface", m);
+  }
+  void rhs(const char* m, int n, const int* i, const double* v, int insert) {
+    if (!allocated) throw ErrorHandle("GpuLinAlgebraInterface", m, "the RHS must be allocated before adding values.");
+    dev_->check(hfx_la_set_rhs(la_, n, i, v, insert), "GpuLinAlgebraInterface", m);
+  }
+  Device* dev_;
+  GpuSolverOpts opts_;
+  hfx_la* la_ = nullptr;
+  int nDOFs = 0;
+  bool initialized = false, configured = false, allocated = false, assembled = false;
+};
+
+// ---------------------------------------------------------------- mesh, fields, models
+enum FieldType { Node = 0, Face = 2, Cell = 3 };  // FieldTypes.h
+
+// Simplex mesh: nodes [nNodes][dim], cells [nCells][N] (vertices first).
+struct Mesh {
+  int dim = 0, order = 0;
+  std::vector<double> nodes;
+  std::vector<int> cells;
+  // face topology (filled by GpuHDGSolver::allocate with the MOAB rule)
+  std::vector<int> cell2face, face2cell, faces, boundary;
+  int nFaces = 0;
+  int numCells() const { return (int)(cells.size() / nodesPerCell()); }
+  int numNodes() const { return (int)(nodes.size() / dim); }
+  int nodesPerCell() const { hfx_refel_info i; hfx_refel_query(dim, order, &i); return i.nNodes; }
+  int nodesPerFace() const { hfx_refel_info i; hfx_refel_query(dim, order, &i); return i.nNodesFace; }
+  void computeFaces() {
+    int nF = 0, nB = 0;
+    if (hfx_mesh_compute_topology(dim, order, numCells(), cells.data(), &nF, &nB, nullptr, nullptr, nullptr, nullptr))
+      throw ErrorHandle("Mesh", "computeFaces", "invalid mesh");
+    cell2face.resize((size_t)numCells() * (dim + 1));
+    face2cell.resize(2 * (size_t)nF);
+    faces.resize((size_t)nF * nodesPerFace());
+    boundary.resize(nB);
+    hfx_mesh_compute_topology(dim, order, numCells(), cells.data(), &nF, &nB, cell2face.data(), face2cell.data(),
+                              faces.data(), boundary.data());
+    nFaces = nF;
+  }
+};
+
+struct Field {  // Field.h:14-34: values[entity][objPerEnt][valsPerObj]
+  Field(const Mesh* m, FieldType t, int objPerEnt, int valsPerObj) : type(t), obj(objPerEnt), vals(valsPerObj) {
+    size_t ents = t == Cell ? m->numCells() : (t == Node ? m->numNodes() : 0);
+    if (t == Face) {
+      const_cast<Mesh*>(m)->computeFaces();
+      ents = m->nFaces;
+    }
+    values.assign(ents * obj * vals, 0.0);
+  }
+  FieldType type;
+  int obj, vals;
+  std::vector<double> values;
+  std::vector<double>* getValues() { return &values; }
+};
+
+struct DirichletModel {};  // Set-type boundary model: identity rows + Dirichlet values
+
+struct HDGDiffusionSource {  // HDGDiffusionSource.h; HDGLaplaceModel = no source
+  int sourceMode = HFX_SRC_NONE;
+  double sourceParam = 0.0;
+  std::vector<double> sourceValues;  // [nCells][nIP] for HFX_SRC_VALUES
+  double dt = 0.0;                   // implicit Euler when > 0 (Euler.cpp:18-34)
+};
+struct HDGLaplaceModel : HDGDiffusionSource {};
+
+// ---------------------------------------------------------------- HDGSolver
+class GpuHDGSolver {
+ public:
+  explicit GpuHDGSolver(Device* dev) : dev_(dev) {}
+  void setMesh(Mesh* m) { mesh_ = m; }
+  void setFieldMap(std::map<std::string, Field*>* fm) { fields_ = fm; }
+  void setModel(HDGDiffusionSource* m) { model_ = m; }
+  void setBoundaryModel(DirichletModel* b) { bnd_ = b; }
+  void setLinSystem(GpuSolverOpts opts) { opts_ = opts; haveLin_ = true; }
+  void initialize() { initialized_ = true; }
+
+  void allocate() {  // HDGSolver.cpp:5-106 checks
+    if (!initialized_) throw ErrorHandle("HDGSolver", "allocate", "must initialize the solver before allocating.");
+    if (!mesh_) throw ErrorHandle("HDGSolver", "allocate", "must set the Mesh before allocating.");
+    if (!haveLin_) throw ErrorHandle("HDGSolver", "allocate", "must set the linear system before allocating.");
+    if (!model_) throw ErrorHandle("HDGSolver", "allocate", "must set the model before allocating.");
+    if (!bnd_) throw ErrorHandle("HDGSolver", "allocate", "must set the boundary model before allocating.");
+    if (!fields_ || fields_->empty()) throw ErrorHandle("HDGSolver", "allocate", "must set the fields before allocating.");
+    for (const char* f : {"Solution", "Flux", "Tau", "Trace"})
+      if (!fields_->count(f)) throw ErrorHandle("HDGSolver", "allocate", std::string("the field map must have a ") + f + " field.");
+    if (fields_->at("Solution")->type != Cell) throw ErrorHandle("HDGSolver", "allocate", "the Solution field must be a cell field.");
+    if (fields_->at("Flux")->type != Cell) throw ErrorHandle("HDGSolver", "allocate", "the Flux field must be a cell field.");
+    if (fields_->at("Tau")->type != Face) throw ErrorHandle("HDGSolver", "allocate", "the Tau field must be a face field.");
+    if (fields_->at("Trace")->type != Face) throw ErrorHandle("HDGSolver", "allocate", "the Trace field must be a face field.");
+    mesh_->computeFaces();
+    dev_->check(hfx_mesh_upload(dev_->ctx(), mesh_->dim, mesh_->order, mesh_->numNodes(), mesh_->nodes.data(),
+                                mesh_->numCells(), mesh_->cells.data(), mesh_->nFaces, mesh_->cell2face.data(),
+                                mesh_->face2cell.data(), mesh_->faces.data(), (int)mesh_->boundary.size(),
+                                mesh_->boundary.data()),
+                "HDGSolver", "allocate");
+    allocated_ = true;
+  }
+
+  void assemble() {
+    if (!(initialized_ && allocated_)) throw ErrorHandle("HDGSolver", "assemble", "the solver must be initialized and allocated before assembling.");
+    Field* tau = fields_->at("Tau");
+    dev_->check(hfx_set_tau(dev_->ctx(), tau->values.data(), tau->vals), "HDGSolver", "assemble");
+    if (fields_->count("Dirichlet"))
+      dev_->check(hfx_set_dirichlet(dev_->ctx(), fields_->at("Dirichlet")->values.data()), "HDGSolver", "assemble");
+    if (fields_->count("DiffusionTensor")) {
+      Field* k = fields_->at("DiffusionTensor");
+      dev_->check(hfx_set_kappa(dev_->ctx(), k->values.data(), k->vals, k->type == Node ? 0 : 1), "HDGSolver", "assemble");
+    }
+    dev_->check(hfx_set_source(dev_->ctx(), model_->sourceMode,
+                               model_->sourceValues.empty() ? nullptr : model_->sourceValues.data(), model_->sourceParam),
+                "HDGSolver", "assemble");
+    if (model_->dt > 0.0)
+      dev_->check(hfx_set_time_scheme(dev_->ctx(), model_->dt, fields_->at("Solution")->values.data()), "HDGSolver", "assemble");
+    dev_->check(hfx_assemble(dev_->ctx()), "HDGSolver", "assemble");
+    assembled_ = true;
+  }
+
+  void solve() {
+    if (!assembled_) throw ErrorHandle("HDGSolver", "solve", "system must be assembled before solving");
+    hfx_solve_opts o;
+    hfx_solve_opts_default(&o);
+    o.precond = opts_.precond;
+    o.precision = opts_.precision;
+    o.rtol = opts_.rtol;
+    o.maxits = opts_.maxits;
+    o.restart = opts_.restart;
+    o.method = opts_.method;
+    dev_->check(hfx_solve(dev_->ctx(), &o, fields_->at("Trace")->values.data(), &lastInfo), "HDGSolver", "solve");
+    dev_->check(hfx_recover(dev_->ctx(), fields_->at("Solution")->values.data(), fields_->at("Flux")->values.data()),
+                "HDGSolver", "solve");
+  }
+  hfx_solve_info lastInfo{};
+
+ private:
+  Device* dev_;
+  Mesh* mesh_ = nullptr;
+  std::map<std::string, Field*>* fields_ = nullptr;
+  HDGDiffusionSource* model_ = nullptr;
+  DirichletModel* bnd_ = nullptr;
+  GpuSolverOpts opts_;
+  bool haveLin_ = false, initialized_ = false, allocated_ = false, assembled_ = false;
+};
+
+}  // namespace gpu
+}  // namespace hfx

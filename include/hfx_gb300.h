@@ -46,6 +46,8 @@ extern "C" {
 /* Krylov method / preconditioner / precision (PetscOpts.h:8-29 analogue). */
 #define HFX_KSP_CG 0        /* CG on the symmetric-eliminated trace system */
 #define HFX_KSP_GMRES 1     /* restarted GMRES, any nonsingular system */
+#define HFX_KSP_AUTO 2      /* CG when the trace system is symmetric (diffusion tensor constant
+                               inside every cell), else GMRES (the default) */
 #define HFX_PC_NONE 0
 #define HFX_PC_JACOBI 1
 #define HFX_PC_BLOCK_JACOBI 2 /* one dense block per face (HDG trace systems) */

@@ -1216,6 +1216,26 @@ int orc_refel_tables(int dim, int order, double* nodes, int* faceNodes, double* 
   })
 }
 
+// Cubature rule of a given polynomial order (Cubature.cpp nIPMap); returns the
+// number of points (negative if cap is too small).
+int orc_cubature(int dim, int order, double* X, double* W, int cap) {
+  try {
+    std::vector<std::vector<double>> x;
+    std::vector<double> w;
+    simplex_cubature(dim, order, x, w);
+    int n = (int)w.size();
+    if (n > cap) return -n;
+    for (int i = 0; i < n; ++i) {
+      for (int k = 0; k < dim; ++k) X[i * dim + k] = x[i][k];
+      W[i] = w[i];
+    }
+    return n;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return -1000000;
+  }
+}
+
 // Lagrange basis / gradients at arbitrary reference points (for the reference's
 // Lagrange-property and monomial tests, TestReferenceElement.cpp:117-236).
 int orc_refel_eval(int dim, int order, int npts, const double* pts, double* phi, double* dphi) {

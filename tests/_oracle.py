@@ -34,6 +34,7 @@ def lib():
         L.orc_refel_sizes.argtypes = [ip, ip, vp]
         L.orc_refel_tables.argtypes = [ip, ip] + [vp] * 6
         L.orc_refel_eval.argtypes = [ip, ip, ip, vp, vp, vp]
+        L.orc_cubature.argtypes = [ip, ip, vp, vp, ip]
         L.orc_problem_create.restype = vp
         L.orc_problem_create.argtypes = [ip, ip, ip, vp, ip, vp]
         L.orc_problem_destroy.argtypes = [vp]
@@ -62,6 +63,15 @@ def _ptr(a):
 def _check(rc):
     if rc != 0:
         raise RuntimeError("oracle: " + lib().orc_last_error().decode())
+
+
+def cubature(dim, order):
+    X = np.zeros((200, dim))
+    W = np.zeros(200)
+    n = lib().orc_cubature(dim, order, _ptr(X), _ptr(W), 200)
+    if n < 0:
+        raise RuntimeError("oracle cubature(%d, %d) failed" % (dim, order))
+    return X[:n].copy(), W[:n].copy()
 
 
 class RefEl:

@@ -1,0 +1,152 @@
+// The reference's own unit tests, re-expressed against the C++ host API
+// (TestLinAlgebraInterfaces.cpp:23-150, TestHDGSolver.cpp:14-101).
+// Exits non-zero on the first failed check.
+#include <cmath>
+#include <cstdio>
+#include <functional>
+#include <vector>
+
+#include "../../hyperfox_gb300/host/hfx_host_api.hpp"
+
+using namespace hfx::gpu;
+
+static int failures = 0;
+#define CHECK(c)                                                   \
+  do {                                                             \
+    if (!(c)) {                                                    \
+      std::printf("FAILED %s:%d: %s\n", __FILE__, __LINE__, #c);   \
+      ++failures;                                                  \
+    }                                                              \
+  } while (0)
+static bool throws(const std::function<void()>& f) {
+  try {
+    f();
+  } catch (const ErrorHandle&) {
+    return true;
+  }
+  return false;
+}
+
+int main() {
+  Device dev(0);
+  {  // ordering of initialize -> configure -> allocate (TestLinAlgebraInterfaces.cpp:23-67)
+    GpuSolverOpts o;
+    o.rtol = 1e-16;
+    GpuLinAlgebraInterface L(&dev, o);
+    int i = 0, j = 0;
+    double val = 1;
+    std::vector<double> dv = {1};
+    std::vector<int> iv = {0};
+    CHECK(throws([&] { L.solve(&dv); }));
+    CHECK(throws([&] { L.assemble(); }));
+    CHECK(throws([&] { L.setValsRHS(iv, dv.data()); }));
+    CHECK(throws([&] { L.setValMatrix(i, j, val); }));
+    CHECK(throws([&] { L.allocate(1); }));
+    CHECK(throws([&] { L.configure(); }));
+    L.initialize();
+    CHECK(throws([&] { L.solve(&dv); }));
+    CHECK(throws([&] { L.allocate(1); }));
+    L.configure();
+    CHECK(throws([&] { L.setValRHS(i, val); }));
+    L.allocate(1);
+    L.setValsRHS(iv, dv.data());
+    L.setValRHS(i, val);
+    L.setValsMatrix(iv, iv, dv.data());
+    L.setValMatrix(i, j, val);
+    L.assemble();
+    L.solve(&dv);
+    CHECK(std::fabs(dv[0] - 1.0) < 1e-12);
+    L.clearSystem();
+  }
+  {  // identity and triangular systems (TestLinAlgebraInterfaces.cpp:70-120)
+    GpuSolverOpts o;
+    o.rtol = 1e-16;
+    o.maxits = 5000;
+    GpuLinAlgebraInterface L(&dev, o);
+    for (int k = 1; k <= 40; k += 13) {
+      L.destroySystem();
+      L.initialize();
+      L.configure();
+      L.allocate(k);
+      for (int r = 0; r < k; ++r) {
+        for (int c = 0; c <= r; ++c) L.setValMatrix(r, c, 1.0);
+        L.setValRHS(r, 1.0);
+      }
+      L.assemble();
+      std::vector<double> sol;
+      L.solve(&sol);
+      for (int r = 0; r < k; ++r) CHECK(std::fabs(sol[r] - (r == 0 ? 1.0 : 0.0)) < 1e-12);
+    }
+  }
+  {  // HDGSolver setup sequence and the constant Dirichlet solve (TestHDGSolver.cpp:14-101)
+    Mesh m;
+    m.dim = 2;
+    m.order = 2;
+    // 4x4 squares, two triangles each, p=2 nodes built from the reference nodes
+    const int n = 4;
+    hfx_refel_info info;
+    hfx_refel_query(2, 2, &info);
+    std::vector<double> rn(info.nNodes * 2);
+    hfx_refel_tables(2, 2, rn.data(), nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+    std::vector<double> pts;
+    std::vector<int> cells;
+    auto node_id = [&](double x, double y) {
+      for (size_t k = 0; k < pts.size() / 2; ++k)
+        if (std::fabs(pts[2 * k] - x) < 1e-12 && std::fabs(pts[2 * k + 1] - y) < 1e-12) return (int)k;
+      pts.push_back(x);
+      pts.push_back(y);
+      return (int)(pts.size() / 2 - 1);
+    };
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        double h = 1.0 / n, x0 = i * h, y0 = j * h;
+        double tri[2][3][2] = {{{x0, y0}, {x0 + h, y0}, {x0, y0 + h}}, {{x0 + h, y0 + h}, {x0, y0 + h}, {x0 + h, y0}}};
+        for (auto& t : tri)
+          for (int a = 0; a < info.nNodes; ++a) {
+            double l1 = 0.5 * (rn[2 * a] + 1), l2 = 0.5 * (rn[2 * a + 1] + 1);
+            double x = t[0][0] + l1 * (t[1][0] - t[0][0]) + l2 * (t[2][0] - t[0][0]);
+            double y = t[0][1] + l1 * (t[1][1] - t[0][1]) + l2 * (t[2][1] - t[0][1]);
+            cells.push_back(node_id(x, y));
+          }
+      }
+    m.nodes = pts;
+    m.cells = cells;
+    Field sol(&m, Cell, info.nNodes, 1), flux(&m, Cell, info.nNodes, 2);
+    Field dir(&m, Face, info.nNodesFace, 1), lambda(&m, Face, info.nNodesFace, 1), tau(&m, Face, info.nNodesFace, 1);
+    std::fill(dir.values.begin(), dir.values.end(), 3.0);
+    std::fill(tau.values.begin(), tau.values.end(), 1.0);
+    std::map<std::string, Field*> fm;
+    DirichletModel dirMod;
+    HDGLaplaceModel lap;
+    GpuSolverOpts o;
+    o.rtol = 1e-14;
+    o.maxits = 20000;
+    o.method = HFX_KSP_CG;
+    GpuHDGSolver s(&dev);
+    CHECK(throws([&] { s.solve(); }));
+    CHECK(throws([&] { s.assemble(); }));
+    CHECK(throws([&] { s.allocate(); }));
+    s.setMesh(&m);
+    fm["Solution"] = &sol;
+    fm["Flux"] = &flux;
+    fm["Trace"] = &lambda;
+    fm["Dirichlet"] = &dir;
+    fm["Tau"] = &tau;
+    s.setFieldMap(&fm);
+    s.setLinSystem(o);
+    s.setModel(&lap);
+    CHECK(throws([&] { s.allocate(); }));
+    s.setBoundaryModel(&dirMod);
+    CHECK(throws([&] { s.allocate(); }));  // not initialized
+    s.initialize();
+    s.allocate();
+    CHECK(throws([&] { s.solve(); }));
+    s.assemble();
+    s.solve();
+    for (double v : sol.values) CHECK(std::fabs(v - 3.0) < 1e-12);
+    for (double v : flux.values) CHECK(std::fabs(v) < 1e-11);
+    for (double v : lambda.values) CHECK(std::fabs(v - 3.0) < 1e-12);
+  }
+  std::printf("%s (%d failures)\n", failures ? "FAIL" : "OK", failures);
+  return failures ? 1 : 0;
+}

@@ -28,6 +28,8 @@ def fields(dim, order, coords, cells, faces, nfaces, rng, tau2=False, kappa="non
         tau = rng.uniform(0.5, 2.0, size=(nfaces, Nf, 1))
     if kappa == "scalar":
         kap = rng.uniform(0.5, 3.0, size=(cells.shape[0], N, 1))
+    elif kappa == "cell":  # constant inside each cell: symmetric trace system
+        kap = np.repeat(rng.uniform(0.5, 3.0, size=(cells.shape[0], 1, 1)), N, axis=1)
     elif kappa == "tensor":
         A = rng.normal(size=(cells.shape[0], N, dim, dim)) * 0.3
         kap = np.einsum("enij,enkj->enik", A, A) + np.eye(dim)

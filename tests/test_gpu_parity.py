@@ -80,9 +80,11 @@ def test_topology_matches_oracle(hfx_lib):
 
 @pytest.mark.parametrize("dim,n,order", [(2, 8, 2), (2, 4, 4), (3, 2, 2), (3, 2, 3)])
 @pytest.mark.parametrize("precision", [0, 1])
-def test_solve_and_recover(hfx_lib, dim, n, order, precision):
+@pytest.mark.parametrize("kappa", ["cell", "scalar"])
+def test_solve_and_recover(hfx_lib, dim, n, order, precision, kappa):
+    """kappa constant per cell: CG (symmetric system); nodal kappa: GMRES."""
     from hyperfox_gb300 import capi
-    P, ctx, _ = build_pair(hfx_lib, dim, n, order, tau2=False, kappa="scalar")
+    P, ctx, _ = build_pair(hfx_lib, dim, n, order, tau2=False, kappa=kappa)
     P.assemble()
     ctx.assemble()
     x_ref = P.solve_direct()
@@ -95,6 +97,27 @@ def test_solve_and_recover(hfx_lib, dim, n, order, precision):
     osol, oflux = P.recover(trace)
     assert relerr(sol, osol) < REL
     assert relerr(flux, oflux) < REL
+
+
+def test_cg_refused_on_nonsymmetric_system(hfx_lib):
+    from hyperfox_gb300 import capi
+    P, ctx, _ = build_pair(hfx_lib, 2, 4, 2, tau2=False, kappa="scalar")
+    ctx.assemble()
+    with pytest.raises(capi.HfxError) as ei:
+        ctx.solve(method=capi.KSP_CG)
+    assert ei.value.code == capi.HFX_ERR_ARG
+
+
+@pytest.mark.parametrize("method", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_gmres_and_cg_agree_on_symmetric_system(hfx_lib, method, precision):
+    P, ctx, _ = build_pair(hfx_lib, 3, 2, 3, tau2=True, kappa="cell")
+    P.assemble()
+    ctx.assemble()
+    x_ref = P.solve_direct()
+    trace, info = ctx.solve(method=method, precision=precision, rtol=1e-13, restart=40)
+    assert np.linalg.norm(trace - x_ref) / np.linalg.norm(x_ref) < 1e-8
+    assert info.rel_residual < 1e-12
 
 
 @pytest.mark.parametrize("pc", [0, 1, 2])
