@@ -38,7 +38,11 @@ EXPORTED = [
     "hfx_solve_opts_default", "hfx_solve", "hfx_recover",
     "hfx_la_create", "hfx_la_destroy", "hfx_la_allocate", "hfx_la_set_values", "hfx_la_set_rhs",
     "hfx_la_zero_rows", "hfx_la_assemble", "hfx_la_clear", "hfx_la_solve", "hfx_la_nnz",
+    "hfx_profile_enable", "hfx_kernel_time", "hfx_mark", "hfx_elapsed_ms", "hfx_synchronize",
+    "hfx_trace_solve_noalloc",
 ]
+NOALLOC_MAX_DOFS = 65536
+NOALLOC_MAX_NF = 10
 
 
 class HfxError(RuntimeError):
@@ -107,6 +111,12 @@ def load(path=LIB_PATH):
         "hfx_la_clear": ([vp], ip),
         "hfx_la_solve": ([vp, ctypes.POINTER(SolveOpts), vp, ctypes.POINTER(SolveInfo)], ip),
         "hfx_la_nnz": ([vp, vp], ip),
+        "hfx_profile_enable": ([vp, ip], ip),
+        "hfx_kernel_time": ([vp, ip, vp, vp], ip),
+        "hfx_mark": ([vp, ip], ip),
+        "hfx_elapsed_ms": ([vp, ip, ip, vp], ip),
+        "hfx_synchronize": ([vp], ip),
+        "hfx_trace_solve_noalloc": ([ip, ip, ip, vp, vp, vp, vp, vp, vp, dp, ip, vp, ctypes.POINTER(SolveInfo)], ip),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)

@@ -194,6 +194,29 @@ int hfx_la_clear(hfx_la* la);
 int hfx_la_solve(hfx_la* la, const hfx_solve_opts* opts, double* x, hfx_solve_info* info);
 int hfx_la_nnz(hfx_la* la, int64_t* nnz);
 
+/* ---- allocation-free trace solve -------------------------------------------
+ * No counterpart in the reference. For callers that cannot allocate device
+ * memory: code running while a stream is captured into a CUDA graph, code
+ * under a framework whose caching allocator owns the device memory, real-time
+ * loops that forbid allocation latency. Same FP64 CG + per-face block-Jacobi
+ * solve as hfx_solve (HFX_KSP_CG, HFX_PC_BLOCK_JACOBI) on a trace system the
+ * caller already holds in device memory: browptr[nFaces+1] and bcol[nBlocks]
+ * (face-block pattern), isBoundary[nFaces] (Dirichlet faces), val in the
+ * scalar-CSR order hfx_get_csr exports, rhs and the output x [nFaces*nodesPerFace];
+ * stream is a cudaStream_t. The solver's working memory is one fixed
+ * __device__ array (about 7.9 MB, held by every GPU that loads the library
+ * until exit), so systems above HFX_NOALLOC_MAX_DOFS trace DOFs or
+ * HFX_NOALLOC_MAX_NF nodes per face are refused with HFX_ERR_ARG. The first
+ * call on a device looks up the array's device address: make that first call
+ * before any stream capture. Calls share the array; calls that overlap on the
+ * GPU race and must be serialised by the caller. Returns after convergence
+ * (it synchronises the stream); info may be NULL. */
+#define HFX_NOALLOC_MAX_DOFS 65536
+#define HFX_NOALLOC_MAX_NF 10
+int hfx_trace_solve_noalloc(int dim, int nodesPerFace, int nFaces, const int64_t* browptr, const int* bcol,
+                            const unsigned char* isBoundary, const double* val, const double* rhs, double* x,
+                            double rtol, int maxits, void* stream, hfx_solve_info* info);
+
 #ifdef __cplusplus
 }
 #endif
