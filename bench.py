@@ -168,20 +168,22 @@ def run_ours(args, world, rank, local):
     ctx.set_dirichlet(dir_h)
     ctx.set_source(capi.SRC_SINPROD, param=dim * np.pi ** 2)
     L = ctx.L
-    prec = capi.PREC_MIXED if args.precision == "mixed" else capi.PREC_FP64
+    prec = capi.PREC_FP64 if args.precision == "fp64" else capi.PREC_MIXED
     opts = capi.solve_opts(precision=prec, rtol=args.rtol, precond=capi.PC_BLOCK_JACOBI, maxits=200000,
                            inner_rtol=args.inner_rtol)
     info = capi.SolveInfo()
 
+    asm_prec = capi.PREC_MIXED if args.precision == "mixed" else capi.PREC_FP64
+
     def step_device():
-        ctx._chk(L.hfx_assemble(ctx.h), "assemble")
+        ctx._chk(L.hfx_assemble_ex(ctx.h, asm_prec), "assemble")
         ctx._chk(L.hfx_solve(ctx.h, capi.ctypes.byref(opts), None, capi.ctypes.byref(info)), "solve")
         ctx._chk(L.hfx_recover(ctx.h, None, None), "recover")
 
     def step_e2e():
         ctx.set_tau(tau_h)
         ctx.set_dirichlet(dir_h)
-        ctx._chk(L.hfx_assemble(ctx.h), "assemble")
+        ctx._chk(L.hfx_assemble_ex(ctx.h, asm_prec), "assemble")
         ctx._chk(L.hfx_solve(ctx.h, capi.ctypes.byref(opts), capi._p(trace_h), capi.ctypes.byref(info)), "solve")
         ctx._chk(L.hfx_recover(ctx.h, capi._p(sol_h), capi._p(flux_h)), "recover")
 
@@ -209,7 +211,7 @@ def run_ours(args, world, rank, local):
     dev_ms = barrier_max(world, ms.value)
     kt = {}
     for name, kid in (("local", 0), ("scatter", 1), ("spmv64", 2), ("spmv32", 3), ("update", 4), ("recover", 5),
-                      ("other", 6)):
+                      ("other", 6), ("residual", 7)):
         n_l, t_l = capi.ctypes.c_int(), capi.ctypes.c_double()
         L.hfx_kernel_time(ctx.h, kid, capi.ctypes.byref(n_l), capi.ctypes.byref(t_l))
         kt[name] = (n_l.value, t_l.value)
@@ -217,6 +219,7 @@ def run_ours(args, world, rank, local):
     iters, refinements = info.iterations, info.refinements
     # accuracy of the last solve vs the FP64 reference
     x = np.zeros(ctx.ndofs)
+    ctx._chk(L.hfx_assemble_ex(ctx.h, asm_prec), "assemble")
     ctx._chk(L.hfx_solve(ctx.h, capi.ctypes.byref(opts), capi._p(x), capi.ctypes.byref(info)), "solve")
     rel_err = float(np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref))
     # e2e timed region (host buffers, copies inside)
@@ -231,7 +234,7 @@ def run_ours(args, world, rank, local):
     d2h = trace_h.nbytes + sol_h.nbytes + flux_h.nbytes
     # plain FP64 GPU time-to-solve (same tolerance), for the learned+mixed vs plain comparison
     plain = None
-    if args.precision == "mixed" and not args.no_plain:
+    if args.precision != "fp64" and not args.no_plain:
         fp_opts = capi.solve_opts(precision=capi.PREC_FP64, rtol=args.rtol, precond=capi.PC_BLOCK_JACOBI, maxits=500000)
         fp_info = capi.SolveInfo()
         ctx._chk(L.hfx_mark(ctx.h, 2), "mark")
@@ -249,7 +252,7 @@ def run_ours(args, world, rank, local):
     hbm, peak_kind = peaks()
     nnz, n = ctx.nnz, ctx.ndofs
     nblocks = nnz // (Nf * Nf)
-    dom = max(("local", "spmv64", "spmv32", "update", "scatter", "recover"), key=lambda k: kt[k][1])
+    dom = max(("local", "spmv64", "spmv32", "update", "scatter", "recover", "residual"), key=lambda k: kt[k][1])
     roof = None
     if dom in ("spmv32", "spmv64"):
         sv = 4 if dom == "spmv32" else 8
@@ -342,9 +345,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="cfg2", choices=sorted(CONFIGS))
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--rtol", type=float, default=1e-10)
-    ap.add_argument("--inner-rtol", type=float, default=1e-4)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "mixed-trace", "fp64"],
+                    help="mixed: FP32 assembly + FP64 full-system refinement; mixed-trace: FP64 assembly, "
+                         "FP32 Krylov inside FP64 trace-system refinement; fp64: plain FP64")
+    ap.add_argument("--rtol", type=float, default=1e-10,
+                    help="fp64: trace-system relative residual; mixed: full HDG system relative residual")
+    ap.add_argument("--inner-rtol", type=float, default=1e-5)
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

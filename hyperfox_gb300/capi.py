@@ -34,7 +34,7 @@ EXPORTED = [
     "hfx_refel_query", "hfx_refel_tables",
     "hfx_mesh_upload", "hfx_mesh_sizes", "hfx_mesh_topology", "hfx_mesh_compute_topology",
     "hfx_set_tau", "hfx_set_kappa", "hfx_set_source", "hfx_set_dirichlet", "hfx_set_time_scheme",
-    "hfx_ip_coords", "hfx_assemble", "hfx_get_condensed", "hfx_get_csr",
+    "hfx_ip_coords", "hfx_assemble", "hfx_assemble_ex", "hfx_get_condensed", "hfx_get_csr",
     "hfx_solve_opts_default", "hfx_solve", "hfx_recover",
     "hfx_la_create", "hfx_la_destroy", "hfx_la_allocate", "hfx_la_set_values", "hfx_la_set_rhs",
     "hfx_la_zero_rows", "hfx_la_assemble", "hfx_la_clear", "hfx_la_solve", "hfx_la_nnz",
@@ -96,6 +96,7 @@ def load(path=LIB_PATH):
         "hfx_set_time_scheme": ([vp, dp, vp], ip),
         "hfx_ip_coords": ([vp, vp], ip),
         "hfx_assemble": ([vp], ip),
+        "hfx_assemble_ex": ([vp, ip], ip),
         "hfx_get_condensed": ([vp] * 7, ip),
         "hfx_get_csr": ([vp] * 5, ip),
         "hfx_solve_opts_default": ([ctypes.POINTER(SolveOpts)], None),
@@ -269,8 +270,8 @@ class Context:
         return out
 
     # ---- hot path
-    def assemble(self):
-        self._chk(self.L.hfx_assemble(self.h), "assemble")
+    def assemble(self, precision=PREC_FP64):
+        self._chk(self.L.hfx_assemble_ex(self.h, precision), "assemble")
 
     def condensed(self):
         E, U, Q, Ll = self.nCells, self.lenU, self.lenQ, self.lenL

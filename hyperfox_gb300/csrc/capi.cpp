@@ -14,6 +14,7 @@
 
 #include "../../include/hfx_gb300.h"
 #include "hfx_device.h"
+#include "hdg_mixed.h"
 #include "hfx_host.h"
 #include "krylov.h"
 #include "la_gmres.h"
@@ -104,6 +105,13 @@ struct hfx_ctx {
   TraceWorkspace ws{};
   bool wsReady = false, wsMixed = false;
   int wsRestart = 0;
+  // mixed-precision state: FP32 element blocks, FP64 residual rows
+  bool mixedMode = false;
+  DevMem mixMem;
+  float *d_S32 = nullptr, *d_S032 = nullptr, *d_U32 = nullptr, *d_Q32 = nullptr, *d_U032 = nullptr,
+        *d_Q032 = nullptr, *d_dl32 = nullptr;
+  double *d_ru = nullptr, *d_rq = nullptr, *d_rl = nullptr, *d_rtrace = nullptr, *d_part = nullptr;
+  double mixedBB = 0.0, mixedRR = 0.0;
   // timing
   KernelTimer timer;
   cudaEvent_t marks[8] = {};
@@ -158,6 +166,10 @@ void free_outputs(hfx_ctx* c) {
   c->wsMem.release();
   c->d_S = c->d_S0 = c->d_U = c->d_Q = c->d_U0 = c->d_Q0 = c->d_val = c->d_rhs = c->d_trace = nullptr;
   c->d_sol = c->d_flux = nullptr;
+  c->mixMem.release();
+  c->d_S32 = c->d_S032 = c->d_U32 = c->d_Q32 = c->d_U032 = c->d_Q032 = c->d_dl32 = nullptr;
+  c->d_ru = c->d_rq = c->d_rl = c->d_rtrace = c->d_part = nullptr;
+  c->mixedMode = false;
   c->d_status = nullptr;
   c->wsReady = false;
   c->wsMixed = false;
@@ -192,6 +204,7 @@ int hfx_ctx_destroy(hfx_ctx* c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   c->wsMem.release();
+  c->mixMem.release();
   c->outMem.release();
   c->tau.release();
   c->kappa.release();
@@ -481,10 +494,7 @@ static int ensure_outputs(hfx_ctx* c) {
   return HFX_OK;
 }
 
-int hfx_assemble(hfx_ctx* c) {
-  if (!c) return HFX_ERR_ARG;
-  if (!c->haveMesh) return set_err(c, HFX_ERR_STATE, "assemble: upload a mesh first");
-  cudaSetDevice(c->device);
+static int assemble_fp64(hfx_ctx* c) {
   int rc = ensure_outputs(c);
   if (rc) return rc;
   cudaStream_t s = c->stream;
@@ -551,12 +561,180 @@ int hfx_assemble(hfx_ctx* c) {
   if (status != 0) return set_err(c, HFX_ERR_SINGULAR, "assemble: singular element block in condensation");
   c->assembled = true;
   c->solved = false;
+  c->mixedMode = false;
   return HFX_OK;
 }
+
+static int ensure_workspace(hfx_ctx* c, bool mixed, int restart);
+
+static LocalParams local_params(hfx_ctx* c) {
+  LocalParams p{};
+  p.nCells = c->nCells;
+  p.coords = c->d_coords;
+  p.cells = c->d_cells;
+  p.cell2face = c->d_cell2face;
+  p.perm = c->d_perm;
+  p.face2cell = c->d_face2cell;
+  p.isBoundary = c->d_isBnd;
+  p.tau = c->tau.p;
+  p.tauVals = c->tauVals;
+  p.kappa = c->kappa.p;
+  p.kc = c->kc;
+  p.kappaLayout = c->kLayout;
+  p.srcMode = c->srcMode;
+  p.src = c->src.p;
+  p.srcParam = c->srcParam;
+  p.dirichlet = c->dir.p;
+  p.dt = c->dt;
+  p.uOld = c->uold.p;
+  p.tab = c->d_tab;
+  p.itab = c->d_itab;
+  p.status = c->d_status;
+  return p;
+}
+
+// FP64 residual of the full HDG system at the current (u, q, lambda); returns ||r||^2.
+static int mixed_residual(hfx_ctx* c, double* rr) {
+  const int NF = c->re.nNodesFace, F = c->re.nFaces, LL = F * NF;
+  ResidualParams p{};
+  p.nCells = c->nCells;
+  p.coords = c->d_coords;
+  p.cells = c->d_cells;
+  p.cell2face = c->d_cell2face;
+  p.perm = c->d_perm;
+  p.face2cell = c->d_face2cell;
+  p.tau = c->tau.p;
+  p.tauVals = c->tauVals;
+  p.kappa = c->kappa.p;
+  p.kc = c->kc;
+  p.kappaLayout = c->kLayout;
+  p.srcMode = c->srcMode;
+  p.src = c->src.p;
+  p.srcParam = c->srcParam;
+  p.dt = c->dt;
+  p.uOld = c->uold.p;
+  p.tab = c->d_tab;
+  p.itab = c->d_itab;
+  p.sol = c->d_sol;
+  p.flux = c->d_flux;
+  p.trace = c->d_trace;
+  p.ru = c->d_ru;
+  p.rq = c->d_rq;
+  p.rl = c->d_rl;
+  FaceResidualParams fp{c->topo.nFaces, NF, F, LL, c->d_face2cell, c->d_cell2face, c->d_perm, c->d_isBnd,
+                        c->d_rl, c->dir.p, c->d_trace, c->d_rtrace};
+  c->timer.begin(K_RESIDUAL, c->stream);
+  HFX_CUDA(c, launch_residual(c->dim, c->order, p, fp, c->stream));
+  c->timer.end(K_RESIDUAL, c->stream);
+  const int grid = 1024;
+  const int64_t LU = c->re.nNodes, LQ = (int64_t)c->dim * c->re.nNodes;
+  HFX_CUDA(c, launch_sumsq(c->d_ru, c->nCells * LU, c->d_rq, c->nCells * LQ, c->d_rtrace, c->ndofs(), c->d_part, grid,
+                           c->stream));
+  std::vector<double> hp(grid);
+  HFX_CUDA(c, cudaMemcpyAsync(hp.data(), c->d_part, sizeof(double) * grid, cudaMemcpyDeviceToHost, c->stream));
+  HFX_CUDA(c, cudaStreamSynchronize(c->stream));
+  double acc = 0.0;
+  for (double v : hp) acc += v;
+  *rr = acc;
+  return HFX_OK;
+}
+
+// FP32 element condensation with the residual rows as right-hand side
+static int mixed_condense(hfx_ctx* c, bool writeOps) {
+  LocalParams p = local_params(c);
+  p.fp32 = 1;
+  p.rhsU = c->d_ru;
+  p.rhsQ = c->d_rq;
+  p.writeOps = writeOps ? 1 : 0;
+  p.S = c->d_S32;
+  p.S0 = c->d_S032;
+  p.U = c->d_U32;
+  p.Q = c->d_Q32;
+  p.U0 = c->d_U032;
+  p.Q0 = c->d_Q032;
+  c->timer.begin(K_LOCAL, c->stream);
+  HFX_CUDA(c, launch_local_condense(c->dim, c->order, p, c->stream));
+  c->timer.end(K_LOCAL, c->stream);
+  Scatter32Params sp{};
+  sp.nFaces = c->topo.nFaces;
+  sp.NF = c->re.nNodesFace;
+  sp.LL = c->re.nFaces * c->re.nNodesFace;
+  sp.F = c->re.nFaces;
+  sp.nBlocks = (int64_t)c->bp.col.size();
+  sp.browptr = c->d_browptr;
+  sp.brow = c->d_brow;
+  sp.src0 = c->d_src0;
+  sp.src1 = c->d_src1;
+  sp.loc0 = c->d_loc0;
+  sp.loc1 = c->d_loc1;
+  sp.perm = c->d_perm;
+  sp.cell2face = c->d_cell2face;
+  sp.face2cell = c->d_face2cell;
+  sp.S = c->d_S32;
+  sp.S0 = c->d_S032;
+  sp.rtrace = c->d_rtrace;
+  sp.val = c->ws.val32;
+  sp.rhs = c->ws.rhs32;
+  c->timer.begin(K_SCATTER, c->stream);
+  HFX_CUDA(c, launch_scatter32(sp, writeOps, c->stream));
+  c->timer.end(K_SCATTER, c->stream);
+  return HFX_OK;
+}
+
+static int assemble_mixed(hfx_ctx* c) {
+  int rc = ensure_outputs(c);
+  if (rc) return rc;
+  if ((rc = ensure_workspace(c, true, 0))) return rc;
+  const int64_t E = c->nCells;
+  const int LU = c->re.nNodes, LQ = c->dim * c->re.nNodes, LL = c->re.nFaces * c->re.nNodesFace;
+  if (!c->d_S32) {
+    DevMem& m = c->mixMem;
+    HFX_CUDA(c, dalloc(m, &c->d_S32, (size_t)E * LL * LL));
+    HFX_CUDA(c, dalloc(m, &c->d_S032, (size_t)E * LL));
+    HFX_CUDA(c, dalloc(m, &c->d_U32, (size_t)E * LU * LL));
+    HFX_CUDA(c, dalloc(m, &c->d_Q32, (size_t)E * LQ * LL));
+    HFX_CUDA(c, dalloc(m, &c->d_U032, (size_t)E * LU));
+    HFX_CUDA(c, dalloc(m, &c->d_Q032, (size_t)E * LQ));
+    HFX_CUDA(c, dalloc(m, &c->d_dl32, (size_t)c->ndofs()));
+    HFX_CUDA(c, dalloc(m, &c->d_ru, (size_t)E * LU));
+    HFX_CUDA(c, dalloc(m, &c->d_rq, (size_t)E * LQ));
+    HFX_CUDA(c, dalloc(m, &c->d_rl, (size_t)E * LL));
+    HFX_CUDA(c, dalloc(m, &c->d_rtrace, (size_t)c->ndofs()));
+    HFX_CUDA(c, dalloc(m, &c->d_part, 1024));
+  }
+  cudaStream_t s = c->stream;
+  HFX_CUDA(c, cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
+  HFX_CUDA(c, cudaMemsetAsync(c->d_sol, 0, sizeof(double) * E * LU, s));
+  HFX_CUDA(c, cudaMemsetAsync(c->d_flux, 0, sizeof(double) * E * LQ, s));
+  HFX_CUDA(c, cudaMemsetAsync(c->d_trace, 0, sizeof(double) * c->ndofs(), s));
+  // residual at zero = the right-hand side b of the full system
+  if ((rc = mixed_residual(c, &c->mixedBB))) return rc;
+  c->mixedRR = c->mixedBB;
+  if ((rc = mixed_condense(c, true))) return rc;
+  int status = 0;
+  HFX_CUDA(c, cudaMemcpyAsync(&status, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  HFX_CUDA(c, cudaStreamSynchronize(s));
+  if (status != 0) return set_err(c, HFX_ERR_SINGULAR, "assemble: singular element block in condensation");
+  c->assembled = true;
+  c->solved = false;
+  c->mixedMode = true;
+  return HFX_OK;
+}
+
+int hfx_assemble_ex(hfx_ctx* c, int precision) {
+  if (!c) return HFX_ERR_ARG;
+  if (!c->haveMesh) return set_err(c, HFX_ERR_STATE, "assemble: upload a mesh first");
+  if (precision != HFX_PREC_FP64 && precision != HFX_PREC_MIXED) return set_err(c, HFX_ERR_ARG, "assemble: unknown precision");
+  cudaSetDevice(c->device);
+  return precision == HFX_PREC_MIXED ? assemble_mixed(c) : assemble_fp64(c);
+}
+
+int hfx_assemble(hfx_ctx* c) { return hfx_assemble_ex(c, HFX_PREC_FP64); }
 
 int hfx_get_condensed(hfx_ctx* c, double* S, double* S0, double* U, double* Q, double* U0, double* Q0) {
   if (!c) return HFX_ERR_ARG;
   if (!c->assembled) return set_err(c, HFX_ERR_STATE, "get_condensed: assemble first");
+  if (c->mixedMode) return set_err(c, HFX_ERR_STATE, "get_condensed: the mixed assembly keeps FP32 blocks; use hfx_assemble");
   const int64_t E = c->nCells;
   const int LU = c->re.nNodes, LQ = c->dim * c->re.nNodes, LL = c->re.nFaces * c->re.nNodesFace;
   cudaStream_t s = c->stream;
@@ -576,6 +754,7 @@ int hfx_get_condensed(hfx_ctx* c, double* S, double* S0, double* U, double* Q, d
 int hfx_get_csr(hfx_ctx* c, int64_t* rowptr, int* col, double* val, double* rhs) {
   if (!c) return HFX_ERR_ARG;
   if (!c->assembled && (val || rhs)) return set_err(c, HFX_ERR_STATE, "get_csr: assemble first");
+  if (c->mixedMode && (val || rhs)) return set_err(c, HFX_ERR_STATE, "get_csr: the mixed assembly keeps FP32 values; use hfx_assemble");
   if (!c->haveMesh) return set_err(c, HFX_ERR_STATE, "get_csr: no mesh");
   const int NF = c->re.nNodesFace;
   const int nF = c->topo.nFaces;
@@ -594,9 +773,23 @@ int hfx_get_csr(hfx_ctx* c, int64_t* rowptr, int* col, double* val, double* rhs)
     }
   }
   cudaStream_t s = c->stream;
-  if (val) HFX_CUDA(c, cudaMemcpyAsync(val, c->d_val, sizeof(double) * c->nnz(), cudaMemcpyDeviceToHost, s));
+  std::vector<double> blocks;
+  if (val) {
+    blocks.resize((size_t)c->nnz());
+    HFX_CUDA(c, cudaMemcpyAsync(blocks.data(), c->d_val, sizeof(double) * c->nnz(), cudaMemcpyDeviceToHost, s));
+  }
   if (rhs) HFX_CUDA(c, cudaMemcpyAsync(rhs, c->d_rhs, sizeof(double) * c->ndofs(), cudaMemcpyDeviceToHost, s));
   HFX_CUDA(c, cudaStreamSynchronize(s));
+  if (val) {
+    // device blocks are column-major per Nf x Nf block; AIJ rows are row-major
+    int64_t pos = 0;
+    for (int f = 0; f < nF; ++f) {
+      int64_t b0 = c->bp.rowptr[f], nb = c->bp.rowptr[f + 1] - b0;
+      for (int a = 0; a < NF; ++a)
+        for (int64_t k = 0; k < nb; ++k)
+          for (int b = 0; b < NF; ++b) val[pos++] = blocks[(b0 + k) * NF * NF + (int64_t)b * NF + a];
+    }
+  }
   return HFX_OK;
 }
 
@@ -649,10 +842,88 @@ static int ensure_workspace(hfx_ctx* c, bool mixed, int restart) {
     HFX_CUDA(c, dalloc(m, &w.q32, n));
     HFX_CUDA(c, dalloc(m, &w.d32, n));
     HFX_CUDA(c, dalloc(m, &w.rhs32, n));
+    HFX_CUDA(c, dalloc(m, &w.bS32, n));
     HFX_CUDA(c, cudaMemsetAsync(w.p032, 0, sizeof(float) * n, c->stream));
     HFX_CUDA(c, cudaMemsetAsync(w.p132, 0, sizeof(float) * n, c->stream));
     c->wsMixed = true;
   }
+  return HFX_OK;
+}
+
+// Iterative refinement of the full HDG system: FP64 residual, FP32 condensed
+// correction (element condensation, trace solve, recovery), FP64 update.
+static int solve_mixed(hfx_ctx* c, const hfx_solve_opts& o, int method, int restart, double* trace,
+                       hfx_solve_info* info) {
+  cudaStream_t s = c->stream;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, s);
+  F32SolveArgs a{};
+  a.dim = c->dim;
+  a.A = TraceView{c->topo.nFaces, c->re.nNodesFace, c->d_browptr, c->d_bcol, c->d_isBnd};
+  a.val = c->ws.val32;
+  a.rhs = c->ws.rhs32;
+  a.x = c->d_dl32;
+  a.precond = o.precond;
+  a.gmres = method == HFX_KSP_GMRES;
+  a.restart = restart;
+  a.ws = c->ws;
+  a.stream = s;
+  a.timer = &c->timer;
+  const int LU = c->re.nNodes, LQ = c->dim * c->re.nNodes, LL = c->re.nFaces * c->re.nNodesFace;
+  Correct32Params cp{c->nCells, c->re.nFaces, c->re.nNodesFace, LU, LQ, LL, c->ndofs(), c->d_cell2face, c->d_perm,
+                     c->d_U32, c->d_Q32, c->d_U032, c->d_Q032, c->d_dl32, c->d_sol, c->d_flux, c->d_trace};
+  const double inner = o.inner_rtol > 0 ? o.inner_rtol : 1e-4;
+  int its = 0, refinements = 0, status = 0, rc;
+  double rr = c->mixedRR, bb = c->mixedBB;
+  bool first = true;
+  while (true) {
+    if (!first) {
+      if ((rc = mixed_residual(c, &rr))) return rc;
+      if (!std::isfinite(rr)) {
+        status = HFX_ERR_NAN;
+        break;
+      }
+    }
+    if (rr <= o.rtol * o.rtol * bb) break;
+    if (its >= o.maxits || refinements >= 60) {
+      status = HFX_ERR_NOT_CONVERGED;
+      break;
+    }
+    if (!first && (rc = mixed_condense(c, false))) return rc;
+    a.rtol = std::max(inner, 0.5 * o.rtol * std::sqrt(bb / std::max(rr, 1e-300)));
+    a.maxits = o.maxits - its;
+    a.rebuildPrecond = first;
+    int st = trace_solve_f32(a, &its);
+    if (st != 0 && st != HFX_ERR_NOT_CONVERGED) {
+      status = st;
+      break;
+    }
+    c->timer.begin(K_RECOVER, s);
+    HFX_CUDA(c, launch_correct32(cp, s));
+    c->timer.end(K_RECOVER, s);
+    refinements += 1;
+    first = false;
+  }
+  c->mixedRR = rr;
+  cudaEventRecord(e1, s);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (info) {
+    info->status = status;
+    info->iterations = its;
+    info->refinements = refinements;
+    info->rel_residual = bb > 0 ? std::sqrt(rr / bb) : std::sqrt(rr);
+    info->solve_ms = ms;
+  }
+  if (trace) HFX_CUDA(c, cudaMemcpy(trace, c->d_trace, sizeof(double) * c->ndofs(), cudaMemcpyDeviceToHost));
+  c->solved = true;
+  if (status == HFX_ERR_NOT_CONVERGED) return set_err(c, status, "solve: mixed refinement not converged");
+  if (status != 0) return set_err(c, status, "solve: mixed refinement failed");
   return HFX_OK;
 }
 
@@ -675,6 +946,7 @@ int hfx_solve(hfx_ctx* c, const hfx_solve_opts* opts, double* trace, hfx_solve_i
   bool mixed = o.precision == HFX_PREC_MIXED;
   int rc = ensure_workspace(c, mixed, method == HFX_KSP_GMRES ? restart : 0);
   if (rc) return rc;
+  if (c->mixedMode) return solve_mixed(c, o, method, restart, trace, info);
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -728,11 +1000,13 @@ int hfx_recover(hfx_ctx* c, double* solution, double* flux) {
   cudaSetDevice(c->device);
   const int LU = c->re.nNodes, LQ = c->dim * c->re.nNodes, LL = c->re.nFaces * c->re.nNodesFace;
   const int64_t E = c->nCells;
-  RecoverParams p{c->nCells, c->re.nFaces, c->re.nNodesFace, LU, LQ, LL, c->d_cell2face, c->d_perm,
-                  c->d_U, c->d_Q, c->d_U0, c->d_Q0, c->d_trace, c->d_sol, c->d_flux};
-  c->timer.begin(K_RECOVER, c->stream);
-  HFX_CUDA(c, launch_recover(p, c->stream));
-  c->timer.end(K_RECOVER, c->stream);
+  if (!c->mixedMode) {  // mixed mode: Solution and Flux are the refined FP64 state
+    RecoverParams p{c->nCells, c->re.nFaces, c->re.nNodesFace, LU, LQ, LL, c->d_cell2face, c->d_perm,
+                    c->d_U, c->d_Q, c->d_U0, c->d_Q0, c->d_trace, c->d_sol, c->d_flux};
+    c->timer.begin(K_RECOVER, c->stream);
+    HFX_CUDA(c, launch_recover(p, c->stream));
+    c->timer.end(K_RECOVER, c->stream);
+  }
   // NULL outputs keep Solution and Flux on the device only
   if (solution) HFX_CUDA(c, cudaMemcpyAsync(solution, c->d_sol, sizeof(double) * E * LU, cudaMemcpyDeviceToHost, c->stream));
   if (flux) HFX_CUDA(c, cudaMemcpyAsync(flux, c->d_flux, sizeof(double) * E * LQ, cudaMemcpyDeviceToHost, c->stream));

@@ -289,6 +289,7 @@ __global__ void __launch_bounds__(TPE * EPC)
         }
         for (int a = 0; a < D; ++a) {
           G[qi * D + a] = g[a];
+          if (p.kc == 0) continue;  // identity tensor: the kappa-weighted blocks equal the plain ones
           T acc = 0.0;
           for (int b = 0; b < D; ++b) acc += kq[q * D * D + a + b * D] * g[b];
           KG[qi * D + a] = acc;
@@ -314,10 +315,15 @@ __global__ void __launch_bounds__(TPE * EPC)
       for (int dij = t; dij < D * N * N; dij += TPE) {
         int d = dij / (N * N), i = (dij / N) % N, j = dij % N;
         T c = 0.0, k = 0.0;
-        for (int q = 0; q < NI; ++q) {
-          T pj = phi[q * N + j];
-          c += G[(q * N + i) * D + d] * pj;
-          k += KG[(q * N + i) * D + d] * pj;
+        if (p.kc == 0) {
+          for (int q = 0; q < NI; ++q) c += G[(q * N + i) * D + d] * phi[q * N + j];
+          k = c;
+        } else {
+          for (int q = 0; q < NI; ++q) {
+            T pj = phi[q * N + j];
+            c += G[(q * N + i) * D + d] * pj;
+            k += KG[(q * N + i) * D + d] * pj;
+          }
         }
         Cm[dij] = c;  // Squ[(i,d)][j]
         Km[dij] = k;  // Suq[i][(j,d)] volume part
@@ -330,11 +336,12 @@ __global__ void __launch_bounds__(TPE * EPC)
           T ss = fphi[k * NF + a] * fphi[k * NF + b];
           int fk = f * NIF + k;
           tt += dSt[fk] * ss;
-          for (int d = 0; d < D; ++d) {
-            ee[d] += dSn[fk * D + d] * ss;
-            hh[d] += dSkn[fk * D + d] * ss;
-          }
+          for (int d = 0; d < D; ++d) ee[d] += dSn[fk * D + d] * ss;
+          if (p.kc != 0)
+            for (int d = 0; d < D; ++d) hh[d] += dSkn[fk * D + d] * ss;
         }
+        if (p.kc == 0)
+          for (int d = 0; d < D; ++d) hh[d] = ee[d];
         Tm[fab] = tt;
         for (int d = 0; d < D; ++d) {
           Em[((f * D + d) * NF + a) * NF + b] = ee[d];
@@ -462,20 +469,31 @@ __global__ void __launch_bounds__(TPE * EPC)
       }
     }
     __syncthreads();
-    // ---- LU with partial pivoting of A, applied to the RHS columns
+    // ---- Gauss-Jordan with partial pivoting on [A | Rhs]: Rhs <- A^{-1} Rhs.
+    // The pivot search is a warp argmax and every step updates all rows in
+    // parallel, so no serial back substitution is left.
     bool singular = false;
     for (int k = 0; k < N; ++k) {
-      if (active && t == 0) {
+      if (active && t < 32) {
+        T best = T(-1);
         int pr = k;
-        T best = fabs(Am[k * N + k]);
-        for (int i = k + 1; i < N; ++i) {
+        for (int i = k + t; i < N; i += 32) {
           T v = fabs(Am[i * N + k]);
           if (v > best) {
             best = v;
             pr = i;
           }
         }
-        piv[k] = pr;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          T ob = __shfl_xor_sync(0xffffffffu, best, o);
+          int op = __shfl_xor_sync(0xffffffffu, pr, o);
+          if (ob > best || (ob == best && op < pr)) {
+            best = ob;
+            pr = op;
+          }
+        }
+        if (t == 0) piv[k] = pr;
       }
       __syncthreads();
       if (active) {
@@ -496,12 +514,12 @@ __global__ void __launch_bounds__(TPE * EPC)
       __syncthreads();
       if (active) {
         T akk = Am[k * N + k];
-        if (akk == 0.0) singular = true;
-        T inv = 1.0 / akk;
-        int rows = N - k - 1;
-        int cols = (N - k - 1) + (LL + 1);
-        for (int rc = t; rc < rows * cols; rc += TPE) {
-          int i = k + 1 + rc / cols, c = rc % cols;
+        if (akk == T(0)) singular = true;
+        T inv = T(1) / akk;
+        const int cols = (N - k - 1) + (LL + 1);
+        for (int rc = t; rc < (N - 1) * cols; rc += TPE) {
+          int i = rc / cols, c = rc % cols;
+          if (i >= k) ++i;  // every row but the pivot row
           T l = Am[i * N + k] * inv;
           if (c < N - k - 1) {
             int j = k + 1 + c;
@@ -513,15 +531,15 @@ __global__ void __launch_bounds__(TPE * EPC)
         }
       }
       __syncthreads();
-    }
-    // back substitution, one thread per RHS column; column c < LL holds -U, c == LL holds U0
-    if (active)
-      for (int c = t; c < LL + 1; c += TPE)
-        for (int i = N - 1; i >= 0; --i) {
-          T s = Rhs[i * (LL + 1) + c];
-          for (int j = i + 1; j < N; ++j) s -= Am[i * N + j] * Rhs[j * (LL + 1) + c];
-          Rhs[i * (LL + 1) + c] = s / Am[i * N + i];
+      if (active) {
+        T inv = T(1) / Am[k * N + k];
+        for (int j = t; j < (N - k - 1) + (LL + 1); j += TPE) {
+          if (j < N - k - 1) Am[k * N + k + 1 + j] *= inv;
+          else Rhs[k * (LL + 1) + (j - (N - k - 1))] *= inv;
         }
+      }
+      __syncthreads();
+    }
     if (singular && t == 0) atomicCAS(p.status, 0, 1);
     __syncthreads();
     // U = -A^{-1}(...): negate the Schur solution columns in place

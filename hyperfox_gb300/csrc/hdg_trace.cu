@@ -1,11 +1,12 @@
 // Trace-system scatter, local recovery and integration-point coordinates.
 //
-// Trace values are stored in scalar-CSR order over face-block rows: the Nf
-// scalar rows of face f are contiguous, each of length nb(f)*Nf where nb(f) is
-// the number of neighbour faces (sorted), and within a row the entry of
-// neighbour k, node b sits at k*Nf + b. This is exactly PETSc's AIJ layout of
-// the reference system (sorted columns, explicit zeros kept), so the scalar
-// column array is implied by the face-block columns and is never stored.
+// Trace values are stored per face-block row (rows = faces, blocks = the
+// sorted neighbour faces), block by block in CSR order, each Nf x Nf block
+// column-major: entry (row node a, column node b) of block k at
+// k*Nf*Nf + b*Nf + a. The scalar pattern is PETSc's AIJ pattern of the
+// reference system (sorted columns, explicit zeros kept); the scalar column
+// array is implied by the block columns and never stored, and hfx_get_csr
+// reorders the values row-major for export.
 #include "hfx_device.h"
 
 namespace hfx {
@@ -23,9 +24,6 @@ __global__ void scatter_values(ScatterParams p, const int* brow, int64_t nBlocks
     int64_t k = idx / (NF * NF);
     int ab = (int)(idx % (NF * NF));
     int a = ab / NF, b = ab % NF;
-    int f = brow[k];
-    int64_t b0 = p.browptr[f];
-    int64_t nb = p.browptr[f + 1] - b0;
     double v = 0.0;
     for (int s = 0; s < 2; ++s) {
       int c = s == 0 ? p.src0[k] : p.src1[k];
@@ -42,7 +40,7 @@ __global__ void scatter_values(ScatterParams p, const int* brow, int64_t nBlocks
       }
       v += p.S[(int64_t)c * LL * LL + (li * NF + ja) + (int64_t)(lj * NF + jb) * LL];
     }
-    p.val[b0 * NF * NF + (int64_t)a * nb * NF + (k - b0) * NF + b] = v;
+    p.val[k * NF * NF + (int64_t)b * NF + a] = v;  // block k column-major
   }
 }
 

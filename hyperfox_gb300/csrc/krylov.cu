@@ -12,6 +12,10 @@
 // second FP64 copy of the matrix is stored; the mixed-precision path keeps an
 // FP32 copy of A' for the inner solves and refines in FP64 against A'.
 //
+// Values are stored per face block-row, block by block in the sorted column
+// order, each NF x NF block column-major (entry (a, b) of block k at
+// k*NF*NF + b*NF + a). hfx_get_csr converts to PETSc's row-major AIJ order.
+//
 // CG per iteration is two kernels:
 //   K1: p = z + beta*p_old (computed on the fly for every gathered entry),
 //       q = A' p, partial p.q, and in the last block alpha = rz / p.q;
@@ -21,10 +25,12 @@
 // the last block to finish (atomic ticket, no spin-waits). Once converged (or
 // broken down) every later kernel returns at entry, so the host may queue
 // many iterations between checks.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <vector>
 
+#include "hdg_mixed.h"
 #include "hfx_device.h"
 #include "krylov.h"
 
@@ -86,45 +92,49 @@ __device__ bool block_reduce_last(double (&v)[NV], double* partials, unsigned* t
   return true;
 }
 
+// Thread-per-row mapping: the NF threads of a face slot each own one scalar
+// row; a warp holds FPW = 32/NF faces. Values are stored block by block in CSR
+// order, each NF x NF block column-major, so for a fixed column position the
+// NF threads of a face read NF consecutive values, and each thread computes
+// its whole row: one FMA per stored value and no cross-lane reductions (the
+// reductions' adds, not the FMAs, bounded the FP64 pipe otherwise).
 template <int NF, int NBMAX>
-struct GroupCfg {
+struct RowCfg {
+  static constexpr int FPW = 32 / NF;
   static constexpr int NPOS = NBMAX * NF;
-  static constexpr int GS = NPOS <= 16 ? 16 : 32;
-  static constexpr int KPL = (NPOS + GS - 1) / GS;
 };
 
-// y = A' x on face-block rows. MASKED: apply the reference values with the
-// Dirichlet elimination and the sign flip on the fly (FP64 path); otherwise
-// the values already hold A'.
-template <typename T, int NF, int NBMAX, bool MASKED>
-__device__ __forceinline__ void face_row_spmv(const T* __restrict__ val, int64_t b0, int nb,
-                                              const T (&xv)[GroupCfg<NF, NBMAX>::KPL], int lane,
-                                              T (&yrow)[NF]) {
-  using G = GroupCfg<NF, NBMAX>;
-  const int npos = nb * NF;
-  const T* base = val + b0 * NF * NF;
-  // issue every value load of the face first (NF*KPL independent loads per
-  // lane), then reduce all rows: memory latency overlaps instead of
-  // serialising row by row
-  T vv[NF][G::KPL];
-#pragma unroll
-  for (int a = 0; a < NF; ++a)
-#pragma unroll
-    for (int k = 0; k < G::KPL; ++k) {
-      int m = lane + k * G::GS;
-      vv[a][k] = (m < npos) ? __ldg(base + (int64_t)a * npos + m) : T(0);
-    }
-#pragma unroll
-  for (int a = 0; a < NF; ++a) {
-    T acc = 0;
-#pragma unroll
-    for (int k = 0; k < G::KPL; ++k) acc = fma_t<T>(vv[a][k], xv[k], acc);
-    yrow[a] = acc;
+#define HFX_FACE_SLOTS(NF)                                                                     \
+  constexpr int FPW = RowCfg<NF, NBMAX>::FPW;                                                  \
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;                                  \
+  const int slot = lane / NF, a = lane % NF;                                                   \
+  const bool laneUsed = slot < FPW;                                                            \
+  const int64_t faceStride = (int64_t)gridDim.x * (kThreads / 32) * FPW;
+
+// Gather x for the face: thread a loads column a of every neighbour block.
+template <typename T, int NF, int NBMAX, bool MASKED, bool PUPD>
+__device__ __forceinline__ void gather_x(const TraceView& A, int64_t b0, int nb, bool rowBnd, int a, T beta,
+                                         const T* __restrict__ z, const T* __restrict__ pold, T* xs) {
+  for (int k = 0; k < nb; ++k) {
+    int g = A.bcol[b0 + k];
+    int64_t j = (int64_t)g * NF + a;
+    T v = PUPD ? fma_t<T>(beta, pold[j], z[j]) : z[j];
+    if (MASKED && (rowBnd || A.isBnd[g])) v = T(0);
+    xs[k * NF + a] = v;
   }
+}
+
+// One row of the face block-row: sum over the nb neighbour blocks.
+template <typename T, int NF>
+__device__ __forceinline__ T row_dot(const T* __restrict__ val, int64_t b0, int nb, int a, const T* xs) {
+  const T* base = val + b0 * NF * NF + a;
+  T acc = T(0);
+  for (int k = 0; k < nb; ++k) {
+    const T* blk = base + (int64_t)k * NF * NF;
 #pragma unroll
-  for (int o = G::GS / 2; o > 0; o >>= 1)
-#pragma unroll
-    for (int a = 0; a < NF; ++a) yrow[a] += __shfl_xor_sync(0xffffffffu, yrow[a], o, G::GS);
+    for (int b = 0; b < NF; ++b) acc = fma_t<T>(__ldg(blk + b * NF), xs[k * NF + b], acc);
+  }
+  return acc;
 }
 
 // K1 of CG (see the file comment).
@@ -133,49 +143,30 @@ __global__ void __launch_bounds__(kThreads) cg_spmv(TraceView A, const T* __rest
                                                     const T* __restrict__ z, const T* __restrict__ pold,
                                                     T* __restrict__ pnew, T* __restrict__ q, CgState* st,
                                                     double* partials, int first) {
-  using G = GroupCfg<NF, NBMAX>;
+  __shared__ T xsh[kThreads / 32][RowCfg<NF, NBMAX>::FPW][RowCfg<NF, NBMAX>::NPOS];
   if (st->done) return;
   const T beta = first ? T(0) : (T)st->beta;
-  const int lane = threadIdx.x % G::GS;
-  const int gpb = kThreads / G::GS;
+  HFX_FACE_SLOTS(NF)
   double pq = 0.0;
-  // warp-uniform loop: every lane of a warp takes the same trips (shuffles use
-  // the full mask); a group past the last face works on nothing
-  const int gInWarp = (threadIdx.x & 31) / G::GS;
-  for (int64_t fb = ((int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5)) * (32 / G::GS); fb < A.nFaces;
-       fb += (int64_t)gridDim.x * gpb) {
-    const int64_t f = fb + gInWarp;
-    const bool act = f < A.nFaces;
+  for (int64_t fb = ((int64_t)blockIdx.x * (kThreads / 32) + warp) * FPW; fb < A.nFaces; fb += faceStride) {
+    const int64_t f = fb + slot;
+    const bool act = laneUsed && f < A.nFaces;
     const int64_t b0 = act ? A.browptr[f] : 0;
     const int nb = act ? (int)(A.browptr[f + 1] - b0) : 0;
     const bool rowBnd = MASKED && act && A.isBnd[f];
-    T xv[G::KPL];
-#pragma unroll
-    for (int k = 0; k < G::KPL; ++k) {
-      int m = lane + k * G::GS;
-      T v = 0;
-      if (m < nb * NF) {
-        int g = A.bcol[b0 + m / NF];
-        int64_t j = (int64_t)g * NF + m % NF;
-        v = fma_t<T>(beta, pold[j], z[j]);
-        if (MASKED && (rowBnd || A.isBnd[g])) v = 0;  // eliminated columns
-      }
-      xv[k] = v;
-    }
-    T y[NF];
-    face_row_spmv<T, NF, NBMAX, MASKED>(val, b0, nb, xv, lane, y);
-    if (act && lane < NF) {
-      T ya = 0;
-#pragma unroll
-      for (int a = 0; a < NF; ++a)
-        if (a == lane) ya = y[a];
-      int64_t i = f * NF + lane;
+    T* xs = laneUsed ? xsh[warp][slot] : nullptr;
+    if (act) gather_x<T, NF, NBMAX, MASKED, true>(A, b0, nb, rowBnd, a, beta, z, pold, xs);
+    __syncwarp();
+    if (act) {
+      T y = row_dot<T, NF>(val, b0, nb, a, xs);
+      int64_t i = f * NF + a;
       T pi = fma_t<T>(beta, pold[i], z[i]);
-      T yi = MASKED ? (rowBnd ? pi : -ya) : ya;
+      T yi = MASKED ? (rowBnd ? pi : -y) : y;
       pnew[i] = pi;
       q[i] = yi;
       pq += (double)pi * (double)yi;
     }
+    __syncwarp();
   }
   double v[1] = {pq}, tot[1];
   if (block_reduce_last<1>(v, partials, &st->ticket, tot) && threadIdx.x == 0) {
@@ -190,40 +181,50 @@ __global__ void __launch_bounds__(kThreads) cg_spmv(TraceView A, const T* __rest
 }
 
 // K2 of CG. PC: 0 none, 1 Jacobi (pc = inverse diagonal), 2 block Jacobi
-// (pc = inverse face blocks, row-major NF x NF).
+// (pc = inverse face blocks, column-major NF x NF). Thread per row, the NF
+// threads of a face exchange their residual rows through shared memory.
 template <typename T, int NF, int PC>
 __global__ void __launch_bounds__(kThreads) cg_update(int64_t nFaces, T* __restrict__ x, T* __restrict__ r,
                                                       T* __restrict__ z, const T* __restrict__ p,
                                                       const T* __restrict__ q, const T* __restrict__ pc,
                                                       CgState* st, double* partials, double tol2) {
+  constexpr int FPW = 32 / NF;
+  __shared__ T rsh[kThreads / 32][FPW][NF];
   if (st->done) return;
   const T alpha = (T)st->alpha;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int slot = lane / NF, a = lane % NF;
+  const bool laneUsed = slot < FPW;
+  const int64_t stride = (int64_t)gridDim.x * (kThreads / 32) * FPW;
   double rz = 0.0, rr = 0.0;
-  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < nFaces; f += (int64_t)gridDim.x * blockDim.x) {
-    T rl[NF];
-#pragma unroll
-    for (int a = 0; a < NF; ++a) {
+  for (int64_t fb = ((int64_t)blockIdx.x * (kThreads / 32) + warp) * FPW; fb < nFaces; fb += stride) {
+    const int64_t f = fb + slot;
+    const bool act = laneUsed && f < nFaces;
+    T ra = T(0);
+    if (act) {
       int64_t i = f * NF + a;
       x[i] = fma_t<T>(alpha, p[i], x[i]);
-      rl[a] = fma_t<T>(-alpha, q[i], r[i]);
-      r[i] = rl[a];
-      rr += (double)rl[a] * (double)rl[a];
+      ra = fma_t<T>(-alpha, q[i], r[i]);
+      r[i] = ra;
+      rr += (double)ra * (double)ra;
+      if (PC == 2) rsh[warp][slot][a] = ra;
     }
-#pragma unroll
-    for (int a = 0; a < NF; ++a) {
+    if (PC == 2) __syncwarp();
+    if (act) {
       int64_t i = f * NF + a;
       T zi;
-      if (PC == 0) zi = rl[a];
-      else if (PC == 1) zi = pc[i] * rl[a];
+      if (PC == 0) zi = ra;
+      else if (PC == 1) zi = pc[i] * ra;
       else {
-        zi = 0;
-        const T* B = pc + f * NF * NF + a * NF;
+        zi = T(0);
+        const T* B = pc + f * NF * NF + a;
 #pragma unroll
-        for (int b = 0; b < NF; ++b) zi = fma_t<T>(B[b], rl[b], zi);
+        for (int b = 0; b < NF; ++b) zi = fma_t<T>(B[b * NF], rsh[warp][slot][b], zi);
       }
       z[i] = zi;
-      rz += (double)rl[a] * (double)zi;
+      rz += (double)ra * (double)zi;
     }
+    if (PC == 2) __syncwarp();
   }
   double v[2] = {rz, rr}, tot[2];
   if (block_reduce_last<2>(v, partials, &st->ticket, tot) && threadIdx.x == 0) {
@@ -246,63 +247,52 @@ __global__ void __launch_bounds__(kThreads) cg_update(int64_t nFaces, T* __restr
 }
 
 // r = b' - A' x (FP64, masked reference values) and its norm; also z = M^{-1} r
-// and r.z to start CG. Writes the squared norms to st.
+// and r.z to start CG. Writes the squared norms to st (||b||^2 of the reference rhs).
 template <int NF, int NBMAX, int PC>
 __global__ void __launch_bounds__(kThreads) cg_start(TraceView A, const double* __restrict__ val,
                                                      const double* __restrict__ bS, const double* __restrict__ bref,
                                                      const double* __restrict__ x, double* __restrict__ r,
                                                      double* __restrict__ z, const double* __restrict__ pc, CgState* st,
                                                      double* partials) {
-  using G = GroupCfg<NF, NBMAX>;
-  const int lane = threadIdx.x % G::GS;
-  const int gpb = kThreads / G::GS;
+  __shared__ double xsh[kThreads / 32][RowCfg<NF, NBMAX>::FPW][RowCfg<NF, NBMAX>::NPOS];
+  HFX_FACE_SLOTS(NF)
   double rr = 0.0, rz = 0.0, bb = 0.0;
-  // warp-uniform loop: every lane of a warp takes the same trips (shuffles use
-  // the full mask); a group past the last face works on nothing
-  const int gInWarp = (threadIdx.x & 31) / G::GS;
-  for (int64_t fb = ((int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5)) * (32 / G::GS); fb < A.nFaces;
-       fb += (int64_t)gridDim.x * gpb) {
-    const int64_t f = fb + gInWarp;
-    const bool act = f < A.nFaces;
+  for (int64_t fb = ((int64_t)blockIdx.x * (kThreads / 32) + warp) * FPW; fb < A.nFaces; fb += faceStride) {
+    const int64_t f = fb + slot;
+    const bool act = laneUsed && f < A.nFaces;
     const int64_t b0 = act ? A.browptr[f] : 0;
     const int nb = act ? (int)(A.browptr[f + 1] - b0) : 0;
     const bool rowBnd = act && A.isBnd[f];
-    double xv[G::KPL];
-#pragma unroll
-    for (int k = 0; k < G::KPL; ++k) {
-      int m = lane + k * G::GS;
-      double v = 0;
-      if (m < nb * NF) {
-        int g = A.bcol[b0 + m / NF];
-        v = (rowBnd || A.isBnd[g]) ? 0.0 : x[(int64_t)g * NF + m % NF];
-      }
-      xv[k] = v;
+    double* xs = laneUsed ? xsh[warp][slot] : nullptr;
+    if (act) gather_x<double, NF, NBMAX, true, false>(A, b0, nb, rowBnd, a, 0.0, x, x, xs);
+    __syncwarp();
+    double ra = 0.0;
+    if (act) {
+      double y = row_dot<double, NF>(val, b0, nb, a, xs);
+      int64_t i = f * NF + a;
+      double ax = rowBnd ? x[i] : -y;
+      ra = bS[i] - ax;
+      r[i] = ra;
+      rr += ra * ra;
+      bb += bref[i] * bref[i];
     }
-    double y[NF];
-    face_row_spmv<double, NF, NBMAX, true>(val, b0, nb, xv, lane, y);
-    if (lane == 0 && act) {
-      double rl[NF];
-      for (int a = 0; a < NF; ++a) {
-        int64_t i = f * NF + a;
-        double ax = rowBnd ? x[i] : -y[a];
-        rl[a] = bS[i] - ax;
-        r[i] = rl[a];
-        rr += rl[a] * rl[a];
-        bb += bref[i] * bref[i];
+    __syncwarp();
+    // z for the face needs all NF residual rows: pass them through shared memory
+    if (act) xs[a] = ra;
+    __syncwarp();
+    if (act) {
+      int64_t i = f * NF + a;
+      double zi;
+      if (PC == 0) zi = ra;
+      else if (PC == 1) zi = pc[i] * ra;
+      else {
+        zi = 0.0;
+        for (int b = 0; b < NF; ++b) zi += pc[f * NF * NF + b * NF + a] * xs[b];
       }
-      for (int a = 0; a < NF; ++a) {
-        int64_t i = f * NF + a;
-        double zi;
-        if (PC == 0) zi = rl[a];
-        else if (PC == 1) zi = pc[i] * rl[a];
-        else {
-          zi = 0;
-          for (int b = 0; b < NF; ++b) zi += pc[f * NF * NF + a * NF + b] * rl[b];
-        }
-        z[i] = zi;
-        rz += rl[a] * zi;
-      }
+      z[i] = zi;
+      rz += ra * zi;
     }
+    __syncwarp();
   }
   double v[3] = {rr, rz, bb}, tot[3];
   if (block_reduce_last<3>(v, partials, &st->ticket, tot) && threadIdx.x == 0) {
@@ -318,33 +308,23 @@ template <int NF, int NBMAX>
 __global__ void __launch_bounds__(kThreads) ref_residual(TraceView A, const double* __restrict__ val,
                                                          const double* __restrict__ b, const double* __restrict__ x,
                                                          CgState* st, double* partials) {
-  using G = GroupCfg<NF, NBMAX>;
-  const int lane = threadIdx.x % G::GS;
-  const int gpb = kThreads / G::GS;
+  __shared__ double xsh[kThreads / 32][RowCfg<NF, NBMAX>::FPW][RowCfg<NF, NBMAX>::NPOS];
+  HFX_FACE_SLOTS(NF)
   double rr = 0.0, bb = 0.0;
-  // warp-uniform loop: every lane of a warp takes the same trips (shuffles use
-  // the full mask); a group past the last face works on nothing
-  const int gInWarp = (threadIdx.x & 31) / G::GS;
-  for (int64_t fb = ((int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5)) * (32 / G::GS); fb < A.nFaces;
-       fb += (int64_t)gridDim.x * gpb) {
-    const int64_t f = fb + gInWarp;
-    const bool act = f < A.nFaces;
+  for (int64_t fb = ((int64_t)blockIdx.x * (kThreads / 32) + warp) * FPW; fb < A.nFaces; fb += faceStride) {
+    const int64_t f = fb + slot;
+    const bool act = laneUsed && f < A.nFaces;
     const int64_t b0 = act ? A.browptr[f] : 0;
     const int nb = act ? (int)(A.browptr[f + 1] - b0) : 0;
-    double xv[G::KPL];
-#pragma unroll
-    for (int k = 0; k < G::KPL; ++k) {
-      int m = lane + k * G::GS;
-      xv[k] = m < nb * NF ? x[(int64_t)A.bcol[b0 + m / NF] * NF + m % NF] : 0.0;
+    double* xs = laneUsed ? xsh[warp][slot] : nullptr;
+    if (act) gather_x<double, NF, NBMAX, false, false>(A, b0, nb, false, a, 0.0, x, x, xs);
+    __syncwarp();
+    if (act) {
+      double ri = b[f * NF + a] - row_dot<double, NF>(val, b0, nb, a, xs);
+      rr += ri * ri;
+      bb += b[f * NF + a] * b[f * NF + a];
     }
-    double y[NF];
-    face_row_spmv<double, NF, NBMAX, false>(val, b0, nb, xv, lane, y);
-    if (lane == 0 && act)
-      for (int a = 0; a < NF; ++a) {
-        double ri = b[f * NF + a] - y[a];
-        rr += ri * ri;
-        bb += b[f * NF + a] * b[f * NF + a];
-      }
+    __syncwarp();
   }
   double v[2] = {rr, bb}, tot[2];
   if (block_reduce_last<2>(v, partials, &st->ticket, tot) && threadIdx.x == 0) {
@@ -353,46 +333,35 @@ __global__ void __launch_bounds__(kThreads) ref_residual(TraceView A, const doub
   }
 }
 
-// b' and the FP32 copy of A' (optional), one group per face row.
+// b' and the FP32 copy of A' (optional), thread per row.
 template <int NF, int NBMAX>
 __global__ void __launch_bounds__(kThreads) prepare_system(TraceView A, const double* __restrict__ val,
                                                            const double* __restrict__ b, double* __restrict__ bS,
                                                            float* __restrict__ val32) {
-  using G = GroupCfg<NF, NBMAX>;
-  const int lane = threadIdx.x % G::GS;
-  const int gpb = kThreads / G::GS;
-  // warp-uniform loop: every lane of a warp takes the same trips (shuffles use
-  // the full mask); a group past the last face works on nothing
-  const int gInWarp = (threadIdx.x & 31) / G::GS;
-  for (int64_t fb = ((int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5)) * (32 / G::GS); fb < A.nFaces;
-       fb += (int64_t)gridDim.x * gpb) {
-    const int64_t f = fb + gInWarp;
-    const bool act = f < A.nFaces;
-    const int64_t b0 = act ? A.browptr[f] : 0;
-    const int nb = act ? (int)(A.browptr[f + 1] - b0) : 0;
-    const int npos = nb * NF;
-    const bool rowBnd = act && A.isBnd[f];
-    for (int a = 0; a < NF; ++a) {
-      // lifted Dirichlet values: sum over boundary columns of A_ij g_j
-      double lift = 0.0;
-      for (int m = lane; m < npos; m += G::GS) {
-        int g = A.bcol[b0 + m / NF];
-        int64_t j = (int64_t)g * NF + m % NF;
-        double v = val[b0 * NF * NF + (int64_t)a * npos + m];
-        if (!rowBnd && A.isBnd[g]) lift += v * b[j];
+  HFX_FACE_SLOTS(NF)
+  for (int64_t fb = ((int64_t)blockIdx.x * (kThreads / 32) + warp) * FPW; fb < A.nFaces; fb += faceStride) {
+    const int64_t f = fb + slot;
+    if (!(laneUsed && f < A.nFaces)) continue;
+    const int64_t b0 = A.browptr[f];
+    const int nb = (int)(A.browptr[f + 1] - b0);
+    const bool rowBnd = A.isBnd[f];
+    double lift = 0.0;
+    for (int k = 0; k < nb; ++k) {
+      int g = A.bcol[b0 + k];
+      for (int c = 0; c < NF; ++c) {
+        int64_t idx = (b0 + k) * NF * NF + (int64_t)c * NF + a;
+        double v = val[idx];
+        if (!rowBnd && A.isBnd[g]) lift += v * b[(int64_t)g * NF + c];
         if (val32) {
           float w;
-          if (rowBnd) w = (j == f * NF + a) ? 1.0f : 0.0f;
+          if (rowBnd) w = (g == (int)f && c == a) ? 1.0f : 0.0f;
           else w = A.isBnd[g] ? 0.0f : (float)(-v);
-          val32[b0 * NF * NF + (int64_t)a * npos + m] = w;
+          val32[idx] = w;
         }
       }
-      for (int o = G::GS / 2; o > 0; o >>= 1) lift += __shfl_xor_sync(0xffffffffu, lift, o, G::GS);
-      if (lane == 0 && act) {
-        int64_t i = f * NF + a;
-        bS[i] = rowBnd ? b[i] : -(b[i] - lift);
-      }
     }
+    int64_t i = f * NF + a;
+    bS[i] = rowBnd ? b[i] : -(b[i] - lift);
   }
 }
 
@@ -408,7 +377,7 @@ __global__ void build_precond(TraceView A, const double* __restrict__ val, int p
     double B[NF][2 * NF];
     for (int a = 0; a < NF; ++a)
       for (int b = 0; b < NF; ++b) {
-        double v = A.isBnd[f] ? (a == b ? 1.0 : 0.0) : -val[b0 * NF * NF + (int64_t)a * nb * NF + kd * NF + b];
+        double v = A.isBnd[f] ? (a == b ? 1.0 : 0.0) : -val[(b0 + kd) * NF * NF + (int64_t)b * NF + a];
         B[a][b] = v;
         B[a][NF + b] = (a == b) ? 1.0 : 0.0;
       }
@@ -433,9 +402,76 @@ __global__ void build_precond(TraceView A, const double* __restrict__ val, int p
     }
     for (int a = 0; a < NF; ++a)
       for (int b = 0; b < NF; ++b) {
-        if (pc64) pc64[f * NF * NF + a * NF + b] = B[a][NF + b];
-        if (pc32) pc32[f * NF * NF + a * NF + b] = (float)B[a][NF + b];
+        if (pc64) pc64[f * NF * NF + b * NF + a] = B[a][NF + b];  // column-major
+        if (pc32) pc32[f * NF * NF + b * NF + a] = (float)B[a][NF + b];
       }
+  }
+}
+
+// Reliable update of the mixed-precision CG: the true residual
+// r = b' - A' x (FP64, masked reference values) replaces the FP32 recursive
+// residual; writes r32 = (float) r, z32 = M^{-1} r32 and the sums ||r||^2 (FP64)
+// and r32.z32 into st. The FP32 search direction is kept.
+template <int NF, int NBMAX, int PC>
+__global__ void __launch_bounds__(kThreads) cg_replace(TraceView A, const double* __restrict__ val,
+                                                       const double* __restrict__ bS, const double* __restrict__ bref,
+                                                       const double* __restrict__ x, float* __restrict__ r32,
+                                                       float* __restrict__ z32, const float* __restrict__ pc,
+                                                       CgState* st, double* partials) {
+  __shared__ double xsh[kThreads / 32][RowCfg<NF, NBMAX>::FPW][RowCfg<NF, NBMAX>::NPOS];
+  __shared__ float rsh[kThreads / 32][RowCfg<NF, NBMAX>::FPW][NF];
+  HFX_FACE_SLOTS(NF)
+  double rr = 0.0, rz = 0.0, bb = 0.0;
+  for (int64_t fb = ((int64_t)blockIdx.x * (kThreads / 32) + warp) * FPW; fb < A.nFaces; fb += faceStride) {
+    const int64_t f = fb + slot;
+    const bool act = laneUsed && f < A.nFaces;
+    const int64_t b0 = act ? A.browptr[f] : 0;
+    const int nb = act ? (int)(A.browptr[f + 1] - b0) : 0;
+    const bool rowBnd = act && A.isBnd[f];
+    double* xs = laneUsed ? xsh[warp][slot] : nullptr;
+    if (act) gather_x<double, NF, NBMAX, true, false>(A, b0, nb, rowBnd, a, 0.0, x, x, xs);
+    __syncwarp();
+    float ra = 0.f;
+    if (act) bb += bref[f * NF + a] * bref[f * NF + a];
+    if (act) {
+      double y = row_dot<double, NF>(val, b0, nb, a, xs);
+      int64_t i = f * NF + a;
+      double r = bS[i] - (rowBnd ? x[i] : -y);
+      rr += r * r;
+      ra = (float)r;
+      r32[i] = ra;
+      rsh[warp][slot][a] = ra;
+    }
+    __syncwarp();
+    if (act) {
+      int64_t i = f * NF + a;
+      float zi;
+      if (PC == 0) zi = ra;
+      else if (PC == 1) zi = pc[i] * ra;
+      else {
+        zi = 0.f;
+        const float* B = pc + f * NF * NF + a;
+#pragma unroll
+        for (int b = 0; b < NF; ++b) zi = fmaf(B[b * NF], rsh[warp][slot][b], zi);
+      }
+      z32[i] = zi;
+      rz += (double)ra * (double)zi;
+    }
+    __syncwarp();
+  }
+  double v[3] = {rr, rz, bb}, tot[3];
+  if (block_reduce_last<3>(v, partials, &st->ticket, tot) && threadIdx.x == 0) {
+    st->rr = tot[0];
+    st->rz = tot[1];
+    st->bb = tot[2];
+  }
+}
+
+// x64 += y32, y32 = 0
+__global__ void accum_x(int64_t n, float* __restrict__ y, double* __restrict__ x) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += (double)y[i];
+    y[i] = 0.f;
   }
 }
 
@@ -471,7 +507,7 @@ __global__ void __launch_bounds__(kThreads) cg_start_zero_f32(int64_t nFaces, co
       else if (PC == 1) zi = pc[i] * rl[a];
       else {
         zi = 0.0f;
-        for (int b = 0; b < NF; ++b) zi = fmaf(pc[f * NF * NF + a * NF + b], rl[b], zi);
+        for (int b = 0; b < NF; ++b) zi = fmaf(pc[f * NF * NF + b * NF + a], rl[b], zi);
       }
       z[i] = zi;
       rz += (double)rl[a] * zi;
@@ -490,6 +526,62 @@ __global__ void copy_dirichlet(TraceView A, const double* __restrict__ bS, doubl
   for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < A.nFaces; f += (int64_t)gridDim.x * blockDim.x)
     if (A.isBnd[f])
       for (int a = 0; a < NF; ++a) x[f * NF + a] = bS[f * NF + a];
+}
+
+// b' = [-(b_I - A_ID b_D) ; b_D] from raw values of any precision (thread per row)
+template <typename T, int NF, int NBMAX>
+__global__ void __launch_bounds__(kThreads) prepare_rhs_t(TraceView A, const T* __restrict__ val,
+                                                          const T* __restrict__ b, T* __restrict__ bS) {
+  HFX_FACE_SLOTS(NF)
+  for (int64_t fb = ((int64_t)blockIdx.x * (kThreads / 32) + warp) * FPW; fb < A.nFaces; fb += faceStride) {
+    const int64_t f = fb + slot;
+    if (!(laneUsed && f < A.nFaces)) continue;
+    const int64_t b0 = A.browptr[f];
+    const int nb = (int)(A.browptr[f + 1] - b0);
+    const bool rowBnd = A.isBnd[f];
+    double lift = 0.0;
+    if (!rowBnd)
+      for (int k = 0; k < nb; ++k) {
+        int g = A.bcol[b0 + k];
+        if (!A.isBnd[g]) continue;
+        for (int c = 0; c < NF; ++c)
+          lift += (double)val[(b0 + k) * NF * NF + (int64_t)c * NF + a] * (double)b[(int64_t)g * NF + c];
+      }
+    int64_t i = f * NF + a;
+    bS[i] = rowBnd ? b[i] : (T)(-((double)b[i] - lift));
+  }
+}
+
+template <typename T, int NF>
+__global__ void build_precond_t(TraceView A, const T* __restrict__ val, int pcType, T* pc) {
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < A.nFaces; f += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b0 = A.browptr[f];
+    const int nb = (int)(A.browptr[f + 1] - b0);
+    int kd = 0;
+    for (int k = 0; k < nb; ++k)
+      if (A.bcol[b0 + k] == (int)f) kd = k;
+    double B[NF][2 * NF];
+    for (int a = 0; a < NF; ++a)
+      for (int b = 0; b < NF; ++b) {
+        B[a][b] = A.isBnd[f] ? (a == b ? 1.0 : 0.0) : -(double)val[(b0 + kd) * NF * NF + (int64_t)b * NF + a];
+        B[a][NF + b] = (a == b) ? 1.0 : 0.0;
+      }
+    if (pcType == 1) {
+      for (int a = 0; a < NF; ++a) pc[f * NF + a] = (T)(B[a][a] != 0.0 ? 1.0 / B[a][a] : 1.0);
+      continue;
+    }
+    for (int k = 0; k < NF; ++k) {
+      double inv = 1.0 / B[k][k];
+      for (int j = 0; j < 2 * NF; ++j) B[k][j] *= inv;
+      for (int i = 0; i < NF; ++i) {
+        if (i == k) continue;
+        double l = B[i][k];
+        for (int j = 0; j < 2 * NF; ++j) B[i][j] -= l * B[k][j];
+      }
+    }
+    for (int a = 0; a < NF; ++a)
+      for (int b = 0; b < NF; ++b) pc[f * NF * NF + b * NF + a] = (T)B[a][NF + b];  // column-major
+  }
 }
 
 template <typename KernelT>
@@ -581,50 +673,65 @@ struct Driver {
         totalIters = hst.iters;
       }
     } else {
-      // FP64 iterative refinement around FP32 CG on A'
+      // Mixed-precision CG with reliable updates: one FP32 CG on the FP32 copy
+      // of A' whose recursive residual is replaced by the true FP64 residual
+      // b' - A' x64 whenever it has dropped by delta since the last
+      // replacement; the iterate is accumulated in FP32 between replacements
+      // and added to x64 in FP64. The search direction is never restarted, so
+      // the iteration count stays close to FP64 CG's.
       float *r32 = a.ws.r32, *z32 = a.ws.z32, *p032 = a.ws.p032, *p132 = a.ws.p132, *q32 = a.ws.q32;
-      float *d32 = a.ws.d32, *rhs32 = a.ws.rhs32;
+      float* y32 = a.ws.d32;
+      const double delta = 0.1;
+      const int gridR = grid_of(cg_replace<NF, NBMAX, 2>, kThreads);
       if (!a.use_initial_guess) set_dirichlet_start(A, a.ws.bS, x, s);
-      int innerLeft = a.maxits;
-      while (true) {
-        if ((err = reset_state(innerLeft)) != cudaSuccess) return fail(err);
+      cudaMemsetAsync(y32, 0, sizeof(float) * n, s);
+      // true residual of x (and ||b||^2 of the reference rhs for the tolerance)
+      auto replace = [&]() {
         tm->begin(K_OTHER, s);
-        launch_start(A, a, x, st, partials, 0, gridF, s);  // FP64 residual of A'
+        switch (pcT) {
+          case 0: cg_replace<NF, NBMAX, 0><<<gridR, kThreads, 0, s>>>(A, a.val, a.ws.bS, a.rhs, x, r32, z32, a.ws.pc32, st, partials); break;
+          case 1: cg_replace<NF, NBMAX, 1><<<gridR, kThreads, 0, s>>>(A, a.val, a.ws.bS, a.rhs, x, r32, z32, a.ws.pc32, st, partials); break;
+          default: cg_replace<NF, NBMAX, 2><<<gridR, kThreads, 0, s>>>(A, a.val, a.ws.bS, a.rhs, x, r32, z32, a.ws.pc32, st, partials); break;
+        }
         tm->end(K_OTHER, s);
         cudaMemcpyAsync(&hst, st, sizeof(CgState), cudaMemcpyDeviceToHost, s);
-        cudaStreamSynchronize(s);
-        if (refinements == 0) out->bb = hst.bb;
-        double bb = out->bb;
-        if (!(hst.rr <= a.rtol * a.rtol * bb) && !std::isfinite(hst.rr)) {
+        return cudaStreamSynchronize(s);
+      };
+      if ((err = reset_state(a.maxits)) != cudaSuccess) return fail(err);
+      if ((err = replace()) != cudaSuccess) return fail(err);
+      const double tol2 = a.rtol * a.rtol * hst.bb;
+      double lastR2 = hst.rr;
+      bool first = true;
+      while (hst.rr > tol2) {
+        if (!std::isfinite(hst.rr)) {
           status = 7;
           break;
         }
-        if (hst.rr <= a.rtol * a.rtol * bb) break;
-        if (innerLeft <= 0 || refinements >= a.max_refinements) {
+        if (totalIters >= a.maxits) {
           status = 5;
           break;
         }
-        double rn = std::sqrt(hst.rr);
-        scale_to_f32<<<gridU, kThreads, 0, s>>>(n, a.ws.r, 1.0 / rn, rhs32);
-        if ((err = reset_state(innerLeft)) != cudaSuccess) return fail(err);
-        launch_start_f32(A.nFaces, rhs32, d32, r32, z32, a.ws.pc32, st, partials, pcT, gridU, s);
-        cudaMemcpyAsync(&hst, st, sizeof(CgState), cudaMemcpyDeviceToHost, s);
-        cudaStreamSynchronize(s);
-        // inner target relative to ||rhs32|| = 1, but no tighter than needed
-        double want = a.rtol * std::sqrt(bb) / rn;
-        double inner = a.inner_rtol > want ? a.inner_rtol : want;
-        double tol2 = inner * inner * hst.rr;
-        int it = 0;
+        // the FP32 recurrence runs until its residual has dropped by delta
+        // since the last replacement (never below the final tolerance)
+        const double stretch2 = std::max(delta * delta * lastR2, tol2);
+        hst.done = 0;
+        hst.iters = 0;
+        hst.maxits = a.maxits - totalIters;
+        hst.status = 0;
+        hst.ticket = 0;
+        cudaMemcpyAsync(st, &hst, sizeof(CgState), cudaMemcpyHostToDevice, s);
+        int it = totalIters;  // the ping-pong parity follows completed iterations
         while (true) {
           for (int k = 0; k < a.check_every; ++k, ++it) {
             float* pold = (it & 1) ? p132 : p032;
             float* pnew = (it & 1) ? p032 : p132;
             tm->begin(K_SPMV32, s);
             cg_spmv<float, NF, NBMAX, false><<<gridF32, kThreads, 0, s>>>(A, a.ws.val32, z32, pold, pnew, q32, st,
-                                                                        partials, it == 0);
+                                                                          partials, first ? 1 : 0);
             tm->end(K_SPMV32, s);
+            first = false;
             tm->begin(K_UPDATE, s);
-            launch_update<float>(A.nFaces, d32, r32, z32, pnew, q32, a.ws.pc32, st, partials, tol2, pcT, gridU, s);
+            launch_update<float>(A.nFaces, y32, r32, z32, pnew, q32, a.ws.pc32, st, partials, stretch2, pcT, gridU, s);
             tm->end(K_UPDATE, s);
           }
           if ((err = cudaGetLastError()) != cudaSuccess) return fail(err);
@@ -633,13 +740,21 @@ struct Driver {
           if (hst.done) break;
         }
         totalIters += hst.iters;
-        innerLeft -= hst.iters;
-        refinements += 1;
         if (hst.status != 0 && hst.status != 5) {
           status = hst.status;
           break;
         }
-        axpy_f32_to_f64<<<gridU, kThreads, 0, s>>>(n, rn, d32, x);
+        // r.z of the iteration before the last one: beta = rz_new / rz_prev
+        const double rzPrev = hst.beta != 0.0 ? hst.rz / hst.beta : 0.0;
+        // reliable update: x += y (FP64), r = b' - A' x (FP64), direction kept
+        accum_x<<<gridU, kThreads, 0, s>>>(n, y32, x);
+        hst.ticket = 0;
+        cudaMemcpyAsync(st, &hst, sizeof(CgState), cudaMemcpyHostToDevice, s);
+        if ((err = replace()) != cudaSuccess) return fail(err);
+        refinements += 1;
+        lastR2 = hst.rr;
+        hst.beta = rzPrev > 0.0 ? hst.rz / rzPrev : 0.0;
+        if (hst.iters == 0) first = true;  // nothing ran: restart the direction
       }
     }
     // final residual of the reference system
@@ -755,6 +870,79 @@ static void residual_t(const TraceSolveArgs& a, TraceSolveResult* out) {
   } while (0)
 
 void trace_prepare(const TraceSolveArgs& a) { HFX_DISPATCH_NF(prepare_t, a); }
+
+template <int NF, int NBMAX>
+static void prepare_f32_t(const TraceView& A, const float* val, const float* rhs, float* bS, int pcType, float* pc,
+                          cudaStream_t s) {
+  prepare_rhs_t<float, NF, NBMAX><<<grid_of(prepare_rhs_t<float, NF, NBMAX>, kThreads), kThreads, 0, s>>>(A, val, rhs, bS);
+  if (pcType > 0 && pc)
+    build_precond_t<float, NF><<<(unsigned)((A.nFaces + 127) / 128), 128, 0, s>>>(A, val, pcType, pc);
+}
+
+void trace_prepare_f32(int dim, const TraceView& A, const float* val, const float* rhs, float* bS, int pcType,
+                       float* pc, cudaStream_t s) {
+  struct {
+    int dim;
+    TraceView A;
+  } a{dim, A};
+  HFX_DISPATCH_NF(prepare_f32_t, A, val, rhs, bS, pcType, pc, s);
+}
+
+// FP32 CG on the eliminated system from raw FP32 values (masked on the fly).
+template <int NF, int NBMAX>
+static void cg_f32_t(const F32SolveArgs& a, int* its, int* status) {
+  cudaStream_t s = a.stream;
+  const TraceView& A = a.A;
+  KernelTimer* tm = a.timer;
+  const int gridF = grid_of(cg_spmv<float, NF, NBMAX, true>, kThreads);
+  const int gridU = grid_of(cg_update<float, NF, 2>, kThreads);
+  tm->begin(K_OTHER, s);
+  prepare_f32_t<NF, NBMAX>(A, a.val, a.rhs, a.ws.bS32, a.rebuildPrecond ? a.precond : 0, a.ws.pc32, s);
+  CgState init{}, hst;
+  init.maxits = a.maxits;
+  cudaMemcpyAsync(a.ws.state, &init, sizeof(CgState), cudaMemcpyHostToDevice, s);
+  switch (a.precond) {
+    case 0: cg_start_zero_f32<NF, 0><<<gridU, kThreads, 0, s>>>(A.nFaces, a.ws.bS32, a.x, a.ws.r32, a.ws.z32, a.ws.pc32, a.ws.state, a.ws.partials); break;
+    case 1: cg_start_zero_f32<NF, 1><<<gridU, kThreads, 0, s>>>(A.nFaces, a.ws.bS32, a.x, a.ws.r32, a.ws.z32, a.ws.pc32, a.ws.state, a.ws.partials); break;
+    default: cg_start_zero_f32<NF, 2><<<gridU, kThreads, 0, s>>>(A.nFaces, a.ws.bS32, a.x, a.ws.r32, a.ws.z32, a.ws.pc32, a.ws.state, a.ws.partials); break;
+  }
+  tm->end(K_OTHER, s);
+  cudaMemcpyAsync(&hst, a.ws.state, sizeof(CgState), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  const double tol2 = a.rtol * a.rtol * hst.rr;
+  *status = 0;
+  if (!(hst.rr > tol2)) return;
+  int it = 0;
+  while (true) {
+    for (int k = 0; k < 25; ++k, ++it) {
+      float* pold = (it & 1) ? a.ws.p132 : a.ws.p032;
+      float* pnew = (it & 1) ? a.ws.p032 : a.ws.p132;
+      tm->begin(K_SPMV32, s);
+      cg_spmv<float, NF, NBMAX, true><<<gridF, kThreads, 0, s>>>(A, a.val, a.ws.z32, pold, pnew, a.ws.q32, a.ws.state,
+                                                                  a.ws.partials, it == 0);
+      tm->end(K_SPMV32, s);
+      tm->begin(K_UPDATE, s);
+      switch (a.precond) {
+        case 0: cg_update<float, NF, 0><<<gridU, kThreads, 0, s>>>(A.nFaces, a.x, a.ws.r32, a.ws.z32, pnew, a.ws.q32, a.ws.pc32, a.ws.state, a.ws.partials, tol2); break;
+        case 1: cg_update<float, NF, 1><<<gridU, kThreads, 0, s>>>(A.nFaces, a.x, a.ws.r32, a.ws.z32, pnew, a.ws.q32, a.ws.pc32, a.ws.state, a.ws.partials, tol2); break;
+        default: cg_update<float, NF, 2><<<gridU, kThreads, 0, s>>>(A.nFaces, a.x, a.ws.r32, a.ws.z32, pnew, a.ws.q32, a.ws.pc32, a.ws.state, a.ws.partials, tol2); break;
+      }
+      tm->end(K_UPDATE, s);
+    }
+    cudaMemcpyAsync(&hst, a.ws.state, sizeof(CgState), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    if (hst.done) break;
+  }
+  *its += hst.iters;
+  *status = hst.status;
+}
+
+int trace_solve_f32(const F32SolveArgs& a, int* its) {
+  if (a.gmres) return trace_gmres_f32(a, its);
+  int status = 9;
+  HFX_DISPATCH_NF(cg_f32_t, a, its, &status);
+  return status;
+}
 void trace_ref_residual(const TraceSolveArgs& a, TraceSolveResult* out) { HFX_DISPATCH_NF(residual_t, a, out); }
 
 }  // namespace hfx

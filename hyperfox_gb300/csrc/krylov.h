@@ -29,7 +29,7 @@ struct CgState {
 
 struct TraceWorkspace {
   double *bS, *r, *z, *p0, *p1, *q, *pc64;
-  float *val32, *pc32, *r32, *z32, *p032, *p132, *q32, *d32, *rhs32;
+  float *val32, *pc32, *r32, *z32, *p032, *p132, *q32, *d32, *rhs32, *bS32;
   double* partials;
   CgState* state;
   // GMRES: Krylov bases (restart+1 vectors) and the small device vector of coefficients
@@ -67,6 +67,10 @@ size_t trace_partials_needed();
 // Shared pieces: b', the FP32 copy of A' (mixed) and the preconditioner; the
 // reference-system residual into out->rel_residual.
 void trace_prepare(const TraceSolveArgs& a);
+// FP32 right-hand side b' of the eliminated system and (optionally) the FP32
+// preconditioner, from raw FP32 trace values (mixed-precision corrections).
+void trace_prepare_f32(int dim, const TraceView& A, const float* val, const float* rhs, float* bS, int pcType,
+                       float* pc, cudaStream_t s);
 void trace_ref_residual(const TraceSolveArgs& a, TraceSolveResult* out);
 
 }  // namespace hfx

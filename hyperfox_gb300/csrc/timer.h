@@ -14,7 +14,8 @@ enum KernelId {
   K_UPDATE = 4,     // CG vector update + preconditioner (both precisions)
   K_RECOVER = 5,    // local recovery
   K_OTHER = 6,      // setup kernels of the solve (system prep, preconditioner, residuals)
-  K_COUNT = 7
+  K_RESIDUAL = 7,   // FP64 matrix-free residual of the full HDG system (mixed precision)
+  K_COUNT = 8
 };
 
 class KernelTimer {

@@ -12,6 +12,7 @@
 #include <cmath>
 #include <vector>
 
+#include "hdg_mixed.h"
 #include "krylov.h"
 
 namespace hfx {
@@ -21,69 +22,49 @@ constexpr int kT = 256;
 
 template <int NF, int NBMAX>
 struct Cfg {
+  static constexpr int FPW = 32 / NF;
   static constexpr int NPOS = NBMAX * NF;
-  static constexpr int GS = NPOS <= 16 ? 16 : 32;
-  static constexpr int KPL = (NPOS + GS - 1) / GS;
 };
 
 // out = A' in ; MASKED applies the reference values with the Dirichlet
-// elimination and the sign flip on the fly (FP64), else val holds A'.
+// elimination and the sign flip on the fly, else val holds A'. Thread per row,
+// blocks column-major (same layout and mapping as the CG kernel).
 template <typename T, int NF, int NBMAX, bool MASKED>
 __global__ void __launch_bounds__(kT) op_apply(TraceView A, const T* __restrict__ val, const T* __restrict__ in,
                                                T* __restrict__ out) {
-  using G = Cfg<NF, NBMAX>;
-  const int lane = threadIdx.x % G::GS;
-  const int gpb = kT / G::GS;
-  const int gInWarp = (threadIdx.x & 31) / G::GS;
-  for (int64_t fb = ((int64_t)blockIdx.x * (kT / 32) + (threadIdx.x >> 5)) * (32 / G::GS); fb < A.nFaces;
-       fb += (int64_t)gridDim.x * gpb) {
-    const int64_t f = fb + gInWarp;
-    const bool act = f < A.nFaces;
+  constexpr int FPW = Cfg<NF, NBMAX>::FPW;
+  __shared__ T xsh[kT / 32][FPW][Cfg<NF, NBMAX>::NPOS];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int slot = lane / NF, a = lane % NF;
+  const bool laneUsed = slot < FPW;
+  const int64_t stride = (int64_t)gridDim.x * (kT / 32) * FPW;
+  for (int64_t fb = ((int64_t)blockIdx.x * (kT / 32) + warp) * FPW; fb < A.nFaces; fb += stride) {
+    const int64_t f = fb + slot;
+    const bool act = laneUsed && f < A.nFaces;
     const int64_t b0 = act ? A.browptr[f] : 0;
     const int nb = act ? (int)(A.browptr[f + 1] - b0) : 0;
-    const int npos = nb * NF;
     const bool rowBnd = MASKED && act && A.isBnd[f];
-    T xv[G::KPL];
-#pragma unroll
-    for (int k = 0; k < G::KPL; ++k) {
-      int m = lane + k * G::GS;
-      T v = 0;
-      if (m < npos) {
-        int g = A.bcol[b0 + m / NF];
-        v = in[(int64_t)g * NF + m % NF];
-        if (MASKED && (rowBnd || A.isBnd[g])) v = 0;
+    T* xs = laneUsed ? xsh[warp][slot] : nullptr;
+    if (act)
+      for (int k = 0; k < nb; ++k) {
+        int g = A.bcol[b0 + k];
+        T v = in[(int64_t)g * NF + a];
+        if (MASKED && (rowBnd || A.isBnd[g])) v = T(0);
+        xs[k * NF + a] = v;
       }
-      xv[k] = v;
-    }
-    const T* base = val + b0 * NF * NF;
-    T vv[NF][G::KPL];
+    __syncwarp();
+    if (act) {
+      const T* base = val + b0 * NF * NF + a;
+      T acc = T(0);
+      for (int k = 0; k < nb; ++k) {
+        const T* blk = base + (int64_t)k * NF * NF;
 #pragma unroll
-    for (int a = 0; a < NF; ++a)
-#pragma unroll
-      for (int k = 0; k < G::KPL; ++k) {
-        int m = lane + k * G::GS;
-        vv[a][k] = (m < npos) ? __ldg(base + (int64_t)a * npos + m) : T(0);
+        for (int b = 0; b < NF; ++b) acc += __ldg(blk + b * NF) * xs[k * NF + b];
       }
-    T y[NF];
-#pragma unroll
-    for (int a = 0; a < NF; ++a) {
-      T acc = 0;
-#pragma unroll
-      for (int k = 0; k < G::KPL; ++k) acc += vv[a][k] * xv[k];
-      y[a] = acc;
+      int64_t i = f * NF + a;
+      out[i] = MASKED ? (rowBnd ? in[i] : -acc) : acc;
     }
-#pragma unroll
-    for (int o = G::GS / 2; o > 0; o >>= 1)
-#pragma unroll
-      for (int a = 0; a < NF; ++a) y[a] += __shfl_xor_sync(0xffffffffu, y[a], o, G::GS);
-    if (act && lane < NF) {
-      T ya = 0;
-#pragma unroll
-      for (int a = 0; a < NF; ++a)
-        if (a == lane) ya = y[a];
-      int64_t i = f * NF + lane;
-      out[i] = MASKED ? (rowBnd ? in[i] : -ya) : ya;
-    }
+    __syncwarp();
   }
 }
 
@@ -99,7 +80,7 @@ __global__ void pc_apply(int64_t nFaces, const T* __restrict__ pc, const T* __re
       else if (PC == 1) z = pc[f * NF + a] * v[a];
       else {
         z = 0;
-        for (int b = 0; b < NF; ++b) z += pc[f * NF * NF + a * NF + b] * v[b];
+        for (int b = 0; b < NF; ++b) z += pc[f * NF * NF + b * NF + a] * v[b];  // column-major
       }
       out[f * NF + a] = z;
     }
@@ -425,6 +406,35 @@ int drive(const TraceSolveArgs& a, TraceSolveResult* out) {
 }
 
 }  // namespace
+
+template <int NF, int NBMAX>
+int gmres_f32_t(const F32SolveArgs& a, int* its) {
+  trace_prepare_f32(a.dim, a.A, a.val, a.rhs, a.ws.bS32, a.rebuildPrecond ? a.precond : 0, a.ws.pc32, a.stream);
+  double relres = 0.0;
+  return gmres_run<float, NF, NBMAX, true>(a.A, a.val, a.precond, a.ws.pc32, a.ws.bS32, a.x, a.ws.V32, a.ws.q32,
+                                          a.ws.p032, a.ws.partials, a.ws.hdev, a.restart, a.rtol, a.maxits, its,
+                                          &relres, a.stream, a.timer, K_SPMV32);
+}
+
+int trace_gmres_f32(const F32SolveArgs& a, int* its) {
+  const int NF = a.A.NF;
+  if (a.dim == 2) {
+    switch (NF) {
+      case 2: return gmres_f32_t<2, 5>(a, its);
+      case 3: return gmres_f32_t<3, 5>(a, its);
+      case 4: return gmres_f32_t<4, 5>(a, its);
+      case 5: return gmres_f32_t<5, 5>(a, its);
+      case 6: return gmres_f32_t<6, 5>(a, its);
+    }
+  } else if (a.dim == 3) {
+    switch (NF) {
+      case 3: return gmres_f32_t<3, 7>(a, its);
+      case 6: return gmres_f32_t<6, 7>(a, its);
+      case 10: return gmres_f32_t<10, 7>(a, its);
+    }
+  }
+  return 9;
+}
 
 int trace_gmres(const TraceSolveArgs& a, TraceSolveResult* out) {
   const int NF = a.A.NF;

@@ -141,6 +141,13 @@ int hfx_ip_coords(hfx_ctx* ctx, double* out /* [nCells][nIP][dim] */);
  * (:331-348), Dirichlet Set (:361-529) and the scatter into the trace CSR
  * (:531-675). All on the device, FP64. */
 int hfx_assemble(hfx_ctx* ctx);
+/* hfx_assemble_ex(ctx, HFX_PREC_FP64) == hfx_assemble. HFX_PREC_MIXED assembles
+ * in FP32 for a mixed-precision solve: hfx_solve then refines the full HDG
+ * system (u, q, lambda) with FP64 residuals (matrix free, the reference's
+ * element operators) and FP32 condensed corrections until the FP64 residual
+ * meets rtol; hfx_recover returns the refined FP64 Solution and Flux. The
+ * element blocks and CSR stay FP32 (hfx_get_condensed / hfx_get_csr refuse). */
+int hfx_assemble_ex(hfx_ctx* ctx, int precision);
 /* Condensed element blocks, column-major per element (any pointer may be NULL). */
 int hfx_get_condensed(hfx_ctx* ctx, double* S, double* S0, double* U, double* Q, double* U0,
                       double* Q0);
@@ -171,6 +178,7 @@ int hfx_recover(hfx_ctx* ctx, double* solution, double* flux);
 #define HFX_K_UPDATE 4
 #define HFX_K_RECOVER 5
 #define HFX_K_OTHER 6
+#define HFX_K_RESIDUAL 7
 int hfx_profile_enable(hfx_ctx* ctx, int on);
 int hfx_kernel_time(hfx_ctx* ctx, int kernel, int* launches, double* ms);
 int hfx_mark(hfx_ctx* ctx, int slot);

@@ -192,3 +192,42 @@ def test_manufactured_convergence(hfx_lib):
     rates = np.log2(np.array(errs[:-1]) / np.array(errs[1:]))
     assert errs[-1] < 1e-3
     assert rates.min() > 2.5, (errs, rates)
+
+
+@pytest.mark.parametrize("dim,n,order", [(2, 8, 2), (2, 4, 4), (3, 2, 2), (3, 2, 3)])
+@pytest.mark.parametrize("kappa", ["cell", "scalar"])
+def test_mixed_precision_solve(hfx_lib, dim, n, order, kappa):
+    """FP32 condensation + FP32 Krylov as corrections of the FP64 full-system
+    residual: the refined trace, Solution and Flux equal the FP64 direct solution
+    to 1e-8 relative."""
+    from hyperfox_gb300 import capi
+    P, ctx, _ = build_pair(hfx_lib, dim, n, order, tau2=True, kappa=kappa)
+    P.assemble()
+    x_ref = P.solve_direct()
+    osol, oflux = P.recover(x_ref)
+    ctx.assemble(precision=capi.PREC_MIXED)
+    trace, info = ctx.solve(rtol=1e-12, inner_rtol=1e-5, restart=40)
+    assert info.status == 0 and info.refinements >= 2
+    assert info.rel_residual < 1e-12
+    sol, flux = ctx.recover()
+    assert np.linalg.norm(trace - x_ref) / np.linalg.norm(x_ref) < 1e-8
+    assert np.linalg.norm(sol - osol) / np.linalg.norm(osol) < 1e-8
+    assert np.linalg.norm(flux - oflux) / np.linalg.norm(oflux) < 1e-8
+
+
+def test_mixed_precision_time_scheme_and_values_source(hfx_lib):
+    from hyperfox_gb300 import capi
+    P, ctx, (coords, cells) = build_pair(hfx_lib, 2, 4, 3, tau2=False, kappa="cell", dt=1e-2)
+    P.assemble()
+    x_ref = P.solve_direct()
+    ctx.assemble(precision=capi.PREC_MIXED)
+    trace, info = ctx.solve(rtol=1e-12)
+    assert np.linalg.norm(trace - x_ref) / np.linalg.norm(x_ref) < 1e-8
+
+
+def test_mixed_assembly_refuses_fp64_exports(hfx_lib):
+    from hyperfox_gb300 import capi
+    P, ctx, _ = build_pair(hfx_lib, 2, 3, 2, tau2=False, kappa="none")
+    ctx.assemble(precision=capi.PREC_MIXED)
+    with pytest.raises(capi.HfxError):
+        ctx.condensed()
