@@ -169,8 +169,9 @@ def run_ours(args, world, rank, local):
     ctx.set_source(capi.SRC_SINPROD, param=dim * np.pi ** 2)
     L = ctx.L
     prec = capi.PREC_FP64 if args.precision == "fp64" else capi.PREC_MIXED
-    opts = capi.solve_opts(precision=prec, rtol=args.rtol, precond=capi.PC_BLOCK_JACOBI, maxits=200000,
-                           inner_rtol=args.inner_rtol)
+    pc = capi.PC_TWOLEVEL if args.precond == "twolevel" else capi.PC_BLOCK_JACOBI
+    opts = capi.solve_opts(precision=prec, rtol=args.rtol, precond=pc, maxits=200000,
+                           inner_rtol=args.inner_rtol, coarse_guess=int(args.coarse_guess))
     info = capi.SolveInfo()
 
     asm_prec = capi.PREC_MIXED if args.precision == "mixed" else capi.PREC_FP64
@@ -211,7 +212,7 @@ def run_ours(args, world, rank, local):
     dev_ms = barrier_max(world, ms.value)
     kt = {}
     for name, kid in (("local", 0), ("scatter", 1), ("spmv64", 2), ("spmv32", 3), ("update", 4), ("recover", 5),
-                      ("other", 6), ("residual", 7)):
+                      ("other", 6), ("residual", 7), ("coarse", 8)):
         n_l, t_l = capi.ctypes.c_int(), capi.ctypes.c_double()
         L.hfx_kernel_time(ctx.h, kid, capi.ctypes.byref(n_l), capi.ctypes.byref(t_l))
         kt[name] = (n_l.value, t_l.value)
@@ -289,7 +290,8 @@ def run_ours(args, world, rank, local):
         "dtype": "f64+f32" if prec else "f64",
         "data": "synthetic (seedless structured mesh, manufactured solution)",
         "config": {"workload": cfg["desc"], "elements": E, "order": p, "trace_dofs": n, "csr_nnz": nnz,
-                   "precision": args.precision, "preconditioner": "block-Jacobi (per face)",
+                   "precision": args.precision, "preconditioner": ("two-level: per-face block Jacobi + vertex coarse space (Chebyshev degree %d)"
+                                      % info.coarse_degree) if args.precond == "twolevel" else "block-Jacobi (per face)",
                    "rtol": args.rtol, "l2_flush": "inputs > L2 (no flush needed)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "time_to_solve_s": step_s,
@@ -351,6 +353,9 @@ def main():
     ap.add_argument("--rtol", type=float, default=1e-10,
                     help="fp64: trace-system relative residual; mixed: full HDG system relative residual")
     ap.add_argument("--inner-rtol", type=float, default=1e-5)
+    ap.add_argument("--precond", default="twolevel", choices=["twolevel", "bj"],
+                    help="two-level (block Jacobi + vertex coarse space) or block Jacobi alone")
+    ap.add_argument("--coarse-guess", action="store_true", help="start CG from the prolongated coarse solution")
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

@@ -24,7 +24,7 @@ HFX_ERR_SINGULAR = 8
 HFX_ERR_UNSUPPORTED = 9
 
 KSP_CG, KSP_GMRES, KSP_AUTO = 0, 1, 2
-PC_NONE, PC_JACOBI, PC_BLOCK_JACOBI = 0, 1, 2
+PC_NONE, PC_JACOBI, PC_BLOCK_JACOBI, PC_TWOLEVEL = 0, 1, 2, 3
 PREC_FP64, PREC_MIXED = 0, 1
 SRC_NONE, SRC_VALUES, SRC_SINPROD = 0, 1, 2
 
@@ -35,7 +35,7 @@ EXPORTED = [
     "hfx_mesh_upload", "hfx_mesh_sizes", "hfx_mesh_topology", "hfx_mesh_compute_topology",
     "hfx_set_tau", "hfx_set_kappa", "hfx_set_source", "hfx_set_dirichlet", "hfx_set_time_scheme",
     "hfx_ip_coords", "hfx_assemble", "hfx_assemble_ex", "hfx_get_condensed", "hfx_get_csr",
-    "hfx_solve_opts_default", "hfx_solve", "hfx_recover",
+    "hfx_solve_opts_default", "hfx_solve", "hfx_recover", "hfx_coarse_operator",
     "hfx_la_create", "hfx_la_destroy", "hfx_la_allocate", "hfx_la_set_values", "hfx_la_set_rhs",
     "hfx_la_zero_rows", "hfx_la_assemble", "hfx_la_clear", "hfx_la_solve", "hfx_la_nnz",
     "hfx_profile_enable", "hfx_kernel_time", "hfx_mark", "hfx_elapsed_ms", "hfx_synchronize",
@@ -58,12 +58,14 @@ class RefElInfo(ctypes.Structure):
 class SolveOpts(ctypes.Structure):
     _fields_ = [("method", ctypes.c_int), ("precond", ctypes.c_int), ("precision", ctypes.c_int),
                 ("rtol", ctypes.c_double), ("maxits", ctypes.c_int), ("restart", ctypes.c_int),
-                ("inner_rtol", ctypes.c_double), ("use_initial_guess", ctypes.c_int)]
+                ("inner_rtol", ctypes.c_double), ("use_initial_guess", ctypes.c_int),
+                ("coarse_guess", ctypes.c_int)]
 
 
 class SolveInfo(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int), ("iterations", ctypes.c_int), ("refinements", ctypes.c_int),
-                ("rel_residual", ctypes.c_double), ("solve_ms", ctypes.c_double)]
+                ("rel_residual", ctypes.c_double), ("solve_ms", ctypes.c_double),
+                ("fallback", ctypes.c_int), ("coarse_degree", ctypes.c_int)]
 
 
 _lib = None
@@ -102,6 +104,7 @@ def load(path=LIB_PATH):
         "hfx_solve_opts_default": ([ctypes.POINTER(SolveOpts)], None),
         "hfx_solve": ([vp, ctypes.POINTER(SolveOpts), vp, ctypes.POINTER(SolveInfo)], ip),
         "hfx_recover": ([vp, vp, vp], ip),
+        "hfx_coarse_operator": ([vp, vp, vp, vp, vp, vp, vp], ip),
         "hfx_la_create": ([vp, ctypes.POINTER(vp)], ip),
         "hfx_la_destroy": ([vp], ip),
         "hfx_la_allocate": ([vp, ip], ip),
@@ -296,6 +299,20 @@ class Context:
         rc = self.L.hfx_solve(self.h, ctypes.byref(o), _p(trace), ctypes.byref(info))
         self._chk(rc, "solve")
         return trace, info
+
+    def coarse_operator(self):
+        """Two-level coarse operator: (rowptr, col, val FP32, vertexNode)."""
+        nV = ctypes.c_int()
+        nnz = ctypes.c_int64()
+        self._chk(self.L.hfx_coarse_operator(self.h, ctypes.byref(nV), ctypes.byref(nnz), None, None, None, None),
+                  "coarse_operator")
+        rowptr = np.zeros(nV.value + 1, np.int32)
+        col = np.zeros(nnz.value, np.int32)
+        val = np.zeros(nnz.value, np.float32)
+        vn = np.zeros(nV.value, np.int32)
+        self._chk(self.L.hfx_coarse_operator(self.h, ctypes.byref(nV), ctypes.byref(nnz), _p(rowptr), _p(col),
+                                             _p(val), _p(vn)), "coarse_operator")
+        return rowptr, col, val, vn
 
     def recover(self):
         sol = np.zeros((self.nCells, self.lenU))

@@ -112,6 +112,12 @@ struct hfx_ctx {
         *d_Q032 = nullptr, *d_dl32 = nullptr;
   double *d_ru = nullptr, *d_rq = nullptr, *d_rl = nullptr, *d_rtrace = nullptr, *d_part = nullptr;
   double mixedBB = 0.0, mixedRR = 0.0;
+  // two-level preconditioner: vertex coarse space (built on first use)
+  std::vector<int> cellVerts;  // [nCells][dim+1]
+  CoarseHost coarseHost;
+  CoarseSolver coarse;
+  DevMem coarseMem;
+  bool coarseBuilt = false;
   // timing
   KernelTimer timer;
   cudaEvent_t marks[8] = {};
@@ -296,6 +302,13 @@ int hfx_mesh_upload(hfx_ctx* c, int dim, int order, int nNodes, const double* co
   c->order = order;
   c->nNodes = nNodes;
   c->nCells = nCells;
+  c->cellVerts.resize((size_t)nCells * (dim + 1));
+  for (int64_t e = 0; e < nCells; ++e)
+    for (int m = 0; m <= dim; ++m) c->cellVerts[e * (dim + 1) + m] = cells[e * N + m];
+  c->coarseMem.release();
+  c->coarse = CoarseSolver{};
+  c->coarseHost = CoarseHost{};
+  c->coarseBuilt = false;
   cudaStream_t s = c->stream;
   DevMem& m = c->meshMem;
   // packed tables: phi, dphi, w, fphi, fdphi, fw
@@ -726,6 +739,7 @@ int hfx_assemble_ex(hfx_ctx* c, int precision) {
   if (!c->haveMesh) return set_err(c, HFX_ERR_STATE, "assemble: upload a mesh first");
   if (precision != HFX_PREC_FP64 && precision != HFX_PREC_MIXED) return set_err(c, HFX_ERR_ARG, "assemble: unknown precision");
   cudaSetDevice(c->device);
+  c->coarse.ready = false;  // the coarse operator follows the element matrices
   return precision == HFX_PREC_MIXED ? assemble_mixed(c) : assemble_fp64(c);
 }
 
@@ -793,6 +807,71 @@ int hfx_get_csr(hfx_ctx* c, int64_t* rowptr, int* col, double* val, double* rhs)
   return HFX_OK;
 }
 
+// Coarse space of the two-level preconditioner: host structure and device
+// buffers on first use (mesh-dependent), the operator after every assembly.
+static int ensure_coarse(hfx_ctx* c) {
+  cudaStream_t s = c->stream;
+  if (!c->coarseBuilt) {
+    std::string err;
+    CoarseHost h;
+    if (!build_coarse_host(c->re, c->nCells, c->cellVerts.data(), c->topo, &h, &err))
+      return set_err(c, HFX_ERR_ARG, err);
+    DevMem& m = c->coarseMem;
+    m.release();
+    CoarseDev& d = c->coarse.dev;
+    d = CoarseDev{};
+    d.nV = h.nV;
+    d.dim = h.dim;
+    d.NF = h.NF;
+    d.F = h.F;
+    d.LL = h.LL;
+    d.NV1 = h.NV1;
+    d.nFaces = c->topo.nFaces;
+    d.nCells = c->nCells;
+    d.nnz = (int64_t)h.col.size();
+    int *rowptr, *col, *cptr, *cidx, *rptr, *ridx, *faceV;
+    HFX_CUDA(c, upload(m, &rowptr, h.rowptr.data(), h.rowptr.size(), s));
+    HFX_CUDA(c, upload(m, &col, h.col.data(), h.col.size(), s));
+    HFX_CUDA(c, upload(m, &cptr, h.cptr.data(), h.cptr.size(), s));
+    HFX_CUDA(c, upload(m, &cidx, h.cidx.data(), h.cidx.size(), s));
+    HFX_CUDA(c, upload(m, &rptr, h.rptr.data(), h.rptr.size(), s));
+    HFX_CUDA(c, upload(m, &ridx, h.ridx.data(), h.ridx.size(), s));
+    HFX_CUDA(c, upload(m, &faceV, h.faceV.data(), h.faceV.size(), s));
+    HFX_CUDA(c, upload(m, &d.Wf, h.Wf.data(), h.Wf.size(), s));
+    HFX_CUDA(c, upload(m, &d.Wc, h.Wc.data(), h.Wc.size(), s));
+    d.rowptr = rowptr;
+    d.col = col;
+    d.cptr = cptr;
+    d.cidx = cidx;
+    d.rptr = rptr;
+    d.ridx = ridx;
+    d.faceV = faceV;
+    d.cell2face = c->d_cell2face;
+    d.isBnd = c->d_isBnd;
+    const size_t nV = (size_t)h.nV;
+    HFX_CUDA(c, dalloc(m, &d.Ce, (size_t)c->nCells * h.NV1 * h.NV1));
+    HFX_CUDA(c, dalloc(m, &d.val, h.col.size()));
+    HFX_CUDA(c, dalloc(m, &d.dinv, nV));
+    HFX_CUDA(c, dalloc(m, &d.rc, nV));
+    HFX_CUDA(c, dalloc(m, &d.yc, nV));
+    HFX_CUDA(c, dalloc(m, &d.cr, nV));
+    HFX_CUDA(c, dalloc(m, &d.cd0, nV));
+    HFX_CUDA(c, dalloc(m, &d.cd1, nV));
+    HFX_CUDA(c, dalloc(m, &d.lz, nV));
+    HFX_CUDA(c, dalloc(m, &d.partials, (size_t)152 * 32 + 64));
+    c->coarseHost = std::move(h);
+    c->coarseBuilt = true;
+    c->coarse.ready = false;
+  }
+  if (!c->coarse.ready) {
+    c->timer.begin(K_COARSE, s);
+    cudaError_t e = coarse_setup<double>(&c->coarse, c->d_S, 64, 0.1, s);
+    c->timer.end(K_COARSE, s);
+    if (e != cudaSuccess) return cuda_err(c, e, "coarse setup");
+  }
+  return HFX_OK;
+}
+
 void hfx_solve_opts_default(hfx_solve_opts* o) {
   if (!o) return;
   o->method = HFX_KSP_AUTO;
@@ -803,6 +882,7 @@ void hfx_solve_opts_default(hfx_solve_opts* o) {
   o->restart = 30;
   o->inner_rtol = 1e-4;
   o->use_initial_guess = 0;
+  o->coarse_guess = 0;
 }
 
 static int ensure_workspace(hfx_ctx* c, bool mixed, int restart) {
@@ -919,6 +999,8 @@ static int solve_mixed(hfx_ctx* c, const hfx_solve_opts& o, int method, int rest
     info->refinements = refinements;
     info->rel_residual = bb > 0 ? std::sqrt(rr / bb) : std::sqrt(rr);
     info->solve_ms = ms;
+    info->fallback = 0;
+    info->coarse_degree = 0;
   }
   if (trace) HFX_CUDA(c, cudaMemcpy(trace, c->d_trace, sizeof(double) * c->ndofs(), cudaMemcpyDeviceToHost));
   c->solved = true;
@@ -934,13 +1016,16 @@ int hfx_solve(hfx_ctx* c, const hfx_solve_opts* opts, double* trace, hfx_solve_i
   if (opts) o = *opts;
   else hfx_solve_opts_default(&o);
   if (o.method < HFX_KSP_CG || o.method > HFX_KSP_AUTO) return set_err(c, HFX_ERR_ARG, "solve: unknown method");
-  if (o.precond < HFX_PC_NONE || o.precond > HFX_PC_BLOCK_JACOBI || o.rtol <= 0.0 || o.maxits <= 0)
+  if (o.precond < HFX_PC_NONE || o.precond > HFX_PC_TWOLEVEL || o.rtol <= 0.0 || o.maxits <= 0)
     return set_err(c, HFX_ERR_ARG, "solve: bad options");
   int method = o.method;
   if (method == HFX_KSP_AUTO) method = c->kappaCellConstant ? HFX_KSP_CG : HFX_KSP_GMRES;
   if (method == HFX_KSP_CG && !c->kappaCellConstant)
     return set_err(c, HFX_ERR_ARG,
                    "solve: CG needs a symmetric trace system; the diffusion tensor varies inside cells (use GMRES)");
+  if (o.precond == HFX_PC_TWOLEVEL && (method != HFX_KSP_CG || c->mixedMode))
+    return set_err(c, HFX_ERR_UNSUPPORTED,
+                   "solve: the two-level preconditioner needs CG on the trace system assembled in FP64");
   const int restart = o.restart > 0 ? o.restart : 30;
   cudaSetDevice(c->device);
   bool mixed = o.precision == HFX_PREC_MIXED;
@@ -951,6 +1036,11 @@ int hfx_solve(hfx_ctx* c, const hfx_solve_opts* opts, double* trace, hfx_solve_i
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, c->stream);
+  if (o.precond == HFX_PC_TWOLEVEL && (rc = ensure_coarse(c))) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+  }
   TraceSolveArgs a{};
   a.dim = c->dim;
   a.A = TraceView{c->topo.nFaces, c->re.nNodesFace, c->d_browptr, c->d_bcol, c->d_isBnd};
@@ -969,8 +1059,24 @@ int hfx_solve(hfx_ctx* c, const hfx_solve_opts* opts, double* trace, hfx_solve_i
   a.stream = c->stream;
   a.timer = &c->timer;
   a.restart = restart;
+  a.coarse = o.precond == HFX_PC_TWOLEVEL ? &c->coarse : nullptr;
+  a.coarse_guess = o.coarse_guess;
   TraceSolveResult res;
   int st = method == HFX_KSP_CG ? trace_solve(a, &res) : trace_gmres(a, &res);
+  int fallback = 0;
+  if (o.precond == HFX_PC_TWOLEVEL &&
+      (st == HFX_ERR_BREAKDOWN || st == HFX_ERR_NAN || st == HFX_ERR_NOT_CONVERGED)) {
+    // the plain block-Jacobi solve finishes what the two-level solve could not
+    const int its = res.iterations;
+    a.precond = HFX_PC_BLOCK_JACOBI;
+    a.coarse = nullptr;
+    a.maxits = std::max(1, o.maxits - its);
+    a.use_initial_guess = 0;
+    res = TraceSolveResult{};
+    st = trace_solve(a, &res);
+    res.iterations += its;
+    fallback = 1;
+  }
   cudaEventRecord(e1, c->stream);
   cudaEventSynchronize(e1);
   float ms = 0.f;
@@ -983,6 +1089,8 @@ int hfx_solve(hfx_ctx* c, const hfx_solve_opts* opts, double* trace, hfx_solve_i
     info->refinements = res.refinements;
     info->rel_residual = res.rel_residual;
     info->solve_ms = ms;
+    info->fallback = fallback;
+    info->coarse_degree = o.precond == HFX_PC_TWOLEVEL ? c->coarse.degree : 0;
   }
   if (st == 3) return cuda_err(c, res.cudaErr, "solve");
   if (trace) HFX_CUDA(c, cudaMemcpy(trace, c->d_trace, sizeof(double) * c->ndofs(), cudaMemcpyDeviceToHost));
@@ -991,6 +1099,24 @@ int hfx_solve(hfx_ctx* c, const hfx_solve_opts* opts, double* trace, hfx_solve_i
   if (st == HFX_ERR_BREAKDOWN) return set_err(c, st, "solve: CG breakdown (non-positive curvature)");
   if (st == HFX_ERR_NAN) return set_err(c, st, "solve: NaN or Inf in the Krylov iteration");
   if (st != 0) return set_err(c, st, "solve: failed");
+  return HFX_OK;
+}
+
+int hfx_coarse_operator(hfx_ctx* c, int* nV, int64_t* nnz, int* rowptr, int* col, float* val, int* vertexNode) {
+  if (!c || !nV || !nnz) return HFX_ERR_ARG;
+  if (!c->assembled || c->mixedMode)
+    return set_err(c, HFX_ERR_STATE, "coarse_operator: needs a trace system assembled in FP64");
+  cudaSetDevice(c->device);
+  int rc = ensure_coarse(c);
+  if (rc) return rc;
+  const CoarseHost& h = c->coarseHost;
+  *nV = h.nV;
+  *nnz = (int64_t)h.col.size();
+  if (!rowptr) return HFX_OK;
+  std::copy(h.rowptr.begin(), h.rowptr.end(), rowptr);
+  if (col) std::copy(h.col.begin(), h.col.end(), col);
+  if (vertexNode) std::copy(h.vertexNode.begin(), h.vertexNode.end(), vertexNode);
+  if (val) HFX_CUDA(c, cudaMemcpy(val, c->coarse.dev.val, sizeof(float) * h.col.size(), cudaMemcpyDeviceToHost));
   return HFX_OK;
 }
 
@@ -1135,6 +1261,8 @@ int hfx_la_solve(hfx_la* la, const hfx_solve_opts* opts, double* x, hfx_solve_in
     info->refinements = 0;
     info->rel_residual = r.rel_residual;
     info->solve_ms = r.ms;
+    info->fallback = 0;
+    info->coarse_degree = 0;
   }
   if (st != 0) return set_err(la->ctx, st, err);
   return HFX_OK;

@@ -1,0 +1,503 @@
+// Vertex coarse space of the two-level trace preconditioner (see coarse.h):
+// host construction of the coarse pattern and of the contribution lists, the
+// Galerkin coarse operator from the element matrices, a Lanczos estimate of its
+// Jacobi-scaled spectrum, the Chebyshev coarse solve, restriction and
+// prolongation. Every sum runs in a fixed order (no atomics), so the coarse
+// operator and the preconditioner are bitwise reproducible.
+#include "coarse.h"
+
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+
+namespace hfx {
+
+// ------------------------------------------------------------------ host
+
+// Barycentric coordinates of a reference point w.r.t. the reference vertices
+// (nodes 0..dim): solve sum_m l_m V_m = x, sum_m l_m = 1.
+static void barycentric(const RefEl& re, const double* x, double* lam) {
+  const int d = re.dim;
+  double A[4][5];
+  for (int r = 0; r <= d; ++r) {
+    for (int m = 0; m <= d; ++m) A[r][m] = (r < d) ? re.nodes[m * d + r] : 1.0;
+    A[r][d + 1] = (r < d) ? x[r] : 1.0;
+  }
+  const int n = d + 1;
+  for (int k = 0; k < n; ++k) {
+    int piv = k;
+    for (int i = k + 1; i < n; ++i)
+      if (std::fabs(A[i][k]) > std::fabs(A[piv][k])) piv = i;
+    for (int j = 0; j <= n; ++j) std::swap(A[k][j], A[piv][j]);
+    for (int i = 0; i < n; ++i) {
+      if (i == k) continue;
+      double l = A[i][k] / A[k][k];
+      for (int j = k; j <= n; ++j) A[i][j] -= l * A[k][j];
+    }
+  }
+  for (int m = 0; m < n; ++m) lam[m] = A[m][n] / A[m][m];
+}
+
+bool coarse_weight_tables(const RefEl& re, std::vector<double>* Wf, std::vector<double>* Wc, std::string* err) {
+  const int d = re.dim, F = re.nFaces, NF = re.nNodesFace, NV1 = d + 1;
+  Wc->assign((size_t)F * NF * NV1, 0.0);
+  Wf->assign((size_t)NF * d, 0.0);
+  for (int i = 0; i < F; ++i) {
+    const int* fn = &re.faceNodes[(size_t)i * NF];
+    for (int k = 0; k < d; ++k)
+      if (fn[k] > d) {
+        *err = "coarse space: face vertices are not the first face nodes";
+        return false;
+      }
+    for (int j = 0; j < NF; ++j) {
+      double lam[4];
+      barycentric(re, &re.nodes[(size_t)fn[j] * d], lam);
+      for (int m = 0; m < NV1; ++m) (*Wc)[((size_t)i * NF + j) * NV1 + m] = std::fabs(lam[m]) < 1e-14 ? 0.0 : lam[m];
+      for (int k = 0; k < d; ++k) {
+        double w = lam[fn[k]];
+        if (std::fabs(w) < 1e-14) w = 0.0;
+        if (i == 0) (*Wf)[(size_t)j * d + k] = w;
+        else if (std::fabs((*Wf)[(size_t)j * d + k] - w) > 1e-12) {
+          *err = "coarse space: face weight table differs between faces";
+          return false;
+        }
+      }
+    }
+  }
+  return true;
+}
+
+bool build_coarse_host(const RefEl& re, int nCells, const int* cellVerts, const Topology& t, CoarseHost* out,
+                       std::string* err) {
+  const int d = re.dim, F = re.nFaces, NF = re.nNodesFace, NV1 = d + 1;
+  CoarseHost h;
+  h.dim = d;
+  h.NF = NF;
+  h.F = F;
+  h.LL = F * NF;
+  h.NV1 = NV1;
+  std::vector<double> Wf, Wc;
+  if (!coarse_weight_tables(re, &Wf, &Wc, err)) return false;
+  h.Wf.assign(Wf.begin(), Wf.end());
+  h.Wc.assign(Wc.begin(), Wc.end());
+  // coarse ids of the distinct cell vertices, in order of first appearance
+  int maxNode = 0;
+  for (int64_t i = 0; i < (int64_t)nCells * NV1; ++i) maxNode = std::max(maxNode, cellVerts[i]);
+  std::vector<int> cv((size_t)maxNode + 1, -1);
+  h.cellV.resize((size_t)nCells * NV1);
+  for (int e = 0; e < nCells; ++e)
+    for (int m = 0; m < NV1; ++m) {
+      int node = cellVerts[(int64_t)e * NV1 + m];
+      if (cv[node] < 0) {
+        cv[node] = h.nV++;
+        h.vertexNode.push_back(node);
+      }
+      h.cellV[(size_t)e * NV1 + m] = cv[node];
+    }
+  h.faceV.resize((size_t)t.nFaces * d);
+  for (int f = 0; f < t.nFaces; ++f)
+    for (int k = 0; k < d; ++k) {
+      int node = t.faces[(size_t)f * NF + k];
+      if (node > maxNode || cv[node] < 0) {
+        *err = "coarse space: face vertex is not a cell vertex";
+        return false;
+      }
+      h.faceV[(size_t)f * d + k] = cv[node];
+    }
+  // pattern: vertices sharing a cell; counting sort of (row, col) pairs
+  const int nV = h.nV;
+  std::vector<int64_t> cnt((size_t)nV + 1, 0);
+  for (int e = 0; e < nCells; ++e)
+    for (int m = 0; m < NV1; ++m) cnt[h.cellV[(size_t)e * NV1 + m] + 1] += NV1;
+  for (int v = 0; v < nV; ++v) cnt[v + 1] += cnt[v];
+  std::vector<int> pairs((size_t)cnt[nV]);   // column per (row, contribution)
+  std::vector<int> pairSrc((size_t)cnt[nV]);  // contribution index e*NV1^2 + m*NV1 + m2
+  {
+    std::vector<int64_t> pos(cnt.begin(), cnt.end() - 1);
+    for (int e = 0; e < nCells; ++e)
+      for (int m = 0; m < NV1; ++m) {
+        int v = h.cellV[(size_t)e * NV1 + m];
+        for (int m2 = 0; m2 < NV1; ++m2) {
+          int64_t p = pos[v]++;
+          pairs[p] = h.cellV[(size_t)e * NV1 + m2];
+          pairSrc[p] = (e * NV1 + m) * NV1 + m2;
+        }
+      }
+  }
+  h.rowptr.assign((size_t)nV + 1, 0);
+  h.cptr.push_back(0);
+  std::vector<int> order;
+  for (int v = 0; v < nV; ++v) {
+    const int64_t b = cnt[v], n = cnt[v + 1] - b;
+    order.resize(n);
+    std::iota(order.begin(), order.end(), 0);
+    // stable by column, then by contribution index (fixed summation order)
+    std::sort(order.begin(), order.end(), [&](int x, int y) {
+      if (pairs[b + x] != pairs[b + y]) return pairs[b + x] < pairs[b + y];
+      return pairSrc[b + x] < pairSrc[b + y];
+    });
+    int last = -1;
+    for (int64_t j = 0; j < n; ++j) {
+      int c = pairs[b + order[j]];
+      if (c != last) {
+        if (last >= 0) h.cptr.push_back((int)h.cidx.size());
+        h.col.push_back(c);
+        last = c;
+      }
+      h.cidx.push_back(pairSrc[b + order[j]]);
+    }
+    if (last >= 0) h.cptr.push_back((int)h.cidx.size());
+    h.rowptr[v + 1] = (int)h.col.size();
+  }
+  if ((int64_t)nCells * NV1 * NV1 > 2147483647LL) {
+    *err = "coarse space: too many cells for 32-bit contribution indices";
+    return false;
+  }
+  // restriction lists: faces incident to each vertex
+  h.rptr.assign((size_t)nV + 1, 0);
+  for (int f = 0; f < t.nFaces; ++f)
+    for (int k = 0; k < d; ++k) h.rptr[h.faceV[(size_t)f * d + k] + 1]++;
+  for (int v = 0; v < nV; ++v) h.rptr[v + 1] += h.rptr[v];
+  h.ridx.resize((size_t)h.rptr[nV]);
+  {
+    std::vector<int> pos(h.rptr.begin(), h.rptr.end() - 1);
+    for (int f = 0; f < t.nFaces; ++f)
+      for (int k = 0; k < d; ++k) h.ridx[pos[h.faceV[(size_t)f * d + k]]++] = f * d + k;
+  }
+  *out = std::move(h);
+  return true;
+}
+
+// ------------------------------------------------------------------ device
+
+namespace {
+
+constexpr int kT = 256;
+
+unsigned blocks_for(int64_t n, int threads = kT) {
+  int64_t g = (n + threads - 1) / threads;
+  if (g > 152 * 32) g = 152 * 32;
+  return (unsigned)(g < 1 ? 1 : g);
+}
+
+// C_e = -W_m^T S_e W_m, W_m = cell weights with the rows of Dirichlet faces
+// zeroed (A' = -A on interior rows). One warp per cell; lanes run over rows of
+// S_e (column-major, coalesced), FP32 arithmetic on the stored values.
+template <typename T, int NV1>
+__global__ void coarse_elem(CoarseDev c, const T* __restrict__ S) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warpId = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nWarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int LL = c.LL, NF = c.NF;
+  for (int64_t e = warpId; e < c.nCells; e += nWarps) {
+    const T* Se = S + e * (int64_t)LL * LL;
+    unsigned fmask = 0;  // bit i: face i of the cell is interior
+    for (int i = 0; i < c.F; ++i)
+      if (!c.isBnd[c.cell2face[e * c.F + i]]) fmask |= 1u << i;
+    float acc[NV1][NV1];
+#pragma unroll
+    for (int m = 0; m < NV1; ++m)
+#pragma unroll
+      for (int m2 = 0; m2 < NV1; ++m2) acc[m][m2] = 0.f;
+    for (int r = lane; r < LL; r += 32) {
+      const float maskR = (fmask >> (r / NF)) & 1u ? 1.f : 0.f;
+      float t[NV1];
+#pragma unroll
+      for (int m2 = 0; m2 < NV1; ++m2) t[m2] = 0.f;
+      for (int col = 0; col < LL; ++col) {
+        const float mc = (fmask >> (col / NF)) & 1u ? 1.f : 0.f;
+        const float s = (float)Se[r + (int64_t)col * LL] * mc;
+#pragma unroll
+        for (int m2 = 0; m2 < NV1; ++m2) t[m2] = fmaf(s, c.Wc[col * NV1 + m2], t[m2]);
+      }
+#pragma unroll
+      for (int m = 0; m < NV1; ++m) {
+        const float w = c.Wc[r * NV1 + m] * maskR;
+#pragma unroll
+        for (int m2 = 0; m2 < NV1; ++m2) acc[m][m2] = fmaf(w, t[m2], acc[m][m2]);
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < NV1; ++m)
+#pragma unroll
+      for (int m2 = 0; m2 < NV1; ++m2) {
+        float x = acc[m][m2];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) c.Ce[e * NV1 * NV1 + m * NV1 + m2] = -x;
+      }
+  }
+}
+
+// Coarse values by gathering the element contributions in fixed order, and the
+// inverse diagonal (0 marks a coarse DOF that touches no interior face).
+__global__ void coarse_gather(CoarseDev c) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < c.nV; v += (int64_t)gridDim.x * blockDim.x) {
+    float diag = 0.f;
+    for (int k = c.rowptr[v]; k < c.rowptr[v + 1]; ++k) {
+      float s = 0.f;
+      for (int j = c.cptr[k]; j < c.cptr[k + 1]; ++j) s += c.Ce[c.cidx[j]];
+      c.val[k] = s;
+      if (c.col[k] == v) diag = s;
+    }
+    c.dinv[v] = diag > 0.f ? 1.f / diag : 0.f;
+  }
+}
+
+// ---- Lanczos on D^{-1/2} A_c D^{-1/2} (eigenvalue bounds for Chebyshev)
+
+__device__ __forceinline__ float coarse_row_sym(const CoarseDev& c, int64_t v, const float* __restrict__ x) {
+  const float sv = sqrtf(c.dinv[v]);
+  float y = 0.f;
+  for (int k = c.rowptr[v]; k < c.rowptr[v + 1]; ++k) {
+    const int w = c.col[k];
+    y = fmaf(c.val[k] * sqrtf(c.dinv[w]), x[w], y);
+  }
+  return sv * y;
+}
+
+__device__ void block_partial(double v, double* partials, int slot) {
+  __shared__ double red[kT / 32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+    partials[(size_t)slot * gridDim.x + blockIdx.x] = s;
+  }
+  __syncthreads();
+}
+
+// start vector: deterministic pseudo-random entries on active DOFs; norm^2
+__global__ void lanczos_init(CoarseDev c, float* v, double* partials) {
+  double ss = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < c.nV; i += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t h = (uint32_t)i * 2654435761u + 12345u;
+    h ^= h >> 13;
+    h *= 0x5bd1e995u;
+    h ^= h >> 15;
+    float x = c.dinv[i] > 0.f ? 0.5f + (float)(h & 0xffff) / 65536.f : 0.f;
+    v[i] = x;
+    ss += (double)x * x;
+  }
+  block_partial(ss, partials, 0);
+}
+
+__global__ void lanczos_scale(int64_t n, float* v, float s) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    v[i] *= s;
+}
+
+// w = A v - beta v_prev; partial alpha = w . v
+__global__ void lanczos_apply(CoarseDev c, const float* v, const float* vprev, float beta, float* w,
+                              double* partials) {
+  double a = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < c.nV; i += (int64_t)gridDim.x * blockDim.x) {
+    float y = c.dinv[i] > 0.f ? coarse_row_sym(c, i, v) : 0.f;
+    y -= beta * vprev[i];
+    w[i] = y;
+    a += (double)y * v[i];
+  }
+  block_partial(a, partials, 0);
+}
+
+// w -= alpha v; partial |w|^2
+__global__ void lanczos_orth(int64_t n, const float* v, float alpha, float* w, double* partials) {
+  double ss = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float y = w[i] - alpha * v[i];
+    w[i] = y;
+    ss += (double)y * y;
+  }
+  block_partial(ss, partials, 0);
+}
+
+// ---- coarse solve
+
+// rc = P^T r (interior faces); Chebyshev start: cr = rc, d0 = D^{-1} rc / theta, yc = 0
+template <typename T>
+__global__ void coarse_restrict(CoarseDev c, const T* __restrict__ r, const int* skip) {
+  if (skip && *skip) return;
+  const int d = c.dim, NF = c.NF;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < c.nV; v += (int64_t)gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int j = c.rptr[v]; j < c.rptr[v + 1]; ++j) {
+      const int fk = c.ridx[j];
+      const int64_t f = fk / d;
+      const int k = fk - (int)f * d;
+      if (c.isBnd[f]) continue;
+      const T* rf = r + f * NF;
+      for (int a = 0; a < NF; ++a) s = fmaf(c.Wf[a * d + k], (float)rf[a], s);
+    }
+    c.rc[v] = s;
+    c.cr[v] = s;
+    c.yc[v] = 0.f;
+    c.cd0[v] = c.dinv[v] * s / c.theta;
+  }
+}
+
+// One Chebyshev step: yc += d_k, r -= A d_k, d_{k+1} = c1 d_k + c2 D^{-1} r
+__global__ void coarse_cheb_step(CoarseDev c, const float* __restrict__ dk, float* __restrict__ dn, float c1, float c2,
+                                 int last, const int* skip) {
+  if (skip && *skip) return;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < c.nV; v += (int64_t)gridDim.x * blockDim.x) {
+    const float dv = dk[v];
+    c.yc[v] += dv;
+    if (last) continue;
+    float y = 0.f;
+    for (int k = c.rowptr[v]; k < c.rowptr[v + 1]; ++k) y = fmaf(c.val[k], dk[c.col[k]], y);
+    const float r = c.cr[v] - y;
+    c.cr[v] = r;
+    dn[v] = c1 * dv + c2 * c.dinv[v] * r;
+  }
+}
+
+template <typename T>
+__global__ void coarse_prolong(CoarseDev c, T* __restrict__ x) {
+  const int d = c.dim, NF = c.NF;
+  const int64_t n = c.nFaces * NF;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t f = i / NF;
+    const int a = (int)(i - f * NF);
+    if (c.isBnd[f]) continue;
+    float s = 0.f;
+    for (int k = 0; k < d; ++k) s = fmaf(c.Wf[a * d + k], c.yc[c.faceV[f * d + k]], s);
+    x[i] += (T)s;
+  }
+}
+
+// Sturm count: number of eigenvalues of the tridiagonal (a, b) below x.
+int sturm_below(const std::vector<double>& a, const std::vector<double>& b, double x) {
+  int cnt = 0;
+  double q = 1.0;
+  for (size_t i = 0; i < a.size(); ++i) {
+    double bb = i ? b[i - 1] * b[i - 1] : 0.0;
+    q = a[i] - x - (i ? bb / q : 0.0);
+    if (q == 0.0) q = 1e-300;
+    if (q < 0) ++cnt;
+  }
+  return cnt;
+}
+
+double tridiag_eig(const std::vector<double>& a, const std::vector<double>& b, int k) {
+  double lo = 1e300, hi = -1e300;
+  for (size_t i = 0; i < a.size(); ++i) {
+    double r = (i ? std::fabs(b[i - 1]) : 0.0) + (i + 1 < a.size() ? std::fabs(b[i]) : 0.0);
+    lo = std::min(lo, a[i] - r);
+    hi = std::max(hi, a[i] + r);
+  }
+  for (int it = 0; it < 200; ++it) {
+    double mid = 0.5 * (lo + hi);
+    if (sturm_below(a, b, mid) > k) hi = mid;
+    else lo = mid;
+  }
+  return 0.5 * (lo + hi);
+}
+
+double sum_partials(const double* h, int n) {
+  double s = 0.0;
+  for (int i = 0; i < n; ++i) s += h[i];
+  return s;
+}
+
+}  // namespace
+
+template <typename T>
+cudaError_t coarse_setup(CoarseSolver* cs, const T* S, int maxDegree, double target, cudaStream_t s) {
+  CoarseDev* c = &cs->dev;
+  cs->ready = false;
+  const unsigned gE = blocks_for(c->nCells * 32);
+  if (c->NV1 == 3) coarse_elem<T, 3><<<gE, kT, 0, s>>>(*c, S);
+  else coarse_elem<T, 4><<<gE, kT, 0, s>>>(*c, S);
+  coarse_gather<<<blocks_for(c->nV), kT, 0, s>>>(*c);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  // Lanczos, m steps, on D^{-1/2} A_c D^{-1/2}
+  const unsigned g = blocks_for(c->nV);
+  std::vector<double> hp(g);
+  float *v = c->cd0, *vprev = c->cd1, *w = c->lz;
+  cudaMemsetAsync(vprev, 0, sizeof(float) * c->nV, s);
+  lanczos_init<<<g, kT, 0, s>>>(*c, v, c->partials);
+  cudaMemcpyAsync(hp.data(), c->partials, sizeof(double) * g, cudaMemcpyDeviceToHost, s);
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+  double nrm = std::sqrt(sum_partials(hp.data(), g));
+  if (!(nrm > 0)) {
+    cs->lmin = cs->lmax = 1.0;
+    cs->degree = 0;
+    cs->ready = true;
+    return cudaSuccess;
+  }
+  lanczos_scale<<<g, kT, 0, s>>>(c->nV, v, (float)(1.0 / nrm));
+  std::vector<double> al, be;
+  const int m = (int)std::min<int64_t>(40, c->nV);
+  double beta = 0.0;
+  for (int j = 0; j < m; ++j) {
+    lanczos_apply<<<g, kT, 0, s>>>(*c, v, vprev, (float)beta, w, c->partials);
+    cudaMemcpyAsync(hp.data(), c->partials, sizeof(double) * g, cudaMemcpyDeviceToHost, s);
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+    double alpha = sum_partials(hp.data(), g);
+    al.push_back(alpha);
+    lanczos_orth<<<g, kT, 0, s>>>(c->nV, v, (float)alpha, w, c->partials);
+    cudaMemcpyAsync(hp.data(), c->partials, sizeof(double) * g, cudaMemcpyDeviceToHost, s);
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+    beta = std::sqrt(sum_partials(hp.data(), g));
+    if (j + 1 == m || beta < 1e-10 * std::fabs(alpha)) break;
+    be.push_back(beta);
+    lanczos_scale<<<g, kT, 0, s>>>(c->nV, w, (float)(1.0 / beta));
+    float* t = vprev;
+    vprev = v;
+    v = w;
+    w = t;
+  }
+  be.resize(al.size() > 0 ? al.size() - 1 : 0);
+  const double tmin = tridiag_eig(al, be, 0), tmax = tridiag_eig(al, be, (int)al.size() - 1);
+  // upper bound must cover the spectrum (|p| <= 1 there keeps q(A_c) SPD);
+  // the lower end may be above the true minimum: modes below it are damped less
+  cs->lmax = 1.1 * tmax;
+  cs->lmin = std::max(tmin / 1.5, cs->lmax * 1e-6);
+  const double th = 0.5 * (cs->lmax + cs->lmin), de = 0.5 * (cs->lmax - cs->lmin);
+  const double sig = th / de;
+  int K = (int)std::ceil(std::acosh(1.0 / target) / std::acosh(sig));
+  K = std::max(1, std::min(K, maxDegree));
+  cs->degree = K;
+  c->theta = (float)th;
+  cs->c1.assign(K, 0.f);
+  cs->c2.assign(K, 0.f);
+  double rho = 1.0 / sig;
+  for (int k = 0; k < K; ++k) {
+    double rho1 = 1.0 / (2.0 * sig - rho);
+    cs->c1[k] = (float)(rho1 * rho);
+    cs->c2[k] = (float)(2.0 * rho1 / de);
+    rho = rho1;
+  }
+  cs->ready = true;
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t coarse_apply(const CoarseSolver& cs, const T* r, const int* skip, cudaStream_t s) {
+  const CoarseDev& c = cs.dev;
+  const unsigned g = blocks_for(c.nV);
+  coarse_restrict<T><<<g, kT, 0, s>>>(c, r, skip);
+  float *dk = c.cd0, *dn = c.cd1;
+  for (int k = 0; k < cs.degree; ++k) {
+    coarse_cheb_step<<<g, kT, 0, s>>>(c, dk, dn, cs.c1[k], cs.c2[k], k + 1 == cs.degree, skip);
+    std::swap(dk, dn);
+  }
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t coarse_prolong_add(const CoarseSolver& cs, T* x, cudaStream_t s) {
+  coarse_prolong<T><<<blocks_for(cs.dev.nFaces * cs.dev.NF), kT, 0, s>>>(cs.dev, x);
+  return cudaGetLastError();
+}
+
+template cudaError_t coarse_setup<double>(CoarseSolver*, const double*, int, double, cudaStream_t);
+template cudaError_t coarse_setup<float>(CoarseSolver*, const float*, int, double, cudaStream_t);
+template cudaError_t coarse_apply<double>(const CoarseSolver&, const double*, const int*, cudaStream_t);
+template cudaError_t coarse_apply<float>(const CoarseSolver&, const float*, const int*, cudaStream_t);
+template cudaError_t coarse_prolong_add<double>(const CoarseSolver&, double*, cudaStream_t);
+template cudaError_t coarse_prolong_add<float>(const CoarseSolver&, float*, cudaStream_t);
+
+}  // namespace hfx

@@ -26,6 +26,7 @@
 // broken down) every later kernel returns at entry, so the host may queue
 // many iterations between checks.
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 #include <cstdio>
 #include <vector>
@@ -242,6 +243,92 @@ __global__ void __launch_bounds__(kThreads) cg_update(int64_t nFaces, T* __restr
         st->status = 5;  // HFX_ERR_NOT_CONVERGED
         st->done = 1;
       }
+    }
+  }
+}
+
+// K2 of CG with the two-level preconditioner, first half: x += alpha p,
+// r -= alpha q, ||r||^2 and the convergence test. z follows in tl_apply once the
+// coarse solve of the new residual is done.
+template <typename T, int NF>
+__global__ void __launch_bounds__(kThreads) cg_update_r(int64_t nFaces, T* __restrict__ x, T* __restrict__ r,
+                                                        const T* __restrict__ p, const T* __restrict__ q,
+                                                        CgState* st, double* partials, double tol2) {
+  if (st->done) return;
+  const T alpha = (T)st->alpha;
+  const int64_t n = nFaces * NF;
+  double rr = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kThreads) {
+    x[i] = fma_t<T>(alpha, p[i], x[i]);
+    T ra = fma_t<T>(-alpha, q[i], r[i]);
+    r[i] = ra;
+    rr += (double)ra * (double)ra;
+  }
+  double v[1] = {rr}, tot[1];
+  if (block_reduce_last<1>(v, partials, &st->ticket, tot) && threadIdx.x == 0) {
+    st->iters += 1;
+    st->rr = tot[0];
+    if (!isfinite(tot[0])) {
+      st->status = 7;
+      st->done = 1;
+    } else if (tot[0] <= tol2) {
+      st->done = 1;
+    } else if (st->iters >= st->maxits) {
+      st->status = 5;
+      st->done = 1;
+    }
+  }
+}
+
+// z = B^{-1} r + P yc (face-block Jacobi plus the prolongated coarse solution),
+// r.z; init = 1 stores r.z only (start of CG), else beta = r.z / previous r.z.
+template <typename T, int NF>
+__global__ void __launch_bounds__(kThreads) tl_apply(int64_t nFaces, const T* __restrict__ r, T* __restrict__ z,
+                                                     const T* __restrict__ pc, CoarseDev cd, CgState* st,
+                                                     double* partials, int init) {
+  constexpr int FPW = 32 / NF;
+  __shared__ T rsh[kThreads / 32][FPW][NF];
+  if (st->done) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int slot = lane / NF, a = lane % NF;
+  const bool laneUsed = slot < FPW;
+  const int64_t stride = (int64_t)gridDim.x * (kThreads / 32) * FPW;
+  const int d = cd.dim;
+  double rz = 0.0;
+  for (int64_t fb = ((int64_t)blockIdx.x * (kThreads / 32) + warp) * FPW; fb < nFaces; fb += stride) {
+    const int64_t f = fb + slot;
+    const bool act = laneUsed && f < nFaces;
+    T ra = T(0);
+    if (act) {
+      ra = r[f * NF + a];
+      rsh[warp][slot][a] = ra;
+    }
+    __syncwarp();
+    if (act) {
+      T zi = T(0);
+      const T* B = pc + f * NF * NF + a;
+#pragma unroll
+      for (int b = 0; b < NF; ++b) zi = fma_t<T>(B[b * NF], rsh[warp][slot][b], zi);
+      if (!cd.isBnd[f]) {
+        float s = 0.f;
+        for (int k = 0; k < d; ++k) s = fmaf(cd.Wf[a * d + k], cd.yc[cd.faceV[f * d + k]], s);
+        zi += (T)s;
+      }
+      z[f * NF + a] = zi;
+      rz += (double)ra * (double)zi;
+    }
+    __syncwarp();
+  }
+  double v[1] = {rz}, tot[1];
+  if (block_reduce_last<1>(v, partials, &st->ticket, tot) && threadIdx.x == 0) {
+    if (!isfinite(tot[0])) {
+      st->status = 7;
+      st->done = 1;
+    } else if (init) {
+      st->rz = tot[0];
+    } else {
+      st->beta = tot[0] / st->rz;
+      st->rz = tot[0];
     }
   }
 }
@@ -601,7 +688,9 @@ struct Driver {
     cudaStream_t s = a.stream;
     const TraceView& A = a.A;
     const int64_t n = (int64_t)A.nFaces * NF;
-    const int pcT = a.precond;  // 0 none, 1 Jacobi, 2 block Jacobi
+    // 0 none, 1 Jacobi, 2 block Jacobi, 3 two-level (block Jacobi + coarse space)
+    const bool twoLevel = a.precond == 3 && a.coarse && a.coarse->ready;
+    const int pcT = a.precond == 3 ? 2 : a.precond;  // the block-Jacobi part
     auto fail = [&](cudaError_t e) {
       out->cudaErr = e;
       return 3;
@@ -611,10 +700,22 @@ struct Driver {
     const int gridF32 = grid_of(cg_spmv<float, NF, NBMAX, false>, kThreads);
     const int gridU = grid_of(cg_update<double, NF, 2>, kThreads);
     const int gridS = grid_of(prepare_system<NF, NBMAX>, kThreads);
+    const int gridR1 = grid_of(cg_update_r<double, NF>, kThreads);
+    const int gridT = grid_of(tl_apply<double, NF>, kThreads);
     double* partials = a.ws.partials;
     CgState* st = a.ws.state;
     CgState hst;
     KernelTimer* tm = a.timer;
+    // two-level second half of K2 (coarse solve of r, then z and r.z)
+    auto coarse_z = [&](auto* rv, auto* zv, const auto* pcv, int init) {
+      using T = std::remove_cv_t<std::remove_pointer_t<decltype(rv)>>;
+      tm->begin(K_COARSE, s);
+      coarse_apply<T>(*a.coarse, rv, &st->done, s);
+      tm->end(K_COARSE, s);
+      tm->begin(K_UPDATE, s);
+      tl_apply<T, NF><<<gridT, kThreads, 0, s>>>(A.nFaces, rv, zv, pcv, a.coarse->dev, st, partials, init);
+      tm->end(K_UPDATE, s);
+    };
     // 1. system b', FP32 values if needed, preconditioner
     tm->begin(K_OTHER, s);
     prepare_system<NF, NBMAX><<<gridS, kThreads, 0, s>>>(A, a.val, a.rhs, a.ws.bS,
@@ -644,6 +745,18 @@ struct Driver {
       tm->begin(K_OTHER, s);
       launch_start(A, a, x, st, partials, pcT, gridF, s);
       tm->end(K_OTHER, s);
+      if (twoLevel && a.coarse_guess && !a.use_initial_guess) {
+        // initial guess: x0 = [P q(A_c) P^T b'; g], then the residual again
+        tm->begin(K_COARSE, s);
+        coarse_apply<double>(*a.coarse, a.ws.r, nullptr, s);
+        coarse_prolong_add<double>(*a.coarse, x, s);
+        tm->end(K_COARSE, s);
+        if ((err = reset_state(a.maxits)) != cudaSuccess) return fail(err);
+        tm->begin(K_OTHER, s);
+        launch_start(A, a, x, st, partials, pcT, gridF, s);
+        tm->end(K_OTHER, s);
+      }
+      if (twoLevel) coarse_z(a.ws.r, a.ws.z, (const double*)a.ws.pc64, 1);
       if ((err = cudaMemcpyAsync(&hst, st, sizeof(CgState), cudaMemcpyDeviceToHost, s)) != cudaSuccess) return fail(err);
       cudaStreamSynchronize(s);
       double tol2 = a.rtol * a.rtol * hst.bb;
@@ -659,10 +772,17 @@ struct Driver {
             tm->begin(K_SPMV64, s);
             cg_spmv<double, NF, NBMAX, true><<<gridF, kThreads, 0, s>>>(A, a.val, z, pold, pnew, q, st, partials, it == 0);
             tm->end(K_SPMV64, s);
-            tm->begin(K_UPDATE, s);
-            launch_update<double>(A.nFaces, x, r, z, pnew, q, pcT == 2 ? a.ws.pc64 : (pcT == 1 ? a.ws.pc64 : nullptr),
-                                  st, partials, tol2, pcT, gridU, s);
-            tm->end(K_UPDATE, s);
+            if (twoLevel) {
+              tm->begin(K_UPDATE, s);
+              cg_update_r<double, NF><<<gridR1, kThreads, 0, s>>>(A.nFaces, x, r, pnew, q, st, partials, tol2);
+              tm->end(K_UPDATE, s);
+              coarse_z(r, z, (const double*)a.ws.pc64, 0);
+            } else {
+              tm->begin(K_UPDATE, s);
+              launch_update<double>(A.nFaces, x, r, z, pnew, q, pcT >= 1 ? a.ws.pc64 : nullptr, st, partials, tol2,
+                                    pcT, gridU, s);
+              tm->end(K_UPDATE, s);
+            }
           }
           if ((err = cudaGetLastError()) != cudaSuccess) return fail(err);
           cudaMemcpyAsync(&hst, st, sizeof(CgState), cudaMemcpyDeviceToHost, s);
@@ -694,11 +814,20 @@ struct Driver {
           default: cg_replace<NF, NBMAX, 2><<<gridR, kThreads, 0, s>>>(A, a.val, a.ws.bS, a.rhs, x, r32, z32, a.ws.pc32, st, partials); break;
         }
         tm->end(K_OTHER, s);
+        if (twoLevel) coarse_z(r32, z32, (const float*)a.ws.pc32, 1);
         cudaMemcpyAsync(&hst, st, sizeof(CgState), cudaMemcpyDeviceToHost, s);
         return cudaStreamSynchronize(s);
       };
       if ((err = reset_state(a.maxits)) != cudaSuccess) return fail(err);
       if ((err = replace()) != cudaSuccess) return fail(err);
+      if (twoLevel && a.coarse_guess && !a.use_initial_guess) {
+        tm->begin(K_COARSE, s);
+        coarse_apply<float>(*a.coarse, r32, nullptr, s);
+        coarse_prolong_add<double>(*a.coarse, x, s);
+        tm->end(K_COARSE, s);
+        if ((err = reset_state(a.maxits)) != cudaSuccess) return fail(err);
+        if ((err = replace()) != cudaSuccess) return fail(err);
+      }
       const double tol2 = a.rtol * a.rtol * hst.bb;
       double lastR2 = hst.rr;
       bool first = true;
@@ -730,9 +859,16 @@ struct Driver {
                                                                           partials, first ? 1 : 0);
             tm->end(K_SPMV32, s);
             first = false;
-            tm->begin(K_UPDATE, s);
-            launch_update<float>(A.nFaces, y32, r32, z32, pnew, q32, a.ws.pc32, st, partials, stretch2, pcT, gridU, s);
-            tm->end(K_UPDATE, s);
+            if (twoLevel) {
+              tm->begin(K_UPDATE, s);
+              cg_update_r<float, NF><<<gridR1, kThreads, 0, s>>>(A.nFaces, y32, r32, pnew, q32, st, partials, stretch2);
+              tm->end(K_UPDATE, s);
+              coarse_z(r32, z32, (const float*)a.ws.pc32, 0);
+            } else {
+              tm->begin(K_UPDATE, s);
+              launch_update<float>(A.nFaces, y32, r32, z32, pnew, q32, a.ws.pc32, st, partials, stretch2, pcT, gridU, s);
+              tm->end(K_UPDATE, s);
+            }
           }
           if ((err = cudaGetLastError()) != cudaSuccess) return fail(err);
           cudaMemcpyAsync(&hst, st, sizeof(CgState), cudaMemcpyDeviceToHost, s);

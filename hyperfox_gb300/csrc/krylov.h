@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 
+#include "coarse.h"
 #include "timer.h"
 
 namespace hfx {
@@ -44,7 +45,7 @@ struct TraceSolveArgs {
   const double* val;  // reference values (scalar-CSR order)
   const double* rhs;  // reference right-hand side
   double* x;          // solution (in: initial guess if use_initial_guess)
-  int precond;        // 0 none, 1 Jacobi, 2 block Jacobi
+  int precond;        // 0 none, 1 Jacobi, 2 block Jacobi, 3 two-level (block Jacobi + vertex coarse space)
   int mixed;          // FP32 inner CG inside FP64 refinement
   double rtol, inner_rtol;
   int maxits, max_refinements, check_every, use_initial_guess;
@@ -52,6 +53,8 @@ struct TraceSolveArgs {
   TraceWorkspace ws;
   cudaStream_t stream;
   KernelTimer* timer;
+  const CoarseSolver* coarse;  // set up for precond 3
+  int coarse_guess;            // start from the prolongated coarse solution of b'
 };
 
 struct TraceSolveResult {

@@ -305,6 +305,8 @@ extern "C" int hfx_trace_solve_noalloc(int dim, int nodesPerFace, int nFaces, co
       info->refinements = 0;
       info->rel_residual = 0.0;
       info->solve_ms = 0.0;
+      info->fallback = 0;
+      info->coarse_degree = 0;
     }
     return code;
   };
@@ -370,6 +372,8 @@ extern "C" int hfx_trace_solve_noalloc(int dim, int nodesPerFace, int nFaces, co
     info->refinements = 0;
     info->rel_residual = h.bb > 0 ? std::sqrt(h.res_rr / h.bb) : std::sqrt(h.res_rr);
     info->solve_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    info->fallback = 0;
+    info->coarse_degree = 0;
   }
   return h.status;
 }

@@ -15,7 +15,8 @@ enum KernelId {
   K_RECOVER = 5,    // local recovery
   K_OTHER = 6,      // setup kernels of the solve (system prep, preconditioner, residuals)
   K_RESIDUAL = 7,   // FP64 matrix-free residual of the full HDG system (mixed precision)
-  K_COUNT = 8
+  K_COARSE = 8,     // two-level preconditioner: restriction, Chebyshev coarse solve, coarse setup
+  K_COUNT = 9
 };
 
 class KernelTimer {

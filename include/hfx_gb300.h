@@ -51,6 +51,8 @@ extern "C" {
 #define HFX_PC_NONE 0
 #define HFX_PC_JACOBI 1
 #define HFX_PC_BLOCK_JACOBI 2 /* one dense block per face (HDG trace systems) */
+#define HFX_PC_TWOLEVEL 3     /* block Jacobi + coarse correction on the mesh vertices (CG only;
+                                 no counterpart in the reference, see hfx_solve) */
 #define HFX_PREC_FP64 0
 #define HFX_PREC_MIXED 1    /* FP32 inner Krylov inside FP64 iterative refinement */
 
@@ -74,6 +76,7 @@ typedef struct {
   int restart;           /* GMRES restart length (PETSc default 30) */
   double inner_rtol;     /* mixed precision: inner FP32 reduction per refinement step */
   int use_initial_guess; /* start from the trace already on the device */
+  int coarse_guess;      /* HFX_PC_TWOLEVEL: start from the prolongated coarse solution */
 } hfx_solve_opts;
 
 typedef struct {
@@ -82,6 +85,8 @@ typedef struct {
   int refinements;         /* FP64 refinement steps (mixed precision) */
   double rel_residual;     /* final FP64 ||b-Ax||/||b|| of the reference system */
   double solve_ms;         /* device time of the solve */
+  int fallback;            /* 1: the two-level solve failed and block Jacobi finished it */
+  int coarse_degree;       /* HFX_PC_TWOLEVEL: Chebyshev degree of the coarse solve */
 } hfx_solve_info;
 
 /* ---- context ------------------------------------------------------------ */
@@ -164,6 +169,14 @@ void hfx_solve_opts_default(hfx_solve_opts* opts);
 int hfx_solve(hfx_ctx* ctx, const hfx_solve_opts* opts, double* trace, hfx_solve_info* info);
 int hfx_recover(hfx_ctx* ctx, double* solution, double* flux);
 
+/* Coarse operator of HFX_PC_TWOLEVEL (no counterpart in the reference): one
+ * coarse DOF per mesh vertex (vertexNode[nV] = mesh node id), prolongation
+ * P[f*Nf + a, v] = barycentric coordinate of face node a w.r.t. face vertex v
+ * (rows of Dirichlet faces zero), A_c = P^T A' P with A' the sign-flipped
+ * interior block of the trace system, in CSR (rowptr[nV+1], col/val[nnz],
+ * FP32). Call with rowptr == NULL for the sizes. Needs an assembled system. */
+int hfx_coarse_operator(hfx_ctx* ctx, int* nV, int64_t* nnz, int* rowptr, int* col, float* val, int* vertexNode);
+
 /* ---- timing on the context's stream (CUDA events; no profiler) ---------------
  * hfx_profile_enable(ctx, 1) resets and starts per-kernel event timing;
  * hfx_kernel_time reads launches and total device ms of one kernel class
@@ -179,6 +192,7 @@ int hfx_recover(hfx_ctx* ctx, double* solution, double* flux);
 #define HFX_K_RECOVER 5
 #define HFX_K_OTHER 6
 #define HFX_K_RESIDUAL 7
+#define HFX_K_COARSE 8
 int hfx_profile_enable(hfx_ctx* ctx, int on);
 int hfx_kernel_time(hfx_ctx* ctx, int kernel, int* launches, double* ms);
 int hfx_mark(hfx_ctx* ctx, int slot);

@@ -1,0 +1,122 @@
+"""Two-level trace preconditioner (block Jacobi + vertex coarse space), through the C ABI.
+
+The coarse operator is checked against the Galerkin product P^T A' P formed here
+from the oracle's trace CSR and a prolongation built independently from the face
+geometry (barycentric coordinates of every face node w.r.t. its face's vertices);
+FP32 coarse values, so the bar is 1e-5 of the largest entry. Solves with the
+two-level preconditioner must match the oracle's direct solve like every other
+solve (1e-8 relative L2) and need fewer iterations than block Jacobi.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from test_gpu_parity import build_pair, relerr
+
+pytestmark = pytest.mark.gpu
+
+
+def galerkin_coarse(P, coords, rowptr, col, val, vertex_node):
+    """P^T A' P with A' = -A on interior rows/cols (Dirichlet rows/cols dropped)."""
+    dim = coords.shape[1]
+    nF, Nf = P.faces.shape
+    A = sp.csr_matrix((val, col, rowptr), shape=(nF * Nf, nF * Nf))
+    bnd = np.zeros(nF, bool)
+    bnd[P.boundary] = True
+    interior = np.repeat(~bnd, Nf)
+    V = coords[P.faces[:, :dim]]                     # [nF, dim, dim] face vertices
+    X = coords[P.faces]                              # [nF, Nf, dim] face nodes
+    E = np.stack([V[:, k] - V[:, 0] for k in range(1, dim)], axis=-1)   # [nF, dim, dim-1]
+    lam = np.einsum("fij,fnj->fni", np.linalg.pinv(E), X - V[:, None, 0])
+    bary = np.concatenate([1 - lam.sum(-1, keepdims=True), lam], axis=-1)  # [nF, Nf, dim]
+    cid = -np.ones(coords.shape[0], int)
+    cid[vertex_node] = np.arange(len(vertex_node))
+    fv = cid[P.faces[:, :dim]]
+    assert (fv >= 0).all()
+    rows = np.repeat(np.arange(nF * Nf), dim)
+    cols = np.broadcast_to(fv[:, None, :], (nF, Nf, dim)).reshape(-1)
+    w = (bary * interior.reshape(nF, Nf, 1)).reshape(-1)
+    Pm = sp.csr_matrix((w, (rows, cols)), shape=(nF * Nf, len(vertex_node)))
+    Ai = sp.diags(interior.astype(float)) @ A @ sp.diags(interior.astype(float))
+    return (Pm.T @ (-Ai) @ Pm).toarray()
+
+
+@pytest.mark.parametrize("dim,n,order,tau2", [(2, 5, 2, True), (2, 3, 4, False), (3, 2, 2, True), (3, 2, 3, False)])
+def test_coarse_operator_is_galerkin_product(hfx_lib, dim, n, order, tau2):
+    P, ctx, (coords, cells) = build_pair(hfx_lib, dim, n, order, tau2=tau2, kappa="cell")
+    P.assemble()
+    ctx.assemble()
+    rowptr, col, val, vn = ctx.coarse_operator()
+    nV = len(vn)
+    # one coarse DOF per distinct cell vertex
+    assert sorted(vn) == sorted(np.unique(cells[:, :dim + 1]))
+    G = np.zeros((nV, nV))
+    for v in range(nV):
+        G[v, col[rowptr[v]:rowptr[v + 1]]] = val[rowptr[v]:rowptr[v + 1]]
+    orow, ocol, oval, _ = P.csr()
+    R = galerkin_coarse(P, coords, orow, ocol, oval, vn)
+    assert np.abs(G - R).max() <= 1e-5 * np.abs(R).max()
+    assert np.allclose(G, G.T, atol=1e-5 * np.abs(R).max())
+    # the pattern holds every non-zero of the product
+    mask = np.zeros((nV, nV), bool)
+    for v in range(nV):
+        mask[v, col[rowptr[v]:rowptr[v + 1]]] = True
+    assert np.abs(R[~mask]).max(initial=0.0) <= 1e-12 * np.abs(R).max()
+
+
+@pytest.mark.parametrize("dim,n,order", [(2, 8, 2), (2, 6, 3), (3, 3, 2), (3, 2, 3)])
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("coarse_guess", [0, 1])
+def test_twolevel_solve_matches_direct(hfx_lib, dim, n, order, precision, coarse_guess):
+    from hyperfox_gb300 import capi
+    P, ctx, _ = build_pair(hfx_lib, dim, n, order, tau2=True, kappa="cell")
+    P.assemble()
+    ctx.assemble()
+    x_ref = P.solve_direct()
+    trace, info = ctx.solve(precision=precision, rtol=1e-13, precond=capi.PC_TWOLEVEL, coarse_guess=coarse_guess)
+    assert info.status == 0 and info.fallback == 0
+    assert info.coarse_degree >= 1
+    assert np.linalg.norm(trace - x_ref) / np.linalg.norm(x_ref) < 1e-8
+    assert info.rel_residual < 1e-12
+    sol, flux = ctx.recover()
+    osol, oflux = P.recover(trace)
+    assert relerr(sol, osol) < 1e-12
+    assert relerr(flux, oflux) < 1e-12
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_twolevel_needs_fewer_iterations(hfx_lib, precision):
+    from hyperfox_gb300 import capi
+    P, ctx, _ = build_pair(hfx_lib, 3, 8, 2, tau2=False, kappa="none", jitter=0.0)
+    ctx.assemble()
+    _, bj = ctx.solve(precision=precision, rtol=1e-10, precond=capi.PC_BLOCK_JACOBI)
+    _, tl = ctx.solve(precision=precision, rtol=1e-10, precond=capi.PC_TWOLEVEL)
+    assert bj.status == 0 and tl.status == 0
+    assert tl.iterations < 0.6 * bj.iterations, (tl.iterations, bj.iterations)
+
+
+def test_twolevel_refused_for_gmres_and_mixed_assembly(hfx_lib):
+    from hyperfox_gb300 import capi
+    P, ctx, _ = build_pair(hfx_lib, 2, 4, 2, tau2=False, kappa="cell")
+    ctx.assemble()
+    with pytest.raises(capi.HfxError) as ei:
+        ctx.solve(method=capi.KSP_GMRES, precond=capi.PC_TWOLEVEL)
+    assert ei.value.code == capi.HFX_ERR_UNSUPPORTED
+    ctx.assemble(capi.PREC_MIXED)
+    with pytest.raises(capi.HfxError) as ei:
+        ctx.solve(precond=capi.PC_TWOLEVEL)
+    assert ei.value.code == capi.HFX_ERR_UNSUPPORTED
+
+
+def test_twolevel_falls_back_to_block_jacobi(hfx_lib):
+    """A two-level solve that stops short (maxits) hands over to block Jacobi and says so."""
+    from hyperfox_gb300 import capi
+    P, ctx, _ = build_pair(hfx_lib, 2, 6, 2, tau2=False, kappa="cell")
+    ctx.assemble()
+    o = capi.solve_opts(precond=capi.PC_TWOLEVEL, rtol=1e-12, maxits=2)
+    info = capi.SolveInfo()
+    rc = ctx.L.hfx_solve(ctx.h, ctypes.byref(o), None, ctypes.byref(info))
+    assert rc == capi.HFX_ERR_NOT_CONVERGED
+    assert info.fallback == 1
