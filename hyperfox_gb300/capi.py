@@ -34,7 +34,7 @@ EXPORTED = [
     "hfx_refel_query", "hfx_refel_tables",
     "hfx_mesh_upload", "hfx_mesh_sizes", "hfx_mesh_topology", "hfx_mesh_compute_topology",
     "hfx_set_tau", "hfx_set_kappa", "hfx_set_source", "hfx_set_dirichlet", "hfx_set_time_scheme",
-    "hfx_ip_coords", "hfx_assemble", "hfx_assemble_ex", "hfx_get_condensed", "hfx_get_csr",
+    "hfx_ip_coords", "hfx_assemble", "hfx_assemble_ex", "hfx_set_assembly_path", "hfx_assembly_info", "hfx_get_condensed", "hfx_get_csr",
     "hfx_solve_opts_default", "hfx_solve", "hfx_recover", "hfx_coarse_operator",
     "hfx_la_create", "hfx_la_destroy", "hfx_la_allocate", "hfx_la_set_values", "hfx_la_set_rhs",
     "hfx_la_zero_rows", "hfx_la_assemble", "hfx_la_clear", "hfx_la_solve", "hfx_la_nnz",
@@ -105,6 +105,8 @@ def load(path=LIB_PATH):
         "hfx_solve": ([vp, ctypes.POINTER(SolveOpts), vp, ctypes.POINTER(SolveInfo)], ip),
         "hfx_recover": ([vp, vp, vp], ip),
         "hfx_coarse_operator": ([vp, vp, vp, vp, vp, vp, vp], ip),
+        "hfx_set_assembly_path": ([vp, ip], ip),
+        "hfx_assembly_info": ([vp, vp], ip),
         "hfx_la_create": ([vp, ctypes.POINTER(vp)], ip),
         "hfx_la_destroy": ([vp], ip),
         "hfx_la_allocate": ([vp, ip], ip),

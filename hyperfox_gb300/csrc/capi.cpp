@@ -94,6 +94,15 @@ struct hfx_ctx {
   int srcMode = 0;
   double srcParam = 0.0;
   double dt = 0.0;
+  // affine element path (hdg_affine.cu): straight-sided cells and a symmetric
+  // diffusion tensor constant inside every cell
+  bool affineMesh = false;
+  bool kappaSymmetric = true;
+  int assemblyPath = 0;        // 0 automatic, 1 quadrature kernel always
+  bool lastAffine = false;     // the last FP64 assembly used the affine kernel
+  bool qValid = false;         // d_Q / d_Q0 hold the current Q, Q0
+  double* d_atab = nullptr;    // affine reference operators
+  double* d_geo = nullptr;     // [nCells][D*D + F*D]
   // outputs
   DevMem outMem;
   double *d_S = nullptr, *d_S0 = nullptr, *d_U = nullptr, *d_Q = nullptr, *d_U0 = nullptr, *d_Q0 = nullptr;
@@ -171,7 +180,8 @@ void free_outputs(hfx_ctx* c) {
   c->outMem.release();
   c->wsMem.release();
   c->d_S = c->d_S0 = c->d_U = c->d_Q = c->d_U0 = c->d_Q0 = c->d_val = c->d_rhs = c->d_trace = nullptr;
-  c->d_sol = c->d_flux = nullptr;
+  c->d_sol = c->d_flux = c->d_geo = nullptr;
+  c->qValid = c->lastAffine = false;
   c->mixMem.release();
   c->d_S32 = c->d_S032 = c->d_U32 = c->d_Q32 = c->d_U032 = c->d_Q032 = c->d_dl32 = nullptr;
   c->d_ru = c->d_rq = c->d_rl = c->d_rtrace = c->d_part = nullptr;
@@ -182,6 +192,47 @@ void free_outputs(hfx_ctx* c) {
   c->wsRestart = 0;
   c->ws = TraceWorkspace{};
   c->assembled = c->solved = false;
+}
+
+// True when every cell's nodes are the affine image of the reference nodes
+// (straight-sided simplices): node i sits at sum_m lambda_m(ref node i) x_m,
+// x_m the cell's vertices, within 1e-12 of the cell's size.
+bool cells_affine(const RefEl& re, int nCells, const int* cells, const double* coords) {
+  const int d = re.dim, N = re.nNodes;
+  std::vector<double> lam((size_t)N * (d + 1));
+  for (int i = 0; i < N; ++i) {
+    // reference vertices are nodes 0..d: solve sum_m l_m V_m = x, sum_m l_m = 1
+    double A[4][5];
+    for (int r = 0; r <= d; ++r) {
+      for (int m = 0; m <= d; ++m) A[r][m] = r < d ? re.nodes[m * d + r] : 1.0;
+      A[r][d + 1] = r < d ? re.nodes[i * d + r] : 1.0;
+    }
+    for (int k = 0; k <= d; ++k) {
+      int piv = k;
+      for (int r = k + 1; r <= d; ++r)
+        if (std::fabs(A[r][k]) > std::fabs(A[piv][k])) piv = r;
+      for (int j = 0; j <= d + 1; ++j) std::swap(A[k][j], A[piv][j]);
+      for (int r = 0; r <= d; ++r) {
+        if (r == k) continue;
+        double l = A[r][k] / A[k][k];
+        for (int j = k; j <= d + 1; ++j) A[r][j] -= l * A[k][j];
+      }
+    }
+    for (int m = 0; m <= d; ++m) lam[(size_t)i * (d + 1) + m] = A[m][d + 1] / A[m][m];
+  }
+  for (int64_t e = 0; e < nCells; ++e) {
+    const int* cn = cells + e * N;
+    double h = 0.0;
+    for (int m = 1; m <= d; ++m)
+      for (int k = 0; k < d; ++k) h = std::max(h, std::fabs(coords[(int64_t)cn[m] * d + k] - coords[(int64_t)cn[0] * d + k]));
+    for (int i = d + 1; i < N; ++i)
+      for (int k = 0; k < d; ++k) {
+        double x = 0.0;
+        for (int m = 0; m <= d; ++m) x += lam[(size_t)i * (d + 1) + m] * coords[(int64_t)cn[m] * d + k];
+        if (std::fabs(x - coords[(int64_t)cn[i] * d + k]) > 1e-12 * h) return false;
+      }
+  }
+  return true;
 }
 
 }  // namespace
@@ -339,6 +390,12 @@ int hfx_mesh_upload(hfx_ctx* c, int dim, int order, int nNodes, const double* co
   HFX_CUDA(c, upload(m, &c->d_loc0, c->bp.loc0.data(), c->bp.loc0.size(), s));
   HFX_CUDA(c, upload(m, &c->d_loc1, c->bp.loc1.data(), c->bp.loc1.size(), s));
   HFX_CUDA(c, dalloc(m, &c->d_brow, c->bp.col.size()));
+  {
+    std::vector<double> atab;
+    c->d_atab = nullptr;
+    if (affine_tables(c->re, &atab)) HFX_CUDA(c, upload(m, &c->d_atab, atab.data(), atab.size(), s));
+    c->affineMesh = c->d_atab != nullptr && cells_affine(c->re, nCells, cells, coords);
+  }
   HFX_CUDA(c, launch_block_rows(c->d_browptr, c->topo.nFaces, c->d_brow, s));
   // default fields: tau = 1, Dirichlet = 0, kappa = identity, no source
   std::vector<double> ones((size_t)c->topo.nFaces * Nf, 1.0), zeros((size_t)c->topo.nFaces * Nf, 0.0);
@@ -409,6 +466,7 @@ int hfx_set_kappa(hfx_ctx* c, const double* kappa, int comps, int layout) {
   if (comps == 0) {
     c->kc = 0;
     c->kappaCellConstant = true;
+    c->kappaSymmetric = true;
     c->assembled = false;
     return HFX_OK;
   }
@@ -435,7 +493,19 @@ int hfx_set_kappa(hfx_ctx* c, const double* kappa, int comps, int layout) {
           double b = layout == 0 ? kappa[(int64_t)cells[e * N + i] * comps + k] : kappa[(e * N + i) * comps + k];
           if (a != b) cst = false;
         }
-    c->kappaCellConstant = cst;
+    bool sym = true;  // a dim x dim tensor must be symmetric for the affine kernel and for CG
+    if (comps == c->dim * c->dim) {
+      const int d = c->dim;
+      const int64_t nv = layout == 0 ? (int64_t)c->nNodes : (int64_t)c->nCells * N;
+      for (int64_t v = 0; v < nv && sym; ++v)
+        for (int a = 0; a < d && sym; ++a)
+          for (int b = a + 1; b < d && sym; ++b) {
+            double x = kappa[v * comps + a + b * d], y = kappa[v * comps + b + a * d];
+            if (std::fabs(x - y) > 1e-14 * (std::fabs(x) + std::fabs(y))) sym = false;
+          }
+    }
+    c->kappaSymmetric = sym;
+    c->kappaCellConstant = cst && sym;  // the trace system is symmetric only then
   }
   size_t n = (layout == 0 ? (size_t)c->nNodes : (size_t)c->nCells * c->re.nNodes) * comps;
   return replace_field(c, &c->kappa, kappa, n);
@@ -503,6 +573,7 @@ static int ensure_outputs(hfx_ctx* c) {
   HFX_CUDA(c, dalloc(m, &c->d_status, 1));
   HFX_CUDA(c, dalloc(m, &c->d_sol, (size_t)E * LU));
   HFX_CUDA(c, dalloc(m, &c->d_flux, (size_t)E * LQ));
+  HFX_CUDA(c, dalloc(m, &c->d_geo, (size_t)E * (c->dim * c->dim + c->re.nFaces * c->dim)));
   HFX_CUDA(c, cudaMemsetAsync(c->d_trace, 0, sizeof(double) * c->ndofs(), c->stream));
   return HFX_OK;
 }
@@ -543,9 +614,13 @@ static int assemble_fp64(hfx_ctx* c) {
   p.fp32 = 0;
   p.rhsU = p.rhsQ = nullptr;
   p.writeOps = 1;
+  const bool affine = c->assemblyPath == 0 && c->affineMesh && c->kappaCellConstant && c->d_atab;
   c->timer.begin(K_LOCAL, s);
-  HFX_CUDA(c, launch_local_condense(c->dim, c->order, p, s));
+  if (affine) HFX_CUDA(c, launch_local_affine(c->dim, c->order, p, c->d_atab, c->d_geo, s));
+  else HFX_CUDA(c, launch_local_condense(c->dim, c->order, p, s));
   c->timer.end(K_LOCAL, s);
+  c->lastAffine = affine;
+  c->qValid = !affine;
   ScatterParams sp{};
   sp.nFaces = c->topo.nFaces;
   sp.NF = c->re.nNodesFace;
@@ -745,6 +820,20 @@ int hfx_assemble_ex(hfx_ctx* c, int precision) {
 
 int hfx_assemble(hfx_ctx* c) { return hfx_assemble_ex(c, HFX_PREC_FP64); }
 
+int hfx_set_assembly_path(hfx_ctx* c, int path) {
+  if (!c) return HFX_ERR_ARG;
+  if (path != 0 && path != 1) return set_err(c, HFX_ERR_ARG, "set_assembly_path: 0 (automatic) or 1 (quadrature)");
+  c->assemblyPath = path;
+  c->assembled = false;
+  return HFX_OK;
+}
+
+int hfx_assembly_info(hfx_ctx* c, int* affine) {
+  if (!c || !affine) return HFX_ERR_ARG;
+  *affine = c->lastAffine ? 1 : 0;
+  return HFX_OK;
+}
+
 int hfx_get_condensed(hfx_ctx* c, double* S, double* S0, double* U, double* Q, double* U0, double* Q0) {
   if (!c) return HFX_ERR_ARG;
   if (!c->assembled) return set_err(c, HFX_ERR_STATE, "get_condensed: assemble first");
@@ -755,6 +844,11 @@ int hfx_get_condensed(hfx_ctx* c, double* S, double* S0, double* U, double* Q, d
   auto cp = [&](double* h, const double* d, size_t n) {
     return h ? cudaMemcpyAsync(h, d, sizeof(double) * n, cudaMemcpyDeviceToHost, s) : cudaSuccess;
   };
+  if ((Q || Q0) && !c->qValid) {
+    // the affine path keeps Q, Q0 implicit: form them from U, U0 and the element factors
+    HFX_CUDA(c, launch_q_from_u(c->dim, c->order, c->nCells, c->d_U, c->d_U0, c->d_atab, c->d_geo, c->d_Q, c->d_Q0, s));
+    c->qValid = true;
+  }
   HFX_CUDA(c, cp(S, c->d_S, (size_t)E * LL * LL));
   HFX_CUDA(c, cp(S0, c->d_S0, (size_t)E * LL));
   HFX_CUDA(c, cp(U, c->d_U, (size_t)E * LU * LL));
@@ -1130,7 +1224,8 @@ int hfx_recover(hfx_ctx* c, double* solution, double* flux) {
     RecoverParams p{c->nCells, c->re.nFaces, c->re.nNodesFace, LU, LQ, LL, c->d_cell2face, c->d_perm,
                     c->d_U, c->d_Q, c->d_U0, c->d_Q0, c->d_trace, c->d_sol, c->d_flux};
     c->timer.begin(K_RECOVER, c->stream);
-    HFX_CUDA(c, launch_recover(p, c->stream));
+    if (c->lastAffine) HFX_CUDA(c, launch_recover_affine(c->dim, c->order, p, c->d_atab, c->d_geo, c->stream));
+    else HFX_CUDA(c, launch_recover(p, c->stream));
     c->timer.end(K_RECOVER, c->stream);
   }
   // NULL outputs keep Solution and Flux on the device only

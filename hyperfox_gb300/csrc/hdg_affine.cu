@@ -1,0 +1,664 @@
+// Per-element HDG assembly + static condensation for straight-sided (affine)
+// simplices with a diffusion tensor that is constant and symmetric inside each
+// cell, FP64, sm_103a.
+//
+// Same blocks and the same condensed outputs as hdg_local.cu (which restates
+// HDGBase.cpp:67-158, HDGDiffusion.cpp:74-145, Source.cpp:24-48, Euler.cpp:18-34
+// and the condensation of HDGSolver.cpp:331-348), computed from reference
+// operators instead of quadrature per element. With J the constant Jacobian,
+// G = J^{-1}, K the cell tensor, |F_f| and n_f the face measure and unit outward
+// normal, the reference tables M, C_r (C_r[i][j] = int d_r phi_i phi_j),
+// R_rs = C_r^T M^{-1} C_s, L_f = M^{-1} E_f (E_f the face-mass coupling),
+// P_rf = C_r^T L_f, T_ff' = E_f^T L_f' and T_f[a][b][c] = int_f mu_a mu_b mu_c give
+//   Tm_f = |F_f| sum_c tau_c T_f[.,.,c]                        (tau face mass)
+//   A    = dt (sum_f Tm_f + |J| sum_rs (G^T K G)_sr R_rs) + |J| M [time scheme]
+//   B    = -Tm_f - |F_f| sum_r (n_f^T K G)_r P_rf                (N x LL)
+//   C    = -Tm_f delta_ff' - |F_f||F_f'|/|J| (n_f'^T K n_f) T_ff'
+//   U = -dt A^{-1} B, U0 = A^{-1} f_u, S = C + dt B^T A^{-1} B, S0 = B^T U0
+// (B' = Slu - Slq Xu equals -B^T because K is symmetric: the local system is
+// symmetric after eliminating Q = -Xu U - Xl Lambda). A is symmetric positive
+// definite; with its Cholesky factor L and W = L^{-1} B, S = C + dt W^T W.
+// About 47k FP64 FMAs per p=3 tetrahedron instead of about 0.5M by quadrature.
+//
+// Q and Q0 are not stored: the recovery forms the flux from U and Lambda,
+// Q = -Xu (U Lambda + U0) - Xl Lambda with Xu = G . M^{-1} C and
+// Xl = -(|F_f|/|J|) n_f L_f, from the per-element factors in geo[] =
+// [G (D x D) | (|F_f|/|J|) n_f (F x D)].
+#include <cmath>
+#include <vector>
+
+#include "hfx_device.h"
+#include "hfx_host.h"
+
+namespace hfx {
+
+// ------------------------------------------------------------------ host tables
+
+static bool small_inverse(int n, const std::vector<double>& A, std::vector<double>* inv) {
+  std::vector<double> a(A);
+  inv->assign((size_t)n * n, 0.0);
+  for (int i = 0; i < n; ++i) (*inv)[(size_t)i * n + i] = 1.0;
+  for (int k = 0; k < n; ++k) {
+    int piv = k;
+    for (int i = k + 1; i < n; ++i)
+      if (std::fabs(a[(size_t)i * n + k]) > std::fabs(a[(size_t)piv * n + k])) piv = i;
+    if (a[(size_t)piv * n + k] == 0.0) return false;
+    for (int j = 0; j < n; ++j) {
+      std::swap(a[(size_t)k * n + j], a[(size_t)piv * n + j]);
+      std::swap((*inv)[(size_t)k * n + j], (*inv)[(size_t)piv * n + j]);
+    }
+    double d = 1.0 / a[(size_t)k * n + k];
+    for (int j = 0; j < n; ++j) {
+      a[(size_t)k * n + j] *= d;
+      (*inv)[(size_t)k * n + j] *= d;
+    }
+    for (int i = 0; i < n; ++i) {
+      if (i == k) continue;
+      double l = a[(size_t)i * n + k];
+      if (l == 0.0) continue;
+      for (int j = 0; j < n; ++j) {
+        a[(size_t)i * n + j] -= l * a[(size_t)k * n + j];
+        (*inv)[(size_t)i * n + j] -= l * (*inv)[(size_t)k * n + j];
+      }
+    }
+  }
+  return true;
+}
+
+bool affine_tables(const RefEl& re, std::vector<double>* out) {
+  const int D = re.dim, N = re.nNodes, NF = re.nNodesFace, F = D + 1, NI = re.nIP, NIF = re.nIPFace;
+  const double *phi = re.phi.data(), *dphi = re.dphi.data(), *w = re.ipW.data(), *fphi = re.fPhi.data(),
+               *fw = re.fIpW.data();
+  std::vector<double> M((size_t)N * N, 0.0), Mi;
+  for (int q = 0; q < NI; ++q)
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < N; ++j) M[(size_t)i * N + j] += w[q] * phi[q * N + i] * phi[q * N + j];
+  if (!small_inverse(N, M, &Mi)) return false;
+  std::vector<double> C((size_t)D * N * N, 0.0);  // C[r][i][j] = sum_q w d_r phi_i phi_j
+  for (int q = 0; q < NI; ++q)
+    for (int r = 0; r < D; ++r)
+      for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j)
+          C[((size_t)r * N + i) * N + j] += w[q] * dphi[(q * N + i) * D + r] * phi[q * N + j];
+  std::vector<double> Dr((size_t)D * N * N, 0.0);  // M^{-1} C_r
+  for (int r = 0; r < D; ++r)
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < N; ++j) {
+        double s = 0.0;
+        for (int k = 0; k < N; ++k) s += Mi[(size_t)i * N + k] * C[((size_t)r * N + k) * N + j];
+        Dr[((size_t)r * N + i) * N + j] = s;
+      }
+  std::vector<double> R((size_t)D * D * N * N, 0.0);  // R[r][s][i][j] = sum_m C_r[m][i] Dr_s[m][j]
+  for (int r = 0; r < D; ++r)
+    for (int s = 0; s < D; ++s)
+      for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j) {
+          double v = 0.0;
+          for (int m = 0; m < N; ++m) v += C[((size_t)r * N + m) * N + i] * Dr[((size_t)s * N + m) * N + j];
+          R[(((size_t)r * D + s) * N + i) * N + j] = v;
+        }
+  std::vector<double> Mf((size_t)NF * NF, 0.0), Tf((size_t)NF * NF * NF, 0.0);
+  for (int k = 0; k < NIF; ++k)
+    for (int a = 0; a < NF; ++a)
+      for (int b = 0; b < NF; ++b) {
+        double ab = fw[k] * fphi[k * NF + a] * fphi[k * NF + b];
+        Mf[(size_t)a * NF + b] += ab;
+        for (int c = 0; c < NF; ++c) Tf[((size_t)a * NF + b) * NF + c] += ab * fphi[k * NF + c];
+      }
+  std::vector<double> L((size_t)F * N * NF, 0.0);  // L_f = M^{-1} E_f
+  for (int f = 0; f < F; ++f)
+    for (int i = 0; i < N; ++i)
+      for (int b = 0; b < NF; ++b) {
+        double s = 0.0;
+        for (int a = 0; a < NF; ++a) s += Mi[(size_t)i * N + re.faceNodes[f * NF + a]] * Mf[(size_t)a * NF + b];
+        L[((size_t)f * N + i) * NF + b] = s;
+      }
+  std::vector<double> P((size_t)D * F * N * NF, 0.0);  // P[r][f][i][b] = sum_m C_r[m][i] L_f[m][b]
+  for (int r = 0; r < D; ++r)
+    for (int f = 0; f < F; ++f)
+      for (int i = 0; i < N; ++i)
+        for (int b = 0; b < NF; ++b) {
+          double s = 0.0;
+          for (int m = 0; m < N; ++m) s += C[((size_t)r * N + m) * N + i] * L[((size_t)f * N + m) * NF + b];
+          P[(((size_t)r * F + f) * N + i) * NF + b] = s;
+        }
+  std::vector<double> T((size_t)F * F * NF * NF, 0.0);  // T[f][g][a][b] = sum_a' Mf[a][a'] L_g[fn(f,a')][b]
+  for (int f = 0; f < F; ++f)
+    for (int g = 0; g < F; ++g)
+      for (int a = 0; a < NF; ++a)
+        for (int b = 0; b < NF; ++b) {
+          double s = 0.0;
+          for (int a2 = 0; a2 < NF; ++a2)
+            s += Mf[(size_t)a * NF + a2] * L[((size_t)g * N + re.faceNodes[f * NF + a2]) * NF + b];
+          T[(((size_t)f * F + g) * NF + a) * NF + b] = s;
+        }
+  out->clear();
+  for (auto* v : {&M, &R, &Tf, &P, &T, &Dr, &L}) out->insert(out->end(), v->begin(), v->end());
+  return true;
+}
+
+// ------------------------------------------------------------------ device
+
+namespace {
+
+template <int D, int P>
+struct AffLayout {
+  using K = Dims<D, P>;
+  static constexpr int N = K::N, NF = K::NF, F = K::F, NI = K::NI, NIF = K::NIF, LL = K::LL;
+  // table offsets in the affine table block
+  static constexpr int A_M = 0;
+  static constexpr int A_R = A_M + N * N;
+  static constexpr int A_TF = A_R + D * D * N * N;
+  static constexpr int A_P = A_TF + NF * NF * NF;
+  static constexpr int A_T = A_P + D * F * N * NF;
+  static constexpr int A_D = A_T + F * F * NF * NF;
+  static constexpr int A_L = A_D + D * N * N;
+  static constexpr int A_END = A_L + F * N * NF;
+  // offsets in the packed quadrature table (phi, dphi, w, fphi, fdphi, fw)
+  static constexpr int T_PHI = 0;
+  static constexpr int T_DPHI = T_PHI + NI * N;
+  static constexpr int T_W = T_DPHI + NI * N * D;
+  static constexpr int T_FPHI = T_W + NI;
+  static constexpr int T_FDPHI = T_FPHI + NIF * NF;
+  // per-warp shared region (doubles)
+  static constexpr int LW = LL + 1;              // columns of [B | f_u]
+  static constexpr int X = 0;                    // N*D
+  static constexpr int TAU = X + N * D;          // F*NF
+  static constexpr int KS = TAU + F * NF;        // D*D   cell tensor K[d][b] at d + b*D
+  static constexpr int IV = KS + D * D;          // D*D   G = J^{-1}
+  static constexpr int GAM = IV + D * D;         // D*D   Gamma[r][s]
+  static constexpr int GV = GAM + D * D;         // F*D   (n_f^T K G)_r
+  static constexpr int NRM = GV + F * D;         // F*D   unit normals
+  static constexpr int CFF = NRM + F * D;        // F*F
+  static constexpr int AR = CFF + F * F;         // F     |F_f|
+  static constexpr int SC = AR + F;              // 4     detJ, dts, flags
+  static constexpr int TM = SC + 4;              // F*NF*NF
+  static constexpr int AM = TM + F * NF * NF;    // N*N row-major, then its Cholesky factor
+  static constexpr int BW = AM + N * N;          // N*LW row-major
+  static constexpr int FQ = BW + N * LW;         // NI
+  static constexpr int IDG = FQ + NI;            // N     1 / L[k][k]
+  static constexpr int WARP = (IDG + N + 1) & ~1;
+};
+
+template <int D, int P, int EPC>
+__global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const double* __restrict__ atab,
+                                                         double* __restrict__ geo) {
+  using L = AffLayout<D, P>;
+  constexpr int N = L::N, NF = L::NF, F = L::F, NI = L::NI, LL = L::LL, LW = L::LW;
+  constexpr int DM = D - 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* sm = reinterpret_cast<double*>(smem_raw);
+  __shared__ int sFN[F * NF];
+  __shared__ int sOpp[F];
+  __shared__ int sPos[F * N];
+  for (int i = threadIdx.x; i < F * NF; i += blockDim.x) sFN[i] = p.itab[i];
+  for (int i = threadIdx.x; i < F; i += blockDim.x) sOpp[i] = p.itab[F * NF + i];
+  for (int i = threadIdx.x; i < F * N; i += blockDim.x) sPos[i] = -1;
+  __syncthreads();
+  for (int i = threadIdx.x; i < F * NF; i += blockDim.x) sPos[(i / NF) * N + sFN[i]] = i % NF;
+  __syncthreads();
+
+  const int warp = threadIdx.x >> 5, t = threadIdx.x & 31;
+  double* W = sm + warp * L::WARP;
+  double* X = W + L::X;
+  double* tau = W + L::TAU;
+  double* Ks = W + L::KS;
+  double* iv = W + L::IV;
+  double* gam = W + L::GAM;
+  double* gv = W + L::GV;
+  double* nrm = W + L::NRM;
+  double* cff = W + L::CFF;
+  double* area = W + L::AR;
+  double* sc = W + L::SC;
+  double* Tm = W + L::TM;
+  double* Am = W + L::AM;
+  double* BW = W + L::BW;
+  double* fq = W + L::FQ;
+  double* idg = W + L::IDG;
+  const double* phi = p.tab + L::T_PHI;
+  const double* dphi = p.tab + L::T_DPHI;
+  const double* wq = p.tab + L::T_W;
+  const double* fdphi = p.tab + L::T_FDPHI;
+  const double* tM = atab + L::A_M;
+  const double* tR = atab + L::A_R;
+  const double* tTf = atab + L::A_TF;
+  const double* tP = atab + L::A_P;
+  const double* tT = atab + L::A_T;
+  const double dts = p.dt > 0.0 ? p.dt : 1.0;
+  const int64_t nWarps = (int64_t)gridDim.x * EPC;
+  for (int64_t e = (int64_t)blockIdx.x * EPC + warp; e < p.nCells; e += nWarps) {
+    // ---------------------------------------------------------- gather
+    const int* cell = p.cells + e * N;
+    for (int i = t; i < N * D; i += 32) X[i] = p.coords[(int64_t)cell[i / D] * D + (i % D)];
+    for (int i = t; i < F * NF; i += 32) {
+      int f = p.cell2face[e * F + i / NF];
+      int side = (p.face2cell[2 * (int64_t)f] == (int)e) ? 0 : 1;
+      int q = p.perm[e * F * NF + i];
+      tau[i] = p.tau[((int64_t)f * NF + q) * p.tauVals + (p.tauVals == 2 ? side : 0)];
+    }
+    if (t < D * D) {
+      // cell tensor: the value at the cell's first node (constant inside the cell)
+      const int a = t;
+      double v;
+      if (p.kc == 0) v = (a % (D + 1) == 0) ? 1.0 : 0.0;
+      else {
+        int64_t bk = p.kappaLayout == 0 ? (int64_t)cell[0] * p.kc : (e * N) * p.kc;
+        v = p.kc == 1 ? ((a % (D + 1) == 0) ? p.kappa[bk] : 0.0) : p.kappa[bk + a];
+      }
+      Ks[a] = v;
+    }
+    __syncwarp();
+    // ------------------------------------------------------ geometry
+    if (t == 0) {
+      double J[D][D];
+      for (int r = 0; r < D; ++r)
+        for (int s = 0; s < D; ++s) {
+          double acc = 0.0;
+          for (int i = 0; i < N; ++i) acc += dphi[i * D + r] * X[i * D + s];  // first IP
+          J[r][s] = acc;
+        }
+      double det;
+      if (D == 2) {
+        det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+        double id = 1.0 / det;
+        iv[0] = J[1][1] * id;
+        iv[1] = -J[0][1] * id;
+        iv[2] = -J[1][0] * id;
+        iv[3] = J[0][0] * id;
+      } else {
+        double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+        double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+        double id = 1.0 / det;
+        iv[0 * 3 + 0] = c00 * id;
+        iv[1 * 3 + 0] = c01 * id;
+        iv[2 * 3 + 0] = c02 * id;
+        iv[0 * 3 + 1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+        iv[1 * 3 + 1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+        iv[2 * 3 + 1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+        iv[0 * 3 + 2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+        iv[1 * 3 + 2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+        iv[2 * 3 + 2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+      }
+      sc[0] = det;
+    } else if (t >= 1 && t <= F) {
+      const int f = t - 1;
+      double Jf[D - 1][D];
+      for (int r = 0; r < DM; ++r)
+        for (int s = 0; s < D; ++s) {
+          double acc = 0.0;
+          for (int i = 0; i < NF; ++i) acc += fdphi[i * DM + r] * X[sFN[f * NF + i] * D + s];  // first face IP
+          Jf[r][s] = acc;
+        }
+      double nv[D], ds;
+      if (D == 2) {
+        ds = sqrt(Jf[0][0] * Jf[0][0] + Jf[0][1] * Jf[0][1]);
+        nv[0] = -Jf[0][1];
+        nv[1] = Jf[0][0];
+      } else {
+        double g00 = Jf[0][0] * Jf[0][0] + Jf[0][1] * Jf[0][1] + Jf[0][2] * Jf[0][2];
+        double g11 = Jf[1][0] * Jf[1][0] + Jf[1][1] * Jf[1][1] + Jf[1][2] * Jf[1][2];
+        double g01 = Jf[0][0] * Jf[1][0] + Jf[0][1] * Jf[1][1] + Jf[0][2] * Jf[1][2];
+        ds = sqrt(g00 * g11 - g01 * g01);
+        nv[0] = Jf[0][1] * Jf[1][2] - Jf[0][2] * Jf[1][1];
+        nv[1] = Jf[0][2] * Jf[1][0] - Jf[0][0] * Jf[1][2];
+        nv[2] = Jf[0][0] * Jf[1][1] - Jf[0][1] * Jf[1][0];
+      }
+      double nn = 0.0;
+      for (int a = 0; a < D; ++a) nn += nv[a] * nv[a];
+      nn = 1.0 / sqrt(nn);
+      double prod = 0.0;
+      const int v0 = sFN[f * NF], vn = sOpp[f];
+      for (int a = 0; a < D; ++a) {
+        nv[a] *= nn;
+        prod += (X[vn * D + a] - X[v0 * D + a]) * nv[a];
+      }
+      if (prod > 0)
+        for (int a = 0; a < D; ++a) nv[a] = -nv[a];
+      area[f] = ds;
+      for (int a = 0; a < D; ++a) nrm[f * D + a] = nv[a];
+    }
+    __syncwarp();
+    // derived scalars: Gamma[r][s] = sum_{d,b} K[d][b] G[b][r] G[d][s]; g_f[r] = (n_f^T K G)_r;
+    // c_ff' = |F_f||F_f'|/|J| n_f'^T K n_f
+    const double detJ = sc[0];
+    if (t < D * D) {
+      const int r = t / D, s = t % D;
+      double acc = 0.0;
+      for (int d = 0; d < D; ++d)
+        for (int b = 0; b < D; ++b) acc += Ks[d + b * D] * iv[b * D + r] * iv[d * D + s];
+      gam[t] = acc;
+    } else if (t >= 16 && t < 16 + F * D) {
+      const int f = (t - 16) / D, r = (t - 16) % D;
+      double acc = 0.0;
+      for (int d = 0; d < D; ++d)
+        for (int b = 0; b < D; ++b) acc += nrm[f * D + d] * Ks[d + b * D] * iv[b * D + r];
+      gv[t - 16] = acc;
+    }
+    if (t < F * F) {
+      const int f = t / F, g = t % F;
+      double acc = 0.0;
+      for (int d = 0; d < D; ++d) {
+        double kn = 0.0;
+        for (int b = 0; b < D; ++b) kn += Ks[d + b * D] * nrm[f * D + b];
+        acc += nrm[g * D + d] * kn;
+      }
+      cff[t] = area[f] * area[g] / detJ * acc;
+    }
+    // per-element factors for the recovery of Q
+    if (geo) {
+      double* ge = geo + e * (D * D + F * D);
+      if (t < D * D) ge[t] = iv[t];
+      else if (t < D * D + F * D) {
+        const int k = t - D * D;
+        ge[t] = area[k / D] / detJ * nrm[k];
+      }
+    }
+    // ----------------------------------------------- tau face mass Tm_f
+    for (int idx = t; idx < F * NF * NF; idx += 32) {
+      const int f = idx / (NF * NF), ab = idx % (NF * NF);
+      const double* tf = tTf + ab * NF;
+      double acc = 0.0;
+#pragma unroll
+      for (int c = 0; c < NF; ++c) acc += tau[f * NF + c] * __ldg(tf + c);
+      Tm[idx] = area[f] * acc;
+    }
+    // source at the integration points: f(x_q) dV_q
+    for (int q = t; q < NI; q += 32) {
+      double fval = 0.0;
+      if (p.srcMode == 1) fval = p.src[e * NI + q];
+      else if (p.srcMode == 2) {
+        fval = p.srcParam;
+        for (int k = 0; k < D; ++k) {
+          double xk = 0.0;
+          for (int i = 0; i < N; ++i) xk += phi[q * N + i] * X[i * D + k];
+          fval *= sin(M_PI * xk);
+        }
+      }
+      fq[q] = fval * wq[q] * detJ;
+    }
+    __syncwarp();
+    // ------------------------------------------------- A, B and f_u
+    for (int ij = t; ij < N * N; ij += 32) {
+      const int i = ij / N, j = ij % N;
+      double ts = 0.0;
+      for (int f = 0; f < F; ++f) {
+        const int a = sPos[f * N + i], b = sPos[f * N + j];
+        if (a >= 0 && b >= 0) ts += Tm[(f * NF + a) * NF + b];
+      }
+      double st = 0.0;
+#pragma unroll
+      for (int rs = 0; rs < D * D; ++rs) st += gam[rs] * __ldg(tR + rs * N * N + ij);
+      double v = dts * (ts + detJ * st);
+      if (p.dt > 0.0) v += detJ * __ldg(tM + ij);
+      Am[ij] = v;
+    }
+    for (int ic = t; ic < N * LL; ic += 32) {
+      const int i = ic / LL, c = ic % LL;
+      const int f = c / NF, b = c % NF;
+      double acc = 0.0;
+#pragma unroll
+      for (int r = 0; r < D; ++r) acc += gv[f * D + r] * __ldg(tP + ((r * F + f) * N + i) * NF + b);
+      double v = -area[f] * acc;
+      const int a = sPos[f * N + i];
+      if (a >= 0) v -= Tm[(f * NF + a) * NF + b];
+      BW[i * LW + c] = v;
+    }
+    for (int i = t; i < N; i += 32) {
+      double acc = 0.0;
+      for (int q = 0; q < NI; ++q) acc += phi[q * N + i] * fq[q];
+      double v = dts * acc;
+      if (p.dt > 0.0) {
+        double mu = 0.0;
+        for (int j = 0; j < N; ++j) mu += __ldg(tM + i * N + j) * p.uOld[e * N + j];
+        v += detJ * mu;
+      }
+      BW[i * LW + LL] = v;
+    }
+    __syncwarp();
+    // ------------------------------------- Cholesky A = L L^T (lower, in place)
+    bool bad = false;
+    for (int k = 0; k < N; ++k) {
+      const double akk = Am[k * N + k];
+      if (!(akk > 0.0)) bad = true;
+      const double lkk = sqrt(akk > 0.0 ? akk : 1.0);
+      const double il = 1.0 / lkk;
+      __syncwarp();
+      if (t == 0) {
+        Am[k * N + k] = lkk;
+        idg[k] = il;
+      }
+      for (int i = k + 1 + t; i < N; i += 32) Am[i * N + k] *= il;
+      __syncwarp();
+      const int m = N - k - 1;
+      for (int idx = t; idx < m * m; idx += 32) {
+        const int i = k + 1 + idx / m, j = k + 1 + idx % m;
+        if (j <= i) Am[i * N + j] -= Am[i * N + k] * Am[j * N + k];
+      }
+      __syncwarp();
+    }
+    if (bad && t == 0) atomicCAS(p.status, 0, 1);
+    // ---------------------- forward substitution: [W | y0] = L^{-1} [B | f_u]
+    for (int c = t; c < LW; c += 32) {
+      for (int i = 0; i < N; ++i) {
+        double v = BW[i * LW + c];
+        for (int m = 0; m < i; ++m) v -= Am[i * N + m] * BW[m * LW + c];
+        BW[i * LW + c] = v * idg[i];
+      }
+    }
+    __syncwarp();
+    // ------------------ S = C + dt W^T W (upper triangle, mirrored), S0 = W^T y0
+    {
+      double* Sg = (double*)p.S + e * LL * LL;
+      unsigned bmask = 0;  // bit f: face f of the cell is a Dirichlet face
+      for (int f = 0; f < F; ++f)
+        if (p.isBoundary[p.cell2face[e * F + f]]) bmask |= 1u << f;
+      for (int idx = t; idx < LL * (LL + 1) / 2; idx += 32) {
+        // column c, row r <= c, column-major packing of the upper triangle
+        int c = (int)((sqrtf(8.0f * idx + 1.0f) - 1.0f) * 0.5f);
+        while (c * (c + 1) / 2 > idx) --c;
+        while ((c + 1) * (c + 2) / 2 <= idx) ++c;
+        const int r = idx - c * (c + 1) / 2;
+        const int fr = r / NF, fc = c / NF;
+        double v = 0.0;
+        for (int m = 0; m < N; ++m) v += BW[m * LW + r] * BW[m * LW + c];
+        v *= dts;
+        v -= cff[fr * F + fc] * __ldg(tT + ((fr * F + fc) * NF + (r % NF)) * NF + (c % NF));
+        if (fr == fc) v -= Tm[(fr * NF + r % NF) * NF + (c % NF)];
+        const bool br = (bmask >> fr) & 1u;
+        const bool bc = (bmask >> fc) & 1u;
+        // Dirichlet Set: boundary rows become identity rows (columns are kept)
+        Sg[r + c * LL] = br ? (r == c ? 1.0 : 0.0) : v;
+        if (r != c) Sg[c + r * LL] = bc ? 0.0 : v;
+      }
+      for (int c = t; c < LL; c += 32) {
+        const int f = c / NF;
+        double v;
+        if ((bmask >> f) & 1u) {
+          v = p.dirichlet[(int64_t)p.cell2face[e * F + f] * NF + c % NF];
+        } else {
+          v = 0.0;
+          for (int m = 0; m < N; ++m) v += BW[m * LW + c] * BW[m * LW + LL];
+        }
+        ((double*)p.S0)[e * LL + c] = v;
+      }
+    }
+    __syncwarp();
+    // ------------- back substitution: U = -dt L^{-T} W, U0 = L^{-T} y0 (in place)
+    for (int c = t; c < LW; c += 32) {
+      const double sgn = c < LL ? -dts : 1.0;
+      for (int i = N - 1; i >= 0; --i) {
+        double v = BW[i * LW + c];
+        for (int m = i + 1; m < N; ++m) v -= Am[m * N + i] * BW[m * LW + c];
+        BW[i * LW + c] = v * idg[i];
+      }
+      for (int i = 0; i < N; ++i) BW[i * LW + c] *= sgn;
+    }
+    __syncwarp();
+    double* Ug = (double*)p.U + e * N * LL;
+    for (int idx = t; idx < N * LL; idx += 32) Ug[idx] = BW[(idx % N) * LW + idx / N];
+    for (int i = t; i < N; i += 32) ((double*)p.U0)[e * N + i] = BW[i * LW + LL];
+    __syncwarp();
+  }
+}
+
+// Recovery for the affine path: sol = U lambda + U0, flux = -Xu sol - Xl lambda.
+template <int D, int P>
+__global__ void recover_affine(RecoverParams p, const double* __restrict__ atab, const double* __restrict__ geo) {
+  using L = AffLayout<D, P>;
+  constexpr int N = L::N, NF = L::NF, F = L::F, LL = L::LL;
+  __shared__ double lam[LL];
+  __shared__ double sol[N];
+  __shared__ double ge[D * D + F * D];
+  const double* tD = atab + L::A_D;
+  const double* tL = atab + L::A_L;
+  for (int64_t e = blockIdx.x; e < p.nCells; e += gridDim.x) {
+    for (int j = threadIdx.x; j < LL; j += blockDim.x) {
+      int i = j / NF;
+      int f = p.cell2face[e * F + i];
+      lam[j] = p.trace[(int64_t)f * NF + p.perm[(e * F + i) * NF + (j % NF)]];
+    }
+    for (int j = threadIdx.x; j < D * D + F * D; j += blockDim.x) ge[j] = geo[e * (D * D + F * D) + j];
+    __syncthreads();
+    for (int r = threadIdx.x; r < N; r += blockDim.x) {
+      const double* U = p.U + e * N * LL;
+      double acc = p.U0[e * N + r];
+      for (int c = 0; c < LL; ++c) acc += U[r + (int64_t)c * N] * lam[c];
+      sol[r] = acc;
+      p.sol[e * N + r] = acc;
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < N * D; r += blockDim.x) {
+      const int i = r / D, d = r % D;  // flux node-major (i, d)
+      double acc = 0.0;
+      for (int s = 0; s < D; ++s) {
+        double ds = 0.0;
+        for (int j = 0; j < N; ++j) ds += __ldg(tD + (s * N + i) * N + j) * sol[j];
+        acc -= ge[d * D + s] * ds;
+      }
+      for (int f = 0; f < F; ++f) {
+        double lf = 0.0;
+        for (int b = 0; b < NF; ++b) lf += __ldg(tL + (f * N + i) * NF + b) * lam[f * NF + b];
+        acc += ge[D * D + f * D + d] * lf;
+      }
+      p.flux[e * N * D + r] = acc;
+    }
+    __syncthreads();
+  }
+}
+
+// Q = -Xu U - Xl, Q0 = -Xu U0 (column-major LQ x LL, rows node-major (i, d)), for exports.
+template <int D, int P>
+__global__ void q_from_u(int nCells, const double* __restrict__ U, const double* __restrict__ U0,
+                         const double* __restrict__ atab, const double* __restrict__ geo, double* Q, double* Q0) {
+  using L = AffLayout<D, P>;
+  constexpr int N = L::N, NF = L::NF, F = L::F, LL = L::LL, LQ = D * N;
+  const double* tD = atab + L::A_D;
+  const double* tL = atab + L::A_L;
+  const int64_t total = (int64_t)nCells * LQ * (LL + 1);
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = idx / (LQ * (LL + 1));
+    const int rc = (int)(idx % (LQ * (LL + 1)));
+    const int c = rc / LQ, row = rc % LQ;
+    const int i = row / D, d = row % D;
+    const double* ge = geo + e * (D * D + F * D);
+    const double* u = c < LL ? U + e * N * LL + (int64_t)c * N : U0 + e * N;
+    double acc = 0.0;
+    for (int s = 0; s < D; ++s) {
+      double ds = 0.0;
+      for (int j = 0; j < N; ++j) ds += tD[(s * N + i) * N + j] * u[j];
+      acc -= ge[d * D + s] * ds;
+    }
+    if (c < LL) {
+      const int f = c / NF, b = c % NF;
+      acc += ge[D * D + f * D + d] * tL[(f * N + i) * NF + b];
+      Q[e * LQ * LL + (int64_t)c * LQ + row] = acc;
+    } else {
+      Q0[e * LQ + row] = acc;
+    }
+  }
+}
+
+template <int D, int P>
+cudaError_t launch_affine_t(const LocalParams& p, const double* atab, double* geo, cudaStream_t s) {
+  using L = AffLayout<D, P>;
+  constexpr int EPC = 8;
+  size_t smem = (size_t)EPC * L::WARP * sizeof(double);
+  auto kern = local_affine<D, P, EPC>;
+  cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  int dev = 0, nsm = 0, perSM = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, 32 * EPC, smem);
+  if (err != cudaSuccess) return err;
+  if (perSM < 1) perSM = 1;
+  int64_t need = (p.nCells + EPC - 1) / EPC;
+  int64_t grid = (int64_t)nsm * perSM;
+  if (grid > need) grid = need;
+  if (grid < 1) grid = 1;
+  kern<<<(unsigned)grid, 32 * EPC, smem, s>>>(p, atab, geo);
+  return cudaGetLastError();
+}
+
+unsigned grid_cap(int64_t n, int threads) {
+  int64_t g = (n + threads - 1) / threads;
+  if (g > 152 * 64) g = 152 * 64;
+  return (unsigned)(g < 1 ? 1 : g);
+}
+
+}  // namespace
+
+#define HFX_AFFINE_DISPATCH(FN, ...)                          \
+  if (dim == 2) {                                             \
+    switch (order) {                                          \
+      case 1: return FN<2, 1>(__VA_ARGS__);                   \
+      case 2: return FN<2, 2>(__VA_ARGS__);                   \
+      case 3: return FN<2, 3>(__VA_ARGS__);                   \
+      case 4: return FN<2, 4>(__VA_ARGS__);                   \
+      case 5: return FN<2, 5>(__VA_ARGS__);                   \
+    }                                                         \
+  } else if (dim == 3) {                                      \
+    switch (order) {                                          \
+      case 1: return FN<3, 1>(__VA_ARGS__);                   \
+      case 2: return FN<3, 2>(__VA_ARGS__);                   \
+      case 3: return FN<3, 3>(__VA_ARGS__);                   \
+    }                                                         \
+  }                                                           \
+  return cudaErrorInvalidValue;
+
+cudaError_t launch_local_affine(int dim, int order, const LocalParams& p, const double* atab, double* geo,
+                                cudaStream_t s) {
+  HFX_AFFINE_DISPATCH(launch_affine_t, p, atab, geo, s)
+}
+
+namespace {
+template <int D, int P>
+cudaError_t launch_recover_affine_t(const RecoverParams& p, const double* atab, const double* geo, cudaStream_t s) {
+  int64_t grid = p.nCells < 152 * 64 ? p.nCells : 152 * 64;
+  recover_affine<D, P><<<(unsigned)(grid < 1 ? 1 : grid), 64, 0, s>>>(p, atab, geo);
+  return cudaGetLastError();
+}
+template <int D, int P>
+cudaError_t launch_q_from_u_t(int nCells, const double* U, const double* U0, const double* atab, const double* geo,
+                              double* Q, double* Q0, cudaStream_t s) {
+  using L = AffLayout<D, P>;
+  const int64_t total = (int64_t)nCells * D * L::N * (L::LL + 1);
+  q_from_u<D, P><<<grid_cap(total, 256), 256, 0, s>>>(nCells, U, U0, atab, geo, Q, Q0);
+  return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t launch_recover_affine(int dim, int order, const RecoverParams& p, const double* atab, const double* geo,
+                                  cudaStream_t s) {
+  HFX_AFFINE_DISPATCH(launch_recover_affine_t, p, atab, geo, s)
+}
+
+cudaError_t launch_q_from_u(int dim, int order, int nCells, const double* U, const double* U0, const double* atab,
+                            const double* geo, double* Q, double* Q0, cudaStream_t s) {
+  HFX_AFFINE_DISPATCH(launch_q_from_u_t, nCells, U, U0, atab, geo, Q, Q0, s)
+}
+
+}  // namespace hfx

@@ -63,6 +63,12 @@ struct LocalParams {
 cudaError_t launch_local_condense(int dim, int order, const LocalParams& p, cudaStream_t s);
 bool local_condense_supported(int dim, int order);
 
+// Affine elements with a symmetric, cell-constant diffusion tensor (hdg_affine.cu):
+// S, S0, U, U0 from reference operators; geo[nCells][D*D + F*D] holds the
+// factors the recovery (and the Q export) needs. atab from affine_tables().
+cudaError_t launch_local_affine(int dim, int order, const LocalParams& p, const double* atab, double* geo,
+                                cudaStream_t s);
+
 // Trace-system scatter (face-block rows, values in scalar-CSR order).
 struct ScatterParams {
   int nFaces, NF, LL;
@@ -95,6 +101,10 @@ struct RecoverParams {
   double* flux;
 };
 cudaError_t launch_recover(const RecoverParams& p, cudaStream_t s);
+cudaError_t launch_recover_affine(int dim, int order, const RecoverParams& p, const double* atab, const double* geo,
+                                  cudaStream_t s);
+cudaError_t launch_q_from_u(int dim, int order, int nCells, const double* U, const double* U0, const double* atab,
+                            const double* geo, double* Q, double* Q0, cudaStream_t s);
 
 struct IpCoordParams {
   int nCells, N, NI, D;

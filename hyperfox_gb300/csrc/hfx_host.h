@@ -52,4 +52,8 @@ struct BlockPattern {
 bool compute_block_pattern(const RefEl& re, int nCells, const Topology& t, BlockPattern* out,
                            std::string* err);
 
+// Reference operators of the affine element path (hdg_affine.cu), packed:
+// M, R_rs, T_f, P_rf, T_ff', M^{-1} C_r, L_f. False if M is singular.
+bool affine_tables(const RefEl& re, std::vector<double>* out);
+
 }  // namespace hfx

@@ -153,6 +153,13 @@ int hfx_assemble(hfx_ctx* ctx);
  * meets rtol; hfx_recover returns the refined FP64 Solution and Flux. The
  * element blocks and CSR stay FP32 (hfx_get_condensed / hfx_get_csr refuse). */
 int hfx_assemble_ex(hfx_ctx* ctx, int precision);
+/* Element kernel choice. 0 (default): straight-sided cells with a symmetric diffusion
+ * tensor constant inside every cell use reference operators (same blocks, far fewer
+ * FP64 operations; Q and Q0 are then formed on demand by hfx_get_condensed and by
+ * the recovery); everything else uses per-element quadrature. 1: quadrature always.
+ * hfx_assembly_info reports whether the last FP64 assembly took the affine path. */
+int hfx_set_assembly_path(hfx_ctx* ctx, int path);
+int hfx_assembly_info(hfx_ctx* ctx, int* affine);
 /* Condensed element blocks, column-major per element (any pointer may be NULL). */
 int hfx_get_condensed(hfx_ctx* ctx, double* S, double* S0, double* U, double* Q, double* U0,
                       double* Q0);
