@@ -171,7 +171,8 @@ def run_ours(args, world, rank, local):
     prec = capi.PREC_FP64 if args.precision == "fp64" else capi.PREC_MIXED
     pc = capi.PC_TWOLEVEL if args.precond == "twolevel" else capi.PC_BLOCK_JACOBI
     opts = capi.solve_opts(precision=prec, rtol=args.rtol, precond=pc, maxits=200000,
-                           inner_rtol=args.inner_rtol, coarse_guess=int(args.coarse_guess))
+                           inner_rtol=args.inner_rtol, coarse_guess=int(args.coarse_guess),
+                           coarse_rtol=args.coarse_rtol)
     info = capi.SolveInfo()
 
     asm_prec = capi.PREC_MIXED if args.precision == "mixed" else capi.PREC_FP64
@@ -356,6 +357,7 @@ def main():
     ap.add_argument("--precond", default="twolevel", choices=["twolevel", "bj"],
                     help="two-level (block Jacobi + vertex coarse space) or block Jacobi alone")
     ap.add_argument("--coarse-guess", action="store_true", help="start CG from the prolongated coarse solution")
+    ap.add_argument("--coarse-rtol", type=float, default=0.3, help="Chebyshev coarse-solve reduction target")
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

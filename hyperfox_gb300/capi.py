@@ -59,7 +59,7 @@ class SolveOpts(ctypes.Structure):
     _fields_ = [("method", ctypes.c_int), ("precond", ctypes.c_int), ("precision", ctypes.c_int),
                 ("rtol", ctypes.c_double), ("maxits", ctypes.c_int), ("restart", ctypes.c_int),
                 ("inner_rtol", ctypes.c_double), ("use_initial_guess", ctypes.c_int),
-                ("coarse_guess", ctypes.c_int)]
+                ("coarse_guess", ctypes.c_int), ("coarse_rtol", ctypes.c_double)]
 
 
 class SolveInfo(ctypes.Structure):

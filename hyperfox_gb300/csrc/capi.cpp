@@ -127,6 +127,7 @@ struct hfx_ctx {
   CoarseSolver coarse;
   DevMem coarseMem;
   bool coarseBuilt = false;
+  double coarseTarget = 0.0;
   // timing
   KernelTimer timer;
   cudaEvent_t marks[8] = {};
@@ -903,7 +904,7 @@ int hfx_get_csr(hfx_ctx* c, int64_t* rowptr, int* col, double* val, double* rhs)
 
 // Coarse space of the two-level preconditioner: host structure and device
 // buffers on first use (mesh-dependent), the operator after every assembly.
-static int ensure_coarse(hfx_ctx* c) {
+static int ensure_coarse(hfx_ctx* c, double target) {
   cudaStream_t s = c->stream;
   if (!c->coarseBuilt) {
     std::string err;
@@ -932,6 +933,13 @@ static int ensure_coarse(hfx_ctx* c) {
     HFX_CUDA(c, upload(m, &ridx, h.ridx.data(), h.ridx.size(), s));
     HFX_CUDA(c, upload(m, &faceV, h.faceV.data(), h.faceV.size(), s));
     HFX_CUDA(c, upload(m, &d.Wf, h.Wf.data(), h.Wf.size(), s));
+    int *ellCol, *ellSrc;
+    HFX_CUDA(c, upload(m, &ellCol, h.ellCol.data(), h.ellCol.size(), s));
+    HFX_CUDA(c, upload(m, &ellSrc, h.ellSrc.data(), h.ellSrc.size(), s));
+    HFX_CUDA(c, dalloc(m, &d.ellVal, h.ellCol.size()));
+    d.ellW = h.ellW;
+    d.ellCol = ellCol;
+    d.ellSrc = ellSrc;
     HFX_CUDA(c, upload(m, &d.Wc, h.Wc.data(), h.Wc.size(), s));
     d.rowptr = rowptr;
     d.col = col;
@@ -953,13 +961,18 @@ static int ensure_coarse(hfx_ctx* c) {
     HFX_CUDA(c, dalloc(m, &d.cd1, nV));
     HFX_CUDA(c, dalloc(m, &d.lz, nV));
     HFX_CUDA(c, dalloc(m, &d.partials, (size_t)152 * 32 + 64));
+    HFX_CUDA(c, dalloc(m, &d.barrier, 2));
+    HFX_CUDA(c, dalloc(m, &d.error, 1));
+    HFX_CUDA(c, cudaMemsetAsync(d.barrier, 0, 2 * sizeof(unsigned), s));
+    HFX_CUDA(c, cudaMemsetAsync(d.error, 0, sizeof(int), s));
     c->coarseHost = std::move(h);
     c->coarseBuilt = true;
     c->coarse.ready = false;
   }
-  if (!c->coarse.ready) {
+  if (!c->coarse.ready || c->coarseTarget != target) {
+    c->coarseTarget = target;
     c->timer.begin(K_COARSE, s);
-    cudaError_t e = coarse_setup<double>(&c->coarse, c->d_S, 64, 0.1, s);
+    cudaError_t e = coarse_setup<double>(&c->coarse, c->d_S, 64, target, s);
     c->timer.end(K_COARSE, s);
     if (e != cudaSuccess) return cuda_err(c, e, "coarse setup");
   }
@@ -977,6 +990,7 @@ void hfx_solve_opts_default(hfx_solve_opts* o) {
   o->inner_rtol = 1e-4;
   o->use_initial_guess = 0;
   o->coarse_guess = 0;
+  o->coarse_rtol = 0.1;
 }
 
 static int ensure_workspace(hfx_ctx* c, bool mixed, int restart) {
@@ -1130,7 +1144,8 @@ int hfx_solve(hfx_ctx* c, const hfx_solve_opts* opts, double* trace, hfx_solve_i
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, c->stream);
-  if (o.precond == HFX_PC_TWOLEVEL && (rc = ensure_coarse(c))) {
+  const double ctarget = o.coarse_rtol > 0.0 && o.coarse_rtol < 1.0 ? o.coarse_rtol : 0.1;
+  if (o.precond == HFX_PC_TWOLEVEL && (rc = ensure_coarse(c, ctarget))) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return rc;
@@ -1158,6 +1173,17 @@ int hfx_solve(hfx_ctx* c, const hfx_solve_opts* opts, double* trace, hfx_solve_i
   TraceSolveResult res;
   int st = method == HFX_KSP_CG ? trace_solve(a, &res) : trace_gmres(a, &res);
   int fallback = 0;
+  if (o.precond == HFX_PC_TWOLEVEL && st != 3) {
+    // a coarse-solve barrier that gave up invalidates the two-level iterates
+    int berr = 0;
+    HFX_CUDA(c, cudaMemcpy(&berr, c->coarse.dev.error, sizeof(int), cudaMemcpyDeviceToHost));
+    if (berr) {
+      HFX_CUDA(c, cudaMemset(c->coarse.dev.error, 0, sizeof(int)));
+      HFX_CUDA(c, cudaMemset(c->coarse.dev.barrier, 0, 2 * sizeof(unsigned)));
+      c->coarse.coopGrid = 0;  // launch-per-step coarse solve from now on
+      st = HFX_ERR_BREAKDOWN;
+    }
+  }
   if (o.precond == HFX_PC_TWOLEVEL &&
       (st == HFX_ERR_BREAKDOWN || st == HFX_ERR_NAN || st == HFX_ERR_NOT_CONVERGED)) {
     // the plain block-Jacobi solve finishes what the two-level solve could not
@@ -1201,7 +1227,7 @@ int hfx_coarse_operator(hfx_ctx* c, int* nV, int64_t* nnz, int* rowptr, int* col
   if (!c->assembled || c->mixedMode)
     return set_err(c, HFX_ERR_STATE, "coarse_operator: needs a trace system assembled in FP64");
   cudaSetDevice(c->device);
-  int rc = ensure_coarse(c);
+  int rc = ensure_coarse(c, c->coarseTarget > 0.0 ? c->coarseTarget : 0.1);
   if (rc) return rc;
   const CoarseHost& h = c->coarseHost;
   *nV = h.nV;

@@ -153,6 +153,18 @@ bool build_coarse_host(const RefEl& re, int nCells, const int* cellVerts, const 
     *err = "coarse space: too many cells for 32-bit contribution indices";
     return false;
   }
+  // ELL copy (column-major by slot): coalesced, fixed-width rows for the Chebyshev steps
+  for (int v = 0; v < nV; ++v) h.ellW = std::max(h.ellW, h.rowptr[v + 1] - h.rowptr[v]);
+  h.ellW = (h.ellW + 7) / 8 * 8;  // whole batches of 8 loads in flight, no serial tail
+  h.ellCol.assign((size_t)h.ellW * nV, 0);
+  h.ellSrc.assign((size_t)h.ellW * nV, -1);
+  for (int v = 0; v < nV; ++v)
+    for (int k = 0; k < h.ellW; ++k) {
+      const int q = h.rowptr[v] + k;
+      const bool in = q < h.rowptr[v + 1];
+      h.ellCol[(size_t)k * nV + v] = in ? h.col[q] : v;
+      h.ellSrc[(size_t)k * nV + v] = in ? q : -1;
+    }
   // restriction lists: faces incident to each vertex
   h.rptr.assign((size_t)nV + 1, 0);
   for (int f = 0; f < t.nFaces; ++f)
@@ -243,6 +255,37 @@ __global__ void coarse_gather(CoarseDev c) {
   }
 }
 
+__global__ void coarse_fill_ell(CoarseDev c) {
+  const int64_t n = (int64_t)c.ellW * c.nV;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int q = c.ellSrc[i];
+    c.ellVal[i] = q >= 0 ? c.val[q] : 0.f;
+  }
+}
+
+// y_v = sum_k ell[k][v] x[col] with up to 8 loads in flight (x read through L2:
+// other blocks write it between grid barriers)
+__device__ __forceinline__ float ell_row(const CoarseDev& c, int64_t v, const float* x) {
+  float y = 0.f;
+  const int W = c.ellW;
+  int k = 0;
+  for (; k + 8 <= W; k += 8) {
+    int cc[8];
+    float aa[8], xx[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      cc[u] = c.ellCol[(int64_t)(k + u) * c.nV + v];
+      aa[u] = c.ellVal[(int64_t)(k + u) * c.nV + v];
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) xx[u] = __ldcg(x + cc[u]);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) y = fmaf(aa[u], xx[u], y);
+  }
+  for (; k < W; ++k) y = fmaf(c.ellVal[(int64_t)k * c.nV + v], __ldcg(x + c.ellCol[(int64_t)k * c.nV + v]), y);
+  return y;
+}
+
 // ---- Lanczos on D^{-1/2} A_c D^{-1/2} (eigenvalue bounds for Chebyshev)
 
 __device__ __forceinline__ float coarse_row_sym(const CoarseDev& c, int64_t v, const float* __restrict__ x) {
@@ -288,29 +331,27 @@ __global__ void lanczos_scale(int64_t n, float* v, float s) {
     v[i] *= s;
 }
 
-// w = A v - beta v_prev; partial alpha = w . v
+// w = A v - beta v_prev; partials alpha = w . v and |w|^2 (|w - alpha v|^2 = |w|^2 - alpha^2)
 __global__ void lanczos_apply(CoarseDev c, const float* v, const float* vprev, float beta, float* w,
                               double* partials) {
-  double a = 0.0;
+  double a = 0.0, ww = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < c.nV; i += (int64_t)gridDim.x * blockDim.x) {
     float y = c.dinv[i] > 0.f ? coarse_row_sym(c, i, v) : 0.f;
     y -= beta * vprev[i];
     w[i] = y;
     a += (double)y * v[i];
+    ww += (double)y * y;
   }
   block_partial(a, partials, 0);
+  block_partial(ww, partials, 1);
 }
 
-// w -= alpha v; partial |w|^2
-__global__ void lanczos_orth(int64_t n, const float* v, float alpha, float* w, double* partials) {
-  double ss = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    float y = w[i] - alpha * v[i];
-    w[i] = y;
-    ss += (double)y * y;
-  }
-  block_partial(ss, partials, 0);
+// v_next = (w - alpha v) / beta
+__global__ void lanczos_next(int64_t n, const float* v, float alpha, float ib, float* w) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    w[i] = (w[i] - alpha * v[i]) * ib;
 }
+
 
 // ---- coarse solve
 
@@ -344,11 +385,100 @@ __global__ void coarse_cheb_step(CoarseDev c, const float* __restrict__ dk, floa
     const float dv = dk[v];
     c.yc[v] += dv;
     if (last) continue;
-    float y = 0.f;
-    for (int k = c.rowptr[v]; k < c.rowptr[v + 1]; ++k) y = fmaf(c.val[k], dk[c.col[k]], y);
+    const float y = ell_row(c, v, dk);
     const float r = c.cr[v] - y;
     c.cr[v] = r;
     dn[v] = c1 * dv + c2 * c.dinv[v] * r;
+  }
+}
+
+// ---- one-launch coarse solve: restriction and all Chebyshev steps in a
+// cooperative kernel (every block resident), separated by a grid barrier.
+
+constexpr int kMaxDegree = 64;
+constexpr long long kBarrierSpin = 1LL << 22;  // about a second: then the error flag
+
+struct ChebSchedule {
+  float c1[kMaxDegree], c2[kMaxDegree];
+  int degree;
+};
+
+// Grid-wide barrier with a bounded wait. The arrival counter starts each launch
+// at 0 and only grows within it: the k-th barrier completes when it reaches
+// k * gridDim.x. Arrival is a release add, the wait an acquire load; a wait that
+// runs out sets *error and returns (never spins forever).
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void red_release_add(unsigned* p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ void grid_barrier(unsigned* count, unsigned target, int* error) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    red_release_add(count, 1u);
+    long long it = 0;
+    while ((int)(ld_acquire(count) - target) < 0) {
+      if (++it > kBarrierSpin) {
+        atomicExch(error, 1);
+        break;
+      }
+    }
+  }
+  __syncthreads();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(512) coarse_solve_coop(CoarseDev c, const T* __restrict__ r, const int* skip,
+                                                         ChebSchedule cs) {
+  if (skip && *skip) return;  // the same value for every block: set before this launch
+  // barrier[0] counts arrivals and starts every launch at 0: the last block to
+  // leave (counted in barrier[1]) resets both, after every wait has finished
+  const int d = c.dim, NF = c.NF;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t v0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (int64_t v = v0; v < c.nV; v += stride) {
+    float s = 0.f;
+    for (int j = c.rptr[v]; j < c.rptr[v + 1]; ++j) {
+      const int fk = c.ridx[j];
+      const int64_t f = fk / d;
+      const int k = fk - (int)f * d;
+      if (c.isBnd[f]) continue;
+      const T* rf = r + f * NF;
+      for (int a = 0; a < NF; ++a) s = fmaf(c.Wf[a * d + k], (float)rf[a], s);
+    }
+    c.cr[v] = s;
+    c.yc[v] = 0.f;
+    c.cd0[v] = c.dinv[v] * s / c.theta;
+  }
+  float* dk = c.cd0;
+  float* dn = c.cd1;
+  for (int k = 0; k < cs.degree; ++k) {
+    grid_barrier(c.barrier, (unsigned)(k + 1) * gridDim.x, c.error);
+    const bool last = k + 1 == cs.degree;
+    for (int64_t v = v0; v < c.nV; v += stride) {
+      const float dv = __ldcg(dk + v);
+      c.yc[v] += dv;
+      if (last) continue;
+      const float y = ell_row(c, v, dk);
+      const float rr = c.cr[v] - y;
+      c.cr[v] = rr;
+      dn[v] = cs.c1[k] * dv + cs.c2[k] * c.dinv[v] * rr;
+    }
+    float* t = dk;
+    dk = dn;
+    dn = t;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned left = atomicAdd(c.barrier + 1, 1u) + 1u;
+    if (left == gridDim.x) {
+      atomicExch(c.barrier, 0u);
+      atomicExch(c.barrier + 1, 0u);
+    }
   }
 }
 
@@ -410,11 +540,12 @@ cudaError_t coarse_setup(CoarseSolver* cs, const T* S, int maxDegree, double tar
   if (c->NV1 == 3) coarse_elem<T, 3><<<gE, kT, 0, s>>>(*c, S);
   else coarse_elem<T, 4><<<gE, kT, 0, s>>>(*c, S);
   coarse_gather<<<blocks_for(c->nV), kT, 0, s>>>(*c);
+  coarse_fill_ell<<<blocks_for((int64_t)c->ellW * c->nV), kT, 0, s>>>(*c);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   // Lanczos, m steps, on D^{-1/2} A_c D^{-1/2}
   const unsigned g = blocks_for(c->nV);
-  std::vector<double> hp(g);
+  std::vector<double> hp(2 * g);
   float *v = c->cd0, *vprev = c->cd1, *w = c->lz;
   cudaMemsetAsync(vprev, 0, sizeof(float) * c->nV, s);
   lanczos_init<<<g, kT, 0, s>>>(*c, v, c->partials);
@@ -432,18 +563,17 @@ cudaError_t coarse_setup(CoarseSolver* cs, const T* S, int maxDegree, double tar
   const int m = (int)std::min<int64_t>(40, c->nV);
   double beta = 0.0;
   for (int j = 0; j < m; ++j) {
+    // one host round trip per step: alpha and |w|^2 from the same pass
     lanczos_apply<<<g, kT, 0, s>>>(*c, v, vprev, (float)beta, w, c->partials);
-    cudaMemcpyAsync(hp.data(), c->partials, sizeof(double) * g, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(hp.data(), c->partials, sizeof(double) * 2 * g, cudaMemcpyDeviceToHost, s);
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
-    double alpha = sum_partials(hp.data(), g);
+    const double alpha = sum_partials(hp.data(), g);
+    const double ww = sum_partials(hp.data() + g, g);
     al.push_back(alpha);
-    lanczos_orth<<<g, kT, 0, s>>>(c->nV, v, (float)alpha, w, c->partials);
-    cudaMemcpyAsync(hp.data(), c->partials, sizeof(double) * g, cudaMemcpyDeviceToHost, s);
-    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
-    beta = std::sqrt(sum_partials(hp.data(), g));
-    if (j + 1 == m || beta < 1e-10 * std::fabs(alpha)) break;
+    beta = std::sqrt(std::max(ww - alpha * alpha, 0.0));
+    if (j + 1 == m || beta < 1e-6 * std::sqrt(ww)) break;
     be.push_back(beta);
-    lanczos_scale<<<g, kT, 0, s>>>(c->nV, w, (float)(1.0 / beta));
+    lanczos_next<<<g, kT, 0, s>>>(c->nV, v, (float)alpha, (float)(1.0 / beta), w);
     float* t = vprev;
     vprev = v;
     v = w;
@@ -470,6 +600,19 @@ cudaError_t coarse_setup(CoarseSolver* cs, const T* S, int maxDegree, double tar
     cs->c2[k] = (float)(2.0 * rho1 / de);
     rho = rho1;
   }
+  // one-launch solve: every block must be resident (cooperative launch)
+  cs->coopGrid = 0;
+  int dev = 0, coop = 0, nsm = 0, perSM = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (coop && c->barrier && K <= kMaxDegree &&
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, coarse_solve_coop<double>, 512, 0) == cudaSuccess &&
+      perSM >= 1) {
+    int64_t want = (c->nV + 511) / 512;
+    int g = (int)std::min<int64_t>(want, (int64_t)nsm);  // one block per SM at most
+    cs->coopGrid = std::max(g, 1);
+  }
   cs->ready = true;
   return cudaGetLastError();
 }
@@ -477,6 +620,18 @@ cudaError_t coarse_setup(CoarseSolver* cs, const T* S, int maxDegree, double tar
 template <typename T>
 cudaError_t coarse_apply(const CoarseSolver& cs, const T* r, const int* skip, cudaStream_t s) {
   const CoarseDev& c = cs.dev;
+  if (cs.coopGrid > 0 && cs.degree <= kMaxDegree) {
+    ChebSchedule sch;
+    sch.degree = cs.degree;
+    for (int k = 0; k < cs.degree; ++k) {
+      sch.c1[k] = cs.c1[k];
+      sch.c2[k] = cs.c2[k];
+    }
+    CoarseDev cv = c;
+    const T* rr = r;
+    void* args[] = {&cv, (void*)&rr, (void*)&skip, &sch};
+    return cudaLaunchCooperativeKernel((const void*)coarse_solve_coop<T>, dim3(cs.coopGrid), dim3(512), args, 0, s);
+  }
   const unsigned g = blocks_for(c.nV);
   coarse_restrict<T><<<g, kT, 0, s>>>(c, r, skip);
   float *dk = c.cd0, *dn = c.cd1;

@@ -33,6 +33,8 @@ struct CoarseHost {
   std::vector<int> rowptr, col;   // coarse CSR pattern (vertices sharing a cell)
   std::vector<int> cptr, cidx;    // per coarse non-zero: element contributions (cell*NV1^2 + m*NV1 + m2)
   std::vector<int> rptr, ridx;    // per vertex: incident (face*dim + k)
+  int ellW = 0;
+  std::vector<int> ellCol, ellSrc; // [ellW][nV]
   std::vector<float> Wf;          // [NF][dim] default face weights (barycentric)
   std::vector<float> Wc;          // [F*NF][NV1] cell-local weights (barycentric, element face-node order)
 };
@@ -53,15 +55,22 @@ struct CoarseDev {
   float *Wf, *Wc;       // [NF*dim], [LL*NV1] (device, current weights)
   float* Ce;            // [nCells][NV1*NV1]
   float *val, *dinv;    // coarse operator values, inverse diagonal (0 for inactive)
+  int ellW;             // ELL copy of the coarse operator for the Chebyshev steps:
+  const int* ellCol;    // [ellW][nV] column (padding: the row itself)
+  float* ellVal;        // [ellW][nV] value (padding: 0)
+  const int* ellSrc;    // [ellW][nV] position in the CSR values (-1: padding)
   float *rc, *yc, *cr, *cd0, *cd1, *lz;  // work vectors [nV]
   double* partials;     // reductions for the eigenvalue estimate
   float theta;          // Chebyshev centre (start: d0 = D^{-1} r / theta)
+  unsigned* barrier;    // [2] grid barrier of the one-launch coarse solve: count, generation
+  int* error;           // set when a grid barrier wait ran out (the solve is then invalid)
 };
 
 // Coarse solver state: device view plus the Chebyshev schedule.
 struct CoarseSolver {
   CoarseDev dev{};
   bool ready = false;   // operator and schedule match the assembled system
+  int coopGrid = 0;     // >0: blocks of the cooperative one-launch Chebyshev solve
   int degree = 0;
   double lmin = 0.0, lmax = 0.0;
   std::vector<float> c1, c2;  // per step: d_{k+1} = c1[k] d_k + c2[k] D^{-1} r_{k+1}

@@ -77,6 +77,7 @@ typedef struct {
   double inner_rtol;     /* mixed precision: inner FP32 reduction per refinement step */
   int use_initial_guess; /* start from the trace already on the device */
   int coarse_guess;      /* HFX_PC_TWOLEVEL: start from the prolongated coarse solution */
+  double coarse_rtol;    /* HFX_PC_TWOLEVEL: residual reduction the Chebyshev coarse solve targets */
 } hfx_solve_opts;
 
 typedef struct {

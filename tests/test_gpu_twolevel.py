@@ -87,14 +87,20 @@ def test_twolevel_solve_matches_direct(hfx_lib, dim, n, order, precision, coarse
 
 
 @pytest.mark.parametrize("precision", [0, 1])
-def test_twolevel_needs_fewer_iterations(hfx_lib, precision):
+def test_twolevel_iterations_grow_slower_than_block_jacobi(hfx_lib, precision):
+    """Block-Jacobi CG iterations grow like 1/h; the coarse space removes most of that growth."""
     from hyperfox_gb300 import capi
-    P, ctx, _ = build_pair(hfx_lib, 3, 8, 2, tau2=False, kappa="none", jitter=0.0)
-    ctx.assemble()
-    _, bj = ctx.solve(precision=precision, rtol=1e-10, precond=capi.PC_BLOCK_JACOBI)
-    _, tl = ctx.solve(precision=precision, rtol=1e-10, precond=capi.PC_TWOLEVEL)
-    assert bj.status == 0 and tl.status == 0
-    assert tl.iterations < 0.6 * bj.iterations, (tl.iterations, bj.iterations)
+    its = {}
+    for n in (5, 10):
+        P, ctx, _ = build_pair(hfx_lib, 3, n, 2, tau2=False, kappa="none", jitter=0.0)
+        ctx.assemble()
+        _, bj = ctx.solve(precision=precision, rtol=1e-10, precond=capi.PC_BLOCK_JACOBI)
+        _, tl = ctx.solve(precision=precision, rtol=1e-10, precond=capi.PC_TWOLEVEL)
+        assert bj.status == 0 and tl.status == 0 and tl.fallback == 0
+        its[n] = (bj.iterations, tl.iterations)
+    (bj5, tl5), (bj10, tl10) = its[5], its[10]
+    assert tl10 < 0.6 * bj10, its
+    assert tl10 - tl5 < 0.5 * (bj10 - bj5), its
 
 
 def test_twolevel_refused_for_gmres_and_mixed_assembly(hfx_lib):
