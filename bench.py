@@ -172,7 +172,8 @@ def run_ours(args, world, rank, local):
     pc = capi.PC_TWOLEVEL if args.precond == "twolevel" else capi.PC_BLOCK_JACOBI
     opts = capi.solve_opts(precision=prec, rtol=args.rtol, precond=pc, maxits=200000,
                            inner_rtol=args.inner_rtol, coarse_guess=int(args.coarse_guess),
-                           coarse_rtol=args.coarse_rtol)
+                           coarse_rtol=args.coarse_rtol,
+                           coarse_mode=capi.COARSE_LEARNED if args.coarse == "learned" else capi.COARSE_CHEBYSHEV)
     info = capi.SolveInfo()
 
     asm_prec = capi.PREC_MIXED if args.precision == "mixed" else capi.PREC_FP64
@@ -195,6 +196,13 @@ def run_ours(args, world, rank, local):
     ref_info = capi.SolveInfo()
     x_ref = np.zeros(ctx.ndofs)
     ctx._chk(L.hfx_solve(ctx.h, capi.ctypes.byref(ref_opts), capi._p(x_ref), capi.ctypes.byref(ref_info)), "ref solve")
+    # learned coarse polynomial: trained once on this system's own coarse residuals (setup, untimed)
+    learned = None
+    if args.precond == "twolevel" and args.coarse == "learned" and args.precision != "mixed":
+        ti = ctx.coarse_train(degree=args.coarse_degree, samples=16, steps=300)
+        learned = dict(degree=ti.degree, samples=ti.samples, steps=ti.steps, accepted=bool(ti.accepted),
+                       loss_chebyshev_same_degree=ti.loss_chebyshev, loss_learned=ti.loss_learned,
+                       max_residual_polynomial=ti.max_poly, train_s=ti.train_ms / 1e3)
     for _ in range(args.warmup):
         step_device()
     # device-resident timed region
@@ -291,8 +299,9 @@ def run_ours(args, world, rank, local):
         "dtype": "f64+f32" if prec else "f64",
         "data": "synthetic (seedless structured mesh, manufactured solution)",
         "config": {"workload": cfg["desc"], "elements": E, "order": p, "trace_dofs": n, "csr_nnz": nnz,
-                   "precision": args.precision, "preconditioner": ("two-level: per-face block Jacobi + vertex coarse space (Chebyshev degree %d)"
-                                      % info.coarse_degree) if args.precond == "twolevel" else "block-Jacobi (per face)",
+                   "precision": args.precision, "preconditioner": ("two-level: per-face block Jacobi + vertex coarse space (%s coarse polynomial, degree %d)"
+                                      % ("learned" if info.coarse_learned else "Chebyshev", info.coarse_degree))
+                                     if args.precond == "twolevel" else "block-Jacobi (per face)",
                    "rtol": args.rtol, "l2_flush": "inputs > L2 (no flush needed)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "time_to_solve_s": step_s,
@@ -302,6 +311,7 @@ def run_ours(args, world, rank, local):
         "rel_err_vs_fp64": rel_err,
         "fp64_reference_iterations": ref_info.iterations,
         "plain_fp64": plain,
+        "learned_coarse": learned,
         "kernel_ms": {k: dict(launches=v[0], total_ms=round(v[1], 3)) for k, v in kt.items()},
         "roofline": roof,
         "clocks": clk,
@@ -358,6 +368,9 @@ def main():
                     help="two-level (block Jacobi + vertex coarse space) or block Jacobi alone")
     ap.add_argument("--coarse-guess", action="store_true", help="start CG from the prolongated coarse solution")
     ap.add_argument("--coarse-rtol", type=float, default=0.3, help="Chebyshev coarse-solve reduction target")
+    ap.add_argument("--coarse", default="learned", choices=["learned", "chebyshev"],
+                    help="coarse solve of the two-level preconditioner: trained polynomial or Chebyshev")
+    ap.add_argument("--coarse-degree", type=int, default=6, help="degree of the learned coarse polynomial")
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

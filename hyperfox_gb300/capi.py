@@ -25,6 +25,7 @@ HFX_ERR_UNSUPPORTED = 9
 
 KSP_CG, KSP_GMRES, KSP_AUTO = 0, 1, 2
 PC_NONE, PC_JACOBI, PC_BLOCK_JACOBI, PC_TWOLEVEL = 0, 1, 2, 3
+COARSE_CHEBYSHEV, COARSE_LEARNED = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 SRC_NONE, SRC_VALUES, SRC_SINPROD = 0, 1, 2
 
@@ -35,7 +36,8 @@ EXPORTED = [
     "hfx_mesh_upload", "hfx_mesh_sizes", "hfx_mesh_topology", "hfx_mesh_compute_topology",
     "hfx_set_tau", "hfx_set_kappa", "hfx_set_source", "hfx_set_dirichlet", "hfx_set_time_scheme",
     "hfx_ip_coords", "hfx_assemble", "hfx_assemble_ex", "hfx_set_assembly_path", "hfx_assembly_info", "hfx_get_condensed", "hfx_get_csr",
-    "hfx_solve_opts_default", "hfx_solve", "hfx_recover", "hfx_coarse_operator",
+    "hfx_solve_opts_default", "hfx_solve", "hfx_recover", "hfx_coarse_operator", "hfx_coarse_train",
+    "hfx_coarse_loss_grad",
     "hfx_la_create", "hfx_la_destroy", "hfx_la_allocate", "hfx_la_set_values", "hfx_la_set_rhs",
     "hfx_la_zero_rows", "hfx_la_assemble", "hfx_la_clear", "hfx_la_solve", "hfx_la_nnz",
     "hfx_profile_enable", "hfx_kernel_time", "hfx_mark", "hfx_elapsed_ms", "hfx_synchronize",
@@ -59,13 +61,20 @@ class SolveOpts(ctypes.Structure):
     _fields_ = [("method", ctypes.c_int), ("precond", ctypes.c_int), ("precision", ctypes.c_int),
                 ("rtol", ctypes.c_double), ("maxits", ctypes.c_int), ("restart", ctypes.c_int),
                 ("inner_rtol", ctypes.c_double), ("use_initial_guess", ctypes.c_int),
-                ("coarse_guess", ctypes.c_int), ("coarse_rtol", ctypes.c_double)]
+                ("coarse_guess", ctypes.c_int), ("coarse_rtol", ctypes.c_double), ("coarse_mode", ctypes.c_int)]
 
 
 class SolveInfo(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int), ("iterations", ctypes.c_int), ("refinements", ctypes.c_int),
                 ("rel_residual", ctypes.c_double), ("solve_ms", ctypes.c_double),
-                ("fallback", ctypes.c_int), ("coarse_degree", ctypes.c_int)]
+                ("fallback", ctypes.c_int), ("coarse_degree", ctypes.c_int), ("coarse_learned", ctypes.c_int)]
+
+
+class TrainInfo(ctypes.Structure):
+    _fields_ = [("degree", ctypes.c_int), ("samples", ctypes.c_int), ("steps", ctypes.c_int),
+                ("accepted", ctypes.c_int), ("loss_chebyshev", ctypes.c_double), ("loss_learned", ctypes.c_double),
+                ("max_poly", ctypes.c_double), ("train_ms", ctypes.c_double), ("loss_first_step", ctypes.c_double),
+                ("lower_steps", ctypes.c_int), ("rejected_steps", ctypes.c_int)]
 
 
 _lib = None
@@ -105,6 +114,8 @@ def load(path=LIB_PATH):
         "hfx_solve": ([vp, ctypes.POINTER(SolveOpts), vp, ctypes.POINTER(SolveInfo)], ip),
         "hfx_recover": ([vp, vp, vp], ip),
         "hfx_coarse_operator": ([vp, vp, vp, vp, vp, vp, vp], ip),
+        "hfx_coarse_train": ([vp, ip, ip, ip, ctypes.POINTER(TrainInfo)], ip),
+        "hfx_coarse_loss_grad": ([vp, ip, vp, ip, vp, vp, vp], ip),
         "hfx_set_assembly_path": ([vp, ip], ip),
         "hfx_assembly_info": ([vp, vp], ip),
         "hfx_la_create": ([vp, ctypes.POINTER(vp)], ip),
@@ -315,6 +326,20 @@ class Context:
         self._chk(self.L.hfx_coarse_operator(self.h, ctypes.byref(nV), ctypes.byref(nnz), _p(rowptr), _p(col),
                                              _p(val), _p(vn)), "coarse_operator")
         return rowptr, col, val, vn
+
+    def coarse_train(self, degree=4, samples=16, steps=300):
+        info = TrainInfo()
+        self._chk(self.L.hfx_coarse_train(self.h, degree, samples, steps, ctypes.byref(info)), "coarse_train")
+        return info
+
+    def coarse_loss_grad(self, theta, samples):
+        theta = np.ascontiguousarray(theta, np.float64)
+        samples = np.ascontiguousarray(samples, np.float32)
+        loss = ctypes.c_double()
+        grad = np.zeros(len(theta))
+        self._chk(self.L.hfx_coarse_loss_grad(self.h, len(theta), _p(theta), samples.shape[0], _p(samples),
+                                              ctypes.byref(loss), _p(grad)), "coarse_loss_grad")
+        return loss.value, grad
 
     def recover(self):
         sol = np.zeros((self.nCells, self.lenU))

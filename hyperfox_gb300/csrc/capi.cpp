@@ -1,3 +1,4 @@
+#include <chrono>
 // C ABI of the GB300 HDG hot path (declared in include/hfx_gb300.h).
 //
 // The context owns every device buffer and one CUDA stream. Host arrays are
@@ -991,6 +992,7 @@ void hfx_solve_opts_default(hfx_solve_opts* o) {
   o->use_initial_guess = 0;
   o->coarse_guess = 0;
   o->coarse_rtol = 0.1;
+  o->coarse_mode = HFX_COARSE_CHEBYSHEV;
 }
 
 static int ensure_workspace(hfx_ctx* c, bool mixed, int restart) {
@@ -1109,6 +1111,7 @@ static int solve_mixed(hfx_ctx* c, const hfx_solve_opts& o, int method, int rest
     info->solve_ms = ms;
     info->fallback = 0;
     info->coarse_degree = 0;
+    info->coarse_learned = 0;
   }
   if (trace) HFX_CUDA(c, cudaMemcpy(trace, c->d_trace, sizeof(double) * c->ndofs(), cudaMemcpyDeviceToHost));
   c->solved = true;
@@ -1170,6 +1173,9 @@ int hfx_solve(hfx_ctx* c, const hfx_solve_opts* opts, double* trace, hfx_solve_i
   a.restart = restart;
   a.coarse = o.precond == HFX_PC_TWOLEVEL ? &c->coarse : nullptr;
   a.coarse_guess = o.coarse_guess;
+  const bool learned = o.precond == HFX_PC_TWOLEVEL && o.coarse_mode == HFX_COARSE_LEARNED &&
+                       !c->coarse.thetaHat.empty();
+  c->coarse.useLearned = learned;
   TraceSolveResult res;
   int st = method == HFX_KSP_CG ? trace_solve(a, &res) : trace_gmres(a, &res);
   int fallback = 0;
@@ -1210,8 +1216,11 @@ int hfx_solve(hfx_ctx* c, const hfx_solve_opts* opts, double* trace, hfx_solve_i
     info->rel_residual = res.rel_residual;
     info->solve_ms = ms;
     info->fallback = fallback;
-    info->coarse_degree = o.precond == HFX_PC_TWOLEVEL ? c->coarse.degree : 0;
+    info->coarse_degree =
+        o.precond != HFX_PC_TWOLEVEL ? 0 : (learned ? (int)c->coarse.thetaHat.size() : c->coarse.degree);
+    info->coarse_learned = learned ? 1 : 0;
   }
+  c->coarse.useLearned = false;
   if (st == 3) return cuda_err(c, res.cudaErr, "solve");
   if (trace) HFX_CUDA(c, cudaMemcpy(trace, c->d_trace, sizeof(double) * c->ndofs(), cudaMemcpyDeviceToHost));
   c->solved = true;
@@ -1237,6 +1246,90 @@ int hfx_coarse_operator(hfx_ctx* c, int* nV, int64_t* nnz, int* rowptr, int* col
   if (col) std::copy(h.col.begin(), h.col.end(), col);
   if (vertexNode) std::copy(h.vertexNode.begin(), h.vertexNode.end(), vertexNode);
   if (val) HFX_CUDA(c, cudaMemcpy(val, c->coarse.dev.val, sizeof(float) * h.col.size(), cudaMemcpyDeviceToHost));
+  return HFX_OK;
+}
+
+int hfx_coarse_train(hfx_ctx* c, int degree, int samples, int steps, hfx_train_info* info) {
+  if (!c) return HFX_ERR_ARG;
+  if (degree < 1 || degree > 16 || samples < 1 || samples > 32 || steps < 0)
+    return set_err(c, HFX_ERR_ARG, "coarse_train: degree 1..16, samples 1..32, steps >= 0");
+  if (!c->assembled || c->mixedMode)
+    return set_err(c, HFX_ERR_STATE, "coarse_train: needs a trace system assembled in FP64");
+  if (!c->kappaCellConstant)
+    return set_err(c, HFX_ERR_UNSUPPORTED, "coarse_train: the two-level preconditioner needs a symmetric system");
+  cudaSetDevice(c->device);
+  auto t0 = std::chrono::steady_clock::now();
+  int rc = ensure_workspace(c, false, 0);
+  if (rc) return rc;
+  if ((rc = ensure_coarse(c, c->coarseTarget > 0.0 ? c->coarseTarget : 0.1))) return rc;
+  const int64_t nV = c->coarse.dev.nV;
+  float* buf = nullptr;
+  HFX_CUDA(c, cudaMalloc(&buf, sizeof(float) * (size_t)samples * nV));
+  // samples: the coarse residuals of a two-level CG run on this system (Chebyshev coarse solve)
+  TraceSolveArgs a{};
+  a.dim = c->dim;
+  a.A = TraceView{c->topo.nFaces, c->re.nNodesFace, c->d_browptr, c->d_bcol, c->d_isBnd};
+  a.val = c->d_val;
+  a.rhs = c->d_rhs;
+  a.x = c->d_trace;
+  a.precond = HFX_PC_TWOLEVEL;
+  a.mixed = 0;
+  a.rtol = 1e-300;
+  a.maxits = 2 * samples;
+  a.check_every = 25;
+  a.ws = c->ws;
+  a.stream = c->stream;
+  a.timer = &c->timer;
+  a.coarse = &c->coarse;
+  a.sampleBuf = buf;
+  a.sampleCap = samples;
+  a.sampleStride = 2;
+  int taken = 0;
+  a.sampleCount = &taken;
+  c->coarse.useLearned = false;
+  TraceSolveResult res;
+  int st = trace_solve(a, &res);
+  c->solved = false;
+  if (st == 3) {
+    cudaFree(buf);
+    return cuda_err(c, res.cudaErr, "coarse_train samples");
+  }
+  const int S = std::min(taken, samples);
+  CoarseTrainResult tr;
+  cudaError_t e = coarse_train(&c->coarse, buf, S, degree, steps, 0.05, c->stream, &tr);
+  cudaFree(buf);
+  if (e != cudaSuccess) return cuda_err(c, e, "coarse_train");
+  if (info) {
+    info->degree = tr.degree;
+    info->samples = S;
+    info->steps = tr.steps;
+    info->accepted = tr.accepted;
+    info->loss_chebyshev = tr.lossChebyshev;
+    info->loss_learned = tr.lossLearned;
+    info->max_poly = tr.maxGain;
+    info->train_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    info->loss_first_step = tr.lossFirstStep;
+    info->lower_steps = tr.lowerSteps;
+    info->rejected_steps = tr.rejectedSteps;
+  }
+  return HFX_OK;
+}
+
+int hfx_coarse_loss_grad(hfx_ctx* c, int degree, const double* theta, int samples, const float* values, double* loss,
+                         double* grad) {
+  if (!c || !theta || !values || !loss || !grad || degree < 1 || degree > 16 || samples < 1) return HFX_ERR_ARG;
+  if (!c->assembled || c->mixedMode)
+    return set_err(c, HFX_ERR_STATE, "coarse_loss_grad: needs a trace system assembled in FP64");
+  cudaSetDevice(c->device);
+  int rc = ensure_coarse(c, c->coarseTarget > 0.0 ? c->coarseTarget : 0.1);
+  if (rc) return rc;
+  const int64_t nV = c->coarse.dev.nV;
+  float* buf = nullptr;
+  HFX_CUDA(c, cudaMalloc(&buf, sizeof(float) * (size_t)samples * nV));
+  cudaError_t e = cudaMemcpy(buf, values, sizeof(float) * (size_t)samples * nV, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = coarse_loss_grad(c->coarse, buf, samples, degree, theta, loss, grad, c->stream);
+  cudaFree(buf);
+  if (e != cudaSuccess) return cuda_err(c, e, "coarse_loss_grad");
   return HFX_OK;
 }
 
@@ -1384,6 +1477,7 @@ int hfx_la_solve(hfx_la* la, const hfx_solve_opts* opts, double* x, hfx_solve_in
     info->solve_ms = r.ms;
     info->fallback = 0;
     info->coarse_degree = 0;
+    info->coarse_learned = 0;
   }
   if (st != 0) return set_err(la->ctx, st, err);
   return HFX_OK;

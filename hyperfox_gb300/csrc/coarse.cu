@@ -7,6 +7,7 @@
 #include "coarse.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <numeric>
 
@@ -357,7 +358,7 @@ __global__ void lanczos_next(int64_t n, const float* v, float alpha, float ib, f
 
 // rc = P^T r (interior faces); Chebyshev start: cr = rc, d0 = D^{-1} rc / theta, yc = 0
 template <typename T>
-__global__ void coarse_restrict(CoarseDev c, const T* __restrict__ r, const int* skip) {
+__global__ void coarse_restrict(CoarseDev c, const T* __restrict__ r, const int* skip, float d0scale) {
   if (skip && *skip) return;
   const int d = c.dim, NF = c.NF;
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < c.nV; v += (int64_t)gridDim.x * blockDim.x) {
@@ -373,7 +374,7 @@ __global__ void coarse_restrict(CoarseDev c, const T* __restrict__ r, const int*
     c.rc[v] = s;
     c.cr[v] = s;
     c.yc[v] = 0.f;
-    c.cd0[v] = c.dinv[v] * s / c.theta;
+    c.cd0[v] = c.dinv[v] * s * d0scale;
   }
 }
 
@@ -400,6 +401,7 @@ constexpr long long kBarrierSpin = 1LL << 22;  // about a second: then the error
 
 struct ChebSchedule {
   float c1[kMaxDegree], c2[kMaxDegree];
+  float d0scale;
   int degree;
 };
 
@@ -450,9 +452,10 @@ __global__ void __launch_bounds__(512) coarse_solve_coop(CoarseDev c, const T* _
       const T* rf = r + f * NF;
       for (int a = 0; a < NF; ++a) s = fmaf(c.Wf[a * d + k], (float)rf[a], s);
     }
+    c.rc[v] = s;
     c.cr[v] = s;
     c.yc[v] = 0.f;
-    c.cd0[v] = c.dinv[v] * s / c.theta;
+    c.cd0[v] = c.dinv[v] * s * cs.d0scale;
   }
   float* dk = c.cd0;
   float* dn = c.cd1;
@@ -494,6 +497,228 @@ __global__ void coarse_prolong(CoarseDev c, T* __restrict__ x) {
     for (int k = 0; k < d; ++k) s = fmaf(c.Wf[a * d + k], c.yc[c.faceV[f * d + k]], s);
     x[i] += (T)s;
   }
+}
+
+// ---- learned coarse polynomial: forward and backward kernels.
+// Samples and every intermediate are [S][nV] (sample s contiguous). The model
+// propagates coarse errors U through the Richardson steps,
+// U_{k+1} = U_k - theta_k D^{-1} A_c U_k, and the loss is their energy after K
+// steps, L = sum_s w_s U_K[s]^T A_c U_K[s], w_s = 1 / (S U_0[s]^T A_c U_0[s]):
+// the A_c-norm error reduction of the coarse solve on the solver's own coarse
+// errors (U_0 = A_c^{-1} P^T r from its Krylov residuals r).
+
+__device__ __forceinline__ float ell_row_plain(const CoarseDev& c, int64_t v, const float* x) {
+  float y = 0.f;
+  for (int k = 0; k < c.ellW; ++k)
+    y = fmaf(c.ellVal[(int64_t)k * c.nV + v], x[c.ellCol[(int64_t)k * c.nV + v]], y);
+  return y;
+}
+
+__device__ __forceinline__ void block_sum_to(double v, double* out) {
+  __shared__ double red[kT / 32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    *out = t;
+  }
+  __syncthreads();
+}
+
+// grid (Gx, S). AX = A X; partials of X . AX per sample at partials[s * Gx + bx]
+__global__ void learn_energy(CoarseDev c, const float* X, float* AX, double* partials) {
+  const int sm = blockIdx.y;
+  const float* x = X + (int64_t)sm * c.nV;
+  double acc = 0.0;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < c.nV; v += (int64_t)gridDim.x * blockDim.x) {
+    const float y = c.dinv[v] > 0.f ? ell_row_plain(c, v, x) : 0.f;
+    AX[(int64_t)sm * c.nV + v] = y;
+    acc += (double)x[v] * y;
+  }
+  block_sum_to(acc, partials + (int64_t)sm * gridDim.x + blockIdx.x);
+}
+
+// Y = D^{-1} A X, Xn = X - theta Y
+__global__ void learn_fwd(CoarseDev c, const float* X, float* Y, float* Xn, float theta) {
+  const int sm = blockIdx.y;
+  const float* x = X + (int64_t)sm * c.nV;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < c.nV; v += (int64_t)gridDim.x * blockDim.x) {
+    const float y = c.dinv[v] > 0.f ? c.dinv[v] * ell_row_plain(c, v, x) : 0.f;
+    Y[(int64_t)sm * c.nV + v] = y;
+    Xn[(int64_t)sm * c.nV + v] = x[v] - theta * y;
+  }
+}
+
+// loss partials w_s U . AU and the adjoint seed G = 2 w_s AU (AU from learn_energy)
+__global__ void learn_seed(CoarseDev c, const float* U, const float* AU, const double* w, float* G, double* partials) {
+  const int sm = blockIdx.y;
+  const double ws = w[sm];
+  double acc = 0.0;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < c.nV; v += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = (int64_t)sm * c.nV + v;
+    acc += ws * (double)U[i] * AU[i];
+    G[i] = (float)(2.0 * ws * AU[i]);
+  }
+  block_sum_to(acc, partials + (int64_t)sm * gridDim.x + blockIdx.x);
+}
+
+// dL/dtheta_k partials = -sum G_{k+1} . Y_k, and G_k = G_{k+1} - theta_k A_c D^{-1} G_{k+1}
+__global__ void learn_bwd(CoarseDev c, const float* G, const float* Yk, float* Gn, float theta, double* partials) {
+  const int sm = blockIdx.y;
+  const float* g = G + (int64_t)sm * c.nV;
+  double acc = 0.0;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < c.nV; v += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = (int64_t)sm * c.nV + v;
+    acc -= (double)g[v] * Yk[i];
+    float ag = 0.f;
+    if (c.dinv[v] > 0.f)
+      for (int k = 0; k < c.ellW; ++k) {
+        const int col = c.ellCol[(int64_t)k * c.nV + v];
+        ag = fmaf(c.ellVal[(int64_t)k * c.nV + v] * c.dinv[col], g[col], ag);
+      }
+    Gn[i] = g[v] - theta * ag;
+  }
+  block_sum_to(acc, partials + (int64_t)sm * gridDim.x + blockIdx.x);
+}
+
+// batched Chebyshev step on coarse vectors (errors of the training samples):
+// Y += D_k; R -= A D_k; D_{k+1} = c1 D_k + c2 D^{-1} R
+__global__ void learn_cheb(CoarseDev c, const float* Dk, float* Dn, float* R, float* Y, float c1, float c2, int last) {
+  const int sm = blockIdx.y;
+  const float* d = Dk + (int64_t)sm * c.nV;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < c.nV; v += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = (int64_t)sm * c.nV + v;
+    Y[i] += d[v];
+    if (last) continue;
+    const float ad = c.dinv[v] > 0.f ? ell_row_plain(c, v, d) : 0.f;
+    const float r = R[i] - ad;
+    R[i] = r;
+    Dn[i] = c1 * d[v] + c2 * c.dinv[v] * r;
+  }
+}
+
+__global__ void learn_cheb_start(CoarseDev c, const float* R, float* D0, float* Y, float scale) {
+  const int sm = blockIdx.y;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < c.nV; v += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = (int64_t)sm * c.nV + v;
+    D0[i] = c.dinv[v] * R[i] * scale;
+    Y[i] = 0.f;
+  }
+}
+
+struct LearnWork {
+  float *E, *Y, *G0, *G1;
+  double *w, *part;
+  int Gx;
+};
+
+// Forward and backward pass for theta (unscaled): loss and dL/dtheta.
+cudaError_t learn_pass(const CoarseDev& c, const LearnWork& lw, int S, int K, const double* theta, double* loss,
+                       double* grad, std::vector<double>& hp, cudaStream_t s) {
+  const int64_t nV = c.nV;
+  const dim3 grid(lw.Gx, S);
+  for (int k = 0; k < K; ++k)
+    learn_fwd<<<grid, kT, 0, s>>>(c, lw.E + (int64_t)k * S * nV, lw.Y + (int64_t)k * S * nV,
+                                  lw.E + (int64_t)(k + 1) * S * nV, (float)theta[k]);
+  // A U_K into G1, then the loss and the seed G0
+  learn_energy<<<grid, kT, 0, s>>>(c, lw.E + (int64_t)K * S * nV, lw.G1, lw.part);
+  learn_seed<<<grid, kT, 0, s>>>(c, lw.E + (int64_t)K * S * nV, lw.G1, lw.w, lw.G0, lw.part);
+  float *g = lw.G0, *gn = lw.G1;
+  for (int k = K - 1; k >= 0; --k) {
+    learn_bwd<<<grid, kT, 0, s>>>(c, g, lw.Y + (int64_t)k * S * nV, gn, (float)theta[k],
+                                  lw.part + (int64_t)(k + 1) * S * lw.Gx);
+    std::swap(g, gn);
+  }
+  const size_t np = (size_t)(K + 1) * S * lw.Gx;
+  hp.resize(np);
+  cudaError_t e = cudaMemcpyAsync(hp.data(), lw.part, sizeof(double) * np, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return e;
+  const size_t slot = (size_t)S * lw.Gx;
+  double L = 0.0;
+  for (size_t i = 0; i < slot; ++i) L += hp[i];
+  *loss = L;
+  for (int k = 0; k < K; ++k) {
+    double gk = 0.0;
+    for (size_t i = 0; i < slot; ++i) gk += hp[(k + 1) * slot + i];
+    grad[k] = gk;
+  }
+  return cudaSuccess;
+}
+
+// Work buffers; E_0 = the error samples [S][nV] and their weights.
+cudaError_t learn_setup(const CoarseDev& c, const float* samples, int S, int K, LearnWork* lw, cudaStream_t s) {
+  const int64_t nV = c.nV;
+  lw->Gx = (int)std::min<int64_t>((nV + kT - 1) / kT, 64);
+  cudaError_t e;
+  if ((e = cudaMalloc(&lw->E, sizeof(float) * (size_t)(K + 1) * S * nV)) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&lw->Y, sizeof(float) * (size_t)std::max(K, 1) * S * nV)) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&lw->G0, sizeof(float) * (size_t)S * nV)) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&lw->G1, sizeof(float) * (size_t)S * nV)) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&lw->w, sizeof(double) * S)) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&lw->part, sizeof(double) * (size_t)(K + 1) * S * lw->Gx)) != cudaSuccess) return e;
+  cudaMemcpyAsync(lw->E, samples, sizeof(float) * (size_t)S * nV, cudaMemcpyDeviceToDevice, s);
+  learn_energy<<<dim3(lw->Gx, S), kT, 0, s>>>(c, lw->E, lw->G1, lw->part);
+  std::vector<double> hp((size_t)S * lw->Gx), w(S);
+  cudaMemcpyAsync(hp.data(), lw->part, sizeof(double) * hp.size(), cudaMemcpyDeviceToHost, s);
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+  for (int sm = 0; sm < S; ++sm) {
+    double t = 0.0;
+    for (int b = 0; b < lw->Gx; ++b) t += hp[(size_t)sm * lw->Gx + b];
+    w[sm] = t > 0.0 ? 1.0 / (t * S) : 0.0;  // every sample weighs 1/S
+  }
+  cudaMemcpyAsync(lw->w, w.data(), sizeof(double) * S, cudaMemcpyHostToDevice, s);
+  return cudaGetLastError();
+}
+
+void learn_free(LearnWork* lw) {
+  cudaFree(lw->E);
+  cudaFree(lw->Y);
+  cudaFree(lw->G0);
+  cudaFree(lw->G1);
+  cudaFree(lw->w);
+  cudaFree(lw->part);
+}
+
+// Soft constraint keeping the residual polynomial below 1 on [0, lhi]: penalty
+// P = 100 mean_i relu(q(lambda_i) - 0.999)^2 on a grid and its gradient in theta.
+double poly_penalty(const std::vector<double>& theta, double lhi, std::vector<double>* grad) {
+  const int K = (int)theta.size(), n = 1024;
+  double P = 0.0;
+  grad->assign(K, 0.0);
+  for (int i = 1; i <= n; ++i) {
+    const double l = lhi * i / n;
+    double q = 1.0;
+    for (double t : theta) q *= 1.0 - t * l;
+    const double ex = q - 0.999;
+    if (ex <= 0.0) continue;
+    P += ex * ex;
+    for (int k = 0; k < K; ++k) {
+      double dq = -l;  // d/dtheta_k of prod_j (1 - theta_j l)
+      for (int j = 0; j < K; ++j)
+        if (j != k) dq *= 1.0 - theta[j] * l;
+      (*grad)[k] += 2.0 * ex * dq;
+    }
+  }
+  const double sc = 100.0 / n;
+  for (auto& g : *grad) g *= sc;
+  return P * sc;
+}
+
+// max over [0, lhi] of prod_k (1 - theta_k lambda) (the coarse solve stays
+// positive semidefinite when this is <= 1 on the spectrum; lhi is the upper
+// Chebyshev bound, 1.1 x the largest Lanczos Ritz value)
+double poly_max(const std::vector<double>& theta, double lhi) {
+  double m = -1e300;
+  for (int i = 0; i <= 4096; ++i) {
+    const double l = lhi * i / 4096.0;
+    double q = 1.0;
+    for (double t : theta) q *= 1.0 - t * l;
+    m = std::max(m, q);
+  }
+  return m;
 }
 
 // Sturm count: number of eigenvalues of the tridiagonal (a, b) below x.
@@ -617,26 +842,44 @@ cudaError_t coarse_setup(CoarseSolver* cs, const T* S, int maxDegree, double tar
   return cudaGetLastError();
 }
 
+static ChebSchedule poly_schedule(const CoarseSolver& cs) {
+  ChebSchedule sch{};
+  if (cs.useLearned && !cs.thetaHat.empty()) {
+    // Richardson steps with the learned weights
+    const int K = (int)cs.thetaHat.size();
+    sch.degree = K;
+    sch.d0scale = (float)(cs.thetaHat[0] / cs.lmax);
+    for (int k = 0; k < K; ++k) {
+      sch.c1[k] = 0.f;
+      sch.c2[k] = k + 1 < K ? (float)(cs.thetaHat[k + 1] / cs.lmax) : 0.f;
+    }
+    return sch;
+  }
+  sch.degree = cs.degree;
+  sch.d0scale = 1.0f / cs.dev.theta;
+  for (int k = 0; k < cs.degree; ++k) {
+    sch.c1[k] = cs.c1[k];
+    sch.c2[k] = cs.c2[k];
+  }
+  return sch;
+}
+
 template <typename T>
 cudaError_t coarse_apply(const CoarseSolver& cs, const T* r, const int* skip, cudaStream_t s) {
   const CoarseDev& c = cs.dev;
-  if (cs.coopGrid > 0 && cs.degree <= kMaxDegree) {
-    ChebSchedule sch;
-    sch.degree = cs.degree;
-    for (int k = 0; k < cs.degree; ++k) {
-      sch.c1[k] = cs.c1[k];
-      sch.c2[k] = cs.c2[k];
-    }
+  const ChebSchedule sch = poly_schedule(cs);
+  if (cs.coopGrid > 0 && sch.degree <= kMaxDegree) {
     CoarseDev cv = c;
     const T* rr = r;
-    void* args[] = {&cv, (void*)&rr, (void*)&skip, &sch};
+    ChebSchedule sc = sch;
+    void* args[] = {&cv, (void*)&rr, (void*)&skip, &sc};
     return cudaLaunchCooperativeKernel((const void*)coarse_solve_coop<T>, dim3(cs.coopGrid), dim3(512), args, 0, s);
   }
   const unsigned g = blocks_for(c.nV);
-  coarse_restrict<T><<<g, kT, 0, s>>>(c, r, skip);
+  coarse_restrict<T><<<g, kT, 0, s>>>(c, r, skip, sch.d0scale);
   float *dk = c.cd0, *dn = c.cd1;
-  for (int k = 0; k < cs.degree; ++k) {
-    coarse_cheb_step<<<g, kT, 0, s>>>(c, dk, dn, cs.c1[k], cs.c2[k], k + 1 == cs.degree, skip);
+  for (int k = 0; k < sch.degree; ++k) {
+    coarse_cheb_step<<<g, kT, 0, s>>>(c, dk, dn, sch.c1[k], sch.c2[k], k + 1 == sch.degree, skip);
     std::swap(dk, dn);
   }
   return cudaGetLastError();
@@ -646,6 +889,157 @@ template <typename T>
 cudaError_t coarse_prolong_add(const CoarseSolver& cs, T* x, cudaStream_t s) {
   coarse_prolong<T><<<blocks_for(cs.dev.nFaces * cs.dev.NF), kT, 0, s>>>(cs.dev, x);
   return cudaGetLastError();
+}
+
+// Errors of the coarse residual samples: Y ~ A_c^{-1} R by Chebyshev on
+// [lmin, lmax] of D^{-1} A_c, degree for a reduction `target` (at most maxDeg).
+cudaError_t coarse_errors(const CoarseSolver& cs, const float* R0, int S, double target, int maxDeg, float** out,
+                          cudaStream_t s) {
+  const CoarseDev& c = cs.dev;
+  const int64_t n = (int64_t)S * c.nV;
+  float *R = nullptr, *D0 = nullptr, *D1 = nullptr, *Y = nullptr;
+  cudaError_t e = cudaMalloc(&R, sizeof(float) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&D0, sizeof(float) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&D1, sizeof(float) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&Y, sizeof(float) * n);
+  if (e != cudaSuccess) {
+    cudaFree(R);
+    cudaFree(D0);
+    cudaFree(D1);
+    cudaFree(Y);
+    return e;
+  }
+  cudaMemcpyAsync(R, R0, sizeof(float) * n, cudaMemcpyDeviceToDevice, s);
+  const double th = 0.5 * (cs.lmax + cs.lmin), de = 0.5 * (cs.lmax - cs.lmin), sig = th / de;
+  int K = (int)std::ceil(std::acosh(1.0 / target) / std::acosh(sig));
+  K = std::max(1, std::min(K, maxDeg));
+  const dim3 grid((unsigned)std::min<int64_t>((c.nV + kT - 1) / kT, 64), S);
+  learn_cheb_start<<<grid, kT, 0, s>>>(c, R, D0, Y, (float)(1.0 / th));
+  double rho = 1.0 / sig;
+  float *dk = D0, *dn = D1;
+  for (int k = 0; k < K; ++k) {
+    const double rho1 = 1.0 / (2.0 * sig - rho);
+    learn_cheb<<<grid, kT, 0, s>>>(c, dk, dn, R, Y, (float)(rho1 * rho), (float)(2.0 * rho1 / de), k + 1 == K);
+    rho = rho1;
+    std::swap(dk, dn);
+  }
+  cudaFree(R);
+  cudaFree(D0);
+  cudaFree(D1);
+  *out = Y;
+  return cudaGetLastError();
+}
+
+cudaError_t coarse_loss_grad(const CoarseSolver& cs, const float* samples, int S, int K, const double* theta,
+                             double* loss, double* grad, cudaStream_t s) {
+  LearnWork lw{};
+  cudaError_t e = learn_setup(cs.dev, samples, S, K, &lw, s);
+  std::vector<double> hp;
+  if (e == cudaSuccess) e = learn_pass(cs.dev, lw, S, K, theta, loss, grad, hp, s);
+  learn_free(&lw);
+  return e;
+}
+
+cudaError_t coarse_train(CoarseSolver* cs, const float* samples, int S, int K, int steps, double lr, cudaStream_t s,
+                         CoarseTrainResult* out) {
+  *out = CoarseTrainResult{};
+  out->degree = K;
+  out->samples = S;
+  out->steps = steps;
+  auto t0 = std::chrono::steady_clock::now();
+  const double lmax = cs->lmax, lmin = cs->lmin;
+  // training errors U_0 = A_c^{-1} (P^T r): Chebyshev to 1e-4 on the residual samples
+  float* U0 = nullptr;
+  cudaError_t e = coarse_errors(*cs, samples, S, 1e-4, 256, &U0, s);
+  LearnWork lw{};
+  if (e == cudaSuccess) e = learn_setup(cs->dev, U0, S, K, &lw, s);
+  cudaFree(U0);
+  if (e != cudaSuccess) {
+    learn_free(&lw);
+    return e;
+  }
+  // start from Chebyshev of the same degree on [lmin, lmax]: its residual
+  // polynomial has the roots lambda_j of T_K mapped to the interval
+  std::vector<double> phi(K), theta(K), grad(K), hp, best(K);
+  for (int j = 0; j < K; ++j) {
+    const double lj = 0.5 * (lmax + lmin) + 0.5 * (lmax - lmin) * std::cos(M_PI * (2 * j + 1) / (2.0 * K));
+    phi[j] = std::log(lmax / lj);  // theta_j = e^phi / lmax = 1 / lambda_j
+  }
+  auto thetas = [&]() {
+    for (int k = 0; k < K; ++k) theta[k] = std::exp(phi[k]) / lmax;
+  };
+  thetas();
+  double L = 0.0;
+  if ((e = learn_pass(cs->dev, lw, S, K, theta.data(), &L, grad.data(), hp, s)) != cudaSuccess) {
+    learn_free(&lw);
+    return e;
+  }
+  out->lossChebyshev = L;
+  double bestL = L;
+  best = phi;
+  std::vector<double> m1(K, 0.0), m2(K, 0.0);
+  const double b1 = 0.9, b2 = 0.999;
+  std::vector<double> pgrad(K);
+  for (int it = 0; it < steps; ++it) {
+    poly_penalty(theta, lmax, &pgrad);
+    for (int k = 0; k < K; ++k) {
+      const double g = (grad[k] + pgrad[k]) * theta[k];  // d/dphi of loss + penalty
+      m1[k] = b1 * m1[k] + (1 - b1) * g;
+      m2[k] = b2 * m2[k] + (1 - b2) * g * g;
+      const double mh = m1[k] / (1 - std::pow(b1, it + 1)), vh = m2[k] / (1 - std::pow(b2, it + 1));
+      phi[k] -= lr * mh / (std::sqrt(vh) + 1e-12);
+    }
+    thetas();
+    if ((e = learn_pass(cs->dev, lw, S, K, theta.data(), &L, grad.data(), hp, s)) != cudaSuccess) break;
+    if (it == 0) out->lossFirstStep = L;
+    if (std::isfinite(L) && L < bestL) {
+      // keep only polynomials that leave the coarse solve positive semidefinite
+      std::vector<double> th(K);
+      for (int k = 0; k < K; ++k) th[k] = std::exp(phi[k]) / lmax;
+      if (poly_max(th, lmax) <= 1.0 + 1e-9) {
+        bestL = L;
+        best = phi;
+        ++out->lowerSteps;
+      } else {
+        ++out->rejectedSteps;
+      }
+    }
+  }
+  learn_free(&lw);
+  if (e != cudaSuccess) return e;
+  out->lossLearned = bestL;
+  out->lossStart = out->lossChebyshev;
+  std::vector<double> th(K);
+  for (int k = 0; k < K; ++k) th[k] = std::exp(best[k]) / lmax;
+  out->maxGain = poly_max(th, lmax);
+  out->accepted = bestL < out->lossChebyshev ? 1 : 0;
+  if (out->accepted) {
+    // Leja order of the roots 1/theta (largest first, then each maximising the
+    // product of distances to those already taken): the same polynomial, with
+    // bounded growth of the partial products in FP32
+    std::vector<double> roots(K), ordered;
+    for (int k = 0; k < K; ++k) roots[k] = 1.0 / std::exp(best[k]);  // in units of lmax
+    std::vector<bool> used(K, false);
+    for (int n = 0; n < K; ++n) {
+      int pick = -1;
+      double bestScore = -1.0;
+      for (int k = 0; k < K; ++k) {
+        if (used[k]) continue;
+        double score = n == 0 ? std::fabs(roots[k]) : 1.0;
+        for (double r : ordered) score *= std::fabs(roots[k] - r);
+        if (score > bestScore) {
+          bestScore = score;
+          pick = k;
+        }
+      }
+      used[pick] = true;
+      ordered.push_back(roots[pick]);
+    }
+    cs->thetaHat.resize(K);
+    for (int k = 0; k < K; ++k) cs->thetaHat[k] = 1.0 / ordered[k];  // theta * lmax
+  }
+  out->ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return cudaSuccess;
 }
 
 template cudaError_t coarse_setup<double>(CoarseSolver*, const double*, int, double, cudaStream_t);

@@ -66,15 +66,46 @@ struct CoarseDev {
   int* error;           // set when a grid barrier wait ran out (the solve is then invalid)
 };
 
-// Coarse solver state: device view plus the Chebyshev schedule.
+// Coarse solver state: device view plus the polynomial schedule. Both coarse
+// solves run y = sum_k d_k with r_{k+1} = r_k - A_c d_k and
+// d_{k+1} = c1[k] d_k + c2[k] D^{-1} r_{k+1}, d_0 = d0scale D^{-1} r_0:
+//  - Chebyshev on [lmin, lmax] of D^{-1} A_c (the default), or
+//  - the learned polynomial: Richardson steps with trained weights theta_k
+//    (c1 = 0, c2[k] = theta_{k+1}, d0scale = theta_0), i.e. the residual
+//    polynomial prod_k (1 - theta_k lambda) fitted to the coarse residuals the
+//    solver itself produces (coarse_train).
 struct CoarseSolver {
   CoarseDev dev{};
   bool ready = false;   // operator and schedule match the assembled system
-  int coopGrid = 0;     // >0: blocks of the cooperative one-launch Chebyshev solve
+  int coopGrid = 0;     // >0: blocks of the cooperative one-launch coarse solve
   int degree = 0;
   double lmin = 0.0, lmax = 0.0;
-  std::vector<float> c1, c2;  // per step: d_{k+1} = c1[k] d_k + c2[k] D^{-1} r_{k+1}
+  std::vector<float> c1, c2;  // Chebyshev schedule
+  // learned polynomial: weights scaled by lmax (theta_k = thetaHat_k / lmax), so
+  // that a trained schedule carries over to a re-assembled operator
+  std::vector<double> thetaHat;
+  bool useLearned = false;    // apply the learned schedule (set per solve)
 };
+
+// Result of training the learned coarse polynomial.
+struct CoarseTrainResult {
+  int degree = 0, samples = 0, steps = 0, accepted = 0;
+  double lossStart = 0.0, lossChebyshev = 0.0, lossLearned = 0.0, maxGain = 0.0, ms = 0.0;
+  int lowerSteps = 0, rejectedSteps = 0;  // steps that lowered the loss / were refused by the polynomial check
+  double lossFirstStep = 0.0;
+};
+
+// Fit theta (K weights) to the coarse residual samples [S][nV] (column-major:
+// sample s contiguous) by Adam on log(theta * lmax), with the project's forward
+// and backward kernels. Accepted only if prod_k (1 - theta_k lambda) <= 1 on
+// [0, lmax] (the coarse solve then stays symmetric positive semidefinite)
+// and the loss beats Chebyshev of the same degree.
+cudaError_t coarse_train(CoarseSolver* c, const float* samples, int S, int K, int steps, double lr, cudaStream_t s,
+                         CoarseTrainResult* out);
+// Loss and gradient of the learned polynomial for given theta (unscaled) on
+// samples [S][nV]: the GPU kernels coarse_train uses (for gradient checks).
+cudaError_t coarse_loss_grad(const CoarseSolver& c, const float* samples, int S, int K, const double* theta,
+                             double* loss, double* grad, cudaStream_t s);
 
 // Coarse operator from the condensed element matrices (T = double or float),
 // its eigenvalue bounds and the Chebyshev schedule. Returns a CUDA error.

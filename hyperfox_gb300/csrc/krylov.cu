@@ -708,11 +708,20 @@ struct Driver {
     CgState hst;
     KernelTimer* tm = a.timer;
     // two-level second half of K2 (coarse solve of r, then z and r.z)
+    int coarseApplies = 0;
     auto coarse_z = [&](auto* rv, auto* zv, const auto* pcv, int init) {
       using T = std::remove_cv_t<std::remove_pointer_t<decltype(rv)>>;
       tm->begin(K_COARSE, s);
       coarse_apply<T>(*a.coarse, rv, &st->done, s);
       tm->end(K_COARSE, s);
+      if (a.sampleBuf && a.sampleCount && coarseApplies % std::max(1, a.sampleStride) == 0 &&
+          *a.sampleCount < a.sampleCap) {
+        const int64_t nV = a.coarse->dev.nV;
+        cudaMemcpyAsync(a.sampleBuf + (int64_t)(*a.sampleCount) * nV, a.coarse->dev.rc, sizeof(float) * nV,
+                        cudaMemcpyDeviceToDevice, s);
+        ++*a.sampleCount;
+      }
+      ++coarseApplies;
       tm->begin(K_UPDATE, s);
       tl_apply<T, NF><<<gridT, kThreads, 0, s>>>(A.nFaces, rv, zv, pcv, a.coarse->dev, st, partials, init);
       tm->end(K_UPDATE, s);

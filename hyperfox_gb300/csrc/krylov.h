@@ -55,6 +55,11 @@ struct TraceSolveArgs {
   KernelTimer* timer;
   const CoarseSolver* coarse;  // set up for precond 3
   int coarse_guess;            // start from the prolongated coarse solution of b'
+  // training samples of the learned coarse polynomial (FP64 two-level CG only):
+  // every sampleStride-th coarse solve copies its restricted residual P^T r
+  float* sampleBuf;            // [sampleCap][nV]
+  int sampleCap, sampleStride;
+  int* sampleCount;            // host counter
 };
 
 struct TraceSolveResult {

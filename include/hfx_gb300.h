@@ -78,7 +78,13 @@ typedef struct {
   int use_initial_guess; /* start from the trace already on the device */
   int coarse_guess;      /* HFX_PC_TWOLEVEL: start from the prolongated coarse solution */
   double coarse_rtol;    /* HFX_PC_TWOLEVEL: residual reduction the Chebyshev coarse solve targets */
+  int coarse_mode;       /* HFX_PC_TWOLEVEL: HFX_COARSE_CHEBYSHEV or HFX_COARSE_LEARNED */
 } hfx_solve_opts;
+
+/* Coarse solve of HFX_PC_TWOLEVEL. LEARNED applies the polynomial trained by
+ * hfx_coarse_train (Chebyshev until one has been accepted). */
+#define HFX_COARSE_CHEBYSHEV 0
+#define HFX_COARSE_LEARNED 1
 
 typedef struct {
   int status;              /* HFX_OK or an error code */
@@ -87,8 +93,20 @@ typedef struct {
   double rel_residual;     /* final FP64 ||b-Ax||/||b|| of the reference system */
   double solve_ms;         /* device time of the solve */
   int fallback;            /* 1: the two-level solve failed and block Jacobi finished it */
-  int coarse_degree;       /* HFX_PC_TWOLEVEL: Chebyshev degree of the coarse solve */
+  int coarse_degree;       /* HFX_PC_TWOLEVEL: degree of the coarse polynomial used */
+  int coarse_learned;      /* 1: the learned coarse polynomial was applied */
 } hfx_solve_info;
+
+typedef struct {
+  int degree, samples, steps, accepted;
+  double loss_chebyshev;   /* loss of Chebyshev of the same degree (the starting point) */
+  double loss_learned;     /* loss after training (accepted only if lower) */
+  double max_poly;         /* max of the residual polynomial on [0, lmax]: <= 1 keeps CG valid */
+  double train_ms;         /* sample collection + training, host wall time */
+  double loss_first_step;  /* loss after the first optimiser step */
+  int lower_steps;         /* optimiser steps that lowered the best loss */
+  int rejected_steps;      /* lower-loss steps refused by the polynomial check */
+} hfx_train_info;
 
 /* ---- context ------------------------------------------------------------ */
 int hfx_ctx_create(int device, hfx_ctx** out);
@@ -184,6 +202,23 @@ int hfx_recover(hfx_ctx* ctx, double* solution, double* flux);
  * interior block of the trace system, in CSR (rowptr[nV+1], col/val[nnz],
  * FP32). Call with rowptr == NULL for the sizes. Needs an assembled system. */
 int hfx_coarse_operator(hfx_ctx* ctx, int* nV, int64_t* nnz, int* rowptr, int* col, float* val, int* vertexNode);
+
+/* Learned coarse correction (no counterpart in the reference). The coarse solve
+ * of HFX_PC_TWOLEVEL becomes a degree-K polynomial in D^{-1} A_c, Richardson
+ * steps y += theta_k D^{-1} (r - A_c y), whose weights are trained on the GPU
+ * with this library's forward and backward kernels to minimise the energy
+ * (A_c-norm) of the coarse error left after the solve, averaged over `samples`
+ * coarse errors A_c^{-1} P^T r taken from the residuals r of a two-level CG run
+ * on the current system (every second iteration). Training starts from
+ * Chebyshev of degree K; the result is kept only if it beats it and keeps the
+ * coarse solve positive semidefinite. hfx_solve(coarse_mode =
+ * HFX_COARSE_LEARNED) then applies it; block-Jacobi CG stays the fallback of
+ * the whole two-level solve. hfx_coarse_loss_grad evaluates the same loss and
+ * its gradient for given theta on caller error samples [S][nV] (host, FP32)
+ * with the same kernels. */
+int hfx_coarse_train(hfx_ctx* ctx, int degree, int samples, int steps, hfx_train_info* info);
+int hfx_coarse_loss_grad(hfx_ctx* ctx, int degree, const double* theta, int samples, const float* values,
+                         double* loss, double* grad);
 
 /* ---- timing on the context's stream (CUDA events; no profiler) ---------------
  * hfx_profile_enable(ctx, 1) resets and starts per-kernel event timing;
