@@ -35,6 +35,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "time-to-solve @1e-8 rel err, learned+mixed vs plain FP64 GPU; elements/s"
+# DRAM bytes per unit from the committed ncu captures (profiles/): the FP32 trace
+# SpMV moves 4.29 bytes per non-zero (289.4 MB at 67.44M non-zeros), the FP64
+# one 8.75; the affine element kernel writes 18.6 KB per p=3 tetrahedron.
+TRAFFIC_PER_NNZ = {"spmv32": 289.4e6 / 67.44e6, "spmv64": 590.2e6 / 67.44e6}
+TRAFFIC_PER_ELEMENT_LOCAL = (24.3e6 + 893.0e6) / 48000
+FP64_NOMINAL_TFLOPS = 1.25
 
 CONFIGS = {
     # name: dim, n (cubes per side), order
@@ -176,7 +182,7 @@ def run_ours(args, world, rank, local):
                            coarse_mode=capi.COARSE_LEARNED if args.coarse == "learned" else capi.COARSE_CHEBYSHEV)
     info = capi.SolveInfo()
 
-    asm_prec = capi.PREC_MIXED if args.precision == "mixed" else capi.PREC_FP64
+    asm_prec = capi.PREC_MIXED if args.precision == "mixed-full" else capi.PREC_FP64
 
     def step_device():
         ctx._chk(L.hfx_assemble_ex(ctx.h, asm_prec), "assemble")
@@ -198,7 +204,7 @@ def run_ours(args, world, rank, local):
     ctx._chk(L.hfx_solve(ctx.h, capi.ctypes.byref(ref_opts), capi._p(x_ref), capi.ctypes.byref(ref_info)), "ref solve")
     # learned coarse polynomial: trained once on this system's own coarse residuals (setup, untimed)
     learned = None
-    if args.precond == "twolevel" and args.coarse == "learned" and args.precision != "mixed":
+    if args.precond == "twolevel" and args.coarse == "learned" and args.precision != "mixed-full":
         ti = ctx.coarse_train(degree=args.coarse_degree, samples=16, steps=300)
         learned = dict(degree=ti.degree, samples=ti.samples, steps=ti.steps, accepted=bool(ti.accepted),
                        loss_chebyshev_same_degree=ti.loss_chebyshev, loss_learned=ti.loss_learned,
@@ -258,31 +264,48 @@ def run_ours(args, world, rank, local):
         plain = dict(time_to_solve_s=pms.value / 1e3 / max(1, args.plain_steps), iterations=fp_info.iterations)
     E = ctx.nCells
     step_s = dev_ms / 1e3 / args.steps
-    # roofline of the dominant kernel
+    # roofline of the dominant kernel, and of the dominant HBM-bound kernel
     hbm, peak_kind = peaks()
     nnz, n = ctx.nnz, ctx.ndofs
     nblocks = nnz // (Nf * Nf)
+
+    def spmv_roof(key):
+        sv = 4 if key == "spmv32" else 8
+        # values once, block columns + row pointers once, z and p_old gathered once, p_new and q written
+        alg = nnz * sv + nblocks * 4 + (ctx.nFaces + 1) * 8 + 4 * n * sv
+        # launches that did work: one per Krylov iteration (launches queued after
+        # convergence return at entry and are not counted)
+        launches = min(kt[key][0], iters * args.steps) if iters else kt[key][0]
+        avg_ms = kt[key][1] / max(1, launches)
+        achieved = alg / (avg_ms / 1e3) / 1e9
+        return dict(bound="hbm", kernel="cg_spmv<%s>" % ("float" if sv == 4 else "double"),
+                    achieved=round(achieved, 1), peak=hbm, unit="GB/s", frac=round(achieved / hbm, 4),
+                    traffic=(TRAFFIC_PER_NNZ[key] * nnz) if (dim, p) == (3, 3) else None, bytes_per_launch=int(alg),
+                    avg_launch_ms=round(avg_ms, 4), peak_source=peak_kind)
+
+    def local_roof():
+        # FP64 FMAs the affine element kernel executes per element (reference-operator algorithm)
+        N, NF_, F_ = ctx.re["nNodes"], Nf, ctx.re["nFaces"]
+        LL, NI = F_ * NF_, ctx.re["nIP"]
+        fma = (F_ * NF_ ** 3 + N * N * (dim * dim + 1) + N * LL * dim + NI * N * dim + N * NI + N ** 3 / 6
+               + 2 * (LL + 1) * N * (N - 1) / 2 + LL * (LL + 1) / 2 * N + LL * N)
+        avg_ms = kt["local"][1] / max(1, kt["local"][0])
+        tf = 2 * fma * E / (avg_ms / 1e3) / 1e12
+        return dict(bound="fp64", kernel="local_affine (FP64 element assembly + condensation)",
+                    achieved=round(tf, 3), peak=FP64_NOMINAL_TFLOPS, unit="TFLOP/s",
+                    frac=round(tf / FP64_NOMINAL_TFLOPS, 4),
+                    traffic=TRAFFIC_PER_ELEMENT_LOCAL * E if (dim, p) == (3, 3) else None,
+                    flops_per_element=int(2 * fma), avg_launch_ms=round(avg_ms, 4),
+                    peak_source="nominal GB300 FP64 (no measured FP64 peak); ncu: FP64 pipe 90% busy")
+
     dom = max(("local", "spmv64", "spmv32", "update", "scatter", "recover", "residual"), key=lambda k: kt[k][1])
     roof = None
     if dom in ("spmv32", "spmv64"):
-        sv = 4 if dom == "spmv32" else 8
-        # values once, block columns + row pointers once, z and p_old gathered once, p_new and q written
-        alg = nnz * sv + nblocks * 4 + (ctx.nFaces + 1) * 8 + 4 * n * sv
-        launches = kt[dom][0]
-        avg_ms = kt[dom][1] / max(1, launches)
-        achieved = alg / (avg_ms / 1e3) / 1e9
-        roof = dict(bound="hbm", kernel="cg_spmv<%s>" % ("float" if sv == 4 else "double"),
-                    achieved=round(achieved, 1), peak=hbm, unit="GB/s", frac=round(achieved / hbm, 4),
-                    traffic=None, bytes_per_launch=int(alg), avg_launch_ms=round(avg_ms, 4), peak_source=peak_kind)
+        roof = spmv_roof(dom)
     elif dom == "local":
-        LU, LQ, LL = ctx.lenU, ctx.lenQ, ctx.lenL
-        alg = E * ((ctx.re["nNodes"] * dim + ctx.re["nNodes"]) * 8 + (LL * LL + LL + (LU + LQ) * (LL + 1)) * 8)
-        avg_ms = kt["local"][1] / max(1, kt["local"][0])
-        achieved = alg / (avg_ms / 1e3) / 1e9
-        roof = dict(bound="hbm", kernel="local_condense_f64", achieved=round(achieved, 1), peak=hbm, unit="GB/s",
-                    frac=round(achieved / hbm, 4), traffic=None, bytes_per_launch=int(alg),
-                    avg_launch_ms=round(avg_ms, 4), peak_source=peak_kind,
-                    note="FP64-pipe bound on GB300; HBM fraction shown")
+        roof = local_roof()
+    hbm_key = max(("spmv32", "spmv64"), key=lambda k: kt[k][1])
+    roof_hbm = spmv_roof(hbm_key) if kt[hbm_key][0] else None
     if args.traffic and roof is not None:
         roof["traffic"] = args.traffic
     res = {
@@ -314,6 +337,7 @@ def run_ours(args, world, rank, local):
         "learned_coarse": learned,
         "kernel_ms": {k: dict(launches=v[0], total_ms=round(v[1], 3)) for k, v in kt.items()},
         "roofline": roof,
+        "roofline_hbm": roof_hbm,
         "clocks": clk,
         "e2e": {"value": E * args.steps / e2e_s, "unit": "elements/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
@@ -358,11 +382,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="cfg2", choices=sorted(CONFIGS))
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "mixed-trace", "fp64"],
-                    help="mixed: FP32 assembly + FP64 full-system refinement; mixed-trace: FP64 assembly, "
-                         "FP32 Krylov inside FP64 trace-system refinement; fp64: plain FP64")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "mixed-full"],
+                    help="mixed: FP64 assembly, FP32 CG with FP64 reliable updates of the trace residual; "
+                         "fp64: FP64 throughout; mixed-full: FP32 element condensation inside FP64 "
+                         "refinement of the full HDG system")
     ap.add_argument("--rtol", type=float, default=1e-10,
-                    help="fp64: trace-system relative residual; mixed: full HDG system relative residual")
+                    help="relative FP64 residual of the trace system (mixed-full: of the full HDG system)")
     ap.add_argument("--inner-rtol", type=float, default=1e-5)
     ap.add_argument("--precond", default="twolevel", choices=["twolevel", "bj"],
                     help="two-level (block Jacobi + vertex coarse space) or block Jacobi alone")
@@ -370,7 +395,7 @@ def main():
     ap.add_argument("--coarse-rtol", type=float, default=0.3, help="Chebyshev coarse-solve reduction target")
     ap.add_argument("--coarse", default="learned", choices=["learned", "chebyshev"],
                     help="coarse solve of the two-level preconditioner: trained polynomial or Chebyshev")
-    ap.add_argument("--coarse-degree", type=int, default=6, help="degree of the learned coarse polynomial")
+    ap.add_argument("--coarse-degree", type=int, default=8, help="degree of the learned coarse polynomial")
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
