@@ -178,6 +178,8 @@ struct AffLayout {
   static constexpr int FQ = BW + N * LW;         // NI
   static constexpr int IDG = FQ + NI;            // N     1 / L[k][k]
   static constexpr int WARP = (IDG + N + 1) & ~1;
+  // the geometry scratch (Jacobian entries) lives in AM and BW before they are built
+  static_assert(N * N + N * LW >= D * D + F * (D - 1) * D, "geometry scratch does not fit");
 };
 
 template <int D, int P, int EPC>
@@ -249,14 +251,24 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
     }
     __syncwarp();
     // ------------------------------------------------------ geometry
+    // Jacobian entries J[r][s] (first IP) and face Jacobian entries, one per lane
+    double* jw = Am;  // scratch: D*D volume + F*(D-1)*D face entries (A is built later)
+    for (int e2 = t; e2 < D * D + F * DM * D; e2 += 32) {
+      double acc = 0.0;
+      if (e2 < D * D) {
+        const int r = e2 / D, c = e2 % D;
+        for (int i = 0; i < N; ++i) acc += dphi[i * D + r] * X[i * D + c];
+      } else {
+        const int q = e2 - D * D, f = q / (DM * D), r = (q / D) % DM, c = q % D;
+        for (int i = 0; i < NF; ++i) acc += fdphi[i * DM + r] * X[sFN[f * NF + i] * D + c];
+      }
+      jw[e2] = acc;
+    }
+    __syncwarp();
     if (t == 0) {
       double J[D][D];
       for (int r = 0; r < D; ++r)
-        for (int s = 0; s < D; ++s) {
-          double acc = 0.0;
-          for (int i = 0; i < N; ++i) acc += dphi[i * D + r] * X[i * D + s];  // first IP
-          J[r][s] = acc;
-        }
+        for (int c = 0; c < D; ++c) J[r][c] = jw[r * D + c];
       double det;
       if (D == 2) {
         det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
@@ -284,13 +296,10 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
       sc[0] = det;
     } else if (t >= 1 && t <= F) {
       const int f = t - 1;
+      const double* jf = jw + D * D + f * DM * D;
       double Jf[D - 1][D];
       for (int r = 0; r < DM; ++r)
-        for (int s = 0; s < D; ++s) {
-          double acc = 0.0;
-          for (int i = 0; i < NF; ++i) acc += fdphi[i * DM + r] * X[sFN[f * NF + i] * D + s];  // first face IP
-          Jf[r][s] = acc;
-        }
+        for (int c = 0; c < D; ++c) Jf[r][c] = jf[r * D + c];
       double nv[D], ds;
       if (D == 2) {
         ds = sqrt(Jf[0][0] * Jf[0][0] + Jf[0][1] * Jf[0][1]);
@@ -356,13 +365,23 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
       }
     }
     // ----------------------------------------------- tau face mass Tm_f
-    for (int idx = t; idx < F * NF * NF; idx += 32) {
-      const int f = idx / (NF * NF), ab = idx % (NF * NF);
-      const double* tf = tTf + ab * NF;
+    // symmetric in (a, b): the upper triangle, mirrored
+    constexpr int NT = NF * (NF + 1) / 2;
+    for (int idx = t; idx < F * NT; idx += 32) {
+      const int f = idx / NT;
+      int q = idx % NT, a = 0;
+      while (q >= NF - a) {
+        q -= NF - a;
+        ++a;
+      }
+      const int b = a + q;
+      const double* tf = tTf + (a * NF + b) * NF;
       double acc = 0.0;
 #pragma unroll
       for (int c = 0; c < NF; ++c) acc += tau[f * NF + c] * __ldg(tf + c);
-      Tm[idx] = area[f] * acc;
+      acc *= area[f];
+      Tm[(f * NF + a) * NF + b] = acc;
+      Tm[(f * NF + b) * NF + a] = acc;
     }
     // source at the integration points: f(x_q) dV_q
     for (int q = t; q < NI; q += 32) {
@@ -380,8 +399,13 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
     }
     __syncwarp();
     // ------------------------------------------------- A, B and f_u
-    for (int ij = t; ij < N * N; ij += 32) {
-      const int i = ij / N, j = ij % N;
+    for (int lij = t; lij < N * (N + 1) / 2; lij += 32) {
+      // lower triangle i >= j, mirrored (A is symmetric)
+      int i = (int)((sqrtf(8.0f * lij + 1.0f) - 1.0f) * 0.5f);
+      while (i * (i + 1) / 2 > lij) --i;
+      while ((i + 1) * (i + 2) / 2 <= lij) ++i;
+      const int j = lij - i * (i + 1) / 2;
+      const int ij = i * N + j;
       double ts = 0.0;
       for (int f = 0; f < F; ++f) {
         const int a = sPos[f * N + i], b = sPos[f * N + j];
@@ -393,6 +417,7 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
       double v = dts * (ts + detJ * st);
       if (p.dt > 0.0) v += detJ * __ldg(tM + ij);
       Am[ij] = v;
+      Am[j * N + i] = v;
     }
     for (int ic = t; ic < N * LL; ic += 32) {
       const int i = ic / LL, c = ic % LL;
@@ -440,14 +465,18 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
     }
     if (bad && t == 0) atomicCAS(p.status, 0, 1);
     // ---------------------- forward substitution: [W | y0] = L^{-1} [B | f_u]
-    for (int c = t; c < LW; c += 32) {
-      for (int i = 0; i < N; ++i) {
-        double v = BW[i * LW + c];
-        for (int m = 0; m < i; ++m) v -= Am[i * N + m] * BW[m * LW + c];
-        BW[i * LW + c] = v * idg[i];
+    // row-oriented: after row k is final, every lane updates (row, column)
+    // pairs below it, so all 32 lanes stay busy whatever the column count
+    for (int k = 0; k < N; ++k) {
+      for (int c = t; c < LW; c += 32) BW[k * LW + c] *= idg[k];
+      __syncwarp();
+      const int rows = N - k - 1;
+      for (int ic = t; ic < rows * LW; ic += 32) {
+        const int i = k + 1 + ic / LW, c = ic % LW;
+        BW[i * LW + c] -= Am[i * N + k] * BW[k * LW + c];
       }
+      __syncwarp();
     }
-    __syncwarp();
     // ------------------ S = C + dt W^T W (upper triangle, mirrored), S0 = W^T y0
     {
       double* Sg = (double*)p.S + e * LL * LL;
@@ -486,18 +515,18 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
     }
     __syncwarp();
     // ------------- back substitution: U = -dt L^{-T} W, U0 = L^{-T} y0 (in place)
-    for (int c = t; c < LW; c += 32) {
-      const double sgn = c < LL ? -dts : 1.0;
-      for (int i = N - 1; i >= 0; --i) {
-        double v = BW[i * LW + c];
-        for (int m = i + 1; m < N; ++m) v -= Am[m * N + i] * BW[m * LW + c];
-        BW[i * LW + c] = v * idg[i];
+    for (int k = N - 1; k >= 0; --k) {
+      for (int c = t; c < LW; c += 32) BW[k * LW + c] *= idg[k];
+      __syncwarp();
+      // rows above k: BW[i] -= L[k][i] * x_k
+      for (int ic = t; ic < k * LW; ic += 32) {
+        const int i = ic / LW, c = ic % LW;
+        BW[i * LW + c] -= Am[k * N + i] * BW[k * LW + c];
       }
-      for (int i = 0; i < N; ++i) BW[i * LW + c] *= sgn;
+      __syncwarp();
     }
-    __syncwarp();
     double* Ug = (double*)p.U + e * N * LL;
-    for (int idx = t; idx < N * LL; idx += 32) Ug[idx] = BW[(idx % N) * LW + idx / N];
+    for (int idx = t; idx < N * LL; idx += 32) Ug[idx] = -dts * BW[(idx % N) * LW + idx / N];
     for (int i = t; i < N; i += 32) ((double*)p.U0)[e * N + i] = BW[i * LW + LL];
     __syncwarp();
   }
