@@ -785,7 +785,7 @@ cudaError_t coarse_setup(CoarseSolver* cs, const T* S, int maxDegree, double tar
   }
   lanczos_scale<<<g, kT, 0, s>>>(c->nV, v, (float)(1.0 / nrm));
   std::vector<double> al, be;
-  const int m = (int)std::min<int64_t>(40, c->nV);
+  const int m = (int)std::min<int64_t>(30, c->nV);
   double beta = 0.0;
   for (int j = 0; j < m; ++j) {
     // one host round trip per step: alpha and |w|^2 from the same pass

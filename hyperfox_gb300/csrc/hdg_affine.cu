@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
       }
       double nn = 0.0;
       for (int a = 0; a < D; ++a) nn += nv[a] * nv[a];
-      nn = 1.0 / sqrt(nn);
+      nn = rsqrt(nn);
       double prod = 0.0;
       const int v0 = sFN[f * NF], vn = sOpp[f];
       for (int a = 0; a < D; ++a) {
@@ -447,8 +447,8 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
     for (int k = 0; k < N; ++k) {
       const double akk = Am[k * N + k];
       if (!(akk > 0.0)) bad = true;
-      const double lkk = sqrt(akk > 0.0 ? akk : 1.0);
-      const double il = 1.0 / lkk;
+      const double il = rsqrt(akk > 0.0 ? akk : 1.0);  // 1 / L[k][k]
+      const double lkk = (akk > 0.0 ? akk : 1.0) * il;
       __syncwarp();
       if (t == 0) {
         Am[k * N + k] = lkk;
@@ -532,13 +532,17 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
   }
 }
 
-// Recovery for the affine path: sol = U lambda + U0, flux = -Xu sol - Xl lambda.
+// Recovery for the affine path: sol = U lambda + U0, flux = -Xu sol - Xl lambda,
+// with the products shared: t_s = M^{-1} C_s sol and l_f = L_f lambda_f once
+// per element, then flux(i, d) = -sum_s G[d][s] t_s[i] + sum_f g_f[d] l_f[i].
 template <int D, int P>
 __global__ void recover_affine(RecoverParams p, const double* __restrict__ atab, const double* __restrict__ geo) {
   using L = AffLayout<D, P>;
   constexpr int N = L::N, NF = L::NF, F = L::F, LL = L::LL;
   __shared__ double lam[LL];
   __shared__ double sol[N];
+  __shared__ double ts[D * N];
+  __shared__ double lf[F * N];
   __shared__ double ge[D * D + F * D];
   const double* tD = atab + L::A_D;
   const double* tL = atab + L::A_L;
@@ -557,20 +561,25 @@ __global__ void recover_affine(RecoverParams p, const double* __restrict__ atab,
       sol[r] = acc;
       p.sol[e * N + r] = acc;
     }
+    for (int fi = threadIdx.x; fi < F * N; fi += blockDim.x) {
+      const int f = fi / N, i = fi % N;
+      double acc = 0.0;
+      for (int b = 0; b < NF; ++b) acc += __ldg(tL + (f * N + i) * NF + b) * lam[f * NF + b];
+      lf[fi] = acc;
+    }
+    __syncthreads();
+    for (int si = threadIdx.x; si < D * N; si += blockDim.x) {
+      const int sd = si / N, i = si % N;
+      double acc = 0.0;
+      for (int j = 0; j < N; ++j) acc += __ldg(tD + (sd * N + i) * N + j) * sol[j];
+      ts[si] = acc;
+    }
     __syncthreads();
     for (int r = threadIdx.x; r < N * D; r += blockDim.x) {
       const int i = r / D, d = r % D;  // flux node-major (i, d)
       double acc = 0.0;
-      for (int s = 0; s < D; ++s) {
-        double ds = 0.0;
-        for (int j = 0; j < N; ++j) ds += __ldg(tD + (s * N + i) * N + j) * sol[j];
-        acc -= ge[d * D + s] * ds;
-      }
-      for (int f = 0; f < F; ++f) {
-        double lf = 0.0;
-        for (int b = 0; b < NF; ++b) lf += __ldg(tL + (f * N + i) * NF + b) * lam[f * NF + b];
-        acc += ge[D * D + f * D + d] * lf;
-      }
+      for (int sd = 0; sd < D; ++sd) acc -= ge[d * D + sd] * ts[sd * N + i];
+      for (int f = 0; f < F; ++f) acc += ge[D * D + f * D + d] * lf[f * N + i];
       p.flux[e * N * D + r] = acc;
     }
     __syncthreads();

@@ -44,6 +44,46 @@ __global__ void scatter_values(ScatterParams p, const int* brow, int64_t nBlocks
   }
 }
 
+// Same values, one warp per block: the warp inverts the (at most two) face
+// permutations once into shared memory, then writes the block's NF*NF values
+// with consecutive lanes on consecutive (column-major) positions.
+constexpr int kScatterWarps = 8;
+__global__ void __launch_bounds__(32 * kScatterWarps) scatter_values_w(ScatterParams p) {
+  const int NF = p.NF, LL = p.LL, F = p.F;
+  __shared__ uint8_t inv[kScatterWarps][2][2][16];  // [warp][contribution][row, col][face position]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t nW = (int64_t)gridDim.x * kScatterWarps;
+  for (int64_t k = (int64_t)blockIdx.x * kScatterWarps + warp; k < p.nBlocks; k += nW) {
+    const int c0 = p.src0[k], c1 = p.src1[k];
+    const int l0 = p.loc0[k], l1 = p.loc1[k];
+    {
+      const int sIdx = lane >> 4, q = lane & 15;
+      const int c = sIdx == 0 ? c0 : c1;
+      const int loc = sIdx == 0 ? l0 : l1;
+      if (q < NF && c >= 0) {
+        const int li = loc >> 4, lj = loc & 15;
+        inv[warp][sIdx][0][p.perm[((int64_t)c * F + li) * NF + q]] = (uint8_t)q;
+        inv[warp][sIdx][1][p.perm[((int64_t)c * F + lj) * NF + q]] = (uint8_t)q;
+      }
+    }
+    __syncwarp();
+    for (int idx = lane; idx < NF * NF; idx += 32) {
+      const int a = idx % NF, b = idx / NF;
+      double v = 0.0;
+      if (c0 >= 0) {
+        const int li = l0 >> 4, lj = l0 & 15;
+        v += p.S[(int64_t)c0 * LL * LL + (li * NF + inv[warp][0][0][a]) + (int64_t)(lj * NF + inv[warp][0][1][b]) * LL];
+      }
+      if (c1 >= 0) {
+        const int li = l1 >> 4, lj = l1 & 15;
+        v += p.S[(int64_t)c1 * LL * LL + (li * NF + inv[warp][1][0][a]) + (int64_t)(lj * NF + inv[warp][1][1][b]) * LL];
+      }
+      p.val[k * NF * NF + idx] = v;  // block k column-major: (a, b) at b*NF + a
+    }
+    __syncwarp();
+  }
+}
+
 __global__ void scatter_rhs(ScatterParams p) {
   const int NF = p.NF, LL = p.LL, F = p.F;
   const int64_t total = (int64_t)p.nFaces * NF;
@@ -130,7 +170,13 @@ cudaError_t launch_block_rows(const int64_t* browptr, int nFaces, int* brow, cud
 }
 
 cudaError_t launch_scatter(const ScatterParams& p, cudaStream_t s) {
-  scatter_values<<<grid_for(p.nBlocks * p.NF * p.NF, 256), 256, 0, s>>>(p, p.brow, p.nBlocks);
+  if (p.NF <= 16) {
+    int64_t g = (p.nBlocks + kScatterWarps - 1) / kScatterWarps;
+    if (g > 152 * 64) g = 152 * 64;
+    scatter_values_w<<<(unsigned)(g < 1 ? 1 : g), 32 * kScatterWarps, 0, s>>>(p);
+  } else {
+    scatter_values<<<grid_for(p.nBlocks * p.NF * p.NF, 256), 256, 0, s>>>(p, p.brow, p.nBlocks);
+  }
   scatter_rhs<<<grid_for((int64_t)p.nFaces * p.NF, 256), 256, 0, s>>>(p);
   return cudaGetLastError();
 }
