@@ -84,6 +84,8 @@ struct hfx_ctx {
   uint8_t* d_isBnd = nullptr;
   int64_t* d_browptr = nullptr;
   int* d_bcol = nullptr;
+  int* d_hidx = nullptr;     // symmetric half storage map of the face blocks
+  int64_t nHalf = 0;
   int* d_brow = nullptr;
   int *d_src0 = nullptr, *d_src1 = nullptr;
   uint8_t *d_loc0 = nullptr, *d_loc1 = nullptr;
@@ -392,6 +394,31 @@ int hfx_mesh_upload(hfx_ctx* c, int dim, int order, int nNodes, const double* co
   HFX_CUDA(c, upload(m, &c->d_loc0, c->bp.loc0.data(), c->bp.loc0.size(), s));
   HFX_CUDA(c, upload(m, &c->d_loc1, c->bp.loc1.data(), c->bp.loc1.size(), s));
   HFX_CUDA(c, dalloc(m, &c->d_brow, c->bp.col.size()));
+  {
+    // half storage of symmetric trace operators: block (f, g >= f) stored, (g < f) mirrored
+    const std::vector<int64_t>& rp = c->bp.rowptr;
+    const std::vector<int>& cl = c->bp.col;
+    std::vector<int> hidx(cl.size(), 0);
+    int64_t nh = 0;
+    bool ok = cl.size() < (size_t)2147483647;
+    for (int f = 0; f < c->topo.nFaces && ok; ++f)
+      for (int64_t k = rp[f]; k < rp[f + 1]; ++k) {
+        const int g = cl[k];
+        if (g >= f) {
+          hidx[k] = (int)nh++;
+        } else {
+          auto it = std::lower_bound(cl.begin() + rp[g], cl.begin() + rp[g + 1], f);
+          if (it == cl.begin() + rp[g + 1] || *it != f) {
+            ok = false;  // pattern not structurally symmetric
+            break;
+          }
+          hidx[k] = -(hidx[it - cl.begin()] + 1);
+        }
+      }
+    c->nHalf = ok ? nh : 0;
+    c->d_hidx = nullptr;
+    if (ok) HFX_CUDA(c, upload(m, &c->d_hidx, hidx.data(), hidx.size(), s));
+  }
   {
     std::vector<double> atab;
     c->d_atab = nullptr;
@@ -1024,6 +1051,8 @@ static int ensure_workspace(hfx_ctx* c, bool mixed, int restart) {
   }
   if (mixed && !c->wsMixed) {
     HFX_CUDA(c, dalloc(m, &w.val32, nnz));
+    w.val32h = nullptr;
+    if (c->nHalf > 0) HFX_CUDA(c, dalloc(m, &w.val32h, (size_t)c->nHalf * NF * NF));
     HFX_CUDA(c, dalloc(m, &w.pc32, (size_t)c->topo.nFaces * NF * NF));
     HFX_CUDA(c, dalloc(m, &w.r32, n));
     HFX_CUDA(c, dalloc(m, &w.z32, n));
@@ -1156,6 +1185,10 @@ int hfx_solve(hfx_ctx* c, const hfx_solve_opts* opts, double* trace, hfx_solve_i
   TraceSolveArgs a{};
   a.dim = c->dim;
   a.A = TraceView{c->topo.nFaces, c->re.nNodesFace, c->d_browptr, c->d_bcol, c->d_isBnd};
+  if (method == HFX_KSP_CG && c->kappaCellConstant) {
+    a.A.hidx = c->d_hidx;  // symmetric operator: FP32 copy in half storage
+    a.A.nHalf = c->nHalf;
+  }
   a.val = c->d_val;
   a.rhs = c->d_rhs;
   a.x = c->d_trace;

@@ -138,6 +138,69 @@ __device__ __forceinline__ T row_dot(const T* __restrict__ val, int64_t b0, int 
   return acc;
 }
 
+// Row of the face block-row from the symmetric half storage: stored blocks are
+// read by column (coalesced), mirrored ones by row (the 400-byte block comes
+// through L1 once).
+template <int NF>
+__device__ __forceinline__ float row_dot_half(const float* __restrict__ valh, const int* __restrict__ hidx, int64_t b0,
+                                              int nb, int a, const float* xs) {
+  float acc = 0.f;
+  for (int k = 0; k < nb; ++k) {
+    const int h = hidx[b0 + k];
+    if (h >= 0) {
+      const float* blk = valh + (int64_t)h * NF * NF + a;
+#pragma unroll
+      for (int b = 0; b < NF; ++b) acc = fmaf(__ldg(blk + b * NF), xs[k * NF + b], acc);
+    } else {
+      const float* blk = valh + (int64_t)(-h - 1) * NF * NF + (int64_t)a * NF;
+#pragma unroll
+      for (int b = 0; b < NF; ++b) acc = fmaf(__ldg(blk + b), xs[k * NF + b], acc);
+    }
+  }
+  return acc;
+}
+
+// K1 of CG on the FP32 half storage (mixed precision, symmetric A').
+template <int NF, int NBMAX>
+__global__ void __launch_bounds__(kThreads) cg_spmv_half(TraceView A, const float* __restrict__ valh,
+                                                         const float* __restrict__ z, const float* __restrict__ pold,
+                                                         float* __restrict__ pnew, float* __restrict__ q, CgState* st,
+                                                         double* partials, int first) {
+  __shared__ float xsh[kThreads / 32][RowCfg<NF, NBMAX>::FPW][RowCfg<NF, NBMAX>::NPOS];
+  if (st->done) return;
+  const float beta = first ? 0.f : (float)st->beta;
+  HFX_FACE_SLOTS(NF)
+  double pq = 0.0;
+  for (int64_t fb = ((int64_t)blockIdx.x * (kThreads / 32) + warp) * FPW; fb < A.nFaces; fb += faceStride) {
+    const int64_t f = fb + slot;
+    const bool act = laneUsed && f < A.nFaces;
+    const int64_t b0 = act ? A.browptr[f] : 0;
+    const int nb = act ? (int)(A.browptr[f + 1] - b0) : 0;
+    float* xs = laneUsed ? xsh[warp][slot] : nullptr;
+    if (act) gather_x<float, NF, NBMAX, false, true>(A, b0, nb, false, a, beta, z, pold, xs);
+    __syncwarp();
+    if (act) {
+      const float y = row_dot_half<NF>(valh, A.hidx, b0, nb, a, xs);
+      const int64_t i = f * NF + a;
+      const float pi = fmaf(beta, pold[i], z[i]);
+      pnew[i] = pi;
+      q[i] = y;
+      pq += (double)pi * (double)y;
+    }
+    __syncwarp();
+  }
+  double v[1] = {pq}, tot[1];
+  if (block_reduce_last<1>(v, partials, &st->ticket, tot) && threadIdx.x == 0) {
+    double pAp = tot[0];
+    if (!(pAp > 0.0) || !isfinite(pAp)) {
+      st->status = isfinite(pAp) ? 6 : 7;
+      st->done = 1;
+    } else {
+      st->alpha = st->rz / pAp;
+    }
+  }
+}
+
 // K1 of CG (see the file comment).
 template <typename T, int NF, int NBMAX, bool MASKED>
 __global__ void __launch_bounds__(kThreads) cg_spmv(TraceView A, const T* __restrict__ val,
@@ -424,7 +487,7 @@ __global__ void __launch_bounds__(kThreads) ref_residual(TraceView A, const doub
 template <int NF, int NBMAX>
 __global__ void __launch_bounds__(kThreads) prepare_system(TraceView A, const double* __restrict__ val,
                                                            const double* __restrict__ b, double* __restrict__ bS,
-                                                           float* __restrict__ val32) {
+                                                           float* __restrict__ val32, float* __restrict__ val32h = nullptr) {
   HFX_FACE_SLOTS(NF)
   for (int64_t fb = ((int64_t)blockIdx.x * (kThreads / 32) + warp) * FPW; fb < A.nFaces; fb += faceStride) {
     const int64_t f = fb + slot;
@@ -439,11 +502,15 @@ __global__ void __launch_bounds__(kThreads) prepare_system(TraceView A, const do
         int64_t idx = (b0 + k) * NF * NF + (int64_t)c * NF + a;
         double v = val[idx];
         if (!rowBnd && A.isBnd[g]) lift += v * b[(int64_t)g * NF + c];
-        if (val32) {
+        if (val32 || val32h) {
           float w;
           if (rowBnd) w = (g == (int)f && c == a) ? 1.0f : 0.0f;
           else w = A.isBnd[g] ? 0.0f : (float)(-v);
-          val32[idx] = w;
+          if (val32) val32[idx] = w;
+          if (val32h) {
+            const int h = A.hidx[b0 + k];
+            if (h >= 0) val32h[(int64_t)h * NF * NF + (int64_t)c * NF + a] = w;
+          }
         }
       }
     }
@@ -728,8 +795,10 @@ struct Driver {
     };
     // 1. system b', FP32 values if needed, preconditioner
     tm->begin(K_OTHER, s);
+    const bool half = a.mixed && A.hidx && a.ws.val32h;  // FP32 operator in symmetric half storage
     prepare_system<NF, NBMAX><<<gridS, kThreads, 0, s>>>(A, a.val, a.rhs, a.ws.bS,
-                                                           a.mixed ? a.ws.val32 : nullptr);
+                                                           a.mixed && !half ? a.ws.val32 : nullptr,
+                                                           half ? a.ws.val32h : nullptr);
     if (pcT > 0) {
       // the mixed-precision solve only applies the FP32 copy: invert in FP32
       if (a.mixed)
@@ -876,8 +945,12 @@ struct Driver {
             float* pold = (it & 1) ? p132 : p032;
             float* pnew = (it & 1) ? p032 : p132;
             tm->begin(K_SPMV32, s);
-            cg_spmv<float, NF, NBMAX, false><<<gridF32, kThreads, 0, s>>>(A, a.ws.val32, z32, pold, pnew, q32, st,
-                                                                          partials, first ? 1 : 0);
+            if (half)
+              cg_spmv_half<NF, NBMAX><<<gridF32, kThreads, 0, s>>>(A, a.ws.val32h, z32, pold, pnew, q32, st, partials,
+                                                                    first ? 1 : 0);
+            else
+              cg_spmv<float, NF, NBMAX, false><<<gridF32, kThreads, 0, s>>>(A, a.ws.val32, z32, pold, pnew, q32, st,
+                                                                            partials, first ? 1 : 0);
             tm->end(K_SPMV32, s);
             first = false;
             if (twoLevel) {

@@ -16,6 +16,11 @@ struct TraceView {
   const int64_t* browptr;
   const int* bcol;
   const uint8_t* isBnd;  // Dirichlet (boundary) faces
+  // Symmetric half storage of the FP32 operator (optional): for block k of row
+  // f, hidx[k] >= 0 is the stored block (f, g >= f), column-major; hidx[k] < 0
+  // means block (g, f) stored at -hidx[k]-1, read transposed.
+  const int* hidx = nullptr;
+  int64_t nHalf = 0;
 };
 
 // Device-resident solver scalars. Reductions finish in the last block, which
@@ -31,6 +36,7 @@ struct CgState {
 struct TraceWorkspace {
   double *bS, *r, *z, *p0, *p1, *q, *pc64;
   float *val32, *pc32, *r32, *z32, *p032, *p132, *q32, *d32, *rhs32, *bS32;
+  float* val32h;  // symmetric half storage of A' (FP32), nHalf blocks
   double* partials;
   CgState* state;
   // GMRES: Krylov bases (restart+1 vectors) and the small device vector of coefficients
