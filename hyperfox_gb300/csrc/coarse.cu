@@ -433,6 +433,10 @@ __device__ __forceinline__ void grid_barrier(unsigned* count, unsigned target, i
   __syncthreads();
 }
 
+// Four lanes per coarse row: the restriction splits the row's incident faces
+// and every step splits the ELL slots between them (a shuffle sum joins them),
+// which shortens each lane's chain of dependent L2 loads four-fold.
+constexpr int kCoarseLanes = 4;
 template <typename T>
 __global__ void __launch_bounds__(512) coarse_solve_coop(CoarseDev c, const T* __restrict__ r, const int* skip,
                                                          ChebSchedule cs) {
@@ -440,36 +444,64 @@ __global__ void __launch_bounds__(512) coarse_solve_coop(CoarseDev c, const T* _
   // barrier[0] counts arrivals and starts every launch at 0: the last block to
   // leave (counted in barrier[1]) resets both, after every wait has finished
   const int d = c.dim, NF = c.NF;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  const int64_t v0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  for (int64_t v = v0; v < c.nV; v += stride) {
+  const int sub = threadIdx.x % kCoarseLanes;
+  const int64_t groups = (int64_t)gridDim.x * (blockDim.x / kCoarseLanes);
+  const int64_t g0 = (int64_t)blockIdx.x * (blockDim.x / kCoarseLanes) + threadIdx.x / kCoarseLanes;
+  // rows are walked in whole warps so that every lane reaches the shuffles
+  const int64_t nVr = (c.nV + 7) / 8 * 8;
+  for (int64_t v = g0; v < nVr; v += groups) {
     float s = 0.f;
-    for (int j = c.rptr[v]; j < c.rptr[v + 1]; ++j) {
-      const int fk = c.ridx[j];
-      const int64_t f = fk / d;
-      const int k = fk - (int)f * d;
-      if (c.isBnd[f]) continue;
-      const T* rf = r + f * NF;
-      for (int a = 0; a < NF; ++a) s = fmaf(c.Wf[a * d + k], (float)rf[a], s);
+    if (v < c.nV)
+      for (int j = c.rptr[v] + sub; j < c.rptr[v + 1]; j += kCoarseLanes) {
+        const int fk = c.ridx[j];
+        const int64_t f = fk / d;
+        const int k = fk - (int)f * d;
+        if (c.isBnd[f]) continue;
+        const T* rf = r + f * NF;
+        for (int a = 0; a < NF; ++a) s = fmaf(c.Wf[a * d + k], (float)rf[a], s);
+      }
+    s += __shfl_xor_sync(0xffffffffu, s, 1);
+    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    if (sub == 0 && v < c.nV) {
+      c.rc[v] = s;
+      c.cr[v] = s;
+      c.yc[v] = 0.f;
+      c.cd0[v] = c.dinv[v] * s * cs.d0scale;
     }
-    c.rc[v] = s;
-    c.cr[v] = s;
-    c.yc[v] = 0.f;
-    c.cd0[v] = c.dinv[v] * s * cs.d0scale;
   }
   float* dk = c.cd0;
   float* dn = c.cd1;
   for (int k = 0; k < cs.degree; ++k) {
     grid_barrier(c.barrier, (unsigned)(k + 1) * gridDim.x, c.error);
     const bool last = k + 1 == cs.degree;
-    for (int64_t v = v0; v < c.nV; v += stride) {
-      const float dv = __ldcg(dk + v);
-      c.yc[v] += dv;
-      if (last) continue;
-      const float y = ell_row(c, v, dk);
-      const float rr = c.cr[v] - y;
-      c.cr[v] = rr;
-      dn[v] = cs.c1[k] * dv + cs.c2[k] * c.dinv[v] * rr;
+    for (int64_t v = g0; v < nVr; v += groups) {
+      float y = 0.f;
+      if (!last && v < c.nV) {
+        int cc[4];
+        float aa[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int slot = sub + u * kCoarseLanes;
+          const bool in = slot < c.ellW;
+          cc[u] = in ? c.ellCol[(int64_t)slot * c.nV + v] : (int)v;
+          aa[u] = in ? c.ellVal[(int64_t)slot * c.nV + v] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) y = fmaf(aa[u], __ldcg(dk + cc[u]), y);
+        for (int slot = sub + 16; slot < c.ellW; slot += kCoarseLanes)
+          y = fmaf(c.ellVal[(int64_t)slot * c.nV + v], __ldcg(dk + c.ellCol[(int64_t)slot * c.nV + v]), y);
+      }
+      y += __shfl_xor_sync(0xffffffffu, y, 1);
+      y += __shfl_xor_sync(0xffffffffu, y, 2);
+      if (sub == 0 && v < c.nV) {
+        const float dv = __ldcg(dk + v);
+        c.yc[v] += dv;
+        if (!last) {
+          const float rr = c.cr[v] - y;
+          c.cr[v] = rr;
+          dn[v] = cs.c1[k] * dv + cs.c2[k] * c.dinv[v] * rr;
+        }
+      }
     }
     float* t = dk;
     dk = dn;
@@ -834,8 +866,9 @@ cudaError_t coarse_setup(CoarseSolver* cs, const T* S, int maxDegree, double tar
   if (coop && c->barrier && K <= kMaxDegree &&
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, coarse_solve_coop<double>, 512, 0) == cudaSuccess &&
       perSM >= 1) {
-    int64_t want = (c->nV + 511) / 512;
-    int g = (int)std::min<int64_t>(want, (int64_t)nsm);  // one block per SM at most
+    // 128 rows per block of 512 threads; every block must be resident at once
+    int64_t want = (c->nV + 127) / 128;
+    int g = (int)std::min<int64_t>(want, (int64_t)nsm * std::min(perSM, 2));
     cs->coopGrid = std::max(g, 1);
   }
   cs->ready = true;

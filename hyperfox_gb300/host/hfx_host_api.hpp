@@ -57,6 +57,10 @@ struct GpuSolverOpts {  // PetscOpts (PetscOpts.h:8-29) analogue
   double rtol = 1e-6;
   int maxits = 1000;
   int restart = 30;
+  // HFX_PC_TWOLEVEL only: coarse solve, and the degree of the learned coarse
+  // polynomial GpuHDGSolver trains on its first solve (HFX_COARSE_LEARNED)
+  int coarseMode = HFX_COARSE_CHEBYSHEV;
+  int learnedDegree = 8;
 };
 
 class GpuLinAlgebraInterface {
@@ -136,6 +140,7 @@ class GpuLinAlgebraInterface {
   }
   int getNumDofs() const { return nDOFs; }
   hfx_solve_info lastInfo{};
+  hfx_train_info trainInfo{};
 
  private:
   void vals(const char* m, int nr, const int* r, int nc, const int* cc, const double* v, int insert) {
@@ -269,11 +274,18 @@ class GpuHDGSolver {
     o.maxits = opts_.maxits;
     o.restart = opts_.restart;
     o.method = opts_.method;
+    o.coarse_mode = opts_.coarseMode;
+    if (opts_.precond == HFX_PC_TWOLEVEL && opts_.coarseMode == HFX_COARSE_LEARNED && !trained_) {
+      // the learned coarse solve is trained once per mesh, on this system's own coarse errors
+      dev_->check(hfx_coarse_train(dev_->ctx(), opts_.learnedDegree, 16, 300, &trainInfo), "HDGSolver", "solve");
+      trained_ = true;
+    }
     dev_->check(hfx_solve(dev_->ctx(), &o, fields_->at("Trace")->values.data(), &lastInfo), "HDGSolver", "solve");
     dev_->check(hfx_recover(dev_->ctx(), fields_->at("Solution")->values.data(), fields_->at("Flux")->values.data()),
                 "HDGSolver", "solve");
   }
   hfx_solve_info lastInfo{};
+  hfx_train_info trainInfo{};
 
  private:
   Device* dev_;
@@ -282,7 +294,7 @@ class GpuHDGSolver {
   HDGDiffusionSource* model_ = nullptr;
   DirichletModel* bnd_ = nullptr;
   GpuSolverOpts opts_;
-  bool haveLin_ = false, initialized_ = false, allocated_ = false, assembled_ = false;
+  bool haveLin_ = false, initialized_ = false, allocated_ = false, assembled_ = false, trained_ = false;
 };
 
 }  // namespace gpu

@@ -146,6 +146,26 @@ int main() {
     for (double v : sol.values) CHECK(std::fabs(v - 3.0) < 1e-12);
     for (double v : flux.values) CHECK(std::fabs(v) < 1e-11);
     for (double v : lambda.values) CHECK(std::fabs(v - 3.0) < 1e-12);
+    // the same solve with the two-level preconditioner, mixed precision and the learned coarse solve
+    GpuSolverOpts o2 = o;
+    o2.precond = HFX_PC_TWOLEVEL;
+    o2.precision = HFX_PREC_MIXED;
+    o2.coarseMode = HFX_COARSE_LEARNED;
+    o2.learnedDegree = 4;
+    o2.rtol = 1e-13;
+    GpuHDGSolver s2(&dev);
+    s2.setMesh(&m);
+    s2.setFieldMap(&fm);
+    s2.setLinSystem(o2);
+    s2.setModel(&lap);
+    s2.setBoundaryModel(&dirMod);
+    s2.initialize();
+    s2.allocate();
+    s2.assemble();
+    s2.solve();
+    CHECK(s2.lastInfo.status == 0 && s2.lastInfo.fallback == 0);
+    for (double v : sol.values) CHECK(std::fabs(v - 3.0) < 1e-11);
+    for (double v : lambda.values) CHECK(std::fabs(v - 3.0) < 1e-11);
   }
   std::printf("%s (%d failures)\n", failures ? "FAIL" : "OK", failures);
   return failures ? 1 : 0;
