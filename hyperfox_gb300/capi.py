@@ -34,6 +34,7 @@ EXPORTED = [
     "hfx_ctx_create", "hfx_ctx_destroy", "hfx_last_error", "hfx_version",
     "hfx_refel_query", "hfx_refel_tables",
     "hfx_mesh_upload", "hfx_mesh_sizes", "hfx_mesh_topology", "hfx_mesh_compute_topology",
+    "hfx_gmsh_read", "hfx_mesh_high_order", "hfx_mesh_io_error",
     "hfx_set_tau", "hfx_set_kappa", "hfx_set_source", "hfx_set_dirichlet", "hfx_set_time_scheme",
     "hfx_ip_coords", "hfx_assemble", "hfx_assemble_ex", "hfx_set_assembly_path", "hfx_assembly_info", "hfx_get_condensed", "hfx_get_csr",
     "hfx_solve_opts_default", "hfx_solve", "hfx_recover", "hfx_coarse_operator", "hfx_coarse_train",
@@ -117,6 +118,9 @@ def load(path=LIB_PATH):
         "hfx_coarse_train": ([vp, ip, ip, ip, ctypes.POINTER(TrainInfo)], ip),
         "hfx_coarse_loss_grad": ([vp, ip, vp, ip, vp, vp, vp], ip),
         "hfx_set_assembly_path": ([vp, ip], ip),
+        "hfx_gmsh_read": ([ctypes.c_char_p, ip, vp, vp, vp, vp], ip),
+        "hfx_mesh_high_order": ([ip, ip, ip, vp, ip, vp, vp, vp, vp], ip),
+        "hfx_mesh_io_error": ([], ctypes.c_char_p),
         "hfx_assembly_info": ([vp, vp], ip),
         "hfx_la_create": ([vp, ctypes.POINTER(vp)], ip),
         "hfx_la_destroy": ([vp], ip),
@@ -187,6 +191,40 @@ def mesh_topology(dim, order, cells):
     if rc:
         raise HfxError(rc, "mesh_compute_topology")
     return c2f, f2c, faces, bnd
+
+
+def gmsh_read(path, dim):
+    """Linear simplex mesh of dimension dim from a gmsh 2.2 ASCII file (host only)."""
+    L = load()
+    nn, nc = ctypes.c_int(), ctypes.c_int()
+    rc = L.hfx_gmsh_read(str(path).encode(), dim, ctypes.byref(nn), ctypes.byref(nc), None, None)
+    if rc:
+        raise HfxError(rc, "gmsh_read: " + L.hfx_mesh_io_error().decode())
+    coords = np.zeros((nn.value, dim))
+    cells = np.zeros((nc.value, dim + 1), np.int32)
+    rc = L.hfx_gmsh_read(str(path).encode(), dim, ctypes.byref(nn), ctypes.byref(nc), _p(coords), _p(cells))
+    if rc:
+        raise HfxError(rc, "gmsh_read: " + L.hfx_mesh_io_error().decode())
+    return coords, cells
+
+
+def mesh_high_order(dim, order, coords, cells):
+    """High-order nodes of a linear simplex mesh (host only): (coords [n][dim], cells [nCells][N])."""
+    L = load()
+    coords = np.ascontiguousarray(coords, np.float64)
+    cells = np.ascontiguousarray(cells, np.int32)
+    nn = ctypes.c_int()
+    args = (dim, order, coords.shape[0], _p(coords), cells.shape[0], _p(cells), ctypes.byref(nn))
+    rc = L.hfx_mesh_high_order(*args, None, None)
+    if rc:
+        raise HfxError(rc, "mesh_high_order: " + L.hfx_mesh_io_error().decode())
+    N = refel(dim, order)["nNodes"]
+    out_c = np.zeros((nn.value, dim))
+    out_e = np.zeros((cells.shape[0], N), np.int32)
+    rc = L.hfx_mesh_high_order(*args, _p(out_c), _p(out_e))
+    if rc:
+        raise HfxError(rc, "mesh_high_order: " + L.hfx_mesh_io_error().decode())
+    return out_c, out_e
 
 
 def solve_opts(**kw):

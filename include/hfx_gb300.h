@@ -144,6 +144,21 @@ int hfx_mesh_compute_topology(int dim, int order, int nCells, const int* cells, 
                               int* cell2face, int* face2cell, int* faces, int* boundary);
 int hfx_mesh_topology(hfx_ctx* ctx, int* cell2face, int* face2cell, int* faces, int* boundary);
 
+/* ---- mesh input (host, no GPU needed) ----------------------------------------
+ * Replaces tools/convertGmsh2H5HO.cpp:117-257,367-398 (gmsh reading through
+ * MOAB and high-order node construction) without MOAB. hfx_gmsh_read reads a
+ * gmsh .msh file (format 2.2, ASCII) and returns the linear simplex mesh of
+ * dimension dim: coords [nNodes][dim] (vertices used by the cells, in gmsh id
+ * order) and cells [nCells][dim+1] (0-based); call with coords == NULL for the
+ * sizes. hfx_mesh_high_order maps the reference nodes of order `order` into every
+ * linear cell and merges coincident nodes: coords [nNodes][dim], cells
+ * [nCells][N] in reference-node order, ready for hfx_mesh_upload (two-call
+ * likewise). hfx_mesh_io_error returns the last message of these two. */
+int hfx_gmsh_read(const char* path, int dim, int* nNodes, int* nCells, double* coords, int* cells);
+int hfx_mesh_high_order(int dim, int order, int nLinNodes, const double* linCoords, int nCells, const int* linCells,
+                        int* nNodes, double* coords, int* cells);
+const char* hfx_mesh_io_error(void);
+
 /* ---- fields (the HDGSolver field map) --------------------------------------
  * Tau: Face field, nVals 1 or 2 (double valued, side 0 = face2cell[0]).
  * Kappa (DiffusionTensor, HDGDiffusionSource.cpp:60-79): comps 0 (identity),
