@@ -26,6 +26,7 @@ HFX_ERR_UNSUPPORTED = 9
 KSP_CG, KSP_GMRES, KSP_AUTO = 0, 1, 2
 PC_NONE, PC_JACOBI, PC_BLOCK_JACOBI, PC_TWOLEVEL = 0, 1, 2, 3
 COARSE_CHEBYSHEV, COARSE_LEARNED = 0, 1
+IMPLICIT, WEXPLICIT, SEXPLICIT = 0, 1, 2
 PREC_FP64, PREC_MIXED = 0, 1
 SRC_NONE, SRC_VALUES, SRC_SINPROD = 0, 1, 2
 
@@ -36,7 +37,7 @@ EXPORTED = [
     "hfx_mesh_upload", "hfx_mesh_sizes", "hfx_mesh_topology", "hfx_mesh_compute_topology",
     "hfx_gmsh_read", "hfx_mesh_high_order", "hfx_mesh_io_error",
     "hfx_set_tau", "hfx_set_kappa", "hfx_set_source", "hfx_set_dirichlet", "hfx_set_time_scheme",
-    "hfx_ip_coords", "hfx_assemble", "hfx_assemble_ex", "hfx_set_assembly_path", "hfx_assembly_info", "hfx_get_condensed", "hfx_get_csr",
+    "hfx_ip_coords", "hfx_assemble", "hfx_assemble_ex", "hfx_set_solver_type", "hfx_set_state", "hfx_set_assembly_path", "hfx_assembly_info", "hfx_get_condensed", "hfx_get_csr",
     "hfx_solve_opts_default", "hfx_solve", "hfx_recover", "hfx_coarse_operator", "hfx_coarse_train",
     "hfx_coarse_loss_grad",
     "hfx_la_create", "hfx_la_destroy", "hfx_la_allocate", "hfx_la_set_values", "hfx_la_set_rhs",
@@ -118,6 +119,8 @@ def load(path=LIB_PATH):
         "hfx_coarse_train": ([vp, ip, ip, ip, ctypes.POINTER(TrainInfo)], ip),
         "hfx_coarse_loss_grad": ([vp, ip, vp, ip, vp, vp, vp], ip),
         "hfx_set_assembly_path": ([vp, ip], ip),
+        "hfx_set_solver_type": ([vp, ip], ip),
+        "hfx_set_state": ([vp, vp, vp], ip),
         "hfx_gmsh_read": ([ctypes.c_char_p, ip, vp, vp, vp, vp], ip),
         "hfx_mesh_high_order": ([ip, ip, ip, vp, ip, vp, vp, vp, vp], ip),
         "hfx_mesh_io_error": ([], ctypes.c_char_p),
@@ -364,6 +367,14 @@ class Context:
         self._chk(self.L.hfx_coarse_operator(self.h, ctypes.byref(nV), ctypes.byref(nnz), _p(rowptr), _p(col),
                                              _p(val), _p(vn)), "coarse_operator")
         return rowptr, col, val, vn
+
+    def set_solver_type(self, t):
+        self._chk(self.L.hfx_set_solver_type(self.h, t), "set_solver_type")
+
+    def set_state(self, sol, flux):
+        sol = np.ascontiguousarray(sol, np.float64)
+        flux = np.ascontiguousarray(flux, np.float64)
+        self._chk(self.L.hfx_set_state(self.h, _p(sol), _p(flux)), "set_state")
 
     def coarse_train(self, degree=4, samples=16, steps=300):
         info = TrainInfo()

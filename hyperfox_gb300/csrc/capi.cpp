@@ -102,6 +102,7 @@ struct hfx_ctx {
   bool affineMesh = false;
   bool kappaSymmetric = true;
   int assemblyPath = 0;        // 0 automatic, 1 quadrature kernel always
+  int solverType = 0;          // HFX_IMPLICIT / HFX_WEXPLICIT / HFX_SEXPLICIT
   bool lastAffine = false;     // the last FP64 assembly used the affine kernel
   bool qValid = false;         // d_Q / d_Q0 hold the current Q, Q0
   double* d_atab = nullptr;    // affine reference operators
@@ -603,6 +604,9 @@ static int ensure_outputs(hfx_ctx* c) {
   HFX_CUDA(c, dalloc(m, &c->d_sol, (size_t)E * LU));
   HFX_CUDA(c, dalloc(m, &c->d_flux, (size_t)E * LQ));
   HFX_CUDA(c, dalloc(m, &c->d_geo, (size_t)E * (c->dim * c->dim + c->re.nFaces * c->dim)));
+  // Solution and Flux start at 0 (the state the explicit modes read before a first recovery)
+  HFX_CUDA(c, cudaMemsetAsync(c->d_sol, 0, sizeof(double) * E * LU, c->stream));
+  HFX_CUDA(c, cudaMemsetAsync(c->d_flux, 0, sizeof(double) * E * LQ, c->stream));
   HFX_CUDA(c, cudaMemsetAsync(c->d_trace, 0, sizeof(double) * c->ndofs(), c->stream));
   return HFX_OK;
 }
@@ -643,6 +647,9 @@ static int assemble_fp64(hfx_ctx* c) {
   p.fp32 = 0;
   p.rhsU = p.rhsQ = nullptr;
   p.writeOps = 1;
+  p.explicitMode = c->solverType;
+  p.solState = c->d_sol;
+  p.fluxState = c->d_flux;
   const bool affine = c->assemblyPath == 0 && c->affineMesh && c->kappaCellConstant && c->d_atab;
   c->timer.begin(K_LOCAL, s);
   if (affine) HFX_CUDA(c, launch_local_affine(c->dim, c->order, p, c->d_atab, c->d_geo, s));
@@ -844,6 +851,8 @@ int hfx_assemble_ex(hfx_ctx* c, int precision) {
   if (precision != HFX_PREC_FP64 && precision != HFX_PREC_MIXED) return set_err(c, HFX_ERR_ARG, "assemble: unknown precision");
   cudaSetDevice(c->device);
   c->coarse.ready = false;  // the coarse operator follows the element matrices
+  if (precision == HFX_PREC_MIXED && c->solverType != HFX_IMPLICIT)
+    return set_err(c, HFX_ERR_UNSUPPORTED, "assemble: the explicit modes assemble in FP64");
   return precision == HFX_PREC_MIXED ? assemble_mixed(c) : assemble_fp64(c);
 }
 
@@ -853,6 +862,30 @@ int hfx_set_assembly_path(hfx_ctx* c, int path) {
   if (!c) return HFX_ERR_ARG;
   if (path != 0 && path != 1) return set_err(c, HFX_ERR_ARG, "set_assembly_path: 0 (automatic) or 1 (quadrature)");
   c->assemblyPath = path;
+  c->assembled = false;
+  return HFX_OK;
+}
+
+int hfx_set_solver_type(hfx_ctx* c, int type) {
+  if (!c) return HFX_ERR_ARG;
+  if (type != HFX_IMPLICIT && type != HFX_WEXPLICIT && type != HFX_SEXPLICIT)
+    return set_err(c, HFX_ERR_ARG, "set_solver_type: HFX_IMPLICIT, HFX_WEXPLICIT or HFX_SEXPLICIT");
+  c->solverType = type;
+  c->assembled = false;
+  return HFX_OK;
+}
+
+int hfx_set_state(hfx_ctx* c, const double* solution, const double* flux) {
+  if (!c || !solution || !flux) return HFX_ERR_ARG;
+  if (!c->haveMesh) return set_err(c, HFX_ERR_STATE, "set_state: upload a mesh first");
+  cudaSetDevice(c->device);
+  int rc = ensure_outputs(c);
+  if (rc) return rc;
+  const size_t E = (size_t)c->nCells;
+  HFX_CUDA(c, cudaMemcpyAsync(c->d_sol, solution, sizeof(double) * E * c->re.nNodes, cudaMemcpyHostToDevice, c->stream));
+  HFX_CUDA(c, cudaMemcpyAsync(c->d_flux, flux, sizeof(double) * E * c->re.nNodes * c->dim, cudaMemcpyHostToDevice,
+                              c->stream));
+  HFX_CUDA(c, cudaStreamSynchronize(c->stream));
   c->assembled = false;
   return HFX_OK;
 }
@@ -1172,6 +1205,35 @@ int hfx_solve(hfx_ctx* c, const hfx_solve_opts* opts, double* trace, hfx_solve_i
   int rc = ensure_workspace(c, mixed, method == HFX_KSP_GMRES ? restart : 0);
   if (rc) return rc;
   if (c->mixedMode) return solve_mixed(c, o, method, restart, trace, info);
+  if (c->solverType == HFX_SEXPLICIT) {
+    // no global solve: each face solves its own block
+    cudaEvent_t f0, f1;
+    cudaEventCreate(&f0);
+    cudaEventCreate(&f1);
+    cudaEventRecord(f0, c->stream);
+    HFX_CUDA(c, cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream));
+    c->timer.begin(K_OTHER, c->stream);
+    HFX_CUDA(c, launch_face_block_solve(c->topo.nFaces, c->re.nNodesFace, c->d_browptr, c->d_bcol, c->d_val,
+                                        c->d_rhs, c->d_trace, c->d_status, c->stream));
+    c->timer.end(K_OTHER, c->stream);
+    cudaEventRecord(f1, c->stream);
+    int fst = 0;
+    HFX_CUDA(c, cudaMemcpyAsync(&fst, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    HFX_CUDA(c, cudaStreamSynchronize(c->stream));
+    float fms = 0.f;
+    cudaEventElapsedTime(&fms, f0, f1);
+    cudaEventDestroy(f0);
+    cudaEventDestroy(f1);
+    if (info) {
+      *info = hfx_solve_info{};
+      info->status = fst ? HFX_ERR_SINGULAR : HFX_OK;
+      info->solve_ms = fms;
+    }
+    if (fst) return set_err(c, HFX_ERR_SINGULAR, "solve: singular face block (SEXPLICIT)");
+    if (trace) HFX_CUDA(c, cudaMemcpy(trace, c->d_trace, sizeof(double) * c->ndofs(), cudaMemcpyDeviceToHost));
+    c->solved = true;
+    return HFX_OK;
+  }
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);

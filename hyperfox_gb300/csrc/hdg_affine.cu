@@ -483,7 +483,43 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
       unsigned bmask = 0;  // bit f: face f of the cell is a Dirichlet face
       for (int f = 0; f < F; ++f)
         if (p.isBoundary[p.cell2face[e * F + f]]) bmask |= 1u << f;
-      for (int idx = t; idx < LL * (LL + 1) / 2; idx += 32) {
+      if (p.explicitMode) {
+        // explicit modes: S = Sll (block diagonal), S0 = -Slu sol + Hm flux
+        for (int idx = t; idx < LL * LL; idx += 32) {
+          const int r = idx % LL, c = idx / LL, fr = r / NF;
+          double v;
+          if ((bmask >> fr) & 1u) v = r == c ? 1.0 : 0.0;
+          else v = (c / NF == fr) ? -Tm[(fr * NF + r % NF) * NF + (c % NF)] : 0.0;
+          Sg[idx] = v;
+        }
+        const double* sol = p.solState + e * N;
+        const double* flx = p.fluxState + e * N * D;
+        for (int c = t; c < LL; c += 32) {
+          const int f = c / NF, a = c % NF;
+          double v;
+          if ((bmask >> f) & 1u) {
+            v = p.dirichlet[(int64_t)p.cell2face[e * F + f] * NF + a];
+          } else {
+            double kn[D];
+            for (int dd = 0; dd < D; ++dd) {
+              double acc = 0.0;
+              for (int b2 = 0; b2 < D; ++b2) acc += Ks[dd + b2 * D] * nrm[f * D + b2];
+              kn[dd] = acc;
+            }
+            v = 0.0;
+            for (int b = 0; b < NF; ++b) {
+              const int nb = sFN[f * NF + b];
+              double mf = 0.0;  // face mass: sum_c T_f[a][b][c] (the face shapes sum to 1)
+              for (int cc = 0; cc < NF; ++cc) mf += __ldg(tTf + (a * NF + b) * NF + cc);
+              double qn = 0.0;
+              for (int dd = 0; dd < D; ++dd) qn += kn[dd] * flx[nb * D + dd];
+              v += -Tm[(f * NF + a) * NF + b] * sol[nb] + area[f] * mf * qn;
+            }
+          }
+          ((double*)p.S0)[e * LL + c] = v;
+        }
+      }
+      for (int idx = t; !p.explicitMode && idx < LL * (LL + 1) / 2; idx += 32) {
         // column c, row r <= c, column-major packing of the upper triangle
         int c = (int)((sqrtf(8.0f * idx + 1.0f) - 1.0f) * 0.5f);
         while (c * (c + 1) / 2 > idx) --c;
@@ -501,7 +537,7 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
         Sg[r + c * LL] = br ? (r == c ? 1.0 : 0.0) : v;
         if (r != c) Sg[c + r * LL] = bc ? 0.0 : v;
       }
-      for (int c = t; c < LL; c += 32) {
+      for (int c = t; !p.explicitMode && c < LL; c += 32) {
         const int f = c / NF;
         double v;
         if ((bmask >> f) & 1u) {

@@ -588,6 +588,8 @@ __global__ void __launch_bounds__(TPE * EPC)
         T v;
         if (bnd[f]) {
           v = (row == c) ? 1.0 : 0.0;
+        } else if (p.explicitMode) {
+          v = (c / NF == f) ? -Tm[(f * NF + a) * NF + (c % NF)] : T(0);  // S = Sll
         } else {
           v = (c / NF == f) ? -Tm[(f * NF + a) * NF + (c % NF)] : 0.0;
           for (int b = 0; b < NF; ++b) {
@@ -603,6 +605,15 @@ __global__ void __launch_bounds__(TPE * EPC)
         T v;
         if (bnd[f]) {
           v = rhsMode ? T(0) : (T)p.dirichlet[(int64_t)faceId[f] * NF + a];
+        } else if (p.explicitMode) {
+          // S0 = -Slu sol - Slq flux with the current state
+          v = 0.0;
+          for (int b = 0; b < NF; ++b) {
+            int nb = sFaceNodes[f * NF + b];
+            v -= Tm[(f * NF + a) * NF + b] * (T)p.solState[e * N + nb];
+            for (int d = 0; d < D; ++d)
+              v += Hm[((f * D + d) * NF + a) * NF + b] * (T)p.fluxState[e * N * D + nb * D + d];
+          }
         } else {
           v = 0.0;
           for (int b = 0; b < NF; ++b) {

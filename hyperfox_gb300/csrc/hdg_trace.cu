@@ -107,6 +107,57 @@ __global__ void scatter_rhs(ScatterParams p) {
   }
 }
 
+// SEXPLICIT trace (HDGSolver.cpp:709-729): every face solves its own block,
+// trace_f = S_f^{-1} S0_f, S_f being the diagonal block of the assembled system
+// (the explicit modes' system has no other block). One thread per face,
+// Gauss-Jordan with partial pivoting; a zero pivot sets *status.
+__global__ void face_block_solve(int nFaces, int NF, const int64_t* __restrict__ browptr, const int* __restrict__ bcol,
+                                 const double* __restrict__ val, const double* __restrict__ rhs, double* __restrict__ x,
+                                 int* status) {
+  for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nFaces; f += gridDim.x * blockDim.x) {
+    int64_t kd = -1;
+    for (int64_t k = browptr[f]; k < browptr[f + 1]; ++k)
+      if (bcol[k] == f) kd = k;
+    if (kd < 0) {
+      atomicCAS(status, 0, 2);
+      continue;
+    }
+    double B[10][11];
+    for (int a = 0; a < NF; ++a) {
+      for (int b = 0; b < NF; ++b) B[a][b] = val[kd * NF * NF + (int64_t)b * NF + a];
+      B[a][NF] = rhs[(int64_t)f * NF + a];
+    }
+    bool ok = true;
+    for (int k = 0; k < NF; ++k) {
+      int pr = k;
+      for (int i = k + 1; i < NF; ++i)
+        if (fabs(B[i][k]) > fabs(B[pr][k])) pr = i;
+      if (B[pr][k] == 0.0) {
+        ok = false;
+        break;
+      }
+      if (pr != k)
+        for (int j = 0; j <= NF; ++j) {
+          double t = B[k][j];
+          B[k][j] = B[pr][j];
+          B[pr][j] = t;
+        }
+      const double inv = 1.0 / B[k][k];
+      for (int j = k; j <= NF; ++j) B[k][j] *= inv;
+      for (int i = 0; i < NF; ++i) {
+        if (i == k) continue;
+        const double l = B[i][k];
+        for (int j = k; j <= NF; ++j) B[i][j] -= l * B[k][j];
+      }
+    }
+    if (!ok) {
+      atomicCAS(status, 0, 1);
+      continue;
+    }
+    for (int a = 0; a < NF; ++a) x[(int64_t)f * NF + a] = B[a][NF];
+  }
+}
+
 __global__ void block_rows(const int64_t* browptr, int nFaces, int* brow) {
   for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nFaces; f += gridDim.x * blockDim.x)
     for (int64_t k = browptr[f]; k < browptr[f + 1]; ++k) brow[k] = f;
@@ -166,6 +217,13 @@ unsigned grid_for(int64_t n, int threads) {
 
 cudaError_t launch_block_rows(const int64_t* browptr, int nFaces, int* brow, cudaStream_t s) {
   block_rows<<<grid_for(nFaces, 256), 256, 0, s>>>(browptr, nFaces, brow);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_face_block_solve(int nFaces, int NF, const int64_t* browptr, const int* bcol, const double* val,
+                                   const double* rhs, double* x, int* status, cudaStream_t s) {
+  if (NF > 10) return cudaErrorInvalidValue;
+  face_block_solve<<<grid_for(nFaces, 128), 128, 0, s>>>(nFaces, NF, browptr, bcol, val, rhs, x, status);
   return cudaGetLastError();
 }
 

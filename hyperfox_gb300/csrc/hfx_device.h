@@ -58,6 +58,11 @@ struct LocalParams {
   const double* rhsU;          // [nCells][N]
   const double* rhsQ;          // [nCells][N*D]
   int writeOps;                // write S, U, Q (else only S0, U0, Q0)
+  // HDGSolverType (HDGSolverOpts.h:6-10) 1 WEXPLICIT / 2 SEXPLICIT: S = Sll and
+  // S0 = -Slu sol - Slq flux from the current state (HDGSolver.cpp:349-354)
+  int explicitMode;
+  const double* solState;      // [nCells][N]
+  const double* fluxState;     // [nCells][N*D] node-major
 };
 
 cudaError_t launch_local_condense(int dim, int order, const LocalParams& p, cudaStream_t s);
@@ -90,6 +95,9 @@ struct ScatterParams {
 };
 cudaError_t launch_scatter(const ScatterParams& p, cudaStream_t s);
 cudaError_t launch_block_rows(const int64_t* browptr, int nFaces, int* brow, cudaStream_t s);
+// trace_f = S_f^{-1} S0_f with S_f the diagonal face block (SEXPLICIT); status 1: singular block
+cudaError_t launch_face_block_solve(int nFaces, int NF, const int64_t* browptr, const int* bcol, const double* val,
+                                   const double* rhs, double* x, int* status, cudaStream_t s);
 
 struct RecoverParams {
   int nCells, F, NF, LU, LQ, LL;

@@ -172,6 +172,17 @@ int hfx_set_kappa(hfx_ctx* ctx, const double* kappa, int comps, int layout);
 int hfx_set_source(hfx_ctx* ctx, int mode, const double* values, double param);
 int hfx_set_dirichlet(hfx_ctx* ctx, const double* values);
 int hfx_set_time_scheme(hfx_ctx* ctx, double dt, const double* uOld);
+/* HDGSolverType (HDGSolverOpts.h:6-10). IMPLICIT (default) condenses as usual.
+ * WEXPLICIT and SEXPLICIT (HDGSolver.cpp:349-354,709-729) build the trace system
+ * from the current Solution and Flux: S = Sll, S0 = -Slu Solution - Slq Flux; WEXPLICIT
+ * solves it with hfx_solve's Krylov method, SEXPLICIT face by face (S_f^{-1} S0_f).
+ * The state is the last hfx_recover result, or what hfx_set_state uploads
+ * (Solution [nCells][N], Flux [nCells][N*dim] node-major); it starts at 0. */
+#define HFX_IMPLICIT 0
+#define HFX_WEXPLICIT 1
+#define HFX_SEXPLICIT 2
+int hfx_set_solver_type(hfx_ctx* ctx, int type);
+int hfx_set_state(hfx_ctx* ctx, const double* solution, const double* flux);
 int hfx_ip_coords(hfx_ctx* ctx, double* out /* [nCells][nIP][dim] */);
 
 /* ---- assembly ----------------------------------------------------------------

@@ -672,6 +672,11 @@ struct Problem {
   std::vector<double> dirichlet;  // face field nFaces*Nf
   double dt = 0.0;            // > 0: implicit Euler (Euler.cpp:18-34)
   std::vector<double> uOld;   // nCells*N
+  // HDGSolverType (HDGSolverOpts.h:6-10): 0 IMPLICIT, 1 WEXPLICIT, 2 SEXPLICIT; the
+  // explicit modes build S, S0 from the current Solution and Flux (HDGSolver.cpp:349-354)
+  int solverType = 0;
+  std::vector<double> solState;   // nCells*N
+  std::vector<double> fluxState;  // nCells*N*dim, node-major (i, d)
   // outputs
   int lenU, lenQ, lenL, nloc;
   std::vector<double> S, S0, U, Q, U0, Q0;
@@ -938,12 +943,21 @@ static void condense(Problem& P, int iEl, const Mat& A, const std::vector<double
   Mat Q0(lenQ, 1);
   gemm(-1.0, Xu, U0, 0.0, Q0);
   Mat S = block(A, sL, sL, lenL, lenL);
-  gemm(1.0, block(A, sL, sU, lenL, lenU), Ul, 1.0, S);
-  gemm(1.0, block(A, sL, sQ, lenL, lenQ), Qm, 1.0, S);
   Mat S0(lenL, 1);
   for (int i = 0; i < lenL; ++i) S0(i, 0) = r[sL + i];
-  gemm(-1.0, block(A, sL, sU, lenL, lenU), U0, 1.0, S0);
-  gemm(-1.0, block(A, sL, sQ, lenL, lenQ), Q0, 1.0, S0);
+  if (P.solverType == 0) {
+    gemm(1.0, block(A, sL, sU, lenL, lenU), Ul, 1.0, S);
+    gemm(1.0, block(A, sL, sQ, lenL, lenQ), Qm, 1.0, S);
+    gemm(-1.0, block(A, sL, sU, lenL, lenU), U0, 1.0, S0);
+    gemm(-1.0, block(A, sL, sQ, lenL, lenQ), Q0, 1.0, S0);
+  } else {
+    // explicit modes (HDGSolver.cpp:349-354): S = Sll, S0 = f_L - Slu sol - Slq flux
+    Mat sol(lenU, 1), flux(lenQ, 1);
+    for (int i = 0; i < lenU; ++i) sol(i, 0) = P.solState[(size_t)iEl * lenU + i];
+    for (int i = 0; i < lenQ; ++i) flux(i, 0) = P.fluxState[(size_t)iEl * lenQ + i];
+    gemm(-1.0, block(A, sL, sU, lenL, lenU), sol, 1.0, S0);
+    gemm(-1.0, block(A, sL, sQ, lenL, lenQ), flux, 1.0, S0);
+  }
   std::copy(S.a.begin(), S.a.end(), P.S.begin() + (size_t)iEl * lenL * lenL);
   std::copy(S0.a.begin(), S0.a.end(), P.S0.begin() + (size_t)iEl * lenL);
   std::copy(Ul.a.begin(), Ul.a.end(), P.U.begin() + (size_t)iEl * lenU * lenL);
@@ -1430,6 +1444,47 @@ int orc_problem_recover(void* h, const double* trace, double* sol, double* flux)
 }
 
 // Stage timings in seconds: local, dirichlet, scatter, solve, recover.
+int orc_problem_set_solver(void* h, int type, const double* sol, const double* flux) {
+  ORC_TRY({
+    Problem& P = *(Problem*)h;
+    if (type < 0 || type > 2) throw std::runtime_error("solver type 0..2");
+    P.solverType = type;
+    if (type != 0) {
+      if (!sol || !flux) throw std::runtime_error("explicit modes need Solution and Flux");
+      P.solState.assign(sol, sol + (size_t)P.nCells * P.lenU);
+      P.fluxState.assign(flux, flux + (size_t)P.nCells * P.lenQ);
+    }
+  });
+  return 0;
+}
+
+// SEXPLICIT trace (HDGSolver.cpp:709-729): every face solves its own assembled
+// block, trace_f = S_f^{-1} S0_f. The per-face S_f, S0_f are the sums of the
+// element face blocks (Add), which here are the diagonal blocks of the CSR.
+int orc_problem_solve_faces(void* h, double* x) {
+  ORC_TRY({
+    Problem& P = *(Problem*)h;
+    const int Nf = P.re->face->nNodes;
+    const int nF = (int)P.mf.face2cell.size() / 2;
+    for (int f = 0; f < nF; ++f) {
+      Mat B(Nf, Nf), b(Nf, 1);
+      for (int a = 0; a < Nf; ++a) {
+        const int row = f * Nf + a;
+        b(a, 0) = P.rhs[row];
+        for (int k = P.rowptr[row]; k < P.rowptr[row + 1]; ++k) {
+          const int c = P.col[k];
+          if (c / Nf == f) B(a, c % Nf) = P.val[k];
+        }
+      }
+      std::vector<int> piv;
+      if (!lu_factor(B, piv)) throw std::runtime_error("singular face block");
+      lu_solve(B, piv, b);
+      for (int a = 0; a < Nf; ++a) x[(size_t)f * Nf + a] = b(a, 0);
+    }
+  });
+  return 0;
+}
+
 int orc_problem_timings(void* h, double* out) {
   Problem* P = (Problem*)h;
   out[0] = P->t_local;

@@ -52,6 +52,8 @@ def lib():
         L.orc_problem_solve.argtypes = [vp, dp, ip, ip, vp]
         L.orc_problem_recover.argtypes = [vp] * 4
         L.orc_problem_timings.argtypes = [vp, vp]
+        L.orc_problem_set_solver.argtypes = [vp, ip, vp, vp]
+        L.orc_problem_solve_faces.argtypes = [vp, vp]
         _lib = L
     return _lib
 
@@ -205,6 +207,18 @@ class Problem:
         flux = np.zeros((self.nCells, self.lenQ))
         _check(lib().orc_problem_recover(self.h, _ptr(trace), _ptr(sol), _ptr(flux)))
         return sol, flux
+
+    def set_solver(self, type_, sol=None, flux=None):
+        """HDGSolverType: 0 IMPLICIT, 1 WEXPLICIT, 2 SEXPLICIT (explicit modes read sol, flux)."""
+        sol = None if sol is None else np.ascontiguousarray(sol, dtype=np.float64)
+        flux = None if flux is None else np.ascontiguousarray(flux, dtype=np.float64)
+        self._keep_state = (sol, flux)
+        _check(lib().orc_problem_set_solver(self.h, type_, _ptr(sol), _ptr(flux)))
+
+    def solve_faces(self):
+        x = np.zeros(self.ndofs)
+        _check(lib().orc_problem_solve_faces(self.h, _ptr(x)))
+        return x
 
     def timings(self):
         t = np.zeros(5)
