@@ -388,7 +388,8 @@ def main():
                          "refinement of the full HDG system")
     ap.add_argument("--rtol", type=float, default=1e-10,
                     help="relative FP64 residual of the trace system (mixed-full: of the full HDG system)")
-    ap.add_argument("--inner-rtol", type=float, default=1e-5)
+    ap.add_argument("--inner-rtol", type=float, default=1e-2,
+                    help="FP32 reduction between FP64 residual replacements (mixed)")
     ap.add_argument("--precond", default="twolevel", choices=["twolevel", "bj"],
                     help="two-level (block Jacobi + vertex coarse space) or block Jacobi alone")
     ap.add_argument("--coarse-guess", action="store_true", help="start CG from the prolongated coarse solution")

@@ -1048,7 +1048,7 @@ void hfx_solve_opts_default(hfx_solve_opts* o) {
   o->rtol = 1e-10;
   o->maxits = 20000;
   o->restart = 30;
-  o->inner_rtol = 1e-4;
+  o->inner_rtol = 1e-2;
   o->use_initial_guess = 0;
   o->coarse_guess = 0;
   o->coarse_rtol = 0.1;
@@ -1257,7 +1257,7 @@ int hfx_solve(hfx_ctx* c, const hfx_solve_opts* opts, double* trace, hfx_solve_i
   a.precond = o.precond;
   a.mixed = mixed;
   a.rtol = o.rtol;
-  a.inner_rtol = o.inner_rtol > 0 ? o.inner_rtol : 1e-4;
+  a.inner_rtol = o.inner_rtol > 0 ? o.inner_rtol : 1e-2;
   a.maxits = o.maxits;
   a.max_refinements = 50;
   a.check_every = 25;

@@ -139,22 +139,27 @@ __device__ __forceinline__ T row_dot(const T* __restrict__ val, int64_t b0, int 
 }
 
 // Row of the face block-row from the symmetric half storage: stored blocks are
-// read by column (coalesced), mirrored ones by row (the 400-byte block comes
-// through L1 once).
-template <int NF>
+// read by column (stride NF), mirrored ones by row (stride 1, the 400-byte block
+// comes through L1 once). All block indices are loaded first and every block's
+// NF values are issued before use, so the loads of a row are in flight together.
+template <int NF, int NBMAX>
 __device__ __forceinline__ float row_dot_half(const float* __restrict__ valh, const int* __restrict__ hidx, int64_t b0,
                                               int nb, int a, const float* xs) {
+  int hh[NBMAX];
+#pragma unroll
+  for (int k = 0; k < NBMAX; ++k) hh[k] = k < nb ? __ldg(hidx + b0 + k) : 0;
   float acc = 0.f;
-  for (int k = 0; k < nb; ++k) {
-    const int h = hidx[b0 + k];
-    if (h >= 0) {
-      const float* blk = valh + (int64_t)h * NF * NF + a;
 #pragma unroll
-      for (int b = 0; b < NF; ++b) acc = fmaf(__ldg(blk + b * NF), xs[k * NF + b], acc);
-    } else {
-      const float* blk = valh + (int64_t)(-h - 1) * NF * NF + (int64_t)a * NF;
+  for (int k = 0; k < NBMAX; ++k) {
+    if (k < nb) {
+      const int h = hh[k];
+      const float* blk = h >= 0 ? valh + (int64_t)h * NF * NF + a : valh + (int64_t)(-h - 1) * NF * NF + (int64_t)a * NF;
+      const int st = h >= 0 ? NF : 1;
+      float v[NF];
 #pragma unroll
-      for (int b = 0; b < NF; ++b) acc = fmaf(__ldg(blk + b), xs[k * NF + b], acc);
+      for (int b = 0; b < NF; ++b) v[b] = __ldg(blk + b * st);
+#pragma unroll
+      for (int b = 0; b < NF; ++b) acc = fmaf(v[b], xs[k * NF + b], acc);
     }
   }
   return acc;
@@ -180,7 +185,7 @@ __global__ void __launch_bounds__(kThreads) cg_spmv_half(TraceView A, const floa
     if (act) gather_x<float, NF, NBMAX, false, true>(A, b0, nb, false, a, beta, z, pold, xs);
     __syncwarp();
     if (act) {
-      const float y = row_dot_half<NF>(valh, A.hidx, b0, nb, a, xs);
+      const float y = row_dot_half<NF, NBMAX>(valh, A.hidx, b0, nb, a, xs);
       const int64_t i = f * NF + a;
       const float pi = fmaf(beta, pold[i], z[i]);
       pnew[i] = pi;
@@ -887,8 +892,9 @@ struct Driver {
       // the iteration count stays close to FP64 CG's.
       float *r32 = a.ws.r32, *z32 = a.ws.z32, *p032 = a.ws.p032, *p132 = a.ws.p132, *q32 = a.ws.q32;
       float* y32 = a.ws.d32;
-      // replace the residual every two decades of FP32 reduction
-      const double delta = 1e-2;
+      // replace the residual after every inner_rtol of FP32 reduction (two
+      // decades by default); FP32 rounding bounds how far a stretch can go
+      const double delta = std::min(0.5, std::max(1e-4, a.inner_rtol));
       const int gridR = grid_of(cg_replace<NF, NBMAX, 2>, kThreads);
       if (!a.use_initial_guess) set_dirichlet_start(A, a.ws.bS, x, s);
       cudaMemsetAsync(y32, 0, sizeof(float) * n, s);

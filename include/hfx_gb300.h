@@ -74,7 +74,8 @@ typedef struct {
   double rtol;           /* ||b - A x|| <= rtol ||b|| (PetscOpts::rtol) */
   int maxits;            /* total inner iterations allowed (PetscOpts::maxits) */
   int restart;           /* GMRES restart length (PETSc default 30) */
-  double inner_rtol;     /* mixed precision: inner FP32 reduction per refinement step */
+  double inner_rtol;     /* mixed precision: FP32 residual reduction between FP64 residual
+                            replacements (CG) or per refinement step (default 1e-2) */
   int use_initial_guess; /* start from the trace already on the device */
   int coarse_guess;      /* HFX_PC_TWOLEVEL: start from the prolongated coarse solution */
   double coarse_rtol;    /* HFX_PC_TWOLEVEL: residual reduction the Chebyshev coarse solve targets */
