@@ -392,7 +392,7 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
         for (int k = 0; k < D; ++k) {
           double xk = 0.0;
           for (int i = 0; i < N; ++i) xk += phi[q * N + i] * X[i * D + k];
-          fval *= sin(M_PI * xk);
+          fval *= sinpi(xk);  // sin(pi x) without the product's rounding
         }
       }
       fq[q] = fval * wq[q] * detJ;
@@ -457,9 +457,13 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
       for (int i = k + 1 + t; i < N; i += 32) Am[i * N + k] *= il;
       __syncwarp();
       const int m = N - k - 1;
-      for (int idx = t; idx < m * m; idx += 32) {
-        const int i = k + 1 + idx / m, j = k + 1 + idx % m;
-        if (j <= i) Am[i * N + j] -= Am[i * N + k] * Am[j * N + k];
+      for (int idx = t; idx < m * (m + 1) / 2; idx += 32) {
+        // packed lower triangle of the trailing block: row ii >= column jj
+        int ii = (int)((sqrtf(8.0f * idx + 1.0f) - 1.0f) * 0.5f);
+        while (ii * (ii + 1) / 2 > idx) --ii;
+        while ((ii + 1) * (ii + 2) / 2 <= idx) ++ii;
+        const int i = k + 1 + ii, j = k + 1 + (idx - ii * (ii + 1) / 2);
+        Am[i * N + j] -= Am[i * N + k] * Am[j * N + k];
       }
       __syncwarp();
     }
