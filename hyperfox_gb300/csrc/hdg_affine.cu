@@ -141,6 +141,25 @@ bool affine_tables(const RefEl& re, std::vector<double>* out) {
 
 namespace {
 
+// W^T W in double-float arithmetic on the FP32 pipe (GB300's FP32 pipe is
+// about 64x its FP64 one): every W entry is a pair hi + lo of floats, products
+// are split exactly with an FMA (two-product) and sums carried with Knuth's
+// two-sum, the double-float scheme of Dekker (1971) and of the QD library
+// (Hida, Li, Bailey 2001); about 44 significant bits per accumulated term.
+// The _rn intrinsics keep the compiler from contracting the error terms.
+__device__ __forceinline__ void ds_mac(float& sh, float& sl, float2 a, float2 b) {
+  const float p = __fmul_rn(a.x, b.x);
+  float e = fmaf(a.x, b.x, -p);
+  e = fmaf(a.x, b.y, e);
+  e = fmaf(a.y, b.x, e);
+  const float s = __fadd_rn(sh, p);
+  const float bb = __fsub_rn(s, sh);
+  float t = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  t = __fadd_rn(t, __fadd_rn(sl, e));
+  sh = __fadd_rn(s, t);
+  sl = __fsub_rn(t, __fsub_rn(sh, s));
+}
+
 template <int D, int P>
 struct AffLayout {
   using K = Dims<D, P>;
@@ -177,7 +196,8 @@ struct AffLayout {
   static constexpr int BW = AM + N * N;          // N*LW row-major
   static constexpr int FQ = BW + N * LW;         // NI
   static constexpr int IDG = FQ + NI;            // N     1 / L[k][k]
-  static constexpr int WARP = (IDG + N + 1) & ~1;
+  static constexpr int WDS = (IDG + N + 1) & ~1; // N*LL  W as float pairs (hi, lo)
+  static constexpr int WARP = WDS + N * LL;
   // the geometry scratch (Jacobian entries) lives in AM and BW before they are built
   static_assert(N * N + N * LW >= D * D + F * (D - 1) * D, "geometry scratch does not fit");
 };
@@ -217,6 +237,7 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
   double* BW = W + L::BW;
   double* fq = W + L::FQ;
   double* idg = W + L::IDG;
+  float2* wds = reinterpret_cast<float2*>(W + L::WDS);
   const double* phi = p.tab + L::T_PHI;
   const double* dphi = p.tab + L::T_DPHI;
   const double* wq = p.tab + L::T_W;
@@ -481,6 +502,14 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
       }
       __syncwarp();
     }
+    // W as double-float pairs for the product below
+    for (int idx = t; !p.explicitMode && idx < N * LL; idx += 32) {
+      const int m = idx / LL, c = idx % LL;
+      const double w = BW[m * LW + c];
+      const float hi = __double2float_rn(w);
+      wds[idx] = make_float2(hi, __double2float_rn(w - (double)hi));
+    }
+    __syncwarp();
     // ------------------ S = C + dt W^T W (upper triangle, mirrored), S0 = W^T y0
     {
       double* Sg = (double*)p.S + e * LL * LL;
@@ -530,9 +559,10 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
         while ((c + 1) * (c + 2) / 2 <= idx) ++c;
         const int r = idx - c * (c + 1) / 2;
         const int fr = r / NF, fc = c / NF;
-        double v = 0.0;
-        for (int m = 0; m < N; ++m) v += BW[m * LW + r] * BW[m * LW + c];
-        v *= dts;
+        float sh = 0.f, sl = 0.f;
+#pragma unroll 4
+        for (int m = 0; m < N; ++m) ds_mac(sh, sl, wds[m * LL + r], wds[m * LL + c]);
+        double v = ((double)sh + (double)sl) * dts;
         v -= cff[fr * F + fc] * __ldg(tT + ((fr * F + fc) * NF + (r % NF)) * NF + (c % NF));
         if (fr == fc) v -= Tm[(fr * NF + r % NF) * NF + (c % NF)];
         const bool br = (bmask >> fr) & 1u;
