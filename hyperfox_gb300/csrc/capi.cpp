@@ -107,6 +107,7 @@ struct hfx_ctx {
   bool qValid = false;         // d_Q / d_Q0 hold the current Q, Q0
   double* d_atab = nullptr;    // affine reference operators
   double* d_geo = nullptr;     // [nCells][D*D + F*D]
+  double* d_prep = nullptr;    // [nCells][affine_prep_doubles] per-element affine record
   // outputs
   DevMem outMem;
   double *d_S = nullptr, *d_S0 = nullptr, *d_U = nullptr, *d_Q = nullptr, *d_U0 = nullptr, *d_Q0 = nullptr;
@@ -185,7 +186,7 @@ void free_outputs(hfx_ctx* c) {
   c->outMem.release();
   c->wsMem.release();
   c->d_S = c->d_S0 = c->d_U = c->d_Q = c->d_U0 = c->d_Q0 = c->d_val = c->d_rhs = c->d_trace = nullptr;
-  c->d_sol = c->d_flux = c->d_geo = nullptr;
+  c->d_sol = c->d_flux = c->d_geo = c->d_prep = nullptr;
   c->qValid = c->lastAffine = false;
   c->mixMem.release();
   c->d_S32 = c->d_S032 = c->d_U32 = c->d_Q32 = c->d_U032 = c->d_Q032 = c->d_dl32 = nullptr;
@@ -604,6 +605,7 @@ static int ensure_outputs(hfx_ctx* c) {
   HFX_CUDA(c, dalloc(m, &c->d_sol, (size_t)E * LU));
   HFX_CUDA(c, dalloc(m, &c->d_flux, (size_t)E * LQ));
   HFX_CUDA(c, dalloc(m, &c->d_geo, (size_t)E * (c->dim * c->dim + c->re.nFaces * c->dim)));
+  if (c->d_atab) HFX_CUDA(c, dalloc(m, &c->d_prep, (size_t)E * affine_prep_doubles(c->dim, c->order)));
   // Solution and Flux start at 0 (the state the explicit modes read before a first recovery)
   HFX_CUDA(c, cudaMemsetAsync(c->d_sol, 0, sizeof(double) * E * LU, c->stream));
   HFX_CUDA(c, cudaMemsetAsync(c->d_flux, 0, sizeof(double) * E * LQ, c->stream));
@@ -650,9 +652,9 @@ static int assemble_fp64(hfx_ctx* c) {
   p.explicitMode = c->solverType;
   p.solState = c->d_sol;
   p.fluxState = c->d_flux;
-  const bool affine = c->assemblyPath == 0 && c->affineMesh && c->kappaCellConstant && c->d_atab;
+  const bool affine = c->assemblyPath == 0 && c->affineMesh && c->kappaCellConstant && c->d_atab && c->d_prep;
   c->timer.begin(K_LOCAL, s);
-  if (affine) HFX_CUDA(c, launch_local_affine(c->dim, c->order, p, c->d_atab, c->d_geo, s));
+  if (affine) HFX_CUDA(c, launch_local_affine(c->dim, c->order, p, c->d_atab, c->d_geo, c->d_prep, s));
   else HFX_CUDA(c, launch_local_condense(c->dim, c->order, p, s));
   c->timer.end(K_LOCAL, s);
   c->lastAffine = affine;

@@ -134,6 +134,7 @@ bool affine_tables(const RefEl& re, std::vector<double>* out) {
         }
   out->clear();
   for (auto* v : {&M, &R, &Tf, &P, &T, &Dr, &L}) out->insert(out->end(), v->begin(), v->end());
+  out->insert(out->end(), re.ipX.begin(), re.ipX.end());  // volume IPs, for the source
   return true;
 }
 
@@ -172,7 +173,13 @@ struct AffLayout {
   static constexpr int A_T = A_P + D * F * N * NF;
   static constexpr int A_D = A_T + F * F * NF * NF;
   static constexpr int A_L = A_D + D * N * N;
-  static constexpr int A_END = A_L + F * N * NF;
+  static constexpr int A_X = A_L + F * N * NF;  // [NI][D] reference IP coordinates
+  static constexpr int A_END = A_X + NI * D;
+  // per-element precomputed factors (affine_prep): G, |J|, |F_f|, n_f, Gamma,
+  // g_f, c_ff', f(x_q) w_q |J|, K
+  static constexpr int P_IV = 0, P_DET = P_IV + D * D, P_AR = P_DET + 1, P_NRM = P_AR + F, P_GAM = P_NRM + F * D;
+  static constexpr int P_GV = P_GAM + D * D, P_CFF = P_GV + F * D, P_FQ = P_CFF + F * F, P_KS = P_FQ + NI;
+  static constexpr int PREP = P_KS + D * D;
   // offsets in the packed quadrature table (phi, dphi, w, fphi, fdphi, fw)
   static constexpr int T_PHI = 0;
   static constexpr int T_DPHI = T_PHI + NI * N;
@@ -181,30 +188,167 @@ struct AffLayout {
   static constexpr int T_FDPHI = T_FPHI + NIF * NF;
   // per-warp shared region (doubles)
   static constexpr int LW = LL + 1;              // columns of [B | f_u]
-  static constexpr int X = 0;                    // N*D
-  static constexpr int TAU = X + N * D;          // F*NF
-  static constexpr int KS = TAU + F * NF;        // D*D   cell tensor K[d][b] at d + b*D
-  static constexpr int IV = KS + D * D;          // D*D   G = J^{-1}
-  static constexpr int GAM = IV + D * D;         // D*D   Gamma[r][s]
-  static constexpr int GV = GAM + D * D;         // F*D   (n_f^T K G)_r
-  static constexpr int NRM = GV + F * D;         // F*D   unit normals
-  static constexpr int CFF = NRM + F * D;        // F*F
-  static constexpr int AR = CFF + F * F;         // F     |F_f|
-  static constexpr int SC = AR + F;              // 4     detJ, dts, flags
-  static constexpr int TM = SC + 4;              // F*NF*NF
+  static constexpr int PR = 0;                   // PREP  the element's affine_prep record
+  static constexpr int TAU = PR + PREP;          // F*NF
+  static constexpr int TM = TAU + F * NF;        // F*NF*NF
   static constexpr int AM = TM + F * NF * NF;    // N*N row-major, then its Cholesky factor
   static constexpr int BW = AM + N * N;          // N*LW row-major
-  static constexpr int FQ = BW + N * LW;         // NI
-  static constexpr int IDG = FQ + NI;            // N     1 / L[k][k]
+  static constexpr int IDG = BW + N * LW;        // N     1 / L[k][k]
   static constexpr int WDS = (IDG + N + 1) & ~1; // N*LL  W as float pairs (hi, lo)
   static constexpr int WARP = WDS + N * LL;
-  // the geometry scratch (Jacobian entries) lives in AM and BW before they are built
-  static_assert(N * N + N * LW >= D * D + F * (D - 1) * D, "geometry scratch does not fit");
 };
+
+// Per-element geometry and source, one thread per element (full warps): the
+// affine Jacobian from the vertices (J[r][s] = (x_{r+1} - x_0)_s / 2 on the
+// reference simplex with vertices (-1,..), e_r), its inverse G, the face
+// measures and outward unit normals (face vertices first in every face-node
+// list), Gamma = G^T K G, g_f = n_f^T K G, c_ff', the source at the IPs
+// (affine map of the reference IPs), the cell tensor K, and the recovery factors.
+template <int D, int P>
+__global__ void affine_prep(LocalParams p, const double* __restrict__ atab, double* __restrict__ prep,
+                            double* __restrict__ geo) {
+  using L = AffLayout<D, P>;
+  constexpr int N = L::N, NF = L::NF, F = L::F, NI = L::NI;
+  const int* fnAll = p.itab;          // faceNodes [F][NF]
+  const int* opp = p.itab + F * NF;   // faceOpposite [F]
+  const double* ipx = atab + L::A_X;
+  const double* wq = p.tab + L::T_W;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < p.nCells; e += (int64_t)gridDim.x * blockDim.x) {
+    const int* cell = p.cells + e * N;
+    double* out = prep + e * L::PREP;
+    double X[D + 1][D];
+    for (int m = 0; m <= D; ++m)
+      for (int c = 0; c < D; ++c) X[m][c] = p.coords[(int64_t)cell[m] * D + c];
+    double K[D][D];  // K[d][b] from the column-major cell tensor
+    for (int a = 0; a < D * D; ++a) {
+      double v;
+      if (p.kc == 0) v = (a % (D + 1) == 0) ? 1.0 : 0.0;
+      else {
+        int64_t bk = p.kappaLayout == 0 ? (int64_t)cell[0] * p.kc : (e * N) * p.kc;
+        v = p.kc == 1 ? ((a % (D + 1) == 0) ? p.kappa[bk] : 0.0) : p.kappa[bk + a];
+      }
+      K[a % D][a / D] = v;
+      out[L::P_KS + a] = v;
+    }
+    double J[D][D], iv[D][D], det;
+    for (int r = 0; r < D; ++r)
+      for (int c = 0; c < D; ++c) J[r][c] = 0.5 * (X[r + 1][c] - X[0][c]);
+    if (D == 2) {
+      det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+      const double id = 1.0 / det;
+      iv[0][0] = J[1][1] * id;
+      iv[0][1] = -J[0][1] * id;
+      iv[1][0] = -J[1][0] * id;
+      iv[1][1] = J[0][0] * id;
+    } else {
+      const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+      const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+      const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+      det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+      const double id = 1.0 / det;
+      iv[0][0] = c00 * id;
+      iv[1][0] = c01 * id;
+      iv[2][0] = c02 * id;
+      iv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+      iv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+      iv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+      iv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+      iv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+      iv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+    }
+    for (int a = 0; a < D; ++a)
+      for (int b = 0; b < D; ++b) out[L::P_IV + a * D + b] = iv[a][b];
+    out[L::P_DET] = det;
+    double area[F], nrm[F][D];
+    for (int f = 0; f < F; ++f) {
+      const int* fv = fnAll + f * NF;  // the face's vertices are its first D nodes
+      double Jf[D - 1][D];
+      for (int r = 0; r < D - 1; ++r)
+        for (int c = 0; c < D; ++c) Jf[r][c] = 0.5 * (X[fv[r + 1]][c] - X[fv[0]][c]);
+      double nv[D], ds;
+      if (D == 2) {
+        ds = sqrt(Jf[0][0] * Jf[0][0] + Jf[0][1] * Jf[0][1]);
+        nv[0] = -Jf[0][1];
+        nv[1] = Jf[0][0];
+      } else {
+        const double g00 = Jf[0][0] * Jf[0][0] + Jf[0][1] * Jf[0][1] + Jf[0][2] * Jf[0][2];
+        const double g11 = Jf[1][0] * Jf[1][0] + Jf[1][1] * Jf[1][1] + Jf[1][2] * Jf[1][2];
+        const double g01 = Jf[0][0] * Jf[1][0] + Jf[0][1] * Jf[1][1] + Jf[0][2] * Jf[1][2];
+        ds = sqrt(g00 * g11 - g01 * g01);
+        nv[0] = Jf[0][1] * Jf[1][2] - Jf[0][2] * Jf[1][1];
+        nv[1] = Jf[0][2] * Jf[1][0] - Jf[0][0] * Jf[1][2];
+        nv[2] = Jf[0][0] * Jf[1][1] - Jf[0][1] * Jf[1][0];
+      }
+      double nn = 0.0;
+      for (int a = 0; a < D; ++a) nn += nv[a] * nv[a];
+      nn = rsqrt(nn);
+      double prod = 0.0;
+      for (int a = 0; a < D; ++a) {
+        nv[a] *= nn;
+        prod += (X[opp[f]][a] - X[fv[0]][a]) * nv[a];
+      }
+      if (prod > 0)
+        for (int a = 0; a < D; ++a) nv[a] = -nv[a];
+      area[f] = ds;
+      out[L::P_AR + f] = ds;
+      for (int a = 0; a < D; ++a) {
+        nrm[f][a] = nv[a];
+        out[L::P_NRM + f * D + a] = nv[a];
+      }
+    }
+    for (int r = 0; r < D; ++r)
+      for (int c = 0; c < D; ++c) {
+        double acc = 0.0;
+        for (int d = 0; d < D; ++d)
+          for (int b = 0; b < D; ++b) acc += K[d][b] * iv[b][r] * iv[d][c];
+        out[L::P_GAM + r * D + c] = acc;
+      }
+    double kn[F][D];
+    for (int f = 0; f < F; ++f) {
+      for (int r = 0; r < D; ++r) {
+        double acc = 0.0;
+        for (int d = 0; d < D; ++d)
+          for (int b = 0; b < D; ++b) acc += nrm[f][d] * K[d][b] * iv[b][r];
+        out[L::P_GV + f * D + r] = acc;
+      }
+      for (int d = 0; d < D; ++d) {
+        double acc = 0.0;
+        for (int b = 0; b < D; ++b) acc += K[d][b] * nrm[f][b];
+        kn[f][d] = acc;
+      }
+    }
+    for (int f = 0; f < F; ++f)
+      for (int g = 0; g < F; ++g) {
+        double acc = 0.0;
+        for (int d = 0; d < D; ++d) acc += nrm[g][d] * kn[f][d];
+        out[L::P_CFF + f * F + g] = area[f] * area[g] / det * acc;
+      }
+    for (int q = 0; q < NI; ++q) {
+      double fval = 0.0;
+      if (p.srcMode == 1) fval = p.src[e * NI + q];
+      else if (p.srcMode == 2) {
+        fval = p.srcParam;
+        for (int c = 0; c < D; ++c) {
+          double xc = X[0][c];
+          for (int r = 0; r < D; ++r) xc += 0.5 * (ipx[q * D + r] + 1.0) * (X[r + 1][c] - X[0][c]);
+          fval *= sinpi(xc);  // sin(pi x) without the product's rounding
+        }
+      }
+      out[L::P_FQ + q] = fval * wq[q] * det;
+    }
+    if (geo) {
+      double* ge = geo + e * (D * D + F * D);
+      for (int a = 0; a < D; ++a)
+        for (int b = 0; b < D; ++b) ge[a * D + b] = iv[a][b];
+      for (int f = 0; f < F; ++f)
+        for (int a = 0; a < D; ++a) ge[D * D + f * D + a] = area[f] / det * nrm[f][a];
+    }
+  }
+}
 
 template <int D, int P, int EPC>
 __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const double* __restrict__ atab,
-                                                         double* __restrict__ geo) {
+                                                         const double* __restrict__ prep) {
   using L = AffLayout<D, P>;
   constexpr int N = L::N, NF = L::NF, F = L::F, NI = L::NI, LL = L::LL, LW = L::LW;
   constexpr int DM = D - 1;
@@ -222,26 +366,21 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
 
   const int warp = threadIdx.x >> 5, t = threadIdx.x & 31;
   double* W = sm + warp * L::WARP;
-  double* X = W + L::X;
+  double* pr = W + L::PR;
   double* tau = W + L::TAU;
-  double* Ks = W + L::KS;
-  double* iv = W + L::IV;
-  double* gam = W + L::GAM;
-  double* gv = W + L::GV;
-  double* nrm = W + L::NRM;
-  double* cff = W + L::CFF;
-  double* area = W + L::AR;
-  double* sc = W + L::SC;
+  const double* Ks = pr + L::P_KS;
+  const double* gam = pr + L::P_GAM;
+  const double* gv = pr + L::P_GV;
+  const double* nrm = pr + L::P_NRM;
+  const double* cff = pr + L::P_CFF;
+  const double* area = pr + L::P_AR;
+  const double* fq = pr + L::P_FQ;
   double* Tm = W + L::TM;
   double* Am = W + L::AM;
   double* BW = W + L::BW;
-  double* fq = W + L::FQ;
   double* idg = W + L::IDG;
   float2* wds = reinterpret_cast<float2*>(W + L::WDS);
   const double* phi = p.tab + L::T_PHI;
-  const double* dphi = p.tab + L::T_DPHI;
-  const double* wq = p.tab + L::T_W;
-  const double* fdphi = p.tab + L::T_FDPHI;
   const double* tM = atab + L::A_M;
   const double* tR = atab + L::A_R;
   const double* tTf = atab + L::A_TF;
@@ -250,141 +389,16 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
   const double dts = p.dt > 0.0 ? p.dt : 1.0;
   const int64_t nWarps = (int64_t)gridDim.x * EPC;
   for (int64_t e = (int64_t)blockIdx.x * EPC + warp; e < p.nCells; e += nWarps) {
-    // ---------------------------------------------------------- gather
-    const int* cell = p.cells + e * N;
-    for (int i = t; i < N * D; i += 32) X[i] = p.coords[(int64_t)cell[i / D] * D + (i % D)];
+    // ------------------------------------- gather: prep record and face tau
+    for (int i = t; i < L::PREP; i += 32) pr[i] = prep[e * L::PREP + i];
     for (int i = t; i < F * NF; i += 32) {
       int f = p.cell2face[e * F + i / NF];
       int side = (p.face2cell[2 * (int64_t)f] == (int)e) ? 0 : 1;
       int q = p.perm[e * F * NF + i];
       tau[i] = p.tau[((int64_t)f * NF + q) * p.tauVals + (p.tauVals == 2 ? side : 0)];
     }
-    if (t < D * D) {
-      // cell tensor: the value at the cell's first node (constant inside the cell)
-      const int a = t;
-      double v;
-      if (p.kc == 0) v = (a % (D + 1) == 0) ? 1.0 : 0.0;
-      else {
-        int64_t bk = p.kappaLayout == 0 ? (int64_t)cell[0] * p.kc : (e * N) * p.kc;
-        v = p.kc == 1 ? ((a % (D + 1) == 0) ? p.kappa[bk] : 0.0) : p.kappa[bk + a];
-      }
-      Ks[a] = v;
-    }
     __syncwarp();
-    // ------------------------------------------------------ geometry
-    // Jacobian entries J[r][s] (first IP) and face Jacobian entries, one per lane
-    double* jw = Am;  // scratch: D*D volume + F*(D-1)*D face entries (A is built later)
-    for (int e2 = t; e2 < D * D + F * DM * D; e2 += 32) {
-      double acc = 0.0;
-      if (e2 < D * D) {
-        const int r = e2 / D, c = e2 % D;
-        for (int i = 0; i < N; ++i) acc += dphi[i * D + r] * X[i * D + c];
-      } else {
-        const int q = e2 - D * D, f = q / (DM * D), r = (q / D) % DM, c = q % D;
-        for (int i = 0; i < NF; ++i) acc += fdphi[i * DM + r] * X[sFN[f * NF + i] * D + c];
-      }
-      jw[e2] = acc;
-    }
-    __syncwarp();
-    if (t == 0) {
-      double J[D][D];
-      for (int r = 0; r < D; ++r)
-        for (int c = 0; c < D; ++c) J[r][c] = jw[r * D + c];
-      double det;
-      if (D == 2) {
-        det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
-        double id = 1.0 / det;
-        iv[0] = J[1][1] * id;
-        iv[1] = -J[0][1] * id;
-        iv[2] = -J[1][0] * id;
-        iv[3] = J[0][0] * id;
-      } else {
-        double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
-        double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
-        double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
-        det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
-        double id = 1.0 / det;
-        iv[0 * 3 + 0] = c00 * id;
-        iv[1 * 3 + 0] = c01 * id;
-        iv[2 * 3 + 0] = c02 * id;
-        iv[0 * 3 + 1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
-        iv[1 * 3 + 1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
-        iv[2 * 3 + 1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
-        iv[0 * 3 + 2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
-        iv[1 * 3 + 2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
-        iv[2 * 3 + 2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
-      }
-      sc[0] = det;
-    } else if (t >= 1 && t <= F) {
-      const int f = t - 1;
-      const double* jf = jw + D * D + f * DM * D;
-      double Jf[D - 1][D];
-      for (int r = 0; r < DM; ++r)
-        for (int c = 0; c < D; ++c) Jf[r][c] = jf[r * D + c];
-      double nv[D], ds;
-      if (D == 2) {
-        ds = sqrt(Jf[0][0] * Jf[0][0] + Jf[0][1] * Jf[0][1]);
-        nv[0] = -Jf[0][1];
-        nv[1] = Jf[0][0];
-      } else {
-        double g00 = Jf[0][0] * Jf[0][0] + Jf[0][1] * Jf[0][1] + Jf[0][2] * Jf[0][2];
-        double g11 = Jf[1][0] * Jf[1][0] + Jf[1][1] * Jf[1][1] + Jf[1][2] * Jf[1][2];
-        double g01 = Jf[0][0] * Jf[1][0] + Jf[0][1] * Jf[1][1] + Jf[0][2] * Jf[1][2];
-        ds = sqrt(g00 * g11 - g01 * g01);
-        nv[0] = Jf[0][1] * Jf[1][2] - Jf[0][2] * Jf[1][1];
-        nv[1] = Jf[0][2] * Jf[1][0] - Jf[0][0] * Jf[1][2];
-        nv[2] = Jf[0][0] * Jf[1][1] - Jf[0][1] * Jf[1][0];
-      }
-      double nn = 0.0;
-      for (int a = 0; a < D; ++a) nn += nv[a] * nv[a];
-      nn = rsqrt(nn);
-      double prod = 0.0;
-      const int v0 = sFN[f * NF], vn = sOpp[f];
-      for (int a = 0; a < D; ++a) {
-        nv[a] *= nn;
-        prod += (X[vn * D + a] - X[v0 * D + a]) * nv[a];
-      }
-      if (prod > 0)
-        for (int a = 0; a < D; ++a) nv[a] = -nv[a];
-      area[f] = ds;
-      for (int a = 0; a < D; ++a) nrm[f * D + a] = nv[a];
-    }
-    __syncwarp();
-    // derived scalars: Gamma[r][s] = sum_{d,b} K[d][b] G[b][r] G[d][s]; g_f[r] = (n_f^T K G)_r;
-    // c_ff' = |F_f||F_f'|/|J| n_f'^T K n_f
-    const double detJ = sc[0];
-    if (t < D * D) {
-      const int r = t / D, s = t % D;
-      double acc = 0.0;
-      for (int d = 0; d < D; ++d)
-        for (int b = 0; b < D; ++b) acc += Ks[d + b * D] * iv[b * D + r] * iv[d * D + s];
-      gam[t] = acc;
-    } else if (t >= 16 && t < 16 + F * D) {
-      const int f = (t - 16) / D, r = (t - 16) % D;
-      double acc = 0.0;
-      for (int d = 0; d < D; ++d)
-        for (int b = 0; b < D; ++b) acc += nrm[f * D + d] * Ks[d + b * D] * iv[b * D + r];
-      gv[t - 16] = acc;
-    }
-    if (t < F * F) {
-      const int f = t / F, g = t % F;
-      double acc = 0.0;
-      for (int d = 0; d < D; ++d) {
-        double kn = 0.0;
-        for (int b = 0; b < D; ++b) kn += Ks[d + b * D] * nrm[f * D + b];
-        acc += nrm[g * D + d] * kn;
-      }
-      cff[t] = area[f] * area[g] / detJ * acc;
-    }
-    // per-element factors for the recovery of Q
-    if (geo) {
-      double* ge = geo + e * (D * D + F * D);
-      if (t < D * D) ge[t] = iv[t];
-      else if (t < D * D + F * D) {
-        const int k = t - D * D;
-        ge[t] = area[k / D] / detJ * nrm[k];
-      }
-    }
+    const double detJ = pr[L::P_DET];
     // ----------------------------------------------- tau face mass Tm_f
     // symmetric in (a, b): the upper triangle, mirrored
     constexpr int NT = NF * (NF + 1) / 2;
@@ -403,20 +417,6 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
       acc *= area[f];
       Tm[(f * NF + a) * NF + b] = acc;
       Tm[(f * NF + b) * NF + a] = acc;
-    }
-    // source at the integration points: f(x_q) dV_q
-    for (int q = t; q < NI; q += 32) {
-      double fval = 0.0;
-      if (p.srcMode == 1) fval = p.src[e * NI + q];
-      else if (p.srcMode == 2) {
-        fval = p.srcParam;
-        for (int k = 0; k < D; ++k) {
-          double xk = 0.0;
-          for (int i = 0; i < N; ++i) xk += phi[q * N + i] * X[i * D + k];
-          fval *= sinpi(xk);  // sin(pi x) without the product's rounding
-        }
-      }
-      fq[q] = fval * wq[q] * detJ;
     }
     __syncwarp();
     // ------------------------------------------------- A, B and f_u
@@ -689,10 +689,17 @@ __global__ void q_from_u(int nCells, const double* __restrict__ U, const double*
   }
 }
 
+unsigned grid_cap(int64_t n, int threads) {
+  int64_t g = (n + threads - 1) / threads;
+  if (g > 152 * 64) g = 152 * 64;
+  return (unsigned)(g < 1 ? 1 : g);
+}
+
 template <int D, int P>
-cudaError_t launch_affine_t(const LocalParams& p, const double* atab, double* geo, cudaStream_t s) {
+cudaError_t launch_affine_t(const LocalParams& p, const double* atab, double* geo, double* prep, cudaStream_t s) {
   using L = AffLayout<D, P>;
   constexpr int EPC = 8;
+  affine_prep<D, P><<<grid_cap(p.nCells, 128), 128, 0, s>>>(p, atab, prep, geo);
   size_t smem = (size_t)EPC * L::WARP * sizeof(double);
   auto kern = local_affine<D, P, EPC>;
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -707,14 +714,8 @@ cudaError_t launch_affine_t(const LocalParams& p, const double* atab, double* ge
   int64_t grid = (int64_t)nsm * perSM;
   if (grid > need) grid = need;
   if (grid < 1) grid = 1;
-  kern<<<(unsigned)grid, 32 * EPC, smem, s>>>(p, atab, geo);
+  kern<<<(unsigned)grid, 32 * EPC, smem, s>>>(p, atab, prep);
   return cudaGetLastError();
-}
-
-unsigned grid_cap(int64_t n, int threads) {
-  int64_t g = (n + threads - 1) / threads;
-  if (g > 152 * 64) g = 152 * 64;
-  return (unsigned)(g < 1 ? 1 : g);
 }
 
 }  // namespace
@@ -738,8 +739,28 @@ unsigned grid_cap(int64_t n, int threads) {
   return cudaErrorInvalidValue;
 
 cudaError_t launch_local_affine(int dim, int order, const LocalParams& p, const double* atab, double* geo,
-                                cudaStream_t s) {
-  HFX_AFFINE_DISPATCH(launch_affine_t, p, atab, geo, s)
+                                double* prep, cudaStream_t s) {
+  HFX_AFFINE_DISPATCH(launch_affine_t, p, atab, geo, prep, s)
+}
+
+namespace {
+template <int D, int P>
+int64_t affine_prep_doubles_t() {
+  return AffLayout<D, P>::PREP;
+}
+}  // namespace
+
+int64_t affine_prep_doubles(int dim, int order) {
+  if (dim == 2 && order >= 1 && order <= 5) {
+    const int64_t v[] = {affine_prep_doubles_t<2, 1>(), affine_prep_doubles_t<2, 2>(), affine_prep_doubles_t<2, 3>(),
+                         affine_prep_doubles_t<2, 4>(), affine_prep_doubles_t<2, 5>()};
+    return v[order - 1];
+  }
+  if (dim == 3 && order >= 1 && order <= 3) {
+    const int64_t v[] = {affine_prep_doubles_t<3, 1>(), affine_prep_doubles_t<3, 2>(), affine_prep_doubles_t<3, 3>()};
+    return v[order - 1];
+  }
+  return 0;
 }
 
 namespace {

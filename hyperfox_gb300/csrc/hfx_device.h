@@ -72,7 +72,9 @@ bool local_condense_supported(int dim, int order);
 // S, S0, U, U0 from reference operators; geo[nCells][D*D + F*D] holds the
 // factors the recovery (and the Q export) needs. atab from affine_tables().
 cudaError_t launch_local_affine(int dim, int order, const LocalParams& p, const double* atab, double* geo,
-                                cudaStream_t s);
+                                double* prep, cudaStream_t s);
+// doubles per element of the affine per-element record (geometry, coefficients, source)
+int64_t affine_prep_doubles(int dim, int order);
 
 // Trace-system scatter (face-block rows, values in scalar-CSR order).
 struct ScatterParams {
