@@ -36,9 +36,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "time-to-solve @1e-8 rel err, learned+mixed vs plain FP64 GPU; elements/s"
 # DRAM bytes per unit from the committed ncu captures (profiles/): the FP32 trace
-# SpMV moves 4.29 bytes per non-zero (289.4 MB at 67.44M non-zeros), the FP64
-# one 8.75; the affine element kernel writes 18.6 KB per p=3 tetrahedron.
-TRAFFIC_PER_NNZ = {"spmv32": 289.4e6 / 67.44e6, "spmv64": 590.2e6 / 67.44e6}
+# SpMV over the symmetric half storage moves 2.60 bytes per non-zero of the full
+# operator (175.5 MB at 67.44M non-zeros), the FP64 one (full storage) 8.75; the
+# affine element kernel writes 18.6 KB per p=3 tetrahedron.
+TRAFFIC_PER_NNZ = {"spmv32": 175.5e6 / 67.44e6, "spmv64": 590.2e6 / 67.44e6}
 TRAFFIC_PER_ELEMENT_LOCAL = (24.3e6 + 893.0e6) / 48000
 FP64_NOMINAL_TFLOPS = 1.25
 
@@ -273,14 +274,20 @@ def run_ours(args, world, rank, local):
 
     def spmv_roof(key):
         sv = 4 if key == "spmv32" else 8
-        # values once, block columns + row pointers once, z and p_old gathered once, p_new and q written
-        alg = nnz * sv + nblocks * 4 + (ctx.nFaces + 1) * 8 + 4 * n * sv
+        # values once, block columns + row pointers once, z and p_old gathered once, p_new and q written;
+        # the FP32 operator of a symmetric problem is stored as its upper block triangle
+        # (diagonal blocks + half the off-diagonal ones) plus one int per block locating it
+        if key == "spmv32":
+            n_half = (nblocks - ctx.nFaces) // 2 + ctx.nFaces
+            alg = n_half * Nf * Nf * sv + nblocks * 8 + (ctx.nFaces + 1) * 8 + 4 * n * sv
+        else:
+            alg = nnz * sv + nblocks * 4 + (ctx.nFaces + 1) * 8 + 4 * n * sv
         # launches that did work: one per Krylov iteration (launches queued after
         # convergence return at entry and are not counted)
         launches = min(kt[key][0], iters * args.steps) if iters else kt[key][0]
         avg_ms = kt[key][1] / max(1, launches)
         achieved = alg / (avg_ms / 1e3) / 1e9
-        return dict(bound="hbm", kernel="cg_spmv<%s>" % ("float" if sv == 4 else "double"),
+        return dict(bound="hbm", kernel="cg_spmv_half<float>" if sv == 4 else "cg_spmv<double>",
                     achieved=round(achieved, 1), peak=hbm, unit="GB/s", frac=round(achieved / hbm, 4),
                     traffic=(TRAFFIC_PER_NNZ[key] * nnz) if (dim, p) == (3, 3) else None, bytes_per_launch=int(alg),
                     avg_launch_ms=round(avg_ms, 4), peak_source=peak_kind)

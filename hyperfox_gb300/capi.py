@@ -36,6 +36,7 @@ EXPORTED = [
     "hfx_refel_query", "hfx_refel_tables",
     "hfx_mesh_upload", "hfx_mesh_sizes", "hfx_mesh_topology", "hfx_mesh_compute_topology",
     "hfx_gmsh_read", "hfx_mesh_high_order", "hfx_mesh_io_error",
+    "hfx_h5_read_mesh", "hfx_h5_field_names", "hfx_h5_read_field", "hfx_h5_write",
     "hfx_set_tau", "hfx_set_kappa", "hfx_set_source", "hfx_set_dirichlet", "hfx_set_time_scheme",
     "hfx_ip_coords", "hfx_assemble", "hfx_assemble_ex", "hfx_set_solver_type", "hfx_set_state", "hfx_set_assembly_path", "hfx_assembly_info", "hfx_get_condensed", "hfx_get_csr",
     "hfx_solve_opts_default", "hfx_solve", "hfx_recover", "hfx_coarse_operator", "hfx_coarse_train",
@@ -124,6 +125,10 @@ def load(path=LIB_PATH):
         "hfx_gmsh_read": ([ctypes.c_char_p, ip, vp, vp, vp, vp], ip),
         "hfx_mesh_high_order": ([ip, ip, ip, vp, ip, vp, vp, vp, vp], ip),
         "hfx_mesh_io_error": ([], ctypes.c_char_p),
+        "hfx_h5_read_mesh": ([ctypes.c_char_p, vp, vp, vp, vp, vp, vp], ip),
+        "hfx_h5_field_names": ([ctypes.c_char_p, ctypes.c_char_p, ip, vp, vp], ip),
+        "hfx_h5_read_field": ([ctypes.c_char_p, ctypes.c_char_p, vp, vp, vp], ip),
+        "hfx_h5_write": ([ctypes.c_char_p, ip, ip, vp, ip, ip, vp, ip, vp, vp, vp, vp], ip),
         "hfx_assembly_info": ([vp, vp], ip),
         "hfx_la_create": ([vp, ctypes.POINTER(vp)], ip),
         "hfx_la_destroy": ([vp], ip),
@@ -228,6 +233,89 @@ def mesh_high_order(dim, order, coords, cells):
     if rc:
         raise HfxError(rc, "mesh_high_order: " + L.hfx_mesh_io_error().decode())
     return out_c, out_e
+
+
+FIELD_NONE, FIELD_NODE, FIELD_EDGE, FIELD_FACE, FIELD_CELL = -1, 0, 1, 2, 3
+
+
+def h5_read_mesh(path):
+    """(coords [nNodes][nodeDim], cells [nCells][nodesPerCell]) from /Mesh of an HDF5 file (host only)."""
+    L = load()
+    nd, nn, nc, npc = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    refs = (ctypes.byref(nd), ctypes.byref(nn), ctypes.byref(nc), ctypes.byref(npc))
+    rc = L.hfx_h5_read_mesh(str(path).encode(), *refs, None, None)
+    if rc:
+        raise HfxError(rc, "h5_read_mesh: " + L.hfx_mesh_io_error().decode())
+    coords = np.zeros((nn.value, nd.value))
+    cells = np.zeros((nc.value, npc.value), np.int32)
+    rc = L.hfx_h5_read_mesh(str(path).encode(), *refs, _p(coords), _p(cells))
+    if rc:
+        raise HfxError(rc, "h5_read_mesh: " + L.hfx_mesh_io_error().decode())
+    return coords, cells
+
+
+def h5_field_names(path):
+    """Names of the datasets under /FieldData (sorted)."""
+    L = load()
+    n, need = ctypes.c_int(), ctypes.c_int()
+    rc = L.hfx_h5_field_names(str(path).encode(), None, 0, ctypes.byref(n), ctypes.byref(need))
+    if rc:
+        raise HfxError(rc, "h5_field_names: " + L.hfx_mesh_io_error().decode())
+    buf = ctypes.create_string_buffer(need.value)
+    rc = L.hfx_h5_field_names(str(path).encode(), buf, need.value, ctypes.byref(n), ctypes.byref(need))
+    if rc:
+        raise HfxError(rc, "h5_field_names: " + L.hfx_mesh_io_error().decode())
+    return [x for x in buf.value.decode().split("\n") if x]
+
+
+def h5_read_field(path, name):
+    """(ftype, values [entities][objs][vals]) of /FieldData/<name>."""
+    L = load()
+    ft = ctypes.c_int()
+    shape = np.zeros(3, np.int64)
+    rc = L.hfx_h5_read_field(str(path).encode(), name.encode(), ctypes.byref(ft), _p(shape), None)
+    if rc:
+        raise HfxError(rc, "h5_read_field: " + L.hfx_mesh_io_error().decode())
+    vals = np.zeros(tuple(int(x) for x in shape))
+    rc = L.hfx_h5_read_field(str(path).encode(), name.encode(), ctypes.byref(ft), _p(shape), _p(vals))
+    if rc:
+        raise HfxError(rc, "h5_read_field: " + L.hfx_mesh_io_error().decode())
+    return ft.value, vals
+
+
+def h5_write(path, coords=None, cells=None, fields=None):
+    """Write /Mesh (when coords and cells are given) and /FieldData (fields: {name: (ftype, values)},
+    values reshaped to [entities][objs][vals] when 3-D, [entities][objs][1] when 2-D)."""
+    L = load()
+    nd = nn = nc = npc = 0
+    pc = pe = None
+    if coords is not None:
+        coords = np.ascontiguousarray(coords, np.float64)
+        cells = np.ascontiguousarray(cells, np.int32)
+        nn, nd = coords.shape
+        nc, npc = cells.shape
+        pc, pe = _p(coords), _p(cells)
+    fields = fields or {}
+    names = (ctypes.c_char_p * max(1, len(fields)))()
+    ftypes = np.zeros(max(1, len(fields)), np.int32)
+    shapes = np.zeros(3 * max(1, len(fields)), np.int64)
+    vptrs = (ctypes.c_void_p * max(1, len(fields)))()
+    keep = []
+    for i, (name, (ft, vals)) in enumerate(fields.items()):
+        v = np.ascontiguousarray(vals, np.float64)
+        if v.ndim == 2:
+            v = v[:, :, None]
+        if v.ndim != 3:
+            raise ValueError("field values must be 2-D or 3-D")
+        keep.append(v)
+        names[i] = name.encode()
+        ftypes[i] = ft
+        shapes[3 * i:3 * i + 3] = v.shape
+        vptrs[i] = v.ctypes.data
+    rc = L.hfx_h5_write(str(path).encode(), nd, nn, pc, nc, npc, pe, len(fields), ctypes.cast(names, ctypes.c_void_p),
+                        _p(ftypes), _p(shapes), ctypes.cast(vptrs, ctypes.c_void_p))
+    if rc:
+        raise HfxError(rc, "h5_write: " + L.hfx_mesh_io_error().decode())
 
 
 def solve_opts(**kw):

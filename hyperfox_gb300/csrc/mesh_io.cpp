@@ -187,6 +187,9 @@ int high_order(int dim, int order, int nLin, const double* lin, int nCells, cons
 }
 
 }  // namespace
+
+void set_io_error(const std::string& m) { g_ioErr = m; }
+
 }  // namespace hfx
 
 using namespace hfx;

@@ -159,7 +159,7 @@ class GpuLinAlgebraInterface {
 };
 
 // ---------------------------------------------------------------- mesh, fields, models
-enum FieldType { Node = 0, Face = 2, Cell = 3 };  // FieldTypes.h
+enum FieldType { None = -1, Node = 0, Edge = 1, Face = 2, Cell = 3 };  // FieldTypes.h
 
 // Simplex mesh: nodes [nNodes][dim], cells [nCells][N] (vertices first).
 struct Mesh {
@@ -295,6 +295,75 @@ class GpuHDGSolver {
   DirichletModel* bnd_ = nullptr;
   GpuSolverOpts opts_;
   bool haveLin_ = false, initialized_ = false, allocated_ = false, assembled_ = false, trained_ = false;
+};
+
+// ---------------------------------------------------------------- HDF5Io
+// HDF5Io (src/io/HDF5Io.cpp:13-393) on the host reader/writer: load() fills the
+// mesh from /Mesh when present and every registered field from /FieldData (the
+// field's type and shape come from the file); write() stores the mesh and the
+// registered fields. The mesh's dim and order select the reference element, as
+// for Mesh(dim, order, "simplex") before HDF5Io::load.
+class HDF5Io {
+ public:
+  HDF5Io() = default;
+  explicit HDF5Io(Mesh* m) : mesh_(m) {}
+  void setMesh(Mesh* m) { mesh_ = m; }
+  void setField(const std::string& name, Field* f) { fields_[name] = f; }
+  void load(const std::string& path) {
+    if (!mesh_) throw ErrorHandle("HDF5Io", "load", "must enter a mesh into the io before loading a file.");
+    int nd = 0, nn = 0, nc = 0, npc = 0;
+    int rc = hfx_h5_read_mesh(path.c_str(), &nd, &nn, &nc, &npc, nullptr, nullptr);
+    const bool haveMesh = rc == HFX_OK;
+    if (haveMesh) {
+      if (nd != mesh_->dim || npc != mesh_->nodesPerCell())
+        throw ErrorHandle("HDF5Io", "load", "the file's mesh does not match the mesh's dimension and order");
+      mesh_->nodes.assign((size_t)nn * nd, 0.0);
+      mesh_->cells.assign((size_t)nc * npc, 0);
+      check(hfx_h5_read_mesh(path.c_str(), &nd, &nn, &nc, &npc, mesh_->nodes.data(), mesh_->cells.data()), "load");
+      mesh_->nFaces = 0;
+    }
+    int nf = 0, need = 0;
+    const bool haveFields = hfx_h5_field_names(path.c_str(), nullptr, 0, &nf, &need) == HFX_OK && nf > 0;
+    if (!haveMesh && !haveFields)
+      throw ErrorHandle("HDF5Io", "load", "could not find Mesh or FieldData groups in file: " + std::string(hfx_mesh_io_error()));
+    for (auto& kv : fields_) {
+      int ft = 0;
+      int64_t shape[3] = {0, 0, 0};
+      check(hfx_h5_read_field(path.c_str(), kv.first.c_str(), &ft, shape, nullptr), "load");
+      Field* f = kv.second;
+      f->type = (FieldType)ft;
+      f->obj = (int)shape[1];
+      f->vals = (int)shape[2];
+      f->values.assign((size_t)(shape[0] * shape[1] * shape[2]), 0.0);
+      check(hfx_h5_read_field(path.c_str(), kv.first.c_str(), &ft, shape, f->values.data()), "load");
+    }
+  }
+  void write(const std::string& path) {
+    std::vector<const char*> names;
+    std::vector<int> types;
+    std::vector<int64_t> shapes;
+    std::vector<const double*> vals;
+    for (auto& kv : fields_) {
+      const Field* f = kv.second;
+      const int64_t per = (int64_t)f->obj * f->vals;
+      names.push_back(kv.first.c_str());
+      types.push_back((int)f->type);
+      shapes.insert(shapes.end(), {per ? (int64_t)f->values.size() / per : 0, (int64_t)f->obj, (int64_t)f->vals});
+      vals.push_back(f->values.data());
+    }
+    const bool m = mesh_ && !mesh_->cells.empty();
+    check(hfx_h5_write(path.c_str(), m ? mesh_->dim : 0, m ? mesh_->numNodes() : 0, m ? mesh_->nodes.data() : nullptr,
+                       m ? mesh_->numCells() : 0, m ? mesh_->nodesPerCell() : 0, m ? mesh_->cells.data() : nullptr,
+                       (int)names.size(), names.data(), types.data(), shapes.data(), vals.data()),
+          "write");
+  }
+
+ private:
+  static void check(int rc, const char* where) {
+    if (rc) throw ErrorHandle("HDF5Io", where, hfx_mesh_io_error());
+  }
+  Mesh* mesh_ = nullptr;
+  std::map<std::string, Field*> fields_;
 };
 
 }  // namespace gpu

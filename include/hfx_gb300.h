@@ -154,11 +154,33 @@ int hfx_mesh_topology(hfx_ctx* ctx, int* cell2face, int* face2cell, int* faces, 
  * sizes. hfx_mesh_high_order maps the reference nodes of order `order` into every
  * linear cell and merges coincident nodes: coords [nNodes][dim], cells
  * [nCells][N] in reference-node order, ready for hfx_mesh_upload (two-call
- * likewise). hfx_mesh_io_error returns the last message of these two. */
+ * likewise). hfx_mesh_io_error returns the last message of these and of the HDF5 calls below. */
 int hfx_gmsh_read(const char* path, int dim, int* nNodes, int* nCells, double* coords, int* cells);
 int hfx_mesh_high_order(int dim, int order, int nLinNodes, const double* linCoords, int nCells, const int* linCells,
                         int* nNodes, double* coords, int* cells);
 const char* hfx_mesh_io_error(void);
+
+/* ---- HDF5 mesh and field files (host, no GPU, no HDF5 library) --------------
+ * Replace HDF5Io::load / loadMesh / loadFields and HDF5Io::write / writeMesh /
+ * writeFields (src/io/HDF5Io.cpp:13-62,111-191 and :64-109,193-393) for the
+ * files they exchange: /Mesh/Nodes float64 [nNodes][nodeDim], /Mesh/Cells int32
+ * [nCells][nodesPerCell], /FieldData/<name> float64 [entities][objs][vals] with
+ * the int attribute "ftype" (FieldType: -1 None, 0 Node, 1 Edge, 2 Face, 3 Cell).
+ * hfx_h5_read_mesh: call with coords == cells == NULL for the sizes.
+ * hfx_h5_field_names: the names under /FieldData, each followed by '\n', into
+ * buf (truncated to bufLen-1 and terminated); *needLen = the length it needs.
+ * hfx_h5_read_field: shape[3] and *ftype always; values when not NULL. Missing
+ * field or attribute -> HFX_ERR_ARG with the reference's message.
+ * hfx_h5_write: mesh when nNodes > 0, then nFields fields (names[i], ftypes[i],
+ * shapes[3*i..3*i+2], values[i]); at least one of the two. Errors in
+ * hfx_mesh_io_error(). */
+int hfx_h5_read_mesh(const char* path, int* nodeDim, int* nNodes, int* nCells, int* nodesPerCell, double* coords,
+                     int* cells);
+int hfx_h5_field_names(const char* path, char* buf, int bufLen, int* nFields, int* needLen);
+int hfx_h5_read_field(const char* path, const char* name, int* ftype, int64_t* shape, double* values);
+int hfx_h5_write(const char* path, int nodeDim, int nNodes, const double* coords, int nCells, int nodesPerCell,
+                 const int* cells, int nFields, const char* const* names, const int* ftypes, const int64_t* shapes,
+                 const double* const* values);
 
 /* ---- fields (the HDGSolver field map) --------------------------------------
  * Tau: Face field, nVals 1 or 2 (double valued, side 0 = face2cell[0]).

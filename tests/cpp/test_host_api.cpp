@@ -1,9 +1,11 @@
 // The reference's own unit tests, re-expressed against the C++ host API
-// (TestLinAlgebraInterfaces.cpp:23-150, TestHDGSolver.cpp:14-101).
+// (TestLinAlgebraInterfaces.cpp:23-150, TestHDGSolver.cpp:14-101, TestHDF5Io.cpp
+// write mesh / write field sections).
 // Exits non-zero on the first failed check.
 #include <cmath>
 #include <cstdio>
 #include <functional>
+#include <string>
 #include <vector>
 
 #include "../../hyperfox_gb300/host/hfx_host_api.hpp"
@@ -27,7 +29,46 @@ static bool throws(const std::function<void()>& f) {
   return false;
 }
 
-int main() {
+int main(int argc, char** argv) {
+  {  // HDF5Io write then load of a mesh and two fields (TestHDF5Io.cpp "Test write mesh file", "Write test field")
+    const std::string path = std::string(argc > 1 ? argv[1] : ".") + "/tmp.h5";
+    Mesh m;
+    m.dim = 2;
+    m.order = 1;
+    m.nodes = {0, 0, 1, 0, 1, 1, 0, 1, 0.5, 0.5, 0.5, 0, 1, 0.5, 0.5, 1, 0, 0.5};
+    m.cells = {0, 5, 4, 5, 1, 4, 1, 6, 4, 6, 2, 4, 2, 7, 4, 7, 3, 4, 3, 8, 4, 8, 0, 4};
+    Field nodeField(&m, Node, 1, 1), cellField(&m, Cell, 2, 1);
+    for (int i = 0; i < 9; ++i) nodeField.values[i] = i;
+    for (int i = 0; i < 8; ++i) {
+      cellField.values[2 * i] = i;
+      cellField.values[2 * i + 1] = -i;
+    }
+    HDF5Io io(&m);
+    io.setField("NodeField", &nodeField);
+    io.setField("CellField", &cellField);
+    io.write(path);
+    Mesh m2;
+    m2.dim = 2;
+    m2.order = 1;
+    Field nf2(&m2, None, 1, 1), cf2(&m2, None, 1, 1);
+    HDF5Io io2(&m2);
+    io2.setField("NodeField", &nf2);
+    io2.setField("CellField", &cf2);
+    io2.load(path);
+    CHECK(m2.nodes == m.nodes && m2.cells == m.cells);
+    CHECK(nf2.type == Node && nf2.values == nodeField.values);
+    CHECK(cf2.type == Cell && cf2.obj == 2 && cf2.values == cellField.values);
+    Field missing(&m2, None, 1, 1);
+    io2.setField("Solution", &missing);
+    CHECK(throws([&] { io2.load(path); }));
+    HDF5Io noMesh;
+    CHECK(throws([&] { noMesh.load(path); }));
+    Mesh wrongOrder;
+    wrongOrder.dim = 2;
+    wrongOrder.order = 2;
+    HDF5Io io3(&wrongOrder);
+    CHECK(throws([&] { io3.load(path); }));
+  }
   Device dev(0);
   {  // ordering of initialize -> configure -> allocate (TestLinAlgebraInterfaces.cpp:23-67)
     GpuSolverOpts o;

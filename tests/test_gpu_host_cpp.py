@@ -1,6 +1,6 @@
 """The reference's own unit tests re-expressed in C++ against the host API
 (tests/cpp/test_host_api.cpp: TestLinAlgebraInterfaces.cpp ordering/identity/
-triangular, TestHDGSolver.cpp setup sequence + constant Dirichlet)."""
+triangular, TestHDGSolver.cpp setup sequence + constant Dirichlet, TestHDF5Io.cpp write/load)."""
 import os
 import subprocess
 
@@ -18,6 +18,6 @@ def test_cpp_host_api(hfx_lib, tmp_path):
                            "-I", os.path.join(ROOT, "hyperfox_gb300", "host"),
                            os.path.join(ROOT, "tests", "cpp", "test_host_api.cpp"), "-L", lib, "-lhfx_gb300",
                            "-Wl,-rpath," + lib, "-o", exe])
-    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    r = subprocess.run([exe, str(tmp_path)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "OK" in r.stdout
