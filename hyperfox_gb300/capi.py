@@ -37,6 +37,8 @@ EXPORTED = [
     "hfx_mesh_upload", "hfx_mesh_sizes", "hfx_mesh_topology", "hfx_mesh_compute_topology",
     "hfx_gmsh_read", "hfx_mesh_high_order", "hfx_mesh_io_error",
     "hfx_h5_read_mesh", "hfx_h5_field_names", "hfx_h5_read_field", "hfx_h5_write",
+    "hfx_rk_butcher", "hfx_rk_set", "hfx_rk_set_type", "hfx_rk_begin_step", "hfx_rk_compute_stage",
+    "hfx_rk_compute_solution", "hfx_set_trace", "hfx_get_state",
     "hfx_set_tau", "hfx_set_kappa", "hfx_set_source", "hfx_set_dirichlet", "hfx_set_time_scheme",
     "hfx_ip_coords", "hfx_assemble", "hfx_assemble_ex", "hfx_set_solver_type", "hfx_set_state", "hfx_set_assembly_path", "hfx_assembly_info", "hfx_get_condensed", "hfx_get_csr",
     "hfx_solve_opts_default", "hfx_solve", "hfx_recover", "hfx_coarse_operator", "hfx_coarse_train",
@@ -129,6 +131,14 @@ def load(path=LIB_PATH):
         "hfx_h5_field_names": ([ctypes.c_char_p, ctypes.c_char_p, ip, vp, vp], ip),
         "hfx_h5_read_field": ([ctypes.c_char_p, ctypes.c_char_p, vp, vp, vp], ip),
         "hfx_h5_write": ([ctypes.c_char_p, ip, ip, vp, ip, ip, vp, ip, vp, vp, vp, vp], ip),
+        "hfx_rk_butcher": ([ip, vp, vp], ip),
+        "hfx_rk_set": ([vp, ip, vp, ctypes.c_double], ip),
+        "hfx_rk_set_type": ([vp, ip, ctypes.c_double], ip),
+        "hfx_rk_begin_step": ([vp], ip),
+        "hfx_rk_compute_stage": ([vp], ip),
+        "hfx_rk_compute_solution": ([vp], ip),
+        "hfx_set_trace": ([vp, vp], ip),
+        "hfx_get_state": ([vp, vp, vp, vp], ip),
         "hfx_assembly_info": ([vp, vp], ip),
         "hfx_la_create": ([vp, ctypes.POINTER(vp)], ip),
         "hfx_la_destroy": ([vp], ip),
@@ -236,6 +246,23 @@ def mesh_high_order(dim, order, coords, cells):
 
 
 FIELD_NONE, FIELD_NODE, FIELD_EDGE, FIELD_FACE, FIELD_CELL = -1, 0, 1, 2, 3
+
+# RKType (RKType.h): explicit FEuler..RK4, implicit BEuler..RK43
+RK_TYPES = ["FEuler", "EMidpoint", "Heun", "Kutta3", "Heun3", "SSPRK3", "RK4",
+            "BEuler", "IMidpoint", "CrankNicolson", "KS2", "QZ2", "ALX2", "RK43"]
+
+
+def rk_butcher(rk_type):
+    """Butcher table [(S+1) x (S+1)] of a named scheme (index or name in RK_TYPES)."""
+    L = load()
+    t = RK_TYPES.index(rk_type) if isinstance(rk_type, str) else int(rk_type)
+    S = ctypes.c_int()
+    rc = L.hfx_rk_butcher(t, ctypes.byref(S), None)
+    if rc:
+        raise HfxError(rc, "rk_butcher: unknown type")
+    tab = np.zeros((S.value + 1, S.value + 1))
+    L.hfx_rk_butcher(t, ctypes.byref(S), _p(tab))
+    return tab
 
 
 def h5_read_mesh(path):
@@ -456,6 +483,12 @@ class Context:
                                              _p(val), _p(vn)), "coarse_operator")
         return rowptr, col, val, vn
 
+    def assembly_info(self):
+        """1 when the last FP64 assembly ran the affine element kernel, else 0."""
+        v = ctypes.c_int()
+        self._chk(self.L.hfx_assembly_info(self.h, ctypes.byref(v)), "assembly_info")
+        return v.value
+
     def set_solver_type(self, t):
         self._chk(self.L.hfx_set_solver_type(self.h, t), "set_solver_type")
 
@@ -463,6 +496,39 @@ class Context:
         sol = np.ascontiguousarray(sol, np.float64)
         flux = np.ascontiguousarray(flux, np.float64)
         self._chk(self.L.hfx_set_state(self.h, _p(sol), _p(flux)), "set_state")
+
+    def set_trace(self, trace):
+        trace = np.ascontiguousarray(trace, np.float64)
+        self._chk(self.L.hfx_set_trace(self.h, _p(trace)), "set_trace")
+
+    def get_state(self):
+        """(Solution [nCells][N], Flux [nCells][N*dim], Trace [ndofs]) as held on the device."""
+        sol = np.zeros((self.nCells, self.lenU))
+        flux = np.zeros((self.nCells, self.lenQ))
+        trace = np.zeros(self.ndofs)
+        self._chk(self.L.hfx_get_state(self.h, _p(sol), _p(flux), _p(trace)), "get_state")
+        return sol, flux, trace
+
+    def rk_set(self, scheme, dt):
+        """Runge-Kutta scheme: a name / RKType index (table taken as is) or a user
+        table (checked like RungeKutta::setButcherTable); None switches it off."""
+        if scheme is None:
+            self._chk(self.L.hfx_rk_set(self.h, 0, None, 0.0), "rk_set")
+        elif isinstance(scheme, (str, int)):
+            t = RK_TYPES.index(scheme) if isinstance(scheme, str) else scheme
+            self._chk(self.L.hfx_rk_set_type(self.h, t, dt), "rk_set_type")
+        else:
+            tab = np.ascontiguousarray(scheme, np.float64)
+            self._chk(self.L.hfx_rk_set(self.h, tab.shape[0] - 1, _p(tab), dt), "rk_set")
+
+    def rk_begin_step(self):
+        self._chk(self.L.hfx_rk_begin_step(self.h), "rk_begin_step")
+
+    def rk_compute_stage(self):
+        self._chk(self.L.hfx_rk_compute_stage(self.h), "rk_compute_stage")
+
+    def rk_compute_solution(self):
+        self._chk(self.L.hfx_rk_compute_solution(self.h), "rk_compute_solution")
 
     def coarse_train(self, degree=4, samples=16, steps=300):
         info = TrainInfo()

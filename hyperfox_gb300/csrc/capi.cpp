@@ -108,6 +108,15 @@ struct hfx_ctx {
   double* d_atab = nullptr;    // affine reference operators
   double* d_geo = nullptr;     // [nCells][D*D + F*D]
   double* d_prep = nullptr;    // [nCells][affine_prep_doubles] per-element affine record
+  // Runge-Kutta (RungeKutta.cpp): Butcher table (S+1)^2 row-major, stage counter,
+  // Old*/RKStage_* fields and the stage vector w on the device
+  int rkStages = 0, rkStage = 0;
+  std::vector<double> rkTable;
+  double rkDt = 0.0;
+  DevMem rkMem;
+  double *d_oldSol = nullptr, *d_oldFlux = nullptr, *d_oldTrace = nullptr;
+  std::vector<double*> d_kSol, d_kFlux, d_kTrace;
+  double *d_wU = nullptr, *d_wQ = nullptr, *d_wL = nullptr;
   // outputs
   DevMem outMem;
   double *d_S = nullptr, *d_S0 = nullptr, *d_U = nullptr, *d_Q = nullptr, *d_U0 = nullptr, *d_Q0 = nullptr;
@@ -187,6 +196,12 @@ void free_outputs(hfx_ctx* c) {
   c->wsMem.release();
   c->d_S = c->d_S0 = c->d_U = c->d_Q = c->d_U0 = c->d_Q0 = c->d_val = c->d_rhs = c->d_trace = nullptr;
   c->d_sol = c->d_flux = c->d_geo = c->d_prep = nullptr;
+  c->rkStages = c->rkStage = 0;  // Runge-Kutta fields follow the mesh
+  c->rkMem.release();
+  c->d_kSol.clear();
+  c->d_kFlux.clear();
+  c->d_kTrace.clear();
+  c->d_oldSol = c->d_oldFlux = c->d_oldTrace = c->d_wU = c->d_wQ = c->d_wL = nullptr;
   c->qValid = c->lastAffine = false;
   c->mixMem.release();
   c->d_S32 = c->d_S032 = c->d_U32 = c->d_Q32 = c->d_U032 = c->d_Q032 = c->d_dl32 = nullptr;
@@ -652,6 +667,30 @@ static int assemble_fp64(hfx_ctx* c) {
   p.explicitMode = c->solverType;
   p.solState = c->d_sol;
   p.fluxState = c->d_flux;
+  if (c->rkStages > 0) {
+    // RungeKutta::apply (RungeKutta.cpp:90-129) for stage s: w = (dt - c) ut + dt^2 sum_{i<s} a_si k_i
+    const int S = c->rkStages, st = c->rkStage;
+    const double dt = c->rkDt, cst = dt * c->rkTable[(size_t)st * (S + 1) + 1 + st];
+    const int64_t E = c->nCells, LU = c->re.nNodes, LQ = (int64_t)c->dim * c->re.nNodes;
+    double* outs[3] = {c->d_wU, c->d_wQ, c->d_wL};
+    const double* olds[3] = {c->d_oldSol, c->d_oldFlux, c->d_oldTrace};
+    const std::vector<double*>* ks[3] = {&c->d_kSol, &c->d_kFlux, &c->d_kTrace};
+    const int64_t len[3] = {E * LU, E * LQ, c->ndofs()};
+    for (int f = 0; f < 3; ++f) {
+      RkTerms tr{};
+      for (int i = 0; i < st; ++i) {
+        tr.coef[tr.n] = dt * dt * c->rkTable[(size_t)st * (S + 1) + 1 + i];
+        tr.ptr[tr.n++] = (*ks[f])[i];
+      }
+      HFX_CUDA(c, launch_rk_lincomb(len[f], outs[f], dt - cst, olds[f], tr, s));
+    }
+    p.dt = dt;
+    p.uOld = c->d_oldSol;
+    p.cStiff = cst;
+    p.rkWu = c->d_wU;
+    p.rkWq = c->d_wQ;
+    p.rkWl = c->d_wL;
+  }
   const bool affine = c->assemblyPath == 0 && c->affineMesh && c->kappaCellConstant && c->d_atab && c->d_prep;
   c->timer.begin(K_LOCAL, s);
   if (affine) HFX_CUDA(c, launch_local_affine(c->dim, c->order, p, c->d_atab, c->d_geo, c->d_prep, s));
@@ -855,6 +894,8 @@ int hfx_assemble_ex(hfx_ctx* c, int precision) {
   c->coarse.ready = false;  // the coarse operator follows the element matrices
   if (precision == HFX_PREC_MIXED && c->solverType != HFX_IMPLICIT)
     return set_err(c, HFX_ERR_UNSUPPORTED, "assemble: the explicit modes assemble in FP64");
+  if (precision == HFX_PREC_MIXED && c->rkStages > 0)
+    return set_err(c, HFX_ERR_UNSUPPORTED, "assemble: Runge-Kutta stages assemble in FP64");
   return precision == HFX_PREC_MIXED ? assemble_mixed(c) : assemble_fp64(c);
 }
 
@@ -889,6 +930,226 @@ int hfx_set_state(hfx_ctx* c, const double* solution, const double* flux) {
                               c->stream));
   HFX_CUDA(c, cudaStreamSynchronize(c->stream));
   c->assembled = false;
+  return HFX_OK;
+}
+
+int hfx_set_trace(hfx_ctx* c, const double* trace) {
+  if (!c || !trace) return HFX_ERR_ARG;
+  if (!c->haveMesh) return set_err(c, HFX_ERR_STATE, "set_trace: upload a mesh first");
+  cudaSetDevice(c->device);
+  int rc = ensure_outputs(c);
+  if (rc) return rc;
+  HFX_CUDA(c, cudaMemcpyAsync(c->d_trace, trace, sizeof(double) * c->ndofs(), cudaMemcpyHostToDevice, c->stream));
+  HFX_CUDA(c, cudaStreamSynchronize(c->stream));
+  return HFX_OK;
+}
+
+int hfx_get_state(hfx_ctx* c, double* solution, double* flux, double* trace) {
+  if (!c) return HFX_ERR_ARG;
+  if (!c->haveMesh) return set_err(c, HFX_ERR_STATE, "get_state: upload a mesh first");
+  cudaSetDevice(c->device);
+  int rc = ensure_outputs(c);
+  if (rc) return rc;
+  const size_t E = (size_t)c->nCells;
+  if (solution)
+    HFX_CUDA(c, cudaMemcpyAsync(solution, c->d_sol, sizeof(double) * E * c->re.nNodes, cudaMemcpyDeviceToHost,
+                                c->stream));
+  if (flux)
+    HFX_CUDA(c, cudaMemcpyAsync(flux, c->d_flux, sizeof(double) * E * c->re.nNodes * c->dim, cudaMemcpyDeviceToHost,
+                                c->stream));
+  if (trace)
+    HFX_CUDA(c, cudaMemcpyAsync(trace, c->d_trace, sizeof(double) * c->ndofs(), cudaMemcpyDeviceToHost, c->stream));
+  HFX_CUDA(c, cudaStreamSynchronize(c->stream));
+  return HFX_OK;
+}
+
+// Butcher tables of RungeKutta::setUpDB (RungeKutta.cpp:215-286), the published
+// coefficients of each scheme; rows [c_i | a_i0 .. a_i(s-1)], last row [0 | b].
+int hfx_rk_butcher(int type, int* nStages, double* table) {
+  if (!nStages) return HFX_ERR_ARG;
+  const double g = 1.0 - std::sqrt(2.0) / 2.0;
+  std::vector<double> t;
+  int S = 0;
+  switch (type) {
+    case HFX_RK_FEULER: S = 1; t = {0, 0, 0, 1}; break;
+    case HFX_RK_EMIDPOINT: S = 2; t = {0, 0, 0, 0.5, 0.5, 0, 0, 0, 1}; break;
+    case HFX_RK_HEUN: S = 2; t = {0, 0, 0, 1, 1, 0, 0, 0.5, 0.5}; break;
+    case HFX_RK_KUTTA3: S = 3; t = {0, 0, 0, 0, 0.5, 0.5, 0, 0, 1, -1, 2, 0, 0, 1.0 / 6, 2.0 / 3, 1.0 / 6}; break;
+    case HFX_RK_HEUN3: S = 3; t = {0, 0, 0, 0, 1.0 / 3, 1.0 / 3, 0, 0, 2.0 / 3, 0, 2.0 / 3, 0, 0, 0.25, 0, 0.75}; break;
+    case HFX_RK_SSPRK3: S = 3; t = {0, 0, 0, 0, 1, 1, 0, 0, 0.5, 0.25, 0.25, 0, 0, 1.0 / 6, 1.0 / 6, 2.0 / 3}; break;
+    case HFX_RK_RK4:
+      S = 4;
+      t = {0, 0, 0, 0, 0, 0.5, 0.5, 0, 0, 0, 0.5, 0, 0.5, 0, 0, 1, 0, 0, 1, 0, 0, 1.0 / 6, 1.0 / 3, 1.0 / 3, 1.0 / 6};
+      break;
+    case HFX_RK_BEULER: S = 1; t = {1, 1, 0, 1}; break;
+    case HFX_RK_IMIDPOINT: S = 1; t = {0.5, 0.5, 0, 1}; break;
+    case HFX_RK_CRANKNICOLSON: S = 2; t = {0, 0, 0, 1, 0.5, 0.5, 0, 0.5, 0.5}; break;
+    case HFX_RK_KS2: S = 2; t = {0.5, 0.5, 0, 1.5, -0.5, 2, 0, -0.5, 1.5}; break;
+    case HFX_RK_QZ2: S = 2; t = {0.25, 0.25, 0, 0.75, 0.5, 0.25, 0, 0.5, 0.5}; break;
+    case HFX_RK_ALX2: S = 2; t = {g, g, 0, 1, 1 - g, g, 0, 1 - g, g}; break;
+    case HFX_RK_RK43:
+      S = 4;
+      t = {0.5, 0.5, 0, 0, 0, 2.0 / 3, 1.0 / 6, 0.5, 0, 0, 0.5, -0.5, 0.5, 0.5, 0, 1, 1.5, -1.5, 0.5, 0.5,
+           0, 1.5, -1.5, 0.5, 0.5};
+      break;
+    default: return HFX_ERR_ARG;
+  }
+  *nStages = S;
+  if (table) std::copy(t.begin(), t.end(), table);
+  return HFX_OK;
+}
+
+static void rk_clear(hfx_ctx* c) {
+  cudaStreamSynchronize(c->stream);
+  c->rkStages = c->rkStage = 0;
+  c->rkMem.release();
+  c->d_kSol.clear();
+  c->d_kFlux.clear();
+  c->d_kTrace.clear();
+  c->d_oldSol = c->d_oldFlux = c->d_oldTrace = c->d_wU = c->d_wQ = c->d_wL = nullptr;
+}
+
+static int rk_configure(hfx_ctx* c, int nStages, const double* table, double dt) {
+  if (!(dt > 0.0)) return set_err(c, HFX_ERR_ARG, "rk_set: the time step needs to be set and it should not be 0");
+  const int W = nStages + 1;
+  cudaSetDevice(c->device);
+  int rc = ensure_outputs(c);
+  if (rc) return rc;
+  rk_clear(c);
+  c->d_kSol.assign(nStages, nullptr);
+  c->d_kFlux.assign(nStages, nullptr);
+  c->d_kTrace.assign(nStages, nullptr);
+  const size_t E = (size_t)c->nCells, LU = c->re.nNodes, LQ = (size_t)c->dim * c->re.nNodes, n = c->ndofs();
+  DevMem& m = c->rkMem;
+  HFX_CUDA(c, dalloc(m, &c->d_oldSol, E * LU));
+  HFX_CUDA(c, dalloc(m, &c->d_oldFlux, E * LQ));
+  HFX_CUDA(c, dalloc(m, &c->d_oldTrace, n));
+  HFX_CUDA(c, dalloc(m, &c->d_wU, E * LU));
+  HFX_CUDA(c, dalloc(m, &c->d_wQ, E * LQ));
+  HFX_CUDA(c, dalloc(m, &c->d_wL, n));
+  for (int k = 0; k < nStages; ++k) {
+    HFX_CUDA(c, dalloc(m, &c->d_kSol[k], E * LU));
+    HFX_CUDA(c, dalloc(m, &c->d_kFlux[k], E * LQ));
+    HFX_CUDA(c, dalloc(m, &c->d_kTrace[k], n));
+  }
+  c->rkTable.assign(table, table + (size_t)W * W);
+  c->rkStages = nStages;
+  c->rkStage = 0;
+  c->rkDt = dt;
+  c->assembled = false;
+  // Old* = the current fields until the first begin_step
+  HFX_CUDA(c, cudaMemcpyAsync(c->d_oldSol, c->d_sol, sizeof(double) * E * LU, cudaMemcpyDeviceToDevice, c->stream));
+  HFX_CUDA(c, cudaMemcpyAsync(c->d_oldFlux, c->d_flux, sizeof(double) * E * LQ, cudaMemcpyDeviceToDevice, c->stream));
+  HFX_CUDA(c, cudaMemcpyAsync(c->d_oldTrace, c->d_trace, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
+  HFX_CUDA(c, cudaStreamSynchronize(c->stream));
+  return HFX_OK;
+}
+
+// RungeKutta::setButcherTable(EMatrix) (RungeKutta.cpp:18-32): a square table
+// whose strictly upper part (first column included) is zero; 0 stages = off.
+int hfx_rk_set(hfx_ctx* c, int nStages, const double* table, double dt) {
+  if (!c) return HFX_ERR_ARG;
+  if (!c->haveMesh) return set_err(c, HFX_ERR_STATE, "rk_set: upload a mesh first");
+  if (nStages == 0) {
+    rk_clear(c);
+    c->assembled = false;
+    return HFX_OK;
+  }
+  if (nStages < 0 || nStages > RkTerms::MAX || !table) return set_err(c, HFX_ERR_ARG, "rk_set: 1..8 stages and a table");
+  const int W = nStages + 1;
+  for (int i = 0; i < W; ++i)
+    for (int j = i + 1; j < W; ++j)
+      if (table[i * W + j] != 0.0)
+        return set_err(c, HFX_ERR_ARG,
+                       "rk_set: the upper triangular part of the Butcher table should be null (no fully implicit "
+                       "implementation as of yet)");
+  return rk_configure(c, nStages, table, dt);
+}
+
+// RungeKutta(re, RKType) (RungeKutta.cpp:5-16): a named table, taken as is.
+int hfx_rk_set_type(hfx_ctx* c, int type, double dt) {
+  if (!c) return HFX_ERR_ARG;
+  if (!c->haveMesh) return set_err(c, HFX_ERR_STATE, "rk_set_type: upload a mesh first");
+  int S = 0;
+  if (hfx_rk_butcher(type, &S, nullptr)) return set_err(c, HFX_ERR_ARG, "rk_set_type: unknown Runge-Kutta type");
+  std::vector<double> t((size_t)(S + 1) * (S + 1));
+  hfx_rk_butcher(type, &S, t.data());
+  return rk_configure(c, S, t.data(), dt);
+}
+
+int hfx_rk_begin_step(hfx_ctx* c) {
+  if (!c) return HFX_ERR_ARG;
+  if (c->rkStages == 0) return set_err(c, HFX_ERR_STATE, "rk_begin_step: no Runge-Kutta scheme set");
+  if (c->rkStage != 0) return set_err(c, HFX_ERR_STATE, "rk_begin_step: the previous step has stages left");
+  const size_t E = (size_t)c->nCells, LU = c->re.nNodes, LQ = (size_t)c->dim * c->re.nNodes, n = c->ndofs();
+  HFX_CUDA(c, cudaMemcpyAsync(c->d_oldSol, c->d_sol, sizeof(double) * E * LU, cudaMemcpyDeviceToDevice, c->stream));
+  HFX_CUDA(c, cudaMemcpyAsync(c->d_oldFlux, c->d_flux, sizeof(double) * E * LQ, cudaMemcpyDeviceToDevice, c->stream));
+  HFX_CUDA(c, cudaMemcpyAsync(c->d_oldTrace, c->d_trace, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
+  c->assembled = false;
+  return HFX_OK;
+}
+
+// RungeKutta::computeStage (RungeKutta.cpp:131-170): k_s = (x - x_old) / dt,
+// x = x_old + dt sum_{j<=s} a_sj k_j for Solution, Flux and Trace.
+int hfx_rk_compute_stage(hfx_ctx* c) {
+  if (!c) return HFX_ERR_ARG;
+  if (c->rkStages == 0) return set_err(c, HFX_ERR_STATE, "rk_compute_stage: no Runge-Kutta scheme set");
+  if (c->rkStage >= c->rkStages)
+    return set_err(c, HFX_ERR_STATE,
+                   "rk_compute_stage: cannot compute more stages than the method allows, think about computing the "
+                   "solution");
+  const int S = c->rkStages, st = c->rkStage;
+  const double dt = c->rkDt;
+  const int64_t E = c->nCells, LU = c->re.nNodes, LQ = (int64_t)c->dim * c->re.nNodes;
+  double* xs[3] = {c->d_sol, c->d_flux, c->d_trace};
+  const double* olds[3] = {c->d_oldSol, c->d_oldFlux, c->d_oldTrace};
+  std::vector<double*>* ks[3] = {&c->d_kSol, &c->d_kFlux, &c->d_kTrace};
+  const int64_t len[3] = {E * LU, E * LQ, c->ndofs()};
+  for (int f = 0; f < 3; ++f) {
+    RkTerms d{};
+    d.n = 1;
+    d.coef[0] = -1.0 / dt;
+    d.ptr[0] = olds[f];
+    HFX_CUDA(c, launch_rk_lincomb(len[f], (*ks[f])[st], 1.0 / dt, xs[f], d, c->stream));
+    RkTerms u{};
+    for (int j = 0; j <= st; ++j) {
+      u.coef[u.n] = dt * c->rkTable[(size_t)st * (S + 1) + 1 + j];
+      u.ptr[u.n++] = (*ks[f])[j];
+    }
+    HFX_CUDA(c, launch_rk_lincomb(len[f], xs[f], 1.0, olds[f], u, c->stream));
+  }
+  HFX_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->rkStage += 1;
+  c->assembled = false;
+  c->qValid = false;
+  return HFX_OK;
+}
+
+// RungeKutta::computeSolution (RungeKutta.cpp:172-213): x = x_old + dt sum_k b_k k_k.
+int hfx_rk_compute_solution(hfx_ctx* c) {
+  if (!c) return HFX_ERR_ARG;
+  if (c->rkStages == 0) return set_err(c, HFX_ERR_STATE, "rk_compute_solution: no Runge-Kutta scheme set");
+  if (c->rkStage != c->rkStages)
+    return set_err(c, HFX_ERR_STATE, "rk_compute_solution: all stages must be computed before computing the solution");
+  const int S = c->rkStages;
+  const double dt = c->rkDt;
+  const int64_t E = c->nCells, LU = c->re.nNodes, LQ = (int64_t)c->dim * c->re.nNodes;
+  double* xs[3] = {c->d_sol, c->d_flux, c->d_trace};
+  const double* olds[3] = {c->d_oldSol, c->d_oldFlux, c->d_oldTrace};
+  std::vector<double*>* ks[3] = {&c->d_kSol, &c->d_kFlux, &c->d_kTrace};
+  const int64_t len[3] = {E * LU, E * LQ, c->ndofs()};
+  for (int f = 0; f < 3; ++f) {
+    RkTerms u{};
+    for (int k = 0; k < S; ++k) {
+      u.coef[u.n] = dt * c->rkTable[(size_t)S * (S + 1) + 1 + k];
+      u.ptr[u.n++] = (*ks[f])[k];
+    }
+    HFX_CUDA(c, launch_rk_lincomb(len[f], xs[f], 1.0, olds[f], u, c->stream));
+  }
+  HFX_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->rkStage = 0;
+  c->assembled = false;
+  c->qValid = false;
   return HFX_OK;
 }
 

@@ -135,6 +135,8 @@ bool affine_tables(const RefEl& re, std::vector<double>* out) {
   out->clear();
   for (auto* v : {&M, &R, &Tf, &P, &T, &Dr, &L}) out->insert(out->end(), v->begin(), v->end());
   out->insert(out->end(), re.ipX.begin(), re.ipX.end());  // volume IPs, for the source
+  out->insert(out->end(), C.begin(), C.end());            // C_r, for Runge-Kutta stages
+  out->insert(out->end(), Mf.begin(), Mf.end());          // face mass
   return true;
 }
 
@@ -174,7 +176,9 @@ struct AffLayout {
   static constexpr int A_D = A_T + F * F * NF * NF;
   static constexpr int A_L = A_D + D * N * N;
   static constexpr int A_X = A_L + F * N * NF;  // [NI][D] reference IP coordinates
-  static constexpr int A_END = A_X + NI * D;
+  static constexpr int A_C = A_X + NI * D;      // [D][N][N] C_r[i][j] = sum_q w d_r phi_i phi_j
+  static constexpr int A_MF = A_C + D * N * N;  // [NF][NF] reference face mass
+  static constexpr int A_END = A_MF + NF * NF;
   // per-element precomputed factors (affine_prep): G, |J|, |F_f|, n_f, Gamma,
   // g_f, c_ff', f(x_q) w_q |J|, K
   static constexpr int P_IV = 0, P_DET = P_IV + D * D, P_AR = P_DET + 1, P_NRM = P_AR + F, P_GAM = P_NRM + F * D;
@@ -195,7 +199,14 @@ struct AffLayout {
   static constexpr int BW = AM + N * N;          // N*LW row-major
   static constexpr int IDG = BW + N * LW;        // N     1 / L[k][k]
   static constexpr int WDS = (IDG + N + 1) & ~1; // N*LL  W as float pairs (hi, lo)
-  static constexpr int WARP = WDS + N * LL;
+  // Runge-Kutta stage vector w (u, q, lambda parts), y_r = (K G)^T w_q, K n_f, K G
+  static constexpr int RKU = WDS + N * LL;       // N
+  static constexpr int RKQ = RKU + N;            // N*D
+  static constexpr int RKL = RKQ + N * D;        // F*NF
+  static constexpr int RKY = RKL + F * NF;       // D*N
+  static constexpr int RKN = RKY + D * N;        // F*D
+  static constexpr int RKG = RKN + F * D;        // D*D
+  static constexpr int WARP = RKG + D * D;
 };
 
 // Per-element geometry and source, one thread per element (full warps): the
@@ -380,6 +391,13 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
   double* BW = W + L::BW;
   double* idg = W + L::IDG;
   float2* wds = reinterpret_cast<float2*>(W + L::WDS);
+  double* rku = W + L::RKU;
+  double* rkq = W + L::RKQ;
+  double* rkl = W + L::RKL;
+  double* rky = W + L::RKY;
+  double* rkn = W + L::RKN;
+  double* rkg = W + L::RKG;
+  const bool rk = p.rkWu != nullptr;
   const double* phi = p.tab + L::T_PHI;
   const double* tM = atab + L::A_M;
   const double* tR = atab + L::A_R;
@@ -387,6 +405,7 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
   const double* tP = atab + L::A_P;
   const double* tT = atab + L::A_T;
   const double dts = p.dt > 0.0 ? p.dt : 1.0;
+  const double cs = rk ? p.cStiff : dts;  // scale of the U rows' stiffness
   const int64_t nWarps = (int64_t)gridDim.x * EPC;
   for (int64_t e = (int64_t)blockIdx.x * EPC + warp; e < p.nCells; e += nWarps) {
     // ------------------------------------- gather: prep record and face tau
@@ -397,8 +416,36 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
       int q = p.perm[e * F * NF + i];
       tau[i] = p.tau[((int64_t)f * NF + q) * p.tauVals + (p.tauVals == 2 ? side : 0)];
     }
+    if (rk) {
+      for (int i = t; i < N; i += 32) rku[i] = p.rkWu[e * N + i];
+      for (int i = t; i < N * D; i += 32) rkq[i] = p.rkWq[e * N * D + i];
+      for (int i = t; i < F * NF; i += 32)
+        rkl[i] = p.rkWl[(int64_t)p.cell2face[e * F + i / NF] * NF + p.perm[e * F * NF + i]];
+    }
     __syncwarp();
     const double detJ = pr[L::P_DET];
+    if (rk) {
+      // (K G)[k][r] and K n_f, then y_r[j] = sum_k (K G)[k][r] w_q[j][k]
+      const double* iv = pr + L::P_IV;
+      if (t < D * D) {
+        const int k = t / D, r = t % D;
+        double acc = 0.0;
+        for (int b = 0; b < D; ++b) acc += Ks[k + b * D] * iv[b * D + r];
+        rkg[t] = acc;
+      } else if (t >= 16 && t < 16 + F * D) {
+        const int f = (t - 16) / D, k = (t - 16) % D;
+        double acc = 0.0;
+        for (int b = 0; b < D; ++b) acc += Ks[k + b * D] * nrm[f * D + b];
+        rkn[t - 16] = acc;
+      }
+      __syncwarp();
+      for (int rj = t; rj < D * N; rj += 32) {
+        const int r = rj / N, j = rj % N;
+        double acc = 0.0;
+        for (int k = 0; k < D; ++k) acc += rkg[k * D + r] * rkq[j * D + k];
+        rky[rj] = acc;
+      }
+    }
     // ----------------------------------------------- tau face mass Tm_f
     // symmetric in (a, b): the upper triangle, mirrored
     constexpr int NT = NF * (NF + 1) / 2;
@@ -435,7 +482,7 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
       double st = 0.0;
 #pragma unroll
       for (int rs = 0; rs < D * D; ++rs) st += gam[rs] * __ldg(tR + rs * N * N + ij);
-      double v = dts * (ts + detJ * st);
+      double v = cs * (ts + detJ * st);
       if (p.dt > 0.0) v += detJ * __ldg(tM + ij);
       Am[ij] = v;
       Am[j * N + i] = v;
@@ -459,6 +506,26 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
         double mu = 0.0;
         for (int j = 0; j < N; ++j) mu += __ldg(tM + i * N + j) * p.uOld[e * N + j];
         v += detJ * mu;
+      }
+      if (rk) {
+        // - (K w)_i: tau face masses on (w_u - w_lambda), the flux coupling on w_q
+        double kw = 0.0;
+        const double* tC = atab + L::A_C;
+        const double* tMf = atab + L::A_MF;
+        for (int f = 0; f < F; ++f) {
+          const int a = sPos[f * N + i];
+          if (a < 0) continue;
+          for (int b = 0; b < NF; ++b) {
+            const int nb = sFN[f * NF + b];
+            double qn = 0.0;
+            for (int k = 0; k < D; ++k) qn += rkn[f * D + k] * rkq[nb * D + k];
+            kw += Tm[(f * NF + a) * NF + b] * (rku[nb] - rkl[f * NF + b]) - area[f] * __ldg(tMf + a * NF + b) * qn;
+          }
+        }
+        double vol = 0.0;
+        for (int r = 0; r < D; ++r)
+          for (int j = 0; j < N; ++j) vol += __ldg(tC + (r * N + i) * N + j) * rky[r * N + j];
+        v -= kw + detJ * vol;
       }
       BW[i * LW + LL] = v;
     }
@@ -562,7 +629,7 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
         float sh = 0.f, sl = 0.f;
 #pragma unroll 4
         for (int m = 0; m < N; ++m) ds_mac(sh, sl, wds[m * LL + r], wds[m * LL + c]);
-        double v = ((double)sh + (double)sl) * dts;
+        double v = ((double)sh + (double)sl) * cs;
         v -= cff[fr * F + fc] * __ldg(tT + ((fr * F + fc) * NF + (r % NF)) * NF + (c % NF));
         if (fr == fc) v -= Tm[(fr * NF + r % NF) * NF + (c % NF)];
         const bool br = (bmask >> fr) & 1u;
@@ -596,7 +663,7 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
       __syncwarp();
     }
     double* Ug = (double*)p.U + e * N * LL;
-    for (int idx = t; idx < N * LL; idx += 32) Ug[idx] = -dts * BW[(idx % N) * LW + idx / N];
+    for (int idx = t; idx < N * LL; idx += 32) Ug[idx] = -cs * BW[(idx % N) * LW + idx / N];
     for (int i = t; i < N; i += 32) ((double*)p.U0)[e * N + i] = BW[i * LW + LL];
     __syncwarp();
   }

@@ -416,6 +416,7 @@ __global__ void __launch_bounds__(TPE * EPC)
     // ---- A = dt*(Suu - Suq Xu) + M_mass ; Rhs = [dt*(Sul - Suq Xl) | fu']
     // (without a time scheme dt_eff = 1 and no mass term)
     const T dts = p.dt > 0.0 ? p.dt : 1.0;
+    const T cs = p.rkWu ? (T)p.cStiff : dts;  // scale of the U rows' stiffness (Runge-Kutta stage)
     if (active) {
       for (int ij = t; ij < N * N; ij += TPE) {
         int i = ij / N, j = ij % N;
@@ -432,7 +433,7 @@ __global__ void __launch_bounds__(TPE * EPC)
           // mass of the time scheme: M = sum_q dV phi phi (Mass.cpp:5-38)
           T mm = 0.0;
           for (int q = 0; q < NI; ++q) mm += dV[q] * phi[q * N + i] * phi[q * N + j];
-          v = dts * v + mm;
+          v = cs * v + mm;
         }
         Am[ij] = v;
       }
@@ -446,7 +447,7 @@ __global__ void __launch_bounds__(TPE * EPC)
           T acc = 0.0;
           for (int d = 0; d < D; ++d)
             for (int m = 0; m < N; ++m) acc += Km[(d * N + i) * N + m] * Xl[(d * N + m) * LL + c];
-          v = dts * (sul - acc);
+          v = cs * (sul - acc);
         } else if (rhsMode) {
           // r_u - dt Suq M^{-1} r_q (the residual already carries the time scheme)
           T acc = 0.0;
@@ -463,6 +464,22 @@ __global__ void __launch_bounds__(TPE * EPC)
               mu += mm * p.uOld[e * N + j];
             }
             v += mu;
+          }
+          if (p.rkWu) {
+            // - (K w)_i over the unscaled U rows: [Suu | Suq | Sul] w
+            T kw = 0.0;
+            for (int f = 0; f < F; ++f) {
+              const int a = sPos[f * N + i];
+              if (a < 0) continue;
+              const int64_t fc = p.cell2face[e * F + f];
+              for (int b = 0; b < NF; ++b) {
+                const T wl = (T)p.rkWl[fc * NF + p.perm[(e * F + f) * NF + b]];
+                kw += Tm[(f * NF + a) * NF + b] * ((T)p.rkWu[e * N + sFaceNodes[f * NF + b]] - wl);
+              }
+            }
+            for (int d = 0; d < D; ++d)
+              for (int m = 0; m < N; ++m) kw += Km[(d * N + i) * N + m] * (T)p.rkWq[(e * N + m) * D + d];
+            v -= kw;
           }
         }
         Rhs[ic] = v;

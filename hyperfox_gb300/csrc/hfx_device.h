@@ -63,9 +63,27 @@ struct LocalParams {
   int explicitMode;
   const double* solState;      // [nCells][N]
   const double* fluxState;     // [nCells][N*D] node-major
+  // RungeKutta stage (RungeKutta.cpp:90-129) on the U rows of the local system:
+  // K' = cStiff K + [M 0 0], f' = dt f + M uOld - K w with the stage vector
+  // w = (dt - cStiff) ut + dt^2 sum_{i<s} a_si k_i, cStiff = dt a_ss; w given as its
+  // cell parts and its face part (trace numbering). rkWu == nullptr: no stage.
+  double cStiff;
+  const double* rkWu;          // [nCells][N]
+  const double* rkWq;          // [nCells][N*D] node-major
+  const double* rkWl;          // [nFaces][NF]
 };
 
 cudaError_t launch_local_condense(int dim, int order, const LocalParams& p, cudaStream_t s);
+
+// out[i] = alpha a[i] + sum_j coef[j] ptr[j][i] (rk.cu), element by element (out may alias an input)
+struct RkTerms {
+  static constexpr int MAX = 8;
+  int n;
+  double coef[MAX];
+  const double* ptr[MAX];
+};
+cudaError_t launch_rk_lincomb(int64_t n, double* out, double alpha, const double* a, const RkTerms& terms,
+                              cudaStream_t s);
 bool local_condense_supported(int dim, int order);
 
 // Affine elements with a symmetric, cell-constant diffusion tensor (hdg_affine.cu):

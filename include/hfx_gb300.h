@@ -228,6 +228,43 @@ int hfx_assemble_ex(hfx_ctx* ctx, int precision);
  * hfx_assembly_info reports whether the last FP64 assembly took the affine path. */
 int hfx_set_assembly_path(hfx_ctx* ctx, int path);
 int hfx_assembly_info(hfx_ctx* ctx, int* affine);
+
+/* ---- Runge-Kutta time integration (RungeKutta.cpp:5-213, HDGModel.cpp:39-47) --
+ * A scheme applies to the U rows of every element system at hfx_assemble:
+ * K' = dt a_ss K + M, f' = dt f - dt K uj + K' ut (ut the Old fields, uj = ut +
+ * dt sum_{i<s} a_si k_i over Solution, Flux and Trace, the reference's
+ * auxiliary fields {"Flux", "Trace"}). The fields live on the device:
+ * Solution/Flux are the last recovery (or hfx_set_state), Trace the last solve
+ * (or hfx_set_trace). Per time step: hfx_rk_begin_step (Old* = current), then per
+ * stage hfx_assemble, hfx_solve, hfx_recover, hfx_rk_compute_stage, and finally
+ * hfx_rk_compute_solution. hfx_rk_set takes a user table ((S+1)^2 row-major, rows
+ * [c_i | a_i.], last row [0 | b]) whose strictly upper part must be zero
+ * (RungeKutta::setButcherTable(EMatrix)); hfx_rk_set_type takes a named table
+ * as is; nStages 0 switches the scheme off. FP64 assembly only (the
+ * mixed-precision assembly refuses a scheme). While a scheme is set it replaces
+ * hfx_set_time_scheme's implicit Euler. */
+#define HFX_RK_FEULER 0
+#define HFX_RK_EMIDPOINT 1
+#define HFX_RK_HEUN 2
+#define HFX_RK_KUTTA3 3
+#define HFX_RK_HEUN3 4
+#define HFX_RK_SSPRK3 5
+#define HFX_RK_RK4 6
+#define HFX_RK_BEULER 7
+#define HFX_RK_IMIDPOINT 8
+#define HFX_RK_CRANKNICOLSON 9
+#define HFX_RK_KS2 10
+#define HFX_RK_QZ2 11
+#define HFX_RK_ALX2 12
+#define HFX_RK_RK43 13
+int hfx_rk_butcher(int type, int* nStages, double* table);
+int hfx_rk_set(hfx_ctx* ctx, int nStages, const double* table, double dt);
+int hfx_rk_set_type(hfx_ctx* ctx, int type, double dt);
+int hfx_rk_begin_step(hfx_ctx* ctx);
+int hfx_rk_compute_stage(hfx_ctx* ctx);
+int hfx_rk_compute_solution(hfx_ctx* ctx);
+int hfx_set_trace(hfx_ctx* ctx, const double* trace);
+int hfx_get_state(hfx_ctx* ctx, double* solution, double* flux, double* trace);
 /* Condensed element blocks, column-major per element (any pointer may be NULL). */
 int hfx_get_condensed(hfx_ctx* ctx, double* S, double* S0, double* U, double* Q, double* U0,
                       double* Q0);

@@ -672,6 +672,11 @@ struct Problem {
   std::vector<double> dirichlet;  // face field nFaces*Nf
   double dt = 0.0;            // > 0: implicit Euler (Euler.cpp:18-34)
   std::vector<double> uOld;   // nCells*N
+  // Runge-Kutta stage (RungeKutta::apply, RungeKutta.cpp:90-129): rkDt > 0 turns it
+  // on; rkDiag = a_ss; rkOld* = OldSolution/OldFlux/OldTrace; rkComb* = sum_{i<s}
+  // a_si RKStage_*_i (cell fields nCells*N, nCells*N*d node-major; face field nFaces*Nf)
+  double rkDt = 0.0, rkDiag = 0.0;
+  std::vector<double> rkOldU, rkOldQ, rkOldL, rkCombU, rkCombQ, rkCombL;
   // HDGSolverType (HDGSolverOpts.h:6-10): 0 IMPLICIT, 1 WEXPLICIT, 2 SEXPLICIT; the
   // explicit modes build S, S0 from the current Solution and Flux (HDGSolver.cpp:349-354)
   int solverType = 0;
@@ -895,8 +900,42 @@ static void local_system(const Problem& P, int iEl, Mat& A, std::vector<double>&
       for (int i = 0; i < N; ++i) rhs[i] += re->phi[q][i] * lm;
     }
   }
-  // implicit Euler on the U rows (HDGModel.cpp:39-47, Euler.cpp:18-34, Mass.cpp:5-38)
-  if (P.dt > 0.0) {
+  if (P.rkDt > 0.0) {
+    // RungeKutta::apply on the U rows of the local system (HDGModel.cpp:39-47):
+    // s = dt s - dt K uj; K = dt a_ss K; K[:, U] += M; s += K ut
+    const double dt = P.rkDt;
+    Mat M(N, N);
+    for (int q = 0; q < nI; ++q)
+      for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j) M(i, j) += re->phi[q][i] * re->phi[q][j] * dV[q];
+    std::vector<double> ut(n, 0.0), uj(n, 0.0);
+    for (int i = 0; i < N; ++i) {
+      ut[i] = P.rkOldU[(size_t)iEl * N + i];
+      uj[i] = P.rkCombU[(size_t)iEl * N + i];
+      for (int k = 0; k < d; ++k) {
+        ut[lenU + i * d + k] = P.rkOldQ[((size_t)iEl * N + i) * d + k];
+        uj[lenU + i * d + k] = P.rkCombQ[((size_t)iEl * N + i) * d + k];
+      }
+    }
+    for (int fi = 0; fi < F; ++fi)
+      for (int j = 0; j < Nf; ++j) {
+        const size_t g = (size_t)facesIn[fi] * Nf + f2c[fi * Nf + j];
+        ut[startL + fi * Nf + j] = P.rkOldL[g];
+        uj[startL + fi * Nf + j] = P.rkCombL[g];
+      }
+    for (int j = 0; j < n; ++j) uj[j] = dt * uj[j] + ut[j];
+    for (int i = 0; i < lenU; ++i) {
+      double kuj = 0.0;
+      for (int j = 0; j < n; ++j) kuj += A(i, j) * uj[j];
+      rhs[i] = dt * rhs[i] - dt * kuj;
+      for (int j = 0; j < n; ++j) A(i, j) *= dt * P.rkDiag;
+      for (int j = 0; j < N; ++j) A(i, j) += M(i, j);
+      double kut = 0.0;
+      for (int j = 0; j < n; ++j) kut += A(i, j) * ut[j];
+      rhs[i] += kut;
+    }
+  } else if (P.dt > 0.0) {
+    // implicit Euler on the U rows (HDGModel.cpp:39-47, Euler.cpp:18-34, Mass.cpp:5-38)
     Mat M(N, N);
     for (int q = 0; q < nI; ++q)
       for (int i = 0; i < N; ++i)
@@ -1331,6 +1370,26 @@ int orc_problem_set_fields(void* h, const double* tau, int tauVals, const double
     if (dirichlet) P->dirichlet.assign(dirichlet, dirichlet + (size_t)P->mf.nFaces * Nf);
     P->dt = dt;
     if (dt > 0.0) P->uOld.assign(uOld, uOld + (size_t)P->nCells * N);
+  })
+}
+
+// Runge-Kutta stage on the U rows (RungeKutta.cpp:90-129); dt <= 0 switches it off.
+int orc_problem_set_rk(void* h, double dt, double aDiag, const double* oldU, const double* oldQ,
+                       const double* oldL, const double* combU, const double* combQ, const double* combL) {
+  ORC_TRY({
+    Problem* P = (Problem*)h;
+    P->rkDt = dt;
+    P->rkDiag = aDiag;
+    if (dt > 0.0) {
+      const size_t nu = (size_t)P->nCells * P->re->nNodes, nq = nu * P->dim,
+                   nl = (size_t)P->mf.nFaces * P->re->face->nNodes;
+      P->rkOldU.assign(oldU, oldU + nu);
+      P->rkOldQ.assign(oldQ, oldQ + nq);
+      P->rkOldL.assign(oldL, oldL + nl);
+      P->rkCombU.assign(combU, combU + nu);
+      P->rkCombQ.assign(combQ, combQ + nq);
+      P->rkCombL.assign(combL, combL + nl);
+    }
   })
 }
 

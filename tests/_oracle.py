@@ -54,6 +54,7 @@ def lib():
         L.orc_problem_timings.argtypes = [vp, vp]
         L.orc_problem_set_solver.argtypes = [vp, ip, vp, vp]
         L.orc_problem_solve_faces.argtypes = [vp, vp]
+        L.orc_problem_set_rk.argtypes = [vp, dp, dp] + [vp] * 6
         _lib = L
     return _lib
 
@@ -215,6 +216,17 @@ class Problem:
         self._keep_state = (sol, flux)
         _check(lib().orc_problem_set_solver(self.h, type_, _ptr(sol), _ptr(flux)))
 
+    def set_rk(self, dt, a_diag=0.0, old=None, comb=None):
+        """Runge-Kutta stage on the U rows (RungeKutta::apply): old = (OldSolution,
+        OldFlux, OldTrace), comb = sum_{i<s} a_si (RKStage_i, RKStage_Flux_i,
+        RKStage_Trace_i); dt <= 0 switches it off."""
+        if dt <= 0:
+            _check(lib().orc_problem_set_rk(self.h, 0.0, 0.0, None, None, None, None, None, None))
+            return
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (*old, *comb)]
+        self._keep_rk = arrs
+        _check(lib().orc_problem_set_rk(self.h, dt, a_diag, *[_ptr(a) for a in arrs]))
+
     def solve_faces(self):
         x = np.zeros(self.ndofs)
         _check(lib().orc_problem_solve_faces(self.h, _ptr(x)))
@@ -224,3 +236,66 @@ class Problem:
         t = np.zeros(5)
         lib().orc_problem_timings(self.h, _ptr(t))
         return dict(local=t[0], dirichlet=t[1], scatter=t[2], solve=t[3], recover=t[4])
+
+
+# Butcher tables of RungeKutta::setUpDB (RungeKutta.cpp:215-286): rows [c_i | a_i.], last row [0 | b]
+_G = 1.0 - np.sqrt(2.0) / 2.0
+BUTCHER = {
+    "FEuler": [[0, 0], [0, 1]],
+    "EMidpoint": [[0, 0, 0], [0.5, 0.5, 0], [0, 0, 1]],
+    "Heun": [[0, 0, 0], [1, 1, 0], [0, 0.5, 0.5]],
+    "Kutta3": [[0, 0, 0, 0], [0.5, 0.5, 0, 0], [1, -1, 2, 0], [0, 1 / 6, 2 / 3, 1 / 6]],
+    "Heun3": [[0, 0, 0, 0], [1 / 3, 1 / 3, 0, 0], [2 / 3, 0, 2 / 3, 0], [0, 1 / 4, 0, 3 / 4]],
+    "SSPRK3": [[0, 0, 0, 0], [1, 1, 0, 0], [0.5, 0.25, 0.25, 0], [0, 1 / 6, 1 / 6, 2 / 3]],
+    "RK4": [[0, 0, 0, 0, 0], [0.5, 0.5, 0, 0, 0], [0.5, 0, 0.5, 0, 0], [1, 0, 0, 1, 0],
+            [0, 1 / 6, 1 / 3, 1 / 3, 1 / 6]],
+    "BEuler": [[1, 1], [0, 1]],
+    "IMidpoint": [[0.5, 0.5], [0, 1]],
+    "CrankNicolson": [[0, 0, 0], [1, 0.5, 0.5], [0, 0.5, 0.5]],
+    "KS2": [[0.5, 0.5, 0], [1.5, -0.5, 2], [0, -0.5, 1.5]],
+    "QZ2": [[0.25, 0.25, 0], [0.75, 0.5, 0.25], [0, 0.5, 0.5]],
+    "ALX2": [[_G, _G, 0], [1, 1 - _G, _G], [0, 1 - _G, _G]],
+    "RK43": [[0.5, 0.5, 0, 0, 0], [2 / 3, 1 / 6, 0.5, 0, 0], [0.5, -0.5, 0.5, 0.5, 0], [1, 1.5, -1.5, 0.5, 0.5],
+             [0, 1.5, -1.5, 0.5, 0.5]],
+}
+
+
+class RungeKutta:
+    """RungeKutta.cpp restated on host arrays: fields is a dict of the current
+    Solution / Flux / Trace arrays (updated in place), stage() and solution()
+    follow computeStage (:131-170) and computeSolution (:172-213); apply() sets the
+    oracle problem's U-row modification for the current stage (:90-129)."""
+
+    NAMES = ("Solution", "Flux", "Trace")
+
+    def __init__(self, table, dt):
+        self.b = np.array(table, dtype=np.float64)
+        self.S = self.b.shape[0] - 1
+        self.dt = dt
+        self.stage_counter = 0
+        self.old = None
+        self.k = {n: [] for n in self.NAMES}
+
+    def begin_step(self, fields):
+        self.old = {n: fields[n].copy() for n in self.NAMES}
+        self.k = {n: [None] * self.S for n in self.NAMES}
+
+    def apply(self, problem):
+        s = self.stage_counter
+        a = self.b[s, 1:]
+        comb = [sum((a[i] * self.k[n][i] for i in range(s)), np.zeros_like(self.old[n])) for n in self.NAMES]
+        problem.set_rk(self.dt, a[s], [self.old[n] for n in self.NAMES], comb)
+
+    def stage(self, fields):
+        s = self.stage_counter
+        a = self.b[s, 1:]
+        for n in self.NAMES:
+            self.k[n][s] = (fields[n] - self.old[n]) / self.dt
+            fields[n][...] = self.old[n] + self.dt * sum(a[j] * self.k[n][j] for j in range(s + 1))
+        self.stage_counter += 1
+
+    def solution(self, fields):
+        bs = self.b[self.S, 1:]
+        for n in self.NAMES:
+            fields[n][...] = self.old[n] + sum(bs[k] * self.dt * self.k[n][k] for k in range(self.S))
+        self.stage_counter = 0
