@@ -341,6 +341,7 @@ def run_ours(args, world, rank, local):
         "krylov_iterations": iters,
         "refinements": refinements,
         "rel_err_vs_fp64": rel_err,
+        "meets_1e-8_rel_err": bool(rel_err <= 1e-8),
         "fp64_reference_iterations": ref_info.iterations,
         "plain_fp64": plain,
         "learned_coarse": learned,
@@ -395,8 +396,10 @@ def main():
                     help="mixed: FP64 assembly, FP32 CG with FP64 reliable updates of the trace residual; "
                          "fp64: FP64 throughout; mixed-full: FP32 element condensation inside FP64 "
                          "refinement of the full HDG system")
-    ap.add_argument("--rtol", type=float, default=1e-10,
-                    help="relative FP64 residual of the trace system (mixed-full: of the full HDG system)")
+    ap.add_argument("--rtol", type=float, default=1e-8,
+                    help="relative FP64 residual of the trace system (mixed-full: of the full HDG system); "
+                         "both arms stop there, and the error against the FP64 solution (rtol 1e-13) is "
+                         "reported as rel_err_vs_fp64")
     ap.add_argument("--inner-rtol", type=float, default=1e-2,
                     help="FP32 reduction between FP64 residual replacements (mixed)")
     ap.add_argument("--precond", default="twolevel", choices=["twolevel", "bj"],
