@@ -194,19 +194,21 @@ struct AffLayout {
   static constexpr int LW = LL + 1;              // columns of [B | f_u]
   static constexpr int PR = 0;                   // PREP  the element's affine_prep record
   static constexpr int TAU = PR + PREP;          // F*NF
-  static constexpr int TM = TAU + F * NF;        // F*NF*NF
-  static constexpr int AM = TM + F * NF * NF;    // N*N row-major, then its Cholesky factor
-  static constexpr int BW = AM + N * N;          // N*LW row-major
+  static constexpr int NT = NF * (NF + 1) / 2;
+  static constexpr int TM = TAU + F * NF;        // F*NT  tau face masses, symmetric, packed
+  static constexpr int AM = TM + F * NT;         // N(N+1)/2  lower triangle of A, packed by rows, then L
+  static constexpr int BW = AM + N * (N + 1) / 2; // N*LW row-major
   static constexpr int IDG = BW + N * LW;        // N     1 / L[k][k]
   static constexpr int WDS = (IDG + N + 1) & ~1; // N*LL  W as float pairs (hi, lo)
-  // Runge-Kutta stage vector w (u, q, lambda parts), y_r = (K G)^T w_q, K n_f, K G
-  static constexpr int RKU = WDS + N * LL;       // N
+  // Runge-Kutta stage vector w (u, q, lambda parts), y_r = (K G)^T w_q, K n_f, K G:
+  // dead before W exists, so they share its region
+  static constexpr int RKU = WDS;                // N
   static constexpr int RKQ = RKU + N;            // N*D
   static constexpr int RKL = RKQ + N * D;        // F*NF
   static constexpr int RKY = RKL + F * NF;       // D*N
   static constexpr int RKN = RKY + D * N;        // F*D
   static constexpr int RKG = RKN + F * D;        // D*D
-  static constexpr int WARP = RKG + D * D;
+  static constexpr int WARP = (WDS + N * LL > RKG + D * D) ? WDS + N * LL : RKG + D * D;
 };
 
 // Per-element geometry and source, one thread per element (full warps): the
@@ -357,6 +359,15 @@ __global__ void affine_prep(LocalParams p, const double* __restrict__ atab, doub
   }
 }
 
+// packed symmetric face block (a, b) of face f, rows a <= b of length NF - a
+template <int NF>
+__device__ __forceinline__ int tm_index(int f, int a, int b) {
+  const int lo = a < b ? a : b, hi = a < b ? b : a;
+  return f * (NF * (NF + 1) / 2) + lo * NF - lo * (lo - 1) / 2 + (hi - lo);
+}
+// packed lower triangle by rows, (i, j) with j <= i
+__device__ __forceinline__ int pl_index(int i, int j) { return i * (i + 1) / 2 + j; }
+
 template <int D, int P, int EPC>
 __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const double* __restrict__ atab,
                                                          const double* __restrict__ prep) {
@@ -462,8 +473,7 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
 #pragma unroll
       for (int c = 0; c < NF; ++c) acc += tau[f * NF + c] * __ldg(tf + c);
       acc *= area[f];
-      Tm[(f * NF + a) * NF + b] = acc;
-      Tm[(f * NF + b) * NF + a] = acc;
+      Tm[f * L::NT + idx % NT] = acc;
     }
     __syncwarp();
     // ------------------------------------------------- A, B and f_u
@@ -477,15 +487,14 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
       double ts = 0.0;
       for (int f = 0; f < F; ++f) {
         const int a = sPos[f * N + i], b = sPos[f * N + j];
-        if (a >= 0 && b >= 0) ts += Tm[(f * NF + a) * NF + b];
+        if (a >= 0 && b >= 0) ts += Tm[tm_index<NF>(f, a, b)];
       }
       double st = 0.0;
 #pragma unroll
       for (int rs = 0; rs < D * D; ++rs) st += gam[rs] * __ldg(tR + rs * N * N + ij);
       double v = cs * (ts + detJ * st);
       if (p.dt > 0.0) v += detJ * __ldg(tM + ij);
-      Am[ij] = v;
-      Am[j * N + i] = v;
+      Am[pl_index(i, j)] = v;
     }
     for (int ic = t; ic < N * LL; ic += 32) {
       const int i = ic / LL, c = ic % LL;
@@ -495,7 +504,7 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
       for (int r = 0; r < D; ++r) acc += gv[f * D + r] * __ldg(tP + ((r * F + f) * N + i) * NF + b);
       double v = -area[f] * acc;
       const int a = sPos[f * N + i];
-      if (a >= 0) v -= Tm[(f * NF + a) * NF + b];
+      if (a >= 0) v -= Tm[tm_index<NF>(f, a, b)];
       BW[i * LW + c] = v;
     }
     for (int i = t; i < N; i += 32) {
@@ -519,7 +528,7 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
             const int nb = sFN[f * NF + b];
             double qn = 0.0;
             for (int k = 0; k < D; ++k) qn += rkn[f * D + k] * rkq[nb * D + k];
-            kw += Tm[(f * NF + a) * NF + b] * (rku[nb] - rkl[f * NF + b]) - area[f] * __ldg(tMf + a * NF + b) * qn;
+            kw += Tm[tm_index<NF>(f, a, b)] * (rku[nb] - rkl[f * NF + b]) - area[f] * __ldg(tMf + a * NF + b) * qn;
           }
         }
         double vol = 0.0;
@@ -533,16 +542,16 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
     // ------------------------------------- Cholesky A = L L^T (lower, in place)
     bool bad = false;
     for (int k = 0; k < N; ++k) {
-      const double akk = Am[k * N + k];
+      const double akk = Am[pl_index(k, k)];
       if (!(akk > 0.0)) bad = true;
       const double il = rsqrt(akk > 0.0 ? akk : 1.0);  // 1 / L[k][k]
       const double lkk = (akk > 0.0 ? akk : 1.0) * il;
       __syncwarp();
       if (t == 0) {
-        Am[k * N + k] = lkk;
+        Am[pl_index(k, k)] = lkk;
         idg[k] = il;
       }
-      for (int i = k + 1 + t; i < N; i += 32) Am[i * N + k] *= il;
+      for (int i = k + 1 + t; i < N; i += 32) Am[pl_index(i, k)] *= il;
       __syncwarp();
       const int m = N - k - 1;
       for (int idx = t; idx < m * (m + 1) / 2; idx += 32) {
@@ -551,7 +560,7 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
         while (ii * (ii + 1) / 2 > idx) --ii;
         while ((ii + 1) * (ii + 2) / 2 <= idx) ++ii;
         const int i = k + 1 + ii, j = k + 1 + (idx - ii * (ii + 1) / 2);
-        Am[i * N + j] -= Am[i * N + k] * Am[j * N + k];
+        Am[pl_index(i, j)] -= Am[pl_index(i, k)] * Am[pl_index(j, k)];
       }
       __syncwarp();
     }
@@ -565,7 +574,7 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
       const int rows = N - k - 1;
       for (int ic = t; ic < rows * LW; ic += 32) {
         const int i = k + 1 + ic / LW, c = ic % LW;
-        BW[i * LW + c] -= Am[i * N + k] * BW[k * LW + c];
+        BW[i * LW + c] -= Am[pl_index(i, k)] * BW[k * LW + c];
       }
       __syncwarp();
     }
@@ -589,7 +598,7 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
           const int r = idx % LL, c = idx / LL, fr = r / NF;
           double v;
           if ((bmask >> fr) & 1u) v = r == c ? 1.0 : 0.0;
-          else v = (c / NF == fr) ? -Tm[(fr * NF + r % NF) * NF + (c % NF)] : 0.0;
+          else v = (c / NF == fr) ? -Tm[tm_index<NF>(fr, r % NF, c % NF)] : 0.0;
           Sg[idx] = v;
         }
         const double* sol = p.solState + e * N;
@@ -613,7 +622,7 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
               for (int cc = 0; cc < NF; ++cc) mf += __ldg(tTf + (a * NF + b) * NF + cc);
               double qn = 0.0;
               for (int dd = 0; dd < D; ++dd) qn += kn[dd] * flx[nb * D + dd];
-              v += -Tm[(f * NF + a) * NF + b] * sol[nb] + area[f] * mf * qn;
+              v += -Tm[tm_index<NF>(f, a, b)] * sol[nb] + area[f] * mf * qn;
             }
           }
           ((double*)p.S0)[e * LL + c] = v;
@@ -631,7 +640,7 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
         for (int m = 0; m < N; ++m) ds_mac(sh, sl, wds[m * LL + r], wds[m * LL + c]);
         double v = ((double)sh + (double)sl) * cs;
         v -= cff[fr * F + fc] * __ldg(tT + ((fr * F + fc) * NF + (r % NF)) * NF + (c % NF));
-        if (fr == fc) v -= Tm[(fr * NF + r % NF) * NF + (c % NF)];
+        if (fr == fc) v -= Tm[tm_index<NF>(fr, r % NF, c % NF)];
         const bool br = (bmask >> fr) & 1u;
         const bool bc = (bmask >> fc) & 1u;
         // Dirichlet Set: boundary rows become identity rows (columns are kept)
@@ -658,7 +667,7 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
       // rows above k: BW[i] -= L[k][i] * x_k
       for (int ic = t; ic < k * LW; ic += 32) {
         const int i = ic / LW, c = ic % LW;
-        BW[i * LW + c] -= Am[k * N + i] * BW[k * LW + c];
+        BW[i * LW + c] -= Am[pl_index(k, i)] * BW[k * LW + c];
       }
       __syncwarp();
     }
@@ -765,7 +774,9 @@ unsigned grid_cap(int64_t n, int threads) {
 template <int D, int P>
 cudaError_t launch_affine_t(const LocalParams& p, const double* atab, double* geo, double* prep, cudaStream_t s) {
   using L = AffLayout<D, P>;
-  constexpr int EPC = 8;
+  // warps (elements) per block: 4 when a warp's region is large, so that the
+  // shared memory of an SM is used by several blocks without a remainder
+  constexpr int EPC = L::WARP * 8 * 8 > 96 * 1024 ? 4 : 8;
   affine_prep<D, P><<<grid_cap(p.nCells, 128), 128, 0, s>>>(p, atab, prep, geo);
   size_t smem = (size_t)EPC * L::WARP * sizeof(double);
   auto kern = local_affine<D, P, EPC>;
