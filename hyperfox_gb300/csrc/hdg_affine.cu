@@ -182,8 +182,9 @@ struct AffLayout {
   // per-element precomputed factors (affine_prep): G, |J|, |F_f|, n_f, Gamma,
   // g_f, c_ff', f(x_q) w_q |J|, K
   static constexpr int P_IV = 0, P_DET = P_IV + D * D, P_AR = P_DET + 1, P_NRM = P_AR + F, P_GAM = P_NRM + F * D;
-  static constexpr int P_GV = P_GAM + D * D, P_CFF = P_GV + F * D, P_FQ = P_CFF + F * F, P_KS = P_FQ + NI;
-  static constexpr int PREP = P_KS + D * D;
+  static constexpr int P_GV = P_GAM + D * D, P_CFF = P_GV + F * D, P_KS = P_CFF + F * F, P_FQ = P_KS + D * D;
+  static constexpr int PREP = P_FQ + NI;
+  static constexpr int P_SMEM = P_FQ;  // the part of the record staged in shared memory
   // offsets in the packed quadrature table (phi, dphi, w, fphi, fdphi, fw)
   static constexpr int T_PHI = 0;
   static constexpr int T_DPHI = T_PHI + NI * N;
@@ -192,23 +193,27 @@ struct AffLayout {
   static constexpr int T_FDPHI = T_FPHI + NIF * NF;
   // per-warp shared region (doubles)
   static constexpr int LW = LL + 1;              // columns of [B | f_u]
-  static constexpr int PR = 0;                   // PREP  the element's affine_prep record
-  static constexpr int TAU = PR + PREP;          // F*NF
+  static constexpr int H0 = LL / 2;              // columns of B in the first pass
+  static constexpr int LWH = LL - H0 + 1;        // widest pass: the second, with f_u
   static constexpr int NT = NF * (NF + 1) / 2;
-  static constexpr int TM = TAU + F * NF;        // F*NT  tau face masses, symmetric, packed
-  static constexpr int AM = TM + F * NT;         // N(N+1)/2  lower triangle of A, packed by rows, then L
-  static constexpr int BW = AM + N * (N + 1) / 2; // N*LW row-major
-  static constexpr int IDG = BW + N * LW;        // N     1 / L[k][k]
-  static constexpr int WDS = (IDG + N + 1) & ~1; // N*LL  W as float pairs (hi, lo)
-  // Runge-Kutta stage vector w (u, q, lambda parts), y_r = (K G)^T w_q, K n_f, K G:
-  // dead before W exists, so they share its region
+  static constexpr int PR = 0;                   // P_SMEM  the element's affine_prep record
+  static constexpr int TM = PR + P_SMEM;         // F*NT  tau face masses, symmetric, packed
+  static constexpr int AM = TM + F * NT;         // N(N+1)/2  lower triangle of A by rows, then L
+                                                 //   with 1 / L[k][k] on the diagonal
+  static constexpr int BW = AM + N * (N + 1) / 2; // N*LWH  the columns of one pass, row-major
+  static constexpr int FU = BW + N * LWH;        // N     f_u
+  static constexpr int Y0P = FU + N;             // N     y0 = L^{-1} f_u as float pairs
+  static constexpr int WDS = (Y0P + N + 1) & ~1; // N*LL  W as float pairs (hi, lo)
+  // before W exists its region holds the Runge-Kutta stage vector w (u, q,
+  // lambda parts), y_r = (K G)^T w_q, K n_f, K G, and the face tau values
   static constexpr int RKU = WDS;                // N
   static constexpr int RKQ = RKU + N;            // N*D
   static constexpr int RKL = RKQ + N * D;        // F*NF
   static constexpr int RKY = RKL + F * NF;       // D*N
   static constexpr int RKN = RKY + D * N;        // F*D
   static constexpr int RKG = RKN + F * D;        // D*D
-  static constexpr int WARP = (WDS + N * LL > RKG + D * D) ? WDS + N * LL : RKG + D * D;
+  static constexpr int TAU = RKG + D * D;        // F*NF
+  static constexpr int WARP = (WDS + N * LL > TAU + F * NF) ? WDS + N * LL : TAU + F * NF;
 };
 
 // Per-element geometry and source, one thread per element (full warps): the
@@ -372,8 +377,7 @@ template <int D, int P, int EPC>
 __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const double* __restrict__ atab,
                                                          const double* __restrict__ prep) {
   using L = AffLayout<D, P>;
-  constexpr int N = L::N, NF = L::NF, F = L::F, NI = L::NI, LL = L::LL, LW = L::LW;
-  constexpr int DM = D - 1;
+  constexpr int N = L::N, NF = L::NF, F = L::F, NI = L::NI, LL = L::LL;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* sm = reinterpret_cast<double*>(smem_raw);
   __shared__ int sFN[F * NF];
@@ -396,11 +400,11 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
   const double* nrm = pr + L::P_NRM;
   const double* cff = pr + L::P_CFF;
   const double* area = pr + L::P_AR;
-  const double* fq = pr + L::P_FQ;
   double* Tm = W + L::TM;
   double* Am = W + L::AM;
   double* BW = W + L::BW;
-  double* idg = W + L::IDG;
+  double* FUv = W + L::FU;
+  float2* y0p = reinterpret_cast<float2*>(W + L::Y0P);
   float2* wds = reinterpret_cast<float2*>(W + L::WDS);
   double* rku = W + L::RKU;
   double* rkq = W + L::RKQ;
@@ -420,7 +424,8 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
   const int64_t nWarps = (int64_t)gridDim.x * EPC;
   for (int64_t e = (int64_t)blockIdx.x * EPC + warp; e < p.nCells; e += nWarps) {
     // ------------------------------------- gather: prep record and face tau
-    for (int i = t; i < L::PREP; i += 32) pr[i] = prep[e * L::PREP + i];
+    for (int i = t; i < L::P_SMEM; i += 32) pr[i] = prep[e * L::PREP + i];
+    const double* fq = prep + e * L::PREP + L::P_FQ;  // read once, from global
     for (int i = t; i < F * NF; i += 32) {
       int f = p.cell2face[e * F + i / NF];
       int side = (p.face2cell[2 * (int64_t)f] == (int)e) ? 0 : 1;
@@ -496,17 +501,6 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
       if (p.dt > 0.0) v += detJ * __ldg(tM + ij);
       Am[pl_index(i, j)] = v;
     }
-    for (int ic = t; ic < N * LL; ic += 32) {
-      const int i = ic / LL, c = ic % LL;
-      const int f = c / NF, b = c % NF;
-      double acc = 0.0;
-#pragma unroll
-      for (int r = 0; r < D; ++r) acc += gv[f * D + r] * __ldg(tP + ((r * F + f) * N + i) * NF + b);
-      double v = -area[f] * acc;
-      const int a = sPos[f * N + i];
-      if (a >= 0) v -= Tm[tm_index<NF>(f, a, b)];
-      BW[i * LW + c] = v;
-    }
     for (int i = t; i < N; i += 32) {
       double acc = 0.0;
       for (int q = 0; q < NI; ++q) acc += phi[q * N + i] * fq[q];
@@ -536,7 +530,7 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
           for (int j = 0; j < N; ++j) vol += __ldg(tC + (r * N + i) * N + j) * rky[r * N + j];
         v -= kw + detJ * vol;
       }
-      BW[i * LW + LL] = v;
+      FUv[i] = v;
     }
     __syncwarp();
     // ------------------------------------- Cholesky A = L L^T (lower, in place)
@@ -545,12 +539,8 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
       const double akk = Am[pl_index(k, k)];
       if (!(akk > 0.0)) bad = true;
       const double il = rsqrt(akk > 0.0 ? akk : 1.0);  // 1 / L[k][k]
-      const double lkk = (akk > 0.0 ? akk : 1.0) * il;
       __syncwarp();
-      if (t == 0) {
-        Am[pl_index(k, k)] = lkk;
-        idg[k] = il;
-      }
+      if (t == 0) Am[pl_index(k, k)] = il;  // only 1 / L[k][k] is used from here on
       for (int i = k + 1 + t; i < N; i += 32) Am[pl_index(i, k)] *= il;
       __syncwarp();
       const int m = N - k - 1;
@@ -565,27 +555,75 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
       __syncwarp();
     }
     if (bad && t == 0) atomicCAS(p.status, 0, 1);
-    // ---------------------- forward substitution: [W | y0] = L^{-1} [B | f_u]
-    // row-oriented: after row k is final, every lane updates (row, column)
-    // pairs below it, so all 32 lanes stay busy whatever the column count
-    for (int k = 0; k < N; ++k) {
-      for (int c = t; c < LW; c += 32) BW[k * LW + c] *= idg[k];
+    // ---------------- two passes over the columns of B ([0, H0), then the rest
+    // with f_u): each forms its columns of B, forward- and back-substitutes them
+    // in FP64 ([W | y0] = L^{-1} [B | f_u], then L^{-T}), keeps W as double-float
+    // pairs for S and writes its columns of U = -dt L^{-T} W (and U0).
+    double* Ug = (double*)p.U + e * N * LL;
+    constexpr int LWH = L::LWH;
+    for (int h = 0; h < 2; ++h) {
+      const int c0 = h ? L::H0 : 0, nc = h ? LL - L::H0 : L::H0, wc = nc + h;
+      for (int ic = t; ic < N * nc; ic += 32) {
+        const int i = ic / nc, cl = ic % nc, c = c0 + cl;
+        const int f = c / NF, b = c % NF;
+        double acc = 0.0;
+#pragma unroll
+        for (int r = 0; r < D; ++r) acc += gv[f * D + r] * __ldg(tP + ((r * F + f) * N + i) * NF + b);
+        double v = -area[f] * acc;
+        const int a = sPos[f * N + i];
+        if (a >= 0) v -= Tm[tm_index<NF>(f, a, b)];
+        BW[i * LWH + cl] = v;
+      }
+      if (h)
+        for (int i = t; i < N; i += 32) BW[i * LWH + nc] = FUv[i];
       __syncwarp();
-      const int rows = N - k - 1;
-      for (int ic = t; ic < rows * LW; ic += 32) {
-        const int i = k + 1 + ic / LW, c = ic % LW;
-        BW[i * LW + c] -= Am[pl_index(i, k)] * BW[k * LW + c];
+      // forward, row-oriented: after row k is final every lane updates (row, column)
+      // pairs below it, so all 32 lanes stay busy whatever the column count
+      for (int k = 0; k < N; ++k) {
+        const double ik = Am[pl_index(k, k)];
+        for (int c = t; c < wc; c += 32) BW[k * LWH + c] *= ik;
+        __syncwarp();
+        const int rows = N - k - 1;
+        for (int ic = t; ic < rows * wc; ic += 32) {
+          const int i = k + 1 + ic / wc, c = ic % wc;
+          BW[i * LWH + c] -= Am[pl_index(i, k)] * BW[k * LWH + c];
+        }
+        __syncwarp();
+      }
+      if (!p.explicitMode) {
+        for (int idx = t; idx < N * nc; idx += 32) {
+          const int m = idx / nc, cl = idx % nc;
+          const double w = BW[m * LWH + cl];
+          const float hi = __double2float_rn(w);
+          wds[m * LL + c0 + cl] = make_float2(hi, __double2float_rn(w - (double)hi));
+        }
+        if (h)
+          for (int m = t; m < N; m += 32) {
+            const double y = BW[m * LWH + nc];
+            const float hi = __double2float_rn(y);
+            y0p[m] = make_float2(hi, __double2float_rn(y - (double)hi));
+          }
       }
       __syncwarp();
+      // back substitution in place: rows above k get BW[i] -= L[k][i] x_k
+      for (int k = N - 1; k >= 0; --k) {
+        const double ik = Am[pl_index(k, k)];
+        for (int c = t; c < wc; c += 32) BW[k * LWH + c] *= ik;
+        __syncwarp();
+        for (int ic = t; ic < k * wc; ic += 32) {
+          const int i = ic / wc, c = ic % wc;
+          BW[i * LWH + c] -= Am[pl_index(k, i)] * BW[k * LWH + c];
+        }
+        __syncwarp();
+      }
+      for (int idx = t; idx < N * nc; idx += 32) {
+        const int i = idx % N, cl = idx / N;
+        Ug[(c0 + cl) * N + i] = -cs * BW[i * LWH + cl];
+      }
+      if (h)
+        for (int i = t; i < N; i += 32) ((double*)p.U0)[e * N + i] = BW[i * LWH + nc];
+      __syncwarp();
     }
-    // W as double-float pairs for the product below
-    for (int idx = t; !p.explicitMode && idx < N * LL; idx += 32) {
-      const int m = idx / LL, c = idx % LL;
-      const double w = BW[m * LW + c];
-      const float hi = __double2float_rn(w);
-      wds[idx] = make_float2(hi, __double2float_rn(w - (double)hi));
-    }
-    __syncwarp();
     // ------------------ S = C + dt W^T W (upper triangle, mirrored), S0 = W^T y0
     {
       double* Sg = (double*)p.S + e * LL * LL;
@@ -653,27 +691,14 @@ __global__ void __launch_bounds__(32 * EPC) local_affine(LocalParams p, const do
         if ((bmask >> f) & 1u) {
           v = p.dirichlet[(int64_t)p.cell2face[e * F + f] * NF + c % NF];
         } else {
-          v = 0.0;
-          for (int m = 0; m < N; ++m) v += BW[m * LW + c] * BW[m * LW + LL];
+          float sh = 0.f, sl = 0.f;  // S0 = W^T y0
+          for (int m = 0; m < N; ++m) ds_mac(sh, sl, wds[m * LL + c], y0p[m]);
+          v = (double)sh + (double)sl;
         }
         ((double*)p.S0)[e * LL + c] = v;
       }
     }
     __syncwarp();
-    // ------------- back substitution: U = -dt L^{-T} W, U0 = L^{-T} y0 (in place)
-    for (int k = N - 1; k >= 0; --k) {
-      for (int c = t; c < LW; c += 32) BW[k * LW + c] *= idg[k];
-      __syncwarp();
-      // rows above k: BW[i] -= L[k][i] * x_k
-      for (int ic = t; ic < k * LW; ic += 32) {
-        const int i = ic / LW, c = ic % LW;
-        BW[i * LW + c] -= Am[pl_index(k, i)] * BW[k * LW + c];
-      }
-      __syncwarp();
-    }
-    double* Ug = (double*)p.U + e * N * LL;
-    for (int idx = t; idx < N * LL; idx += 32) Ug[idx] = -cs * BW[(idx % N) * LW + idx / N];
-    for (int i = t; i < N; i += 32) ((double*)p.U0)[e * N + i] = BW[i * LW + LL];
     __syncwarp();
   }
 }
