@@ -217,7 +217,8 @@ __global__ void coarse_elem(CoarseDev c, const T* __restrict__ S) {
       float t[NV1];
 #pragma unroll
       for (int m2 = 0; m2 < NV1; ++m2) t[m2] = 0.f;
-      for (int col = 0; col < LL; ++col) {
+#pragma unroll 8
+      for (int col = 0; col < LL; ++col) {  // unrolled: eight rows of S in flight per lane
         const float mc = (fmask >> (col / NF)) & 1u ? 1.f : 0.f;
         const float s = (float)Se[r + (int64_t)col * LL] * mc;
 #pragma unroll

@@ -526,46 +526,78 @@ __global__ void __launch_bounds__(kThreads) prepare_system(TraceView A, const do
 
 // Inverse diagonal / inverse diagonal face blocks of A' (FP64 and FP32 copies).
 // TM: arithmetic of the inversion (float when only the FP32 copy is wanted).
+// Block-Jacobi inverses of the diagonal face blocks, one face per NF lanes
+// (three faces per warp at NF = 10): lane a holds row a of [B | I] in
+// registers and every Gauss-Jordan step takes the pivot row from its lane by
+// shuffles (SPD blocks: no pivoting). Lane a reads row a of the stored
+// column-major block, coalesced with the face's other rows.
 template <int NF, typename TM = double>
-__global__ void build_precond(TraceView A, const double* __restrict__ val, int pcType, double* pc64, float* pc32) {
-  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < A.nFaces; f += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t b0 = A.browptr[f];
-    const int nb = (int)(A.browptr[f + 1] - b0);
-    int kd = 0;
-    for (int k = 0; k < nb; ++k)
-      if (A.bcol[b0 + k] == (int)f) kd = k;
-    TM B[NF][2 * NF];
-    for (int a = 0; a < NF; ++a)
-      for (int b = 0; b < NF; ++b) {
-        TM v = A.isBnd[f] ? TM(a == b ? 1 : 0) : -(TM)val[(b0 + kd) * NF * NF + (int64_t)b * NF + a];
-        B[a][b] = v;
-        B[a][NF + b] = TM(a == b ? 1 : 0);
-      }
+__global__ void __launch_bounds__(kThreads) build_precond(TraceView A, const double* __restrict__ val, int pcType,
+                                                          double* pc64, float* pc32) {
+  constexpr int NBMAX = 1;  // only the face slots of the row layout are used here
+  HFX_FACE_SLOTS(NF)
+  const int base = (laneUsed ? slot : 0) * NF;  // spare lanes follow the first face
+  for (int64_t fb = ((int64_t)blockIdx.x * (kThreads / 32) + warp) * FPW; fb < A.nFaces; fb += faceStride) {
+    const int64_t f = fb + slot;
+    const bool act = laneUsed && f < A.nFaces;
+    int64_t bd = 0;  // the diagonal block
+    bool bnd = false;
+    if (act) {
+      const int64_t b0 = A.browptr[f];
+      const int nb = (int)(A.browptr[f + 1] - b0);
+      bd = b0;
+      for (int k = 0; k < nb; ++k)
+        if (A.bcol[b0 + k] == (int)f) bd = b0 + k;
+      bnd = A.isBnd[f] != 0;
+    }
+    TM row[2 * NF];
+#pragma unroll
+    for (int b = 0; b < NF; ++b) {
+      row[b] = (!act || bnd) ? TM(a == b ? 1 : 0) : -(TM)val[bd * NF * NF + (int64_t)b * NF + a];
+      row[NF + b] = TM(a == b ? 1 : 0);
+    }
     if (pcType == 1) {
-      for (int a = 0; a < NF; ++a) {
-        TM d = B[a][a];
-        TM v = d != TM(0) ? TM(1) / d : TM(1);
-        if (pc64) pc64[f * NF + a] = v;
+      if (act) {
+        TM d = TM(0);  // row[a] without a dynamic index (keeps row in registers)
+#pragma unroll
+        for (int b = 0; b < NF; ++b)
+          if (b == a) d = row[b];
+        const TM v = d != TM(0) ? TM(1) / d : TM(1);
+        if (pc64) pc64[f * NF + a] = (double)v;
         if (pc32) pc32[f * NF + a] = (float)v;
       }
       continue;
     }
-    // Gauss-Jordan (SPD block, no pivoting)
+#pragma unroll
     for (int k = 0; k < NF; ++k) {
-      TM inv = TM(1) / B[k][k];
-      for (int j = 0; j < 2 * NF; ++j) B[k][j] *= inv;
-      for (int i = 0; i < NF; ++i) {
-        if (i == k) continue;
-        TM l = B[i][k];
-        for (int j = 0; j < 2 * NF; ++j) B[i][j] -= l * B[k][j];
+      TM piv[2 * NF];
+#pragma unroll
+      for (int j = 0; j < 2 * NF; ++j) piv[j] = __shfl_sync(0xffffffffu, row[j], base + k);
+      const TM inv = TM(1) / piv[k];
+      if (laneUsed && a == k) {
+#pragma unroll
+        for (int j = 0; j < 2 * NF; ++j) row[j] = piv[j] * inv;
+      } else {
+        const TM l = row[k] * inv;
+#pragma unroll
+        for (int j = 0; j < 2 * NF; ++j) row[j] -= l * piv[j];
       }
     }
-    for (int a = 0; a < NF; ++a)
-      for (int b = 0; b < NF; ++b) {
-        if (pc64) pc64[f * NF * NF + b * NF + a] = B[a][NF + b];  // column-major
-        if (pc32) pc32[f * NF * NF + b * NF + a] = (float)B[a][NF + b];
+    if (act)
+#pragma unroll
+      for (int b = 0; b < NF; ++b) {  // column-major inverse
+        if (pc64) pc64[f * NF * NF + b * NF + a] = (double)row[NF + b];
+        if (pc32) pc32[f * NF * NF + b * NF + a] = (float)row[NF + b];
       }
   }
+}
+
+template <int NF>
+unsigned precond_grid(int64_t nFaces) {
+  const int64_t perBlock = (kThreads / 32) * (32 / NF);
+  int64_t g = (nFaces + perBlock - 1) / perBlock;
+  if (g > 152 * 8) g = 152 * 8;
+  return (unsigned)(g < 1 ? 1 : g);
 }
 
 // Reliable update of the mixed-precision CG: the true residual
@@ -807,10 +839,10 @@ struct Driver {
     if (pcT > 0) {
       // the mixed-precision solve only applies the FP32 copy: invert in FP32
       if (a.mixed)
-        build_precond<NF, float><<<(unsigned)((A.nFaces + 127) / 128), 128, 0, s>>>(A, a.val, pcT, nullptr,
+        build_precond<NF, float><<<precond_grid<NF>(A.nFaces), kThreads, 0, s>>>(A, a.val, pcT, nullptr,
                                                                                        a.ws.pc32);
       else
-        build_precond<NF><<<(unsigned)((A.nFaces + 127) / 128), 128, 0, s>>>(A, a.val, pcT, a.ws.pc64, nullptr);
+        build_precond<NF><<<precond_grid<NF>(A.nFaces), kThreads, 0, s>>>(A, a.val, pcT, a.ws.pc64, nullptr);
     }
     tm->end(K_OTHER, s);
     if ((err = cudaGetLastError()) != cudaSuccess) return fail(err);
@@ -1079,7 +1111,7 @@ static void prepare_t(const TraceSolveArgs& a) {
   a.timer->begin(K_OTHER, s);
   prepare_system<NF, NBMAX><<<gridS, kThreads, 0, s>>>(a.A, a.val, a.rhs, a.ws.bS, a.mixed ? a.ws.val32 : nullptr);
   if (a.precond > 0)
-    build_precond<NF><<<(unsigned)((a.A.nFaces + 127) / 128), 128, 0, s>>>(a.A, a.val, a.precond, a.ws.pc64,
+    build_precond<NF><<<precond_grid<NF>(a.A.nFaces), kThreads, 0, s>>>(a.A, a.val, a.precond, a.ws.pc64,
                                                                            a.mixed ? a.ws.pc32 : nullptr);
   a.timer->end(K_OTHER, s);
 }
