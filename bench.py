@@ -359,8 +359,9 @@ def run_ours(args, world, rank, local):
     return res, ctx
 
 
-def cpu_sample(cfg_name, nthreads, budget_elems=None):
-    """Time the CPU oracle on a bounded sample: a sub-cube of the same workload."""
+def cpu_sample(cfg_name, nthreads, rtol, budget_elems=None):
+    """Time the CPU oracle on a bounded sample: a sub-cube of the same workload, solved to
+    the same relative residual as the GPU arm."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import _oracle as O
     from hyperfox_gb300 import meshgen
@@ -376,12 +377,12 @@ def cpu_sample(cfg_name, nthreads, budget_elems=None):
     P.set_fields(np.ones(P.ndofs), src_mode=2, dirichlet=g.ravel())
     t0 = time.perf_counter()
     P.assemble(nthreads)
-    x, it = P.solve_gmres(1e-10, 200000, nthreads)
+    x, it = P.solve_gmres(rtol, 200000, nthreads)
     P.recover(x)
     dt = time.perf_counter() - t0
     return dict(value=P.nCells / dt, unit="elements/s", cores=nthreads, kind="port",
                 sample="%s sub-mesh n=%d (%d elements, %d trace DOFs): oracle assemble+condense+scatter, "
-                       "GMRES(30)+Jacobi to 1e-10 (%d its), recovery" % (cfg_name, n, P.nCells, P.ndofs, it),
+                       "GMRES(30)+Jacobi to %g (%d its), recovery" % (cfg_name, n, P.nCells, P.ndofs, rtol, it),
                 seconds=dt)
 
 
@@ -421,7 +422,7 @@ def main():
         nthreads = os.cpu_count() or 1
         vals = []
         for i in range(args.warmup + args.steps):
-            r = cpu_sample(args.config, nthreads)
+            r = cpu_sample(args.config, nthreads, args.rtol)
             if i >= args.warmup:
                 vals.append(r["value"])
         v = statistics.median(vals)
@@ -437,7 +438,7 @@ def main():
     if rank == 0:
         if not args.no_cpu:
             try:
-                res["cpu_baseline"] = cpu_sample(args.config, os.cpu_count() or 1)
+                res["cpu_baseline"] = cpu_sample(args.config, os.cpu_count() or 1, args.rtol)
             except Exception as e:  # the baseline is reported, not required
                 res["cpu_baseline"] = {"error": str(e)}
         print(json.dumps(res))
