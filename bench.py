@@ -37,10 +37,10 @@ sys.path.insert(0, ROOT)
 METRIC = "time-to-solve @1e-8 rel err, learned+mixed vs plain FP64 GPU; elements/s"
 # DRAM bytes per unit from the committed ncu captures (profiles/): the FP32 trace
 # SpMV over the symmetric half storage moves 2.60 bytes per non-zero of the full
-# operator (175.5 MB at 67.44M non-zeros), the FP64 one (full storage) 8.75; the
-# affine element kernel writes 18.6 KB per p=3 tetrahedron.
-TRAFFIC_PER_NNZ = {"spmv32": 175.5e6 / 67.44e6, "spmv64": 590.2e6 / 67.44e6}
-TRAFFIC_PER_ELEMENT_LOCAL = (24.3e6 + 893.0e6) / 48000
+# operator (175.1 MB at 67.44M non-zeros), the FP64 one (full storage) 8.75; the
+# affine element kernel reads and writes 19.7 KB per p=3 tetrahedron.
+TRAFFIC_PER_NNZ = {"spmv32": 175.1e6 / 67.44e6, "spmv64": 590.2e6 / 67.44e6}
+TRAFFIC_PER_ELEMENT_LOCAL = (54.0e6 + 890.3e6) / 48000
 FP64_NOMINAL_TFLOPS = 1.25
 
 CONFIGS = {
@@ -305,7 +305,7 @@ def run_ours(args, world, rank, local):
                     frac=round(tf / FP64_NOMINAL_TFLOPS, 4),
                     traffic=TRAFFIC_PER_ELEMENT_LOCAL * E if (dim, p) == (3, 3) else None,
                     flops_per_element=int(2 * fma), avg_launch_ms=round(avg_ms, 4),
-                    peak_source="nominal GB300 FP64 (no measured FP64 peak); ncu: FP64 pipe 90% busy")
+                    peak_source="nominal GB300 FP64 (no measured FP64 peak); ncu: FP64 pipe 86% active")
 
     dom = max(("local", "spmv64", "spmv32", "update", "scatter", "recover", "residual"), key=lambda k: kt[k][1])
     roof = None
