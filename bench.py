@@ -278,8 +278,10 @@ def run_ours(args, world, rank, local):
         # the FP32 operator of a symmetric problem is stored as its upper block triangle
         # (diagonal blocks + half the off-diagonal ones) plus one int per block locating it
         if key == "spmv32":
+            # rows as fixed-width (block column, block location) slots: 8 bytes per slot
             n_half = (nblocks - ctx.nFaces) // 2 + ctx.nFaces
-            alg = n_half * Nf * Nf * sv + nblocks * 8 + (ctx.nFaces + 1) * 8 + 4 * n * sv
+            width = 7 if dim == 3 else 5
+            alg = n_half * Nf * Nf * sv + ctx.nFaces * width * 8 + 4 * n * sv
         else:
             alg = nnz * sv + nblocks * 4 + (ctx.nFaces + 1) * 8 + 4 * n * sv
         # launches that did work: one per Krylov iteration (launches queued after
@@ -287,7 +289,7 @@ def run_ours(args, world, rank, local):
         launches = min(kt[key][0], iters * args.steps) if iters else kt[key][0]
         avg_ms = kt[key][1] / max(1, launches)
         achieved = alg / (avg_ms / 1e3) / 1e9
-        return dict(bound="hbm", kernel="cg_spmv_half<float>" if sv == 4 else "cg_spmv<double>",
+        return dict(bound="hbm", kernel="cg_spmv_half_ell<float>" if sv == 4 else "cg_spmv<double>",
                     achieved=round(achieved, 1), peak=hbm, unit="GB/s", frac=round(achieved / hbm, 4),
                     traffic=(TRAFFIC_PER_NNZ[key] * nnz) if (dim, p) == (3, 3) else None, bytes_per_launch=int(alg),
                     avg_launch_ms=round(avg_ms, 4), peak_source=peak_kind)

@@ -85,6 +85,8 @@ struct hfx_ctx {
   int64_t* d_browptr = nullptr;
   int* d_bcol = nullptr;
   int* d_hidx = nullptr;     // symmetric half storage map of the face blocks
+  int2* d_ell = nullptr;     // the rows as fixed-width (bcol, hidx) slots
+  int ellWidth = 0;
   int64_t nHalf = 0;
   int* d_brow = nullptr;
   int *d_src0 = nullptr, *d_src1 = nullptr;
@@ -434,7 +436,22 @@ int hfx_mesh_upload(hfx_ctx* c, int dim, int order, int nNodes, const double* co
       }
     c->nHalf = ok ? nh : 0;
     c->d_hidx = nullptr;
-    if (ok) HFX_CUDA(c, upload(m, &c->d_hidx, hidx.data(), hidx.size(), s));
+    c->d_ell = nullptr;
+    c->ellWidth = 0;
+    if (ok) {
+      HFX_CUDA(c, upload(m, &c->d_hidx, hidx.data(), hidx.size(), s));
+      // fixed-width rows (bcol, hidx) for the half-storage SpMV: no row pointers to chase
+      const int W = dim == 2 ? 5 : 7;
+      bool fits = true;
+      for (int f = 0; f < c->topo.nFaces && fits; ++f) fits = rp[f + 1] - rp[f] <= W;
+      if (fits) {
+        std::vector<int2> ell((size_t)c->topo.nFaces * W, make_int2(0, INT32_MIN));
+        for (int f = 0; f < c->topo.nFaces; ++f)
+          for (int64_t k = rp[f]; k < rp[f + 1]; ++k) ell[(size_t)f * W + (k - rp[f])] = make_int2(cl[k], hidx[k]);
+        HFX_CUDA(c, upload(m, &c->d_ell, ell.data(), ell.size(), s));
+        c->ellWidth = W;
+      }
+    }
   }
   {
     std::vector<double> atab;
@@ -1512,6 +1529,8 @@ int hfx_solve(hfx_ctx* c, const hfx_solve_opts* opts, double* trace, hfx_solve_i
   a.A = TraceView{c->topo.nFaces, c->re.nNodesFace, c->d_browptr, c->d_bcol, c->d_isBnd};
   if (method == HFX_KSP_CG && c->kappaCellConstant) {
     a.A.hidx = c->d_hidx;  // symmetric operator: FP32 copy in half storage
+    a.A.ell = c->d_ell;
+    a.A.ellWidth = c->ellWidth;
     a.A.nHalf = c->nHalf;
   }
   a.val = c->d_val;

@@ -26,6 +26,7 @@
 // broken down) every later kernel returns at entry, so the host may queue
 // many iterations between checks.
 #include <algorithm>
+#include <climits>
 #include <type_traits>
 #include <cmath>
 #include <cstdio>
@@ -191,6 +192,76 @@ __global__ void __launch_bounds__(kThreads) cg_spmv_half(TraceView A, const floa
       pnew[i] = pi;
       q[i] = y;
       pq += (double)pi * (double)y;
+    }
+    __syncwarp();
+  }
+  double v[1] = {pq}, tot[1];
+  if (block_reduce_last<1>(v, partials, &st->ticket, tot) && threadIdx.x == 0) {
+    double pAp = tot[0];
+    if (!(pAp > 0.0) || !isfinite(pAp)) {
+      st->status = isfinite(pAp) ? 6 : 7;
+      st->done = 1;
+    } else {
+      st->alpha = st->rz / pAp;
+    }
+  }
+}
+
+// cg_spmv_half over the fixed-width rows: the (block column, block location)
+// pairs of a face are one 8-byte load per slot at f * NBMAX + k, so no row
+// pointer has to arrive before the gather and the value loads can start; the
+// products are the same, in the same order. At most six 256-thread blocks per
+// SM keep the register count of the row-pointer version.
+template <int NF, int NBMAX>
+__global__ void __launch_bounds__(kThreads, 6) cg_spmv_half_ell(TraceView A, const float* __restrict__ valh,
+                                                                const float* __restrict__ z,
+                                                                const float* __restrict__ pold,
+                                                                float* __restrict__ pnew, float* __restrict__ q,
+                                                                CgState* st, double* partials, int first) {
+  __shared__ float xsh[kThreads / 32][RowCfg<NF, NBMAX>::FPW][RowCfg<NF, NBMAX>::NPOS];
+  if (st->done) return;
+  const float beta = first ? 0.f : (float)st->beta;
+  HFX_FACE_SLOTS(NF)
+  double pq = 0.0;
+  for (int64_t fb = ((int64_t)blockIdx.x * (kThreads / 32) + warp) * FPW; fb < A.nFaces; fb += faceStride) {
+    const int64_t f = fb + slot;
+    const bool act = laneUsed && f < A.nFaces;
+    float* xs = laneUsed ? xsh[warp][slot] : nullptr;
+    int hh[NBMAX];
+#pragma unroll
+    for (int k = 0; k < NBMAX; ++k) hh[k] = INT_MIN;
+    if (act) {
+      const int2* row = A.ell + f * NBMAX;
+      for (int k = 0; k < NBMAX; ++k) {
+        const int2 e2 = __ldg(row + k);
+        hh[k] = e2.y;
+        if (e2.y != INT_MIN) {
+          const int64_t j = (int64_t)e2.x * NF + a;
+          xs[k * NF + a] = fmaf(beta, pold[j], z[j]);
+        }
+      }
+    }
+    __syncwarp();
+    if (act) {
+      float acc = 0.f;
+#pragma unroll
+      for (int k = 0; k < NBMAX; ++k) {
+        const int h = hh[k];
+        if (h != INT_MIN) {
+          const float* blk = h >= 0 ? valh + (int64_t)h * NF * NF + a : valh + (int64_t)(-h - 1) * NF * NF + (int64_t)a * NF;
+          const int sb = h >= 0 ? NF : 1;
+          float v[NF];
+#pragma unroll
+          for (int b = 0; b < NF; ++b) v[b] = __ldg(blk + b * sb);
+#pragma unroll
+          for (int b = 0; b < NF; ++b) acc = fmaf(v[b], xs[k * NF + b], acc);
+        }
+      }
+      const int64_t i = f * NF + a;
+      const float pi = fmaf(beta, pold[i], z[i]);
+      pnew[i] = pi;
+      q[i] = acc;
+      pq += (double)pi * (double)acc;
     }
     __syncwarp();
   }
@@ -803,6 +874,7 @@ struct Driver {
     cudaError_t err;
     const int gridF = grid_of(cg_spmv<double, NF, NBMAX, true>, kThreads);
     const int gridF32 = grid_of(cg_spmv<float, NF, NBMAX, false>, kThreads);
+    const int gridE = grid_of(cg_spmv_half_ell<NF, NBMAX>, kThreads);
     const int gridU = grid_of(cg_update<double, NF, 2>, kThreads);
     const int gridS = grid_of(prepare_system<NF, NBMAX>, kThreads);
     const int gridR1 = grid_of(cg_update_r<double, NF>, kThreads);
@@ -983,7 +1055,10 @@ struct Driver {
             float* pold = (it & 1) ? p132 : p032;
             float* pnew = (it & 1) ? p032 : p132;
             tm->begin(K_SPMV32, s);
-            if (half)
+            if (half && A.ell && A.ellWidth == NBMAX)
+              cg_spmv_half_ell<NF, NBMAX><<<gridE, kThreads, 0, s>>>(A, a.ws.val32h, z32, pold, pnew, q32, st,
+                                                                      partials, first ? 1 : 0);
+            else if (half)
               cg_spmv_half<NF, NBMAX><<<gridF32, kThreads, 0, s>>>(A, a.ws.val32h, z32, pold, pnew, q32, st, partials,
                                                                     first ? 1 : 0);
             else

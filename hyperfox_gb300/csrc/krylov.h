@@ -21,6 +21,10 @@ struct TraceView {
   // means block (g, f) stored at -hidx[k]-1, read transposed.
   const int* hidx = nullptr;
   int64_t nHalf = 0;
+  // the same rows as a fixed-width table (ELL): slot k of face f holds (bcol, hidx)
+  // at ell[f * ellWidth + k], unused slots (0, INT_MIN); nullptr when not built
+  const int2* ell = nullptr;
+  int ellWidth = 0;
 };
 
 // Device-resident solver scalars. Reductions finish in the last block, which
