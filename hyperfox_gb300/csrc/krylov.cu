@@ -1005,7 +1005,9 @@ struct Driver {
       // true residual of x (and ||b||^2 of the reference rhs for the tolerance)
       auto replace = [&]() {
         tm->begin(K_OTHER, s);
-        switch (pcT) {
+        // with the two-level preconditioner tl_apply forms z and r.z right after:
+        // the replacement skips its own block-Jacobi product
+        switch (twoLevel ? 0 : pcT) {
           case 0: cg_replace<NF, NBMAX, 0><<<gridR, kThreads, 0, s>>>(A, a.val, a.ws.bS, a.rhs, x, r32, z32, a.ws.pc32, st, partials); break;
           case 1: cg_replace<NF, NBMAX, 1><<<gridR, kThreads, 0, s>>>(A, a.val, a.ws.bS, a.rhs, x, r32, z32, a.ws.pc32, st, partials); break;
           default: cg_replace<NF, NBMAX, 2><<<gridR, kThreads, 0, s>>>(A, a.val, a.ws.bS, a.rhs, x, r32, z32, a.ws.pc32, st, partials); break;
@@ -1093,6 +1095,7 @@ struct Driver {
         // reliable update: x += y (FP64), r = b' - A' x (FP64), direction kept
         accum_x<<<gridU, kThreads, 0, s>>>(n, y32, x);
         hst.ticket = 0;
+        hst.done = 0;  // the stretch's stop flag would make the two-level z of the replacement return at entry
         cudaMemcpyAsync(st, &hst, sizeof(CgState), cudaMemcpyHostToDevice, s);
         if ((err = replace()) != cudaSuccess) return fail(err);
         refinements += 1;
