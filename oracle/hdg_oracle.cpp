@@ -691,6 +691,25 @@ struct Problem {
   int iters = 0;
 };
 
+// RungeKutta::apply (RungeKutta.cpp:90-129) on the first lenU rows of A (all n
+// columns) and of rhs: uj = dt comb + ut (comb = sum_{i<s} a_si k_i), then
+// s = dt s - dt K uj; K = dt a_ss K; K[:, :lenU] += M; s += K ut.
+static void rk_apply(Mat& A, std::vector<double>& rhs, int lenU, int n, const Mat& M, const std::vector<double>& ut,
+                     const std::vector<double>& comb, double dt, double aDiag) {
+  std::vector<double> uj(n);
+  for (int j = 0; j < n; ++j) uj[j] = dt * comb[j] + ut[j];
+  for (int i = 0; i < lenU; ++i) {
+    double kuj = 0.0;
+    for (int j = 0; j < n; ++j) kuj += A(i, j) * uj[j];
+    rhs[i] = dt * rhs[i] - dt * kuj;
+    for (int j = 0; j < n; ++j) A(i, j) *= dt * aDiag;
+    for (int j = 0; j < lenU; ++j) A(i, j) += M(i, j);
+    double kut = 0.0;
+    for (int j = 0; j < n; ++j) kut += A(i, j) * ut[j];
+    rhs[i] += kut;
+  }
+}
+
 // Local matrix + RHS for one element (HDGDiffusionSource::computeLocalMatrix /
 // computeLocalRHS, HDGDiffusionSource.cpp:43-85, HDGModel.cpp:35-85).
 static void local_system(const Problem& P, int iEl, Mat& A, std::vector<double>& rhs,
@@ -923,17 +942,7 @@ static void local_system(const Problem& P, int iEl, Mat& A, std::vector<double>&
         ut[startL + fi * Nf + j] = P.rkOldL[g];
         uj[startL + fi * Nf + j] = P.rkCombL[g];
       }
-    for (int j = 0; j < n; ++j) uj[j] = dt * uj[j] + ut[j];
-    for (int i = 0; i < lenU; ++i) {
-      double kuj = 0.0;
-      for (int j = 0; j < n; ++j) kuj += A(i, j) * uj[j];
-      rhs[i] = dt * rhs[i] - dt * kuj;
-      for (int j = 0; j < n; ++j) A(i, j) *= dt * P.rkDiag;
-      for (int j = 0; j < N; ++j) A(i, j) += M(i, j);
-      double kut = 0.0;
-      for (int j = 0; j < n; ++j) kut += A(i, j) * ut[j];
-      rhs[i] += kut;
-    }
+    rk_apply(A, rhs, lenU, n, M, ut, uj, dt, P.rkDiag);
   } else if (P.dt > 0.0) {
     // implicit Euler on the U rows (HDGModel.cpp:39-47, Euler.cpp:18-34, Mass.cpp:5-38)
     Mat M(N, N);
@@ -1370,6 +1379,21 @@ int orc_problem_set_fields(void* h, const double* tau, int tauVals, const double
     if (dirichlet) P->dirichlet.assign(dirichlet, dirichlet + (size_t)P->mf.nFaces * Nf);
     P->dt = dt;
     if (dt > 0.0) P->uOld.assign(uOld, uOld + (size_t)P->nCells * N);
+  })
+}
+
+// RungeKutta::apply on a given stiffness K (lenU x n, column-major) and rhs (lenU),
+// mass M (lenU x lenU): the same algebra the element systems get.
+int orc_rk_apply(int lenU, int n, double* K, double* rhs, const double* M, const double* ut, const double* comb,
+                 double dt, double aDiag) {
+  ORC_TRY({
+    Mat A(lenU, n), Mm(lenU, lenU);
+    std::copy(K, K + (size_t)lenU * n, A.a.begin());
+    std::copy(M, M + (size_t)lenU * lenU, Mm.a.begin());
+    std::vector<double> r(rhs, rhs + lenU), u(ut, ut + n), c(comb, comb + n);
+    rk_apply(A, r, lenU, n, Mm, u, c, dt, aDiag);
+    std::copy(A.a.begin(), A.a.end(), K);
+    std::copy(r.begin(), r.end(), rhs);
   })
 }
 

@@ -55,6 +55,7 @@ def lib():
         L.orc_problem_set_solver.argtypes = [vp, ip, vp, vp]
         L.orc_problem_solve_faces.argtypes = [vp, vp]
         L.orc_problem_set_rk.argtypes = [vp, dp, dp] + [vp] * 6
+        L.orc_rk_apply.argtypes = [ip, ip, vp, vp, vp, vp, vp, dp, dp]
         _lib = L
     return _lib
 
@@ -236,6 +237,18 @@ class Problem:
         t = np.zeros(5)
         lib().orc_problem_timings(self.h, _ptr(t))
         return dict(local=t[0], dirichlet=t[1], scatter=t[2], solve=t[3], recover=t[4])
+
+
+def rk_apply(K, rhs, M, ut, comb, dt, a_diag):
+    """RungeKutta::apply on a dense stiffness K [lenU x n] and rhs [lenU] (the oracle's code)."""
+    K = np.asfortranarray(K, dtype=np.float64).copy(order="F")
+    rhs = np.ascontiguousarray(rhs, dtype=np.float64).copy()
+    M = np.asfortranarray(M, dtype=np.float64)
+    ut = np.ascontiguousarray(ut, dtype=np.float64)
+    comb = np.ascontiguousarray(comb, dtype=np.float64)
+    _check(lib().orc_rk_apply(K.shape[0], K.shape[1], K.ctypes.data, rhs.ctypes.data, M.ctypes.data,
+                              ut.ctypes.data, comb.ctypes.data, dt, a_diag))
+    return K, rhs
 
 
 # Butcher tables of RungeKutta::setUpDB (RungeKutta.cpp:215-286): rows [c_i | a_i.], last row [0 | b]

@@ -77,3 +77,55 @@ def test_steady_solution_is_a_fixed_point(name):
     run_oracle(P, g, O.BUTCHER[name], 1e-3, 2, fields)
     for k, ref in (("Solution", sol), ("Flux", flux), ("Trace", x)):
         assert np.abs(fields[k] - ref).max() < 1e-9 * np.abs(ref).max(), (name, k)
+
+
+def _operators(n, seed):
+    """A mass-like SPD M and a convection-like C (any matrices do: apply is linear algebra)."""
+    rng = np.random.default_rng(seed)
+    B = rng.normal(size=(n, n))
+    return B @ B.T + n * np.eye(n), rng.normal(size=(n, n))
+
+
+@pytest.mark.parametrize("n", [3, 6, 10])
+def test_apply_matches_reference_unit_test(n):
+    """tests/unittests/operator/TestRungeKutta.cpp: the stage matrices and right-hand sides
+    of BEuler, FEuler and Crank-Nicolson (stages 0 and 1) for K = C, f = 1, OldSolution =
+    RKStage_k = 0, 1, ..., n-1, dt = 0.1; computeStage gives (1 - 2)/dt for Solution 1 and
+    OldSolution 2, and computeSolution the b-weighted update."""
+    M, C = _operators(n, n)
+    dt, f = 0.1, np.ones(n)
+    old = np.arange(n, dtype=float)   # fm["OldSolution"], also every fm["RKStage_k"]
+    zero = np.zeros(n)
+    # BEuler (a_00 = 1): M + dt C, M old + dt f
+    K, s = O.rk_apply(C, f, M, old, zero, dt, 1.0)
+    assert np.abs(K - (M + dt * C)).max() < 1e-12 * np.abs(M).max()
+    assert np.abs(s - (M @ old + dt * f)).max() < 1e-12 * np.abs(M @ old).max()
+    # FEuler (a_00 = 0): M, (M - dt C) old + dt f
+    K, s = O.rk_apply(C, f, M, old, zero, dt, 0.0)
+    assert np.abs(K - M).max() == 0.0
+    assert np.abs(s - ((M - dt * C) @ old + dt * f)).max() < 1e-12 * np.abs(M @ old).max()
+    # Crank-Nicolson stage 0 (a_00 = 0): M, dt (-C old + f) + M old
+    K, s = O.rk_apply(C, f, M, old, zero, dt, 0.0)
+    assert np.abs(s - (dt * (-C @ old + f) + M @ old)).max() < 1e-12 * np.abs(M @ old).max()
+    # stage 1 (a_10 = a_11 = 1/2, k_0 = RKStage_0 = 0..n-1): M + dt/2 C,
+    # dt (-C (old + dt/2 k_0) + f) + (M + dt/2 C) old
+    K, s = O.rk_apply(C, f, M, old, 0.5 * old, dt, 0.5)
+    A1 = M + dt / 2 * C
+    assert np.abs(K - A1).max() < 1e-12 * np.abs(M).max()
+    ref = dt * (-C @ (old + dt / 2 * old) + f) + A1 @ old
+    assert np.abs(s - ref).max() < 1e-12 * np.abs(ref).max()
+    # computeStage / computeSolution on the Field values of the test: Solution 1, OldSolution 2
+    for name in ("BEuler", "FEuler", "CrankNicolson"):
+        rk = O.RungeKutta(O.BUTCHER[name], dt)
+        fields = {"Solution": np.full(n, 2.0), "Flux": np.zeros(n), "Trace": np.zeros(n)}
+        rk.begin_step(fields)
+        fields["Solution"][...] = 1.0
+        rk.stage(fields)
+        assert np.all(rk.k["Solution"][0] == (1.0 - 2.0) / dt)
+        if rk.S == 2:  # the second stage of Crank-Nicolson leaves Solution unchanged: k_1 = 0
+            rk.stage(fields)
+            assert np.all(rk.k["Solution"][1] == 0.0)
+        rk.solution(fields)
+        b = np.array(O.BUTCHER[name])[-1, 1:]
+        expect = 2.0 + dt * sum(b[k] * rk.k["Solution"][k] for k in range(rk.S))
+        assert np.abs(fields["Solution"] - expect).max() < 1e-12
