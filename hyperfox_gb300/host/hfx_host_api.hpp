@@ -204,11 +204,104 @@ struct Field {  // Field.h:14-34: values[entity][objPerEnt][valsPerObj]
 
 struct DirichletModel {};  // Set-type boundary model: identity rows + Dirichlet values
 
+// RungeKutta (src/operator/RungeKutta.h, RKType.h) with the auxiliary fields
+// {"Flux", "Trace"}: the stages run on the device. A model with this time scheme
+// has its U rows modified at every assemble (RungeKutta::apply); at the first
+// stage of a step the solver takes the field map's Solution, Flux and Trace as
+// the Old fields (the reference's tests copy them into OldSolution/OldFlux/
+// OldTrace by hand), and computeStage / computeSolution update the device fields
+// and copy Solution, Flux and Trace back into the field map.
+enum RKType { FEuler, EMidpoint, Heun, Kutta3, Heun3, SSPRK3, RK4, BEuler, IMidpoint, CrankNicolson, KS2, QZ2, ALX2, RK43 };
+
+class RungeKutta {
+ public:
+  explicit RungeKutta(RKType type = CrankNicolson) { setButcherTable(type); }
+  void setButcherTable(RKType type) {
+    int S = 0;
+    if (hfx_rk_butcher((int)type, &S, nullptr)) throw ErrorHandle("RungeKutta", "setButcherTable", "unknown RKType");
+    table_.assign((size_t)(S + 1) * (S + 1), 0.0);
+    hfx_rk_butcher((int)type, &S, table_.data());
+    type_ = (int)type;
+    dirty_ = true;
+  }
+  // row-major (S+1) x (S+1); the strictly upper part must be zero (RungeKutta.cpp:18-32)
+  void setButcherTable(const std::vector<double>& table, int rows, int cols) {
+    if (rows != cols || (int)table.size() != rows * cols)
+      throw ErrorHandle("RungeKutta", "setButcherTable", "the Butcher table should be square");
+    for (int i = 0; i < rows; ++i)
+      for (int j = i + 1; j < cols; ++j)
+        if (table[(size_t)i * cols + j] != 0.0)
+          throw ErrorHandle("RungeKutta", "setButcherTable",
+                            "the upper triangular part of the Butcher table should be null (no fully implicit "
+                            "implementation as of yet)");
+    table_ = table;
+    type_ = -1;
+    dirty_ = true;
+  }
+  void setTimeStep(double dt) {
+    dt_ = dt;
+    dirty_ = true;
+  }
+  int getNumStages() const { return (int)std::lround(std::sqrt((double)table_.size())) - 1; }
+  int getStage() const { return stage_; }
+  void computeStage(std::map<std::string, Field*>* fm) {
+    if (!ctx_) throw ErrorHandle("RungeKutta", "computeStage", "the scheme must be assembled by a solver first");
+    if (stage_ >= getNumStages())
+      throw ErrorHandle("RungeKutta", "computeStage",
+                        "cannot compute more stages than the method allows, think about computing the solution");
+    check(hfx_rk_compute_stage(ctx_), "computeStage");
+    ++stage_;
+    download(fm, "computeStage");
+  }
+  void computeSolution(std::map<std::string, Field*>* fm) {
+    if (!ctx_ || stage_ != getNumStages())
+      throw ErrorHandle("RungeKutta", "computeSolution", "all stages must be computed before computing the solution");
+    check(hfx_rk_compute_solution(ctx_), "computeSolution");
+    stage_ = 0;
+    download(fm, "computeSolution");
+  }
+
+ private:
+  friend class GpuHDGSolver;
+  void check(int rc, const char* where) {
+    if (rc) throw ErrorHandle("RungeKutta", where, ctx_ ? hfx_last_error(ctx_) : "no device context");
+  }
+  // called by the solver before each assemble
+  void prepare(hfx_ctx* ctx, std::map<std::string, Field*>* fm) {
+    if (dt_ == 0.0) throw ErrorHandle("RungeKutta", "apply", "the time step needs to be set before applying and it should not be 0");
+    ctx_ = ctx;
+    if (dirty_) {
+      const int S = getNumStages();
+      check(type_ >= 0 ? hfx_rk_set_type(ctx, type_, dt_) : hfx_rk_set(ctx, S, table_.data(), dt_), "apply");
+      dirty_ = false;
+      stage_ = 0;
+    }
+    if (stage_ == 0) {  // a new step: the field map's state becomes the Old fields
+      check(hfx_set_state(ctx, fm->at("Solution")->values.data(), fm->at("Flux")->values.data()), "apply");
+      check(hfx_set_trace(ctx, fm->at("Trace")->values.data()), "apply");
+      check(hfx_rk_begin_step(ctx), "apply");
+    }
+  }
+  void download(std::map<std::string, Field*>* fm, const char* where) {
+    check(hfx_get_state(ctx_, fm->at("Solution")->values.data(), fm->at("Flux")->values.data(),
+                        fm->at("Trace")->values.data()),
+          where);
+  }
+  std::vector<double> table_;
+  int type_ = -1;
+  double dt_ = 0.0;
+  int stage_ = 0;
+  bool dirty_ = true;
+  hfx_ctx* ctx_ = nullptr;
+};
+
 struct HDGDiffusionSource {  // HDGDiffusionSource.h; HDGLaplaceModel = no source
   int sourceMode = HFX_SRC_NONE;
   double sourceParam = 0.0;
   std::vector<double> sourceValues;  // [nCells][nIP] for HFX_SRC_VALUES
   double dt = 0.0;                   // implicit Euler when > 0 (Euler.cpp:18-34)
+  RungeKutta* timeScheme = nullptr;  // Model::setTimeScheme; replaces dt when set
+  void setTimeScheme(RungeKutta* ts) { timeScheme = ts; }
 };
 struct HDGLaplaceModel : HDGDiffusionSource {};
 
@@ -258,7 +351,9 @@ class GpuHDGSolver {
     dev_->check(hfx_set_source(dev_->ctx(), model_->sourceMode,
                                model_->sourceValues.empty() ? nullptr : model_->sourceValues.data(), model_->sourceParam),
                 "HDGSolver", "assemble");
-    if (model_->dt > 0.0)
+    if (model_->timeScheme)
+      model_->timeScheme->prepare(dev_->ctx(), fields_);
+    else if (model_->dt > 0.0)
       dev_->check(hfx_set_time_scheme(dev_->ctx(), model_->dt, fields_->at("Solution")->values.data()), "HDGSolver", "assemble");
     dev_->check(hfx_assemble(dev_->ctx()), "HDGSolver", "assemble");
     assembled_ = true;

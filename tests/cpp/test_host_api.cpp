@@ -207,6 +207,38 @@ int main(int argc, char** argv) {
     CHECK(s2.lastInfo.status == 0 && s2.lastInfo.fallback == 0);
     for (double v : sol.values) CHECK(std::fabs(v - 3.0) < 1e-11);
     for (double v : lambda.values) CHECK(std::fabs(v - 3.0) < 1e-11);
+
+    // RungeKutta through the host API (TestHDGDiffusionSource.cpp:213-249 loop): the
+    // steady state Solution = Trace = 3, Flux = 0 is a fixed point of every scheme
+    // (dt within RK4's explicit stability limit on this mesh: rounding must not grow)
+    RungeKutta ts(RK4);
+    CHECK(ts.getNumStages() == 4);
+    CHECK(throws([&] { ts.setButcherTable(std::vector<double>(4, 1.0), 2, 2); }));
+    CHECK(throws([&] { ts.computeSolution(&fm); }));
+    ts.setTimeStep(1e-3);
+    HDGLaplaceModel lapT;
+    lapT.setTimeScheme(&ts);
+    GpuHDGSolver s3(&dev);
+    s3.setMesh(&m);
+    s3.setFieldMap(&fm);
+    s3.setLinSystem(o);
+    s3.setModel(&lapT);
+    s3.setBoundaryModel(&dirMod);
+    s3.initialize();
+    s3.allocate();
+    for (int step = 0; step < 2; ++step) {
+      for (int k = 0; k < ts.getNumStages(); ++k) {
+        s3.assemble();
+        s3.solve();
+        ts.computeStage(&fm);
+      }
+      CHECK(throws([&] { ts.computeStage(&fm); }));
+      ts.computeSolution(&fm);
+      CHECK(ts.getStage() == 0);
+    }
+    for (double v : sol.values) CHECK(std::fabs(v - 3.0) < 1e-10);
+    for (double v : lambda.values) CHECK(std::fabs(v - 3.0) < 1e-10);
+    for (double v : flux.values) CHECK(std::fabs(v) < 1e-9);
   }
   std::printf("%s (%d failures)\n", failures ? "FAIL" : "OK", failures);
   return failures ? 1 : 0;
