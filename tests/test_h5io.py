@@ -120,3 +120,23 @@ def test_h5_errors(tmp_path):
     cut.write_bytes(data[: len(data) // 2])
     with pytest.raises(capi.HfxError):
         capi.h5_read_mesh(cut)
+
+
+@have_ref
+def test_every_shipped_h5_file_reads():
+    """All HDF5 files the reference ships (meshes and field files) open, and their
+    meshes are consistent (cells index existing nodes)."""
+    import glob
+    files = sorted(glob.glob(os.path.join(os.path.dirname(REF), "**", "*.h5"), recursive=True))
+    assert len(files) >= 60
+    meshes = 0
+    for f in files:
+        for name in capi.h5_field_names(f):
+            capi.h5_read_field(f, name)
+        try:
+            c, e = capi.h5_read_mesh(f)
+        except capi.HfxError:
+            continue  # field-only files
+        meshes += 1
+        assert e.min() >= 0 and e.max() < c.shape[0] and c.shape[1] in (1, 2, 3)
+    assert meshes >= 50
