@@ -1227,6 +1227,485 @@ static void recover(const Problem& P, const double* trace, double* sol, double* 
   }
 }
 
+// ============================================================ Burgers (vector unknowns)
+// HDGBurgersModel (HDGBurgersModel.cpp:35-125): nd = dim unknowns per node, local
+// matrix = HDGBase + HDGUNabU (+ HDGDiffusion when a diffusion tensor is given), RHS =
+// HDGUNabU's RHS + one scalar Source per component, implicit Euler (Euler.cpp:18-34)
+// with the mass multiplied over the components (Mass.cpp:5-38, Operator.cpp:86-97).
+// Local index layout (HDGBase.cpp:85-91): U (i*nd + c), Q ((i*d + k)*nd + c),
+// L ((f*Nf + a)*nd + c).
+struct BurgersFields {
+  std::vector<double> tau;    // [nFaces][Nf][sides][nd*nd] column-major nd x nd
+  int tauSides = 1;
+  std::vector<double> nu;     // [nCells][N][kc] (kc 0 = no diffusion operator, 1, d*d)
+  int kc = 0;
+  std::vector<double> src;    // [nCells][nI][nd] values at the integration points, or empty
+  std::vector<double> dir;    // [nFaces][Nf][nd]
+  double dt = 0.0;
+  std::vector<double> old;    // "Solution" read by Euler: [nCells][N*nd]
+  std::vector<double> buf;    // BufferSolution [nCells][N*nd]
+  std::vector<double> trace;  // Trace [nFaces][Nf*nd]
+};
+static std::map<const Problem*, BurgersFields> g_burgers;
+
+struct ElemGeo {
+  NodeList X;
+  std::vector<Mat> invJ;
+  std::vector<double> dV;
+  std::vector<std::vector<double>> normals;
+  std::vector<int> facesIn, f2c;
+};
+
+// Element nodes, face2CellMap (HDGSolver.cpp:258-275), volume and face Jacobians
+// (Operator.cpp:14-84, HDGModel.cpp:53-85) and outward normals (HDGBase.cpp:34-65):
+// the same arithmetic as in local_system above.
+static void element_geometry(const Problem& P, int iEl, ElemGeo& g) {
+  const RefEl* re = P.re;
+  const RefEl* fe = re->face;
+  int d = P.dim, N = re->nNodes, F = re->nFaces, Nf = fe->nNodes, nI = re->nIP, nIf = fe->nIP;
+  const int* cell = &P.cells[(size_t)iEl * N];
+  g.X.assign(N, std::vector<double>(d));
+  for (int i = 0; i < N; ++i)
+    for (int k = 0; k < d; ++k) g.X[i][k] = P.coords[(size_t)cell[i] * d + k];
+  g.facesIn.assign(F, 0);
+  g.f2c.assign(F * Nf, 0);
+  for (int i = 0; i < F; ++i) g.facesIn[i] = P.mf.cell2face[(size_t)iEl * F + i];
+  for (int i = 0; i < F; ++i) {
+    const int* face = &P.mf.faces[(size_t)g.facesIn[i] * Nf];
+    for (int j = 0; j < Nf; ++j) {
+      int node = cell[re->faceNodes[i][j]], pos = -1;
+      for (int q = 0; q < Nf; ++q)
+        if (face[q] == node) { pos = q; break; }
+      if (pos < 0) throw std::runtime_error("couldn't find cell node in face");
+      g.f2c[i * Nf + j] = pos;
+    }
+  }
+  g.invJ.assign(nI, Mat());
+  g.dV.assign(nI + F * nIf, 0.0);
+  for (int q = 0; q < nI; ++q) {
+    Mat J(d, d);
+    for (int i = 0; i < N; ++i)
+      for (int r = 0; r < d; ++r)
+        for (int s = 0; s < d; ++s) J(r, s) += re->dphi[q][i][r] * g.X[i][s];
+    g.dV[q] = re->ipW[q] * det_small(J);
+    g.invJ[q] = inverse(J);
+  }
+  g.normals.assign(F * nIf, std::vector<double>(d));
+  for (int f = 0; f < F; ++f) {
+    int v0 = re->faceNodes[f][0], vn = -1;
+    for (int k = 0; k < N; ++k)
+      if (std::find(re->faceNodes[f].begin(), re->faceNodes[f].end(), k) == re->faceNodes[f].end()) {
+        vn = k;
+        break;
+      }
+    std::vector<double> test(d);
+    for (int k = 0; k < d; ++k) test[k] = g.X[vn][k] - g.X[v0][k];
+    for (int q = 0; q < nIf; ++q) {
+      Mat J(d - 1, d);
+      for (int i = 0; i < Nf; ++i)
+        for (int r = 0; r < d - 1; ++r)
+          for (int s = 0; s < d; ++s) J(r, s) += fe->dphi[q][i][r] * g.X[re->faceNodes[f][i]][s];
+      Mat JJt(d - 1, d - 1);
+      for (int a = 0; a < d - 1; ++a)
+        for (int b = 0; b < d - 1; ++b)
+          for (int s = 0; s < d; ++s) JJt(a, b) += J(a, s) * J(b, s);
+      g.dV[nI + f * nIf + q] = fe->ipW[q] * std::sqrt(det_small(JJt));
+      std::vector<double> nv(d);
+      if (d == 2) {
+        nv[0] = -J(0, 1);
+        nv[1] = J(0, 0);
+      } else {
+        nv[0] = J(0, 1) * J(1, 2) - J(0, 2) * J(1, 1);
+        nv[1] = J(0, 2) * J(1, 0) - J(0, 0) * J(1, 2);
+        nv[2] = J(0, 0) * J(1, 1) - J(0, 1) * J(1, 0);
+      }
+      double nrm = 0.0;
+      for (double v : nv) nrm += v * v;
+      nrm = std::sqrt(nrm);
+      double prod = 0.0;
+      for (int k = 0; k < d; ++k) {
+        nv[k] /= nrm;
+        prod += test[k] * nv[k];
+      }
+      if (prod > 0)
+        for (int k = 0; k < d; ++k) nv[k] = -nv[k];
+      g.normals[f * nIf + q] = nv;
+    }
+  }
+}
+
+// HDGBase::assemble with nd unknowns per node (HDGBase.cpp:67-158); tauIP holds the
+// nd x nd tau (column-major) at every face integration point (HDGBase::setTau,
+// HDGBase.cpp:18-32).
+static void base_nd(const RefEl* re, int nd, const std::vector<double>& dV, const std::vector<Mat>& invJ,
+                    const std::vector<std::vector<double>>& normals, const std::vector<double>& tauIP, Mat& op) {
+  const RefEl* fe = re->face;
+  int d = re->dim, N = re->nNodes, F = re->nFaces, Nf = fe->nNodes, nI = re->nIP, nIf = fe->nIP;
+  int sQ = N * nd, sL = N * (d + 1) * nd, n = sL + F * Nf * nd, st = nd * nd;
+  op = Mat(n, n);
+  for (int q = 0; q < nIf; ++q) {
+    const auto& sh = fe->phi[q];
+    for (int f = 0; f < F; ++f) {
+      int off = f * nIf + q;
+      const auto& fn = re->faceNodes[f];
+      double ds = dV[nI + off];
+      for (int iN = 0; iN < Nf; ++iN)
+        for (int c = 0; c < nd; ++c)
+          for (int jN = 0; jN < Nf; ++jN) {
+            double ss = sh[iN] * sh[jN];
+            for (int m = 0; m < nd; ++m) {
+              double val = ds * tauIP[(size_t)off * st + m * nd + c] * ss;
+              op(sL + (f * Nf + iN) * nd + c, sL + (f * Nf + jN) * nd + m) -= val;
+              op(sL + (f * Nf + iN) * nd + c, fn[jN] * nd + m) += val;
+              op(fn[iN] * nd + c, fn[jN] * nd + m) += val;
+              op(fn[iN] * nd + c, sL + (f * Nf + jN) * nd + m) -= val;
+            }
+            for (int k = 0; k < d; ++k)
+              op(sQ + (fn[iN] * d + k) * nd + c, sL + (f * Nf + jN) * nd + c) -= ds * normals[off][k] * ss;
+          }
+    }
+  }
+  for (int q = 0; q < nI; ++q) {
+    const auto& sh = re->phi[q];
+    for (int iN = 0; iN < N; ++iN) {
+      std::vector<double> vm(d, 0.0);
+      for (int a = 0; a < d; ++a) {
+        for (int b = 0; b < d; ++b) vm[a] += invJ[q](a, b) * re->dphi[q][iN][b];
+        vm[a] *= dV[q];
+      }
+      for (int k = 0; k < d; ++k)
+        for (int c = 0; c < nd; ++c)
+          for (int jN = 0; jN < N; ++jN) {
+            op(sQ + (iN * d + k) * nd + c, jN * nd + c) += vm[k] * sh[jN];
+            op(sQ + (iN * d + k) * nd + c, sQ + (jN * d + k) * nd + c) += dV[q] * sh[iN] * sh[jN];
+          }
+    }
+  }
+}
+
+// HDGDiffusion::assemble with nd unknowns per node (HDGDiffusion.cpp:74-145); Ds =
+// the d x d tensor (column-major) at the volume then the face integration points
+// (HDGDiffusion::setDiffusionTensor, HDGDiffusion.cpp:31-72).
+static void diffusion_nd(const RefEl* re, int nd, const std::vector<double>& dV, const std::vector<Mat>& invJ,
+                         const std::vector<std::vector<double>>& normals, const std::vector<Mat>& Ds, Mat& op) {
+  const RefEl* fe = re->face;
+  int d = re->dim, N = re->nNodes, F = re->nFaces, Nf = fe->nNodes, nI = re->nIP, nIf = fe->nIP;
+  int lenU = N * nd, lenQ = d * lenU, n = lenU + lenQ + F * Nf * nd;
+  op = Mat(n, n);
+  for (int f = 0; f < F; ++f) {
+    const auto& fn = re->faceNodes[f];
+    for (int q = 0; q < nIf; ++q) {
+      const auto& sh = fe->phi[q];
+      int off = f * nIf + q;
+      std::vector<double> bv(d, 0.0);
+      for (int a = 0; a < d; ++a) {
+        for (int b = 0; b < d; ++b) bv[a] += Ds[nI + off](a, b) * normals[off][b];
+        bv[a] *= dV[nI + off];
+      }
+      for (int iN = 0; iN < Nf; ++iN)
+        for (int c = 0; c < nd; ++c)
+          for (int jN = 0; jN < Nf; ++jN)
+            for (int k = 0; k < d; ++k) {
+              double v = bv[k] * sh[iN] * sh[jN];
+              op(lenU + lenQ + (f * Nf + iN) * nd + c, lenU + (fn[jN] * d + k) * nd + c) -= v;
+              op(fn[iN] * nd + c, lenU + (fn[jN] * d + k) * nd + c) -= v;
+            }
+    }
+  }
+  for (int q = 0; q < nI; ++q) {
+    const auto& sh = re->phi[q];
+    for (int iN = 0; iN < N; ++iN) {
+      std::vector<double> g(d, 0.0), bv(d, 0.0);
+      for (int a = 0; a < d; ++a)
+        for (int b = 0; b < d; ++b) g[a] += invJ[q](a, b) * re->dphi[q][iN][b];
+      for (int a = 0; a < d; ++a) {
+        for (int b = 0; b < d; ++b) bv[a] += Ds[q](a, b) * g[b];
+        bv[a] *= dV[q];
+      }
+      for (int c = 0; c < nd; ++c)
+        for (int jN = 0; jN < N; ++jN)
+          for (int k = 0; k < d; ++k) op(iN * nd + c, lenU + (jN * d + k) * nd + c) += bv[k] * sh[jN];
+    }
+  }
+}
+
+// HDGUNabU (HDGUNabU.cpp:27-193): the u.grad(u) term linearised about the nodal
+// solution sol[N][nd] and the local-order trace tr[F*Nf][nd]; face terms into the L
+// rows, those rows summed into the U rows of their face nodes, volume terms into the
+// U-U block, RHS = op [u; 0; t] / 2 on the U and L rows.
+static void unabu_nd(const RefEl* re, int nd, const std::vector<double>& dV, const std::vector<Mat>& invJ,
+                     const std::vector<std::vector<double>>& normals, const std::vector<double>& sol,
+                     const std::vector<double>& tr, Mat& op, std::vector<double>& rhs) {
+  const RefEl* fe = re->face;
+  int d = re->dim, N = re->nNodes, F = re->nFaces, Nf = fe->nNodes, nI = re->nIP, nIf = fe->nIP;
+  int lenU = N * nd, sL = N * (d + 1) * nd, lenL = F * Nf * nd, n = sL + lenL;
+  op = Mat(n, n);
+  // setSolution / setTrace (HDGUNabU.cpp:27-99): values at the integration points
+  std::vector<double> sols((size_t)nI * nd, 0.0), fsols((size_t)F * nIf * nd, 0.0), trs((size_t)F * nIf * nd, 0.0);
+  for (int q = 0; q < nI; ++q)
+    for (int i = 0; i < N; ++i)
+      for (int c = 0; c < nd; ++c) sols[q * nd + c] += re->phi[q][i] * sol[i * nd + c];
+  for (int f = 0; f < F; ++f)
+    for (int q = 0; q < nIf; ++q)
+      for (int a = 0; a < Nf; ++a)
+        for (int c = 0; c < nd; ++c) {
+          fsols[(f * nIf + q) * nd + c] += fe->phi[q][a] * sol[re->faceNodes[f][a] * nd + c];
+          trs[(f * nIf + q) * nd + c] += fe->phi[q][a] * tr[(f * Nf + a) * nd + c];
+        }
+  // face integrals (HDGUNabU.cpp:126-145)
+  for (int f = 0; f < F; ++f)
+    for (int q = 0; q < nIf; ++q) {
+      const auto& sh = fe->phi[q];
+      int off = f * nIf + q;
+      double ds = dV[nI + off], tn = 0.0;
+      for (int k = 0; k < d; ++k) tn += trs[off * nd + k] * normals[off][k];
+      tn *= ds;
+      for (int iN = 0; iN < Nf; ++iN)
+        for (int c = 0; c < nd; ++c)
+          for (int jN = 0; jN < Nf; ++jN) {
+            op(sL + (f * Nf + iN) * nd + c, sL + (f * Nf + jN) * nd + c) += tn * sh[jN] * sh[iN];
+            for (int m = 0; m < nd; ++m)
+              op(sL + (f * Nf + iN) * nd + c, sL + (f * Nf + jN) * nd + m) +=
+                  fsols[off * nd + c] * sh[jN] * sh[iN] * normals[off][m] * ds;
+          }
+    }
+  // face rows summed into the U rows of the face's nodes (HDGUNabU.cpp:147-152)
+  for (int f = 0; f < F; ++f)
+    for (int iN = 0; iN < Nf; ++iN)
+      for (int c = 0; c < nd; ++c)
+        for (int j = 0; j < lenL; ++j)
+          op(re->faceNodes[f][iN] * nd + c, sL + j) += op(sL + (f * Nf + iN) * nd + c, sL + j);
+  // volume integrals (HDGUNabU.cpp:153-177)
+  for (int q = 0; q < nI; ++q) {
+    const auto& sh = re->phi[q];
+    std::vector<double> G((size_t)N * d, 0.0);
+    for (int i = 0; i < N; ++i)
+      for (int a = 0; a < d; ++a)
+        for (int b = 0; b < d; ++b) G[i * d + a] += invJ[q](a, b) * re->dphi[q][i][b];
+    double divSol = 0.0;  // trace of sum_i grad(phi_i) u_i^T (needs nd == d)
+    for (int i = 0; i < N; ++i)
+      for (int k = 0; k < d; ++k) divSol += G[i * d + k] * sol[i * nd + k];
+    for (int iN = 0; iN < N; ++iN) {
+      double sg = 0.0;
+      for (int k = 0; k < d; ++k) sg += sols[q * nd + k] * G[iN * d + k];
+      for (int c = 0; c < nd; ++c)
+        for (int jN = 0; jN < N; ++jN) {
+          op(iN * nd + c, jN * nd + c) -= (divSol * sh[iN] + sg) * dV[q] * sh[jN];
+          for (int m = 0; m < nd; ++m)
+            op(iN * nd + c, jN * nd + m) -=
+                sols[q * nd + c] * (G[jN * d + m] * sh[iN] + G[iN * d + m] * sh[jN]) * dV[q];
+        }
+    }
+  }
+  // RHS (HDGUNabU.cpp:178-190)
+  rhs.assign(n, 0.0);
+  for (int i = 0; i < lenU; ++i) {
+    double s = 0.0;
+    for (int j = 0; j < lenU; ++j) s += op(i, j) * sol[j] / 2.0;
+    for (int j = 0; j < lenL; ++j) s += op(i, sL + j) * tr[j] / 2.0;
+    rhs[i] += s;
+  }
+  for (int i = 0; i < lenL; ++i) {
+    double s = 0.0;
+    for (int j = 0; j < lenU; ++j) s += op(sL + i, j) * sol[j] / 2.0;
+    for (int j = 0; j < lenL; ++j) s += op(sL + i, sL + j) * tr[j] / 2.0;
+    rhs[sL + i] += s;
+  }
+}
+
+// HDGBurgersModel::computeLocalMatrix / computeLocalRHS (HDGBurgersModel.cpp:93-125)
+// for one element of the mesh, then HDGModel::compute's time scheme (HDGModel.cpp:35-51).
+static void burgers_local_system(const Problem& P, const BurgersFields& B, int iEl, Mat& A,
+                                 std::vector<double>& rhs) {
+  const RefEl* re = P.re;
+  const RefEl* fe = re->face;
+  int d = P.dim, nd = d, N = re->nNodes, F = re->nFaces, Nf = fe->nNodes, nI = re->nIP, nIf = fe->nIP;
+  int lenU = N * nd, st = nd * nd, n = P.nloc;
+  ElemGeo g;
+  element_geometry(P, iEl, g);
+  // local fields (HDGSolver.cpp:276-326): tau side select, face fields in local order
+  std::vector<double> tauLoc((size_t)F * Nf * st), trLoc((size_t)F * Nf * nd);
+  for (int i = 0; i < F; ++i) {
+    int f = g.facesIn[i];
+    int side = (P.mf.face2cell[2 * f] == iEl) ? 0 : 1;
+    for (int j = 0; j < Nf; ++j) {
+      int qn = g.f2c[i * Nf + j];
+      for (int v = 0; v < st; ++v)
+        tauLoc[(i * Nf + j) * st + v] = B.tau[(((size_t)f * Nf + qn) * B.tauSides + (B.tauSides == 2 ? side : 0)) * st + v];
+      for (int c = 0; c < nd; ++c) trLoc[(i * Nf + j) * nd + c] = B.trace[((size_t)f * Nf + qn) * nd + c];
+    }
+  }
+  std::vector<double> tauIP((size_t)F * nIf * st, 0.0);
+  for (int f = 0; f < F; ++f)
+    for (int q = 0; q < nIf; ++q)
+      for (int a = 0; a < Nf; ++a)
+        for (int v = 0; v < st; ++v) tauIP[(f * nIf + q) * st + v] += tauLoc[(f * Nf + a) * st + v] * fe->phi[q][a];
+  std::vector<double> sol(B.buf.begin() + (size_t)iEl * lenU, B.buf.begin() + (size_t)(iEl + 1) * lenU);
+  Mat Ab, Ac, Ad;
+  std::vector<double> rc;
+  base_nd(re, nd, g.dV, g.invJ, g.normals, tauIP, Ab);
+  unabu_nd(re, nd, g.dV, g.invJ, g.normals, sol, trLoc, Ac, rc);
+  A = Mat(n, n);
+  for (size_t i = 0; i < A.a.size(); ++i) A.a[i] = Ab.a[i] + Ac.a[i];
+  if (B.kc != 0) {
+    // parseDiffusionVals (HDGBurgersModel.cpp:128-150): scalar times identity or a d x d tensor
+    std::vector<Mat> Dn(N, Mat(d, d));
+    for (int i = 0; i < N; ++i) {
+      if (B.kc == 1)
+        for (int k = 0; k < d; ++k) Dn[i](k, k) = B.nu[(size_t)iEl * N + i];
+      else
+        for (int a = 0; a < d * d; ++a) Dn[i].a[a] = B.nu[((size_t)iEl * N + i) * d * d + a];
+    }
+    std::vector<Mat> Ds(nI + F * nIf, Mat(d, d));
+    for (int q = 0; q < nI; ++q)
+      for (int a = 0; a < d * d; ++a) {
+        double s = 0.0;
+        for (int i = 0; i < N; ++i) s += re->phi[q][i] * Dn[i].a[a];
+        Ds[q].a[a] = s;
+      }
+    for (int f = 0; f < F; ++f)
+      for (int q = 0; q < nIf; ++q)
+        for (int a = 0; a < d * d; ++a) {
+          double s = 0.0;
+          for (int i = 0; i < Nf; ++i) s += fe->phi[q][i] * Dn[re->faceNodes[f][i]].a[a];
+          Ds[nI + f * nIf + q].a[a] = s;
+        }
+    diffusion_nd(re, nd, g.dV, g.invJ, g.normals, Ds, Ad);
+    for (size_t i = 0; i < A.a.size(); ++i) A.a[i] += Ad.a[i];
+  }
+  rhs = rc;
+  if (!B.src.empty()) {
+    // one scalar Source per component (Source.cpp:24-48, HDGBurgersModel.cpp:114-123)
+    for (int c = 0; c < nd; ++c)
+      for (int q = 0; q < nI; ++q) {
+        double lm = B.src[((size_t)iEl * nI + q) * nd + c] * g.dV[q];
+        for (int i = 0; i < N; ++i) rhs[i * nd + c] += re->phi[q][i] * lm;
+      }
+  }
+  if (B.dt > 0.0) {
+    // Euler::apply (Euler.cpp:18-34), implicit: U rows times dt, plus M (x) I_nd
+    Mat M(N, N);
+    for (int q = 0; q < nI; ++q)
+      for (int i = 0; i < N; ++i)
+        for (int j = i; j < N; ++j) M(i, j) += re->phi[q][i] * re->phi[q][j] * g.dV[q];
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < i; ++j) M(i, j) = M(j, i);
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < lenU; ++i) A(i, j) *= B.dt;
+    for (int i = 0; i < lenU; ++i) rhs[i] *= B.dt;
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < N; ++j)
+        for (int c = 0; c < nd; ++c) {
+          A(i * nd + c, j * nd + c) += M(i, j);
+          rhs[i * nd + c] += M(i, j) * B.old[(size_t)iEl * lenU + j * nd + c];
+        }
+  }
+}
+
+// Dirichlet Set on the boundary faces with nd values per node (HDGSolver.cpp:361-529,
+// DirichletModel.cpp:19-44): the model's identity and its face-ordered values are
+// added to the element's local face rows as they are, without the face2CellMap
+// permutation (HDGSolver.cpp:493-497), as apply_dirichlet above.
+static void apply_dirichlet_nd(Problem& P, int nd, const std::vector<double>& dir) {
+  int F = P.re->nFaces, Nf = P.re->face->nNodes, lenL = P.lenL, lenT = Nf * nd;
+  for (int f : P.mf.boundary) {
+    int c = P.mf.face2cell[2 * f];
+    int loc = 0;
+    while (P.mf.cell2face[(size_t)c * F + loc] != f) ++loc;
+    double* S = &P.S[(size_t)c * lenL * lenL];
+    double* S0 = &P.S0[(size_t)c * lenL];
+    for (int i = 0; i < lenT; ++i) {
+      int row = loc * lenT + i;
+      for (int j = 0; j < lenL; ++j) S[row + (size_t)j * lenL] = 0.0;
+      S0[row] = 0.0;
+    }
+    for (int i = 0; i < lenT; ++i) {
+      int row = loc * lenT + i;
+      S[row + (size_t)row * lenL] += 1.0;
+      S0[row] += dir[(size_t)f * lenT + i];
+    }
+  }
+}
+
+// Global trace index (faceID*Nf + face2CellMap)*nd + k (HDGSolver.cpp:589-598) and
+// the AIJ pattern with every entry of every element block kept.
+static void build_csr_nd(Problem& P, int nd) {
+  int F = P.re->nFaces, Nf = P.re->face->nNodes, N = P.re->nNodes, lenL = P.lenL, B = Nf * nd;
+  int ndofs = P.mf.nFaces * B;
+  std::vector<std::set<int>> faceNbr(P.mf.nFaces);
+  for (int c = 0; c < P.nCells; ++c)
+    for (int i = 0; i < F; ++i)
+      for (int j = 0; j < F; ++j) faceNbr[P.mf.cell2face[(size_t)c * F + i]].insert(P.mf.cell2face[(size_t)c * F + j]);
+  P.rowptr.assign(ndofs + 1, 0);
+  for (int f = 0; f < P.mf.nFaces; ++f)
+    for (int a = 0; a < B; ++a) P.rowptr[f * B + a + 1] = (int)faceNbr[f].size() * B;
+  for (int r = 0; r < ndofs; ++r) P.rowptr[r + 1] += P.rowptr[r];
+  P.col.assign(P.rowptr[ndofs], 0);
+  for (int f = 0; f < P.mf.nFaces; ++f)
+    for (int a = 0; a < B; ++a) {
+      int k = P.rowptr[f * B + a];
+      for (int g : faceNbr[f])
+        for (int b = 0; b < B; ++b) P.col[k++] = g * B + b;
+    }
+  P.val.assign(P.col.size(), 0.0);
+  P.rhs.assign(ndofs, 0.0);
+  std::vector<int> rc(lenL);
+  for (int c = 0; c < P.nCells; ++c) {
+    const int* cell = &P.cells[(size_t)c * N];
+    for (int i = 0; i < F; ++i) {
+      int f = P.mf.cell2face[(size_t)c * F + i];
+      const int* face = &P.mf.faces[(size_t)f * Nf];
+      for (int j = 0; j < Nf; ++j) {
+        int node = cell[P.re->faceNodes[i][j]], pos = 0;
+        while (face[pos] != node) ++pos;
+        for (int k = 0; k < nd; ++k) rc[(i * Nf + j) * nd + k] = (f * Nf + pos) * nd + k;
+      }
+    }
+    const double* S = &P.S[(size_t)c * lenL * lenL];
+    for (int i = 0; i < lenL; ++i) {
+      int row = rc[i];
+      int* cb = &P.col[P.rowptr[row]];
+      int len = P.rowptr[row + 1] - P.rowptr[row];
+      for (int j = 0; j < lenL; ++j) {
+        int k = (int)(std::lower_bound(cb, cb + len, rc[j]) - cb);
+        P.val[P.rowptr[row] + k] += S[i + (size_t)j * lenL];
+      }
+      P.rhs[row] += P.S0[(size_t)c * lenL + i];
+    }
+  }
+}
+
+// Local recovery (HDGSolver.cpp:741-775) with nd values per trace node.
+static void recover_nd(const Problem& P, int nd, const double* trace, double* sol, double* flux) {
+  int F = P.re->nFaces, Nf = P.re->face->nNodes, N = P.re->nNodes;
+  int lenU = P.lenU, lenQ = P.lenQ, lenL = P.lenL;
+  std::vector<double> lam(lenL);
+  for (int c = 0; c < P.nCells; ++c) {
+    const int* cell = &P.cells[(size_t)c * N];
+    for (int i = 0; i < F; ++i) {
+      int f = P.mf.cell2face[(size_t)c * F + i];
+      const int* face = &P.mf.faces[(size_t)f * Nf];
+      for (int j = 0; j < Nf; ++j) {
+        int node = cell[P.re->faceNodes[i][j]], pos = 0;
+        while (face[pos] != node) ++pos;
+        for (int k = 0; k < nd; ++k) lam[(i * Nf + j) * nd + k] = trace[((size_t)f * Nf + pos) * nd + k];
+      }
+    }
+    const double* U = &P.U[(size_t)c * lenU * lenL];
+    const double* Q = &P.Q[(size_t)c * lenQ * lenL];
+    for (int i = 0; i < lenU; ++i) {
+      double s = 0.0;
+      for (int j = 0; j < lenL; ++j) s += U[i + (size_t)j * lenU] * lam[j];
+      sol[(size_t)c * lenU + i] = s + P.U0[(size_t)c * lenU + i];
+    }
+    for (int i = 0; i < lenQ; ++i) {
+      double s = 0.0;
+      for (int j = 0; j < lenL; ++j) s += Q[i + (size_t)j * lenQ] * lam[j];
+      flux[(size_t)c * lenQ + i] = s + P.Q0[(size_t)c * lenQ + i];
+    }
+  }
+}
+
 }  // namespace orc
 
 using namespace orc;
@@ -1576,6 +2055,157 @@ int orc_problem_timings(void* h, double* out) {
   out[3] = P->t_solve;
   out[4] = P->t_recover;
   return 0;
+}
+
+// ---------------------------------------------------------------- Burgers
+// A problem with nd = dim unknowns per node (HDGBurgersModel.cpp:35-60). Defaults:
+// tau = identity, no diffusion, no source, Dirichlet 0, stationary, buffer and trace 0.
+void* orc_burgers_create(int dim, int order, int nNodes, const double* coords, int nCells, const int* cells) {
+  Problem* P = (Problem*)orc_problem_create(dim, order, nNodes, coords, nCells, cells);
+  if (!P) return nullptr;
+  const int nd = dim, N = P->re->nNodes, F = P->re->nFaces, Nf = P->re->face->nNodes;
+  P->lenU = N * nd;
+  P->lenQ = dim * N * nd;
+  P->lenL = F * Nf * nd;
+  P->nloc = P->lenU + P->lenQ + P->lenL;
+  BurgersFields& B = g_burgers[P];
+  B.tau.assign((size_t)P->mf.nFaces * Nf * nd * nd, 0.0);
+  for (size_t k = 0; k < (size_t)P->mf.nFaces * Nf; ++k)
+    for (int c = 0; c < nd; ++c) B.tau[k * nd * nd + c * nd + c] = 1.0;
+  B.dir.assign((size_t)P->mf.nFaces * Nf * nd, 0.0);
+  B.buf.assign((size_t)nCells * N * nd, 0.0);
+  B.trace.assign((size_t)P->mf.nFaces * Nf * nd, 0.0);
+  return P;
+}
+
+void orc_burgers_destroy(void* h) {
+  g_burgers.erase((Problem*)h);
+  delete (Problem*)h;
+}
+
+// tau [nFaces][Nf][sides][nd*nd]; nu [nCells][N][kc] (kc 0, 1 or d*d); src
+// [nCells][nI][nd] or null; dir [nFaces][Nf][nd]; dt > 0: implicit Euler on
+// old [nCells][N*nd].
+int orc_burgers_set_fields(void* h, const double* tau, int tauSides, const double* nu, int kc, const double* src,
+                           const double* dir, double dt, const double* old) {
+  ORC_TRY({
+    Problem* P = (Problem*)h;
+    BurgersFields& B = g_burgers.at(P);
+    const int nd = P->dim, N = P->re->nNodes, Nf = P->re->face->nNodes;
+    if (tau) {
+      B.tauSides = tauSides;
+      B.tau.assign(tau, tau + (size_t)P->mf.nFaces * Nf * tauSides * nd * nd);
+    }
+    B.kc = kc;
+    B.nu.assign(nu, nu + (kc ? (size_t)P->nCells * N * kc : 0));
+    B.src.assign(src, src + (src ? (size_t)P->nCells * P->re->nIP * nd : 0));
+    if (dir) B.dir.assign(dir, dir + (size_t)P->mf.nFaces * Nf * nd);
+    B.dt = dt;
+    B.old.assign(old, old + (dt > 0.0 ? (size_t)P->nCells * N * nd : 0));
+  })
+}
+
+// BufferSolution [nCells][N*nd] and Trace [nFaces][Nf*nd] the operator is linearised about.
+int orc_burgers_set_state(void* h, const double* buf, const double* trace) {
+  ORC_TRY({
+    Problem* P = (Problem*)h;
+    BurgersFields& B = g_burgers.at(P);
+    if (buf) std::copy(buf, buf + B.buf.size(), B.buf.begin());
+    if (trace) std::copy(trace, trace + B.trace.size(), B.trace.begin());
+  })
+}
+
+int orc_burgers_local_matrix(void* h, int iEl, double* A, double* rhs) {
+  ORC_TRY({
+    Problem* P = (Problem*)h;
+    Mat M;
+    std::vector<double> r;
+    burgers_local_system(*P, g_burgers.at(P), iEl, M, r);
+    std::copy(M.a.begin(), M.a.end(), A);
+    std::copy(r.begin(), r.end(), rhs);
+  })
+}
+
+// HDGSolver::assemble (HDGSolver.cpp:166-174) with the Burgers model: local systems,
+// condensation, Dirichlet Set, CSR.
+int orc_burgers_assemble(void* h, int nthreads) {
+  ORC_TRY({
+    Problem* P = (Problem*)h;
+    const BurgersFields& B = g_burgers.at(P);
+    P->S.assign((size_t)P->nCells * P->lenL * P->lenL, 0.0);
+    P->S0.assign((size_t)P->nCells * P->lenL, 0.0);
+    P->U.assign((size_t)P->nCells * P->lenU * P->lenL, 0.0);
+    P->Q.assign((size_t)P->nCells * P->lenQ * P->lenL, 0.0);
+    P->U0.assign((size_t)P->nCells * P->lenU, 0.0);
+    P->Q0.assign((size_t)P->nCells * P->lenQ, 0.0);
+    P->solverType = 0;
+    double t0 = now();
+    parallel_for(P->nCells, nthreads, [&](int iEl) {
+      Mat A;
+      std::vector<double> r;
+      burgers_local_system(*P, B, iEl, A, r);
+      condense(*P, iEl, A, r);
+    });
+    double t1 = now();
+    apply_dirichlet_nd(*P, P->dim, B.dir);
+    build_csr_nd(*P, P->dim);
+    P->t_local = t1 - t0;
+    P->t_scatter = now() - t1;
+  })
+}
+
+int orc_burgers_recover(void* h, const double* trace, double* sol, double* flux) {
+  ORC_TRY({
+    Problem* P = (Problem*)h;
+    recover_nd(*P, P->dim, trace, sol, flux);
+  })
+}
+
+// HDGUNabU assembled on the reference element the way its unit test sets it up
+// (TestHDGUNabU.cpp:36-66): identity volume Jacobians with dV = the cubature weights,
+// face measures from the face Jacobians of the reference faces, the reference normals
+// (TestUtils.h getRefNormals). sol [N][nd], trace [F*Nf][nd] (nd = dim); op n x n
+// column-major, rhs n.
+int orc_unabu_refel(int dim, int order, const double* sol, const double* trace, double* op, double* rhs) {
+  ORC_TRY({
+    RefEl* re = get_refel(dim, order);
+    const RefEl* fe = re->face;
+    int nI = re->nIP, nIf = fe->nIP, F = re->nFaces, Nf = fe->nNodes, nd = dim;
+    std::vector<double> dV(nI + F * nIf, 0.0);
+    std::vector<Mat> invJ(nI, Mat(dim, dim));
+    for (int q = 0; q < nI; ++q) {
+      dV[q] = re->ipW[q];
+      for (int k = 0; k < dim; ++k) invJ[q](k, k) = 1.0;
+    }
+    for (int f = 0; f < F; ++f)
+      for (int q = 0; q < nIf; ++q) {
+        Mat J(dim - 1, dim);
+        for (int i = 0; i < Nf; ++i)
+          for (int r = 0; r < dim - 1; ++r)
+            for (int s = 0; s < dim; ++s) J(r, s) += fe->dphi[q][i][r] * re->nodes[re->faceNodes[f][i]][s];
+        Mat JJt(dim - 1, dim - 1);
+        for (int a = 0; a < dim - 1; ++a)
+          for (int b = 0; b < dim - 1; ++b)
+            for (int s = 0; s < dim; ++s) JJt(a, b) += J(a, s) * J(b, s);
+        dV[nI + f * nIf + q] = fe->ipW[q] * std::sqrt(det_small(JJt));
+      }
+    std::vector<std::vector<double>> refN;
+    if (dim == 2) {
+      refN = {{0, -1}, {1.0 / std::sqrt(2.0), 1.0 / std::sqrt(2.0)}, {-1, 0}};
+    } else {
+      double s3 = 1.0 / std::sqrt(3.0);
+      refN = {{0, -1, 0}, {s3, s3, s3}, {-1, 0, 0}, {0, 0, -1}};
+    }
+    std::vector<std::vector<double>> normals(F * nIf);
+    for (int f = 0; f < F; ++f)
+      for (int q = 0; q < nIf; ++q) normals[f * nIf + q] = refN[f];
+    std::vector<double> u(sol, sol + (size_t)re->nNodes * nd), t(trace, trace + (size_t)F * Nf * nd);
+    Mat A;
+    std::vector<double> r;
+    unabu_nd(re, nd, dV, invJ, normals, u, t, A, r);
+    std::copy(A.a.begin(), A.a.end(), op);
+    std::copy(r.begin(), r.end(), rhs);
+  })
 }
 
 }  // extern "C"

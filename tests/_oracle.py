@@ -312,3 +312,140 @@ class RungeKutta:
         for n in self.NAMES:
             fields[n][...] = self.old[n] + sum(bs[k] * self.dt * self.k[n][k] for k in range(self.S))
         self.stage_counter = 0
+
+
+def _burgers_sigs(L):
+    vp, ip, dp = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    if getattr(L, "_burgers_sigs", False):
+        return
+    L.orc_burgers_create.restype = vp
+    L.orc_burgers_create.argtypes = [ip, ip, ip, vp, ip, vp]
+    L.orc_burgers_destroy.argtypes = [vp]
+    L.orc_burgers_set_fields.argtypes = [vp, vp, ip, vp, ip, vp, vp, dp, vp]
+    L.orc_burgers_set_state.argtypes = [vp, vp, vp]
+    L.orc_burgers_local_matrix.argtypes = [vp, ip, vp, vp]
+    L.orc_burgers_assemble.argtypes = [vp, ip]
+    L.orc_burgers_recover.argtypes = [vp] * 4
+    L.orc_unabu_refel.argtypes = [ip, ip, vp, vp, vp, vp]
+    L._burgers_sigs = True
+
+
+def unabu_refel(dim, order, sol, trace):
+    """HDGUNabU on the reference element as TestHDGUNabU.cpp sets it up; returns (op, rhs)."""
+    L = lib()
+    _burgers_sigs(L)
+    re = RefEl(dim, order)
+    N, F, Nf = re.nNodes, re.nFaces, re.nNodesFace
+    n = N * dim * (dim + 1) + F * Nf * dim
+    sol = np.ascontiguousarray(sol, dtype=np.float64).reshape(N * dim)
+    trace = np.ascontiguousarray(trace, dtype=np.float64).reshape(F * Nf * dim)
+    op = np.zeros((n, n), order="F")
+    rhs = np.zeros(n)
+    _check(L.orc_unabu_refel(dim, order, _ptr(sol), _ptr(trace), op.ctypes.data, _ptr(rhs)))
+    return op, rhs
+
+
+class BurgersProblem(Problem):
+    """HDGBurgersModel on the oracle: nd = dim unknowns per node (vector Burgers,
+    HDGBurgersModel.cpp:35-60), the HDGSolver assembly / recovery of the nd-valued
+    trace system, and NonLinearWrapper's loop (newton)."""
+
+    def __init__(self, dim, order, coords, cells):
+        L = lib()
+        _burgers_sigs(L)
+        self.dim, self.order = dim, order
+        self.coords = np.ascontiguousarray(coords, dtype=np.float64)
+        self.cells = np.ascontiguousarray(cells, dtype=np.int32)
+        self.h = L.orc_burgers_create(dim, order, self.coords.shape[0], _ptr(self.coords),
+                                      self.cells.shape[0], _ptr(self.cells))
+        if not self.h:
+            raise RuntimeError("oracle: " + L.orc_last_error().decode())
+        self.re = RefEl(dim, order)
+        c = np.zeros(2, dtype=np.int32)
+        L.orc_problem_face_counts(self.h, _ptr(c))
+        self.nFaces, self.nBoundary = int(c[0]), int(c[1])
+        F, Nf, N = self.re.nFaces, self.re.nNodesFace, self.re.nNodes
+        nC = self.cells.shape[0]
+        self.cell2face = np.zeros((nC, F), dtype=np.int32)
+        self.face2cell = np.zeros((self.nFaces, 2), dtype=np.int32)
+        self.faces = np.zeros((self.nFaces, Nf), dtype=np.int32)
+        self.boundary = np.zeros(self.nBoundary, dtype=np.int32)
+        L.orc_problem_faces(self.h, _ptr(self.cell2face), _ptr(self.face2cell), _ptr(self.faces),
+                            _ptr(self.boundary))
+        self.nCells = nC
+        self.nd = dim
+        self.lenU = N * dim
+        self.lenQ = dim * N * dim
+        self.lenL = F * Nf * dim
+        self.ndofs = self.nFaces * Nf * dim
+        self.buf = np.zeros((nC, self.lenU))
+        self.trace = np.zeros(self.ndofs)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_burgers_destroy(self.h)
+            self.h = None
+
+    def set_fields(self, tau=None, tau_sides=1, nu=None, src=None, dirichlet=None, dt=0.0, old=None):
+        """tau [nFaces][Nf][sides][nd*nd]; nu [nCells][N][kc] with kc 1 or d*d (None: no
+        diffusion operator); src [nCells][nI][nd]; dirichlet [nFaces][Nf][nd]; dt > 0:
+        implicit Euler about old [nCells][N*nd]."""
+        arr = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+        tau, nu, src, dirichlet, old = arr(tau), arr(nu), arr(src), arr(dirichlet), arr(old)
+        kc = 0 if nu is None else nu.size // (self.nCells * self.re.nNodes)
+        self._keep = (tau, nu, src, dirichlet, old)
+        _check(lib().orc_burgers_set_fields(self.h, _ptr(tau), tau_sides, _ptr(nu), kc, _ptr(src),
+                                            _ptr(dirichlet), float(dt), _ptr(old)))
+
+    def set_state(self, buf=None, trace=None):
+        if buf is not None:
+            self.buf = np.ascontiguousarray(buf, dtype=np.float64).reshape(self.nCells, self.lenU).copy()
+        if trace is not None:
+            self.trace = np.ascontiguousarray(trace, dtype=np.float64).reshape(self.ndofs).copy()
+        _check(lib().orc_burgers_set_state(self.h, _ptr(self.buf), _ptr(self.trace)))
+
+    def assemble(self, nthreads=1):
+        _check(lib().orc_burgers_assemble(self.h, nthreads))
+
+    def local_matrix(self, iel):
+        n = self.lenU + self.lenQ + self.lenL
+        A = np.zeros((n, n), order="F")
+        r = np.zeros(n)
+        _check(lib().orc_burgers_local_matrix(self.h, iel, A.ctypes.data, _ptr(r)))
+        return A, r
+
+    def recover(self, trace):
+        trace = np.ascontiguousarray(trace, dtype=np.float64)
+        sol = np.zeros((self.nCells, self.lenU))
+        flux = np.zeros((self.nCells, self.lenQ))
+        _check(lib().orc_burgers_recover(self.h, _ptr(trace), _ptr(sol), _ptr(flux)))
+        return sol, flux
+
+    def linearized_solve(self):
+        """NonLinearWrapper::vanillaLinearizedSolver (NonLinearWrapper.cpp:36-39):
+        assemble about (buf, trace), solve the trace system (direct FP64), recover."""
+        self.set_state(self.buf, self.trace)
+        self.assemble()
+        x = self.solve_direct()
+        sol, flux = self.recover(x)
+        self.trace = x
+        return sol, flux
+
+    def newton(self, res_tol=1e-6, max_iters=20, dampening=0.0):
+        """NonLinearWrapper::solve (NonLinearWrapper.cpp:41-79) on host arrays: the
+        residual is ||sol - buf|| / ||buf|| (||sol - buf|| when buf = 0); while it
+        is above res_tol, both become (1 - d) sol + d buf. Returns (sol, flux,
+        iterations, residual history)."""
+        hist = []
+        sol = flux = None
+        for it in range(max_iters):
+            sol, flux = self.linearized_solve()
+            diff = float(np.sum((sol - self.buf) ** 2))
+            ref = float(np.sum(self.buf ** 2))
+            res = np.sqrt(diff / ref) if ref != 0 else np.sqrt(diff)
+            hist.append(res)
+            if res < res_tol:
+                return sol, flux, it + 1, hist
+            self.buf = (1.0 - dampening) * sol + dampening * self.buf
+            sol = self.buf.copy()
+        return sol, flux, max_iters, hist
