@@ -50,7 +50,14 @@ CONFIGS = {
     "small3d": dict(dim=3, n=12, order=3, desc="3D HDG diffusion-source, 12^3x6 tets, p=3"),
     "mid3d": dict(dim=3, n=20, order=3, desc="3D HDG diffusion-source, 20^3x6 tets (48k), p=3"),
     "cfg5mesh": dict(dim=3, n=60, order=2, desc="3D HDG diffusion-source, 60^3x6 tets (1.296M), p=2"),
+    # viscous Burgers (HDGBurgersModel + HDGUNabU, nd = 2), implicit Euler, Newton every step
+    "cfg4": dict(dim=2, n=180, order=3, burgers=True, nu=1e-2, dt=1e-3, time_steps=200,
+                 desc="2D viscous Burgers HDG, unit square 180x180x2 tris (64,800), p=3, nu=1e-2, "
+                      "implicit Euler dt=1e-3, Newton to 1e-6 every step"),
+    "burgers-small": dict(dim=2, n=48, order=3, burgers=True, nu=1e-2, dt=1e-3, time_steps=20,
+                          desc="2D viscous Burgers HDG, 48x48x2 tris (4,608), p=3, nu=1e-2, dt=1e-3"),
 }
+BURGERS_METRIC = "implicit-Euler Burgers step time (Newton to 1e-6, GMRES 1e-10); elements x steps / s"
 
 
 def peaks():
@@ -371,6 +378,193 @@ def run_ours(args, world, rank, local):
     return res, ctx
 
 
+def burgers_initial(coords, cells, seed=0):
+    """u0 = sin(2 pi x) sin(2 pi y) + N(0, 0.01) (seeded), the same field on both components."""
+    x = coords[cells]
+    u0 = np.sin(2 * np.pi * x[..., 0]) * np.sin(2 * np.pi * x[..., 1])
+    u = np.stack([u0, u0], -1) + np.random.default_rng(seed).normal(0.0, 0.01, size=x.shape)
+    return u.reshape(cells.shape[0], -1)
+
+
+def burgers_flops_per_element(N, NF, F, NI, NIF, D=2):
+    """FP64 operations the Burgers element kernel executes per element (its loops)."""
+    ND, NT = D, D * D
+    NU, NQ, NLF = N * ND, D * N * ND, NF * ND
+    NL = F * NLF
+    W = NU + NL + 1
+    ops = 2 * NI * N * D * D + 2 * NI * N * D * D * (N + 1)            # G, K G
+    ops += F * NIF * (4 * ND * NF + 2 * NT * NF + 2 * D * D * NF + 4 * D)  # face IP values
+    ops += 2 * NI * N * ND + 2 * NI * N * D                              # u, div u at the IPs
+    ops += N * N * NI * (2 + 4 * D)                                      # M, C_k, K'_k
+    ops += F * NF * NF * NIF * (4 * D + 2 * NT)                          # E, H, tau masses
+    ops += F * NLF * NLF * NIF * 6 + NU * NU * NI * 12                  # convection blocks
+    ops += N * (N - 1) * 2 * N * 2 + 2 * D * N * N * N + 2 * D * N * F * NF * NF  # M^-1, M^-1 C, M^-1 E
+    ops += NU * NU * 4 * D * N + NU * NL * 4 * D * N + NU * (2 * NU + 2 * NL)      # [A | -B | Fu]
+    ops += sum(2 * (NU - 1) * (W - k - 1) for k in range(NU))           # Gauss-Jordan
+    ops += NQ * (NL + 1) * 2 * N + NL * (NL + 1) * NF * (2 * ND + 2 * D)  # Q, S
+    return ops
+
+
+def run_burgers(args, world, rank, local):
+    import torch
+    from hyperfox_gb300 import capi
+    torch.cuda.set_device(local)
+    cfg = CONFIGS[args.config]
+    p = cfg["order"]
+    t0 = time.time()
+    coords, cells = make_problem(cfg)
+    ctx = capi.Context(local)
+    ctx.upload_mesh(2, p, coords, cells)
+    B = capi.Burgers(ctx)
+    Nf = ctx.re["nNodesFace"]
+    tau = np.zeros((ctx.nFaces, Nf, 2, 4))
+    tau[..., 0] = tau[..., 3] = 1.0                  # tau = I on both sides (TestHDGBurgers.cpp:290-297)
+    B.set_tau(tau, 2)
+    B.set_diffusion(np.full((coords.shape[0], 1), cfg["nu"]), layout=0)
+    B.set_dirichlet(np.zeros((ctx.nFaces, Nf, 2)))  # u0 vanishes on the boundary
+    B.set_time_step(cfg["dt"])
+    u0 = burgers_initial(coords, cells)
+    t_setup = time.time() - t0
+    L = ctx.L
+    pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    sol_h = pin(u0.shape)
+    sol_h[:] = u0
+
+    def newton(warm):
+        o = capi.newton_opts(res_tol=1e-6, max_iters=20, warm_start=int(warm), lin_rtol=1e-10,
+                             lin_precond=capi.PC_BLOCK_JACOBI, lin_maxits=20000)
+        info = capi.NewtonInfo()
+        ctx._chk(L.hfx_burgers_newton(ctx.h, capi.ctypes.byref(o), capi.ctypes.byref(info)), "burgers_newton")
+        return info
+
+    steps = args.steps if args.steps_given else cfg["time_steps"] - args.warmup
+    warm = not args.cold_start
+    B.set_state(solution=u0, trace=np.zeros(B.ndofs))
+    for _ in range(args.warmup):
+        ctx._chk(L.hfx_burgers_begin_step(ctx.h), "begin_step")
+        newton(warm)
+    barrier(world)
+    ctx._chk(L.hfx_synchronize(ctx.h), "sync")
+    clocks = ClockSampler(local)
+    clocks.start()
+    ctx._chk(L.hfx_profile_enable(ctx.h, 1), "profile")
+    ctx._chk(L.hfx_mark(ctx.h, 0), "mark")
+    its, kits = [], []
+    for _ in range(steps):
+        ctx._chk(L.hfx_burgers_begin_step(ctx.h), "begin_step")
+        info = newton(warm)
+        its.append(info.iterations)
+        kits.append(info.krylov_iterations)
+    ctx._chk(L.hfx_mark(ctx.h, 1), "mark")
+    ms = capi.ctypes.c_double()
+    ctx._chk(L.hfx_elapsed_ms(ctx.h, 0, 1, capi.ctypes.byref(ms)), "elapsed")
+    clk = clocks.stop()
+    dev_ms = barrier_max(world, ms.value)
+    kt = {}
+    for name, kid in (("local", 0), ("scatter", 1), ("spmv64", 2), ("update", 4), ("recover", 5), ("other", 6)):
+        n_l, t_l = capi.ctypes.c_int(), capi.ctypes.c_double()
+        L.hfx_kernel_time(ctx.h, kid, capi.ctypes.byref(n_l), capi.ctypes.byref(t_l))
+        kt[name] = (n_l.value, t_l.value)
+    ctx._chk(L.hfx_profile_enable(ctx.h, 0), "profile")
+    # the Krylov start compared: a few steps from the same state with the other choice
+    sol_keep, _, trace_keep, _ = B.get_state()
+    alt = []
+    for _ in range(5):
+        ctx._chk(L.hfx_burgers_begin_step(ctx.h), "begin_step")
+        alt.append(newton(not warm))
+    B.set_state(solution=sol_keep, trace=trace_keep)
+    # e2e: the step's Solution uploaded from pinned host memory and downloaded after the Newton loop
+    barrier(world)
+    ctx._chk(L.hfx_synchronize(ctx.h), "sync")
+    e2e_steps = min(steps, 20)
+    t1 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ctx._chk(L.hfx_burgers_set_state(ctx.h, capi._p(sol_h), None, None, None), "set_state")
+        ctx._chk(L.hfx_burgers_begin_step(ctx.h), "begin_step")
+        newton(warm)
+        ctx._chk(L.hfx_burgers_get_state(ctx.h, capi._p(sol_h), None, None, None), "get_state")
+    e2e_s = barrier_max(world, time.perf_counter() - t1)
+    E = ctx.nCells
+    step_s = dev_ms / 1e3 / steps
+    re = ctx.re
+    flops = burgers_flops_per_element(re["nNodes"], Nf, re["nFaces"], re["nIP"], re["nIPFace"])
+    avg_ms = kt["local"][1] / max(1, kt["local"][0])
+    tf = flops * E / (avg_ms / 1e3) / 1e12
+    roof = dict(bound="fp64", kernel="burgers_local<2,3> (FP64 assembly + condensation, vector Burgers)",
+                achieved=round(tf, 3), peak=FP64_NOMINAL_TFLOPS, unit="TFLOP/s", frac=round(tf / FP64_NOMINAL_TFLOPS, 4),
+                traffic=args.traffic, flops_per_element=int(flops), avg_launch_ms=round(avg_ms, 4),
+                peak_source="nominal GB300 FP64 (no measured FP64 peak)")
+    nl = sum(its)
+    res = {
+        "metric": BURGERS_METRIC,
+        "value": E * steps / (dev_ms / 1e3),
+        "unit": "elements*steps/s",
+        "n_gpus": world, "steps": steps, "warmup": args.warmup,
+        "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (structured mesh, seeded initial noise N(0, 0.01) on both components)",
+        "config": {"workload": cfg["desc"], "elements": E, "order": p, "trace_dofs": B.ndofs, "csr_nnz": B.nnz,
+                   "krylov": "GMRES(30) + per-face block Jacobi, FP64, rtol 1e-10",
+                   "krylov_start": "previous trace (warm)" if warm else "zero (PETSc default)",
+                   "l2_flush": "none: inputs (element blocks 1.1 GB) exceed L2", "parallelism": "single GPU"},
+        "newton_iterations_per_step": nl / steps,
+        "krylov_iterations_per_newton": sum(kits) / max(1, nl),
+        "other_krylov_start": {"krylov_start": "zero (PETSc default)" if warm else "previous trace (warm)",
+                               "newton_iterations_per_step": sum(a.iterations for a in alt) / len(alt),
+                               "krylov_iterations_per_newton": sum(a.krylov_iterations for a in alt) /
+                               max(1, sum(a.iterations for a in alt)),
+                               "assemble_plus_solve_ms_per_step": sum(a.assemble_ms + a.solve_ms for a in alt) / len(alt)},
+        "element_kernel_elements_per_s": E / (avg_ms / 1e3),
+        "kernel_ms": {k: dict(launches=v[0], total_ms=round(v[1], 3)) for k, v in kt.items()},
+        "roofline": roof,
+        "clocks": clk,
+        "e2e": {"value": E * e2e_steps / e2e_s, "unit": "elements*steps/s", "h2d_bytes_per_step": int(sol_h.nbytes),
+                "d2h_bytes_per_step": int(sol_h.nbytes)},
+        "gpu_launches": int(sum(v[0] for v in kt.values())),
+        "setup_s": t_setup,
+    }
+    return res, ctx
+
+
+def burgers_cpu_sample(cfg_name, nthreads, n=64):
+    """The oracle (HDGBurgersModel restatement, dense LU condensation, GMRES(30)+Jacobi)
+    on a bounded sample: one implicit Euler step of the same physics on an n x n x 2 mesh."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import _oracle as O
+    from hyperfox_gb300 import meshgen
+    cfg = CONFIGS[cfg_name]
+    p = cfg["order"]
+    re = O.RefEl(2, p)
+    v, s = meshgen.square_simplices(n)
+    coords, cells = meshgen.high_order(v, s, re.nodes)
+    P = O.BurgersProblem(2, p, coords, cells)
+    tau = np.zeros((P.nFaces, re.nNodesFace, 2, 4))
+    tau[..., 0] = tau[..., 3] = 1.0
+    u0 = burgers_initial(coords, cells)
+    P.set_fields(tau=tau, tau_sides=2, nu=np.full((P.nCells, re.nNodes, 1), cfg["nu"]),
+                 dirichlet=np.zeros((P.nFaces, re.nNodesFace, 2)), dt=cfg["dt"], old=u0)
+    P.buf, P.trace = u0.copy(), np.zeros(P.ndofs)
+    t0 = time.perf_counter()
+    its = kits = 0
+    for _ in range(20):
+        P.set_state(P.buf, P.trace)
+        P.assemble(nthreads)
+        x, k = P.solve_gmres(1e-10, 200000, nthreads)
+        sol, _ = P.recover(x)
+        P.trace = x
+        its += 1
+        kits += abs(k)
+        diff, ref = float(np.sum((sol - P.buf) ** 2)), float(np.sum(P.buf ** 2))
+        if np.sqrt(diff / ref) < 1e-6:
+            break
+        P.buf = sol
+    dt = time.perf_counter() - t0
+    return dict(value=P.nCells / dt, unit="elements*steps/s", cores=nthreads, kind="port",
+                sample="one implicit Euler step (Newton %d iterations, %d GMRES(30)+Jacobi iterations) on %dx%dx2 "
+                       "tris (%d elements, %d trace DOFs): oracle assemble + LU condense + scatter + solve + recover"
+                       % (its, kits, n, n, P.nCells, P.ndofs), seconds=dt)
+
+
 def cpu_sample(cfg_name, nthreads, rtol, budget_elems=None):
     """Time the CPU oracle on a bounded sample: a sub-cube of the same workload, solved to
     the same relative residual as the GPU arm."""
@@ -401,7 +595,7 @@ def cpu_sample(cfg_name, nthreads, rtol, budget_elems=None):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="cfg2", choices=sorted(CONFIGS))
@@ -426,8 +620,41 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--traffic", type=float, default=None, help="ncu DRAM bytes per launch of the top kernel")
+    ap.add_argument("--cold-start", action="store_true", help="Burgers: start every Krylov solve from zero")
     args = ap.parse_args()
+    args.steps_given = args.steps is not None
+    if args.steps is None:
+        args.steps = 5
     world, rank, local = dist_init()
+    burgers = CONFIGS[args.config].get("burgers", False)
+    if args.impl == "reference" and burgers:
+        if rank != 0:
+            return
+        nthreads = os.cpu_count() or 1
+        vals = []
+        for i in range(args.warmup + args.steps):
+            r = burgers_cpu_sample(args.config, nthreads)
+            if i >= args.warmup:
+                vals.append(r["value"])
+        v = statistics.median(vals)
+        out = {"impl": "reference", "metric": BURGERS_METRIC, "value": v, "unit": "elements*steps/s",
+               "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+               "config": {"workload": CONFIGS[args.config]["desc"]}, "cpu_baseline": dict(r, value=v),
+               "e2e": {"value": v, "unit": "elements*steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(out))
+        return
+    if burgers:
+        res, ctx = run_burgers(args, world, rank, local)
+        if rank == 0:
+            if not args.no_cpu:
+                try:
+                    res["cpu_baseline"] = burgers_cpu_sample(args.config, os.cpu_count() or 1)
+                except Exception as e:  # the baseline is reported, not required
+                    res["cpu_baseline"] = {"error": str(e)}
+            print(json.dumps(res))
+        ctx.close()
+        return
     if args.impl == "reference":
         if rank != 0:
             return

@@ -46,6 +46,10 @@ EXPORTED = [
     "hfx_la_create", "hfx_la_destroy", "hfx_la_allocate", "hfx_la_set_values", "hfx_la_set_rhs",
     "hfx_la_zero_rows", "hfx_la_assemble", "hfx_la_clear", "hfx_la_solve", "hfx_la_nnz",
     "hfx_profile_enable", "hfx_kernel_time", "hfx_mark", "hfx_elapsed_ms", "hfx_synchronize",
+    "hfx_burgers_setup", "hfx_burgers_set_tau", "hfx_burgers_set_diffusion", "hfx_burgers_set_source",
+    "hfx_burgers_set_dirichlet", "hfx_burgers_set_time_step", "hfx_burgers_set_state", "hfx_burgers_get_state",
+    "hfx_burgers_begin_step", "hfx_burgers_assemble", "hfx_burgers_solve", "hfx_newton_opts_default",
+    "hfx_burgers_newton", "hfx_burgers_get_condensed", "hfx_burgers_nnz", "hfx_burgers_get_csr",
     "hfx_trace_solve_noalloc",
 ]
 NOALLOC_MAX_DOFS = 65536
@@ -80,6 +84,17 @@ class TrainInfo(ctypes.Structure):
                 ("accepted", ctypes.c_int), ("loss_chebyshev", ctypes.c_double), ("loss_learned", ctypes.c_double),
                 ("max_poly", ctypes.c_double), ("train_ms", ctypes.c_double), ("loss_first_step", ctypes.c_double),
                 ("lower_steps", ctypes.c_int), ("rejected_steps", ctypes.c_int)]
+
+
+class NewtonOpts(ctypes.Structure):
+    _fields_ = [("res_tol", ctypes.c_double), ("max_iters", ctypes.c_int), ("dampening", ctypes.c_double),
+                ("lin", SolveOpts), ("warm_start", ctypes.c_int)]
+
+
+class NewtonInfo(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("iterations", ctypes.c_int), ("residual", ctypes.c_double),
+                ("krylov_iterations", ctypes.c_int), ("assemble_ms", ctypes.c_double),
+                ("solve_ms", ctypes.c_double), ("recover_ms", ctypes.c_double)]
 
 
 _lib = None
@@ -155,6 +170,22 @@ def load(path=LIB_PATH):
         "hfx_mark": ([vp, ip], ip),
         "hfx_elapsed_ms": ([vp, ip, ip, vp], ip),
         "hfx_synchronize": ([vp], ip),
+        "hfx_burgers_setup": ([vp], ip),
+        "hfx_burgers_set_tau": ([vp, vp, ip], ip),
+        "hfx_burgers_set_diffusion": ([vp, vp, ip, ip], ip),
+        "hfx_burgers_set_source": ([vp, vp], ip),
+        "hfx_burgers_set_dirichlet": ([vp, vp], ip),
+        "hfx_burgers_set_time_step": ([vp, dp], ip),
+        "hfx_burgers_set_state": ([vp, vp, vp, vp, vp], ip),
+        "hfx_burgers_get_state": ([vp, vp, vp, vp, vp], ip),
+        "hfx_burgers_begin_step": ([vp], ip),
+        "hfx_burgers_assemble": ([vp], ip),
+        "hfx_burgers_solve": ([vp, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveInfo)], ip),
+        "hfx_newton_opts_default": ([ctypes.POINTER(NewtonOpts)], None),
+        "hfx_burgers_newton": ([vp, ctypes.POINTER(NewtonOpts), ctypes.POINTER(NewtonInfo)], ip),
+        "hfx_burgers_get_condensed": ([vp] * 7, ip),
+        "hfx_burgers_nnz": ([vp, vp], ip),
+        "hfx_burgers_get_csr": ([vp] * 5, ip),
         "hfx_trace_solve_noalloc": ([ip, ip, ip, vp, vp, vp, vp, vp, vp, dp, ip, vp, ctypes.POINTER(SolveInfo)], ip),
     }
     for name, (args, res) in sig.items():
@@ -599,3 +630,110 @@ class LinearSystem:
         x = np.zeros(self.n)
         self.ctx._chk(self.ctx.L.hfx_la_solve(self.h, ctypes.byref(o), _p(x), ctypes.byref(info)), "la_solve")
         return x, info
+
+
+def newton_opts(**kw):
+    """hfx_newton_opts with the library defaults; lin_* keys set the linear solve's options."""
+    o = NewtonOpts()
+    load().hfx_newton_opts_default(ctypes.byref(o))
+    for k, v in kw.items():
+        if k.startswith("lin_"):
+            setattr(o.lin, k[4:], v)
+        else:
+            setattr(o, k, v)
+    return o
+
+
+class Burgers:
+    """Vector Burgers (HDGBurgersModel + NonLinearWrapper) on a context's mesh:
+    nd = dim unknowns per node, fields and outputs of its own."""
+
+    def __init__(self, ctx):
+        self.c = ctx
+        ctx._chk(ctx.L.hfx_burgers_setup(ctx.h), "burgers_setup")
+        re = ctx.re
+        self.nd = ctx.dim
+        self.NLF = re["nNodesFace"] * self.nd
+        self.lenU = re["nNodes"] * self.nd
+        self.lenQ = ctx.dim * re["nNodes"] * self.nd
+        self.lenL = re["nFaces"] * self.NLF
+        self.ndofs = ctx.nFaces * self.NLF
+        nnz = ctypes.c_int64()
+        ctx._chk(ctx.L.hfx_burgers_nnz(ctx.h, ctypes.byref(nnz)), "burgers_nnz")
+        self.nnz = nnz.value
+        self._keep = {}
+
+    def _arr(self, name, a):
+        a = None if a is None else np.ascontiguousarray(a, np.float64)
+        self._keep[name] = a
+        return a
+
+    def set_tau(self, tau, sides=1):
+        t = self._arr("tau", tau)
+        self.c._chk(self.c.L.hfx_burgers_set_tau(self.c.h, _p(t), sides), "burgers_set_tau")
+
+    def set_diffusion(self, nu, layout=1):
+        if nu is None:
+            self.c._chk(self.c.L.hfx_burgers_set_diffusion(self.c.h, None, 0, 0), "burgers_set_diffusion")
+            return
+        v = self._arr("nu", nu)
+        rows = self.c.nCells * self.c.re["nNodes"] if layout == 1 else v.shape[0]
+        self.c._chk(self.c.L.hfx_burgers_set_diffusion(self.c.h, _p(v), v.size // rows, layout),
+                    "burgers_set_diffusion")
+
+    def set_source(self, values):
+        v = self._arr("src", values)
+        self.c._chk(self.c.L.hfx_burgers_set_source(self.c.h, _p(v)), "burgers_set_source")
+
+    def set_dirichlet(self, values):
+        v = self._arr("dir", values)
+        self.c._chk(self.c.L.hfx_burgers_set_dirichlet(self.c.h, _p(v)), "burgers_set_dirichlet")
+
+    def set_time_step(self, dt):
+        self.c._chk(self.c.L.hfx_burgers_set_time_step(self.c.h, float(dt)), "burgers_set_time_step")
+
+    def set_state(self, solution=None, buffer=None, trace=None, old=None):
+        a = [None if x is None else np.ascontiguousarray(x, np.float64) for x in (solution, buffer, trace, old)]
+        self.c._chk(self.c.L.hfx_burgers_set_state(self.c.h, *[_p(x) for x in a]), "burgers_set_state")
+
+    def get_state(self):
+        E = self.c.nCells
+        sol, flux = np.zeros((E, self.lenU)), np.zeros((E, self.lenQ))
+        trace, buf = np.zeros(self.ndofs), np.zeros((E, self.lenU))
+        self.c._chk(self.c.L.hfx_burgers_get_state(self.c.h, _p(sol), _p(flux), _p(trace), _p(buf)),
+                    "burgers_get_state")
+        return sol, flux, trace, buf
+
+    def begin_step(self):
+        self.c._chk(self.c.L.hfx_burgers_begin_step(self.c.h), "burgers_begin_step")
+
+    def assemble(self):
+        self.c._chk(self.c.L.hfx_burgers_assemble(self.c.h), "burgers_assemble")
+
+    def solve(self, **opts):
+        o = solve_opts(**dict({"method": KSP_GMRES}, **opts))
+        info = SolveInfo()
+        self.c._chk(self.c.L.hfx_burgers_solve(self.c.h, ctypes.byref(o), ctypes.byref(info)), "burgers_solve")
+        return info
+
+    def newton(self, **kw):
+        o = newton_opts(**kw)
+        info = NewtonInfo()
+        self.c._chk(self.c.L.hfx_burgers_newton(self.c.h, ctypes.byref(o), ctypes.byref(info)), "burgers_newton")
+        return info
+
+    def condensed(self):
+        E, U, Q, Ll = self.c.nCells, self.lenU, self.lenQ, self.lenL
+        out = dict(S=np.zeros((E, Ll * Ll)), S0=np.zeros((E, Ll)), U=np.zeros((E, U * Ll)), Q=np.zeros((E, Q * Ll)),
+                   U0=np.zeros((E, U)), Q0=np.zeros((E, Q)))
+        self.c._chk(self.c.L.hfx_burgers_get_condensed(self.c.h, *[_p(out[k]) for k in ("S", "S0", "U", "Q", "U0", "Q0")]),
+                    "burgers_get_condensed")
+        return out
+
+    def csr(self):
+        rowptr = np.zeros(self.ndofs + 1, np.int64)
+        col = np.zeros(self.nnz, np.int32)
+        val = np.zeros(self.nnz)
+        rhs = np.zeros(self.ndofs)
+        self.c._chk(self.c.L.hfx_burgers_get_csr(self.c.h, _p(rowptr), _p(col), _p(val), _p(rhs)), "burgers_get_csr")
+        return rowptr, col, val, rhs

@@ -59,6 +59,41 @@ struct FieldBuf {
   }
 };
 
+// Vector Burgers problem on the context's mesh (hfx_burgers_*): nd = dim unknowns
+// per node, its own fields, element outputs, trace system and Krylov workspace.
+struct BurgersState {
+  bool ready = false, assembled = false, solved = false;
+  int nd = 0, NLF = 0, NU = 0, NQ = 0, NL = 0;
+  int64_t nDofs = 0, nnz = 0;
+  int tauSides = 1, kc = 0, nuLayout = 0;
+  bool haveSrc = false;
+  double dt = 0.0;
+  FieldBuf tau, nu, src, dir;
+  DevMem mem;
+  double *buf = nullptr, *sol = nullptr, *old = nullptr, *flux = nullptr, *trace = nullptr;
+  double *S = nullptr, *S0 = nullptr, *U = nullptr, *Q = nullptr, *U0 = nullptr, *Q0 = nullptr;
+  double *val = nullptr, *rhs = nullptr, *partials = nullptr, *red = nullptr;
+  uint8_t* permx = nullptr;  // face2CellMap at DOF level: [nCells][F][Nf*nd]
+  int* status = nullptr;
+  unsigned* ticket = nullptr;
+  DevMem wsMem;
+  TraceWorkspace ws{};
+  bool wsReady = false;
+  int wsRestart = 0;
+  void release() {
+    wsMem.release();
+    ws = TraceWorkspace{};
+    wsReady = false;
+    wsRestart = 0;
+    mem.release();
+    tau.release();
+    nu.release();
+    src.release();
+    dir.release();
+    ready = assembled = solved = false;
+  }
+};
+
 }  // namespace
 
 struct hfx_ctx {
@@ -144,6 +179,8 @@ struct hfx_ctx {
   DevMem coarseMem;
   bool coarseBuilt = false;
   double coarseTarget = 0.0;
+  // vector Burgers (hfx_burgers_*)
+  BurgersState burgers;
   // timing
   KernelTimer timer;
   cudaEvent_t marks[8] = {};
@@ -283,6 +320,7 @@ int hfx_ctx_destroy(hfx_ctx* c) {
   if (!c) return HFX_OK;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  c->burgers.release();
   c->wsMem.release();
   c->mixMem.release();
   c->outMem.release();
@@ -367,6 +405,7 @@ int hfx_mesh_upload(hfx_ctx* c, int dim, int order, int nNodes, const double* co
   if (!compute_block_pattern(re, nCells, topo, &bp, &err)) return set_err(c, HFX_ERR_ARG, err);
   // release previous state
   free_outputs(c);
+  c->burgers.release();
   c->meshMem.release();
   c->re = std::move(re);
   c->topo = std::move(topo);
@@ -1857,6 +1896,498 @@ int hfx_la_solve(hfx_la* la, const hfx_solve_opts* opts, double* x, hfx_solve_in
     info->coarse_learned = 0;
   }
   if (st != 0) return set_err(la->ctx, st, err);
+  return HFX_OK;
+}
+
+// ---------------------------------------------------------------- Burgers
+// HDGSolver with HDGBurgersModel and NonLinearWrapper (HDGSolver.cpp:81-175,677-779,
+// HDGBurgersModel.cpp:35-125, NonLinearWrapper.cpp:41-79): nd = dim unknowns per node.
+// The trace system is the scalar path's face-block pattern with Nf*nd x Nf*nd blocks:
+// the global DOF (face*Nf + node)*nd + k is face*(Nf*nd) + (node*nd + k).
+
+static int burgers_ready(hfx_ctx* c, const char* who) {
+  if (!c) return HFX_ERR_ARG;
+  if (!c->burgers.ready) return set_err(c, HFX_ERR_STATE, std::string(who) + ": call hfx_burgers_setup first");
+  cudaSetDevice(c->device);
+  return HFX_OK;
+}
+
+int hfx_burgers_setup(hfx_ctx* c) {
+  if (!c) return HFX_ERR_ARG;
+  if (!c->haveMesh) return set_err(c, HFX_ERR_STATE, "burgers_setup: upload a mesh first");
+  if (!burgers_supported(c->dim, c->order))
+    return set_err(c, HFX_ERR_UNSUPPORTED, "burgers_setup: the Burgers element kernel is built for 2D cells, p <= 5");
+  cudaSetDevice(c->device);
+  BurgersState& B = c->burgers;
+  B.release();
+  const int nd = c->dim, N = c->re.nNodes, F = c->re.nFaces, Nf = c->re.nNodesFace;
+  B.nd = nd;
+  B.NLF = Nf * nd;
+  B.NU = N * nd;
+  B.NQ = c->dim * N * nd;
+  B.NL = F * Nf * nd;
+  B.nDofs = (int64_t)c->topo.nFaces * B.NLF;
+  B.nnz = (int64_t)c->bp.col.size() * B.NLF * B.NLF;
+  if (B.NLF > 16) return set_err(c, HFX_ERR_UNSUPPORTED, "burgers_setup: more than 16 trace values per face");
+  const int64_t E = c->nCells;
+  cudaStream_t s = c->stream;
+  DevMem& m = B.mem;
+  HFX_CUDA(c, dalloc(m, &B.buf, (size_t)E * B.NU));
+  HFX_CUDA(c, dalloc(m, &B.sol, (size_t)E * B.NU));
+  HFX_CUDA(c, dalloc(m, &B.old, (size_t)E * B.NU));
+  HFX_CUDA(c, dalloc(m, &B.flux, (size_t)E * B.NQ));
+  HFX_CUDA(c, dalloc(m, &B.trace, (size_t)B.nDofs));
+  HFX_CUDA(c, dalloc(m, &B.S, (size_t)E * B.NL * B.NL));
+  HFX_CUDA(c, dalloc(m, &B.S0, (size_t)E * B.NL));
+  HFX_CUDA(c, dalloc(m, &B.U, (size_t)E * B.NU * B.NL));
+  HFX_CUDA(c, dalloc(m, &B.Q, (size_t)E * B.NQ * B.NL));
+  HFX_CUDA(c, dalloc(m, &B.U0, (size_t)E * B.NU));
+  HFX_CUDA(c, dalloc(m, &B.Q0, (size_t)E * B.NQ));
+  HFX_CUDA(c, dalloc(m, &B.val, (size_t)B.nnz));
+  HFX_CUDA(c, dalloc(m, &B.rhs, (size_t)B.nDofs));
+  HFX_CUDA(c, dalloc(m, &B.partials, newton_partials_needed()));
+  HFX_CUDA(c, dalloc(m, &B.red, 2));
+  HFX_CUDA(c, dalloc(m, &B.status, 1));
+  HFX_CUDA(c, dalloc(m, &B.ticket, 1));
+  HFX_CUDA(c, cudaMemsetAsync(B.ticket, 0, sizeof(unsigned), s));
+  for (double* p : {B.buf, B.sol, B.old})
+    HFX_CUDA(c, cudaMemsetAsync(p, 0, sizeof(double) * E * B.NU, s));
+  HFX_CUDA(c, cudaMemsetAsync(B.flux, 0, sizeof(double) * E * B.NQ, s));
+  HFX_CUDA(c, cudaMemsetAsync(B.trace, 0, sizeof(double) * B.nDofs, s));
+  std::vector<uint8_t> px((size_t)E * F * B.NLF);
+  for (int64_t e = 0; e < E; ++e)
+    for (int f = 0; f < F; ++f)
+      for (int a = 0; a < Nf; ++a)
+        for (int k = 0; k < nd; ++k)
+          px[((size_t)e * F + f) * B.NLF + a * nd + k] = (uint8_t)(c->perm[((size_t)e * F + f) * Nf + a] * nd + k);
+  HFX_CUDA(c, upload(m, &B.permx, px.data(), px.size(), s));
+  std::vector<double> tau((size_t)c->topo.nFaces * Nf * nd * nd, 0.0);
+  for (size_t k = 0; k < (size_t)c->topo.nFaces * Nf; ++k)
+    for (int q = 0; q < nd; ++q) tau[k * nd * nd + q * nd + q] = 1.0;
+  HFX_CUDA(c, B.tau.set(tau.data(), tau.size(), s));
+  std::vector<double> zeros((size_t)B.nDofs, 0.0);
+  HFX_CUDA(c, B.dir.set(zeros.data(), zeros.size(), s));
+  B.tauSides = 1;
+  B.kc = 0;
+  B.haveSrc = false;
+  B.dt = 0.0;
+  HFX_CUDA(c, cudaStreamSynchronize(s));
+  B.ready = true;
+  return HFX_OK;
+}
+
+int hfx_burgers_set_tau(hfx_ctx* c, const double* tau, int sides) {
+  if (int rc = burgers_ready(c, "burgers_set_tau")) return rc;
+  if (!tau || (sides != 1 && sides != 2)) return set_err(c, HFX_ERR_ARG, "burgers_set_tau: tau and sides 1 or 2");
+  BurgersState& B = c->burgers;
+  B.tauSides = sides;
+  HFX_CUDA(c, B.tau.set(tau, (size_t)c->topo.nFaces * c->re.nNodesFace * sides * B.nd * B.nd, c->stream));
+  HFX_CUDA(c, cudaStreamSynchronize(c->stream));
+  return HFX_OK;
+}
+
+int hfx_burgers_set_diffusion(hfx_ctx* c, const double* nu, int comps, int layout) {
+  if (int rc = burgers_ready(c, "burgers_set_diffusion")) return rc;
+  BurgersState& B = c->burgers;
+  if (!nu || comps == 0) {
+    B.kc = 0;
+    return HFX_OK;
+  }
+  if ((comps != 1 && comps != c->dim * c->dim) || (layout != 0 && layout != 1))
+    return set_err(c, HFX_ERR_ARG, "burgers_set_diffusion: comps 1 or dim*dim, layout 0 (mesh nodes) or 1 (cell nodes)");
+  const size_t n = (size_t)(layout == 0 ? c->nNodes : (int64_t)c->nCells * c->re.nNodes) * comps;
+  HFX_CUDA(c, B.nu.set(nu, n, c->stream));
+  HFX_CUDA(c, cudaStreamSynchronize(c->stream));
+  B.kc = comps;
+  B.nuLayout = layout;
+  return HFX_OK;
+}
+
+int hfx_burgers_set_source(hfx_ctx* c, const double* values) {
+  if (int rc = burgers_ready(c, "burgers_set_source")) return rc;
+  BurgersState& B = c->burgers;
+  B.haveSrc = values != nullptr;
+  if (values) {
+    HFX_CUDA(c, B.src.set(values, (size_t)c->nCells * c->re.nIP * B.nd, c->stream));
+    HFX_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  return HFX_OK;
+}
+
+int hfx_burgers_set_dirichlet(hfx_ctx* c, const double* values) {
+  if (int rc = burgers_ready(c, "burgers_set_dirichlet")) return rc;
+  if (!values) return set_err(c, HFX_ERR_ARG, "burgers_set_dirichlet: values");
+  HFX_CUDA(c, c->burgers.dir.set(values, (size_t)c->burgers.nDofs, c->stream));
+  HFX_CUDA(c, cudaStreamSynchronize(c->stream));
+  return HFX_OK;
+}
+
+int hfx_burgers_set_time_step(hfx_ctx* c, double dt) {
+  if (int rc = burgers_ready(c, "burgers_set_time_step")) return rc;
+  if (!(dt >= 0.0)) return set_err(c, HFX_ERR_ARG, "burgers_set_time_step: dt >= 0");
+  c->burgers.dt = dt;
+  return HFX_OK;
+}
+
+int hfx_burgers_set_state(hfx_ctx* c, const double* solution, const double* buffer, const double* trace,
+                          const double* oldSolution) {
+  if (int rc = burgers_ready(c, "burgers_set_state")) return rc;
+  BurgersState& B = c->burgers;
+  const size_t nu = (size_t)c->nCells * B.NU;
+  cudaStream_t s = c->stream;
+  if (solution) HFX_CUDA(c, cudaMemcpyAsync(B.sol, solution, sizeof(double) * nu, cudaMemcpyHostToDevice, s));
+  if (buffer) HFX_CUDA(c, cudaMemcpyAsync(B.buf, buffer, sizeof(double) * nu, cudaMemcpyHostToDevice, s));
+  if (oldSolution) HFX_CUDA(c, cudaMemcpyAsync(B.old, oldSolution, sizeof(double) * nu, cudaMemcpyHostToDevice, s));
+  if (trace) HFX_CUDA(c, cudaMemcpyAsync(B.trace, trace, sizeof(double) * B.nDofs, cudaMemcpyHostToDevice, s));
+  HFX_CUDA(c, cudaStreamSynchronize(s));
+  return HFX_OK;
+}
+
+int hfx_burgers_get_state(hfx_ctx* c, double* solution, double* flux, double* trace, double* buffer) {
+  if (int rc = burgers_ready(c, "burgers_get_state")) return rc;
+  BurgersState& B = c->burgers;
+  const size_t nu = (size_t)c->nCells * B.NU;
+  cudaStream_t s = c->stream;
+  if (solution) HFX_CUDA(c, cudaMemcpyAsync(solution, B.sol, sizeof(double) * nu, cudaMemcpyDeviceToHost, s));
+  if (flux)
+    HFX_CUDA(c, cudaMemcpyAsync(flux, B.flux, sizeof(double) * c->nCells * B.NQ, cudaMemcpyDeviceToHost, s));
+  if (trace) HFX_CUDA(c, cudaMemcpyAsync(trace, B.trace, sizeof(double) * B.nDofs, cudaMemcpyDeviceToHost, s));
+  if (buffer) HFX_CUDA(c, cudaMemcpyAsync(buffer, B.buf, sizeof(double) * nu, cudaMemcpyDeviceToHost, s));
+  HFX_CUDA(c, cudaStreamSynchronize(s));
+  return HFX_OK;
+}
+
+int hfx_burgers_begin_step(hfx_ctx* c) {
+  if (int rc = burgers_ready(c, "burgers_begin_step")) return rc;
+  BurgersState& B = c->burgers;
+  const size_t nu = (size_t)c->nCells * B.NU;
+  HFX_CUDA(c, cudaMemcpyAsync(B.buf, B.sol, sizeof(double) * nu, cudaMemcpyDeviceToDevice, c->stream));
+  HFX_CUDA(c, cudaMemcpyAsync(B.old, B.sol, sizeof(double) * nu, cudaMemcpyDeviceToDevice, c->stream));
+  return HFX_OK;
+}
+
+// Element kernel + scatter, queued on the stream; *status is read by the caller.
+static int burgers_assemble_async(hfx_ctx* c) {
+  BurgersState& B = c->burgers;
+  cudaStream_t s = c->stream;
+  BurgersParams p{};
+  p.nCells = c->nCells;
+  p.coords = c->d_coords;
+  p.cells = c->d_cells;
+  p.cell2face = c->d_cell2face;
+  p.perm = c->d_perm;
+  p.face2cell = c->d_face2cell;
+  p.isBoundary = c->d_isBnd;
+  p.tau = B.tau.p;
+  p.tauSides = B.tauSides;
+  p.nu = B.kc ? B.nu.p : nullptr;
+  p.kc = B.kc;
+  p.nuLayout = B.nuLayout;
+  p.src = B.haveSrc ? B.src.p : nullptr;
+  p.dirichlet = B.dir.p;
+  p.dt = B.dt;
+  p.uOld = B.old;
+  p.buf = B.buf;
+  p.trace = B.trace;
+  p.tab = c->d_tab;
+  p.itab = c->d_itab;
+  p.S = B.S;
+  p.S0 = B.S0;
+  p.U = B.U;
+  p.Q = B.Q;
+  p.U0 = B.U0;
+  p.Q0 = B.Q0;
+  p.status = B.status;
+  HFX_CUDA(c, cudaMemsetAsync(B.status, 0, sizeof(int), s));
+  c->timer.begin(K_LOCAL, s);
+  HFX_CUDA(c, launch_burgers_local(c->dim, c->order, p, s));
+  c->timer.end(K_LOCAL, s);
+  ScatterParams sp{};
+  sp.nFaces = c->topo.nFaces;
+  sp.NF = B.NLF;
+  sp.LL = B.NL;
+  sp.browptr = c->d_browptr;
+  sp.brow = c->d_brow;
+  sp.nBlocks = (int64_t)c->bp.col.size();
+  sp.src0 = c->d_src0;
+  sp.src1 = c->d_src1;
+  sp.loc0 = c->d_loc0;
+  sp.loc1 = c->d_loc1;
+  sp.perm = B.permx;
+  sp.S = B.S;
+  sp.S0 = B.S0;
+  sp.cell2face = c->d_cell2face;
+  sp.face2cell = c->d_face2cell;
+  sp.F = c->re.nFaces;
+  sp.val = B.val;
+  sp.rhs = B.rhs;
+  c->timer.begin(K_SCATTER, s);
+  HFX_CUDA(c, launch_scatter(sp, s));
+  c->timer.end(K_SCATTER, s);
+  return HFX_OK;
+}
+
+int hfx_burgers_assemble(hfx_ctx* c) {
+  if (int rc = burgers_ready(c, "burgers_assemble")) return rc;
+  BurgersState& B = c->burgers;
+  if (int rc = burgers_assemble_async(c)) return rc;
+  int status = 0;
+  HFX_CUDA(c, cudaMemcpyAsync(&status, B.status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  HFX_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (status) return set_err(c, HFX_ERR_SINGULAR, "burgers_assemble: singular Schur block in condensation");
+  B.assembled = true;
+  B.solved = false;
+  return HFX_OK;
+}
+
+static int burgers_check_opts(hfx_ctx* c, const hfx_solve_opts& o) {
+  if (o.method == HFX_KSP_CG)
+    return set_err(c, HFX_ERR_ARG, "burgers_solve: the Burgers trace system is not symmetric (use GMRES)");
+  if (o.precision != HFX_PREC_FP64)
+    return set_err(c, HFX_ERR_UNSUPPORTED, "burgers_solve: FP64 GMRES only");
+  if (o.precond < HFX_PC_NONE || o.precond > HFX_PC_BLOCK_JACOBI || o.rtol <= 0.0 || o.maxits <= 0)
+    return set_err(c, HFX_ERR_ARG, "burgers_solve: precond none / Jacobi / block Jacobi, rtol > 0, maxits > 0");
+  return HFX_OK;
+}
+
+// GMRES + recovery, queued on the stream; returns the Krylov status.
+static int burgers_solve_core(hfx_ctx* c, const hfx_solve_opts& o, TraceSolveResult* res, int* kst) {
+  BurgersState& B = c->burgers;
+  const int restart = o.restart > 0 ? o.restart : 30;
+  DevMem& m = B.wsMem;
+  TraceWorkspace& w = B.ws;
+  const size_t n = (size_t)B.nDofs;
+  if (restart > B.wsRestart) {
+    HFX_CUDA(c, dalloc(m, &w.V64, n * (restart + 1)));
+    HFX_CUDA(c, dalloc(m, &w.hdev, (size_t)restart + 1));
+    B.wsRestart = restart;
+  }
+  if (!B.wsReady) {
+    HFX_CUDA(c, dalloc(m, &w.bS, n));
+    HFX_CUDA(c, dalloc(m, &w.r, n));
+    HFX_CUDA(c, dalloc(m, &w.z, n));
+    HFX_CUDA(c, dalloc(m, &w.q, n));
+    HFX_CUDA(c, dalloc(m, &w.p0, n));
+    HFX_CUDA(c, dalloc(m, &w.pc64, (size_t)c->topo.nFaces * B.NLF * B.NLF));
+    HFX_CUDA(c, dalloc(m, &w.partials, trace_partials_needed()));
+    HFX_CUDA(c, dalloc(m, &w.state, 1));
+    B.wsReady = true;
+  }
+  TraceSolveArgs a{};
+  a.dim = c->dim;
+  a.A = TraceView{c->topo.nFaces, B.NLF, c->d_browptr, c->d_bcol, c->d_isBnd};
+  a.val = B.val;
+  a.rhs = B.rhs;
+  a.x = B.trace;
+  a.precond = o.precond;
+  a.mixed = 0;
+  a.rtol = o.rtol;
+  a.inner_rtol = 1e-2;
+  a.maxits = o.maxits;
+  a.max_refinements = 1;
+  a.check_every = 25;
+  a.use_initial_guess = o.use_initial_guess;
+  a.ws = B.ws;
+  a.stream = c->stream;
+  a.timer = &c->timer;
+  a.restart = restart;
+  *kst = trace_gmres(a, res);
+  if (*kst == 3) return cuda_err(c, res->cudaErr, "burgers_solve");
+  RecoverParams rp{c->nCells, c->re.nFaces, B.NLF, B.NU, B.NQ, B.NL, c->d_cell2face, B.permx,
+                   B.U, B.Q, B.U0, B.Q0, B.trace, B.sol, B.flux};
+  c->timer.begin(K_RECOVER, c->stream);
+  HFX_CUDA(c, launch_recover(rp, c->stream));
+  c->timer.end(K_RECOVER, c->stream);
+  return HFX_OK;
+}
+
+static int burgers_krylov_err(hfx_ctx* c, int st) {
+  if (st == HFX_ERR_NOT_CONVERGED) return set_err(c, st, "burgers_solve: GMRES not converged within maxits");
+  if (st == HFX_ERR_BREAKDOWN) return set_err(c, st, "burgers_solve: GMRES breakdown");
+  if (st == HFX_ERR_NAN) return set_err(c, st, "burgers_solve: NaN or Inf in GMRES");
+  if (st == HFX_ERR_UNSUPPORTED) return set_err(c, st, "burgers_solve: trace block size not built into GMRES");
+  return set_err(c, st, "burgers_solve: failed");
+}
+
+int hfx_burgers_solve(hfx_ctx* c, const hfx_solve_opts* opts, hfx_solve_info* info) {
+  if (int rc = burgers_ready(c, "burgers_solve")) return rc;
+  BurgersState& B = c->burgers;
+  if (!B.assembled) return set_err(c, HFX_ERR_STATE, "burgers_solve: assemble first");
+  hfx_solve_opts o;
+  if (opts) o = *opts;
+  else {
+    hfx_solve_opts_default(&o);
+    o.method = HFX_KSP_GMRES;
+  }
+  if (int rc = burgers_check_opts(c, o)) return rc;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, c->stream);
+  TraceSolveResult res;
+  int st = 0;
+  int rc = burgers_solve_core(c, o, &res, &st);
+  cudaEventRecord(e1, c->stream);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  if (info) {
+    *info = hfx_solve_info{};
+    info->status = st;
+    info->iterations = res.iterations;
+    info->rel_residual = res.rel_residual;
+    info->solve_ms = ms;
+  }
+  B.solved = true;
+  if (st != 0) return burgers_krylov_err(c, st);
+  return HFX_OK;
+}
+
+void hfx_newton_opts_default(hfx_newton_opts* o) {
+  if (!o) return;
+  o->res_tol = 1e-6;
+  o->max_iters = 20;
+  o->dampening = 0.0;
+  hfx_solve_opts_default(&o->lin);
+  o->lin.method = HFX_KSP_GMRES;
+  o->lin.rtol = 1e-12;
+  o->warm_start = 0;
+}
+
+int hfx_burgers_newton(hfx_ctx* c, const hfx_newton_opts* opts, hfx_newton_info* info) {
+  if (int rc = burgers_ready(c, "burgers_newton")) return rc;
+  BurgersState& B = c->burgers;
+  hfx_newton_opts o;
+  if (opts) o = *opts;
+  else hfx_newton_opts_default(&o);
+  if (!(o.res_tol > 0.0) || o.max_iters <= 0 || !(o.dampening >= 0.0 && o.dampening < 1.0))
+    return set_err(c, HFX_ERR_ARG, "burgers_newton: res_tol > 0, max_iters > 0, 0 <= dampening < 1");
+  if (int rc = burgers_check_opts(c, o.lin)) return rc;
+  hfx_solve_opts lin = o.lin;
+  lin.use_initial_guess = o.warm_start ? 1 : 0;
+  cudaStream_t s = c->stream;
+  const int64_t nu = (int64_t)c->nCells * B.NU;
+  cudaEvent_t ev[4];
+  for (auto& e : ev) cudaEventCreate(&e);
+  hfx_newton_info out{};
+  int rc = HFX_OK;
+  for (int it = 0; it < o.max_iters; ++it) {
+    cudaEventRecord(ev[0], s);
+    if ((rc = burgers_assemble_async(c))) break;
+    cudaEventRecord(ev[1], s);
+    TraceSolveResult res;
+    int st = 0;
+    if ((rc = burgers_solve_core(c, lin, &res, &st))) break;
+    cudaEventRecord(ev[2], s);
+    if (cudaError_t e = launch_newton_residual(nu, B.sol, B.buf, B.partials, B.ticket, B.red, s)) {
+      rc = cuda_err(c, e, "burgers_newton: residual");
+      break;
+    }
+    double red[2] = {0.0, 0.0};
+    int kstatus = 0;
+    cudaMemcpyAsync(red, B.red, sizeof(red), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&kstatus, B.status, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaEventRecord(ev[3], s);
+    if (cudaError_t e = cudaStreamSynchronize(s)) {
+      rc = cuda_err(c, e, "burgers_newton");
+      break;
+    }
+    float ta = 0.f, ts = 0.f;
+    cudaEventElapsedTime(&ta, ev[0], ev[1]);
+    cudaEventElapsedTime(&ts, ev[1], ev[2]);
+    out.assemble_ms += ta;
+    out.solve_ms += ts;
+    out.krylov_iterations += res.iterations;
+    out.iterations = it + 1;
+    if (kstatus) {
+      rc = set_err(c, HFX_ERR_SINGULAR, "burgers_newton: singular Schur block in condensation");
+      break;
+    }
+    if (st != 0) {
+      rc = burgers_krylov_err(c, st);
+      break;
+    }
+    out.residual = red[1] != 0.0 ? std::sqrt(red[0] / red[1]) : std::sqrt(red[0]);
+    if (out.residual < o.res_tol) break;
+    if (cudaError_t e = launch_newton_update(nu, o.dampening, B.sol, B.buf, s)) {
+      rc = cuda_err(c, e, "burgers_newton: update");
+      break;
+    }
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  out.status = rc;
+  B.assembled = true;
+  B.solved = rc == HFX_OK;
+  if (info) *info = out;
+  return rc;
+}
+
+int hfx_burgers_get_condensed(hfx_ctx* c, double* S, double* S0, double* U, double* Q, double* U0, double* Q0) {
+  if (int rc = burgers_ready(c, "burgers_get_condensed")) return rc;
+  BurgersState& B = c->burgers;
+  if (!B.assembled) return set_err(c, HFX_ERR_STATE, "burgers_get_condensed: assemble first");
+  const size_t E = (size_t)c->nCells;
+  cudaStream_t s = c->stream;
+  auto cp = [&](double* h, const double* d, size_t n) {
+    return h ? cudaMemcpyAsync(h, d, sizeof(double) * n, cudaMemcpyDeviceToHost, s) : cudaSuccess;
+  };
+  HFX_CUDA(c, cp(S, B.S, E * B.NL * B.NL));
+  HFX_CUDA(c, cp(S0, B.S0, E * B.NL));
+  HFX_CUDA(c, cp(U, B.U, E * B.NU * B.NL));
+  HFX_CUDA(c, cp(Q, B.Q, E * B.NQ * B.NL));
+  HFX_CUDA(c, cp(U0, B.U0, E * B.NU));
+  HFX_CUDA(c, cp(Q0, B.Q0, E * B.NQ));
+  HFX_CUDA(c, cudaStreamSynchronize(s));
+  return HFX_OK;
+}
+
+int hfx_burgers_nnz(hfx_ctx* c, int64_t* nnz) {
+  if (int rc = burgers_ready(c, "burgers_nnz")) return rc;
+  if (!nnz) return set_err(c, HFX_ERR_ARG, "burgers_nnz: nnz");
+  *nnz = c->burgers.nnz;
+  return HFX_OK;
+}
+
+int hfx_burgers_get_csr(hfx_ctx* c, int64_t* rowptr, int* col, double* val, double* rhs) {
+  if (int rc = burgers_ready(c, "burgers_get_csr")) return rc;
+  BurgersState& B = c->burgers;
+  if (!B.assembled && (val || rhs)) return set_err(c, HFX_ERR_STATE, "burgers_get_csr: assemble first");
+  const int NB = B.NLF;
+  const int nF = c->topo.nFaces;
+  if (rowptr || col) {
+    int64_t pos = 0;
+    if (rowptr) rowptr[0] = 0;
+    for (int f = 0; f < nF; ++f) {
+      int64_t b0 = c->bp.rowptr[f], nb = c->bp.rowptr[f + 1] - b0;
+      for (int a = 0; a < NB; ++a) {
+        if (col)
+          for (int64_t k = 0; k < nb; ++k)
+            for (int b = 0; b < NB; ++b) col[pos + k * NB + b] = c->bp.col[b0 + k] * NB + b;
+        pos += nb * NB;
+        if (rowptr) rowptr[(int64_t)f * NB + a + 1] = pos;
+      }
+    }
+  }
+  cudaStream_t s = c->stream;
+  std::vector<double> blocks;
+  if (val) {
+    blocks.resize((size_t)B.nnz);
+    HFX_CUDA(c, cudaMemcpyAsync(blocks.data(), B.val, sizeof(double) * B.nnz, cudaMemcpyDeviceToHost, s));
+  }
+  if (rhs) HFX_CUDA(c, cudaMemcpyAsync(rhs, B.rhs, sizeof(double) * B.nDofs, cudaMemcpyDeviceToHost, s));
+  HFX_CUDA(c, cudaStreamSynchronize(s));
+  if (val) {
+    int64_t pos = 0;
+    for (int f = 0; f < nF; ++f) {
+      int64_t b0 = c->bp.rowptr[f], nb = c->bp.rowptr[f + 1] - b0;
+      for (int a = 0; a < NB; ++a)
+        for (int64_t k = 0; k < nb; ++k)
+          for (int b = 0; b < NB; ++b) val[pos++] = blocks[(b0 + k) * NB * NB + (int64_t)b * NB + a];
+    }
+  }
   return HFX_OK;
 }
 

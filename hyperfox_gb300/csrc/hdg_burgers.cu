@@ -1,0 +1,683 @@
+// HDG viscous Burgers element kernel (vector unknowns, nd = dim), FP64, sm_103a.
+//
+// One CTA of kBT threads owns one element at a time (grid-stride loop over the
+// elements); the reference tables are staged once per CTA in shared memory.
+// Restates, per element (HyperFox file:line):
+//   Jacobians / measures / inverse   Operator.cpp:14-84, HDGModel.cpp:53-85
+//   normals                          HDGBase.cpp:34-65
+//   tau (nd x nd) at face IPs        HDGBase.cpp:18-32
+//   HDGBase blocks, nd unknowns      HDGBase.cpp:67-158
+//   HDGUNabU (u.grad u linearised)   HDGUNabU.cpp:27-193
+//   HDGDiffusion blocks, nd unknowns HDGDiffusion.cpp:31-145
+//   model composition                HDGBurgersModel.cpp:93-125 (one Source per component)
+//   implicit Euler on the U rows     HDGModel.cpp:35-51, Euler.cpp:18-34, Operator.cpp:86-97
+//   condensation U,Q,U0,Q0,S,S0      HDGSolver.cpp:331-348
+//   Dirichlet Set on boundary faces  HDGSolver.cpp:361-529, DirichletModel.cpp:19-44
+//
+// Local layout (HDGBase.cpp:85-91): U row (i, c) = i*ND + c, Q row
+// ((i*D + k)*ND + c), L row ((f*NF + a)*ND + c). The local matrix is never formed
+// as a whole: the kernel builds the scalar blocks (mass M, C_k, the diffusion
+// coupling K'_k, the face blocks E, H, the tau masses T and the convection face
+// block) and condenses with Sqq = M (x) I, so Sqq^{-1} is one N x N inverse;
+// the Schur block A = s (Suu - Suq Sqq^{-1} Squ) (+ M (x) I) couples the
+// components and is solved by Gauss-Jordan with partial pivoting. Results equal
+// the reference's dense QR condensation up to round-off.
+#include <cstdio>
+
+#include "hfx_device.h"
+
+namespace hfx {
+namespace {
+
+constexpr int kBT = 128;  // threads per CTA = per element
+
+template <int D, int P>
+struct BL {
+  using K = Dims<D, P>;
+  static constexpr int N = K::N, NF = K::NF, F = K::F, NI = K::NI, NIF = K::NIF;
+  static constexpr int ND = D, DM = D - 1, NT = ND * ND;
+  static constexpr int NU = N * ND, NQ = D * N * ND, NLF = NF * ND, NL = F * NLF;
+  static constexpr int W = NU + NL + 1;  // augmented row [A | -B | Fu]
+  // tables, same packing as the quadrature kernel (phi, dphi, w, fphi, fdphi, fw)
+  static constexpr int T_PHI = 0;
+  static constexpr int T_DPHI = T_PHI + NI * N;
+  static constexpr int T_W = T_DPHI + NI * N * D;
+  static constexpr int T_FPHI = T_W + NI;
+  static constexpr int T_FDPHI = T_FPHI + NIF * NF;
+  static constexpr int T_FW = T_FDPHI + NIF * NF * DM;
+  static constexpr int TAB = (T_FW + NIF + 1) & ~1;
+  // element region (doubles, offsets from TAB)
+  static constexpr int X = 0;                       // N*D coordinates
+  static constexpr int UB = X + N * D;              // NU BufferSolution
+  static constexpr int UO = UB + NU;                // NU old solution (implicit Euler)
+  static constexpr int TR = UO + NU;                // NL local trace
+  static constexpr int TAU = TR + NL;               // F*NF*NT local tau
+  static constexpr int KAP = TAU + F * NF * NT;     // N*D*D nodal diffusion tensor
+  static constexpr int IJ = KAP + N * D * D;        // NI*D*D inverse Jacobians
+  static constexpr int DV = IJ + NI * D * D;        // NI
+  static constexpr int DS = DV + NI;                // F*NIF
+  static constexpr int NRM = DS + F * NIF;          // F*NIF*D
+  static constexpr int G = NRM + F * NIF * D;       // NI*N*D  J^-1 grad phi
+  static constexpr int KG = G + NI * N * D;         // NI*N*D  Ds J^-1 grad phi
+  static constexpr int SOL = KG + NI * N * D;       // NI*ND   u at the IPs
+  static constexpr int DIV = SOL + NI * ND;         // NI      div u
+  static constexpr int FSOL = DIV + NI;             // F*NIF*ND u (interior) at face IPs
+  static constexpr int TN = FSOL + F * NIF * ND;    // F*NIF   (t.n) dS
+  static constexpr int TAUQ = TN + F * NIF;         // F*NIF*NT dS tau
+  static constexpr int DSKN = TAUQ + F * NIF * NT;  // F*NIF*D dS Ds n
+  static constexpr int MM = DSKN + F * NIF * D;     // N*N mass
+  static constexpr int MI = MM + N * N;             // N*2N Gauss-Jordan [M | I] -> [I | M^-1]
+  static constexpr int CK = MI + 2 * N * N;         // D*N*N  C_k
+  static constexpr int MC = CK + D * N * N;         // D*N*N  M^-1 C_k
+  static constexpr int KP = MC + D * N * N;         // D*N*N  K'_k
+  static constexpr int EF = KP + D * N * N;         // F*D*NF*NF  E_fk
+  static constexpr int ME = EF + F * D * NF * NF;   // D*N*F*NF   M^-1 E
+  static constexpr int HF = ME + D * N * F * NF;    // F*D*NF*NF  H_fk
+  static constexpr int TM = HF + F * D * NF * NF;   // F*NT*NF*NF tau masses [f][c][m][a][b]
+  static constexpr int CLL = TM + F * NT * NF * NF; // F*NLF*NLF convection face blocks
+  static constexpr int CUU = CLL + F * NLF * NLF;   // NU*NU convection volume block
+  static constexpr int AUG = CUU + NU * NU;         // NU*W row-major
+  static constexpr int QS = AUG + NU * W;           // NQ*(NL+1) row-major [Q | Q0]
+  static constexpr int FL = QS + NQ * (NL + 1);     // NL
+  static constexpr int TOTAL = TAB + FL + NL + 2;   // + pivot scalars
+  static_assert(TOTAL * 8 <= 227 * 1024, "element region exceeds the shared memory of one CTA");
+};
+
+template <int D, int P>
+__global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
+  using L = BL<D, P>;
+  constexpr int N = L::N, NF = L::NF, F = L::F, NI = L::NI, NIF = L::NIF, DM = L::DM;
+  constexpr int ND = L::ND, NT = L::NT, NU = L::NU, NQ = L::NQ, NLF = L::NLF, NL = L::NL, W = L::W;
+  static_assert(D == 2, "the Burgers element kernel is built for 2D cells");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* smem = reinterpret_cast<double*>(smem_raw);
+  __shared__ int sFaceNodes[F * NF];
+  __shared__ int sOpp[F];
+  __shared__ int sPos[F * N];  // position of element node i on face f, -1 if not on it
+  __shared__ int sFace[F], sBnd[F], sPiv;
+  const int tid = threadIdx.x;
+  {
+    constexpr int nTab = L::T_FW + NIF;
+    for (int i = tid; i < nTab; i += kBT) smem[i] = p.tab[i];
+    for (int i = tid; i < F * NF; i += kBT) sFaceNodes[i] = p.itab[i];
+    for (int i = tid; i < F; i += kBT) sOpp[i] = p.itab[F * NF + i];
+    for (int i = tid; i < F * N; i += kBT) sPos[i] = -1;
+    __syncthreads();
+    for (int i = tid; i < F * NF; i += kBT) sPos[(i / NF) * N + sFaceNodes[i]] = i % NF;
+    __syncthreads();
+  }
+  const double* phi = smem + L::T_PHI;
+  const double* dphi = smem + L::T_DPHI;
+  const double* w = smem + L::T_W;
+  const double* fphi = smem + L::T_FPHI;
+  const double* fdphi = smem + L::T_FDPHI;
+  const double* fw = smem + L::T_FW;
+  double* R = smem + L::TAB;
+  double* X = R + L::X;
+  double* ub = R + L::UB;
+  double* uo = R + L::UO;
+  double* tr = R + L::TR;
+  double* tauL = R + L::TAU;
+  double* kap = R + L::KAP;
+  double* iJ = R + L::IJ;
+  double* dV = R + L::DV;
+  double* dS = R + L::DS;
+  double* nrm = R + L::NRM;
+  double* G = R + L::G;
+  double* KG = R + L::KG;
+  double* sol = R + L::SOL;
+  double* divu = R + L::DIV;
+  double* fsol = R + L::FSOL;
+  double* tn = R + L::TN;
+  double* tauq = R + L::TAUQ;
+  double* dskn = R + L::DSKN;
+  double* Mm = R + L::MM;
+  double* MI = R + L::MI;
+  double* Ck = R + L::CK;
+  double* MC = R + L::MC;
+  double* KP = R + L::KP;
+  double* Ef = R + L::EF;
+  double* ME = R + L::ME;
+  double* Hf = R + L::HF;
+  double* Tm = R + L::TM;
+  double* Cll = R + L::CLL;
+  double* Cuu = R + L::CUU;
+  double* Aug = R + L::AUG;
+  double* Qs = R + L::QS;
+  double* Fl = R + L::FL;
+  double* pivInv = R + L::FL + NL;
+  const bool diff = p.kc != 0;
+  const bool euler = p.dt > 0.0;
+  const double s = euler ? p.dt : 1.0;
+
+  for (int64_t e = blockIdx.x; e < p.nCells; e += gridDim.x) {
+    // ------------------------------------------------------------ gather
+    const int* cell = p.cells + e * N;
+    for (int i = tid; i < N * D; i += kBT) X[i] = p.coords[(int64_t)cell[i / D] * D + (i % D)];
+    for (int i = tid; i < NU; i += kBT) {
+      ub[i] = p.buf[e * NU + i];
+      uo[i] = euler ? p.uOld[e * NU + i] : 0.0;
+    }
+    for (int i = tid; i < F; i += kBT) {
+      const int f = p.cell2face[e * F + i];
+      sFace[i] = f;
+      sBnd[i] = p.isBoundary[f];
+    }
+    for (int i = tid; i < F * NF; i += kBT) {
+      const int f = p.cell2face[e * F + i / NF];
+      const int side = (p.face2cell[2 * (int64_t)f] == (int)e) ? 0 : 1;
+      const int q = p.perm[e * F * NF + i];
+      for (int c = 0; c < ND; ++c) tr[i * ND + c] = p.trace[((int64_t)f * NF + q) * ND + c];
+      const int64_t tb = (((int64_t)f * NF + q) * p.tauSides + (p.tauSides == 2 ? side : 0)) * NT;
+      for (int v = 0; v < NT; ++v) tauL[i * NT + v] = p.tau[tb + v];
+    }
+    for (int i = tid; i < N * D * D; i += kBT) {
+      const int n = i / (D * D), a = i % (D * D);
+      double v = 0.0;
+      if (diff) {
+        const int64_t bk = p.nuLayout == 0 ? (int64_t)cell[n] * p.kc : (e * N + n) * p.kc;
+        v = p.kc == 1 ? ((a % (D + 1) == 0) ? p.nu[bk] : 0.0) : p.nu[bk + a];
+      }
+      kap[i] = v;
+    }
+    __syncthreads();
+    // ---------------------------------------------------------- geometry
+    for (int q = tid; q < NI; q += kBT) {
+      double J[D][D];
+      for (int r = 0; r < D; ++r)
+        for (int c = 0; c < D; ++c) {
+          double acc = 0.0;
+          for (int i = 0; i < N; ++i) acc += dphi[(q * N + i) * D + r] * X[i * D + c];
+          J[r][c] = acc;
+        }
+      const double det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+      const double id = 1.0 / det;
+      iJ[q * 4 + 0] = J[1][1] * id;   // (0,0)
+      iJ[q * 4 + 1] = -J[0][1] * id;  // (0,1)
+      iJ[q * 4 + 2] = -J[1][0] * id;  // (1,0)
+      iJ[q * 4 + 3] = J[0][0] * id;   // (1,1)
+      dV[q] = w[q] * det;
+    }
+    for (int fk = tid; fk < F * NIF; fk += kBT) {
+      const int f = fk / NIF, k = fk % NIF;
+      double j0 = 0.0, j1 = 0.0;
+      for (int i = 0; i < NF; ++i) {
+        const double g = fdphi[(k * NF + i) * DM];
+        j0 += g * X[sFaceNodes[f * NF + i] * D + 0];
+        j1 += g * X[sFaceNodes[f * NF + i] * D + 1];
+      }
+      const double ds = sqrt(j0 * j0 + j1 * j1);
+      double n0 = -j1 / ds, n1 = j0 / ds;
+      const int v0 = sFaceNodes[f * NF], vn = sOpp[f];
+      const double prod = (X[vn * D] - X[v0 * D]) * n0 + (X[vn * D + 1] - X[v0 * D + 1]) * n1;
+      if (prod > 0) {
+        n0 = -n0;
+        n1 = -n1;
+      }
+      dS[fk] = fw[k] * ds;
+      nrm[fk * D] = n0;
+      nrm[fk * D + 1] = n1;
+    }
+    __syncthreads();
+    // ------------------------------------------- values at the integration points
+    for (int qi = tid; qi < NI * N; qi += kBT) {
+      const int q = qi / N, i = qi % N;
+      double g[D];
+      for (int a = 0; a < D; ++a) {
+        double acc = 0.0;
+        for (int b = 0; b < D; ++b) acc += iJ[q * 4 + a * 2 + b] * dphi[(q * N + i) * D + b];
+        g[a] = acc;
+        G[qi * D + a] = acc;
+      }
+      for (int a = 0; a < D; ++a) {
+        double acc = 0.0;
+        if (diff)
+          for (int b = 0; b < D; ++b) {
+            double dab = 0.0;  // Ds(a, b) at q, column-major (HDGDiffusion.cpp:52-57)
+            for (int n = 0; n < N; ++n) dab += phi[q * N + n] * kap[n * D * D + a + b * D];
+            acc += dab * g[b];
+          }
+        KG[qi * D + a] = acc;
+      }
+    }
+    for (int fq = tid; fq < F * NIF; fq += kBT) {
+      const int f = fq / NIF, k = fq % NIF;
+      const double ds = dS[fq];
+      double trq[ND], dsf[D * D];
+      for (int c = 0; c < ND; ++c) {
+        double a1 = 0.0, a2 = 0.0;
+        for (int a = 0; a < NF; ++a) {
+          const double sh = fphi[k * NF + a];
+          a1 += sh * ub[sFaceNodes[f * NF + a] * ND + c];
+          a2 += sh * tr[(f * NF + a) * ND + c];
+        }
+        fsol[fq * ND + c] = a1;
+        trq[c] = a2;
+      }
+      double t = 0.0;
+      for (int c = 0; c < D; ++c) t += trq[c] * nrm[fq * D + c];
+      tn[fq] = t * ds;
+      for (int v = 0; v < NT; ++v) {
+        double acc = 0.0;
+        for (int a = 0; a < NF; ++a) acc += fphi[k * NF + a] * tauL[(f * NF + a) * NT + v];
+        tauq[fq * NT + v] = ds * acc;
+      }
+      for (int v = 0; v < D * D; ++v) {
+        double acc = 0.0;
+        for (int a = 0; a < NF; ++a) acc += fphi[k * NF + a] * kap[sFaceNodes[f * NF + a] * D * D + v];
+        dsf[v] = acc;
+      }
+      for (int a = 0; a < D; ++a) {
+        double acc = 0.0;
+        for (int b = 0; b < D; ++b) acc += dsf[a + b * D] * nrm[fq * D + b];
+        dskn[fq * D + a] = ds * acc;
+      }
+    }
+    for (int q = tid; q < NI; q += kBT) {
+      for (int c = 0; c < ND; ++c) {
+        double acc = 0.0;
+        for (int i = 0; i < N; ++i) acc += phi[q * N + i] * ub[i * ND + c];
+        sol[q * ND + c] = acc;
+      }
+    }
+    __syncthreads();
+    for (int q = tid; q < NI; q += kBT) {
+      double acc = 0.0;  // trace of sum_i grad(phi_i) u_i^T (HDGUNabU.cpp:160-166)
+      for (int i = 0; i < N; ++i)
+        for (int k = 0; k < D; ++k) acc += G[(q * N + i) * D + k] * ub[i * ND + k];
+      divu[q] = acc;
+    }
+    __syncthreads();
+    // ------------------------------------------------------ scalar blocks
+    for (int ij = tid; ij < N * N; ij += kBT) {
+      const int i = ij / N, j = ij % N;
+      double m = 0.0, c[D] = {}, kp[D] = {};
+      for (int q = 0; q < NI; ++q) {
+        const double pj = phi[q * N + j] * dV[q];
+        m += phi[q * N + i] * pj;
+        for (int k = 0; k < D; ++k) {
+          c[k] += G[(q * N + i) * D + k] * pj;
+          kp[k] += KG[(q * N + i) * D + k] * pj;
+        }
+      }
+      if (diff)
+        for (int f = 0; f < F; ++f) {
+          const int a = sPos[f * N + i], b = sPos[f * N + j];
+          if (a < 0 || b < 0) continue;
+          for (int k2 = 0; k2 < NIF; ++k2) {
+            const double ss = fphi[k2 * NF + a] * fphi[k2 * NF + b];
+            for (int k = 0; k < D; ++k) kp[k] -= dskn[(f * NIF + k2) * D + k] * ss;
+          }
+        }
+      Mm[ij] = m;
+      MI[i * 2 * N + j] = m;
+      MI[i * 2 * N + N + j] = (i == j) ? 1.0 : 0.0;
+      for (int k = 0; k < D; ++k) {
+        Ck[k * N * N + ij] = c[k];
+        KP[k * N * N + ij] = diff ? kp[k] : 0.0;
+      }
+    }
+    for (int x = tid; x < F * NF * NF; x += kBT) {
+      const int f = x / (NF * NF), a = (x / NF) % NF, b = x % NF;
+      double ev[D] = {}, hv[D] = {}, tv[NT] = {};
+      for (int k2 = 0; k2 < NIF; ++k2) {
+        const int fq = f * NIF + k2;
+        const double ss = fphi[k2 * NF + a] * fphi[k2 * NF + b];
+        for (int k = 0; k < D; ++k) {
+          ev[k] += dS[fq] * nrm[fq * D + k] * ss;
+          hv[k] += dskn[fq * D + k] * ss;
+        }
+        for (int v = 0; v < NT; ++v) tv[v] += tauq[fq * NT + v] * ss;
+      }
+      for (int k = 0; k < D; ++k) {
+        Ef[((f * D + k) * NF + a) * NF + b] = ev[k];
+        Hf[((f * D + k) * NF + a) * NF + b] = diff ? hv[k] : 0.0;
+      }
+      // tau column-major: (c, m) at m*ND + c
+      for (int c = 0; c < ND; ++c)
+        for (int m = 0; m < ND; ++m) Tm[(((f * ND + c) * ND + m) * NF + a) * NF + b] = tv[m * ND + c];
+    }
+    for (int x = tid; x < F * NLF * NLF; x += kBT) {
+      // HDGUNabU face block (HDGUNabU.cpp:126-145): row (a, c), column (b, m)
+      const int f = x / (NLF * NLF), r = (x / NLF) % NLF, cc = x % NLF;
+      const int a = r / ND, c = r % ND, b = cc / ND, m = cc % ND;
+      double acc = 0.0;
+      for (int k2 = 0; k2 < NIF; ++k2) {
+        const int fq = f * NIF + k2;
+        const double ss = fphi[k2 * NF + a] * fphi[k2 * NF + b];
+        acc += ((c == m ? tn[fq] : 0.0) + fsol[fq * ND + c] * nrm[fq * D + m] * dS[fq]) * ss;
+      }
+      Cll[x] = acc;
+    }
+    for (int x = tid; x < NU * NU; x += kBT) {
+      // HDGUNabU volume block (HDGUNabU.cpp:153-177): row (i, c), column (j, m)
+      const int r = x / NU, cc = x % NU;
+      const int i = r / ND, c = r % ND, j = cc / ND, m = cc % ND;
+      double acc = 0.0;
+      for (int q = 0; q < NI; ++q) {
+        const double pi = phi[q * N + i], pj = phi[q * N + j];
+        double v = sol[q * ND + c] * (G[(q * N + j) * D + m] * pi + G[(q * N + i) * D + m] * pj);
+        if (c == m) {
+          double sg = 0.0;
+          for (int k = 0; k < D; ++k) sg += sol[q * ND + k] * G[(q * N + i) * D + k];
+          v += (divu[q] * pi + sg) * pj;
+        }
+        acc -= v * dV[q];
+      }
+      Cuu[x] = acc;
+    }
+    __syncthreads();
+    // mass inverse: Gauss-Jordan on [M | I] (M is symmetric positive definite)
+    for (int k = 0; k < N; ++k) {
+      if (tid == 0) pivInv[0] = 1.0 / MI[k * 2 * N + k];
+      __syncthreads();
+      const double pinv = pivInv[0];
+      for (int j = tid; j < 2 * N; j += kBT) MI[k * 2 * N + j] *= pinv;
+      __syncthreads();
+      for (int x = tid; x < (N - 1) * 2 * N; x += kBT) {
+        int i = x / (2 * N), j = x % (2 * N);
+        if (i >= k) ++i;
+        const double l = MI[i * 2 * N + k];
+        if (j != k) MI[i * 2 * N + j] -= l * MI[k * 2 * N + j];
+      }
+      __syncthreads();
+      for (int i = tid; i < N; i += kBT)
+        if (i != k) MI[i * 2 * N + k] = 0.0;
+      __syncthreads();
+    }
+    for (int x = tid; x < D * N * N; x += kBT) {
+      const int k = x / (N * N), l = (x / N) % N, j = x % N;
+      double acc = 0.0;
+      for (int i = 0; i < N; ++i) acc += MI[l * 2 * N + N + i] * Ck[k * N * N + i * N + j];
+      MC[x] = acc;
+    }
+    for (int x = tid; x < D * N * F * NF; x += kBT) {
+      const int k = x / (N * F * NF), l = (x / (F * NF)) % N, fb = x % (F * NF);
+      const int f = fb / NF, b = fb % NF;
+      double acc = 0.0;
+      for (int a = 0; a < NF; ++a)
+        acc += MI[l * 2 * N + N + sFaceNodes[f * NF + a]] * Ef[((f * D + k) * NF + a) * NF + b];
+      ME[x] = acc;
+    }
+    __syncthreads();
+    // ------------------------------------- augmented Schur system [A | -B | Fu]
+    for (int x = tid; x < NU * W; x += kBT) {
+      const int r = x / W, col = x % W;
+      const int i = r / ND, c = r % ND;
+      double v;
+      if (col < NU) {
+        const int j = col / ND, m = col % ND;
+        double base = 0.0;
+        for (int f = 0; f < F; ++f) {
+          const int a = sPos[f * N + i], b = sPos[f * N + j];
+          if (a >= 0 && b >= 0) base += Tm[(((f * ND + c) * ND + m) * NF + a) * NF + b];
+        }
+        double schur = 0.0;
+        if (c == m && diff)
+          for (int k = 0; k < D; ++k)
+            for (int l = 0; l < N; ++l) schur += KP[k * N * N + i * N + l] * MC[k * N * N + l * N + j];
+        v = s * (base + Cuu[r * NU + col] - schur) + ((euler && c == m) ? Mm[i * N + j] : 0.0);
+      } else if (col < NU + NL) {
+        const int cl = col - NU, f = cl / NLF, b = (cl % NLF) / ND, m = cl % ND;
+        const int a = sPos[f * N + i];
+        double sul = 0.0;
+        if (a >= 0) sul = -Tm[(((f * ND + c) * ND + m) * NF + a) * NF + b] + Cll[(f * NLF + a * ND + c) * NLF + b * ND + m];
+        double schur = 0.0;
+        if (c == m && diff)
+          for (int k = 0; k < D; ++k)
+            for (int l = 0; l < N; ++l) schur += KP[k * N * N + i * N + l] * ME[(k * N + l) * F * NF + f * NF + b];
+        v = -s * (sul + schur);
+      } else {
+        // HDGUNabU RHS on the U rows: (Cuu u + Cul t) / 2 (HDGUNabU.cpp:178-190)
+        double cr = 0.0;
+        for (int cc = 0; cc < NU; ++cc) cr += Cuu[r * NU + cc] * ub[cc];
+        for (int f = 0; f < F; ++f) {
+          const int a = sPos[f * N + i];
+          if (a < 0) continue;
+          for (int cc = 0; cc < NLF; ++cc) cr += Cll[(f * NLF + a * ND + c) * NLF + cc] * tr[f * NLF + cc];
+        }
+        double fu = 0.5 * cr;
+        if (p.src)
+          for (int q = 0; q < NI; ++q) fu += phi[q * N + i] * p.src[(e * NI + q) * ND + c] * dV[q];
+        v = s * fu;
+        if (euler)
+          for (int j = 0; j < N; ++j) v += Mm[i * N + j] * uo[j * ND + c];
+      }
+      Aug[x] = v;
+    }
+    for (int x = tid; x < NL; x += kBT) {
+      // HDGUNabU RHS on the L rows: Cll t / 2 (the L-U convection block is zero)
+      const int f = x / NLF, rr = x % NLF;
+      double acc = 0.0;
+      for (int cc = 0; cc < NLF; ++cc) acc += Cll[(f * NLF + rr) * NLF + cc] * tr[f * NLF + cc];
+      Fl[x] = 0.5 * acc;
+    }
+    __syncthreads();
+    // Gauss-Jordan with partial pivoting: [A | -B | Fu] -> [I | U | U0]
+    bool singular = false;
+    for (int k = 0; k < NU; ++k) {
+      if (tid == 0) {
+        int pr = k;
+        double best = fabs(Aug[k * W + k]);
+        for (int r = k + 1; r < NU; ++r) {
+          const double v = fabs(Aug[r * W + k]);
+          if (v > best) {
+            best = v;
+            pr = r;
+          }
+        }
+        sPiv = best == 0.0 ? -1 : pr;
+      }
+      __syncthreads();
+      const int pr = sPiv;
+      if (pr < 0) {
+        singular = true;
+        break;
+      }
+      if (pr != k)
+        for (int j = tid; j < W; j += kBT) {
+          const double t = Aug[k * W + j];
+          Aug[k * W + j] = Aug[pr * W + j];
+          Aug[pr * W + j] = t;
+        }
+      __syncthreads();
+      if (tid == 0) pivInv[0] = 1.0 / Aug[k * W + k];
+      __syncthreads();
+      const double pinv = pivInv[0];
+      for (int j = tid; j < W; j += kBT) Aug[k * W + j] *= pinv;
+      __syncthreads();
+      for (int x = tid; x < (NU - 1) * (W - k - 1); x += kBT) {
+        int i = x / (W - k - 1);
+        const int j = k + 1 + x % (W - k - 1);
+        if (i >= k) ++i;
+        Aug[i * W + j] -= Aug[i * W + k] * Aug[k * W + j];
+      }
+      __syncthreads();
+      for (int i = tid; i < NU; i += kBT)
+        if (i != k) Aug[i * W + k] = 0.0;
+      __syncthreads();
+    }
+    if (singular) {
+      if (tid == 0) atomicCAS(p.status, 0, 1);
+      __syncthreads();
+      continue;
+    }
+    // ------------------------------------------------ U, U0 out; Q, Q0
+    for (int x = tid; x < NU * (NL + 1); x += kBT) {
+      const int r = x % NU, cl = x / NU;  // consecutive threads on consecutive rows
+      const double v = Aug[r * W + NU + cl];
+      if (cl < NL) p.U[e * NU * NL + (int64_t)cl * NU + r] = v;
+      else p.U0[e * NU + r] = v;
+    }
+    for (int x = tid; x < NQ * (NL + 1); x += kBT) {
+      const int rq = x % NQ, cl = x / NQ;
+      const int l = rq / (D * ND), k = (rq / ND) % D, c = rq % ND;
+      double acc = 0.0;
+      for (int j = 0; j < N; ++j) acc -= MC[k * N * N + l * N + j] * Aug[(j * ND + c) * W + NU + cl];
+      if (cl < NL) {
+        const int f = cl / NLF, b = (cl % NLF) / ND, m = cl % ND;
+        if (m == c) acc += ME[(k * N + l) * F * NF + f * NF + b];
+        p.Q[e * NQ * NL + (int64_t)cl * NQ + rq] = acc;
+      } else {
+        p.Q0[e * NQ + rq] = acc;
+      }
+      Qs[rq * (NL + 1) + cl] = acc;
+    }
+    __syncthreads();
+    // ------------------------------------------- S, S0 (+ Dirichlet Set)
+    for (int x = tid; x < NL * (NL + 1); x += kBT) {
+      const int row = x % NL, cl = x / NL;
+      const int f = row / NLF, a = (row % NLF) / ND, c = row % ND;
+      double v;
+      if (sBnd[f]) {
+        // Set: identity rows, face-ordered Dirichlet values as they are
+        v = cl < NL ? (cl == row ? 1.0 : 0.0) : p.dirichlet[(int64_t)sFace[f] * NLF + (row % NLF)];
+      } else {
+        double acc = 0.0;
+        for (int b = 0; b < NF; ++b) {
+          const int jn = sFaceNodes[f * NF + b];
+          for (int m = 0; m < ND; ++m)
+            acc += Tm[(((f * ND + c) * ND + m) * NF + a) * NF + b] * Aug[(jn * ND + m) * W + NU + cl];
+          if (diff)
+            for (int k = 0; k < D; ++k)
+              acc -= Hf[((f * D + k) * NF + a) * NF + b] * Qs[((jn * D + k) * ND + c) * (NL + 1) + cl];
+        }
+        if (cl < NL) {
+          const int f2 = cl / NLF, b = (cl % NLF) / ND, m = cl % ND;
+          if (f2 == f)
+            acc += -Tm[(((f * ND + c) * ND + m) * NF + a) * NF + b] + Cll[(f * NLF + a * ND + c) * NLF + b * ND + m];
+          v = acc;
+        } else {
+          v = Fl[row] - acc;
+        }
+      }
+      if (cl < NL) p.S[e * NL * NL + (int64_t)cl * NL + row] = v;
+      else p.S0[e * NL + row] = v;
+    }
+    __syncthreads();
+  }
+}
+
+template <int D, int P>
+cudaError_t launch_t(const BurgersParams& p, cudaStream_t s) {
+  using L = BL<D, P>;
+  const size_t bytes = sizeof(double) * L::TOTAL;
+  cudaError_t e = cudaFuncSetAttribute(burgers_local<D, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) return e;
+  int dev = 0, nsm = 0, perSM = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, burgers_local<D, P>, kBT, bytes);
+  if (e != cudaSuccess) return e;
+  if (perSM < 1) return cudaErrorInvalidConfiguration;
+  int64_t grid = (int64_t)nsm * perSM;
+  if (grid > p.nCells) grid = p.nCells;
+  burgers_local<D, P><<<(unsigned)(grid < 1 ? 1 : grid), kBT, bytes, s>>>(p);
+  return cudaGetLastError();
+}
+
+// Newton residual parts of NonLinearWrapper::vanillaResidualComputer
+// (NonLinearWrapper.cpp:14-34): sum (sol - buf)^2 and sum buf^2 per block, the
+// block sums added in block order by the last block (no atomics on the values).
+constexpr int kRT = 256;
+__global__ void __launch_bounds__(kRT) newton_residual(int64_t n, const double* __restrict__ sol,
+                                                       const double* __restrict__ buf, double* __restrict__ partials,
+                                                       unsigned* ticket, double* out) {
+  __shared__ double rd[kRT / 32], rb[kRT / 32];
+  __shared__ bool last;
+  double d2 = 0.0, b2 = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * kRT + threadIdx.x; i < n; i += (int64_t)gridDim.x * kRT) {
+    const double d = sol[i] - buf[i];
+    d2 += d * d;
+    b2 += buf[i] * buf[i];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    d2 += __shfl_down_sync(0xffffffffu, d2, o);
+    b2 += __shfl_down_sync(0xffffffffu, b2, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    rd[threadIdx.x >> 5] = d2;
+    rb[threadIdx.x >> 5] = b2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int k = 0; k < kRT / 32; ++k) {
+      a += rd[k];
+      b += rb[k];
+    }
+    partials[2 * blockIdx.x] = a;
+    partials[2 * blockIdx.x + 1] = b;
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    double a = 0.0, b = 0.0;
+    for (unsigned k = 0; k < gridDim.x; ++k) {
+      a += ((volatile double*)partials)[2 * k];
+      b += ((volatile double*)partials)[2 * k + 1];
+    }
+    out[0] = a;
+    out[1] = b;
+    *ticket = 0u;
+  }
+}
+
+// NonLinearWrapper::solve's update (NonLinearWrapper.cpp:64-70): both fields
+// become (1 - d) sol + d buf.
+__global__ void newton_update(int64_t n, double damp, double* __restrict__ sol, double* __restrict__ buf) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = (1.0 - damp) * sol[i] + damp * buf[i];
+    sol[i] = v;
+    buf[i] = v;
+  }
+}
+
+}  // namespace
+
+bool burgers_supported(int dim, int order) { return dim == 2 && order >= 1 && order <= 5; }
+
+size_t burgers_smem_bytes(int dim, int order) {
+  if (dim != 2) return 0;
+  switch (order) {
+    case 1: return sizeof(double) * BL<2, 1>::TOTAL;
+    case 2: return sizeof(double) * BL<2, 2>::TOTAL;
+    case 3: return sizeof(double) * BL<2, 3>::TOTAL;
+    case 4: return sizeof(double) * BL<2, 4>::TOTAL;
+    case 5: return sizeof(double) * BL<2, 5>::TOTAL;
+  }
+  return 0;
+}
+
+cudaError_t launch_burgers_local(int dim, int order, const BurgersParams& p, cudaStream_t s) {
+  if (dim == 2) switch (order) {
+      case 1: return launch_t<2, 1>(p, s);
+      case 2: return launch_t<2, 2>(p, s);
+      case 3: return launch_t<2, 3>(p, s);
+      case 4: return launch_t<2, 4>(p, s);
+      case 5: return launch_t<2, 5>(p, s);
+    }
+  return cudaErrorInvalidValue;
+}
+
+constexpr int kResidualBlocks = 152 * 2;
+size_t newton_partials_needed() { return 2 * kResidualBlocks; }
+
+cudaError_t launch_newton_residual(int64_t n, const double* sol, const double* buf, double* partials,
+                                   unsigned* ticket, double* out, cudaStream_t s) {
+  int64_t g = (n + kRT - 1) / kRT;
+  if (g > kResidualBlocks) g = kResidualBlocks;
+  newton_residual<<<(unsigned)(g < 1 ? 1 : g), kRT, 0, s>>>(n, sol, buf, partials, ticket, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_newton_update(int64_t n, double damp, double* sol, double* buf, cudaStream_t s) {
+  int64_t g = (n + 255) / 256;
+  if (g > 152 * 16) g = 152 * 16;
+  newton_update<<<(unsigned)(g < 1 ? 1 : g), 256, 0, s>>>(n, damp, sol, buf);
+  return cudaGetLastError();
+}
+
+}  // namespace hfx

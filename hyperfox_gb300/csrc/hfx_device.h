@@ -75,6 +75,40 @@ struct LocalParams {
 
 cudaError_t launch_local_condense(int dim, int order, const LocalParams& p, cudaStream_t s);
 
+// Vector Burgers element kernel (hdg_burgers.cu): nd = dim unknowns per node.
+struct BurgersParams {
+  int nCells;
+  const double* coords;        // [nNodes][D]
+  const int* cells;            // [nCells][N]
+  const int* cell2face;        // [nCells][F]
+  const uint8_t* perm;         // [nCells][F][NF] face2CellMap (node level)
+  const int* face2cell;        // [nFaces][2]
+  const uint8_t* isBoundary;   // [nFaces]
+  const double* tau;           // [nFaces][NF][tauSides][ND*ND], ND x ND column-major
+  int tauSides;                // 1 or 2 (double valued)
+  const double* nu;            // diffusion tensor: layout 0 [nNodes][kc], 1 [nCells][N][kc]
+  int kc, nuLayout;            // kc 0 = no diffusion operator, 1 scalar, D*D tensor
+  const double* src;           // [nCells][NI][ND] source at the IPs, or nullptr
+  const double* dirichlet;     // [nFaces][NF*ND] face order
+  double dt;                   // > 0: implicit Euler about uOld
+  const double* uOld;          // [nCells][N*ND]
+  const double* buf;           // BufferSolution [nCells][N*ND] (linearisation point)
+  const double* trace;         // Trace [nFaces][NF*ND]
+  const double* tab;           // phi, dphi, w, fphi, fdphi, fw
+  const int* itab;             // faceNodes[F*NF], faceOpposite[F]
+  double *S, *S0, *U, *Q, *U0, *Q0;
+  int* status;                 // 1 = singular Schur block
+};
+bool burgers_supported(int dim, int order);
+size_t burgers_smem_bytes(int dim, int order);
+cudaError_t launch_burgers_local(int dim, int order, const BurgersParams& p, cudaStream_t s);
+// NonLinearWrapper pieces: out[0] = sum (sol - buf)^2, out[1] = sum buf^2 (deterministic
+// block order); then both fields <- (1 - damp) sol + damp buf
+size_t newton_partials_needed();
+cudaError_t launch_newton_residual(int64_t n, const double* sol, const double* buf, double* partials,
+                                   unsigned* ticket, double* out, cudaStream_t s);
+cudaError_t launch_newton_update(int64_t n, double damp, double* sol, double* buf, cudaStream_t s);
+
 // out[i] = alpha a[i] + sum_j coef[j] ptr[j][i] (rk.cu), element by element (out may alias an input)
 struct RkTerms {
   static constexpr int MAX = 8;

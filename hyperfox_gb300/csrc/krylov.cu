@@ -1224,7 +1224,18 @@ static void residual_t(const TraceSolveArgs& a, TraceSolveResult* out) {
     }                                                                       \
   } while (0)
 
-void trace_prepare(const TraceSolveArgs& a) { HFX_DISPATCH_NF(prepare_t, a); }
+// The same dispatch with the vector (Burgers) trace blocks of 2D cells, Nf*dim = 8, 10, 12
+// (p = 3, 4, 5), which only the FP64 GMRES path uses.
+#define HFX_DISPATCH_NF_VEC(fn, ...)                                        \
+  do {                                                                      \
+    const int NFV_ = a.A.NF;                                                \
+    if (a.dim == 2 && NFV_ == 8) fn<8, 5>(__VA_ARGS__);                     \
+    else if (a.dim == 2 && NFV_ == 10) fn<10, 5>(__VA_ARGS__);              \
+    else if (a.dim == 2 && NFV_ == 12) fn<12, 5>(__VA_ARGS__);              \
+    else HFX_DISPATCH_NF(fn, __VA_ARGS__);                                  \
+  } while (0)
+
+void trace_prepare(const TraceSolveArgs& a) { HFX_DISPATCH_NF_VEC(prepare_t, a); }
 
 template <int NF, int NBMAX>
 static void prepare_f32_t(const TraceView& A, const float* val, const float* rhs, float* bS, int pcType, float* pc,
@@ -1298,6 +1309,6 @@ int trace_solve_f32(const F32SolveArgs& a, int* its) {
   HFX_DISPATCH_NF(cg_f32_t, a, its, &status);
   return status;
 }
-void trace_ref_residual(const TraceSolveArgs& a, TraceSolveResult* out) { HFX_DISPATCH_NF(residual_t, a, out); }
+void trace_ref_residual(const TraceSolveArgs& a, TraceSolveResult* out) { HFX_DISPATCH_NF_VEC(residual_t, a, out); }
 
 }  // namespace hfx

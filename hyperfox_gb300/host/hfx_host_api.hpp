@@ -6,11 +6,15 @@
 //                                       field map Solution/Flux/Trace/Tau/Dirichlet
 //   hfx::gpu::Mesh / Field / models   ~ the parts of Mesh, Field, HDGDiffusionSource,
 //                                       HDGLaplaceModel and DirichletModel the path reads
+//   hfx::gpu::GpuBurgersSolver        ~ HDGSolver with HDGBurgersModel (vector Burgers)
+//   hfx::gpu::NonLinearWrapper        ~ NonLinearWrapper (NonLinearWrapper.h:14-128)
 // Errors throw ErrorHandle(class, method, message) exactly where HyperFox
 // throws (calls out of order, missing fields); device failures carry the
 // library's message.
 #pragma once
 #include <cmath>
+#include <cstdio>
+#include <functional>
 #include <map>
 #include <stdexcept>
 #include <string>
@@ -390,6 +394,234 @@ class GpuHDGSolver {
   DirichletModel* bnd_ = nullptr;
   GpuSolverOpts opts_;
   bool haveLin_ = false, initialized_ = false, allocated_ = false, assembled_ = false, trained_ = false;
+};
+
+// ---------------------------------------------------------------- Burgers / Newton
+// Euler (src/operator/Euler.h): implicit Euler on the U rows; the model reads the
+// field map's OldSolution as u_old when there is one, else its Solution (the field
+// Euler::setFieldMap takes, Euler.cpp:7-16).
+struct Euler {
+  double dt = 0.0;
+  void setTimeStep(double t) { dt = t; }
+};
+
+// HDGBurgersModel (src/model/HDGBurgersModel.h): vector Burgers, nd = dim unknowns
+// per node; one Source per component given at the volume IPs ([nCells][nIP][nd],
+// the values HDGBurgersModel::setSourceFunction's functor would return there).
+struct HDGBurgersModel {
+  std::vector<double> sourceValues;
+  Euler* timeScheme = nullptr;
+  void setTimeScheme(Euler* ts) { timeScheme = ts; }
+};
+
+// HDGSolver with HDGBurgersModel (HDGSolver.cpp:5-175,677-779): the field map needs
+// Solution, BufferSolution, Flux, Trace, Tau and Dirichlet with nd values per node
+// (HDGBurgersModel::setFieldMap, HDGBurgersModel.cpp:5-33); DiffusionTensor (Node or
+// Cell field, 1 or dim*dim values) adds the diffusion operator. Tau may be double
+// valued (2*nd*nd values per face node). assemble() linearises about BufferSolution
+// and Trace; solve() writes Trace, Solution and Flux back into the field map.
+class GpuBurgersSolver {
+ public:
+  explicit GpuBurgersSolver(Device* dev) : dev_(dev) {}
+  void setMesh(Mesh* m) { mesh_ = m; }
+  void setFieldMap(std::map<std::string, Field*>* fm) { fields_ = fm; }
+  void setModel(HDGBurgersModel* m) { model_ = m; }
+  void setBoundaryModel(DirichletModel* b) { bnd_ = b; }
+  void setLinSystem(GpuSolverOpts opts) { opts_ = opts; haveLin_ = true; }
+  void initialize() { initialized_ = true; }
+
+  void allocate() {
+    if (!initialized_) throw ErrorHandle("HDGSolver", "allocate", "must initialize the solver before allocating.");
+    if (!mesh_) throw ErrorHandle("HDGSolver", "allocate", "must set the Mesh before allocating.");
+    if (!haveLin_) throw ErrorHandle("HDGSolver", "allocate", "must set the linear system before allocating.");
+    if (!model_) throw ErrorHandle("HDGSolver", "allocate", "must set the model before allocating.");
+    if (!bnd_) throw ErrorHandle("HDGSolver", "allocate", "must set the boundary model before allocating.");
+    if (!fields_ || fields_->empty()) throw ErrorHandle("HDGSolver", "allocate", "must set the fields before allocating.");
+    for (const char* f : {"Solution", "BufferSolution", "Flux", "Tau", "Trace", "Dirichlet"})
+      if (!fields_->count(f))
+        throw ErrorHandle("HDGBurgersModel", "setFieldMap", std::string("the field map must have a ") + f + " field");
+    const int nd = mesh_->dim;
+    if (fields_->at("BufferSolution")->vals != nd || fields_->at("Solution")->vals != nd)
+      throw ErrorHandle("HDGBurgersModel", "setFieldMap",
+                        "the BufferSolution must have the same number of DOFs per node as spatial dimensions for the "
+                        "Burgers equation");
+    if (fields_->at("Trace")->vals != nd)
+      throw ErrorHandle("HDGBurgersModel", "setFieldMap",
+                        "the Trace must have the same number of DOFs per node as spatial dimensions for the Burgers "
+                        "equation");
+    const int tv = fields_->at("Tau")->vals;
+    if (tv != nd * nd && tv != 2 * nd * nd)
+      throw ErrorHandle("HDGBurgersModel", "setFieldMap", "the Tau field holds nd*nd (or 2*nd*nd) values per node");
+    mesh_->computeFaces();
+    dev_->check(hfx_mesh_upload(dev_->ctx(), mesh_->dim, mesh_->order, mesh_->numNodes(), mesh_->nodes.data(),
+                                mesh_->numCells(), mesh_->cells.data(), mesh_->nFaces, mesh_->cell2face.data(),
+                                mesh_->face2cell.data(), mesh_->faces.data(), (int)mesh_->boundary.size(),
+                                mesh_->boundary.data()),
+                "HDGSolver", "allocate");
+    dev_->check(hfx_burgers_setup(dev_->ctx()), "HDGSolver", "allocate");
+    allocated_ = true;
+  }
+
+  // every field of the map to the device (HDGSolver::assemble's field gather)
+  void upload() {
+    hfx_ctx* c = dev_->ctx();
+    const int nd = mesh_->dim;
+    Field* tau = fields_->at("Tau");
+    dev_->check(hfx_burgers_set_tau(c, tau->values.data(), tau->vals / (nd * nd)), "HDGSolver", "assemble");
+    dev_->check(hfx_burgers_set_dirichlet(c, fields_->at("Dirichlet")->values.data()), "HDGSolver", "assemble");
+    if (fields_->count("DiffusionTensor")) {
+      Field* k = fields_->at("DiffusionTensor");
+      dev_->check(hfx_burgers_set_diffusion(c, k->values.data(), k->vals, k->type == Node ? 0 : 1), "HDGSolver",
+                  "assemble");
+    } else {
+      dev_->check(hfx_burgers_set_diffusion(c, nullptr, 0, 0), "HDGSolver", "assemble");
+    }
+    dev_->check(hfx_burgers_set_source(c, model_->sourceValues.empty() ? nullptr : model_->sourceValues.data()),
+                "HDGSolver", "assemble");
+    const double dt = model_->timeScheme ? model_->timeScheme->dt : 0.0;
+    if (model_->timeScheme && dt == 0.0)
+      throw ErrorHandle("Euler", "apply", "the time step needs to be set before applying and it should not be 0");
+    dev_->check(hfx_burgers_set_time_step(c, dt), "HDGSolver", "assemble");
+    const Field* old = dt > 0.0 ? (fields_->count("OldSolution") ? fields_->at("OldSolution") : fields_->at("Solution"))
+                                : nullptr;
+    dev_->check(hfx_burgers_set_state(c, fields_->at("Solution")->values.data(),
+                                      fields_->at("BufferSolution")->values.data(), fields_->at("Trace")->values.data(),
+                                      old ? old->values.data() : nullptr),
+                "HDGSolver", "assemble");
+  }
+
+  void assemble() {
+    if (!(initialized_ && allocated_))
+      throw ErrorHandle("HDGSolver", "assemble", "the solver must be initialized and allocated before assembling.");
+    upload();
+    dev_->check(hfx_burgers_assemble(dev_->ctx()), "HDGSolver", "assemble");
+    assembled_ = true;
+  }
+
+  void solve() {
+    if (!assembled_) throw ErrorHandle("HDGSolver", "solve", "system must be assembled before solving");
+    hfx_solve_opts o = linOpts();
+    dev_->check(hfx_burgers_solve(dev_->ctx(), &o, &lastInfo), "HDGSolver", "solve");
+    download(false);
+  }
+
+  hfx_solve_opts linOpts() const {
+    hfx_solve_opts o;
+    hfx_solve_opts_default(&o);
+    o.method = HFX_KSP_GMRES;
+    o.precond = opts_.precond;
+    o.rtol = opts_.rtol;
+    o.maxits = opts_.maxits;
+    o.restart = opts_.restart;
+    return o;
+  }
+  // Solution, Flux, Trace (and BufferSolution) back into the field map
+  void download(bool withBuffer) {
+    dev_->check(hfx_burgers_get_state(dev_->ctx(), fields_->at("Solution")->values.data(),
+                                      fields_->at("Flux")->values.data(), fields_->at("Trace")->values.data(),
+                                      withBuffer ? fields_->at("BufferSolution")->values.data() : nullptr),
+                "HDGSolver", "solve");
+  }
+  bool allocated() const { return allocated_; }
+  Device* device() { return dev_; }
+  std::map<std::string, Field*>* fieldMap() { return fields_; }
+  hfx_solve_info lastInfo{};
+
+ private:
+  Device* dev_;
+  Mesh* mesh_ = nullptr;
+  std::map<std::string, Field*>* fields_ = nullptr;
+  HDGBurgersModel* model_ = nullptr;
+  DirichletModel* bnd_ = nullptr;
+  GpuSolverOpts opts_;
+  bool haveLin_ = false, initialized_ = false, allocated_ = false, assembled_ = false;
+};
+
+// NonLinearWrapper (src/solver/NonLinearWrapper.h, NonLinearWrapper.cpp:5-79). With
+// the vanilla linearised solver and residual computer and the solver's own
+// Solution / BufferSolution as the solution fields, solve() runs the whole loop on
+// the device (hfx_burgers_newton) and copies the fields back at the end; a user
+// linearised solver or residual computer runs the reference's loop on the host.
+class NonLinearWrapper {
+ public:
+  void solve() {
+    if (!mySolver) throw ErrorHandle("NonLinearWrapper", "solve", "the Solver must be set before attempting to solve");
+    if (!currentSolution || !previousSolution)
+      throw ErrorHandle("NonLinearWrapper", "solve", "the current and previous Solutions should be set before attempting to solve");
+    std::map<std::string, Field*>* fm = mySolver->fieldMap();
+    const bool deviceLoop = !linearizedSolver && !residualComputer && mySolver->allocated() && fm &&
+                            fm->count("Solution") && fm->at("Solution") == currentSolution &&
+                            fm->count("BufferSolution") && fm->at("BufferSolution") == previousSolution;
+    if (deviceLoop) {
+      mySolver->upload();
+      hfx_newton_opts o;
+      hfx_newton_opts_default(&o);
+      o.res_tol = resTol;
+      o.max_iters = maxIters;
+      o.dampening = dampening;
+      o.lin = mySolver->linOpts();
+      o.warm_start = warmStart ? 1 : 0;
+      mySolver->device()->check(hfx_burgers_newton(mySolver->device()->ctx(), &o, &lastInfo), "NonLinearWrapper",
+                                "solve");
+      residual = lastInfo.residual;
+      mySolver->download(true);
+      return;
+    }
+    for (int i = 0; i < maxIters; ++i) {
+      if (linearizedSolver) linearizedSolver(mySolver);
+      else {
+        mySolver->assemble();
+        mySolver->solve();
+      }
+      residual = residualComputer ? residualComputer(currentSolution, previousSolution)
+                                  : vanillaResidual(currentSolution, previousSolution);
+      if (verbose) std::printf("\rIteration %d at residual value %f", i + 1, residual);
+      if (residual < resTol) break;
+      std::vector<double>& cur = currentSolution->values;
+      std::vector<double>& prev = previousSolution->values;
+      for (size_t k = 0; k < cur.size(); ++k) {
+        const double v = (1.0 - dampening) * cur[k] + dampening * prev[k];
+        cur[k] = v;
+        prev[k] = v;
+      }
+    }
+    if (verbose) std::printf("\n");
+  }
+  double getResidual() const { return residual; }
+  void setResidualTolerance(double tol) { resTol = tol; }
+  void setMaxIterations(int iters) { maxIters = iters; }
+  void setVerbosity(bool v) { verbose = v; }
+  void setSolutionFields(Field* currentSol, Field* prevSol) {
+    currentSolution = currentSol;
+    previousSolution = prevSol;
+  }
+  void setSolver(GpuBurgersSolver* solver) { mySolver = solver; }
+  void setResidualComputer(std::function<double(Field*, Field*)> f) { residualComputer = f; }
+  void setLinearizedSolver(std::function<void(GpuBurgersSolver*)> f) { linearizedSolver = f; }
+  void setDampening(double d) { dampening = d; }
+  // start every Krylov solve from the current trace (PETSc starts from zero)
+  void setWarmStart(bool on) { warmStart = on; }
+  hfx_newton_info lastInfo{};
+
+  // NonLinearWrapper::vanillaResidualComputer (NonLinearWrapper.cpp:14-34), one rank
+  static double vanillaResidual(Field* cur, Field* prev) {
+    double diff = 0.0, ref = 0.0;
+    for (size_t i = 0; i < cur->values.size(); ++i) {
+      diff += (cur->values[i] - prev->values[i]) * (cur->values[i] - prev->values[i]);
+      ref += prev->values[i] * prev->values[i];
+    }
+    return ref != 0.0 ? std::sqrt(diff / ref) : std::sqrt(diff);
+  }
+
+ private:
+  GpuBurgersSolver* mySolver = nullptr;
+  Field* currentSolution = nullptr;
+  Field* previousSolution = nullptr;
+  std::function<double(Field*, Field*)> residualComputer;
+  std::function<void(GpuBurgersSolver*)> linearizedSolver;
+  double residual = 0.0, resTol = 1e-6, dampening = 0.0;
+  int maxIters = 20;
+  bool verbose = false, warmStart = false;
 };
 
 // ---------------------------------------------------------------- HDF5Io

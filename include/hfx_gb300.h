@@ -345,6 +345,80 @@ int hfx_la_clear(hfx_la* la);
 int hfx_la_solve(hfx_la* la, const hfx_solve_opts* opts, double* x, hfx_solve_info* info);
 int hfx_la_nnz(hfx_la* la, int64_t* nnz);
 
+/* ---- viscous Burgers, Newton (HDGBurgersModel, HDGUNabU, NonLinearWrapper) ----
+ * Vector Burgers with nd = dim unknowns per node (HDGBurgersModel.cpp:35-60): local
+ * matrix HDGBase + HDGUNabU (+ HDGDiffusion when a diffusion tensor is set), RHS the
+ * HDGUNabU RHS + one Source per component, optional implicit Euler (Euler.cpp:18-34),
+ * linearised about BufferSolution and Trace (HDGBurgersModel.cpp:5-33). Built for 2D
+ * cells, p = 1..5; uses the mesh of hfx_mesh_upload and its own fields and outputs
+ * (the scalar path's are untouched). Layouts, nd = dim:
+ *   Tau          [nFaces][nNodesPerFace][sides][nd*nd]  nd x nd column-major, sides 1 or 2
+ *   Dirichlet    [nFaces][nNodesPerFace][nd]            face order (added to the local rows as
+ *                                                       they are, HDGSolver.cpp:493-497)
+ *   Source       [nCells][nIP][nd]                      f_c at the volume IPs
+ *   Solution, BufferSolution, OldSolution [nCells][nNodesPerCell][nd]
+ *   Flux         [nCells][nNodesPerCell][dim][nd]       (local Q order)
+ *   Trace        [nFaces][nNodesPerFace][nd]            global DOF (face*Nf + node)*nd + k
+ *   S,S0,U,Q,U0,Q0 per element, column-major, lenU = N*nd, lenQ = dim*N*nd, lenL = F*Nf*nd */
+typedef struct {
+  double res_tol;          /* NonLinearWrapper::setResidualTolerance (default 1e-6) */
+  int max_iters;           /* NonLinearWrapper::setMaxIterations (default 20) */
+  double dampening;        /* NonLinearWrapper::setDampening (default 0) */
+  hfx_solve_opts lin;      /* the linear solve of every iteration (GMRES, block Jacobi) */
+  int warm_start;          /* 1: each Krylov solve starts from the current trace (PETSc starts
+                              from zero, KSPSetInitialGuessNonzero is not called) */
+} hfx_newton_opts;
+
+typedef struct {
+  int status;              /* HFX_OK, or the linear solve's / element kernel's error */
+  int iterations;          /* Newton iterations run */
+  double residual;         /* last ||Solution - BufferSolution|| / ||BufferSolution|| */
+  int krylov_iterations;   /* summed over the iterations */
+  double assemble_ms, solve_ms, recover_ms;  /* device times, summed */
+} hfx_newton_info;
+
+/* HDGSolver::allocate with HDGBurgersModel (HDGSolver.cpp:81-115, HDGBurgersModel.cpp:35-60):
+ * device fields and outputs; defaults tau = I, no diffusion, no source, Dirichlet 0, stationary,
+ * every state field 0. */
+int hfx_burgers_setup(hfx_ctx* ctx);
+/* Tau field (HDGBase::setTau, HDGBase.cpp:18-32; double valued when sides == 2). */
+int hfx_burgers_set_tau(hfx_ctx* ctx, const double* tau, int sides);
+/* DiffusionTensor (HDGBurgersModel::parseDiffusionVals, HDGBurgersModel.cpp:128-150): comps 1
+ * (scalar) or dim*dim per node; layout 0 per mesh node [nNodes][comps], 1 per cell node
+ * [nCells][N][comps]; nu == NULL or comps == 0: no diffusion operator. */
+int hfx_burgers_set_diffusion(hfx_ctx* ctx, const double* nu, int comps, int layout);
+/* One Source per component (HDGBurgersModel::setSourceFunction, HDGBurgersModel.cpp:80-89), given
+ * at the volume IPs; NULL: none. */
+int hfx_burgers_set_source(hfx_ctx* ctx, const double* values);
+int hfx_burgers_set_dirichlet(hfx_ctx* ctx, const double* values);
+/* Euler::setTimeStep (Euler.h): dt > 0 applies implicit Euler about OldSolution; 0 = stationary. */
+int hfx_burgers_set_time_step(hfx_ctx* ctx, double dt);
+/* Upload fields; a NULL pointer leaves that field as it is. */
+int hfx_burgers_set_state(hfx_ctx* ctx, const double* solution, const double* buffer, const double* trace,
+                          const double* oldSolution);
+/* Download fields; a NULL pointer skips that field. */
+int hfx_burgers_get_state(hfx_ctx* ctx, double* solution, double* flux, double* trace, double* buffer);
+/* A time step's field copies on the device (TestHDGBurgers.cpp:362-365): BufferSolution and
+ * OldSolution <- Solution. */
+int hfx_burgers_begin_step(hfx_ctx* ctx);
+/* HDGSolver::assemble with the Burgers model (HDGSolver.cpp:166-174): element kernel
+ * (assembly + condensation + Dirichlet Set) and the scatter into the trace system. */
+int hfx_burgers_assemble(hfx_ctx* ctx);
+/* HDGSolver::solve (HDGSolver.cpp:677-779): GMRES on the trace system (PetscInterface::solve,
+ * PetscInterface.cpp:222-247), Trace <- the solution, then the local recovery of Solution and Flux. */
+int hfx_burgers_solve(hfx_ctx* ctx, const hfx_solve_opts* opts, hfx_solve_info* info);
+/* NonLinearWrapper::solve (NonLinearWrapper.cpp:41-79) with the vanilla linearised solver and
+ * residual (assemble + solve; ||Solution - BufferSolution|| / ||BufferSolution||), run on the
+ * device: the host reads two numbers per iteration. opts/info may be NULL. Returns HFX_OK also
+ * when max_iters ends the loop (as the reference); info->residual says where it stopped. */
+void hfx_newton_opts_default(hfx_newton_opts* opts);
+int hfx_burgers_newton(hfx_ctx* ctx, const hfx_newton_opts* opts, hfx_newton_info* info);
+int hfx_burgers_get_condensed(hfx_ctx* ctx, double* S, double* S0, double* U, double* Q, double* U0,
+                              double* Q0);
+/* The assembled trace system in PETSc's AIJ layout (sorted columns, explicit zeros kept). */
+int hfx_burgers_nnz(hfx_ctx* ctx, int64_t* nnz);
+int hfx_burgers_get_csr(hfx_ctx* ctx, int64_t* rowptr, int* col, double* val, double* rhs);
+
 /* ---- allocation-free trace solve -------------------------------------------
  * No counterpart in the reference. For callers that cannot allocate device
  * memory: code running while a stream is captured into a CUDA graph, code

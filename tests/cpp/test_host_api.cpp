@@ -2,6 +2,7 @@
 // (TestLinAlgebraInterfaces.cpp:23-150, TestHDGSolver.cpp:14-101, TestHDF5Io.cpp
 // write mesh / write field sections).
 // Exits non-zero on the first failed check.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <functional>
@@ -239,6 +240,139 @@ int main(int argc, char** argv) {
     for (double v : sol.values) CHECK(std::fabs(v - 3.0) < 1e-10);
     for (double v : lambda.values) CHECK(std::fabs(v - 3.0) < 1e-10);
     for (double v : flux.values) CHECK(std::fabs(v) < 1e-9);
+  }
+  {  // NonLinearWrapper with a user linearised solver (TestNonLinearWrapper.cpp:10-47):
+     // x <- x - x^2 / (2x) halves x, the relative change stays 1/2, max iterations end the loop
+    Mesh m;
+    m.dim = 2;
+    m.order = 1;
+    m.nodes = {0, 0, 1, 0, 0, 1};
+    m.cells = {0, 1, 2};
+    Field sol(&m, Node, 1, 1), interSol(&m, Node, 1, 1);
+    GpuBurgersSolver dummy(&dev);
+    NonLinearWrapper wrap;
+    CHECK(throws([&] { wrap.solve(); }));
+    wrap.setVerbosity(false);
+    wrap.setSolver(&dummy);
+    CHECK(throws([&] { wrap.solve(); }));
+    wrap.setSolutionFields(&sol, &interSol);
+    wrap.setLinearizedSolver([&](GpuBurgersSolver*) {
+      for (size_t i = 0; i < sol.values.size(); ++i)
+        sol.values[i] = interSol.values[i] - interSol.values[i] * interSol.values[i] / (2.0 * interSol.values[i]);
+    });
+    for (double start : {1.0, 2.0, -1.0, 0.25, 42.0, 1e-8}) {
+      std::fill(interSol.values.begin(), interSol.values.end(), start);
+      std::fill(sol.values.begin(), sol.values.end(), 0.0);
+      wrap.solve();
+      CHECK(std::fabs(wrap.getResidual() - 0.5) < 1e-12);
+      for (double v : interSol.values) CHECK(std::fabs(v) < 1e-4 * std::max(1.0, std::fabs(start)) * 50);
+    }
+  }
+  {  // stationary Burgers, Cole-Hopf solution (TestHDGBurgersStat.cpp:107-399) through
+     // GpuBurgersSolver + NonLinearWrapper: the device loop and the host loop agree
+    const int p = 2, n = 4;
+    Mesh m;
+    m.dim = 2;
+    m.order = p;
+    hfx_refel_info info;
+    hfx_refel_query(2, p, &info);
+    std::vector<double> rn(info.nNodes * 2);
+    hfx_refel_tables(2, p, rn.data(), nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+    auto node_id = [&](double x, double y) {
+      for (size_t k = 0; k < m.nodes.size() / 2; ++k)
+        if (std::fabs(m.nodes[2 * k] - x) < 1e-12 && std::fabs(m.nodes[2 * k + 1] - y) < 1e-12) return (int)k;
+      m.nodes.push_back(x);
+      m.nodes.push_back(y);
+      return (int)(m.nodes.size() / 2 - 1);
+    };
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        double h = 1.0 / n, x0 = i * h, y0 = j * h;
+        double tri[2][3][2] = {{{x0, y0}, {x0 + h, y0}, {x0, y0 + h}}, {{x0 + h, y0 + h}, {x0, y0 + h}, {x0 + h, y0}}};
+        for (auto& t : tri)
+          for (int a = 0; a < info.nNodes; ++a) {
+            double l1 = 0.5 * (rn[2 * a] + 1), l2 = 0.5 * (rn[2 * a + 1] + 1);
+            m.cells.push_back(node_id(t[0][0] + l1 * (t[1][0] - t[0][0]) + l2 * (t[2][0] - t[0][0]),
+                                      t[0][1] + l1 * (t[1][1] - t[0][1]) + l2 * (t[2][1] - t[0][1])));
+          }
+      }
+    const double D = 1.0, A = 0.5;
+    auto exact = [&](double x, double y, double* u) {
+      const double ep = std::exp(A * (x - 1.0)), em = std::exp(-A * (x - 1.0));
+      const double phi = 0.001 * A * std::exp(2.0 * A) * (1 + x) + (ep + em) * std::cos(A * y);
+      u[0] = -2 * D * (0.001 * A * std::exp(2.0 * A) + A * (ep - em) * std::cos(A * y)) / phi;
+      u[1] = -2 * D * (-A * (ep + em) * std::sin(A * y)) / phi;
+    };
+    Field sol(&m, Cell, info.nNodes, 2), buf(&m, Cell, info.nNodes, 2), flux(&m, Cell, info.nNodes, 4);
+    Field trace(&m, Face, info.nNodesFace, 2), dir(&m, Face, info.nNodesFace, 2), tau(&m, Face, info.nNodesFace, 8);
+    Field nu(&m, Node, 1, 1);
+    std::fill(nu.values.begin(), nu.values.end(), D);
+    for (int f = 0; f < m.nFaces; ++f)
+      for (int a = 0; a < info.nNodesFace; ++a) {
+        const int node = m.faces[(size_t)f * info.nNodesFace + a];
+        exact(m.nodes[2 * node], m.nodes[2 * node + 1], &dir.values[((size_t)f * info.nNodesFace + a) * 2]);
+        for (int side = 0; side < 2; ++side) {
+          double* t = &tau.values[(((size_t)f * info.nNodesFace + a) * 2 + side) * 4];
+          t[0] = t[3] = 2.0 * D * n;  // (D / h) * 2 * I
+        }
+      }
+    std::map<std::string, Field*> fm{{"Solution", &sol}, {"BufferSolution", &buf}, {"Flux", &flux},
+                                     {"Trace", &trace}, {"Tau", &tau}, {"Dirichlet", &dir},
+                                     {"DiffusionTensor", &nu}};
+    DirichletModel dirMod;
+    HDGBurgersModel bm;
+    GpuSolverOpts o;
+    o.precond = HFX_PC_BLOCK_JACOBI;
+    o.rtol = 1e-13;
+    o.maxits = 20000;
+    GpuBurgersSolver s(&dev);
+    CHECK(throws([&] { s.assemble(); }));
+    s.setMesh(&m);
+    s.setFieldMap(&fm);
+    s.setLinSystem(o);
+    s.setModel(&bm);
+    s.setBoundaryModel(&dirMod);
+    s.initialize();
+    s.allocate();
+    NonLinearWrapper w;
+    w.setSolver(&s);
+    w.setSolutionFields(&sol, &buf);
+    w.setMaxIterations(10);
+    w.setResidualTolerance(1e-8);
+    w.solve();  // vanilla: the loop runs on the device
+    CHECK(w.lastInfo.iterations > 1 && w.lastInfo.iterations < 10 && w.getResidual() < 1e-8);
+    std::vector<double> devSol = sol.values;
+    double err2 = 0.0, ref2 = 0.0;
+    for (int e = 0; e < m.numCells(); ++e)
+      for (int a = 0; a < info.nNodes; ++a) {
+        const int node = m.cells[(size_t)e * info.nNodes + a];
+        double u[2];
+        exact(m.nodes[2 * node], m.nodes[2 * node + 1], u);
+        for (int k = 0; k < 2; ++k) {
+          const double d = sol.values[((size_t)e * info.nNodes + a) * 2 + k] - u[k];
+          err2 += d * d;
+          ref2 += u[k] * u[k];
+        }
+      }
+    CHECK(std::sqrt(err2 / ref2) < 1e-3);  // the reference asserts l2Err < 1
+    // the same loop on the host (a user residual computer selects it)
+    std::fill(sol.values.begin(), sol.values.end(), 0.0);
+    std::fill(buf.values.begin(), buf.values.end(), 0.0);
+    std::fill(trace.values.begin(), trace.values.end(), 0.0);
+    NonLinearWrapper wh;
+    wh.setSolver(&s);
+    wh.setSolutionFields(&sol, &buf);
+    wh.setMaxIterations(10);
+    wh.setResidualTolerance(1e-8);
+    wh.setResidualComputer(NonLinearWrapper::vanillaResidual);
+    wh.solve();
+    double dmax = 0.0, smax = 0.0;
+    for (size_t i = 0; i < sol.values.size(); ++i) {
+      dmax = std::max(dmax, std::fabs(sol.values[i] - devSol[i]));
+      smax = std::max(smax, std::fabs(devSol[i]));
+    }
+    CHECK(dmax < 1e-10 * smax);
+    CHECK(std::fabs(wh.getResidual() - w.getResidual()) < 1e-3 * w.getResidual() + 1e-12);
   }
   std::printf("%s (%d failures)\n", failures ? "FAIL" : "OK", failures);
   return failures ? 1 : 0;
