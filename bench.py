@@ -54,6 +54,8 @@ CONFIGS = {
     "cfg4": dict(dim=2, n=180, order=3, burgers=True, nu=1e-2, dt=1e-3, time_steps=200,
                  desc="2D viscous Burgers HDG, unit square 180x180x2 tris (64,800), p=3, nu=1e-2, "
                       "implicit Euler dt=1e-3, Newton to 1e-6 every step"),
+    "burgers-mid": dict(dim=2, n=96, order=3, burgers=True, nu=1e-2, dt=1e-3, time_steps=20,
+                        desc="2D viscous Burgers HDG, 96x96x2 tris (18,432), p=3, nu=1e-2, dt=1e-3"),
     "burgers-small": dict(dim=2, n=48, order=3, burgers=True, nu=1e-2, dt=1e-3, time_steps=20,
                           desc="2D viscous Burgers HDG, 48x48x2 tris (4,608), p=3, nu=1e-2, dt=1e-3"),
 }
@@ -392,15 +394,17 @@ def burgers_flops_per_element(N, NF, F, NI, NIF, D=2):
     NU, NQ, NLF = N * ND, D * N * ND, NF * ND
     NL = F * NLF
     W = NU + NL + 1
-    ops = 2 * NI * N * D * D + 2 * NI * N * D * D * (N + 1)            # G, K G
+    ops = 2 * NI * D * D * N + 4 * NI * N * D * D                     # Ds at the IPs, G, Ds G
     ops += F * NIF * (4 * ND * NF + 2 * NT * NF + 2 * D * D * NF + 4 * D)  # face IP values
-    ops += 2 * NI * N * ND + 2 * NI * N * D                              # u, div u at the IPs
-    ops += N * N * NI * (2 + 4 * D)                                      # M, C_k, K'_k
+    ops += 2 * NI * N * ND + 2 * NI * N * D + NI * N * (2 * D + 3 + 2 * ND)  # u, div u, AQ, BQ
+    ops += N * N * NI * (4 + 4 * D)                                      # M, T1, C_k, K'_k
     ops += F * NF * NF * NIF * (4 * D + 2 * NT)                          # E, H, tau masses
-    ops += F * NLF * NLF * NIF * 6 + NU * NU * NI * 12                  # convection blocks
-    ops += N * (N - 1) * 2 * N * 2 + 2 * D * N * N * N + 2 * D * N * F * NF * NF  # M^-1, M^-1 C, M^-1 E
-    ops += NU * NU * 4 * D * N + NU * NL * 4 * D * N + NU * (2 * NU + 2 * NL)      # [A | -B | Fu]
-    ops += sum(2 * (NU - 1) * (W - k - 1) for k in range(NU))           # Gauss-Jordan
+    ops += F * NLF * NLF * NIF * 6 + NU * NU * (2 * NI + 2)             # convection blocks
+    ops += sum(2 * (N - 1) * (2 * N - k - 1) + (2 * N - k - 1) for k in range(N))  # M^-1 (Gauss-Jordan)
+    ops += 2 * D * N * N * N + 2 * D * N * F * NF * NF                  # M^-1 C, M^-1 E
+    ops += 2 * D * N * (N * N + N * F * NF)                             # sum_k K' M^-1 C, K' M^-1 E
+    ops += NU * NU * 6 + NU * NL * 6 + NU * (2 * NU + 2 * NL + 2 * NI + 2 * N)  # [A | -B | Fu]
+    ops += sum(2 * (NU - 1) * (W - k - 1) + (W - k - 1) for k in range(NU))  # Gauss-Jordan
     ops += NQ * (NL + 1) * 2 * N + NL * (NL + 1) * NF * (2 * ND + 2 * D)  # Q, S
     return ops
 

@@ -57,15 +57,14 @@ struct BL {
   static constexpr int DV = IJ + NI * D * D;        // NI
   static constexpr int DS = DV + NI;                // F*NIF
   static constexpr int NRM = DS + F * NIF;          // F*NIF*D
-  static constexpr int G = NRM + F * NIF * D;       // NI*N*D  J^-1 grad phi
-  static constexpr int KG = G + NI * N * D;         // NI*N*D  Ds J^-1 grad phi
-  static constexpr int SOL = KG + NI * N * D;       // NI*ND   u at the IPs
+  static constexpr int SOL = NRM + F * NIF * D;     // NI*ND   u at the IPs
   static constexpr int DIV = SOL + NI * ND;         // NI      div u
   static constexpr int FSOL = DIV + NI;             // F*NIF*ND u (interior) at face IPs
   static constexpr int TN = FSOL + F * NIF * ND;    // F*NIF   (t.n) dS
   static constexpr int TAUQ = TN + F * NIF;         // F*NIF*NT dS tau
   static constexpr int DSKN = TAUQ + F * NIF * NT;  // F*NIF*D dS Ds n
-  static constexpr int MM = DSKN + F * NIF * D;     // N*N mass
+  static constexpr int T1 = DSKN + F * NIF * D;     // N*N     sum_q AQ_qi phi_qj
+  static constexpr int MM = T1 + N * N;             // N*N mass
   static constexpr int MI = MM + N * N;             // N*2N Gauss-Jordan [M | I] -> [I | M^-1]
   static constexpr int CK = MI + 2 * N * N;         // D*N*N  C_k
   static constexpr int MC = CK + D * N * N;         // D*N*N  M^-1 C_k
@@ -76,9 +75,19 @@ struct BL {
   static constexpr int TM = HF + F * D * NF * NF;   // F*NT*NF*NF tau masses [f][c][m][a][b]
   static constexpr int CLL = TM + F * NT * NF * NF; // F*NLF*NLF convection face blocks
   static constexpr int CUU = CLL + F * NLF * NLF;   // NU*NU convection volume block
-  static constexpr int AUG = CUU + NU * NU;         // NU*W row-major
+  static constexpr int KM = CUU + NU * NU;          // N*N     sum_k K'_k M^-1 C_k
+  static constexpr int KE = KM + N * N;             // N*F*NF  sum_k K'_k M^-1 E_k
+  static constexpr int AUG = KE + N * F * NF;       // NU*W row-major (first holds X, NU*NU)
   static constexpr int QS = AUG + NU * W;           // NQ*(NL+1) row-major [Q | Q0]
-  static constexpr int FL = QS + NQ * (NL + 1);     // NL
+  // the per-IP arrays live in the Q region: all of them are dead before Q is formed
+  static constexpr int G = QS;                      // NI*N*D  J^-1 grad phi
+  static constexpr int KG = G + NI * N * D;         // NI*N*D  Ds J^-1 grad phi
+  static constexpr int DSQ = KG + NI * N * D;       // NI*D*D  Ds at the volume IPs
+  static constexpr int AQ = DSQ + NI * D * D;       // NI*N    (div u phi_i + u.grad phi_i) dV
+  static constexpr int BQ = AQ + NI * N;            // NI*ND*N u_c dV phi_i
+  static constexpr int QSZ = (BQ + NI * ND * N - QS) > NQ * (NL + 1) ? (BQ + NI * ND * N - QS) : NQ * (NL + 1);
+  static_assert(NU * 4 <= NQ * (NL + 1), "right-hand side parts exceed the Q region");
+  static constexpr int FL = QS + QSZ;               // NL
   static constexpr int TOTAL = TAB + FL + NL + 2;   // + pivot scalars
   static_assert(TOTAL * 8 <= 227 * 1024, "element region exceeds the shared memory of one CTA");
 };
@@ -131,6 +140,10 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
   double* tn = R + L::TN;
   double* tauq = R + L::TAUQ;
   double* dskn = R + L::DSKN;
+  double* dsq = R + L::DSQ;
+  double* aq = R + L::AQ;
+  double* bq = R + L::BQ;
+  double* t1 = R + L::T1;
   double* Mm = R + L::MM;
   double* MI = R + L::MI;
   double* Ck = R + L::CK;
@@ -142,7 +155,11 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
   double* Tm = R + L::TM;
   double* Cll = R + L::CLL;
   double* Cuu = R + L::CUU;
+  double* KMs = R + L::KM;
+  double* KEs = R + L::KE;
   double* Aug = R + L::AUG;
+  double* Xc = R + L::AUG;  // X[(i,c),(j,m)] = sum_q u_qc dV_q phi_qi G_qjm, before the Schur system
+  double* rhsPart = R + L::QS;  // NU*4 parts of the right-hand side column, before Q
   double* Qs = R + L::QS;
   double* Fl = R + L::FL;
   double* pivInv = R + L::FL + NL;
@@ -197,6 +214,12 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
       iJ[q * 4 + 2] = -J[1][0] * id;  // (1,0)
       iJ[q * 4 + 3] = J[0][0] * id;   // (1,1)
       dV[q] = w[q] * det;
+      for (int a = 0; a < D * D; ++a) {  // Ds at q, column-major (HDGDiffusion.cpp:52-57)
+        double acc = 0.0;
+        if (diff)
+          for (int n = 0; n < N; ++n) acc += phi[q * N + n] * kap[n * D * D + a];
+        dsq[q * D * D + a] = acc;
+      }
     }
     for (int fk = tid; fk < F * NIF; fk += kBT) {
       const int f = fk / NIF, k = fk % NIF;
@@ -231,12 +254,7 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
       }
       for (int a = 0; a < D; ++a) {
         double acc = 0.0;
-        if (diff)
-          for (int b = 0; b < D; ++b) {
-            double dab = 0.0;  // Ds(a, b) at q, column-major (HDGDiffusion.cpp:52-57)
-            for (int n = 0; n < N; ++n) dab += phi[q * N + n] * kap[n * D * D + a + b * D];
-            acc += dab * g[b];
-          }
+        for (int b = 0; b < D; ++b) acc += dsq[q * D * D + a + b * D] * g[b];
         KG[qi * D + a] = acc;
       }
     }
@@ -288,13 +306,24 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
       divu[q] = acc;
     }
     __syncthreads();
+    for (int qi = tid; qi < NI * N; qi += kBT) {
+      // factors of the volume convection block: AQ_qi = (div u phi_i + u.G_i) dV,
+      // BQ_qci = u_c dV phi_i
+      const int q = qi / N, i = qi % N;
+      double sg = 0.0;
+      for (int k = 0; k < D; ++k) sg += sol[q * ND + k] * G[qi * D + k];
+      aq[qi] = (divu[q] * phi[qi] + sg) * dV[q];
+      for (int c = 0; c < ND; ++c) bq[(q * ND + c) * N + i] = sol[q * ND + c] * dV[q] * phi[qi];
+    }
+    __syncthreads();
     // ------------------------------------------------------ scalar blocks
     for (int ij = tid; ij < N * N; ij += kBT) {
       const int i = ij / N, j = ij % N;
-      double m = 0.0, c[D] = {}, kp[D] = {};
+      double m = 0.0, c[D] = {}, kp[D] = {}, tt = 0.0;
       for (int q = 0; q < NI; ++q) {
         const double pj = phi[q * N + j] * dV[q];
         m += phi[q * N + i] * pj;
+        tt += aq[q * N + i] * phi[q * N + j];
         for (int k = 0; k < D; ++k) {
           c[k] += G[(q * N + i) * D + k] * pj;
           kp[k] += KG[(q * N + i) * D + k] * pj;
@@ -310,6 +339,7 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
           }
         }
       Mm[ij] = m;
+      t1[ij] = tt;
       MI[i * 2 * N + j] = m;
       MI[i * 2 * N + N + j] = (i == j) ? 1.0 : 0.0;
       for (int k = 0; k < D; ++k) {
@@ -317,25 +347,29 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
         KP[k * N * N + ij] = diff ? kp[k] : 0.0;
       }
     }
-    for (int x = tid; x < F * NF * NF; x += kBT) {
-      const int f = x / (NF * NF), a = (x / NF) % NF, b = x % NF;
-      double ev[D] = {}, hv[D] = {}, tv[NT] = {};
+    for (int x = tid; x < F * D * NF * NF; x += kBT) {
+      // E_fk, H_fk: entry ((f*D + k)*NF + a)*NF + b
+      const int f = x / (D * NF * NF), k = (x / (NF * NF)) % D, a = (x / NF) % NF, b = x % NF;
+      double ev = 0.0, hv = 0.0;
       for (int k2 = 0; k2 < NIF; ++k2) {
         const int fq = f * NIF + k2;
         const double ss = fphi[k2 * NF + a] * fphi[k2 * NF + b];
-        for (int k = 0; k < D; ++k) {
-          ev[k] += dS[fq] * nrm[fq * D + k] * ss;
-          hv[k] += dskn[fq * D + k] * ss;
-        }
-        for (int v = 0; v < NT; ++v) tv[v] += tauq[fq * NT + v] * ss;
+        ev += dS[fq] * nrm[fq * D + k] * ss;
+        hv += dskn[fq * D + k] * ss;
       }
-      for (int k = 0; k < D; ++k) {
-        Ef[((f * D + k) * NF + a) * NF + b] = ev[k];
-        Hf[((f * D + k) * NF + a) * NF + b] = diff ? hv[k] : 0.0;
+      Ef[x] = ev;
+      Hf[x] = diff ? hv : 0.0;
+    }
+    for (int x = tid; x < F * NT * NF * NF; x += kBT) {
+      // tau masses: entry (((f*ND + c)*ND + m)*NF + a)*NF + b, tau column-major ((c, m) at m*ND + c)
+      const int f = x / (NT * NF * NF), c = (x / (ND * NF * NF)) % ND, m = (x / (NF * NF)) % ND;
+      const int a = (x / NF) % NF, b = x % NF;
+      double tv = 0.0;
+      for (int k2 = 0; k2 < NIF; ++k2) {
+        const int fq = f * NIF + k2;
+        tv += tauq[fq * NT + m * ND + c] * (fphi[k2 * NF + a] * fphi[k2 * NF + b]);
       }
-      // tau column-major: (c, m) at m*ND + c
-      for (int c = 0; c < ND; ++c)
-        for (int m = 0; m < ND; ++m) Tm[(((f * ND + c) * ND + m) * NF + a) * NF + b] = tv[m * ND + c];
+      Tm[x] = tv;
     }
     for (int x = tid; x < F * NLF * NLF; x += kBT) {
       // HDGUNabU face block (HDGUNabU.cpp:126-145): row (a, c), column (b, m)
@@ -350,39 +384,36 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
       Cll[x] = acc;
     }
     for (int x = tid; x < NU * NU; x += kBT) {
-      // HDGUNabU volume block (HDGUNabU.cpp:153-177): row (i, c), column (j, m)
+      // X[(i,c),(j,m)] = sum_q u_qc dV_q phi_qi G_qjm
       const int r = x / NU, cc = x % NU;
       const int i = r / ND, c = r % ND, j = cc / ND, m = cc % ND;
       double acc = 0.0;
-      for (int q = 0; q < NI; ++q) {
-        const double pi = phi[q * N + i], pj = phi[q * N + j];
-        double v = sol[q * ND + c] * (G[(q * N + j) * D + m] * pi + G[(q * N + i) * D + m] * pj);
-        if (c == m) {
-          double sg = 0.0;
-          for (int k = 0; k < D; ++k) sg += sol[q * ND + k] * G[(q * N + i) * D + k];
-          v += (divu[q] * pi + sg) * pj;
-        }
-        acc -= v * dV[q];
-      }
-      Cuu[x] = acc;
+      for (int q = 0; q < NI; ++q) acc += bq[(q * ND + c) * N + i] * G[(q * N + j) * D + m];
+      Xc[x] = acc;
     }
     __syncthreads();
-    // mass inverse: Gauss-Jordan on [M | I] (M is symmetric positive definite)
+    for (int x = tid; x < NU * NU; x += kBT) {
+      // HDGUNabU volume block (HDGUNabU.cpp:153-177), row (i, c), column (j, m):
+      // -sum_q dV [d_cm (div u phi_i + u.G_i) phi_j + u_c (G_jm phi_i + G_im phi_j)]
+      const int r = x / NU, cc = x % NU;
+      const int i = r / ND, c = r % ND, j = cc / ND, m = cc % ND;
+      Cuu[x] = -((c == m ? t1[i * N + j] : 0.0) + Xc[x] + Xc[(j * ND + c) * NU + i * ND + m]);
+    }
+    __syncthreads();
+    // mass inverse: Gauss-Jordan on [M | I] (M is symmetric positive definite). Only
+    // the columns right of the pivot are updated: the ones left of it are never read
+    // again, and column k is read unchanged as the elimination factors.
     for (int k = 0; k < N; ++k) {
-      if (tid == 0) pivInv[0] = 1.0 / MI[k * 2 * N + k];
+      const double pinv = 1.0 / MI[k * 2 * N + k];
+      for (int j = k + 1 + tid; j < 2 * N; j += kBT) MI[k * 2 * N + j] *= pinv;
       __syncthreads();
-      const double pinv = pivInv[0];
-      for (int j = tid; j < 2 * N; j += kBT) MI[k * 2 * N + j] *= pinv;
-      __syncthreads();
-      for (int x = tid; x < (N - 1) * 2 * N; x += kBT) {
-        int i = x / (2 * N), j = x % (2 * N);
+      const int nc = 2 * N - k - 1;
+      for (int x = tid; x < (N - 1) * nc; x += kBT) {
+        int i = x / nc;
+        const int j = k + 1 + x % nc;
         if (i >= k) ++i;
-        const double l = MI[i * 2 * N + k];
-        if (j != k) MI[i * 2 * N + j] -= l * MI[k * 2 * N + j];
+        MI[i * 2 * N + j] -= MI[i * 2 * N + k] * MI[k * 2 * N + j];
       }
-      __syncthreads();
-      for (int i = tid; i < N; i += kBT)
-        if (i != k) MI[i * 2 * N + k] = 0.0;
       __syncthreads();
     }
     for (int x = tid; x < D * N * N; x += kBT) {
@@ -400,9 +431,27 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
       ME[x] = acc;
     }
     __syncthreads();
+    if (diff) {
+      // the Schur products sum_k K'_k M^-1 C_k and sum_k K'_k M^-1 E_k (shared by every (c, m))
+      for (int x = tid; x < N * N + N * F * NF; x += kBT) {
+        double acc = 0.0;
+        if (x < N * N) {
+          const int i = x / N, j = x % N;
+          for (int k = 0; k < D; ++k)
+            for (int l = 0; l < N; ++l) acc += KP[k * N * N + i * N + l] * MC[k * N * N + l * N + j];
+          KMs[x] = acc;
+        } else {
+          const int y = x - N * N, i = y / (F * NF), fb = y % (F * NF);
+          for (int k = 0; k < D; ++k)
+            for (int l = 0; l < N; ++l) acc += KP[k * N * N + i * N + l] * ME[(k * N + l) * F * NF + fb];
+          KEs[y] = acc;
+        }
+      }
+      __syncthreads();
+    }
     // ------------------------------------- augmented Schur system [A | -B | Fu]
-    for (int x = tid; x < NU * W; x += kBT) {
-      const int r = x / W, col = x % W;
+    for (int x = tid; x < NU * (W - 1); x += kBT) {
+      const int r = x / (W - 1), col = x % (W - 1);
       const int i = r / ND, c = r % ND;
       double v;
       if (col < NU) {
@@ -412,38 +461,39 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
           const int a = sPos[f * N + i], b = sPos[f * N + j];
           if (a >= 0 && b >= 0) base += Tm[(((f * ND + c) * ND + m) * NF + a) * NF + b];
         }
-        double schur = 0.0;
-        if (c == m && diff)
-          for (int k = 0; k < D; ++k)
-            for (int l = 0; l < N; ++l) schur += KP[k * N * N + i * N + l] * MC[k * N * N + l * N + j];
+        const double schur = (c == m && diff) ? KMs[i * N + j] : 0.0;
         v = s * (base + Cuu[r * NU + col] - schur) + ((euler && c == m) ? Mm[i * N + j] : 0.0);
-      } else if (col < NU + NL) {
+      } else {
         const int cl = col - NU, f = cl / NLF, b = (cl % NLF) / ND, m = cl % ND;
         const int a = sPos[f * N + i];
         double sul = 0.0;
         if (a >= 0) sul = -Tm[(((f * ND + c) * ND + m) * NF + a) * NF + b] + Cll[(f * NLF + a * ND + c) * NLF + b * ND + m];
-        double schur = 0.0;
-        if (c == m && diff)
-          for (int k = 0; k < D; ++k)
-            for (int l = 0; l < N; ++l) schur += KP[k * N * N + i * N + l] * ME[(k * N + l) * F * NF + f * NF + b];
+        const double schur = (c == m && diff) ? KEs[i * F * NF + f * NF + b] : 0.0;
         v = -s * (sul + schur);
-      } else {
-        // HDGUNabU RHS on the U rows: (Cuu u + Cul t) / 2 (HDGUNabU.cpp:178-190)
-        double cr = 0.0;
-        for (int cc = 0; cc < NU; ++cc) cr += Cuu[r * NU + cc] * ub[cc];
+      }
+      Aug[r * W + col] = v;
+    }
+    // right-hand side column, four threads per U row: the HDGUNabU RHS (Cuu u + Cul t) / 2
+    // (HDGUNabU.cpp:178-190) in two parts, the source, the implicit-Euler mass term
+    for (int x = tid; x < NU * 4; x += kBT) {
+      const int r = x / 4, part = x % 4;
+      const int i = r / ND, c = r % ND;
+      double acc = 0.0;
+      if (part == 0) {
+        for (int cc = 0; cc < NU; ++cc) acc += Cuu[r * NU + cc] * ub[cc];
+      } else if (part == 1) {
         for (int f = 0; f < F; ++f) {
           const int a = sPos[f * N + i];
           if (a < 0) continue;
-          for (int cc = 0; cc < NLF; ++cc) cr += Cll[(f * NLF + a * ND + c) * NLF + cc] * tr[f * NLF + cc];
+          for (int cc = 0; cc < NLF; ++cc) acc += Cll[(f * NLF + a * ND + c) * NLF + cc] * tr[f * NLF + cc];
         }
-        double fu = 0.5 * cr;
+      } else if (part == 2) {
         if (p.src)
-          for (int q = 0; q < NI; ++q) fu += phi[q * N + i] * p.src[(e * NI + q) * ND + c] * dV[q];
-        v = s * fu;
-        if (euler)
-          for (int j = 0; j < N; ++j) v += Mm[i * N + j] * uo[j * ND + c];
+          for (int q = 0; q < NI; ++q) acc += phi[q * N + i] * p.src[(e * NI + q) * ND + c] * dV[q];
+      } else if (euler) {
+        for (int j = 0; j < N; ++j) acc += Mm[i * N + j] * uo[j * ND + c];
       }
-      Aug[x] = v;
+      rhsPart[x] = acc;
     }
     for (int x = tid; x < NL; x += kBT) {
       // HDGUNabU RHS on the L rows: Cll t / 2 (the L-U convection block is zero)
@@ -453,20 +503,39 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
       Fl[x] = 0.5 * acc;
     }
     __syncthreads();
-    // Gauss-Jordan with partial pivoting: [A | -B | Fu] -> [I | U | U0]
+    for (int r = tid; r < NU; r += kBT) {
+      const double* rp = rhsPart + 4 * r;
+      Aug[r * W + W - 1] = s * (0.5 * (rp[0] + rp[1]) + rp[2]) + rp[3];
+    }
+    __syncthreads();
+    // Gauss-Jordan with partial pivoting: [A | -B | Fu] -> [I | U | U0]. Columns left
+    // of the pivot are never read again and are not updated; column k stays as the
+    // elimination factors.
     bool singular = false;
     for (int k = 0; k < NU; ++k) {
-      if (tid == 0) {
-        int pr = k;
-        double best = fabs(Aug[k * W + k]);
-        for (int r = k + 1; r < NU; ++r) {
+      if (tid < 32) {
+        // pivot: the first row r >= k of largest |A(r, k)| (the serial scan's choice)
+        double best = -1.0;
+        int br = NU;
+        for (int r = k + tid; r < NU; r += 32) {
           const double v = fabs(Aug[r * W + k]);
           if (v > best) {
             best = v;
-            pr = r;
+            br = r;
           }
         }
-        sPiv = best == 0.0 ? -1 : pr;
+        for (int o = 16; o > 0; o >>= 1) {
+          const double ob = __shfl_down_sync(0xffffffffu, best, o);
+          const int orr = __shfl_down_sync(0xffffffffu, br, o);
+          if (ob > best || (ob == best && orr < br)) {
+            best = ob;
+            br = orr;
+          }
+        }
+        if (tid == 0) {
+          sPiv = best > 0.0 ? br : -1;
+          if (best > 0.0) pivInv[0] = 1.0 / Aug[br * W + k];
+        }
       }
       __syncthreads();
       const int pr = sPiv;
@@ -474,27 +543,25 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
         singular = true;
         break;
       }
-      if (pr != k)
-        for (int j = tid; j < W; j += kBT) {
-          const double t = Aug[k * W + j];
-          Aug[k * W + j] = Aug[pr * W + j];
-          Aug[pr * W + j] = t;
-        }
-      __syncthreads();
-      if (tid == 0) pivInv[0] = 1.0 / Aug[k * W + k];
-      __syncthreads();
       const double pinv = pivInv[0];
-      for (int j = tid; j < W; j += kBT) Aug[k * W + j] *= pinv;
+      // swap rows k and pr (columns >= k), scale the new pivot row (columns > k)
+      for (int j = k + tid; j < W; j += kBT) {
+        const double a = Aug[k * W + j], b = Aug[pr * W + j];
+        if (j == k) {
+          Aug[pr * W + j] = a;  // the factor of row pr
+        } else {
+          Aug[k * W + j] = b * pinv;
+          if (pr != k) Aug[pr * W + j] = a;
+        }
+      }
       __syncthreads();
-      for (int x = tid; x < (NU - 1) * (W - k - 1); x += kBT) {
-        int i = x / (W - k - 1);
-        const int j = k + 1 + x % (W - k - 1);
+      const int nc = W - k - 1;
+      for (int x = tid; x < (NU - 1) * nc; x += kBT) {
+        int i = x / nc;
+        const int j = k + 1 + x % nc;
         if (i >= k) ++i;
         Aug[i * W + j] -= Aug[i * W + k] * Aug[k * W + j];
       }
-      __syncthreads();
-      for (int i = tid; i < NU; i += kBT)
-        if (i != k) Aug[i * W + k] = 0.0;
       __syncthreads();
     }
     if (singular) {
