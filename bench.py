@@ -59,7 +59,8 @@ CONFIGS = {
     "burgers-small": dict(dim=2, n=48, order=3, burgers=True, nu=1e-2, dt=1e-3, time_steps=20,
                           desc="2D viscous Burgers HDG, 48x48x2 tris (4,608), p=3, nu=1e-2, dt=1e-3"),
 }
-BURGERS_METRIC = "implicit-Euler Burgers step time (Newton to 1e-6, GMRES 1e-10); elements x steps / s"
+BURGERS_METRIC = ("Burgers implicit-Euler steps, Newton to 1e-6 (GMRES 1e-10): elements x Newton iterations / s "
+                  "(assemble + condense + scatter + Krylov + recover per iteration)")
 
 
 def peaks():
@@ -481,11 +482,12 @@ def run_burgers(args, world, rank, local):
     barrier(world)
     ctx._chk(L.hfx_synchronize(ctx.h), "sync")
     e2e_steps = min(steps, 20)
+    e2e_its = 0
     t1 = time.perf_counter()
     for _ in range(e2e_steps):
         ctx._chk(L.hfx_burgers_set_state(ctx.h, capi._p(sol_h), None, None, None), "set_state")
         ctx._chk(L.hfx_burgers_begin_step(ctx.h), "begin_step")
-        newton(warm)
+        e2e_its += newton(warm).iterations
         ctx._chk(L.hfx_burgers_get_state(ctx.h, capi._p(sol_h), None, None, None), "get_state")
     e2e_s = barrier_max(world, time.perf_counter() - t1)
     E = ctx.nCells
@@ -501,8 +503,9 @@ def run_burgers(args, world, rank, local):
     nl = sum(its)
     res = {
         "metric": BURGERS_METRIC,
-        "value": E * steps / (dev_ms / 1e3),
-        "unit": "elements*steps/s",
+        "value": E * sum(its) / (dev_ms / 1e3),
+        "unit": "elements*newton_iterations/s",
+        "elements_steps_per_s": E * steps / (dev_ms / 1e3),
         "n_gpus": world, "steps": steps, "warmup": args.warmup,
         "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64",
@@ -522,8 +525,8 @@ def run_burgers(args, world, rank, local):
         "kernel_ms": {k: dict(launches=v[0], total_ms=round(v[1], 3)) for k, v in kt.items()},
         "roofline": roof,
         "clocks": clk,
-        "e2e": {"value": E * e2e_steps / e2e_s, "unit": "elements*steps/s", "h2d_bytes_per_step": int(sol_h.nbytes),
-                "d2h_bytes_per_step": int(sol_h.nbytes)},
+        "e2e": {"value": E * e2e_its / e2e_s, "unit": "elements*newton_iterations/s",
+                "h2d_bytes_per_step": int(sol_h.nbytes), "d2h_bytes_per_step": int(sol_h.nbytes)},
         "gpu_launches": int(sum(v[0] for v in kt.values())),
         "setup_s": t_setup,
     }
@@ -532,7 +535,9 @@ def run_burgers(args, world, rank, local):
 
 def burgers_cpu_sample(cfg_name, nthreads, n=64):
     """The oracle (HDGBurgersModel restatement, dense LU condensation, GMRES(30)+Jacobi)
-    on a bounded sample: one implicit Euler step of the same physics on an n x n x 2 mesh."""
+    on a bounded sample: the second implicit Euler step of the same physics on an
+    n x n x 2 mesh (the first, untimed, gives the timed one a trace to start from, as
+    the GPU arm's timed steps have)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import _oracle as O
     from hyperfox_gb300 import meshgen
@@ -544,29 +549,33 @@ def burgers_cpu_sample(cfg_name, nthreads, n=64):
     P = O.BurgersProblem(2, p, coords, cells)
     tau = np.zeros((P.nFaces, re.nNodesFace, 2, 4))
     tau[..., 0] = tau[..., 3] = 1.0
-    u0 = burgers_initial(coords, cells)
-    P.set_fields(tau=tau, tau_sides=2, nu=np.full((P.nCells, re.nNodes, 1), cfg["nu"]),
-                 dirichlet=np.zeros((P.nFaces, re.nNodesFace, 2)), dt=cfg["dt"], old=u0)
-    P.buf, P.trace = u0.copy(), np.zeros(P.ndofs)
-    t0 = time.perf_counter()
-    its = kits = 0
-    for _ in range(20):
-        P.set_state(P.buf, P.trace)
-        P.assemble(nthreads)
-        x, k = P.solve_gmres(1e-10, 200000, nthreads)
-        sol, _ = P.recover(x)
-        P.trace = x
-        its += 1
-        kits += abs(k)
-        diff, ref = float(np.sum((sol - P.buf) ** 2)), float(np.sum(P.buf ** 2))
-        if np.sqrt(diff / ref) < 1e-6:
-            break
-        P.buf = sol
-    dt = time.perf_counter() - t0
-    return dict(value=P.nCells / dt, unit="elements*steps/s", cores=nthreads, kind="port",
-                sample="one implicit Euler step (Newton %d iterations, %d GMRES(30)+Jacobi iterations) on %dx%dx2 "
-                       "tris (%d elements, %d trace DOFs): oracle assemble + LU condense + scatter + solve + recover"
-                       % (its, kits, n, n, P.nCells, P.ndofs), seconds=dt)
+    nu = np.full((P.nCells, re.nNodes, 1), cfg["nu"])
+    zero = np.zeros((P.nFaces, re.nNodesFace, 2))
+    u = burgers_initial(coords, cells)
+    P.trace = np.zeros(P.ndofs)
+    for step in range(2):
+        P.set_fields(tau=tau, tau_sides=2, nu=nu, dirichlet=zero, dt=cfg["dt"], old=u)
+        P.buf = u.copy()
+        t0 = time.perf_counter()
+        its = kits = 0
+        for _ in range(20):
+            P.set_state(P.buf, P.trace)
+            P.assemble(nthreads)
+            x, k = P.solve_gmres(1e-10, 200000, nthreads)
+            sol, _ = P.recover(x)
+            P.trace = x
+            its += 1
+            kits += abs(k)
+            diff, ref = float(np.sum((sol - P.buf) ** 2)), float(np.sum(P.buf ** 2))
+            if np.sqrt(diff / ref) < 1e-6:
+                break
+            P.buf = sol
+        dt = time.perf_counter() - t0
+        u = sol
+    return dict(value=P.nCells * its / dt, unit="elements*newton_iterations/s", cores=nthreads, kind="port",
+                sample="the second implicit Euler step (Newton %d iterations, %d GMRES(30)+Jacobi iterations, "
+                       "Krylov from zero) on %dx%dx2 tris (%d elements, %d trace DOFs): oracle assemble + LU "
+                       "condense + scatter + solve + recover" % (its, kits, n, n, P.nCells, P.ndofs), seconds=dt)
 
 
 def cpu_sample(cfg_name, nthreads, rtol, budget_elems=None):
@@ -641,11 +650,12 @@ def main():
             if i >= args.warmup:
                 vals.append(r["value"])
         v = statistics.median(vals)
-        out = {"impl": "reference", "metric": BURGERS_METRIC, "value": v, "unit": "elements*steps/s",
+        out = {"impl": "reference", "metric": BURGERS_METRIC, "value": v, "unit": "elements*newton_iterations/s",
                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                "config": {"workload": CONFIGS[args.config]["desc"]}, "cpu_baseline": dict(r, value=v),
-               "e2e": {"value": v, "unit": "elements*steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+               "e2e": {"value": v, "unit": "elements*newton_iterations/s", "h2d_bytes_per_step": 0,
+                       "d2h_bytes_per_step": 0}}
         print(json.dumps(out))
         return
     if burgers:
