@@ -50,6 +50,13 @@ CONFIGS = {
     "small3d": dict(dim=3, n=12, order=3, desc="3D HDG diffusion-source, 12^3x6 tets, p=3"),
     "mid3d": dict(dim=3, n=20, order=3, desc="3D HDG diffusion-source, 20^3x6 tets (48k), p=3"),
     "cfg5mesh": dict(dim=3, n=60, order=2, desc="3D HDG diffusion-source, 60^3x6 tets (1.296M), p=2"),
+    # anisotropic lognormal diffusion: kappa = exp(g) (I + 99 a a^T), g a Gaussian random field
+    # (sigma 1.5, correlation length 0.05) sampled at the cell centroids, a a seeded random axis
+    "cfg5": dict(dim=3, n=60, order=2, aniso=dict(sigma=1.5, corr=0.05, ratio=100.0, seed=5), cpu_n=8,
+                 desc="3D anisotropic diffusion, unit cube 60^3x6 tets (1.296M), p=2, kappa = exp(g) x "
+                      "(I + 99 a a^T), g Gaussian random field (sigma 1.5, corr 0.05) per cell, seeded axis a"),
+    "cfg5-small": dict(dim=3, n=20, order=2, aniso=dict(sigma=1.5, corr=0.05, ratio=100.0, seed=5), cpu_n=8,
+                       desc="3D anisotropic diffusion, 20^3x6 tets (48k), p=2, the cfg5 coefficient field"),
     # viscous Burgers (HDGBurgersModel + HDGUNabU, nd = 2), implicit Euler, Newton every step
     "cfg4": dict(dim=2, n=180, order=3, burgers=True, nu=1e-2, dt=1e-3, time_steps=200,
                  desc="2D viscous Burgers HDG, unit square 180x180x2 tris (64,800), p=3, nu=1e-2, "
@@ -124,6 +131,27 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def aniso_kappa(coords, cells, dim, sigma, corr, ratio, seed, modes=256):
+    """Cell-constant anisotropic lognormal diffusion tensor [nCells][N][dim*dim] (column-major,
+    exactly symmetric): exp(g(centroid)) (I + (ratio - 1) a a^T), with g a Gaussian random field
+    of standard deviation sigma and squared-exponential correlation length corr (random Fourier
+    features, seeded) and a a seeded random unit axis."""
+    rng = np.random.default_rng(seed)
+    w = rng.normal(0.0, 1.0 / corr, size=(dim, modes))
+    phase = rng.uniform(0.0, 2.0 * np.pi, size=modes)
+    axis = rng.normal(size=dim)
+    axis /= np.linalg.norm(axis)
+    A = np.eye(dim) + (ratio - 1.0) * np.outer(axis, axis)
+    A = 0.5 * (A + A.T)
+    nC, N = cells.shape
+    cent = coords[cells[:, :dim + 1]].mean(axis=1)
+    g = np.empty(nC)
+    for a in range(0, nC, 65536):
+        g[a:a + 65536] = sigma * np.sqrt(2.0 / modes) * np.cos(cent[a:a + 65536] @ w + phase).sum(axis=1)
+    kap = np.exp(g)[:, None, None] * A.T.reshape(1, 1, dim * dim)
+    return np.ascontiguousarray(np.broadcast_to(kap, (nC, N, dim * dim)))
+
+
 def make_problem(cfg):
     from hyperfox_gb300 import capi, meshgen
     dim, n, p = cfg["dim"], cfg["n"], cfg["order"]
@@ -186,6 +214,8 @@ def run_ours(args, world, rank, local):
     ctx.set_tau(tau_h)
     ctx.set_dirichlet(dir_h)
     ctx.set_source(capi.SRC_SINPROD, param=dim * np.pi ** 2)
+    if cfg.get("aniso"):
+        ctx.set_kappa(aniso_kappa(coords, cells, dim, **cfg["aniso"]), layout=1)
     L = ctx.L
     prec = capi.PREC_FP64 if args.precision == "fp64" else capi.PREC_MIXED
     pc = capi.PC_TWOLEVEL if args.precond == "twolevel" else capi.PC_BLOCK_JACOBI
@@ -221,7 +251,9 @@ def run_ours(args, world, rank, local):
         ti = ctx.coarse_train(degree=args.coarse_degree, samples=16, steps=300)
         learned = dict(degree=ti.degree, samples=ti.samples, steps=ti.steps, accepted=bool(ti.accepted),
                        loss_chebyshev_same_degree=ti.loss_chebyshev, loss_learned=ti.loss_learned,
-                       max_residual_polynomial=ti.max_poly, train_s=ti.train_ms / 1e3)
+                       max_residual_polynomial=ti.max_poly, train_s=ti.train_ms / 1e3,
+                       loss_first_step=ti.loss_first_step, lower_steps=ti.lower_steps,
+                       rejected_steps=ti.rejected_steps)
     for _ in range(args.warmup):
         step_device()
     # device-resident timed region
@@ -586,14 +618,15 @@ def cpu_sample(cfg_name, nthreads, rtol, budget_elems=None):
     from hyperfox_gb300 import meshgen
     cfg = CONFIGS[cfg_name]
     dim, p = cfg["dim"], cfg["order"]
-    n = {3: 12, 2: 32}[dim] if budget_elems is None else budget_elems
+    n = cfg.get("cpu_n", {3: 12, 2: 32}[dim]) if budget_elems is None else budget_elems
     n = min(n, cfg["n"])
     re = O.RefEl(dim, p)
     v, s = meshgen.square_simplices(n) if dim == 2 else meshgen.cube_simplices(n)
     coords, cells = meshgen.high_order(v, s, re.nodes)
     P = O.Problem(dim, p, coords, cells)
     g = np.prod(np.sin(np.pi * coords[P.faces]), axis=-1)
-    P.set_fields(np.ones(P.ndofs), src_mode=2, dirichlet=g.ravel())
+    kap = aniso_kappa(coords, cells, dim, **cfg["aniso"]).ravel() if cfg.get("aniso") else None
+    P.set_fields(np.ones(P.ndofs), kappa=kap, src_mode=2, dirichlet=g.ravel())
     t0 = time.perf_counter()
     P.assemble(nthreads)
     x, it = P.solve_gmres(rtol, 200000, nthreads)

@@ -1713,6 +1713,17 @@ int hfx_coarse_train(hfx_ctx* c, int degree, int samples, int steps, hfx_train_i
   const int S = std::min(taken, samples);
   CoarseTrainResult tr;
   cudaError_t e = coarse_train(&c->coarse, buf, S, degree, steps, 0.05, c->stream, &tr);
+  if (e == cudaSuccess && !tr.accepted && steps > 0) {
+    // no accepted improvement (a spectrum the default step overshoots): one more round
+    // from Chebyshev with a smaller step; a rejected round leaves the coarse solve as it was
+    CoarseTrainResult tr2;
+    e = coarse_train(&c->coarse, buf, S, degree, steps, 0.01, c->stream, &tr2);
+    if (e == cudaSuccess) {
+      tr2.lowerSteps += tr.lowerSteps;
+      tr2.rejectedSteps += tr.rejectedSteps;
+      tr = tr2;
+    }
+  }
   cudaFree(buf);
   if (e != cudaSuccess) return cuda_err(c, e, "coarse_train");
   if (info) {

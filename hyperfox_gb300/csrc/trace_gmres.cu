@@ -9,6 +9,7 @@
 // partial dot products are per-block sums added on the host in block order
 // (deterministic). Mixed precision: FP32 GMRES on the FP32 copy of A' inside
 // FP64 iterative refinement.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -69,21 +70,24 @@ __global__ void __launch_bounds__(kT) op_apply(TraceView A, const T* __restrict_
 }
 
 // out = M^{-1} in, per face (PC: 0 none, 1 Jacobi, 2 block Jacobi)
+// out = M^{-1} in, one thread per trace value (face f, row a): consecutive threads read
+// consecutive entries of the column-major face blocks, the row's sum runs over b in order.
 template <typename T, int NF, int PC>
 __global__ void pc_apply(int64_t nFaces, const T* __restrict__ pc, const T* __restrict__ in, T* __restrict__ out) {
-  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < nFaces; f += (int64_t)gridDim.x * blockDim.x) {
-    T v[NF];
-    for (int a = 0; a < NF; ++a) v[a] = in[f * NF + a];
-    for (int a = 0; a < NF; ++a) {
-      T z;
-      if (PC == 0) z = v[a];
-      else if (PC == 1) z = pc[f * NF + a] * v[a];
-      else {
-        z = 0;
-        for (int b = 0; b < NF; ++b) z += pc[f * NF * NF + b * NF + a] * v[b];  // column-major
-      }
-      out[f * NF + a] = z;
+  const int64_t n = nFaces * NF;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t f = i / NF;
+    const int a = (int)(i % NF);
+    T z;
+    if (PC == 0) z = in[i];
+    else if (PC == 1) z = pc[i] * in[i];
+    else {
+      z = 0;
+      const T* blk = pc + f * NF * NF + a;
+      const T* v = in + f * NF;
+      for (int b = 0; b < NF; ++b) z += blk[b * NF] * v[b];  // column-major
     }
+    out[i] = z;
   }
 }
 
@@ -110,6 +114,28 @@ __global__ void __launch_bounds__(kT) multi_dot(int64_t n, int m, const T* __res
 }
 
 // w -= sum_j V[j] h[j]
+// All m dot products <V_j, w> in one launch: block (x, j) sums a grid-stride chunk of
+// V_j . w, so the m products stream at once at full occupancy (w is re-read from L2);
+// per-block sums go to partial[j * gridDim.x + x], added on the host in block order.
+template <typename T>
+__global__ void __launch_bounds__(kT) multi_dot_cols(int64_t n, const T* __restrict__ V, const T* __restrict__ w,
+                                                     double* __restrict__ partial) {
+  __shared__ double red[kT / 32];
+  const int j = blockIdx.y;
+  const T* v = V + (int64_t)j * n;
+  double acc = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    acc += (double)v[i] * (double)w[i];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sum = 0.0;
+    for (int k = 0; k < kT / 32; ++k) sum += red[k];
+    partial[(int64_t)j * gridDim.x + blockIdx.x] = sum;
+  }
+}
+
 template <typename T>
 __global__ void multi_axpy(int64_t n, int m, const T* __restrict__ V, const double* __restrict__ h, T* __restrict__ w) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -185,7 +211,7 @@ int gmres_run(const TraceView& A, const T* val, int pcT, const T* pc, const T* b
   const int64_t n = A.nFaces * NF;
   const int gOp = grid_for(op_apply<T, NF, NBMAX, MASKED>, kT);
   const int gVec = grid_for(multi_dot<T>, kT);
-  const int gPc = (int)((A.nFaces + 127) / 128);
+  const int gPc = (int)std::min<int64_t>((A.nFaces * NF + 127) / 128, 152 * 64);
   std::vector<double> hp((size_t)(m + 1) * gVec), H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1);
   auto apply_pc = [&](const T* in, T* out) {
     switch (pcT) {
@@ -200,12 +226,15 @@ int gmres_run(const TraceView& A, const T* val, int pcT, const T* pc, const T* b
     tm->end(kid, s);
   };
   auto dots = [&](const T* W, int cnt, const T* Vb, std::vector<double>& out) {
-    multi_dot<T><<<gVec, kT, 0, s>>>(n, cnt, Vb, W, partials);
-    cudaMemcpyAsync(hp.data(), partials, sizeof(double) * cnt * gVec, cudaMemcpyDeviceToHost, s);
+    // Gram-Schmidt: the cnt products side by side, about gVec blocks in all
+    const int gd = cnt > 1 ? std::max(8, gVec / cnt) : gVec;
+    if (cnt > 1) multi_dot_cols<T><<<dim3(gd, cnt), kT, 0, s>>>(n, Vb, W, partials);
+    else multi_dot<T><<<gd, kT, 0, s>>>(n, cnt, Vb, W, partials);
+    cudaMemcpyAsync(hp.data(), partials, sizeof(double) * cnt * gd, cudaMemcpyDeviceToHost, s);
     cudaStreamSynchronize(s);
     out.assign(cnt, 0.0);
     for (int j = 0; j < cnt; ++j)
-      for (int k = 0; k < gVec; ++k) out[j] += hp[(size_t)j * gVec + k];
+      for (int k = 0; k < gd; ++k) out[j] += hp[(size_t)j * gd + k];
   };
   auto norm = [&](const T* W) {
     std::vector<double> o;
