@@ -421,24 +421,34 @@ def burgers_initial(coords, cells, seed=0):
     return u.reshape(cells.shape[0], -1)
 
 
-def burgers_flops_per_element(N, NF, F, NI, NIF, D=2):
-    """FP64 operations the Burgers element kernel executes per element (its loops)."""
+def burgers_flops_per_element(N, NF, F, NI, NIF, D=2, cached=False):
+    """FP64 operations the Burgers element kernel executes per element (its loops);
+    cached: a linearisation that loads the state-independent blocks (M, M^-1 C, M^-1 E,
+    tau masses, H, the Schur products) instead of computing them."""
     ND, NT = D, D * D
     NU, NQ, NLF = N * ND, D * N * ND, NF * ND
     NL = F * NLF
     W = NU + NL + 1
-    ops = 2 * NI * D * D * N + 4 * NI * N * D * D                     # Ds at the IPs, G, Ds G
-    ops += F * NIF * (4 * ND * NF + 2 * NT * NF + 2 * D * D * NF + 4 * D)  # face IP values
+    ops = 2 * NI * D * D * N + 2 * NI * N * D * D                     # G; (Ds at the IPs)
+    ops += 2 * NI * N * D * D                                            # Ds G
+    face_state = F * NIF * (4 * ND * NF + 4 * D)                         # u, t at the face IPs, t.n
+    face_static = F * NIF * (2 * NT * NF + 2 * D * D * NF)               # tau, Ds n at the face IPs
+    ops += face_state + face_static
     ops += 2 * NI * N * ND + 2 * NI * N * D + NI * N * (2 * D + 3 + 2 * ND)  # u, div u, AQ, BQ
-    ops += N * N * NI * (4 + 4 * D)                                      # M, T1, C_k, K'_k
-    ops += F * NF * NF * NIF * (4 * D + 2 * NT)                          # E, H, tau masses
+    t1 = N * N * NI * 2
+    scalar_static = N * N * NI * (2 + 4 * D)                             # M, C_k, K'_k
+    ehT = F * NF * NF * NIF * (4 * D + 2 * NT)                           # E, H, tau masses
+    ops += t1 + scalar_static + ehT
     ops += F * NLF * NLF * NIF * 6 + NU * NU * (2 * NI + 2)             # convection blocks
-    ops += sum(2 * (N - 1) * (2 * N - k - 1) + (2 * N - k - 1) for k in range(N))  # M^-1 (Gauss-Jordan)
-    ops += 2 * D * N * N * N + 2 * D * N * F * NF * NF                  # M^-1 C, M^-1 E
-    ops += 2 * D * N * (N * N + N * F * NF)                             # sum_k K' M^-1 C, K' M^-1 E
+    minv = sum(2 * (N - 1) * (2 * N - k - 1) + (2 * N - k - 1) for k in range(N))  # M^-1 (Gauss-Jordan)
+    mcme = 2 * D * N * N * N + 2 * D * N * F * NF * NF                  # M^-1 C, M^-1 E
+    kmke = 2 * D * N * (N * N + N * F * NF)                             # sum_k K' M^-1 C, K' M^-1 E
+    ops += minv + mcme + kmke
     ops += NU * NU * 6 + NU * NL * 6 + NU * (2 * NU + 2 * NL + 2 * NI + 2 * N)  # [A | -B | Fu]
     ops += sum(2 * (NU - 1) * (W - k - 1) + (W - k - 1) for k in range(NU))  # Gauss-Jordan
     ops += NQ * (NL + 1) * 2 * N + NL * (NL + 1) * NF * (2 * ND + 2 * D)  # Q, S
+    if cached:
+        ops -= 2 * NI * D * D * N + 2 * NI * N * D * D + face_static + scalar_static + ehT + minv + mcme + kmke
     return ops
 
 
@@ -525,10 +535,12 @@ def run_burgers(args, world, rank, local):
     E = ctx.nCells
     step_s = dev_ms / 1e3 / steps
     re = ctx.re
-    flops = burgers_flops_per_element(re["nNodes"], Nf, re["nFaces"], re["nIP"], re["nIPFace"])
+    # the timed linearisations load the state-independent blocks (stored by the first one)
+    flops = burgers_flops_per_element(re["nNodes"], Nf, re["nFaces"], re["nIP"], re["nIPFace"], cached=True)
     avg_ms = kt["local"][1] / max(1, kt["local"][0])
     tf = flops * E / (avg_ms / 1e3) / 1e12
-    roof = dict(bound="fp64", kernel="burgers_local<2,3> (FP64 assembly + condensation, vector Burgers)",
+    roof = dict(bound="fp64", kernel="burgers_local<2,3> (FP64 assembly + condensation, vector Burgers, "
+                                     "state-independent blocks from the per-element cache)",
                 achieved=round(tf, 3), peak=FP64_NOMINAL_TFLOPS, unit="TFLOP/s", frac=round(tf / FP64_NOMINAL_TFLOPS, 4),
                 traffic=args.traffic, flops_per_element=int(flops), avg_launch_ms=round(avg_ms, 4),
                 peak_source="nominal GB300 FP64 (no measured FP64 peak)")

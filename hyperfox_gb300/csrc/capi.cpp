@@ -74,6 +74,8 @@ struct BurgersState {
   double *S = nullptr, *S0 = nullptr, *U = nullptr, *Q = nullptr, *U0 = nullptr, *Q0 = nullptr;
   double *val = nullptr, *rhs = nullptr, *partials = nullptr, *red = nullptr;
   uint8_t* permx = nullptr;  // face2CellMap at DOF level: [nCells][F][Nf*nd]
+  double* cache = nullptr;   // state-independent element blocks, valid while cacheValid
+  bool cacheValid = false;
   int* status = nullptr;
   unsigned* ticket = nullptr;
   DevMem wsMem;
@@ -90,7 +92,7 @@ struct BurgersState {
     nu.release();
     src.release();
     dir.release();
-    ready = assembled = solved = false;
+    ready = assembled = solved = cacheValid = false;
   }
 };
 
@@ -1960,6 +1962,8 @@ int hfx_burgers_setup(hfx_ctx* c) {
   HFX_CUDA(c, dalloc(m, &B.red, 2));
   HFX_CUDA(c, dalloc(m, &B.status, 1));
   HFX_CUDA(c, dalloc(m, &B.ticket, 1));
+  HFX_CUDA(c, dalloc(m, &B.cache, (size_t)E * burgers_cache_doubles(c->dim, c->order)));
+  B.cacheValid = false;
   HFX_CUDA(c, cudaMemsetAsync(B.ticket, 0, sizeof(unsigned), s));
   for (double* p : {B.buf, B.sol, B.old})
     HFX_CUDA(c, cudaMemsetAsync(p, 0, sizeof(double) * E * B.NU, s));
@@ -1992,6 +1996,7 @@ int hfx_burgers_set_tau(hfx_ctx* c, const double* tau, int sides) {
   if (!tau || (sides != 1 && sides != 2)) return set_err(c, HFX_ERR_ARG, "burgers_set_tau: tau and sides 1 or 2");
   BurgersState& B = c->burgers;
   B.tauSides = sides;
+  B.cacheValid = false;
   HFX_CUDA(c, B.tau.set(tau, (size_t)c->topo.nFaces * c->re.nNodesFace * sides * B.nd * B.nd, c->stream));
   HFX_CUDA(c, cudaStreamSynchronize(c->stream));
   return HFX_OK;
@@ -2000,6 +2005,7 @@ int hfx_burgers_set_tau(hfx_ctx* c, const double* tau, int sides) {
 int hfx_burgers_set_diffusion(hfx_ctx* c, const double* nu, int comps, int layout) {
   if (int rc = burgers_ready(c, "burgers_set_diffusion")) return rc;
   BurgersState& B = c->burgers;
+  B.cacheValid = false;
   if (!nu || comps == 0) {
     B.kc = 0;
     return HFX_OK;
@@ -2109,10 +2115,13 @@ static int burgers_assemble_async(hfx_ctx* c) {
   p.U0 = B.U0;
   p.Q0 = B.Q0;
   p.status = B.status;
+  p.cache = B.cache;
+  p.cacheMode = B.cacheValid ? 2 : 1;
   HFX_CUDA(c, cudaMemsetAsync(B.status, 0, sizeof(int), s));
   c->timer.begin(K_LOCAL, s);
   HFX_CUDA(c, launch_burgers_local(c->dim, c->order, p, s));
   c->timer.end(K_LOCAL, s);
+  B.cacheValid = true;  // every element stores its blocks before its Schur solve
   ScatterParams sp{};
   sp.nFaces = c->topo.nFaces;
   sp.NF = B.NLF;

@@ -89,6 +89,16 @@ struct BL {
   static_assert(NU * 4 <= NQ * (NL + 1), "right-hand side parts exceed the Q region");
   static constexpr int FL = QS + QSZ;               // NL
   static constexpr int TOTAL = TAB + FL + NL + 2;   // + pivot scalars
+  // per-element cache of the parts that do not depend on the linearisation state
+  // (geometry, tau, diffusion): M, M^-1 C_k, M^-1 E_k, tau masses, H_fk, the Schur products
+  static constexpr int C_MM = 0;
+  static constexpr int C_MC = C_MM + N * N;
+  static constexpr int C_ME = C_MC + D * N * N;
+  static constexpr int C_TM = C_ME + D * N * F * NF;
+  static constexpr int C_HF = C_TM + F * NT * NF * NF;
+  static constexpr int C_KM = C_HF + F * D * NF * NF;
+  static constexpr int C_KE = C_KM + N * N;
+  static constexpr int CL = C_KE + N * F * NF;
   static_assert(TOTAL * 8 <= 227 * 1024, "element region exceeds the shared memory of one CTA");
 };
 
@@ -165,6 +175,7 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
   double* pivInv = R + L::FL + NL;
   const bool diff = p.kc != 0;
   const bool euler = p.dt > 0.0;
+  const bool load = p.cacheMode == 2, store = p.cacheMode == 1;
   const double s = euler ? p.dt : 1.0;
 
   for (int64_t e = blockIdx.x; e < p.nCells; e += gridDim.x) {
@@ -197,6 +208,16 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
       }
       kap[i] = v;
     }
+    if (load) {
+      const double* ce = p.cache + e * L::CL;
+      for (int i = tid; i < N * N; i += kBT) Mm[i] = ce[L::C_MM + i];
+      for (int i = tid; i < D * N * N; i += kBT) MC[i] = ce[L::C_MC + i];
+      for (int i = tid; i < D * N * F * NF; i += kBT) ME[i] = ce[L::C_ME + i];
+      for (int i = tid; i < F * NT * NF * NF; i += kBT) Tm[i] = ce[L::C_TM + i];
+      for (int i = tid; i < F * D * NF * NF; i += kBT) Hf[i] = ce[L::C_HF + i];
+      for (int i = tid; i < N * N; i += kBT) KMs[i] = ce[L::C_KM + i];
+      for (int i = tid; i < N * F * NF; i += kBT) KEs[i] = ce[L::C_KE + i];
+    }
     __syncthreads();
     // ---------------------------------------------------------- geometry
     for (int q = tid; q < NI; q += kBT) {
@@ -214,12 +235,13 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
       iJ[q * 4 + 2] = -J[1][0] * id;  // (1,0)
       iJ[q * 4 + 3] = J[0][0] * id;   // (1,1)
       dV[q] = w[q] * det;
-      for (int a = 0; a < D * D; ++a) {  // Ds at q, column-major (HDGDiffusion.cpp:52-57)
-        double acc = 0.0;
-        if (diff)
-          for (int n = 0; n < N; ++n) acc += phi[q * N + n] * kap[n * D * D + a];
-        dsq[q * D * D + a] = acc;
-      }
+      if (!load)
+        for (int a = 0; a < D * D; ++a) {  // Ds at q, column-major (HDGDiffusion.cpp:52-57)
+          double acc = 0.0;
+          if (diff)
+            for (int n = 0; n < N; ++n) acc += phi[q * N + n] * kap[n * D * D + a];
+          dsq[q * D * D + a] = acc;
+        }
     }
     for (int fk = tid; fk < F * NIF; fk += kBT) {
       const int f = fk / NIF, k = fk % NIF;
@@ -252,11 +274,12 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
         g[a] = acc;
         G[qi * D + a] = acc;
       }
-      for (int a = 0; a < D; ++a) {
-        double acc = 0.0;
-        for (int b = 0; b < D; ++b) acc += dsq[q * D * D + a + b * D] * g[b];
-        KG[qi * D + a] = acc;
-      }
+      if (!load)
+        for (int a = 0; a < D; ++a) {
+          double acc = 0.0;
+          for (int b = 0; b < D; ++b) acc += dsq[q * D * D + a + b * D] * g[b];
+          KG[qi * D + a] = acc;
+        }
     }
     for (int fq = tid; fq < F * NIF; fq += kBT) {
       const int f = fq / NIF, k = fq % NIF;
@@ -275,6 +298,7 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
       double t = 0.0;
       for (int c = 0; c < D; ++c) t += trq[c] * nrm[fq * D + c];
       tn[fq] = t * ds;
+      if (load) continue;  // tau and the diffusion tensor at the face IPs feed cached blocks only
       for (int v = 0; v < NT; ++v) {
         double acc = 0.0;
         for (int a = 0; a < NF; ++a) acc += fphi[k * NF + a] * tauL[(f * NF + a) * NT + v];
@@ -317,7 +341,14 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
     }
     __syncthreads();
     // ------------------------------------------------------ scalar blocks
-    for (int ij = tid; ij < N * N; ij += kBT) {
+    if (load)
+      for (int ij = tid; ij < N * N; ij += kBT) {
+        const int i = ij / N, j = ij % N;
+        double tt = 0.0;
+        for (int q = 0; q < NI; ++q) tt += aq[q * N + i] * phi[q * N + j];
+        t1[ij] = tt;
+      }
+    for (int ij = tid; ij < N * N && !load; ij += kBT) {
       const int i = ij / N, j = ij % N;
       double m = 0.0, c[D] = {}, kp[D] = {}, tt = 0.0;
       for (int q = 0; q < NI; ++q) {
@@ -347,7 +378,7 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
         KP[k * N * N + ij] = diff ? kp[k] : 0.0;
       }
     }
-    for (int x = tid; x < F * D * NF * NF; x += kBT) {
+    for (int x = tid; x < F * D * NF * NF && !load; x += kBT) {
       // E_fk, H_fk: entry ((f*D + k)*NF + a)*NF + b
       const int f = x / (D * NF * NF), k = (x / (NF * NF)) % D, a = (x / NF) % NF, b = x % NF;
       double ev = 0.0, hv = 0.0;
@@ -360,7 +391,7 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
       Ef[x] = ev;
       Hf[x] = diff ? hv : 0.0;
     }
-    for (int x = tid; x < F * NT * NF * NF; x += kBT) {
+    for (int x = tid; x < F * NT * NF * NF && !load; x += kBT) {
       // tau masses: entry (((f*ND + c)*ND + m)*NF + a)*NF + b, tau column-major ((c, m) at m*ND + c)
       const int f = x / (NT * NF * NF), c = (x / (ND * NF * NF)) % ND, m = (x / (NF * NF)) % ND;
       const int a = (x / NF) % NF, b = x % NF;
@@ -400,54 +431,66 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
       Cuu[x] = -((c == m ? t1[i * N + j] : 0.0) + Xc[x] + Xc[(j * ND + c) * NU + i * ND + m]);
     }
     __syncthreads();
-    // mass inverse: Gauss-Jordan on [M | I] (M is symmetric positive definite). Only
-    // the columns right of the pivot are updated: the ones left of it are never read
-    // again, and column k is read unchanged as the elimination factors.
-    for (int k = 0; k < N; ++k) {
-      const double pinv = 1.0 / MI[k * 2 * N + k];
-      for (int j = k + 1 + tid; j < 2 * N; j += kBT) MI[k * 2 * N + j] *= pinv;
-      __syncthreads();
-      const int nc = 2 * N - k - 1;
-      for (int x = tid; x < (N - 1) * nc; x += kBT) {
-        int i = x / nc;
-        const int j = k + 1 + x % nc;
-        if (i >= k) ++i;
-        MI[i * 2 * N + j] -= MI[i * 2 * N + k] * MI[k * 2 * N + j];
-      }
-      __syncthreads();
-    }
-    for (int x = tid; x < D * N * N; x += kBT) {
-      const int k = x / (N * N), l = (x / N) % N, j = x % N;
-      double acc = 0.0;
-      for (int i = 0; i < N; ++i) acc += MI[l * 2 * N + N + i] * Ck[k * N * N + i * N + j];
-      MC[x] = acc;
-    }
-    for (int x = tid; x < D * N * F * NF; x += kBT) {
-      const int k = x / (N * F * NF), l = (x / (F * NF)) % N, fb = x % (F * NF);
-      const int f = fb / NF, b = fb % NF;
-      double acc = 0.0;
-      for (int a = 0; a < NF; ++a)
-        acc += MI[l * 2 * N + N + sFaceNodes[f * NF + a]] * Ef[((f * D + k) * NF + a) * NF + b];
-      ME[x] = acc;
-    }
-    __syncthreads();
-    if (diff) {
-      // the Schur products sum_k K'_k M^-1 C_k and sum_k K'_k M^-1 E_k (shared by every (c, m))
-      for (int x = tid; x < N * N + N * F * NF; x += kBT) {
-        double acc = 0.0;
-        if (x < N * N) {
-          const int i = x / N, j = x % N;
-          for (int k = 0; k < D; ++k)
-            for (int l = 0; l < N; ++l) acc += KP[k * N * N + i * N + l] * MC[k * N * N + l * N + j];
-          KMs[x] = acc;
-        } else {
-          const int y = x - N * N, i = y / (F * NF), fb = y % (F * NF);
-          for (int k = 0; k < D; ++k)
-            for (int l = 0; l < N; ++l) acc += KP[k * N * N + i * N + l] * ME[(k * N + l) * F * NF + fb];
-          KEs[y] = acc;
+    if (!load) {
+      // mass inverse: Gauss-Jordan on [M | I] (M is symmetric positive definite). Only
+      // the columns right of the pivot are updated: the ones left of it are never read
+      // again, and column k is read unchanged as the elimination factors.
+      for (int k = 0; k < N; ++k) {
+        const double pinv = 1.0 / MI[k * 2 * N + k];
+        for (int j = k + 1 + tid; j < 2 * N; j += kBT) MI[k * 2 * N + j] *= pinv;
+        __syncthreads();
+        const int nc = 2 * N - k - 1;
+        for (int x = tid; x < (N - 1) * nc; x += kBT) {
+          int i = x / nc;
+          const int j = k + 1 + x % nc;
+          if (i >= k) ++i;
+          MI[i * 2 * N + j] -= MI[i * 2 * N + k] * MI[k * 2 * N + j];
         }
+        __syncthreads();
+      }
+      for (int x = tid; x < D * N * N; x += kBT) {
+        const int k = x / (N * N), l = (x / N) % N, j = x % N;
+        double acc = 0.0;
+        for (int i = 0; i < N; ++i) acc += MI[l * 2 * N + N + i] * Ck[k * N * N + i * N + j];
+        MC[x] = acc;
+      }
+      for (int x = tid; x < D * N * F * NF; x += kBT) {
+        const int k = x / (N * F * NF), l = (x / (F * NF)) % N, fb = x % (F * NF);
+        const int f = fb / NF, b = fb % NF;
+        double acc = 0.0;
+        for (int a = 0; a < NF; ++a)
+          acc += MI[l * 2 * N + N + sFaceNodes[f * NF + a]] * Ef[((f * D + k) * NF + a) * NF + b];
+        ME[x] = acc;
       }
       __syncthreads();
+      if (diff) {
+        // the Schur products sum_k K'_k M^-1 C_k and sum_k K'_k M^-1 E_k (shared by every (c, m))
+        for (int x = tid; x < N * N + N * F * NF; x += kBT) {
+          double acc = 0.0;
+          if (x < N * N) {
+            const int i = x / N, j = x % N;
+            for (int k = 0; k < D; ++k)
+              for (int l = 0; l < N; ++l) acc += KP[k * N * N + i * N + l] * MC[k * N * N + l * N + j];
+            KMs[x] = acc;
+          } else {
+            const int y = x - N * N, i = y / (F * NF), fb = y % (F * NF);
+            for (int k = 0; k < D; ++k)
+              for (int l = 0; l < N; ++l) acc += KP[k * N * N + i * N + l] * ME[(k * N + l) * F * NF + fb];
+            KEs[y] = acc;
+          }
+        }
+        __syncthreads();
+      }
+      if (store) {
+        double* ce = p.cache + e * L::CL;
+        for (int i = tid; i < N * N; i += kBT) ce[L::C_MM + i] = Mm[i];
+        for (int i = tid; i < D * N * N; i += kBT) ce[L::C_MC + i] = MC[i];
+        for (int i = tid; i < D * N * F * NF; i += kBT) ce[L::C_ME + i] = ME[i];
+        for (int i = tid; i < F * NT * NF * NF; i += kBT) ce[L::C_TM + i] = Tm[i];
+        for (int i = tid; i < F * D * NF * NF; i += kBT) ce[L::C_HF + i] = Hf[i];
+        for (int i = tid; i < N * N; i += kBT) ce[L::C_KM + i] = diff ? KMs[i] : 0.0;
+        for (int i = tid; i < N * F * NF; i += kBT) ce[L::C_KE + i] = diff ? KEs[i] : 0.0;
+      }
     }
     // ------------------------------------- augmented Schur system [A | -B | Fu]
     for (int x = tid; x < NU * (W - 1); x += kBT) {
@@ -714,6 +757,18 @@ size_t burgers_smem_bytes(int dim, int order) {
     case 3: return sizeof(double) * BL<2, 3>::TOTAL;
     case 4: return sizeof(double) * BL<2, 4>::TOTAL;
     case 5: return sizeof(double) * BL<2, 5>::TOTAL;
+  }
+  return 0;
+}
+
+size_t burgers_cache_doubles(int dim, int order) {
+  if (dim != 2) return 0;
+  switch (order) {
+    case 1: return BL<2, 1>::CL;
+    case 2: return BL<2, 2>::CL;
+    case 3: return BL<2, 3>::CL;
+    case 4: return BL<2, 4>::CL;
+    case 5: return BL<2, 5>::CL;
   }
   return 0;
 }

@@ -98,8 +98,13 @@ struct BurgersParams {
   const int* itab;             // faceNodes[F*NF], faceOpposite[F]
   double *S, *S0, *U, *Q, *U0, *Q0;
   int* status;                 // 1 = singular Schur block
+  // per-element cache of the state-independent blocks ([nCells][burgers_cache_doubles]):
+  // cacheMode 0 compute only, 1 compute and store, 2 load (geometry, tau, diffusion unchanged)
+  double* cache;
+  int cacheMode;
 };
 bool burgers_supported(int dim, int order);
+size_t burgers_cache_doubles(int dim, int order);
 size_t burgers_smem_bytes(int dim, int order);
 cudaError_t launch_burgers_local(int dim, int order, const BurgersParams& p, cudaStream_t s);
 // NonLinearWrapper pieces: out[0] = sum (sol - buf)^2, out[1] = sum buf^2 (deterministic
