@@ -1716,10 +1716,11 @@ int hfx_coarse_train(hfx_ctx* c, int degree, int samples, int steps, hfx_train_i
   CoarseTrainResult tr;
   cudaError_t e = coarse_train(&c->coarse, buf, S, degree, steps, 0.05, c->stream, &tr);
   if (e == cudaSuccess && !tr.accepted && steps > 0) {
-    // no accepted improvement (a spectrum the default step overshoots): one more round
-    // from Chebyshev with a smaller step; a rejected round leaves the coarse solve as it was
+    // no accepted improvement (every lower-loss step left the residual polynomial above 1):
+    // one more round from Chebyshev that keeps each step inside that bound; a rejected
+    // round leaves the coarse solve as it was
     CoarseTrainResult tr2;
-    e = coarse_train(&c->coarse, buf, S, degree, steps, 0.01, c->stream, &tr2);
+    e = coarse_train(&c->coarse, buf, S, degree, steps, 0.05, c->stream, &tr2, true);
     if (e == cudaSuccess) {
       tr2.lowerSteps += tr.lowerSteps;
       tr2.rejectedSteps += tr.rejectedSteps;

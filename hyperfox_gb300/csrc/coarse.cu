@@ -975,7 +975,7 @@ cudaError_t coarse_loss_grad(const CoarseSolver& cs, const float* samples, int S
 }
 
 cudaError_t coarse_train(CoarseSolver* cs, const float* samples, int S, int K, int steps, double lr, cudaStream_t s,
-                         CoarseTrainResult* out) {
+                         CoarseTrainResult* out, bool feasible) {
   *out = CoarseTrainResult{};
   out->degree = K;
   out->samples = S;
@@ -1014,6 +1014,7 @@ cudaError_t coarse_train(CoarseSolver* cs, const float* samples, int S, int K, i
   std::vector<double> m1(K, 0.0), m2(K, 0.0);
   const double b1 = 0.9, b2 = 0.999;
   std::vector<double> pgrad(K);
+  std::vector<double> step(K), trial(K), thTrial(K);
   for (int it = 0; it < steps; ++it) {
     poly_penalty(theta, lmax, &pgrad);
     for (int k = 0; k < K; ++k) {
@@ -1021,7 +1022,27 @@ cudaError_t coarse_train(CoarseSolver* cs, const float* samples, int S, int K, i
       m1[k] = b1 * m1[k] + (1 - b1) * g;
       m2[k] = b2 * m2[k] + (1 - b2) * g * g;
       const double mh = m1[k] / (1 - std::pow(b1, it + 1)), vh = m2[k] / (1 - std::pow(b2, it + 1));
-      phi[k] -= lr * mh / (std::sqrt(vh) + 1e-12);
+      step[k] = lr * mh / (std::sqrt(vh) + 1e-12);
+    }
+    if (feasible) {
+      // stay inside the set where the residual polynomial is <= 1 on [0, lmax]: halve
+      // the step until it is (twelve halvings at most; otherwise no move this step)
+      double sc = 1.0;
+      bool ok = false;
+      for (int bt = 0; bt < 12 && !ok; ++bt, sc *= 0.5) {
+        for (int k = 0; k < K; ++k) {
+          trial[k] = phi[k] - sc * step[k];
+          thTrial[k] = std::exp(trial[k]) / lmax;
+        }
+        ok = poly_max(thTrial, lmax) <= 1.0 + 1e-9;
+      }
+      if (!ok) {
+        ++out->rejectedSteps;
+        continue;
+      }
+      phi = trial;
+    } else {
+      for (int k = 0; k < K; ++k) phi[k] -= step[k];
     }
     thetas();
     if ((e = learn_pass(cs->dev, lw, S, K, theta.data(), &L, grad.data(), hp, s)) != cudaSuccess) break;

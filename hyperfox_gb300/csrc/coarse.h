@@ -99,9 +99,11 @@ struct CoarseTrainResult {
 // sample s contiguous) by Adam on log(theta * lmax), with the project's forward
 // and backward kernels. Accepted only if prod_k (1 - theta_k lambda) <= 1 on
 // [0, lmax] (the coarse solve then stays symmetric positive semidefinite)
-// and the loss beats Chebyshev of the same degree.
+// and the loss beats Chebyshev of the same degree. feasible: every step is shortened
+// (halved, at most twelve times) until the residual polynomial stays <= 1, so the
+// optimiser moves only through polynomials that could be accepted.
 cudaError_t coarse_train(CoarseSolver* c, const float* samples, int S, int K, int steps, double lr, cudaStream_t s,
-                         CoarseTrainResult* out);
+                         CoarseTrainResult* out, bool feasible = false);
 // Loss and gradient of the learned polynomial for given theta (unscaled) on
 // samples [S][nV]: the GPU kernels coarse_train uses (for gradient checks).
 cudaError_t coarse_loss_grad(const CoarseSolver& c, const float* samples, int S, int K, const double* theta,
