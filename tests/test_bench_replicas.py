@@ -51,3 +51,37 @@ def test_reference_arm_under_torchrun_prints_once():
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["value"] > 0 and d["cpu_baseline"]["kind"] == "port"
+
+
+def test_burgers_reference_arm_prints_its_metric():
+    """The Burgers workload's reference arm (the oracle's HDGBurgersModel + Newton loop on
+    a bounded sample) prints one line in the GPU arm's unit."""
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1", "--warmup", "0",
+           "--config", "burgers-small"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["unit"] == "elements*newton_iterations/s" and d["value"] > 0
+    assert d["cpu_baseline"]["kind"] == "port" and "Newton" in d["cpu_baseline"]["sample"]
+
+
+def test_anisotropic_lognormal_field():
+    """The configs[4] coefficient: exp(g) (I + 99 a a^T) per cell, g of standard deviation
+    1.5, exactly symmetric and constant inside every cell (so the trace system is
+    symmetric and the CG path applies)."""
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    import bench
+    cfg = bench.CONFIGS["cfg5-small"]
+    coords, cells = bench.make_problem(cfg)
+    k = bench.aniso_kappa(coords, cells, 3, **cfg["aniso"])
+    assert k.shape == (cells.shape[0], cells.shape[1], 9)
+    assert np.array_equal(k, np.broadcast_to(k[:, :1, :], k.shape))
+    K = k[:, 0, :].reshape(-1, 3, 3)
+    assert np.array_equal(K, np.swapaxes(K, 1, 2))
+    ev = np.linalg.eigvalsh(K)
+    assert np.allclose(ev[:, 2] / ev[:, 0], 100.0)
+    g = np.log(ev[:, 0])
+    assert abs(g.std() - 1.5) < 0.15 and abs(g.mean()) < 0.3
