@@ -477,15 +477,18 @@ def run_burgers(args, world, rank, local):
     sol_h = pin(u0.shape)
     sol_h[:] = u0
 
-    def newton(warm):
-        o = capi.newton_opts(res_tol=1e-6, max_iters=20, warm_start=int(warm), lin_rtol=1e-10,
+    starts = {"zero": (0, 0), "warm": (1, 0), "history": (1, 6)}  # (warm_start, history)
+
+    def newton(mode):
+        ws, hist = starts[mode]
+        o = capi.newton_opts(res_tol=1e-6, max_iters=20, warm_start=ws, history=hist, lin_rtol=1e-10,
                              lin_precond=capi.PC_BLOCK_JACOBI, lin_maxits=20000)
         info = capi.NewtonInfo()
         ctx._chk(L.hfx_burgers_newton(ctx.h, capi.ctypes.byref(o), capi.ctypes.byref(info)), "burgers_newton")
         return info
 
     steps = args.steps if args.steps_given else cfg["time_steps"] - args.warmup
-    warm = not args.cold_start
+    warm = args.krylov_start
     B.set_state(solution=u0, trace=np.zeros(B.ndofs))
     for _ in range(args.warmup):
         ctx._chk(L.hfx_burgers_begin_step(ctx.h), "begin_step")
@@ -513,12 +516,18 @@ def run_burgers(args, world, rank, local):
         L.hfx_kernel_time(ctx.h, kid, capi.ctypes.byref(n_l), capi.ctypes.byref(t_l))
         kt[name] = (n_l.value, t_l.value)
     ctx._chk(L.hfx_profile_enable(ctx.h, 0), "profile")
-    # the Krylov start compared: a few steps from the same state with the other choice
+    # the Krylov starts compared: five steps from the same state with each other choice
     sol_keep, _, trace_keep, _ = B.get_state()
-    alt = []
-    for _ in range(5):
-        ctx._chk(L.hfx_burgers_begin_step(ctx.h), "begin_step")
-        alt.append(newton(not warm))
+    alt = {}
+    for mode in starts:
+        if mode == warm:
+            continue
+        B.set_state(solution=sol_keep, trace=trace_keep)
+        infos = []
+        for _ in range(5):
+            ctx._chk(L.hfx_burgers_begin_step(ctx.h), "begin_step")
+            infos.append(newton(mode))
+        alt[mode] = infos
     B.set_state(solution=sol_keep, trace=trace_keep)
     # e2e: the step's Solution uploaded from pinned host memory and downloaded after the Newton loop
     barrier(world)
@@ -556,15 +565,16 @@ def run_burgers(args, world, rank, local):
         "data": "synthetic (structured mesh, seeded initial noise N(0, 0.01) on both components)",
         "config": {"workload": cfg["desc"], "elements": E, "order": p, "trace_dofs": B.ndofs, "csr_nnz": B.nnz,
                    "krylov": "GMRES(30) + per-face block Jacobi, FP64, rtol 1e-10",
-                   "krylov_start": "previous trace (warm)" if warm else "zero (PETSc default)",
+                   "krylov_start": {"zero": "zero (PETSc default)", "warm": "previous trace (warm)",
+                                    "history": "least-squares fit of the last 6 trace solutions"}[warm],
                    "l2_flush": "none: inputs (element blocks 1.1 GB) exceed L2", "parallelism": "single GPU"},
         "newton_iterations_per_step": nl / steps,
         "krylov_iterations_per_newton": sum(kits) / max(1, nl),
-        "other_krylov_start": {"krylov_start": "zero (PETSc default)" if warm else "previous trace (warm)",
-                               "newton_iterations_per_step": sum(a.iterations for a in alt) / len(alt),
-                               "krylov_iterations_per_newton": sum(a.krylov_iterations for a in alt) /
-                               max(1, sum(a.iterations for a in alt)),
-                               "assemble_plus_solve_ms_per_step": sum(a.assemble_ms + a.solve_ms for a in alt) / len(alt)},
+        "other_krylov_starts": {mode: {"newton_iterations_per_step": sum(a.iterations for a in v) / len(v),
+                                       "krylov_iterations_per_newton": sum(a.krylov_iterations for a in v) /
+                                       max(1, sum(a.iterations for a in v)),
+                                       "assemble_plus_solve_ms_per_step": sum(a.assemble_ms + a.solve_ms for a in v) / len(v)}
+                                for mode, v in alt.items()},
         "element_kernel_elements_per_s": E / (avg_ms / 1e3),
         "kernel_ms": {k: dict(launches=v[0], total_ms=round(v[1], 3)) for k, v in kt.items()},
         "roofline": roof,
@@ -678,7 +688,9 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--traffic", type=float, default=None, help="ncu DRAM bytes per launch of the top kernel")
-    ap.add_argument("--cold-start", action="store_true", help="Burgers: start every Krylov solve from zero")
+    ap.add_argument("--krylov-start", default="history", choices=["zero", "warm", "history"],
+                    help="Burgers: Krylov initial guess: zero (PETSc), the previous trace, or the least-squares "
+                         "fit of the last 6 trace solutions")
     args = ap.parse_args()
     args.steps_given = args.steps is not None
     if args.steps is None:

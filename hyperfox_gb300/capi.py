@@ -88,7 +88,7 @@ class TrainInfo(ctypes.Structure):
 
 class NewtonOpts(ctypes.Structure):
     _fields_ = [("res_tol", ctypes.c_double), ("max_iters", ctypes.c_int), ("dampening", ctypes.c_double),
-                ("lin", SolveOpts), ("warm_start", ctypes.c_int)]
+                ("lin", SolveOpts), ("warm_start", ctypes.c_int), ("history", ctypes.c_int)]
 
 
 class NewtonInfo(ctypes.Structure):

@@ -76,6 +76,9 @@ struct BurgersState {
   uint8_t* permx = nullptr;  // face2CellMap at DOF level: [nCells][F][Nf*nd]
   double* cache = nullptr;   // state-independent element blocks, valid while cacheValid
   bool cacheValid = false;
+  // the last trace solutions (ring, most recent at histHead - 1) and their images under A'
+  double *hist = nullptr, *histY = nullptr;
+  int histCap = 0, histCount = 0, histHead = 0;
   int* status = nullptr;
   unsigned* ticket = nullptr;
   DevMem wsMem;
@@ -93,6 +96,8 @@ struct BurgersState {
     src.release();
     dir.release();
     ready = assembled = solved = cacheValid = false;
+    hist = histY = nullptr;
+    histCap = histCount = histHead = 0;
   }
 };
 
@@ -2056,7 +2061,10 @@ int hfx_burgers_set_state(hfx_ctx* c, const double* solution, const double* buff
   if (solution) HFX_CUDA(c, cudaMemcpyAsync(B.sol, solution, sizeof(double) * nu, cudaMemcpyHostToDevice, s));
   if (buffer) HFX_CUDA(c, cudaMemcpyAsync(B.buf, buffer, sizeof(double) * nu, cudaMemcpyHostToDevice, s));
   if (oldSolution) HFX_CUDA(c, cudaMemcpyAsync(B.old, oldSolution, sizeof(double) * nu, cudaMemcpyHostToDevice, s));
-  if (trace) HFX_CUDA(c, cudaMemcpyAsync(B.trace, trace, sizeof(double) * B.nDofs, cudaMemcpyHostToDevice, s));
+  if (trace) {
+    HFX_CUDA(c, cudaMemcpyAsync(B.trace, trace, sizeof(double) * B.nDofs, cudaMemcpyHostToDevice, s));
+    B.histCount = 0;  // a new trace: the earlier solutions may no longer span it
+  }
   HFX_CUDA(c, cudaStreamSynchronize(s));
   return HFX_OK;
 }
@@ -2171,8 +2179,11 @@ static int burgers_check_opts(hfx_ctx* c, const hfx_solve_opts& o) {
   return HFX_OK;
 }
 
-// GMRES + recovery, queued on the stream; returns the Krylov status.
-static int burgers_solve_core(hfx_ctx* c, const hfx_solve_opts& o, TraceSolveResult* res, int* kst) {
+// GMRES + recovery, queued on the stream; returns the Krylov status. history > 0: the
+// initial guess is the least-squares fit of the last `history` solutions (then the
+// solution joins them).
+static int burgers_solve_core(hfx_ctx* c, const hfx_solve_opts& o, TraceSolveResult* res, int* kst,
+                              int history = 0) {
   BurgersState& B = c->burgers;
   const int restart = o.restart > 0 ? o.restart : 30;
   DevMem& m = B.wsMem;
@@ -2212,8 +2223,30 @@ static int burgers_solve_core(hfx_ctx* c, const hfx_solve_opts& o, TraceSolveRes
   a.stream = c->stream;
   a.timer = &c->timer;
   a.restart = restart;
+  if (history > 0) {
+    if (B.histCap < history) {
+      HFX_CUDA(c, dalloc(m, &B.hist, n * (size_t)history));
+      HFX_CUDA(c, dalloc(m, &B.histY, n * (size_t)history));
+      B.histCap = history;
+      B.histCount = B.histHead = 0;
+    }
+    const int cnt = std::min(B.histCount, history);
+    if (cnt > 0) {
+      trace_prepare(a);
+      a.prepared = 1;
+      const double* X[8];
+      for (int i = 0; i < cnt; ++i) X[i] = B.hist + (size_t)((B.histHead - 1 - i + B.histCap) % B.histCap) * n;
+      if (trace_projection_guess(a, X, cnt, B.histY) > 0) a.use_initial_guess = 1;
+    }
+  }
   *kst = trace_gmres(a, res);
   if (*kst == 3) return cuda_err(c, res->cudaErr, "burgers_solve");
+  if (history > 0 && *kst == 0) {
+    HFX_CUDA(c, cudaMemcpyAsync(B.hist + (size_t)B.histHead * n, B.trace, sizeof(double) * n,
+                                cudaMemcpyDeviceToDevice, c->stream));
+    B.histHead = (B.histHead + 1) % B.histCap;
+    B.histCount = std::min(B.histCount + 1, B.histCap);
+  }
   RecoverParams rp{c->nCells, c->re.nFaces, B.NLF, B.NU, B.NQ, B.NL, c->d_cell2face, B.permx,
                    B.U, B.Q, B.U0, B.Q0, B.trace, B.sol, B.flux};
   c->timer.begin(K_RECOVER, c->stream);
@@ -2276,6 +2309,7 @@ void hfx_newton_opts_default(hfx_newton_opts* o) {
   o->lin.method = HFX_KSP_GMRES;
   o->lin.rtol = 1e-12;
   o->warm_start = 0;
+  o->history = 0;
 }
 
 int hfx_burgers_newton(hfx_ctx* c, const hfx_newton_opts* opts, hfx_newton_info* info) {
@@ -2284,8 +2318,10 @@ int hfx_burgers_newton(hfx_ctx* c, const hfx_newton_opts* opts, hfx_newton_info*
   hfx_newton_opts o;
   if (opts) o = *opts;
   else hfx_newton_opts_default(&o);
-  if (!(o.res_tol > 0.0) || o.max_iters <= 0 || !(o.dampening >= 0.0 && o.dampening < 1.0))
-    return set_err(c, HFX_ERR_ARG, "burgers_newton: res_tol > 0, max_iters > 0, 0 <= dampening < 1");
+  if (!(o.res_tol > 0.0) || o.max_iters <= 0 || !(o.dampening >= 0.0 && o.dampening < 1.0) || o.history < 0 ||
+      o.history > 8)
+    return set_err(c, HFX_ERR_ARG,
+                   "burgers_newton: res_tol > 0, max_iters > 0, 0 <= dampening < 1, 0 <= history <= 8");
   if (int rc = burgers_check_opts(c, o.lin)) return rc;
   hfx_solve_opts lin = o.lin;
   lin.use_initial_guess = o.warm_start ? 1 : 0;
@@ -2301,7 +2337,7 @@ int hfx_burgers_newton(hfx_ctx* c, const hfx_newton_opts* opts, hfx_newton_info*
     cudaEventRecord(ev[1], s);
     TraceSolveResult res;
     int st = 0;
-    if ((rc = burgers_solve_core(c, lin, &res, &st))) break;
+    if ((rc = burgers_solve_core(c, lin, &res, &st, o.history))) break;
     cudaEventRecord(ev[2], s);
     if (cudaError_t e = launch_newton_residual(nu, B.sol, B.buf, B.partials, B.ticket, B.red, s)) {
       rc = cuda_err(c, e, "burgers_newton: residual");

@@ -70,6 +70,7 @@ struct TraceSolveArgs {
   float* sampleBuf;            // [sampleCap][nV]
   int sampleCap, sampleStride;
   int* sampleCount;            // host counter
+  int prepared;                // GMRES: b' and the preconditioner are already in ws (trace_prepare ran)
 };
 
 struct TraceSolveResult {
@@ -81,6 +82,12 @@ struct TraceSolveResult {
 // Returns an HFX status code (0 = converged).
 int trace_solve(const TraceSolveArgs& a, TraceSolveResult* out);   // CG (symmetric systems)
 int trace_gmres(const TraceSolveArgs& a, TraceSolveResult* out);   // GMRES (any system)
+// Least-squares initial guess for the eliminated system A' x = b' from K <= 8 earlier
+// solutions X[i] (projection onto previous solutions for a sequence of systems): writes
+// x0 = sum_i c_i X[i] into a.x with c minimising ||b' - A' sum_i c_i X[i]||_2; Y is
+// K * n scratch. Needs trace_prepare(a) (b' in a.ws.bS). Returns the number of vectors
+// kept (nearly dependent ones are dropped), 0 leaving a.x as it was.
+int trace_projection_guess(const TraceSolveArgs& a, const double* const* X, int K, double* Y);
 size_t trace_partials_needed();
 // Shared pieces: b', the FP32 copy of A' (mixed) and the preconditioner; the
 // reference-system residual into out->rel_residual.

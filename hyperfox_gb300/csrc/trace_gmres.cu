@@ -337,7 +337,7 @@ int drive(const TraceSolveArgs& a, TraceSolveResult* out) {
   const int64_t n = A.nFaces * NF;
   const int m = a.restart;
   KernelTimer* tm = a.timer;
-  trace_prepare(a);
+  if (!a.prepared) trace_prepare(a);
   const int gVec = grid_for(multi_dot<double>, kT);
   double* x = a.x;
   int its = 0, status = 0, refinements = 0;
@@ -435,6 +435,98 @@ int drive(const TraceSolveArgs& a, TraceSolveResult* out) {
 }
 
 }  // namespace
+
+template <int NF, int NBMAX>
+int projection_t(const TraceSolveArgs& a, const double* const* X, int K, double* Y) {
+  cudaStream_t s = a.stream;
+  const TraceView& A = a.A;
+  const int64_t n = A.nFaces * NF;
+  const int gOp = grid_for(op_apply<double, NF, NBMAX, true>, kT);
+  const int gVec = grid_for(multi_dot<double>, kT);
+  for (int i = 0; i < K; ++i) op_apply<double, NF, NBMAX, true><<<gOp, kT, 0, s>>>(A, a.val, X[i], Y + (size_t)i * n);
+  // Gram matrix G_ij = <Y_i, Y_j> and g_i = <Y_i, b'>: one batched dot launch per column
+  std::vector<double> G((size_t)K * K), g(K), hp((size_t)(K + 1) * gVec);
+  auto dots = [&](const double* w, int cnt, std::vector<double>& out) {
+    const int gd = cnt > 1 ? std::max(8, gVec / cnt) : gVec;
+    if (cnt > 1) multi_dot_cols<double><<<dim3(gd, cnt), kT, 0, s>>>(n, Y, w, a.ws.partials);
+    else multi_dot<double><<<gd, kT, 0, s>>>(n, 1, Y, w, a.ws.partials);
+    cudaMemcpyAsync(hp.data(), a.ws.partials, sizeof(double) * cnt * gd, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    out.assign(cnt, 0.0);
+    for (int j = 0; j < cnt; ++j)
+      for (int k = 0; k < gd; ++k) out[j] += hp[(size_t)j * gd + k];
+  };
+  std::vector<double> col;
+  for (int j = 0; j < K; ++j) {
+    dots(Y + (size_t)j * n, K, col);
+    for (int i = 0; i < K; ++i) G[i + (size_t)j * K] = col[i];
+  }
+  dots(a.ws.bS, K, col);
+  g = col;
+  // Cholesky of G with the nearly dependent directions dropped (successive solutions are
+  // close to parallel): a pivot below 1e-12 of the largest diagonal removes that vector
+  double dmax = 0.0;
+  for (int i = 0; i < K; ++i) dmax = std::max(dmax, G[i + (size_t)i * K]);
+  if (!(dmax > 0.0) || !std::isfinite(dmax)) return 0;
+  std::vector<double> Lc((size_t)K * K, 0.0), c(K, 0.0), z(K, 0.0);
+  std::vector<int> keep;
+  for (int i = 0; i < K; ++i) {
+    double d = G[i + (size_t)i * K];
+    for (size_t a2 = 0; a2 < keep.size(); ++a2) d -= Lc[i + (size_t)keep[a2] * K] * Lc[i + (size_t)keep[a2] * K];
+    if (!(d > 1e-12 * dmax)) continue;
+    const double ld = std::sqrt(d);
+    Lc[i + (size_t)i * K] = ld;
+    for (int r = i + 1; r < K; ++r) {
+      double v = G[r + (size_t)i * K];
+      for (int kk : keep) v -= Lc[r + (size_t)kk * K] * Lc[i + (size_t)kk * K];
+      Lc[r + (size_t)i * K] = v / ld;
+    }
+    keep.push_back(i);
+  }
+  if (keep.empty()) return 0;
+  for (size_t a2 = 0; a2 < keep.size(); ++a2) {  // L z = g on the kept indices
+    const int i = keep[a2];
+    double v = g[i];
+    for (size_t b2 = 0; b2 < a2; ++b2) v -= Lc[i + (size_t)keep[b2] * K] * z[keep[b2]];
+    z[i] = v / Lc[i + (size_t)i * K];
+  }
+  for (int a2 = (int)keep.size() - 1; a2 >= 0; --a2) {  // L^T c = z
+    const int i = keep[a2];
+    double v = z[i];
+    for (size_t b2 = a2 + 1; b2 < keep.size(); ++b2) v -= Lc[keep[b2] + (size_t)i * K] * c[keep[b2]];
+    c[i] = v / Lc[i + (size_t)i * K];
+  }
+  for (double v : c)
+    if (!std::isfinite(v)) return 0;
+  // x0 = sum_i c_i X_i: the X_i are separate buffers, so add them one by one
+  scale_into<double><<<gVec, kT, 0, s>>>(n, c[0], X[0], a.x);
+  for (int i = 1; i < K; ++i) add_into<double><<<gVec, kT, 0, s>>>(n, c[i], X[i], a.x);
+  return (int)keep.size();
+}
+
+int trace_projection_guess(const TraceSolveArgs& a, const double* const* X, int K, double* Y) {
+  if (K < 1 || K > 8) return 0;
+  const int NF = a.A.NF;
+  if (a.dim == 2) {
+    switch (NF) {
+      case 2: return projection_t<2, 5>(a, X, K, Y);
+      case 3: return projection_t<3, 5>(a, X, K, Y);
+      case 4: return projection_t<4, 5>(a, X, K, Y);
+      case 5: return projection_t<5, 5>(a, X, K, Y);
+      case 6: return projection_t<6, 5>(a, X, K, Y);
+      case 8: return projection_t<8, 5>(a, X, K, Y);
+      case 10: return projection_t<10, 5>(a, X, K, Y);
+      case 12: return projection_t<12, 5>(a, X, K, Y);
+    }
+  } else if (a.dim == 3) {
+    switch (NF) {
+      case 3: return projection_t<3, 7>(a, X, K, Y);
+      case 6: return projection_t<6, 7>(a, X, K, Y);
+      case 10: return projection_t<10, 7>(a, X, K, Y);
+    }
+  }
+  return 0;
+}
 
 template <int NF, int NBMAX>
 int gmres_f32_t(const F32SolveArgs& a, int* its) {

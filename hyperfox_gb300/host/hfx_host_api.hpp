@@ -561,6 +561,7 @@ class NonLinearWrapper {
       o.dampening = dampening;
       o.lin = mySolver->linOpts();
       o.warm_start = warmStart ? 1 : 0;
+      o.history = history;
       mySolver->device()->check(hfx_burgers_newton(mySolver->device()->ctx(), &o, &lastInfo), "NonLinearWrapper",
                                 "solve");
       residual = lastInfo.residual;
@@ -601,6 +602,9 @@ class NonLinearWrapper {
   void setDampening(double d) { dampening = d; }
   // start every Krylov solve from the current trace (PETSc starts from zero)
   void setWarmStart(bool on) { warmStart = on; }
+  // start every Krylov solve from the least-squares fit of the last k (<= 8) trace
+  // solutions to the new system (device loop only; 0 = off)
+  void setKrylovHistory(int k) { history = k; }
   hfx_newton_info lastInfo{};
 
   // NonLinearWrapper::vanillaResidualComputer (NonLinearWrapper.cpp:14-34), one rank
@@ -620,7 +624,7 @@ class NonLinearWrapper {
   std::function<double(Field*, Field*)> residualComputer;
   std::function<void(GpuBurgersSolver*)> linearizedSolver;
   double residual = 0.0, resTol = 1e-6, dampening = 0.0;
-  int maxIters = 20;
+  int maxIters = 20, history = 0;
   bool verbose = false, warmStart = false;
 };
 

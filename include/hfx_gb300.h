@@ -367,6 +367,10 @@ typedef struct {
   hfx_solve_opts lin;      /* the linear solve of every iteration (GMRES, block Jacobi) */
   int warm_start;          /* 1: each Krylov solve starts from the current trace (PETSc starts
                               from zero, KSPSetInitialGuessNonzero is not called) */
+  int history;             /* 1..8: each Krylov solve starts from the least-squares fit of the
+                              last `history` trace solutions to the new system (min ||b' - A' x||
+                              over their span, which holds the previous solution), 0: off.
+                              No counterpart in the reference. */
 } hfx_newton_opts;
 
 typedef struct {

@@ -286,3 +286,50 @@ def test_state_independent_cache(hfx_lib):
         o, g = P.condensed(), B.condensed()
         for k in ("S", "S0", "U", "Q", "U0", "Q0"):
             assert relerr(g[k], o[k]) < 1e-12, (list(change), k)
+
+
+def test_krylov_history_guess(hfx_lib):
+    """Krylov starts from the least-squares fit of the last trace solutions (history 6):
+    four implicit Euler steps land on the oracle's solution (1e-8) like the warm start,
+    with no more Krylov iterations than the warm start (the fitted span holds the
+    previous solution, so the start's residual is never larger)."""
+    from hyperfox_gb300 import capi
+    p, n = 3, 6
+    re, coords, cells = mesh(2, n, p)
+    P = O.BurgersProblem(2, p, coords, cells)
+    rng = np.random.default_rng(7)
+    x = coords[cells]
+    u0 = np.sin(2 * np.pi * x[..., 0]) * np.sin(2 * np.pi * x[..., 1])
+    u0 = (np.stack([u0, u0], -1) + rng.normal(0, 0.01, size=x.shape)).reshape(P.nCells, -1)
+    tau = np.zeros((P.nFaces, re["nNodesFace"], 2, 4))
+    tau[..., 0] = tau[..., 3] = 1.0
+    nu = np.full((P.nCells, re["nNodes"], 1), 1e-2)
+    zero = np.zeros((P.nFaces, re["nNodesFace"], 2))
+    # oracle trajectory
+    u, trace, ref = u0.copy(), np.zeros(P.ndofs), []
+    for step in range(4):
+        P.set_fields(tau=tau, tau_sides=2, nu=nu, dirichlet=zero, dt=1e-3, old=u)
+        P.buf, P.trace = u.copy(), trace
+        u, _, _, _ = P.newton(res_tol=1e-10, max_iters=10)
+        trace = P.trace
+        ref.append(u)
+    kry = {}
+    for mode, (warm, hist) in {"warm": (1, 0), "history": (1, 6)}.items():
+        ctx = capi.Context(0)
+        ctx.upload_mesh(2, p, coords, cells)
+        B = capi.Burgers(ctx)
+        B.set_tau(tau, 2)
+        B.set_diffusion(nu, layout=1)
+        B.set_dirichlet(zero)
+        B.set_time_step(1e-3)
+        B.set_state(solution=u0)
+        kry[mode] = 0
+        for step in range(4):
+            B.begin_step()
+            info = B.newton(res_tol=1e-10, max_iters=10, lin_rtol=1e-13, warm_start=warm, history=hist)
+            assert info.status == 0
+            kry[mode] += info.krylov_iterations
+            sol, _, _, _ = B.get_state()
+            assert relerr(sol, ref[step]) < 1e-8, (mode, step)
+        ctx.close()
+    assert kry["history"] <= kry["warm"], kry
