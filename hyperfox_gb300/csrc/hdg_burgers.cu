@@ -22,8 +22,13 @@
 // the Schur block A = s (Suu - Suq Sqq^{-1} Squ) (+ M (x) I) couples the
 // components and is solved by Gauss-Jordan with partial pivoting. Results equal
 // the reference's dense QR condensation up to round-off.
-#include <cstdio>
-
+//
+// The blocks that depend only on geometry, tau and the diffusion field (M, M^-1 C_k,
+// M^-1 E_k, the tau masses, H and the two Schur products) are stored per element by
+// the first linearisation (cacheMode 1) and loaded by the later ones (cacheMode 2):
+// a Newton iteration then recomputes only the convection terms, the Schur system,
+// Q and S. The caller invalidates the cache when the mesh, tau or the diffusion
+// field changes.
 #include "hfx_device.h"
 
 namespace hfx {
