@@ -41,9 +41,6 @@ METRIC = "time-to-solve @1e-8 rel err, learned+mixed vs plain FP64 GPU; elements
 # affine element kernel reads and writes 19.7 KB per p=3 tetrahedron.
 TRAFFIC_PER_NNZ = {"spmv32": 175.1e6 / 67.44e6, "spmv64": 590.2e6 / 67.44e6}
 TRAFFIC_PER_ELEMENT_LOCAL = (54.0e6 + 890.3e6) / 48000
-# the Burgers element kernel at 2D p=3 loading its per-element cache (96x96x2 capture):
-# 173.0 MB read + 253.3 MB written for 18,432 elements
-TRAFFIC_PER_ELEMENT_BURGERS_P3 = (173.0e6 + 253.3e6) / 18432
 FP64_NOMINAL_TFLOPS = 1.25
 
 CONFIGS = {
@@ -449,9 +446,12 @@ def burgers_flops_per_element(N, NF, F, NI, NIF, D=2, cached=False):
     ops += minv + mcme + kmke
     ops += NU * NU * 6 + NU * NL * 6 + NU * (2 * NU + 2 * NL + 2 * NI + 2 * N)  # [A | -B | Fu]
     ops += sum(2 * (NU - 1) * (W - k - 1) + (W - k - 1) for k in range(NU))  # Gauss-Jordan
-    ops += NQ * (NL + 1) * 2 * N + NL * (NL + 1) * NF * (2 * ND + 2 * D)  # Q, S
+    hmce = 2 * NF * D * (F * NF * N + F * NF * F * NF)                  # H M^-1 C, H M^-1 E
+    ops += hmce
+    ops += NL * (NL + 1) * (2 * NF * ND + 2 * N)                         # S (Q is not formed)
     if cached:
-        ops -= 2 * NI * D * D * N + 2 * NI * N * D * D + face_static + scalar_static + ehT + minv + mcme + kmke
+        ops -= (2 * NI * D * D * N + 2 * NI * N * D * D + face_static + scalar_static + ehT + minv + mcme + kmke
+                + hmce)
     return ops
 
 
@@ -554,7 +554,7 @@ def run_burgers(args, world, rank, local):
     roof = dict(bound="fp64", kernel="burgers_local<2,3> (FP64 assembly + condensation, vector Burgers, "
                                      "state-independent blocks from the per-element cache)",
                 achieved=round(tf, 3), peak=FP64_NOMINAL_TFLOPS, unit="TFLOP/s", frac=round(tf / FP64_NOMINAL_TFLOPS, 4),
-                traffic=args.traffic or (TRAFFIC_PER_ELEMENT_BURGERS_P3 * E if p == 3 else None),
+                traffic=args.traffic,  # no ncu capture of the current kernel (the committed one still formed Q)
                 flops_per_element=int(flops), avg_launch_ms=round(avg_ms, 4),
                 peak_source="nominal GB300 FP64 (no measured FP64 peak)")
     nl = sum(its)

@@ -2120,9 +2120,7 @@ static int burgers_assemble_async(hfx_ctx* c) {
   p.S = B.S;
   p.S0 = B.S0;
   p.U = B.U;
-  p.Q = B.Q;
   p.U0 = B.U0;
-  p.Q0 = B.Q0;
   p.status = B.status;
   p.cache = B.cache;
   p.cacheMode = B.cacheValid ? 2 : 1;
@@ -2247,10 +2245,9 @@ static int burgers_solve_core(hfx_ctx* c, const hfx_solve_opts& o, TraceSolveRes
     B.histHead = (B.histHead + 1) % B.histCap;
     B.histCount = std::min(B.histCount + 1, B.histCap);
   }
-  RecoverParams rp{c->nCells, c->re.nFaces, B.NLF, B.NU, B.NQ, B.NL, c->d_cell2face, B.permx,
-                   B.U, B.Q, B.U0, B.Q0, B.trace, B.sol, B.flux};
+  BurgersRecoverParams rp{c->nCells, c->d_cell2face, B.permx, B.U, B.U0, B.cache, B.trace, B.sol, B.flux};
   c->timer.begin(K_RECOVER, c->stream);
-  HFX_CUDA(c, launch_recover(rp, c->stream));
+  HFX_CUDA(c, launch_burgers_recover(c->dim, c->order, rp, c->stream));
   c->timer.end(K_RECOVER, c->stream);
   return HFX_OK;
 }
@@ -2391,6 +2388,8 @@ int hfx_burgers_get_condensed(hfx_ctx* c, double* S, double* S0, double* U, doub
   auto cp = [&](double* h, const double* d, size_t n) {
     return h ? cudaMemcpyAsync(h, d, sizeof(double) * n, cudaMemcpyDeviceToHost, s) : cudaSuccess;
   };
+  if (Q || Q0)  // the element kernel does not store Q: form it from U, U0 and the cache
+    HFX_CUDA(c, launch_burgers_q(c->dim, c->order, (int64_t)E, B.U, B.U0, B.cache, B.Q, B.Q0, s));
   HFX_CUDA(c, cp(S, B.S, E * B.NL * B.NL));
   HFX_CUDA(c, cp(S0, B.S0, E * B.NL));
   HFX_CUDA(c, cp(U, B.U, E * B.NU * B.NL));

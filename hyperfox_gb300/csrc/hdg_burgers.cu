@@ -82,16 +82,17 @@ struct BL {
   static constexpr int CUU = CLL + F * NLF * NLF;   // NU*NU convection volume block
   static constexpr int KM = CUU + NU * NU;          // N*N     sum_k K'_k M^-1 C_k
   static constexpr int KE = KM + N * N;             // N*F*NF  sum_k K'_k M^-1 E_k
-  static constexpr int AUG = KE + N * F * NF;       // NU*W row-major (first holds X, NU*NU)
-  static constexpr int QS = AUG + NU * W;           // NQ*(NL+1) row-major [Q | Q0]
-  // the per-IP arrays live in the Q region: all of them are dead before Q is formed
+  static constexpr int HMC = KE + N * F * NF;       // F*NF*N    sum_{b,k} H_fk[a][b] (M^-1 C_k)[fn(b)][j]
+  static constexpr int HME = HMC + F * NF * N;      // F*NF*F*NF sum_{b,k} H_fk[a][b] (M^-1 E_k)[fn(b)][g]
+  static constexpr int AUG = HME + F * NF * F * NF; // NU*W row-major (first holds X, NU*NU)
+  static constexpr int QS = AUG + NU * W;           // per-IP arrays, then the right-hand-side parts
+  // the per-IP arrays are dead before the right-hand-side parts are written
   static constexpr int G = QS;                      // NI*N*D  J^-1 grad phi
   static constexpr int KG = G + NI * N * D;         // NI*N*D  Ds J^-1 grad phi
   static constexpr int DSQ = KG + NI * N * D;       // NI*D*D  Ds at the volume IPs
   static constexpr int AQ = DSQ + NI * D * D;       // NI*N    (div u phi_i + u.grad phi_i) dV
   static constexpr int BQ = AQ + NI * N;            // NI*ND*N u_c dV phi_i
-  static constexpr int QSZ = (BQ + NI * ND * N - QS) > NQ * (NL + 1) ? (BQ + NI * ND * N - QS) : NQ * (NL + 1);
-  static_assert(NU * 4 <= NQ * (NL + 1), "right-hand side parts exceed the Q region");
+  static constexpr int QSZ = (BQ + NI * ND * N - QS) > NU * 4 ? (BQ + NI * ND * N - QS) : NU * 4;
   static constexpr int FL = QS + QSZ;               // NL
   static constexpr int TOTAL = TAB + FL + NL + 2;   // + pivot scalars
   // per-element cache of the parts that do not depend on the linearisation state
@@ -103,7 +104,9 @@ struct BL {
   static constexpr int C_HF = C_TM + F * NT * NF * NF;
   static constexpr int C_KM = C_HF + F * D * NF * NF;
   static constexpr int C_KE = C_KM + N * N;
-  static constexpr int CL = C_KE + N * F * NF;
+  static constexpr int C_HMC = C_KE + N * F * NF;
+  static constexpr int C_HME = C_HMC + F * NF * N;
+  static constexpr int CL = C_HME + F * NF * F * NF;
   static_assert(TOTAL * 8 <= 227 * 1024, "element region exceeds the shared memory of one CTA");
 };
 
@@ -111,7 +114,7 @@ template <int D, int P>
 __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
   using L = BL<D, P>;
   constexpr int N = L::N, NF = L::NF, F = L::F, NI = L::NI, NIF = L::NIF, DM = L::DM;
-  constexpr int ND = L::ND, NT = L::NT, NU = L::NU, NQ = L::NQ, NLF = L::NLF, NL = L::NL, W = L::W;
+  constexpr int ND = L::ND, NT = L::NT, NU = L::NU, NLF = L::NLF, NL = L::NL, W = L::W;
   static_assert(D == 2, "the Burgers element kernel is built for 2D cells");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* smem = reinterpret_cast<double*>(smem_raw);
@@ -172,10 +175,11 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
   double* Cuu = R + L::CUU;
   double* KMs = R + L::KM;
   double* KEs = R + L::KE;
+  double* HMCs = R + L::HMC;
+  double* HMEs = R + L::HME;
   double* Aug = R + L::AUG;
   double* Xc = R + L::AUG;  // X[(i,c),(j,m)] = sum_q u_qc dV_q phi_qi G_qjm, before the Schur system
-  double* rhsPart = R + L::QS;  // NU*4 parts of the right-hand side column, before Q
-  double* Qs = R + L::QS;
+  double* rhsPart = R + L::QS;  // NU*4 parts of the right-hand side column (after the per-IP arrays die)
   double* Fl = R + L::FL;
   double* pivInv = R + L::FL + NL;
   const bool diff = p.kc != 0;
@@ -222,6 +226,8 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
       for (int i = tid; i < F * D * NF * NF; i += kBT) Hf[i] = ce[L::C_HF + i];
       for (int i = tid; i < N * N; i += kBT) KMs[i] = ce[L::C_KM + i];
       for (int i = tid; i < N * F * NF; i += kBT) KEs[i] = ce[L::C_KE + i];
+      for (int i = tid; i < F * NF * N; i += kBT) HMCs[i] = ce[L::C_HMC + i];
+      for (int i = tid; i < F * NF * F * NF; i += kBT) HMEs[i] = ce[L::C_HME + i];
     }
     __syncthreads();
     // ---------------------------------------------------------- geometry
@@ -469,10 +475,27 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
       }
       __syncthreads();
       if (diff) {
-        // the Schur products sum_k K'_k M^-1 C_k and sum_k K'_k M^-1 E_k (shared by every (c, m))
-        for (int x = tid; x < N * N + N * F * NF; x += kBT) {
+        // the Schur products sum_k K'_k M^-1 C_k and sum_k K'_k M^-1 E_k (shared by every
+        // (c, m)), and the face products H M^-1 C, H M^-1 E that give S its Slq Q term
+        constexpr int nKM = N * N, nKE = N * F * NF, nHC = F * NF * N, nHE = F * NF * F * NF;
+        for (int x = tid; x < nKM + nKE + nHC + nHE; x += kBT) {
           double acc = 0.0;
-          if (x < N * N) {
+          if (x >= nKM + nKE) {
+            const int y = x - nKM - nKE;
+            const bool hc = y < nHC;
+            const int fa = hc ? y / N : (y - nHC) / (F * NF);
+            const int col = hc ? y % N : (y - nHC) % (F * NF);
+            const int f = fa / NF, a = fa % NF;
+            for (int b = 0; b < NF; ++b) {
+              const int jn = sFaceNodes[f * NF + b];
+              for (int k = 0; k < D; ++k) {
+                const double h = Hf[((f * D + k) * NF + a) * NF + b];
+                acc += h * (hc ? MC[k * N * N + jn * N + col] : ME[(k * N + jn) * F * NF + col]);
+              }
+            }
+            if (hc) HMCs[y] = acc;
+            else HMEs[y - nHC] = acc;
+          } else if (x < N * N) {
             const int i = x / N, j = x % N;
             for (int k = 0; k < D; ++k)
               for (int l = 0; l < N; ++l) acc += KP[k * N * N + i * N + l] * MC[k * N * N + l * N + j];
@@ -495,6 +518,8 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
         for (int i = tid; i < F * D * NF * NF; i += kBT) ce[L::C_HF + i] = Hf[i];
         for (int i = tid; i < N * N; i += kBT) ce[L::C_KM + i] = diff ? KMs[i] : 0.0;
         for (int i = tid; i < N * F * NF; i += kBT) ce[L::C_KE + i] = diff ? KEs[i] : 0.0;
+        for (int i = tid; i < F * NF * N; i += kBT) ce[L::C_HMC + i] = diff ? HMCs[i] : 0.0;
+        for (int i = tid; i < F * NF * F * NF; i += kBT) ce[L::C_HME + i] = diff ? HMEs[i] : 0.0;
       }
     }
     // ------------------------------------- augmented Schur system [A | -B | Fu]
@@ -624,20 +649,6 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
       if (cl < NL) p.U[e * NU * NL + (int64_t)cl * NU + r] = v;
       else p.U0[e * NU + r] = v;
     }
-    for (int x = tid; x < NQ * (NL + 1); x += kBT) {
-      const int rq = x % NQ, cl = x / NQ;
-      const int l = rq / (D * ND), k = (rq / ND) % D, c = rq % ND;
-      double acc = 0.0;
-      for (int j = 0; j < N; ++j) acc -= MC[k * N * N + l * N + j] * Aug[(j * ND + c) * W + NU + cl];
-      if (cl < NL) {
-        const int f = cl / NLF, b = (cl % NLF) / ND, m = cl % ND;
-        if (m == c) acc += ME[(k * N + l) * F * NF + f * NF + b];
-        p.Q[e * NQ * NL + (int64_t)cl * NQ + rq] = acc;
-      } else {
-        p.Q0[e * NQ + rq] = acc;
-      }
-      Qs[rq * (NL + 1) + cl] = acc;
-    }
     __syncthreads();
     // ------------------------------------------- S, S0 (+ Dirichlet Set)
     for (int x = tid; x < NL * (NL + 1); x += kBT) {
@@ -653,9 +664,11 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
           const int jn = sFaceNodes[f * NF + b];
           for (int m = 0; m < ND; ++m)
             acc += Tm[(((f * ND + c) * ND + m) * NF + a) * NF + b] * Aug[(jn * ND + m) * W + NU + cl];
-          if (diff)
-            for (int k = 0; k < D; ++k)
-              acc -= Hf[((f * D + k) * NF + a) * NF + b] * Qs[((jn * D + k) * ND + c) * (NL + 1) + cl];
+        }
+        if (diff) {
+          // Slq Q with Q = -(M^-1 C (x) I) U + (M^-1 E (x) I): H M^-1 C U - H M^-1 E
+          for (int j = 0; j < N; ++j) acc += HMCs[(f * NF + a) * N + j] * Aug[(j * ND + c) * W + NU + cl];
+          if (cl < NL && cl % ND == c) acc -= HMEs[(f * NF + a) * F * NF + (cl / NLF) * NF + (cl % NLF) / ND];
         }
         if (cl < NL) {
           const int f2 = cl / NLF, b = (cl % NLF) / ND, m = cl % ND;
@@ -670,6 +683,69 @@ __global__ void __launch_bounds__(kBT) burgers_local(BurgersParams p) {
       else p.S0[e * NL + row] = v;
     }
     __syncthreads();
+  }
+}
+
+// Local recovery (HDGSolver.cpp:741-775), one CTA per element: Solution = U lambda + U0,
+// and Flux = Q lambda + Q0 with Q = -(M^-1 C (x) I) U + (M^-1 E (x) I), Q0 = -(M^-1 C (x) I) U0,
+// i.e. Flux = -(M^-1 C (x) I) Solution + (M^-1 E (x) I) lambda from the per-element cache.
+template <int D, int P>
+__global__ void __launch_bounds__(128) burgers_recover(BurgersRecoverParams p) {
+  using L = BL<D, P>;
+  constexpr int N = L::N, NF = L::NF, F = L::F, ND = L::ND, NU = L::NU, NQ = L::NQ, NLF = L::NLF, NL = L::NL;
+  __shared__ double lam[NL], sol[NU];
+  for (int64_t e = blockIdx.x; e < p.nCells; e += gridDim.x) {
+    for (int j = threadIdx.x; j < NL; j += blockDim.x) {
+      const int i = j / NLF;
+      const int f = p.cell2face[e * F + i];
+      lam[j] = p.trace[(int64_t)f * NLF + p.permx[(e * F + i) * NLF + (j % NLF)]];
+    }
+    __syncthreads();
+    const double* U = p.U + e * NU * NL;
+    for (int r = threadIdx.x; r < NU; r += blockDim.x) {
+      double acc = p.U0[e * NU + r];
+      for (int c2 = 0; c2 < NL; ++c2) acc += U[r + (int64_t)c2 * NU] * lam[c2];
+      sol[r] = acc;
+      p.sol[e * NU + r] = acc;
+    }
+    __syncthreads();
+    const double* ce = p.cache + e * L::CL;
+    for (int rq = threadIdx.x; rq < NQ; rq += blockDim.x) {
+      const int l = rq / (D * ND), k = (rq / ND) % D, c = rq % ND;
+      double acc = 0.0;
+      for (int j = 0; j < N; ++j) acc -= ce[L::C_MC + k * N * N + l * N + j] * sol[j * ND + c];
+      for (int g = 0; g < F * NF; ++g) acc += ce[L::C_ME + (k * N + l) * F * NF + g] * lam[g * ND + c];
+      p.flux[e * NQ + rq] = acc;
+    }
+    __syncthreads();
+  }
+}
+
+// Q and Q0 of every element from U, U0 and the cache, for the export of the condensed blocks:
+// Q = -(M^-1 C (x) I) U + (M^-1 E (x) I), Q0 = -(M^-1 C (x) I) U0 (column-major per element).
+template <int D, int P>
+__global__ void burgers_q_from_u(int64_t nCells, const double* __restrict__ U, const double* __restrict__ U0,
+                                 const double* __restrict__ cache, double* __restrict__ Q, double* __restrict__ Q0) {
+  using L = BL<D, P>;
+  constexpr int N = L::N, NF = L::NF, F = L::F, ND = L::ND, NU = L::NU, NQ = L::NQ, NLF = L::NLF, NL = L::NL;
+  const int64_t total = nCells * NQ * (NL + 1);
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = idx / (NQ * (NL + 1));
+    const int r = (int)(idx % (NQ * (NL + 1)));
+    const int rq = r % NQ, cl = r / NQ;
+    const int l = rq / (D * ND), k = (rq / ND) % D, c = rq % ND;
+    const double* ce = cache + e * L::CL;
+    double acc = 0.0;
+    for (int j = 0; j < N; ++j)
+      acc -= ce[L::C_MC + k * N * N + l * N + j] *
+             (cl < NL ? U[e * NU * NL + (int64_t)cl * NU + j * ND + c] : U0[e * NU + j * ND + c]);
+    if (cl < NL) {
+      const int f = cl / NLF, b = (cl % NLF) / ND, m = cl % ND;
+      if (m == c) acc += ce[L::C_ME + (k * N + l) * F * NF + f * NF + b];
+      Q[e * NQ * NL + (int64_t)cl * NQ + rq] = acc;
+    } else {
+      Q0[e * NQ + rq] = acc;
+    }
   }
 }
 
@@ -785,6 +861,32 @@ cudaError_t launch_burgers_local(int dim, int order, const BurgersParams& p, cud
       case 3: return launch_t<2, 3>(p, s);
       case 4: return launch_t<2, 4>(p, s);
       case 5: return launch_t<2, 5>(p, s);
+    }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_burgers_recover(int dim, int order, const BurgersRecoverParams& p, cudaStream_t s) {
+  const int64_t g = p.nCells < 152 * 64 ? p.nCells : 152 * 64;
+  const unsigned grid = (unsigned)(g < 1 ? 1 : g);
+  if (dim == 2) switch (order) {
+      case 1: burgers_recover<2, 1><<<grid, 128, 0, s>>>(p); return cudaGetLastError();
+      case 2: burgers_recover<2, 2><<<grid, 128, 0, s>>>(p); return cudaGetLastError();
+      case 3: burgers_recover<2, 3><<<grid, 128, 0, s>>>(p); return cudaGetLastError();
+      case 4: burgers_recover<2, 4><<<grid, 128, 0, s>>>(p); return cudaGetLastError();
+      case 5: burgers_recover<2, 5><<<grid, 128, 0, s>>>(p); return cudaGetLastError();
+    }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_burgers_q(int dim, int order, int64_t nCells, const double* U, const double* U0,
+                             const double* cache, double* Q, double* Q0, cudaStream_t s) {
+  const unsigned grid = 152 * 16;
+  if (dim == 2) switch (order) {
+      case 1: burgers_q_from_u<2, 1><<<grid, 256, 0, s>>>(nCells, U, U0, cache, Q, Q0); return cudaGetLastError();
+      case 2: burgers_q_from_u<2, 2><<<grid, 256, 0, s>>>(nCells, U, U0, cache, Q, Q0); return cudaGetLastError();
+      case 3: burgers_q_from_u<2, 3><<<grid, 256, 0, s>>>(nCells, U, U0, cache, Q, Q0); return cudaGetLastError();
+      case 4: burgers_q_from_u<2, 4><<<grid, 256, 0, s>>>(nCells, U, U0, cache, Q, Q0); return cudaGetLastError();
+      case 5: burgers_q_from_u<2, 5><<<grid, 256, 0, s>>>(nCells, U, U0, cache, Q, Q0); return cudaGetLastError();
     }
   return cudaErrorInvalidValue;
 }

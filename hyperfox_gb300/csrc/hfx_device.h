@@ -96,7 +96,7 @@ struct BurgersParams {
   const double* trace;         // Trace [nFaces][NF*ND]
   const double* tab;           // phi, dphi, w, fphi, fdphi, fw
   const int* itab;             // faceNodes[F*NF], faceOpposite[F]
-  double *S, *S0, *U, *Q, *U0, *Q0;
+  double *S, *S0, *U, *U0;     // Q, Q0 are not stored: launch_burgers_q forms them on demand
   int* status;                 // 1 = singular Schur block
   // per-element cache of the state-independent blocks ([nCells][burgers_cache_doubles]):
   // cacheMode 0 compute only, 1 compute and store, 2 load (geometry, tau, diffusion unchanged)
@@ -107,6 +107,21 @@ bool burgers_supported(int dim, int order);
 size_t burgers_cache_doubles(int dim, int order);
 size_t burgers_smem_bytes(int dim, int order);
 cudaError_t launch_burgers_local(int dim, int order, const BurgersParams& p, cudaStream_t s);
+// Solution = U lambda + U0 and Flux from the cache (M^-1 C, M^-1 E) of the last assembly
+struct BurgersRecoverParams {
+  int64_t nCells;
+  const int* cell2face;        // [nCells][F]
+  const uint8_t* permx;        // [nCells][F][NF*ND]
+  const double *U, *U0;        // element blocks of the last assembly
+  const double* cache;         // [nCells][burgers_cache_doubles]
+  const double* trace;         // [nFaces][NF*ND]
+  double* sol;                 // [nCells][N*ND]
+  double* flux;                // [nCells][D*N*ND]
+};
+cudaError_t launch_burgers_recover(int dim, int order, const BurgersRecoverParams& p, cudaStream_t s);
+// Q [nCells][NQ*NL] and Q0 [nCells][NQ] (column-major) from U, U0 and the cache
+cudaError_t launch_burgers_q(int dim, int order, int64_t nCells, const double* U, const double* U0,
+                             const double* cache, double* Q, double* Q0, cudaStream_t s);
 // NonLinearWrapper pieces: out[0] = sum (sol - buf)^2, out[1] = sum buf^2 (deterministic
 // block order); then both fields <- (1 - damp) sol + damp buf
 size_t newton_partials_needed();
