@@ -199,3 +199,65 @@ def test_burgers_time_step_reduces_to_mass_solve_when_frozen():
     P.set_state(buf=u_old, trace=g.ravel() * 0 + 0.0)
     sol, _ = P.linearized_solve()
     assert np.abs(sol - u_old).max() < 1e-8
+
+
+@pytest.mark.parametrize("p,dt", [(1, 0.0), (2, 0.0), (3, 1e-2)])
+def test_zero_velocity_is_two_scalar_diffusion_problems(p, dt):
+    """With BufferSolution = 0 and Trace = 0 the HDGUNabU terms vanish, and with
+    tau = tau_s I the Burgers system is nd uncoupled copies of the scalar HDG
+    diffusion-source problem (HDGBase/HDGDiffusion with nd unknowns, Euler with M (x) I):
+    every block equals the scalar oracle's, component by component (data of component 1
+    = 2 x component 0's)."""
+    rng = np.random.default_rng(p)
+    re = O.RefEl(2, p)
+    v, s = meshgen.square_simplices(3)
+    v = meshgen.jitter_vertices(v, 3, 0.15, p)
+    coords, cells = meshgen.high_order(v, s, re.nodes)
+    P1 = O.Problem(2, p, coords, cells)
+    PB = O.BurgersProblem(2, p, coords, cells)
+    Nf, N, nI = re.nNodesFace, re.nNodes, re.nIP
+    tau = rng.uniform(0.5, 2.0, size=(P1.nFaces, Nf))
+    kap = rng.uniform(0.2, 1.0, size=(P1.nCells, N, 1))
+    f = rng.normal(size=(P1.nCells, nI))
+    g = rng.normal(size=(P1.nFaces, Nf))
+    u_old = rng.normal(size=(P1.nCells, N))
+    P1.set_fields(tau.ravel(), kappa=kap.ravel(), src_mode=1, src=f, dirichlet=g.ravel(), dt=dt,
+                  u_old=u_old if dt > 0 else None)
+    tauB = np.zeros((P1.nFaces, Nf, 1, 4))
+    tauB[..., 0, 0] = tauB[..., 0, 3] = tau
+    fB = np.stack([f, 2 * f], -1)
+    gB = np.stack([g, 2 * g], -1)
+    oldB = np.stack([u_old, 2 * u_old], -1).reshape(P1.nCells, -1)
+    PB.set_fields(tau=tauB, tau_sides=1, nu=kap, src=fB, dirichlet=gB, dt=dt, old=oldB if dt > 0 else None)
+    PB.set_state(np.zeros((P1.nCells, PB.lenU)), np.zeros(PB.ndofs))
+    P1.assemble()
+    PB.assemble()
+    a, b = P1.condensed(), PB.condensed()
+    E, F = P1.nCells, re.nFaces
+    LL, LU, LQ = F * Nf, N, 2 * N
+    S1 = a["S"].reshape(E, LL, LL).transpose(0, 2, 1)              # [e][row][col]
+    SB = b["S"].reshape(E, 2 * LL, 2 * LL).transpose(0, 2, 1)      # [e][row][col]
+    scale = np.abs(S1).max()
+    for c in range(2):
+        for c2 in range(2):
+            blk = SB[:, c::2, c2::2]
+            ref = S1 if c == c2 else np.zeros_like(S1)
+            assert np.abs(blk - ref).max() < 1e-12 * scale, (c, c2)
+    # right-hand sides: component c carries (1 + c) x the scalar data (the Dirichlet rows too)
+    S01, S0B = a["S0"], b["S0"].reshape(E, LL, 2)
+    for c in range(2):
+        assert np.abs(S0B[..., c] - (1 + c) * S01).max() < 1e-12 * np.abs(S01).max()
+    # U, U0: rows (i, c), columns (f, a, c')
+    U1 = a["U"].reshape(E, LL, LU).transpose(0, 2, 1)
+    UB = b["U"].reshape(E, 2 * LL, 2 * LU).transpose(0, 2, 1)
+    for c in range(2):
+        assert np.abs(UB[:, c::2, c::2] - U1).max() < 1e-12 * np.abs(U1).max()
+        assert np.abs(UB[:, c::2, (1 - c)::2]).max() < 1e-12 * np.abs(U1).max()
+    U01, U0B = a["U0"], b["U0"].reshape(E, LU, 2)
+    for c in range(2):
+        assert np.abs(U0B[..., c] - (1 + c) * U01).max() < 1e-12 * np.abs(U01).max()
+    # Q: scalar rows (i, k), Burgers rows ((i, k), c)
+    Q1 = a["Q"].reshape(E, LL, LQ).transpose(0, 2, 1)
+    QB = b["Q"].reshape(E, 2 * LL, 2 * LQ).transpose(0, 2, 1)
+    for c in range(2):
+        assert np.abs(QB[:, c::2, c::2] - Q1).max() < 1e-12 * np.abs(Q1).max()
