@@ -57,6 +57,16 @@ CONFIGS = {
                       "(I + 99 a a^T), g Gaussian random field (sigma 1.5, corr 0.05) per cell, seeded axis a"),
     "cfg5-small": dict(dim=3, n=20, order=2, aniso=dict(sigma=1.5, corr=0.05, ratio=100.0, seed=5), cpu_n=8,
                        desc="3D anisotropic diffusion, 20^3x6 tets (48k), p=2, the cfg5 coefficient field"),
+    # independent problems of uneven size and order, one order per problem (a Mesh has one
+    # ReferenceElement), each order's problems solved as one disjoint-union mesh
+    "cfg3": dict(dim=2, batch=dict(count=1024, seed=3, min_elements=200, max_elements=20000), cpu_budget=12000,
+                 desc="1024 independent 2D HDG diffusion-source problems: unit-square meshes of 2n^2 triangles, "
+                      "n = round(sqrt(c/2)), c log-uniform in [200, 20000]; interior vertices jittered "
+                      "U(+-0.2h); p uniform in 1..5 per problem; kappa = exp(g) at the nodes, g Gaussian "
+                      "random field (sigma 1, corr 0.1); tau = 1; f = 2 pi^2 sin(pi x) sin(pi y), "
+                      "Dirichlet u = sin(pi x) sin(pi y)"),
+    "cfg3-small": dict(dim=2, batch=dict(count=64, seed=3, min_elements=200, max_elements=20000), cpu_budget=1500,
+                       desc="64 independent 2D HDG diffusion-source problems, the cfg3 distribution"),
     # viscous Burgers (HDGBurgersModel + HDGUNabU, nd = 2), implicit Euler, Newton every step
     "cfg4": dict(dim=2, n=180, order=3, burgers=True, nu=1e-2, dt=1e-3, time_steps=200,
                  desc="2D viscous Burgers HDG, unit square 180x180x2 tris (64,800), p=3, nu=1e-2, "
@@ -591,6 +601,181 @@ def run_burgers(args, world, rank, local):
     return res, ctx
 
 
+def run_batch(args, world, rank, local):
+    """configs with batch=...: the uneven batch through hyperfox_gb300.batch, one context per
+    order; a step = every group's assembly, Krylov solve (CG, every problem's own relative
+    residual <= rtol) and recovery, groups one after another."""
+    import torch
+    from hyperfox_gb300 import batch as hb, capi
+    torch.cuda.set_device(local)
+    cfg = CONFIGS[args.config]
+    t0 = time.time()
+    probs = hb.uneven_batch(**cfg["batch"])
+    B = hb.Batch(probs, local, capi.SRC_SINPROD, 2 * np.pi ** 2)
+    t_setup = time.time() - t0
+    L = capi.load()
+    # kappa constant per cell: symmetric trace systems, CG; precision and preconditioner as
+    # for the single-problem workloads (the coarse solve Chebyshev: no per-group training)
+    prec = capi.PREC_FP64 if args.precision == "fp64" else capi.PREC_MIXED
+    pc = capi.PC_TWOLEVEL if args.precond == "twolevel" else capi.PC_BLOCK_JACOBI
+    opts = dict(precision=prec, precond=pc, maxits=200000, inner_rtol=args.inner_rtol, coarse_rtol=args.coarse_rtol,
+                coarse_mode=capi.COARSE_CHEBYSHEV)
+    pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    bufs = B.host_buffers(alloc=pin)
+    for g in B.groups.values():  # pinned copies of the per-step inputs
+        g.tau, g.dirichlet = _pinned(pin, g.tau), _pinned(pin, g.dirichlet)
+        if g.kappa is not None:
+            g.kappa = _pinned(pin, g.kappa)
+    for _ in range(args.warmup):
+        B.run(args.rtol, **opts)
+    for g in B.groups.values():
+        g.ctx._chk(L.hfx_profile_enable(g.ctx.h, 1), "profile")
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    step_ms = []
+    for _ in range(args.steps):
+        step_ms.append(sum(B.run(args.rtol, **opts).values()))
+    clk = clocks.stop()
+    torch.cuda.synchronize()
+    dev_ms = barrier_max(world, sum(step_ms))
+    kt = {}
+    names = (("local", 0), ("scatter", 1), ("spmv64", 2), ("spmv32", 3), ("update", 4), ("recover", 5),
+             ("other", 6), ("residual", 7), ("coarse", 8))
+    # algorithmic bytes of the trace SpMV launches that did work (one per Krylov iteration;
+    # launches queued after convergence return at entry), summed over the groups
+    spmv_alg = {"spmv64": 0.0, "spmv32": 0.0}
+    spmv_n = {"spmv64": 0, "spmv32": 0}
+    for q, g in B.groups.items():
+        c = g.ctx
+        its = B.infos[q].iterations
+        for name, kid in names:
+            n_l, t_l = capi.ctypes.c_int(), capi.ctypes.c_double()
+            L.hfx_kernel_time(c.h, kid, capi.ctypes.byref(n_l), capi.ctypes.byref(t_l))
+            a = kt.setdefault(name, [0, 0.0])
+            a[0] += n_l.value
+            a[1] += t_l.value
+            if name in spmv_alg and n_l.value:
+                Nf = g.nf
+                nblocks = c.nnz // (Nf * Nf)
+                if name == "spmv32":  # upper block triangle in fixed-width rows of (column, location) slots
+                    alg = ((nblocks - c.nFaces) // 2 + c.nFaces) * Nf * Nf * 4 + c.nFaces * 5 * 8 + 4 * c.ndofs * 4
+                else:  # values, block columns, row pointers once; z, p_old gathered, p_new, q written
+                    alg = c.nnz * 8 + nblocks * 4 + (c.nFaces + 1) * 8 + 4 * c.ndofs * 8
+                launches = min(n_l.value, its * args.steps) if its else n_l.value
+                spmv_alg[name] += launches * alg
+                spmv_n[name] += launches
+        c._chk(L.hfx_profile_enable(c.h, 0), "profile")
+    infos = {q: dict(iterations=i.iterations, rel_residual=i.rel_residual) for q, i in B.infos.items()}
+    # e2e: field uploads from pinned host buffers, downloads of Trace, Solution, Flux
+    barrier(world)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(args.steps):
+        B.step(args.rtol, bufs, **opts)
+    torch.cuda.synchronize()
+    e2e_s = barrier_max(world, time.perf_counter() - t1)
+    h2d = sum(g.tau.nbytes + g.dirichlet.nbytes + (g.kappa.nbytes if g.kappa is not None else 0)
+              for g in B.groups.values())
+    d2h = sum(a.nbytes for b in bufs.values() for a in b)
+    # accuracy: every problem's trace against an FP64 solve of its group to 1e-12 of the
+    # group's right-hand side (untimed)
+    tr = [t.copy() for t, _, _ in B.results()]
+    worst = None
+    try:
+        B.solve(group_rtol=1e-12, **dict(opts, precision=capi.PREC_FP64))
+        worst = max(float(np.linalg.norm(a - b[0]) / max(np.linalg.norm(b[0]), 1e-300))
+                    for a, b in zip(tr, B.results()))
+    except capi.HfxError as e:  # reported, not required
+        worst = "reference solve: %s" % e
+    E = B.nCells
+    step_s = dev_ms / 1e3 / args.steps
+    hbm, peak_kind = peaks()
+    key = max(("spmv32", "spmv64"), key=lambda k: kt[k][1])
+    roof = None
+    if spmv_n[key]:
+        ach = spmv_alg[key] / (kt[key][1] / 1e3) / 1e9
+        roof = dict(bound="hbm", kernel=("cg_spmv_half_ell<float>" if key == "spmv32" else "cg_spmv<double>")
+                    + " (all order groups)", achieved=round(ach, 1), peak=hbm, unit="GB/s",
+                    frac=round(ach / hbm, 4), traffic=None, bytes_per_launch=int(spmv_alg[key] / spmv_n[key]),
+                    avg_launch_ms=round(kt[key][1] / spmv_n[key], 4),
+                    share_of_step=round(kt[key][1] / max(dev_ms, 1e-9), 3), peak_source=peak_kind)
+    from collections import Counter
+    per_order = Counter()
+    for p in probs:
+        per_order[p.order] += p.nCells
+    res = {
+        "metric": METRIC, "value": E / step_s, "unit": "elements/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64+f32" if prec else "f64",
+        "data": "synthetic (seeded meshes, fields and orders)",
+        "config": {"workload": cfg["desc"], "problems": len(probs), "elements": E,
+                   "elements_per_order": {str(k): v for k, v in sorted(per_order.items())},
+                   "trace_dofs": int(sum(g.ctx.ndofs for g in B.groups.values())),
+                   "precision": args.precision,
+                   "preconditioner": ("two-level: per-face block Jacobi + vertex coarse space (Chebyshev)"
+                                      if pc == capi.PC_TWOLEVEL else "block-Jacobi (per face)"),
+                   "krylov": "CG (symmetric trace systems)",
+                   "rtol": args.rtol, "rtol_per_problem": True,
+                   "group_tolerances": {str(q): g.tol for q, g in B.groups.items()},
+                   "l2_flush": "inputs > L2 (no flush needed)",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "timing": "CUDA events on every order group's stream around its work, groups in sequence"},
+        "time_to_solve_s": step_s,
+        "group_ms": {str(q): round(v, 3) for q, v in B.run(args.rtol, **opts).items()},
+        "krylov": {str(q): v for q, v in infos.items()},
+        "max_rel_err_vs_fp64": worst,
+        "kernel_ms": {k: dict(launches=v[0], total_ms=round(v[1], 3)) for k, v in kt.items()},
+        "roofline": roof, "clocks": clk,
+        "e2e": {"value": E * args.steps / e2e_s, "unit": "elements/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(sum(v[0] for v in kt.values())),
+        "setup_s": t_setup,
+    }
+    return res, B
+
+
+def _pinned(pin, a):
+    out = pin(a.shape)
+    np.copyto(out, a)
+    return out
+
+
+def batch_cpu_sample(cfg_name, nthreads, rtol):
+    """The oracle on a bounded sample of the batch: its problems in order until the
+    config's cpu_budget elements, each solved alone (as the reference runs one problem per Mesh) with
+    GMRES(30)+Jacobi to rtol; assemble + condense + scatter + solve + recover."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import _oracle as O
+    from hyperfox_gb300 import batch as hb
+    cfg = CONFIGS[cfg_name]
+    budget = cfg["cpu_budget"]
+    probs = hb.uneven_batch(**dict(cfg["batch"], count=min(cfg["batch"]["count"], 64)))
+    take, tot = [], 0
+    for p in probs:
+        if tot + p.nCells > budget and take:
+            continue
+        take.append(p)
+        tot += p.nCells
+        if tot >= budget:
+            break
+    dt, its = 0.0, 0
+    for p in take:
+        P = O.Problem(2, p.order, p.coords, p.cells)
+        P.set_fields(p.tau.ravel(), kappa=p.kappa.ravel(), src_mode=2, dirichlet=p.dirichlet.ravel())
+        t0 = time.perf_counter()
+        P.assemble(nthreads)
+        x, it = P.solve_gmres(rtol, 200000, nthreads)
+        P.recover(x)
+        dt += time.perf_counter() - t0
+        its += abs(it)
+    return dict(value=tot / dt, unit="elements/s", cores=nthreads, kind="port",
+                sample="%d of the batch's problems (%d elements, orders %s), each alone: oracle assemble+condense"
+                       "+scatter, GMRES(30)+Jacobi to %g (%d its in all), recovery"
+                       % (len(take), tot, sorted({p.order for p in take}), rtol, its), seconds=dt)
+
+
 def burgers_cpu_sample(cfg_name, nthreads, n=64):
     """The oracle (HDGBurgersModel restatement, dense LU condensation, GMRES(30)+Jacobi)
     on a bounded sample: the second implicit Euler step of the same physics on an
@@ -701,6 +886,37 @@ def main():
         args.steps = 5
     world, rank, local = dist_init()
     burgers = CONFIGS[args.config].get("burgers", False)
+    is_batch = "batch" in CONFIGS[args.config]
+    if is_batch and not args.steps_given:
+        args.steps = 3
+    if is_batch and args.impl == "reference":
+        if rank != 0:
+            return
+        nthreads = os.cpu_count() or 1
+        vals = []
+        for i in range(args.warmup + args.steps):
+            r = batch_cpu_sample(args.config, nthreads, args.rtol)
+            if i >= args.warmup:
+                vals.append(r["value"])
+        v = statistics.median(vals)
+        out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "elements/s", "n_gpus": world,
+               "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+               "config": {"workload": CONFIGS[args.config]["desc"]}, "cpu_baseline": dict(r, value=v),
+               "e2e": {"value": v, "unit": "elements/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(out))
+        return
+    if is_batch:
+        res, B = run_batch(args, world, rank, local)
+        if rank == 0:
+            if not args.no_cpu:
+                try:
+                    res["cpu_baseline"] = batch_cpu_sample(args.config, os.cpu_count() or 1, args.rtol)
+                except Exception as e:  # the baseline is reported, not required
+                    res["cpu_baseline"] = {"error": str(e)}
+            print(json.dumps(res))
+        B.close()
+        return
     if args.impl == "reference" and burgers:
         if rank != 0:
             return

@@ -29,13 +29,11 @@ def _square_vertices(n):
 def square_simplices(n):
     """Vertices and linear triangles of the unit square split into 2*n*n triangles."""
     verts, vid = _square_vertices(n)
-    tris = []
-    for i in range(n):
-        for j in range(n):
-            v00, v10, v01, v11 = vid(i, j), vid(i + 1, j), vid(i, j + 1), vid(i + 1, j + 1)
-            tris.append((v00, v10, v01))
-            tris.append((v11, v01, v10))
-    return verts, np.asarray(tris, dtype=np.int64)
+    # square (i, j) in row-major order, its two triangles (v00, v10, v01) and (v11, v01, v10)
+    i, j = (a.ravel() for a in np.meshgrid(np.arange(n), np.arange(n), indexing="ij"))
+    v00, v10, v01, v11 = vid(i, j), vid(i + 1, j), vid(i, j + 1), vid(i + 1, j + 1)
+    tris = np.stack([np.stack([v00, v10, v01], -1), np.stack([v11, v01, v10], -1)], 1).reshape(-1, 3)
+    return verts, tris.astype(np.int64)
 
 
 def cube_simplices(n):

@@ -85,3 +85,17 @@ def test_anisotropic_lognormal_field():
     assert np.allclose(ev[:, 2] / ev[:, 0], 100.0)
     g = np.log(ev[:, 0])
     assert abs(g.std() - 1.5) < 0.15 and abs(g.mean()) < 0.3
+
+
+def test_batch_reference_arm_prints_its_metric():
+    """The uneven batch's reference arm (the oracle, every sampled problem solved alone)
+    prints one line in the GPU arm's unit."""
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1", "--warmup", "0",
+           "--config", "cfg3-small"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["unit"] == "elements/s" and d["value"] > 0
+    assert d["cpu_baseline"]["kind"] == "port" and "each alone" in d["cpu_baseline"]["sample"]

@@ -1,0 +1,79 @@
+"""Batched independent problems of orders 1-5 on the GPU vs the oracle, problem by problem.
+
+Bars: every problem's trace within 1e-8 relative L2 of its own direct FP64 solve on
+the oracle; Solution and Flux within 1e-12 (max-norm, relative) of the oracle's
+recovery of the same trace; at the group tolerance of rtol = 1e-6 every problem's own
+relative residual (the oracle's CSR) at most 1e-6; the host-buffer step returns what
+the device holds.
+"""
+import numpy as np
+import pytest
+
+import _oracle as O
+from hyperfox_gb300 import batch, capi
+
+pytestmark = pytest.mark.gpu
+
+SRC = 2 * np.pi ** 2
+
+
+def oracle_problem(p):
+    P = O.Problem(p.dim, p.order, p.coords, p.cells)
+    P.set_fields(p.tau.ravel(), kappa=p.kappa.ravel(), src_mode=2, dirichlet=p.dirichlet.ravel())
+    P.assemble()
+    return P
+
+
+def make(count, seed, kappa_at="cells"):
+    probs = batch.uneven_batch(count=count, seed=seed, min_elements=8, max_elements=200, kappa_at=kappa_at)
+    return probs, batch.Batch(probs, 0, capi.SRC_SINPROD, SRC)
+
+
+@pytest.mark.parametrize("kappa_at,precond", [("cells", capi.PC_BLOCK_JACOBI), ("cells", capi.PC_TWOLEVEL),
+                                              ("nodes", capi.PC_BLOCK_JACOBI)])
+def test_batch_matches_oracle_per_problem(hfx_lib, kappa_at, precond):
+    """kappa per cell: CG (affine element kernel); kappa at the nodes: GMRES (quadrature kernel)."""
+    probs, B = make(10, 5, kappa_at)
+    assert len(B.groups) >= 4
+    B.assemble()
+    B.solve(rtol=1e-11, maxits=20000, precond=precond)
+    B.recover()
+    for p, (trace, sol, flux) in zip(probs, B.results()):
+        P = oracle_problem(p)
+        x = P.solve_direct()
+        assert np.linalg.norm(trace - x) <= 1e-8 * np.linalg.norm(x), p.order
+        s, q = P.recover(trace)
+        assert np.abs(sol - s).max() <= 1e-12 * np.abs(s).max(), p.order
+        assert np.abs(flux - q).max() <= 1e-12 * np.abs(q).max(), p.order
+    B.close()
+
+
+def test_group_tolerance_holds_per_problem(hfx_lib):
+    import scipy.sparse as sp
+    probs, B = make(12, 8)
+    B.assemble()
+    rtol = 1e-6
+    tols = B.group_tolerances(rtol)
+    assert all(0 < t <= rtol for t in tols.values())
+    B.solve(rtol=rtol, maxits=20000)
+    for p, (trace, _, _) in zip(probs, B.results()):
+        P = oracle_problem(p)
+        rowptr, col, val, rhs = P.csr()
+        A = sp.csr_matrix((val, col, rowptr), shape=(P.ndofs, P.ndofs))
+        assert np.linalg.norm(rhs - A @ trace) <= rtol * np.linalg.norm(rhs) * (1 + 1e-2), p.order
+    B.close()
+
+
+def test_batch_step_through_host_buffers(hfx_lib):
+    probs, B = make(6, 9)
+    bufs = B.host_buffers()
+    B.step(1e-11, bufs, maxits=20000)
+    res = B.results()
+    for (q, k), (trace, sol, flux) in zip(B.where, res):
+        g = B.groups[q]
+        c0, c1 = g.offsets[1][k], g.offsets[1][k + 1]
+        f0, f1 = g.offsets[2][k], g.offsets[2][k + 1]
+        assert np.array_equal(bufs[q][0][f0 * g.nf:f1 * g.nf], trace)
+        assert np.array_equal(bufs[q][1][c0:c1], sol)
+        assert np.array_equal(bufs[q][2][c0:c1], flux)
+    B.close()
