@@ -1,10 +1,14 @@
 """Batched independent problems of orders 1-5 on the GPU vs the oracle, problem by problem.
 
 Bars: every problem's trace within 1e-8 relative L2 of its own direct FP64 solve on
-the oracle; Solution and Flux within 1e-12 (max-norm, relative) of the oracle's
-recovery of the same trace; at the group tolerance of rtol = 1e-6 every problem's own
-relative residual (the oracle's CSR) at most 1e-6; the host-buffer step returns what
-the device holds.
+the oracle; Solution and Flux within the round-off bound of the element solves of the
+oracle's recovery of the same trace (max-norm, relative): 10 eps max_e cond(A_e), A_e
+the element's local U-Q block, and at least 1e-12. The lognormal coefficients (exp(g),
+sigma 1: a factor of up to ~300 inside a problem) at p = 5 reach cond(A_e) ~ 1e5, so
+the bound is above the 1e-12 of the unit-coefficient parity tests (3.5e-12 measured
+at p = 5, bound 2.8e-10). At the group tolerance of rtol = 1e-6 every problem's own
+relative residual (the oracle's CSR) is at most 1e-6; the host-buffer step returns
+what the device holds.
 """
 import numpy as np
 import pytest
@@ -22,6 +26,12 @@ def oracle_problem(p):
     P.set_fields(p.tau.ravel(), kappa=p.kappa.ravel(), src_mode=2, dirichlet=p.dirichlet.ravel())
     P.assemble()
     return P
+
+
+def roundoff_bound(P):
+    n = P.lenU + P.lenQ
+    cond = max(np.linalg.cond(P.local_matrix(e)[0][:n, :n]) for e in range(P.nCells))
+    return max(1e-12, 10 * np.finfo(np.float64).eps * cond)
 
 
 def make(count, seed, kappa_at="cells"):
@@ -43,8 +53,9 @@ def test_batch_matches_oracle_per_problem(hfx_lib, kappa_at, precond):
         x = P.solve_direct()
         assert np.linalg.norm(trace - x) <= 1e-8 * np.linalg.norm(x), p.order
         s, q = P.recover(trace)
-        assert np.abs(sol - s).max() <= 1e-12 * np.abs(s).max(), p.order
-        assert np.abs(flux - q).max() <= 1e-12 * np.abs(q).max(), p.order
+        bar = roundoff_bound(P)
+        assert np.abs(sol - s).max() <= bar * np.abs(s).max(), (p.order, bar)
+        assert np.abs(flux - q).max() <= bar * np.abs(q).max(), (p.order, bar)
     B.close()
 
 
