@@ -85,22 +85,37 @@ class _Group:
         self.problems = problems
         dim, order = problems[0].dim, problems[0].order
         coords, cells, topo, self.offsets = union(problems)
-        self.ctx = capi.Context(device)
-        self.ctx.upload_mesh(dim, order, coords, cells, topology=topo)
-        self.nf = self.ctx.re["nNodesFace"]
+        N = cells.shape[1]
+        self.nf = topo[2].shape[1]
+        # the fields of the union, checked before any device work
+        for p in problems:
+            if p.tau.size % (p.nFaces * self.nf) or p.dirichlet.size != p.nFaces * self.nf:
+                raise ValueError("batch: tau [nFaces][Nf][1|2] and dirichlet [nFaces][Nf] of every problem")
+        widths = {p.tau.size // (p.nFaces * self.nf) for p in problems}
+        if len(widths) != 1 or widths.pop() not in (1, 2):
+            raise ValueError("batch: within one order every problem's tau has 1, or every one 2, values per node")
         self.tau = np.ascontiguousarray(np.concatenate([p.tau.reshape(p.nFaces, self.nf, -1) for p in problems]))
         self.dirichlet = np.ascontiguousarray(np.concatenate([p.dirichlet.reshape(p.nFaces, self.nf)
                                                               for p in problems]))
         kaps = [p.kappa for p in problems]
         if any(k is None for k in kaps) and not all(k is None for k in kaps):
             raise ValueError("batch: within one order every problem gives kappa, or none does")
-        self.kappa = None if kaps[0] is None else np.ascontiguousarray(np.concatenate(
-            [k.reshape(p.nCells, p.cells.shape[1], -1) for k, p in zip(kaps, problems)]))
+        self.kappa = None
+        if kaps[0] is not None:
+            kcs = {k.size // (p.nCells * N) if k.size % (p.nCells * N) == 0 else -1 for k, p in zip(kaps, problems)}
+            if len(kcs) != 1 or kcs.pop() not in (1, dim * dim):
+                raise ValueError("batch: kappa [nCells][N][1 or dim*dim], the same width within one order")
+            self.kappa = np.ascontiguousarray(np.concatenate(
+                [k.reshape(p.nCells, N, -1) for k, p in zip(kaps, problems)]))
         self.src_mode, self.src_param = src_mode, src_param
         self.source = None
         if src_mode == capi.SRC_VALUES:
+            if any(p.source is None for p in problems):
+                raise ValueError("batch: source values [nCells][nIP] for every problem")
             self.source = np.ascontiguousarray(np.concatenate([p.source.reshape(p.nCells, -1) for p in problems]))
         self.tol = self.rtol = None
+        self.ctx = capi.Context(device)
+        self.ctx.upload_mesh(dim, order, coords, cells, topology=topo)
         self.upload()
 
     def upload(self):

@@ -128,5 +128,25 @@ def test_uneven_batch_workload():
 
 
 def test_batch_rejects_bad_input():
+    """Inconsistent inputs are refused before any device work (no GPU needed)."""
     with pytest.raises(ValueError):
         batch.Batch([])
+    a, b = small_batch(count=40, seed=6, orders=(2,))[:2]
+    b.tau = np.ones((b.nFaces, b.faces.shape[1], 2))  # double valued next to single valued
+    with pytest.raises(ValueError, match="tau"):
+        batch.Batch([a, b])
+    a, b = small_batch(count=40, seed=6, orders=(2,))[:2]
+    b.kappa = None
+    with pytest.raises(ValueError, match="kappa"):
+        batch.Batch([a, b])
+    a, b = small_batch(count=40, seed=6, orders=(2,))[:2]
+    b.kappa = np.ones((b.nCells, b.cells.shape[1], 3))
+    with pytest.raises(ValueError, match="kappa"):
+        batch.Batch([a, b])
+    a, b = small_batch(count=40, seed=6, orders=(2,))[:2]
+    with pytest.raises(ValueError, match="source"):
+        batch.Batch([a, b], src_mode=capi.SRC_VALUES)
+    c = small_batch(count=40, seed=6, orders=(3,))[0]
+    c.dim = 3
+    with pytest.raises(ValueError, match="dimension"):
+        batch.Batch([a, c])
