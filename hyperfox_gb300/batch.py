@@ -287,24 +287,51 @@ def _uneven_problem(args):
     return prob
 
 
-def uneven_batch(count=1024, seed=3, min_elements=200, max_elements=20000, orders=(1, 2, 3, 4, 5),
-                 jitter=0.2, sigma=1.0, corr=0.1, kappa_at="cells"):
-    """Seeded batch of 2D unit-square problems of uneven size and order.
-
-    Problem k: element count c drawn log-uniform in [min_elements, max_elements],
-    mesh n x n x 2 triangles with n = round(sqrt(c / 2)) (so 2 n^2 elements), interior
-    vertices jittered by U(-jitter h, jitter h), order uniform in ``orders``,
-    kappa = exp(g) with g a Gaussian random field (sigma, corr, its own seed) sampled at
-    the cell centroids (kappa_at "cells": constant inside every cell, so the trace system
-    is symmetric and CG with the two-level preconditioner applies) or at the cell nodes
-    ("nodes": GMRES), tau = 1, Dirichlet u = sin(pi x) sin(pi y) at the face nodes. The
-    source is the batch's (the workload uses f = 2 pi^2 sin(pi x) sin(pi y))."""
-    if kappa_at not in ("cells", "nodes"):
-        raise ValueError("uneven_batch: kappa_at is 'cells' or 'nodes'")
+def uneven_plan(count=1024, seed=3, min_elements=200, max_elements=20000, orders=(1, 2, 3, 4, 5)):
+    """The seeded draws of ``uneven_batch``: per problem (n, order, field seed), the mesh
+    n x n x 2 triangles with n = round(sqrt(c / 2)), c log-uniform in
+    [min_elements, max_elements], the order uniform in ``orders``."""
     rng = np.random.default_rng(seed)
     counts = np.exp(rng.uniform(np.log(min_elements), np.log(max_elements), size=count))
     ns = np.maximum(1, np.rint(np.sqrt(counts / 2.0))).astype(int)
     ps = rng.choice(np.asarray(orders), size=count)
     fseeds = rng.integers(0, 2 ** 31, size=count)
-    jobs = [(int(ns[k]), int(ps[k]), int(fseeds[k]), jitter, sigma, corr, kappa_at) for k in range(count)]
-    return [_uneven_problem(j) for j in jobs]
+    return [(int(ns[k]), int(ps[k]), int(fseeds[k])) for k in range(count)]
+
+
+def problem_cost(n, order):
+    """Work estimate of one 2D problem: elements x (trace values per element)^2."""
+    return 2 * n * n * (3 * (order + 1)) ** 2
+
+
+def shard(costs, world):
+    """Problem indices per rank, balanced by cost (longest-processing-time greedy: the
+    most expensive problem first, each to the least loaded rank; ties to the lower rank).
+    Deterministic, so every rank computes the same split without communication."""
+    order = sorted(range(len(costs)), key=lambda i: (-costs[i], i))
+    load = [0.0] * world
+    out = [[] for _ in range(world)]
+    for i in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        out[r].append(i)
+        load[r] += costs[i]
+    return [sorted(o) for o in out]
+
+
+def uneven_batch(count=1024, seed=3, min_elements=200, max_elements=20000, orders=(1, 2, 3, 4, 5),
+                 jitter=0.2, sigma=1.0, corr=0.1, kappa_at="cells", select=None):
+    """Seeded batch of 2D unit-square problems of uneven size and order.
+
+    Problem k (draws of ``uneven_plan``): mesh n x n x 2 triangles, interior vertices
+    jittered by U(-jitter h, jitter h), kappa = exp(g) with g a Gaussian random field
+    (sigma, corr, its own seed) sampled at the cell centroids (kappa_at "cells": constant
+    inside every cell, so the trace system is symmetric and CG with the two-level
+    preconditioner applies) or at the cell nodes ("nodes": GMRES), tau = 1, Dirichlet
+    u = sin(pi x) sin(pi y) at the face nodes. The source is the batch's (the workload uses
+    f = 2 pi^2 sin(pi x) sin(pi y)). select: the problem indices to build (default all),
+    e.g. one rank's ``shard``."""
+    if kappa_at not in ("cells", "nodes"):
+        raise ValueError("uneven_batch: kappa_at is 'cells' or 'nodes'")
+    plan = uneven_plan(count, seed, min_elements, max_elements, orders)
+    idx = range(count) if select is None else select
+    return [_uneven_problem(plan[k] + (jitter, sigma, corr, kappa_at)) for k in idx]

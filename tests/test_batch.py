@@ -150,3 +150,61 @@ def test_batch_rejects_bad_input():
     c.dim = 3
     with pytest.raises(ValueError, match="dimension"):
         batch.Batch([a, c])
+
+
+def test_shard_partitions_and_balances():
+    plan = batch.uneven_plan()
+    costs = [batch.problem_cost(n, q) for n, q, _ in plan]
+    for world in (1, 2, 4, 8):
+        parts = batch.shard(costs, world)
+        flat = sorted(i for part in parts for i in part)
+        assert flat == list(range(len(plan)))
+        loads = [sum(costs[i] for i in part) for part in parts]
+        # greedy LPT: no rank exceeds the mean by more than the largest single problem
+        assert max(loads) - sum(loads) / world <= max(costs)
+        assert batch.shard(costs, world) == parts
+
+
+def test_select_builds_the_same_problems():
+    full = batch.uneven_batch(count=12, seed=4, min_elements=8, max_elements=120)
+    some = batch.uneven_batch(count=12, seed=4, min_elements=8, max_elements=120, select=[3, 7, 11])
+    for k, p in zip([3, 7, 11], some):
+        assert p.order == full[k].order and np.array_equal(p.cells, full[k].cells)
+        assert np.array_equal(p.kappa, full[k].kappa) and np.array_equal(p.coords, full[k].coords)
+
+
+def _shard_worker(rank, world, port, q):
+    import os
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    import torch
+    import torch.distributed as dist
+    from hyperfox_gb300 import batch as hb
+    dist.init_process_group("gloo")
+    plan = hb.uneven_plan(count=64, seed=3)
+    mine = hb.shard([hb.problem_cost(n, p) for n, p, _ in plan], world)[rank]
+    probs = hb.uneven_batch(count=64, seed=3, select=mine[:2])  # each rank builds only its own problems
+    lens = [None] * world
+    dist.all_gather_object(lens, (rank, mine, [p.nCells for p in probs]))
+    q.put(lens)
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_split_the_batch_without_exchange():
+    """World size 2 on CPU: every rank computes the split alone; gathered afterwards, the
+    ranks' problem sets are disjoint and cover the batch."""
+    import multiprocessing as mp
+    import os
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = 29600 + os.getpid() % 1000
+    ps = [ctx.Process(target=_shard_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    outs = [q.get(timeout=180) for _ in ps]
+    for p in ps:
+        p.join(timeout=60)
+    assert outs[0] == outs[1]
+    (r0, s0, e0), (r1, s1, e1) = sorted(outs[0])
+    assert (r0, r1) == (0, 1) and not set(s0) & set(s1) and sorted(s0 + s1) == list(range(64))
+    plan = batch.uneven_plan(count=64, seed=3)
+    assert e0 == [2 * plan[i][0] ** 2 for i in s0[:2]] and e1 == [2 * plan[i][0] ** 2 for i in s1[:2]]
