@@ -15,6 +15,10 @@ Trace, Solution and Flux are inside the timed region.
 Inputs are far larger than L2 (element blocks ~15 GB, trace matrix ~4 GB), so
 no L2 flush is needed between steps.
 
+Other workloads (--config): cfg4 viscous Burgers with Newton every time step, cfg5
+anisotropic lognormal diffusion, cfg3 a batch of 1024 independent problems of orders
+1-5 (hyperfox_gb300.batch: one disjoint-union mesh per order).
+
 --impl reference times the CPU oracle (C++ restatement of HyperFox's path:
 per-element dense assembly + LU condensation, CSR scatter, GMRES(30)+Jacobi,
 recovery) on the host cores with all threads, on a bounded sample of the same
