@@ -6,6 +6,7 @@
 //                                       field map Solution/Flux/Trace/Tau/Dirichlet
 //   hfx::gpu::Mesh / Field / models   ~ the parts of Mesh, Field, HDGDiffusionSource,
 //                                       HDGLaplaceModel and DirichletModel the path reads
+//   hfx::gpu::MeshUnion               ~ many independent Meshes of one order as one
 //   hfx::gpu::GpuBurgersSolver        ~ HDGSolver with HDGBurgersModel (vector Burgers)
 //   hfx::gpu::NonLinearWrapper        ~ NonLinearWrapper (NonLinearWrapper.h:14-128)
 // Errors throw ErrorHandle(class, method, message) exactly where HyperFox
@@ -188,6 +189,55 @@ struct Mesh {
     hfx_mesh_compute_topology(dim, order, numCells(), cells.data(), &nF, &nB, cell2face.data(), face2cell.data(),
                               faces.data(), boundary.data());
     nFaces = nF;
+  }
+};
+
+// Independent problems of one order as ONE mesh (HyperFox runs one problem per Mesh,
+// and a Mesh has one ReferenceElement, Mesh.cpp:24-29). The nodes, cells and faces of
+// problem k follow those of problems 0..k-1. The union's own topology (computeFaces,
+// the MOAB creation-order rule) numbers the faces problem by problem, so problem k's
+// faces are [faceOffset[k], faceOffset[k+1]) in its own order. No face or vertex is
+// shared, so the trace system is block diagonal: one GpuHDGSolver on `mesh` serves every
+// problem. Its Krylov tolerance groupTolerance(rtol, rhs, valsPerFace) bounds every
+// problem's own relative residual by rtol: |r_k| <= |r| <= rtol min_j |b_j| <= rtol |b_k|,
+// over the problems whose part b_k of the right-hand side is non-zero.
+struct MeshUnion {
+  Mesh mesh;
+  std::vector<long long> nodeOffset{0}, cellOffset{0}, faceOffset{0};
+  explicit MeshUnion(const std::vector<const Mesh*>& parts) {
+    if (parts.empty()) throw ErrorHandle("MeshUnion", "MeshUnion", "no problems");
+    mesh.dim = parts[0]->dim;
+    mesh.order = parts[0]->order;
+    for (const Mesh* m : parts) {
+      if (m->dim != mesh.dim || m->order != mesh.order)
+        throw ErrorHandle("MeshUnion", "MeshUnion", "all problems of one union have one dimension and one order");
+      int nF = 0, nB = 0;
+      if (hfx_mesh_compute_topology(m->dim, m->order, m->numCells(), m->cells.data(), &nF, &nB, nullptr, nullptr,
+                                    nullptr, nullptr))
+        throw ErrorHandle("MeshUnion", "MeshUnion", "invalid mesh");
+      const long long shift = nodeOffset.back();
+      mesh.nodes.insert(mesh.nodes.end(), m->nodes.begin(), m->nodes.end());
+      for (int v : m->cells) mesh.cells.push_back((int)(v + shift));
+      nodeOffset.push_back(shift + m->numNodes());
+      cellOffset.push_back(cellOffset.back() + m->numCells());
+      faceOffset.push_back(faceOffset.back() + nF);
+      if (nodeOffset.back() >= (1LL << 31) || faceOffset.back() >= (1LL << 31))
+        throw ErrorHandle("MeshUnion", "MeshUnion", "more than 2^31 - 1 nodes or faces");
+    }
+    mesh.computeFaces();
+    if (mesh.nFaces != faceOffset.back())
+      throw ErrorHandle("MeshUnion", "MeshUnion", "the problems share faces");
+  }
+  int numProblems() const { return (int)cellOffset.size() - 1; }
+  double groupTolerance(double rtol, const std::vector<double>& rhs, int valsPerFace) const {
+    double total = 0.0, least = -1.0;
+    for (int k = 0; k < numProblems(); ++k) {
+      double sq = 0.0;
+      for (long long i = faceOffset[k] * valsPerFace; i < faceOffset[k + 1] * valsPerFace; ++i) sq += rhs[i] * rhs[i];
+      total += sq;
+      if (sq > 0.0 && (least < 0.0 || sq < least)) least = sq;
+    }
+    return (total == 0.0 || least < 0.0) ? rtol : rtol * std::sqrt(least / total);
   }
 };
 
