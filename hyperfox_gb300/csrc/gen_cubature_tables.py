@@ -71,4 +71,7 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("HYPERFOX_REFERENCE")
+    if not root:
+        sys.exit("usage: gen_cubature_tables.py <HyperFox source tree> (or set HYPERFOX_REFERENCE)")
+    main(root)

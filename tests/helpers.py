@@ -1,4 +1,6 @@
 """Shared problem builders for the parity tests (seeded, small)."""
+import os
+
 import numpy as np
 
 from hyperfox_gb300 import capi, meshgen
@@ -38,3 +40,19 @@ def fields(dim, order, coords, cells, faces, nfaces, rng, tau2=False, kappa="non
         kap = None
     g = manufactured(coords, faces)
     return tau, kap, g
+
+
+def reference_meshes():
+    """The HyperFox source tree's mesh fixtures, or None when no tree is known here.
+
+    The tree is HYPERFOX_REFERENCE, else the one oracle/build_ref.sh was built from
+    (recorded in oracle/_ref/REFERENCE_ROOT). Tests that read its fixtures skip
+    without it."""
+    root = os.environ.get("HYPERFOX_REFERENCE")
+    if not root:
+        marker = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref",
+                              "REFERENCE_ROOT")
+        if os.path.exists(marker):
+            root = open(marker).read().strip()
+    path = os.path.join(root, "ressources", "meshes") if root else None
+    return path if path and os.path.isdir(path) else None

@@ -12,9 +12,10 @@ import os
 import numpy as np
 import pytest
 
+from helpers import reference_meshes
 from hyperfox_gb300 import capi, meshgen
 
-REF = "/root/reference/ressources/meshes"
+REF = reference_meshes() or ""
 have_ref = pytest.mark.skipif(not os.path.isdir(REF), reason="reference meshes not present")
 
 # TestHDF5Io.cpp: nodes of the 3x3 square, connectivities of the light meshes

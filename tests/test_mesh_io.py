@@ -11,9 +11,10 @@ import numpy as np
 import pytest
 
 from gmsh_util import write_gmsh22
+from helpers import reference_meshes
 from hyperfox_gb300 import capi, meshgen
 
-REF = "/root/reference/ressources/meshes"
+REF = reference_meshes() or ""
 
 
 @pytest.mark.parametrize("dim,n", [(2, 4), (3, 2)])
