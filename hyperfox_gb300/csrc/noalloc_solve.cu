@@ -1,30 +1,41 @@
 // CG solve of a small trace system that allocates no device memory.
 //
-// Some callers cannot call cudaMalloc: code that runs while a CUDA stream is
-// being captured into a graph (an allocation there breaks or invalidates the
-// capture), code inside a framework whose caching allocator owns all device
-// memory (a raw cudaMalloc would fragment its pool or exceed its budget), and
-// real-time loops that forbid allocation latency. They own their device
-// buffers, hand this entry point the system and the solution buffer, and the
-// solver's own working memory (the CG vectors, the block-Jacobi inverses, the
-// reduction partials and the solver state) lives in one file-scope
-// __device__ array of fixed size, resident on every GPU that loads the
-// library until the process exits.
+// Some callers cannot call cudaMalloc: code inside a framework whose caching
+// allocator owns all device memory (a raw cudaMalloc would fragment its pool
+// or break its memory budget), and real-time loops that cannot take the
+// latency or the possible failure of an allocation in the middle of a step.
+// They own their device buffers and hand this entry point the system and the
+// solution buffer; the solver's own working memory (the CG vectors, the
+// block-Jacobi inverses, the reduction partials and the solver state) lives in
+// one file-scope __device__ array of fixed size, resident on every GPU that
+// loads the library until the process exits.
 //
 // The computation is the FP64 CG + per-face block-Jacobi solve of hfx_solve
 // (HFX_KSP_CG, HFX_PC_BLOCK_JACOBI): the Dirichlet rows are eliminated
 // symmetrically and the interior block negated, and the result is the
-// solution of the stored system. Limits: at most HFX_NOALLOC_MAX_DOFS trace
-// DOFs and HFX_NOALLOC_MAX_NF nodes per face.
+// solution of the stored system. CG needs a symmetric system: the entry point
+// measures the symmetry of the interior block first and refuses a
+// non-symmetric one (HFX_ERR_ARG), as hfx_solve refuses CG there. A face
+// whose block row holds no diagonal block is refused the same way. Limits: at
+// most HFX_NOALLOC_MAX_DOFS trace DOFs and HFX_NOALLOC_MAX_NF nodes per face.
+//
+// The host drives the iteration: it synchronises the caller's stream and reads
+// the solver state between batches of iterations, and returns after the solve.
+//
+// The first call on a device, with that device current, looks up the device
+// address of the scratch array (cudaGetSymbolAddress; the array's name in host
+// code is only a host-side stand-in) and keeps it for later calls: make that
+// first call before any stream capture.
 //
 // Every call shares the scratch array and leaves the last call's contents in
-// it; the entry point clears what must start at zero itself. Calls that
-// overlap on the GPU (two streams, two host threads) race on the scratch and
-// must be serialised by the caller.
+// it; the entry point clears what must start at zero itself (a one-thread
+// kernel resets the solver state). Calls that overlap on the GPU (two streams,
+// two host threads) race on the scratch and must be serialised by the caller.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <mutex>
 
 #include <cuda_runtime.h>
@@ -40,11 +51,17 @@ constexpr int kMaxNF = HFX_NOALLOC_MAX_NF;
 constexpr int kThreads = 256;
 constexpr int kMaxBlocks = 1024;  // reduction partials per value
 constexpr int kStateDoubles = (int)((sizeof(CgState) + sizeof(double) - 1) / sizeof(double));
-// scratch layout (doubles): bS, r, z, p, q | inverse face blocks | partials | state
+// scratch layout (doubles): bS, r, z, p, q | inverse face blocks | partials | state |
+// pattern check words (max |A - A^T| and max |A| of the interior block as the bit patterns
+// of non-negative doubles, which order as the doubles do; a bad-pattern flag)
 constexpr int64_t kOffPc = 5 * kMaxDofs;
 constexpr int64_t kOffPart = kOffPc + kMaxDofs * kMaxNF;
 constexpr int64_t kOffState = kOffPart + 3 * kMaxBlocks;
-constexpr int64_t kScratchDoubles = kOffState + kStateDoubles + 8;
+constexpr int64_t kOffCheck = kOffState + kStateDoubles;
+constexpr int64_t kScratchDoubles = kOffCheck + 8;
+// relative asymmetry above which CG is refused (a symmetric HDG trace system is
+// symmetric to the rounding of its element matrices, about 1e-15)
+constexpr double kSymTol = 1e-10;
 
 __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
 
@@ -93,23 +110,72 @@ __device__ bool reduce_last(double (&v)[NV], double* partials, unsigned* ticket,
   return true;
 }
 
+__device__ inline void max_bits(unsigned long long* w, double v) {
+  atomicMax(w, (unsigned long long)__double_as_longlong(fabs(v)));
+}
+
+// clears the solver state and the pattern-check words the previous call left behind
+__global__ void nk_reset(double* scr, int maxits) {
+  if (threadIdx.x != 0) return;
+  CgState* st = (CgState*)(scr + kOffState);
+  CgState init{};
+  init.maxits = maxits;
+  *st = init;
+  unsigned long long* chk = (unsigned long long*)(scr + kOffCheck);
+  for (int k = 0; k < 3; ++k) chk[k] = 0ull;
+}
+
 // b' (Dirichlet lift, sign flip), inverse diagonal face blocks, x0 = [0, g],
-// r0 = b' - A' x0, z0 = M^{-1} r0, p0 = z0; sums r.z, r.r, ||b||^2.
+// r0 = b' - A' x0, z0 = M^{-1} r0, p0 = z0; sums r.z, r.r, ||b||^2. Also
+// measures the interior block's asymmetry (each interior block (f, g) against
+// the transpose of block (g, f)) and flags a row without its diagonal block or
+// a block without its transposed partner.
 __global__ void __launch_bounds__(kThreads) nk_start(NoallocSys A, double* scr, double* x) {
   const int NF = A.NF;
-  const int64_t n = A.nFaces * NF;
   double *bS = scr, *r = scr + kMaxDofs, *z = scr + 2 * kMaxDofs, *p = scr + 3 * kMaxDofs;
   double* pc = scr + kOffPc;
   CgState* st = (CgState*)(scr + kOffState);
-  double rz = 0.0, rr = 0.0, bb = 0.0;
+  unsigned long long* chk = (unsigned long long*)(scr + kOffCheck);
+  double rz = 0.0, rr = 0.0, bb = 0.0, asym = 0.0, amax = 0.0;
+  bool bad = false;
   for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < A.nFaces; f += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b0 = A.browptr[f];
     const int nb = (int)(A.browptr[f + 1] - b0), npos = nb * NF;
     const bool rb = A.isBnd[f];
     double B[kMaxNF][kMaxNF], Bi[kMaxNF][kMaxNF];
-    int kd = 0;
-    for (int k = 0; k < nb; ++k)
-      if (A.bcol[b0 + k] == (int)f) kd = k;
+    int kd = -1;
+    bool inRange = true;
+    for (int k = 0; k < nb; ++k) {
+      const int g = A.bcol[b0 + k];
+      if (g == (int)f) kd = k;
+      if (g < 0 || g >= A.nFaces) inRange = false;
+    }
+    if (kd < 0 || !inRange) {  // malformed pattern: no diagonal block, or a column outside the system
+      bad = true;
+      continue;
+    }
+    if (!rb) {
+      for (int k = 0; k < nb; ++k) {
+        const int g = A.bcol[b0 + k];
+        if (A.isBnd[g]) continue;
+        const int64_t c0 = A.browptr[g];
+        const int nbg = (int)(A.browptr[g + 1] - c0), nposg = nbg * NF;
+        int kt = -1;
+        for (int k2 = 0; k2 < nbg; ++k2)
+          if (A.bcol[c0 + k2] == (int)f) kt = k2;
+        if (kt < 0) {
+          bad = true;
+          continue;
+        }
+        for (int a = 0; a < NF; ++a)
+          for (int b = 0; b < NF; ++b) {
+            const double v = A.val[b0 * NF * NF + (int64_t)a * npos + k * NF + b];
+            const double vt = A.val[c0 * NF * NF + (int64_t)b * nposg + kt * NF + a];
+            asym = fmax(asym, fabs(v - vt));
+            amax = fmax(amax, fabs(v));
+          }
+      }
+    }
     for (int a = 0; a < NF; ++a) {
       const double* row = A.val + b0 * NF * NF + (int64_t)a * npos;
       double lift = 0.0;
@@ -157,7 +223,9 @@ __global__ void __launch_bounds__(kThreads) nk_start(NoallocSys A, double* scr, 
       rz += rl[a] * zi;
     }
   }
-  (void)n;
+  if (asym > 0.0) max_bits(&chk[0], asym);
+  if (amax > 0.0) max_bits(&chk[1], amax);
+  if (bad) atomicExch(&chk[2], 1ull);
   double v[3] = {rz, rr, bb}, tot[3];
   if (reduce_last<3>(v, scr + kOffPart, &st->ticket, tot) && threadIdx.x == 0) {
     st->rz = tot[0];
@@ -290,6 +358,33 @@ __global__ void __launch_bounds__(kThreads) nk_residual(NoallocSys A, double* sc
 std::mutex g_mutex;
 double* g_dev_ptr[64] = {};
 
+template <class T>
+struct Same {
+  using type = T;
+};
+
+// launches through cudaLaunchKernel, whose return code belongs to this launch
+// alone (cudaGetLastError would also report, and clear, an earlier error of the
+// caller's)
+template <class... KArgs>
+cudaError_t launch(void (*kernel)(KArgs...), int grid, int block, cudaStream_t s, typename Same<KArgs>::type... args) {
+  void* ptrs[] = {(void*)&args...};
+  return cudaLaunchKernel((const void*)kernel, dim3(grid), dim3(block), ptrs, 0, s);
+}
+
+struct HostCheck {
+  CgState st;
+  unsigned long long chk[3];
+};
+
+cudaError_t read_state(HostCheck* h, const double* scr, cudaStream_t s) {
+  cudaError_t e = cudaMemcpyAsync(&h->st, scr + kOffState, sizeof(CgState), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(h->chk, scr + kOffCheck, sizeof(h->chk), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e;
+}
+
 }  // namespace
 }  // namespace hfx
 
@@ -298,18 +393,19 @@ using namespace hfx;
 extern "C" int hfx_trace_solve_noalloc(int dim, int nodesPerFace, int nFaces, const int64_t* browptr, const int* bcol,
                                        const unsigned char* isBoundary, const double* val, const double* rhs,
                                        double* x, double rtol, int maxits, void* stream, hfx_solve_info* info) {
-  auto fail = [&](int code) {
+  auto report = [&](int code, int iters, double relres, double ms) {
     if (info) {
       info->status = code;
-      info->iterations = 0;
+      info->iterations = iters;
       info->refinements = 0;
-      info->rel_residual = 0.0;
-      info->solve_ms = 0.0;
+      info->rel_residual = relres;
+      info->solve_ms = ms;
       info->fallback = 0;
       info->coarse_degree = 0;
     }
     return code;
   };
+  auto fail = [&](int code) { return report(code, 0, 0.0, 0.0); };
   if (dim < 2 || dim > 3 || nodesPerFace < 1 || nodesPerFace > kMaxNF || nFaces < 1 ||
       (int64_t)nFaces * nodesPerFace > kMaxDofs)
     return fail(HFX_ERR_ARG);  // beyond HFX_NOALLOC_MAX_DOFS / HFX_NOALLOC_MAX_NF
@@ -331,49 +427,38 @@ extern "C" int hfx_trace_solve_noalloc(int dim, int nodesPerFace, int nFaces, co
   cudaStream_t s = (cudaStream_t)stream;
   auto t0 = std::chrono::steady_clock::now();
   NoallocSys A{nFaces, nodesPerFace, dim == 2 ? 5 : 7, browptr, bcol, isBoundary, val, rhs};
-  CgState* st = (CgState*)(scr + kOffState);
-  CgState init{};
-  init.maxits = maxits;
-  // clear the state (ticket, flags, counters) the previous call left behind
-  if (cudaMemcpyAsync(st, &init, sizeof(CgState), cudaMemcpyHostToDevice, s) != cudaSuccess) return fail(HFX_ERR_CUDA);
   int nsm = 0;
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return fail(HFX_ERR_CUDA);
   int gridF = (int)std::min<int64_t>(kMaxBlocks, std::max<int64_t>(1, ((int64_t)nFaces * 32 + kThreads - 1) / kThreads));
   int gridV = (int)std::min<int64_t>(kMaxBlocks, std::max<int64_t>(1, ((int64_t)nFaces + kThreads - 1) / kThreads));
   gridF = std::min(gridF, 4 * nsm);
   gridV = std::min(gridV, 4 * nsm);
-  nk_start<<<gridV, kThreads, 0, s>>>(A, scr, x);
-  CgState h;
-  if (cudaMemcpyAsync(&h, st, sizeof(CgState), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-      cudaStreamSynchronize(s) != cudaSuccess)
-    return fail(HFX_ERR_CUDA);
-  const double tol2 = rtol * rtol * h.bb;
-  if (h.rr > tol2) {
+  if (launch(nk_reset, 1, 32, s, scr, maxits) != cudaSuccess) return fail(HFX_ERR_CUDA);
+  if (launch(nk_start, gridV, kThreads, s, A, scr, x) != cudaSuccess) return fail(HFX_ERR_CUDA);
+  HostCheck h;
+  if (read_state(&h, scr, s) != cudaSuccess) return fail(HFX_ERR_CUDA);
+  double asym, amax;
+  memcpy(&asym, &h.chk[0], sizeof(double));
+  memcpy(&amax, &h.chk[1], sizeof(double));
+  // a malformed pattern, or an interior block that is not symmetric: CG does not apply
+  if (h.chk[2] != 0ull || asym > kSymTol * amax) return fail(HFX_ERR_ARG);
+  const double tol2 = rtol * rtol * h.st.bb;
+  if (h.st.rr > tol2) {
     while (true) {
       for (int k = 0; k < 25; ++k) {
-        nk_spmv<<<gridF, kThreads, 0, s>>>(A, scr);
-        nk_update<<<gridV, kThreads, 0, s>>>(A, scr, x, tol2);
-        nk_pupdate<<<gridV, kThreads, 0, s>>>(A, scr);
+        if (launch(nk_spmv, gridF, kThreads, s, A, scr) != cudaSuccess ||
+            launch(nk_update, gridV, kThreads, s, A, scr, x, tol2) != cudaSuccess ||
+            launch(nk_pupdate, gridV, kThreads, s, A, scr) != cudaSuccess)
+          return fail(HFX_ERR_CUDA);
       }
-      if (cudaMemcpyAsync(&h, st, sizeof(CgState), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-          cudaStreamSynchronize(s) != cudaSuccess)
-        return fail(HFX_ERR_CUDA);
-      if (h.done) break;
+      if (read_state(&h, scr, s) != cudaSuccess) return fail(HFX_ERR_CUDA);
+      if (h.st.done) break;
     }
   }
-  nk_residual<<<gridF, kThreads, 0, s>>>(A, scr, x);
-  if (cudaMemcpyAsync(&h, st, sizeof(CgState), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-      cudaStreamSynchronize(s) != cudaSuccess)
+  if (launch(nk_residual, gridF, kThreads, s, A, (double*)scr, (const double*)x) != cudaSuccess)
     return fail(HFX_ERR_CUDA);
-  if (cudaGetLastError() != cudaSuccess) return fail(HFX_ERR_CUDA);
-  if (info) {
-    info->status = h.status;
-    info->iterations = h.iters;
-    info->refinements = 0;
-    info->rel_residual = h.bb > 0 ? std::sqrt(h.res_rr / h.bb) : std::sqrt(h.res_rr);
-    info->solve_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    info->fallback = 0;
-    info->coarse_degree = 0;
-  }
-  return h.status;
+  if (read_state(&h, scr, s) != cudaSuccess) return fail(HFX_ERR_CUDA);
+  const double relres = h.st.bb > 0 ? std::sqrt(h.st.res_rr / h.st.bb) : std::sqrt(h.st.res_rr);
+  const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return report(h.st.status, h.st.iters, relres, ms);
 }

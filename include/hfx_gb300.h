@@ -228,6 +228,17 @@ int hfx_assemble_ex(hfx_ctx* ctx, int precision);
  * hfx_assembly_info reports whether the last FP64 assembly took the affine path. */
 int hfx_set_assembly_path(hfx_ctx* ctx, int path);
 int hfx_assembly_info(hfx_ctx* ctx, int* affine);
+/* The mixed assembly (HFX_PREC_MIXED) contracts the element operators of HDGBase, HDGDiffusion
+ * and Mass (HDGBase.cpp:67-158, HDGDiffusion.cpp:74-145, Mass.cpp:5-38: the volume blocks C_d,
+ * K_d, M and the face blocks T, E_d, H_d) on the tensor cores (tcgen05, TF32 hi/lo split,
+ * FP32 accumulation; agreement with the FP64 quadrature within 2e-5 of each block's largest
+ * entry) for orders 1-5 (2D) / 1-3 (3D) under path 0; path 1 integrates them on the CUDA
+ * cores. *tensorCores = 1 when the last mixed assembly used the tensor cores. */
+int hfx_mixed_assembly_info(hfx_ctx* ctx, int* tensorCores);
+/* Those FP32 blocks for a list of cells, [count][*stride]: volume rows [C_0..C_{d-1} | K_0..
+ * K_{d-1} | M] of N values (row (k, i) = block k, node i), face rows [T | E | H] of Nf values
+ * (T row (f, a); E, H rows (f, k, a)), then the source load f_u (N). */
+int hfx_get_tc_blocks(hfx_ctx* ctx, int count, const int* cells, float* out, int64_t* stride);
 
 /* ---- Runge-Kutta time integration (RungeKutta.cpp:5-213, HDGModel.cpp:39-47) --
  * A scheme applies to the U rows of every element system at hfx_assemble:
@@ -270,6 +281,16 @@ int hfx_get_condensed(hfx_ctx* ctx, double* S, double* S0, double* U, double* Q,
                       double* Q0);
 /* Global trace system in PETSc AIJ form: sorted columns, explicit zeros kept. */
 int hfx_get_csr(hfx_ctx* ctx, int64_t* rowptr, int* col, double* val, double* rhs);
+/* The condensed blocks of a list of elements only, compact ([count][...], column-major per
+ * element, any output may be NULL): element-block inspection of meshes too large to export
+ * whole (HDGSolver's U, Q, S, U0, Q0, S0 fields of those cells). */
+int hfx_get_condensed_sample(hfx_ctx* ctx, int count, const int* cells, double* S, double* S0, double* U,
+                             double* Q, double* U0, double* Q0);
+/* The AIJ rows of a list of distinct faces (every node of each face, in face then node
+ * order), as hfx_get_csr would export them: rowlen[count*Nf], then the rows' col / val
+ * back to back (cap entries at most; HFX_ERR_ARG if cap is too small), rhs[count*Nf]. */
+int hfx_get_csr_rows(hfx_ctx* ctx, int count, const int* faces, int* rowlen, int* col, double* val, double* rhs,
+                     int64_t cap);
 
 /* ---- solve and recovery --------------------------------------------------------
  * hfx_solve replaces LinAlgebraInterface::solve / PetscInterface::solve
@@ -425,21 +446,26 @@ int hfx_burgers_get_csr(hfx_ctx* ctx, int64_t* rowptr, int* col, double* val, do
 
 /* ---- allocation-free trace solve -------------------------------------------
  * No counterpart in the reference. For callers that cannot allocate device
- * memory: code running while a stream is captured into a CUDA graph, code
- * under a framework whose caching allocator owns the device memory, real-time
- * loops that forbid allocation latency. Same FP64 CG + per-face block-Jacobi
- * solve as hfx_solve (HFX_KSP_CG, HFX_PC_BLOCK_JACOBI) on a trace system the
- * caller already holds in device memory: browptr[nFaces+1] and bcol[nBlocks]
- * (face-block pattern), isBoundary[nFaces] (Dirichlet faces), val in the
- * scalar-CSR order hfx_get_csr exports, rhs and the output x [nFaces*nodesPerFace];
- * stream is a cudaStream_t. The solver's working memory is one fixed
- * __device__ array (about 7.9 MB, held by every GPU that loads the library
- * until exit), so systems above HFX_NOALLOC_MAX_DOFS trace DOFs or
- * HFX_NOALLOC_MAX_NF nodes per face are refused with HFX_ERR_ARG. The first
- * call on a device looks up the array's device address: make that first call
+ * memory: code under a framework whose caching allocator owns the device
+ * memory (a raw cudaMalloc would fragment its pool or break its budget), and
+ * real-time loops that cannot take an allocation's latency or failure in the
+ * middle of a step. Same FP64 CG + per-face block-Jacobi solve as hfx_solve
+ * (HFX_KSP_CG, HFX_PC_BLOCK_JACOBI) on a trace system the caller already holds
+ * in device memory: browptr[nFaces+1] and bcol[nBlocks] (face-block pattern),
+ * isBoundary[nFaces] (Dirichlet faces), val in the scalar-CSR order
+ * hfx_get_csr exports, rhs and the output x [nFaces*nodesPerFace]; stream is a
+ * cudaStream_t. The solver's working memory is one fixed __device__ array
+ * (about 7.9 MB, held by every GPU that loads the library until exit), so
+ * systems above HFX_NOALLOC_MAX_DOFS trace DOFs or HFX_NOALLOC_MAX_NF nodes per
+ * face are refused with HFX_ERR_ARG. CG needs a symmetric interior block: a
+ * system whose interior block is not symmetric (relative asymmetry above
+ * 1e-10), or whose pattern has a row without its diagonal block or a block
+ * without its transposed partner, is refused with HFX_ERR_ARG. The first call
+ * on a device looks up the array's device address: make that first call
  * before any stream capture. Calls share the array; calls that overlap on the
- * GPU race and must be serialised by the caller. Returns after convergence
- * (it synchronises the stream); info may be NULL. */
+ * GPU race and must be serialised by the caller. The host drives the
+ * iterations and synchronises the stream; the call returns after the solve,
+ * with HFX_ERR_NOT_CONVERGED when maxits ends it. info may be NULL. */
 #define HFX_NOALLOC_MAX_DOFS 65536
 #define HFX_NOALLOC_MAX_NF 10
 int hfx_trace_solve_noalloc(int dim, int nodesPerFace, int nFaces, const int64_t* browptr, const int* bcol,
