@@ -139,11 +139,21 @@ __global__ void __launch_bounds__(TPE * EPC)
   int* bnd = I + N + F;
 
   const int64_t nGroups = (int64_t)gridDim.x * EPC;
+  // blocks precomputed on the tensor cores (FP32 path): loaded instead of integrated
+  const bool tcMode = sizeof(T) == 4 && p.tcBlocks != nullptr;
   for (int64_t base = (int64_t)blockIdx.x * EPC; base < p.nCells; base += nGroups) {
     const int64_t e = base + grp;
     const bool active = e < p.nCells;
+    const float* tcb = tcMode && active ? p.tcBlocks + e * p.tcStride : nullptr;
     // ---------------------------------------------------------- gather
-    if (active) {
+    if (active && tcMode) {
+      for (int i = t; i < F; i += TPE) {
+        int f = p.cell2face[e * F + i];
+        faceId[i] = f;
+        bnd[i] = p.isBoundary[f];
+      }
+    }
+    if (active && !tcMode) {
       const int* cell = p.cells + e * N;
       for (int i = t; i < N * D; i += TPE) X[i] = p.coords[(int64_t)cell[i / D] * D + (i % D)];
       for (int i = t; i < N * D * D; i += TPE) {
@@ -171,7 +181,7 @@ __global__ void __launch_bounds__(TPE * EPC)
     }
     __syncthreads();
     // ------------------------------------------------- volume geometry
-    if (active) {
+    if (active && !tcMode) {
       for (int q = t; q < NI; q += TPE) {
         T J[D][D];
         for (int r = 0; r < D; ++r)
@@ -278,7 +288,11 @@ __global__ void __launch_bounds__(TPE * EPC)
     }
     __syncthreads();
     // scaled physical gradients G = dV J^{-1} grad phi and KG = kappa G
-    if (active) {
+    if (active && tcMode) {
+      const float* tfu = tcb + (2 * D * N + N) * N + F * NF * (1 + 2 * D) * NF;
+      for (int i = t; i < N; i += TPE) fu[i] = rhsMode ? (T)p.rhsU[e * N + i] : (T)tfu[i];
+    }
+    if (active && !tcMode) {
       for (int qi = t; qi < NI * N; qi += TPE) {
         int q = qi / N, i = qi % N;
         T g[D];
@@ -305,7 +319,21 @@ __global__ void __launch_bounds__(TPE * EPC)
     }
     __syncthreads();
     // ------------------------------------------ volume and face blocks
-    if (active) {
+    if (active && tcMode) {
+      // tensor-core blocks: [C | K | M] rows of N, then [T | E | H] rows of NF (same index order)
+      for (int i = t; i < D * N * N; i += TPE) {
+        Cm[i] = (T)tcb[i];
+        Km[i] = (T)tcb[D * N * N + i];
+      }
+      for (int i = t; i < N * N; i += TPE) Mm[i] = (T)tcb[2 * D * N * N + i];
+      const float* tf = tcb + (2 * D * N + N) * N;
+      for (int i = t; i < F * NF * NF; i += TPE) Tm[i] = (T)tf[i];
+      for (int i = t; i < F * D * NF * NF; i += TPE) {
+        Em[i] = (T)tf[F * NF * NF + i];
+        Hm[i] = (T)tf[F * NF * NF + F * D * NF * NF + i];
+      }
+    }
+    if (active && !tcMode) {
       for (int ij = t; ij < N * N; ij += TPE) {
         int i = ij / N, j = ij % N;
         T m = 0.0;
@@ -432,7 +460,9 @@ __global__ void __launch_bounds__(TPE * EPC)
         if (p.dt > 0.0) {
           // mass of the time scheme: M = sum_q dV phi phi (Mass.cpp:5-38)
           T mm = 0.0;
-          for (int q = 0; q < NI; ++q) mm += dV[q] * phi[q * N + i] * phi[q * N + j];
+          if (tcMode) mm = (T)tcb[2 * D * N * N + i * N + j];
+          else
+            for (int q = 0; q < NI; ++q) mm += dV[q] * phi[q * N + i] * phi[q * N + j];
           v = cs * v + mm;
         }
         Am[ij] = v;
@@ -460,7 +490,9 @@ __global__ void __launch_bounds__(TPE * EPC)
             T mu = 0.0;
             for (int j = 0; j < N; ++j) {
               T mm = 0.0;
-              for (int q = 0; q < NI; ++q) mm += dV[q] * phi[q * N + i] * phi[q * N + j];
+              if (tcMode) mm = (T)tcb[2 * D * N * N + i * N + j];
+              else
+                for (int q = 0; q < NI; ++q) mm += dV[q] * phi[q * N + i] * phi[q * N + j];
               mu += mm * p.uOld[e * N + j];
             }
             v += mu;

@@ -71,6 +71,11 @@ struct LocalParams {
   const double* rkWu;          // [nCells][N]
   const double* rkWq;          // [nCells][N*D] node-major
   const double* rkWl;          // [nFaces][NF]
+  // FP32 path only: the element blocks (C_d, K_d, M, T, E_d, H_d, f_u) from the tensor-core
+  // contraction kernel (tc_assembly.cu), [nCells][tcStride]; when set, the element kernel
+  // loads them instead of integrating over the element (no Runge-Kutta stage, no explicit mode)
+  const float* tcBlocks;
+  int64_t tcStride;
 };
 
 cudaError_t launch_local_condense(int dim, int order, const LocalParams& p, cudaStream_t s);

@@ -16,7 +16,8 @@ enum KernelId {
   K_OTHER = 6,      // setup kernels of the solve (system prep, preconditioner, residuals)
   K_RESIDUAL = 7,   // FP64 matrix-free residual of the full HDG system (mixed precision)
   K_COARSE = 8,     // two-level preconditioner: restriction, Chebyshev coarse solve, coarse setup
-  K_COUNT = 9
+  K_TENSOR = 9,     // element contractions on the tensor cores (tc_assembly.cu)
+  K_COUNT = 10
 };
 
 class KernelTimer {
