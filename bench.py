@@ -59,6 +59,14 @@ CONFIGS = {
     "cfg5": dict(dim=3, n=60, order=2, aniso=dict(sigma=1.5, corr=0.05, ratio=100.0, seed=5), cpu_n=8,
                  desc="3D anisotropic diffusion, unit cube 60^3x6 tets (1.296M), p=2, kappa = exp(g) x "
                       "(I + 99 a a^T), g Gaussian random field (sigma 1.5, corr 0.05) per cell, seeded axis a"),
+    # the cfg2 mesh with a diffusion coefficient that varies inside the cells (HyperFox's nodal
+    # DiffusionTensor field): the general element path (per-element quadrature), GMRES
+    "cfg2-nodal": dict(dim=3, n=40, order=3, nodal_kappa=True,
+                       desc="3D HDG diffusion-source, unit cube 40^3x6 tets (384k), p=3, nodal kappa = "
+                            "exp(0.5 sin(2 pi x) sin(2 pi y) sin(2 pi z))"),
+    "mid3d-nodal": dict(dim=3, n=20, order=3, nodal_kappa=True,
+                        desc="3D HDG diffusion-source, 20^3x6 tets (48k), p=3, nodal kappa = "
+                             "exp(0.5 sin(2 pi x) sin(2 pi y) sin(2 pi z))"),
     "cfg5-small": dict(dim=3, n=20, order=2, aniso=dict(sigma=1.5, corr=0.05, ratio=100.0, seed=5), cpu_n=8,
                        desc="3D anisotropic diffusion, 20^3x6 tets (48k), p=2, the cfg5 coefficient field"),
     # independent problems of uneven size and order, one order per problem (a Mesh has one
@@ -166,6 +174,13 @@ def aniso_kappa(coords, cells, dim, sigma, corr, ratio, seed, modes=256):
     return np.ascontiguousarray(np.broadcast_to(kap, (nC, N, dim * dim)))
 
 
+def nodal_kappa(coords, cells):
+    """Scalar diffusion coefficient at the cell nodes [nCells][N][1], varying inside every cell:
+    exp(0.5 sin(2 pi x) sin(2 pi y) sin(2 pi z))."""
+    x = coords[cells]
+    return np.exp(0.5 * np.prod(np.sin(2 * np.pi * x), axis=-1))[..., None]
+
+
 def make_problem(cfg):
     from hyperfox_gb300 import capi, meshgen
     dim, n, p = cfg["dim"], cfg["n"], cfg["order"]
@@ -230,7 +245,11 @@ def run_ours(args, world, rank, local):
     ctx.set_source(capi.SRC_SINPROD, param=dim * np.pi ** 2)
     if cfg.get("aniso"):
         ctx.set_kappa(aniso_kappa(coords, cells, dim, **cfg["aniso"]), layout=1)
+    if cfg.get("nodal_kappa"):
+        ctx.set_kappa(nodal_kappa(coords, cells), layout=1)
     L = ctx.L
+    if args.assembly_path:
+        ctx._chk(L.hfx_set_assembly_path(ctx.h, args.assembly_path), "assembly_path")
     prec = capi.PREC_FP64 if args.precision == "fp64" else capi.PREC_MIXED
     pc = capi.PC_TWOLEVEL if args.precond == "twolevel" else capi.PC_BLOCK_JACOBI
     opts = capi.solve_opts(precision=prec, rtol=args.rtol, precond=pc, maxits=200000,
@@ -255,7 +274,9 @@ def run_ours(args, world, rank, local):
 
     # accuracy reference: plain FP64 CG to 1e-13 (untimed)
     ctx.assemble()
-    ref_opts = capi.solve_opts(precision=capi.PREC_FP64, rtol=1e-13, precond=capi.PC_BLOCK_JACOBI, maxits=500000)
+    # (a diffusion coefficient varying inside the cells makes the system non-symmetric: GMRES(100) to 1e-11)
+    ref_opts = capi.solve_opts(precision=capi.PREC_FP64, rtol=1e-11 if cfg.get("nodal_kappa") else 1e-13,
+                               precond=capi.PC_BLOCK_JACOBI, maxits=500000, restart=100)
     ref_info = capi.SolveInfo()
     x_ref = np.zeros(ctx.ndofs)
     ctx._chk(L.hfx_solve(ctx.h, capi.ctypes.byref(ref_opts), capi._p(x_ref), capi.ctypes.byref(ref_info)), "ref solve")
@@ -286,7 +307,7 @@ def run_ours(args, world, rank, local):
     dev_ms = barrier_max(world, ms.value)
     kt = {}
     for name, kid in (("local", 0), ("scatter", 1), ("spmv64", 2), ("spmv32", 3), ("update", 4), ("recover", 5),
-                      ("other", 6), ("residual", 7), ("coarse", 8)):
+                      ("other", 6), ("residual", 7), ("coarse", 8), ("tensor", 9)):
         n_l, t_l = capi.ctypes.c_int(), capi.ctypes.c_double()
         L.hfx_kernel_time(ctx.h, kid, capi.ctypes.byref(n_l), capi.ctypes.byref(t_l))
         kt[name] = (n_l.value, t_l.value)
@@ -321,6 +342,67 @@ def run_ours(args, world, rank, local):
         pms = capi.ctypes.c_double()
         ctx._chk(L.hfx_elapsed_ms(ctx.h, 2, 3, capi.ctypes.byref(pms)), "elapsed")
         plain = dict(time_to_solve_s=pms.value / 1e3 / max(1, args.plain_steps), iterations=fp_info.iterations)
+    # the learned coarse solve on its own: the same two-level mixed solve with Chebyshev of the
+    # learned polynomial's degree and with Chebyshev at its adaptive degree, and the first solve
+    # of a new system including the training (wall clock: training + one step)
+    coarse_arms = None
+    if learned is not None and not args.no_plain:
+        coarse_arms = {}
+        for name, kw in (("chebyshev_same_degree", dict(coarse_mode=capi.COARSE_CHEBYSHEV,
+                                                        coarse_degree=args.coarse_degree)),
+                         ("chebyshev_adaptive", dict(coarse_mode=capi.COARSE_CHEBYSHEV, coarse_degree=0)),
+                         ("learned", dict(coarse_mode=capi.COARSE_LEARNED, coarse_degree=0))):
+            o2 = capi.solve_opts(precision=prec, rtol=args.rtol, precond=pc, maxits=200000,
+                                 inner_rtol=args.inner_rtol, coarse_rtol=args.coarse_rtol, **kw)
+            i2 = capi.SolveInfo()
+            x2 = np.zeros(ctx.ndofs)
+            ctx._chk(L.hfx_mark(ctx.h, 4), "mark")
+            for _ in range(max(1, args.plain_steps)):
+                ctx._chk(L.hfx_assemble_ex(ctx.h, asm_prec), "assemble")
+                ctx._chk(L.hfx_solve(ctx.h, capi.ctypes.byref(o2), None, capi.ctypes.byref(i2)), "solve")
+                ctx._chk(L.hfx_recover(ctx.h, None, None), "recover")
+            ctx._chk(L.hfx_mark(ctx.h, 5), "mark")
+            ams = capi.ctypes.c_double()
+            ctx._chk(L.hfx_elapsed_ms(ctx.h, 4, 5, capi.ctypes.byref(ams)), "elapsed")
+            ctx._chk(L.hfx_solve(ctx.h, capi.ctypes.byref(o2), capi._p(x2), capi.ctypes.byref(i2)), "solve")
+            coarse_arms[name] = dict(time_to_solve_s=ams.value / 1e3 / max(1, args.plain_steps),
+                                     iterations=i2.iterations, coarse_degree=i2.coarse_degree,
+                                     coarse_learned=bool(i2.coarse_learned),
+                                     rel_err_vs_fp64=float(np.linalg.norm(x2 - x_ref) / np.linalg.norm(x_ref)))
+        ctx._chk(L.hfx_synchronize(ctx.h), "sync")
+        t0 = time.perf_counter()
+        ti = ctx.coarse_train(degree=args.coarse_degree, samples=16, steps=300)
+        step_device()
+        ctx._chk(L.hfx_synchronize(ctx.h), "sync")
+        coarse_arms["time_to_first_solve_s"] = time.perf_counter() - t0
+        coarse_arms["time_to_first_solve_accepted"] = bool(ti.accepted)
+    # error against the oracle's direct FP64 solve of the 12^3 x 6 sub-cube of this workload
+    # (stored fixture), with the same solver options
+    oracle_check = None
+    gold_path = os.path.join(ROOT, "tests", "golden", "subcube12_p3_trace.npz")
+    if (dim, p) == (3, 3) and not cfg.get("aniso") and not cfg.get("nodal_kappa") and os.path.exists(gold_path):
+        from hyperfox_gb300 import meshgen
+        gold = np.load(gold_path)
+        vs, ss = meshgen.cube_simplices(int(gold["n"]))
+        sc, scl = meshgen.high_order(vs, ss, capi.refel(3, 3)["nodes"])
+        sub = capi.Context(local)
+        sub.upload_mesh(3, 3, sc, scl)
+        _, _, sfaces, _ = sub.topology()
+        sub.set_source(capi.SRC_SINPROD, param=3 * np.pi ** 2)
+        sub.set_dirichlet(np.prod(np.sin(np.pi * sc[sfaces]), axis=-1))
+        if args.assembly_path:
+            sub._chk(sub.L.hfx_set_assembly_path(sub.h, args.assembly_path), "assembly_path")
+        sub._chk(sub.L.hfx_assemble_ex(sub.h, asm_prec), "assemble")
+        if learned is not None:
+            sub.coarse_train(degree=args.coarse_degree, samples=16, steps=300)
+        si = capi.SolveInfo()
+        xs = np.zeros(sub.ndofs)
+        sub._chk(sub.L.hfx_solve(sub.h, capi.ctypes.byref(opts), capi._p(xs), capi.ctypes.byref(si)), "solve")
+        oracle_check = dict(rel_err=float(np.linalg.norm(xs - gold["trace"]) / np.linalg.norm(gold["trace"])),
+                            sample="12^3x6 sub-cube (10,368 elements, 216,000 trace DOFs) of this workload, same "
+                                   "solver options; oracle = FP64 assembly + sparse LU (tests/golden)",
+                            iterations=si.iterations)
+        sub.close()
     E = ctx.nCells
     step_s = dev_ms / 1e3 / args.steps
     # roofline of the dominant kernel, and of the dominant HBM-bound kernel
@@ -356,8 +438,11 @@ def run_ours(args, world, rank, local):
         LL, NI = F_ * NF_, ctx.re["nIP"]
         fma = (F_ * NF_ ** 3 + N * N * (dim * dim + 1) + N * LL * dim + NI * N * dim + N * NI + N ** 3 / 6
                + 2 * (LL + 1) * N * (N - 1) / 2 + LL * (LL + 1) / 2 * N + LL * N)
+        # the symmetric W^T W product runs as double-float pairs on the FP32 pipe: not FP64-pipe work
+        df_fma = LL * (LL + 1) / 2 * N
+        fma64 = fma - df_fma
         avg_ms = kt["local"][1] / max(1, kt["local"][0])
-        tf = 2 * fma * E / (avg_ms / 1e3) / 1e12
+        tf = 2 * fma64 * E / (avg_ms / 1e3) / 1e12
         # the reference's own algorithm per element (dense quadrature assembly plus the dense
         # LU-equivalent condensation of HDGSolver.cpp:331-348): the same elements per second
         # expressed in its FLOP count
@@ -370,7 +455,11 @@ def run_ours(args, world, rank, local):
                     achieved=round(tf, 3), peak=FP64_NOMINAL_TFLOPS, unit="TFLOP/s",
                     frac=round(tf / FP64_NOMINAL_TFLOPS, 4),
                     traffic=TRAFFIC_PER_ELEMENT_LOCAL * E if (dim, p) == (3, 3) else None,
-                    flops_per_element=int(2 * fma), avg_launch_ms=round(avg_ms, 4),
+                    flops_per_element=int(2 * fma64), avg_launch_ms=round(avg_ms, 4),
+                    count="FP64-pipe FLOPs of the executed algorithm (reference operators, Cholesky Schur); "
+                          "the W^T W product's %d double-float multiply-adds per element run on the FP32 pipe "
+                          "and are not counted" % int(df_fma),
+                    double_float_fma_per_element=int(df_fma),
                     flops_per_element_reference_algorithm=int(ref_asm + ref_cond),
                     reference_algorithm_equivalent_tflops=round((ref_asm + ref_cond) * E / (avg_ms / 1e3) / 1e12, 2),
                     peak_source="nominal GB300 FP64 (no measured FP64 peak); ncu: FP64 pipe 86% active")
@@ -409,7 +498,11 @@ def run_ours(args, world, rank, local):
         "krylov_iterations": iters,
         "refinements": refinements,
         "rel_err_vs_fp64": rel_err,
+        "rel_err_vs_fp64_reference": "the same library's FP64 block-Jacobi CG of the same system to relative "
+                                     "residual 1e-13 (GPU)",
+        "rel_err_vs_oracle": oracle_check,
         "meets_1e-8_rel_err": bool(rel_err <= 1e-8),
+        "coarse_solve_comparison": coarse_arms,
         "fp64_reference_iterations": ref_info.iterations,
         "plain_fp64": plain,
         "learned_coarse": learned,
@@ -850,6 +943,8 @@ def cpu_sample(cfg_name, nthreads, rtol, budget_elems=None):
     P = O.Problem(dim, p, coords, cells)
     g = np.prod(np.sin(np.pi * coords[P.faces]), axis=-1)
     kap = aniso_kappa(coords, cells, dim, **cfg["aniso"]).ravel() if cfg.get("aniso") else None
+    if cfg.get("nodal_kappa"):
+        kap = nodal_kappa(coords, cells).ravel()
     P.set_fields(np.ones(P.ndofs), kappa=kap, src_mode=2, dirichlet=g.ravel())
     t0 = time.perf_counter()
     P.assemble(nthreads)
@@ -886,6 +981,9 @@ def main():
     ap.add_argument("--coarse", default="learned", choices=["learned", "chebyshev"],
                     help="coarse solve of the two-level preconditioner: trained polynomial or Chebyshev")
     ap.add_argument("--coarse-degree", type=int, default=8, help="degree of the learned coarse polynomial")
+    ap.add_argument("--assembly-path", type=int, default=0, choices=[0, 1],
+                    help="element kernel choice (hfx_set_assembly_path): 0 automatic (affine kernel, or the "
+                         "tensor-core contractions in the mixed assembly), 1 quadrature on the CUDA cores")
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -982,6 +1080,9 @@ def main():
         if not args.no_cpu:
             try:
                 res["cpu_baseline"] = cpu_sample(args.config, os.cpu_count() or 1, args.rtol)
+                # one thread, as the reference runs per MPI rank (no threading in its element loop)
+                res["cpu_baseline_1t"] = cpu_sample(args.config, 1, args.rtol,
+                                                    budget_elems=8 if CONFIGS[args.config]["dim"] == 3 else None)
             except Exception as e:  # the baseline is reported, not required
                 res["cpu_baseline"] = {"error": str(e)}
         print(json.dumps(res))

@@ -40,7 +40,7 @@ EXPORTED = [
     "hfx_rk_butcher", "hfx_rk_set", "hfx_rk_set_type", "hfx_rk_begin_step", "hfx_rk_compute_stage",
     "hfx_rk_compute_solution", "hfx_set_trace", "hfx_get_state",
     "hfx_set_tau", "hfx_set_kappa", "hfx_set_source", "hfx_set_dirichlet", "hfx_set_time_scheme",
-    "hfx_ip_coords", "hfx_assemble", "hfx_assemble_ex", "hfx_set_solver_type", "hfx_set_state", "hfx_set_assembly_path", "hfx_assembly_info", "hfx_get_condensed", "hfx_get_csr",
+    "hfx_ip_coords", "hfx_assemble", "hfx_assemble_ex", "hfx_set_solver_type", "hfx_set_state", "hfx_set_assembly_path", "hfx_assembly_info", "hfx_get_condensed", "hfx_get_csr", "hfx_get_condensed_sample", "hfx_get_csr_rows", "hfx_mixed_assembly_info", "hfx_get_tc_blocks", "hfx_test_coarse_barrier",
     "hfx_solve_opts_default", "hfx_solve", "hfx_recover", "hfx_coarse_operator", "hfx_coarse_train",
     "hfx_coarse_loss_grad",
     "hfx_la_create", "hfx_la_destroy", "hfx_la_allocate", "hfx_la_set_values", "hfx_la_set_rhs",
@@ -70,7 +70,8 @@ class SolveOpts(ctypes.Structure):
     _fields_ = [("method", ctypes.c_int), ("precond", ctypes.c_int), ("precision", ctypes.c_int),
                 ("rtol", ctypes.c_double), ("maxits", ctypes.c_int), ("restart", ctypes.c_int),
                 ("inner_rtol", ctypes.c_double), ("use_initial_guess", ctypes.c_int),
-                ("coarse_guess", ctypes.c_int), ("coarse_rtol", ctypes.c_double), ("coarse_mode", ctypes.c_int)]
+                ("coarse_guess", ctypes.c_int), ("coarse_rtol", ctypes.c_double), ("coarse_mode", ctypes.c_int),
+                ("coarse_degree", ctypes.c_int)]
 
 
 class SolveInfo(ctypes.Structure):
@@ -130,6 +131,11 @@ def load(path=LIB_PATH):
         "hfx_assemble_ex": ([vp, ip], ip),
         "hfx_get_condensed": ([vp] * 7, ip),
         "hfx_get_csr": ([vp] * 5, ip),
+        "hfx_get_condensed_sample": ([vp, ip, vp] + [vp] * 6, ip),
+        "hfx_mixed_assembly_info": ([vp, vp], ip),
+        "hfx_test_coarse_barrier": ([vp], ip),
+        "hfx_get_tc_blocks": ([vp, ip, vp, vp, vp], ip),
+        "hfx_get_csr_rows": ([vp, ip, vp, vp, vp, vp, vp, ctypes.c_int64], ip),
         "hfx_solve_opts_default": ([ctypes.POINTER(SolveOpts)], None),
         "hfx_solve": ([vp, ctypes.POINTER(SolveOpts), vp, ctypes.POINTER(SolveInfo)], ip),
         "hfx_recover": ([vp, vp, vp], ip),
@@ -484,6 +490,46 @@ class Context:
                   "get_condensed")
         return out
 
+    def mixed_assembly_info(self):
+        """1 when the last mixed assembly contracted the element blocks on the tensor cores."""
+        v = ctypes.c_int()
+        self._chk(self.L.hfx_mixed_assembly_info(self.h, ctypes.byref(v)), "mixed_assembly_info")
+        return v.value
+
+    def tc_blocks(self, cells):
+        """FP32 element blocks of the tensor-core mixed assembly, [len(cells)][stride]."""
+        cells = np.ascontiguousarray(cells, np.int32)
+        st = ctypes.c_int64()
+        self.L.hfx_get_tc_blocks(self.h, 0, None, None, ctypes.byref(st))
+        out = np.zeros((len(cells), st.value), np.float32)
+        self._chk(self.L.hfx_get_tc_blocks(self.h, len(cells), _p(cells), _p(out), ctypes.byref(st)), "get_tc_blocks")
+        return out
+
+    def condensed_sample(self, cells):
+        cells = np.ascontiguousarray(cells, np.int32)
+        n, U, Q, Ll = len(cells), self.lenU, self.lenQ, self.lenL
+        out = dict(S=np.zeros((n, Ll * Ll)), S0=np.zeros((n, Ll)), U=np.zeros((n, U * Ll)), Q=np.zeros((n, Q * Ll)),
+                   U0=np.zeros((n, U)), Q0=np.zeros((n, Q)))
+        self._chk(self.L.hfx_get_condensed_sample(self.h, n, _p(cells),
+                                                  *[_p(out[k]) for k in ("S", "S0", "U", "Q", "U0", "Q0")]),
+                  "get_condensed_sample")
+        return out
+
+    def csr_rows(self, faces):
+        """AIJ rows of the listed faces: (rowlen, col, val, rhs), rows back to back."""
+        faces = np.ascontiguousarray(faces, np.int32)
+        Nf = self.re["nNodesFace"]
+        nr = len(faces) * Nf
+        cap = nr * 2 * self.re["nFaces"] * Nf
+        rowlen = np.zeros(nr, np.int32)
+        col = np.zeros(cap, np.int32)
+        val = np.zeros(cap)
+        rhs = np.zeros(nr)
+        self._chk(self.L.hfx_get_csr_rows(self.h, len(faces), _p(faces), _p(rowlen), _p(col), _p(val), _p(rhs), cap),
+                  "get_csr_rows")
+        n = int(rowlen.sum())
+        return rowlen, col[:n], val[:n], rhs
+
     def csr(self):
         rowptr = np.zeros(self.ndofs + 1, np.int64)
         col = np.zeros(self.nnz, np.int32)
@@ -729,6 +775,46 @@ class Burgers:
         self.c._chk(self.c.L.hfx_burgers_get_condensed(self.c.h, *[_p(out[k]) for k in ("S", "S0", "U", "Q", "U0", "Q0")]),
                     "burgers_get_condensed")
         return out
+
+    def mixed_assembly_info(self):
+        """1 when the last mixed assembly contracted the element blocks on the tensor cores."""
+        v = ctypes.c_int()
+        self._chk(self.L.hfx_mixed_assembly_info(self.h, ctypes.byref(v)), "mixed_assembly_info")
+        return v.value
+
+    def tc_blocks(self, cells):
+        """FP32 element blocks of the tensor-core mixed assembly, [len(cells)][stride]."""
+        cells = np.ascontiguousarray(cells, np.int32)
+        st = ctypes.c_int64()
+        self.L.hfx_get_tc_blocks(self.h, 0, None, None, ctypes.byref(st))
+        out = np.zeros((len(cells), st.value), np.float32)
+        self._chk(self.L.hfx_get_tc_blocks(self.h, len(cells), _p(cells), _p(out), ctypes.byref(st)), "get_tc_blocks")
+        return out
+
+    def condensed_sample(self, cells):
+        cells = np.ascontiguousarray(cells, np.int32)
+        n, U, Q, Ll = len(cells), self.lenU, self.lenQ, self.lenL
+        out = dict(S=np.zeros((n, Ll * Ll)), S0=np.zeros((n, Ll)), U=np.zeros((n, U * Ll)), Q=np.zeros((n, Q * Ll)),
+                   U0=np.zeros((n, U)), Q0=np.zeros((n, Q)))
+        self._chk(self.L.hfx_get_condensed_sample(self.h, n, _p(cells),
+                                                  *[_p(out[k]) for k in ("S", "S0", "U", "Q", "U0", "Q0")]),
+                  "get_condensed_sample")
+        return out
+
+    def csr_rows(self, faces):
+        """AIJ rows of the listed faces: (rowlen, col, val, rhs), rows back to back."""
+        faces = np.ascontiguousarray(faces, np.int32)
+        Nf = self.re["nNodesFace"]
+        nr = len(faces) * Nf
+        cap = nr * 2 * self.re["nFaces"] * Nf
+        rowlen = np.zeros(nr, np.int32)
+        col = np.zeros(cap, np.int32)
+        val = np.zeros(cap)
+        rhs = np.zeros(nr)
+        self._chk(self.L.hfx_get_csr_rows(self.h, len(faces), _p(faces), _p(rowlen), _p(col), _p(val), _p(rhs), cap),
+                  "get_csr_rows")
+        n = int(rowlen.sum())
+        return rowlen, col[:n], val[:n], rhs
 
     def csr(self):
         rowptr = np.zeros(self.ndofs + 1, np.int64)

@@ -19,6 +19,7 @@
 #include "hfx_host.h"
 #include "krylov.h"
 #include "la_gmres.h"
+#include "tc_assembly.h"
 #include "timer.h"
 
 using namespace hfx;
@@ -179,6 +180,11 @@ struct hfx_ctx {
         *d_Q032 = nullptr, *d_dl32 = nullptr;
   double *d_ru = nullptr, *d_rq = nullptr, *d_rl = nullptr, *d_rtrace = nullptr, *d_part = nullptr;
   double mixedBB = 0.0, mixedRR = 0.0;
+  // tensor-core element contractions of the mixed assembly (tc_assembly.cu): packed table
+  // (per mesh order) and the per-element FP32 blocks; lastTensor: the last mixed assembly used them
+  float* d_tctab = nullptr;
+  float* d_tcb = nullptr;
+  bool lastTensor = false;
   // two-level preconditioner: vertex coarse space (built on first use)
   std::vector<int> cellVerts;  // [nCells][dim+1]
   CoarseHost coarseHost;
@@ -186,6 +192,7 @@ struct hfx_ctx {
   DevMem coarseMem;
   bool coarseBuilt = false;
   double coarseTarget = 0.0;
+  int coarseMaxDeg = 64;      // degree cap of the Chebyshev coarse solve (a fixed degree when target ~ 0)
   // vector Burgers (hfx_burgers_*)
   BurgersState burgers;
   // timing
@@ -251,6 +258,8 @@ void free_outputs(hfx_ctx* c) {
   c->qValid = c->lastAffine = false;
   c->mixMem.release();
   c->d_S32 = c->d_S032 = c->d_U32 = c->d_Q32 = c->d_U032 = c->d_Q032 = c->d_dl32 = nullptr;
+  c->d_tctab = c->d_tcb = nullptr;
+  c->lastTensor = false;
   c->d_ru = c->d_rq = c->d_rl = c->d_rtrace = c->d_part = nullptr;
   c->mixedMode = false;
   c->d_status = nullptr;
@@ -880,6 +889,10 @@ static int mixed_condense(hfx_ctx* c, bool writeOps) {
   p.Q = c->d_Q32;
   p.U0 = c->d_U032;
   p.Q0 = c->d_Q032;
+  if (c->lastTensor) {
+    p.tcBlocks = c->d_tcb;
+    p.tcStride = tc_blocks_stride(c->dim, c->order);
+  }
   c->timer.begin(K_LOCAL, c->stream);
   HFX_CUDA(c, launch_local_condense(c->dim, c->order, p, c->stream));
   c->timer.end(K_LOCAL, c->stream);
@@ -935,6 +948,47 @@ static int assemble_mixed(hfx_ctx* c) {
   HFX_CUDA(c, cudaMemsetAsync(c->d_sol, 0, sizeof(double) * E * LU, s));
   HFX_CUDA(c, cudaMemsetAsync(c->d_flux, 0, sizeof(double) * E * LQ, s));
   HFX_CUDA(c, cudaMemsetAsync(c->d_trace, 0, sizeof(double) * c->ndofs(), s));
+  // element blocks contracted on the tensor cores once per assembly; every condensation of
+  // this assembly (the first one and those of the refinement steps) loads them
+  c->lastTensor = false;
+  if (c->assemblyPath == 0 && tc_blocks_supported(c->dim, c->order)) {
+    if (!c->d_tctab) {
+      std::vector<double> tab;
+      tab.insert(tab.end(), c->re.phi.begin(), c->re.phi.end());
+      tab.insert(tab.end(), c->re.dphi.begin(), c->re.dphi.end());
+      tab.insert(tab.end(), c->re.ipW.begin(), c->re.ipW.end());
+      tab.insert(tab.end(), c->re.fPhi.begin(), c->re.fPhi.end());
+      tab.insert(tab.end(), c->re.fDphi.begin(), c->re.fDphi.end());
+      tab.insert(tab.end(), c->re.fIpW.begin(), c->re.fIpW.end());
+      std::vector<float> t = tc_table(c->dim, c->order, tab.data());
+      HFX_CUDA(c, upload(c->mixMem, &c->d_tctab, t.data(), t.size(), s));
+      HFX_CUDA(c, dalloc(c->mixMem, &c->d_tcb, (size_t)E * tc_blocks_stride(c->dim, c->order)));
+    }
+    LocalParams lp = local_params(c);
+    TcBlockParams tp{};
+    tp.nCells = E;
+    tp.coords = lp.coords;
+    tp.cells = lp.cells;
+    tp.cell2face = lp.cell2face;
+    tp.perm = lp.perm;
+    tp.face2cell = lp.face2cell;
+    tp.tau = lp.tau;
+    tp.tauVals = lp.tauVals;
+    tp.kappa = lp.kappa;
+    tp.kc = lp.kc;
+    tp.kappaLayout = lp.kappaLayout;
+    tp.srcMode = lp.srcMode;
+    tp.src = lp.src;
+    tp.srcParam = lp.srcParam;
+    tp.itab = lp.itab;
+    tp.tctab = c->d_tctab;
+    tp.out = c->d_tcb;
+    tp.status = c->d_status;
+    c->timer.begin(K_TENSOR, s);
+    HFX_CUDA(c, launch_tc_blocks(c->dim, c->order, tp, s));
+    c->timer.end(K_TENSOR, s);
+    c->lastTensor = true;
+  }
   // residual at zero = the right-hand side b of the full system
   if ((rc = mixed_residual(c, &c->mixedBB))) return rc;
   c->mixedRR = c->mixedBB;
@@ -942,6 +996,7 @@ static int assemble_mixed(hfx_ctx* c) {
   int status = 0;
   HFX_CUDA(c, cudaMemcpyAsync(&status, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
   HFX_CUDA(c, cudaStreamSynchronize(s));
+  if (status == 2) return set_err(c, HFX_ERR_CUDA, "assemble: a tensor-core wait ran out");
   if (status != 0) return set_err(c, HFX_ERR_SINGULAR, "assemble: singular element block in condensation");
   c->assembled = true;
   c->solved = false;
@@ -967,6 +1022,7 @@ int hfx_assemble(hfx_ctx* c) { return hfx_assemble_ex(c, HFX_PREC_FP64); }
 int hfx_set_assembly_path(hfx_ctx* c, int path) {
   if (!c) return HFX_ERR_ARG;
   if (path != 0 && path != 1) return set_err(c, HFX_ERR_ARG, "set_assembly_path: 0 (automatic) or 1 (quadrature)");
+  c->lastTensor = false;
   c->assemblyPath = path;
   c->assembled = false;
   return HFX_OK;
@@ -1222,6 +1278,37 @@ int hfx_assembly_info(hfx_ctx* c, int* affine) {
   return HFX_OK;
 }
 
+int hfx_test_coarse_barrier(hfx_ctx* c) {
+  if (!c) return HFX_ERR_ARG;
+  if (!c->coarseBuilt || !c->coarse.dev.testHold)
+    return set_err(c, HFX_ERR_STATE, "test_coarse_barrier: no two-level solve has run yet");
+  const int one = 1;
+  HFX_CUDA(c, cudaMemcpyAsync(c->coarse.dev.testHold, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  HFX_CUDA(c, cudaStreamSynchronize(c->stream));
+  return HFX_OK;
+}
+
+int hfx_mixed_assembly_info(hfx_ctx* c, int* tensorCores) {
+  if (!c || !tensorCores) return HFX_ERR_ARG;
+  *tensorCores = (c->mixedMode && c->lastTensor) ? 1 : 0;
+  return HFX_OK;
+}
+
+int hfx_get_tc_blocks(hfx_ctx* c, int count, const int* cells, float* out, int64_t* stride) {
+  if (!c || count < 0 || (count > 0 && (!cells || !out))) return HFX_ERR_ARG;
+  const int64_t st = tc_blocks_stride(c->dim, c->order);
+  if (stride) *stride = st;
+  if (!c->assembled || !c->mixedMode || !c->lastTensor)
+    return set_err(c, HFX_ERR_STATE, "get_tc_blocks: no tensor-core mixed assembly");
+  for (int k = 0; k < count; ++k) {
+    if (cells[k] < 0 || cells[k] >= c->nCells) return set_err(c, HFX_ERR_ARG, "get_tc_blocks: cell out of range");
+    HFX_CUDA(c, cudaMemcpyAsync(out + (size_t)k * st, c->d_tcb + (size_t)cells[k] * st, sizeof(float) * st,
+                                cudaMemcpyDeviceToHost, c->stream));
+  }
+  HFX_CUDA(c, cudaStreamSynchronize(c->stream));
+  return HFX_OK;
+}
+
 int hfx_get_condensed(hfx_ctx* c, double* S, double* S0, double* U, double* Q, double* U0, double* Q0) {
   if (!c) return HFX_ERR_ARG;
   if (!c->assembled) return set_err(c, HFX_ERR_STATE, "get_condensed: assemble first");
@@ -1289,9 +1376,96 @@ int hfx_get_csr(hfx_ctx* c, int64_t* rowptr, int* col, double* val, double* rhs)
   return HFX_OK;
 }
 
+int hfx_get_condensed_sample(hfx_ctx* c, int count, const int* cells, double* S, double* S0, double* U, double* Q,
+                             double* U0, double* Q0) {
+  if (!c || count < 0 || (count > 0 && !cells)) return HFX_ERR_ARG;
+  if (!c->assembled) return set_err(c, HFX_ERR_STATE, "get_condensed_sample: assemble first");
+  if (c->mixedMode)
+    return set_err(c, HFX_ERR_STATE, "get_condensed_sample: the mixed assembly keeps FP32 blocks; use hfx_assemble");
+  for (int k = 0; k < count; ++k)
+    if (cells[k] < 0 || cells[k] >= c->nCells) return set_err(c, HFX_ERR_ARG, "get_condensed_sample: cell out of range");
+  const int64_t LU = c->re.nNodes, LQ = c->dim * c->re.nNodes, LL = c->re.nFaces * c->re.nNodesFace;
+  cudaStream_t s = c->stream;
+  if ((Q || Q0) && !c->qValid) {
+    HFX_CUDA(c, launch_q_from_u(c->dim, c->order, c->nCells, c->d_U, c->d_U0, c->d_atab, c->d_geo, c->d_Q, c->d_Q0, s));
+    c->qValid = true;
+  }
+  auto cp = [&](double* h, const double* d, int64_t n, int k) {
+    return h ? cudaMemcpyAsync(h + (size_t)k * n, d + (size_t)cells[k] * n, sizeof(double) * n, cudaMemcpyDeviceToHost, s)
+             : cudaSuccess;
+  };
+  for (int k = 0; k < count; ++k) {
+    HFX_CUDA(c, cp(S, c->d_S, LL * LL, k));
+    HFX_CUDA(c, cp(S0, c->d_S0, LL, k));
+    HFX_CUDA(c, cp(U, c->d_U, LU * LL, k));
+    HFX_CUDA(c, cp(Q, c->d_Q, LQ * LL, k));
+    HFX_CUDA(c, cp(U0, c->d_U0, LU, k));
+    HFX_CUDA(c, cp(Q0, c->d_Q0, LQ, k));
+  }
+  HFX_CUDA(c, cudaStreamSynchronize(s));
+  return HFX_OK;
+}
+
+int hfx_get_csr_rows(hfx_ctx* c, int count, const int* faces, int* rowlen, int* col, double* val, double* rhs,
+                     int64_t cap) {
+  if (!c || count < 0 || (count > 0 && (!faces || !rowlen))) return HFX_ERR_ARG;
+  if (!c->haveMesh) return set_err(c, HFX_ERR_STATE, "get_csr_rows: no mesh");
+  if (!c->assembled && (val || rhs)) return set_err(c, HFX_ERR_STATE, "get_csr_rows: assemble first");
+  if (c->mixedMode && (val || rhs))
+    return set_err(c, HFX_ERR_STATE, "get_csr_rows: the mixed assembly keeps FP32 values; use hfx_assemble");
+  const int NF = c->re.nNodesFace;
+  const int nF = c->topo.nFaces;
+  int64_t total = 0;
+  std::vector<char> seen;
+  for (int k = 0; k < count; ++k) {
+    const int f = faces[k];
+    if (f < 0 || f >= nF) return set_err(c, HFX_ERR_ARG, "get_csr_rows: face out of range");
+    total += (c->bp.rowptr[f + 1] - c->bp.rowptr[f]) * NF * NF;
+  }
+  {
+    std::vector<int> sorted(faces, faces + count);
+    std::sort(sorted.begin(), sorted.end());
+    if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end())
+      return set_err(c, HFX_ERR_ARG, "get_csr_rows: face listed twice");
+  }
+  if ((col || val) && total > cap) return set_err(c, HFX_ERR_ARG, "get_csr_rows: cap too small");
+  cudaStream_t s = c->stream;
+  std::vector<double> blocks(val ? (size_t)total : 0);
+  int64_t pos = 0;
+  for (int k = 0; k < count; ++k) {
+    const int f = faces[k];
+    const int64_t b0 = c->bp.rowptr[f], nb = c->bp.rowptr[f + 1] - b0;
+    if (val)
+      HFX_CUDA(c, cudaMemcpyAsync(blocks.data() + pos, c->d_val + b0 * NF * NF, sizeof(double) * nb * NF * NF,
+                                  cudaMemcpyDeviceToHost, s));
+    if (rhs)
+      HFX_CUDA(c, cudaMemcpyAsync(rhs + (size_t)k * NF, c->d_rhs + (int64_t)f * NF, sizeof(double) * NF,
+                                  cudaMemcpyDeviceToHost, s));
+    pos += nb * NF * NF;
+  }
+  HFX_CUDA(c, cudaStreamSynchronize(s));
+  // device blocks are column-major per Nf x Nf block; AIJ rows are row-major
+  pos = 0;
+  for (int k = 0; k < count; ++k) {
+    const int f = faces[k];
+    const int64_t b0 = c->bp.rowptr[f], nb = c->bp.rowptr[f + 1] - b0;
+    for (int a = 0; a < NF; ++a) {
+      rowlen[(size_t)k * NF + a] = (int)(nb * NF);
+      for (int64_t kb = 0; kb < nb; ++kb)
+        for (int b = 0; b < NF; ++b) {
+          const int64_t o = pos + (int64_t)a * nb * NF + kb * NF + b;
+          if (col) col[o] = c->bp.col[b0 + kb] * NF + b;
+          if (val) val[o] = blocks[pos + kb * NF * NF + (int64_t)b * NF + a];
+        }
+    }
+    pos += nb * NF * NF;
+  }
+  return HFX_OK;
+}
+
 // Coarse space of the two-level preconditioner: host structure and device
 // buffers on first use (mesh-dependent), the operator after every assembly.
-static int ensure_coarse(hfx_ctx* c, double target) {
+static int ensure_coarse(hfx_ctx* c, double target, int maxDeg = 64) {
   cudaStream_t s = c->stream;
   if (!c->coarseBuilt) {
     std::string err;
@@ -1350,16 +1524,19 @@ static int ensure_coarse(hfx_ctx* c, double target) {
     HFX_CUDA(c, dalloc(m, &d.partials, (size_t)152 * 32 + 64));
     HFX_CUDA(c, dalloc(m, &d.barrier, 2));
     HFX_CUDA(c, dalloc(m, &d.error, 1));
+    HFX_CUDA(c, dalloc(m, &d.testHold, 1));
     HFX_CUDA(c, cudaMemsetAsync(d.barrier, 0, 2 * sizeof(unsigned), s));
     HFX_CUDA(c, cudaMemsetAsync(d.error, 0, sizeof(int), s));
+    HFX_CUDA(c, cudaMemsetAsync(d.testHold, 0, sizeof(int), s));
     c->coarseHost = std::move(h);
     c->coarseBuilt = true;
     c->coarse.ready = false;
   }
-  if (!c->coarse.ready || c->coarseTarget != target) {
+  if (!c->coarse.ready || c->coarseTarget != target || c->coarseMaxDeg != maxDeg) {
     c->coarseTarget = target;
+    c->coarseMaxDeg = maxDeg;
     c->timer.begin(K_COARSE, s);
-    cudaError_t e = coarse_setup<double>(&c->coarse, c->d_S, 64, target, s);
+    cudaError_t e = coarse_setup<double>(&c->coarse, c->d_S, maxDeg, target, s);
     c->timer.end(K_COARSE, s);
     if (e != cudaSuccess) return cuda_err(c, e, "coarse setup");
   }
@@ -1379,6 +1556,7 @@ void hfx_solve_opts_default(hfx_solve_opts* o) {
   o->coarse_guess = 0;
   o->coarse_rtol = 0.1;
   o->coarse_mode = HFX_COARSE_CHEBYSHEV;
+  o->coarse_degree = 0;
 }
 
 static int ensure_workspace(hfx_ctx* c, bool mixed, int restart) {
@@ -1564,8 +1742,10 @@ int hfx_solve(hfx_ctx* c, const hfx_solve_opts* opts, double* trace, hfx_solve_i
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, c->stream);
-  const double ctarget = o.coarse_rtol > 0.0 && o.coarse_rtol < 1.0 ? o.coarse_rtol : 0.1;
-  if (o.precond == HFX_PC_TWOLEVEL && (rc = ensure_coarse(c, ctarget))) {
+  // a fixed Chebyshev degree K: the reduction target is out of reach, so the cap K decides
+  const int cdeg = o.coarse_degree > 0 ? std::min(o.coarse_degree, 64) : 0;
+  const double ctarget = cdeg ? 1e-300 : (o.coarse_rtol > 0.0 && o.coarse_rtol < 1.0 ? o.coarse_rtol : 0.1);
+  if (o.precond == HFX_PC_TWOLEVEL && (rc = ensure_coarse(c, ctarget, cdeg ? cdeg : 64))) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return rc;
@@ -1659,7 +1839,7 @@ int hfx_coarse_operator(hfx_ctx* c, int* nV, int64_t* nnz, int* rowptr, int* col
   if (!c->assembled || c->mixedMode)
     return set_err(c, HFX_ERR_STATE, "coarse_operator: needs a trace system assembled in FP64");
   cudaSetDevice(c->device);
-  int rc = ensure_coarse(c, c->coarseTarget > 0.0 ? c->coarseTarget : 0.1);
+  int rc = ensure_coarse(c, c->coarseTarget > 0.0 ? c->coarseTarget : 0.1, c->coarseMaxDeg);
   if (rc) return rc;
   const CoarseHost& h = c->coarseHost;
   *nV = h.nV;
@@ -1684,7 +1864,7 @@ int hfx_coarse_train(hfx_ctx* c, int degree, int samples, int steps, hfx_train_i
   auto t0 = std::chrono::steady_clock::now();
   int rc = ensure_workspace(c, false, 0);
   if (rc) return rc;
-  if ((rc = ensure_coarse(c, c->coarseTarget > 0.0 ? c->coarseTarget : 0.1))) return rc;
+  if ((rc = ensure_coarse(c, c->coarseTarget > 0.0 ? c->coarseTarget : 0.1, c->coarseMaxDeg))) return rc;
   const int64_t nV = c->coarse.dev.nV;
   float* buf = nullptr;
   HFX_CUDA(c, cudaMalloc(&buf, sizeof(float) * (size_t)samples * nV));
@@ -1756,7 +1936,7 @@ int hfx_coarse_loss_grad(hfx_ctx* c, int degree, const double* theta, int sample
   if (!c->assembled || c->mixedMode)
     return set_err(c, HFX_ERR_STATE, "coarse_loss_grad: needs a trace system assembled in FP64");
   cudaSetDevice(c->device);
-  int rc = ensure_coarse(c, c->coarseTarget > 0.0 ? c->coarseTarget : 0.1);
+  int rc = ensure_coarse(c, c->coarseTarget > 0.0 ? c->coarseTarget : 0.1, c->coarseMaxDeg);
   if (rc) return rc;
   const int64_t nV = c->coarse.dev.nV;
   float* buf = nullptr;

@@ -419,12 +419,16 @@ __device__ __forceinline__ void red_release_add(unsigned* p, unsigned v) {
   asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-__device__ __forceinline__ void grid_barrier(unsigned* count, unsigned target, int* error) {
+// Once any wait has run out (*error set) the later barriers of the solve return
+// at once: its iterates are invalid anyway and the host restarts without them.
+// withhold: this block does not arrive (the test hook that makes the wait run out).
+__device__ __forceinline__ void grid_barrier(unsigned* count, unsigned target, int* error, bool withhold = false) {
   __syncthreads();
   if (threadIdx.x == 0) {
-    red_release_add(count, 1u);
+    if (!withhold) red_release_add(count, 1u);
     long long it = 0;
     while ((int)(ld_acquire(count) - target) < 0) {
+      if (*(volatile int*)error) break;
       if (++it > kBarrierSpin) {
         atomicExch(error, 1);
         break;
@@ -472,8 +476,10 @@ __global__ void __launch_bounds__(512) coarse_solve_coop(CoarseDev c, const T* _
   }
   float* dk = c.cd0;
   float* dn = c.cd1;
+  bool withhold = false;
+  if (c.testHold && blockIdx.x == 0 && threadIdx.x == 0) withhold = atomicExch(c.testHold, 0) != 0;
   for (int k = 0; k < cs.degree; ++k) {
-    grid_barrier(c.barrier, (unsigned)(k + 1) * gridDim.x, c.error);
+    grid_barrier(c.barrier, (unsigned)(k + 1) * gridDim.x, c.error, k == 0 && withhold);
     const bool last = k + 1 == cs.degree;
     for (int64_t v = g0; v < nVr; v += groups) {
       float y = 0.f;

@@ -64,6 +64,7 @@ struct CoarseDev {
   float theta;          // Chebyshev centre (start: d0 = D^{-1} r / theta)
   unsigned* barrier;    // [2] grid barrier of the one-launch coarse solve: count, generation
   int* error;           // set when a grid barrier wait ran out (the solve is then invalid)
+  int* testHold;        // test hook, one shot: block 0 withholds its first barrier arrival
 };
 
 // Coarse solver state: device view plus the polynomial schedule. Both coarse

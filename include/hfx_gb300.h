@@ -80,7 +80,15 @@ typedef struct {
   int coarse_guess;      /* HFX_PC_TWOLEVEL: start from the prolongated coarse solution */
   double coarse_rtol;    /* HFX_PC_TWOLEVEL: residual reduction the Chebyshev coarse solve targets */
   int coarse_mode;       /* HFX_PC_TWOLEVEL: HFX_COARSE_CHEBYSHEV or HFX_COARSE_LEARNED */
+  int coarse_degree;     /* HFX_PC_TWOLEVEL Chebyshev: fixed degree (1-64); 0 = the degree
+                            coarse_rtol asks for */
 } hfx_solve_opts;
+
+/* Test hook of the failure path (no counterpart in the reference): in the next two-level
+ * solve that runs the one-launch coarse solve, one block withholds its first grid-barrier
+ * arrival, so the others' bounded wait (about a second) runs out; the solve must then report
+ * info->fallback = 1 and finish with block-Jacobi CG. One shot. */
+int hfx_test_coarse_barrier(hfx_ctx* ctx);
 
 /* Coarse solve of HFX_PC_TWOLEVEL. LEARNED applies the polynomial trained by
  * hfx_coarse_train (Chebyshev until one has been accepted). */
@@ -343,6 +351,7 @@ int hfx_coarse_loss_grad(hfx_ctx* ctx, int degree, const double* theta, int samp
 #define HFX_K_OTHER 6
 #define HFX_K_RESIDUAL 7
 #define HFX_K_COARSE 8
+#define HFX_K_TENSOR 9   /* element contractions on the tensor cores (mixed assembly) */
 int hfx_profile_enable(hfx_ctx* ctx, int on);
 int hfx_kernel_time(hfx_ctx* ctx, int kernel, int* launches, double* ms);
 int hfx_mark(hfx_ctx* ctx, int slot);

@@ -963,7 +963,21 @@ static void local_system(const Problem& P, int iEl, Mat& A, std::vector<double>&
 }
 
 // Static condensation (HDGSolver.cpp:331-348), IMPLICIT mode.
+// Destination of one element's condensed blocks (column-major, as Problem's arrays).
+struct CondensedOut {
+  double *S, *S0, *U, *Q, *U0, *Q0;
+};
+
+static void condense_to(const Problem& P, int iEl, const Mat& A, const std::vector<double>& r, CondensedOut out);
+
 static void condense(Problem& P, int iEl, const Mat& A, const std::vector<double>& r) {
+  const size_t e = (size_t)iEl;
+  condense_to(P, iEl, A, r,
+              CondensedOut{&P.S[e * P.lenL * P.lenL], &P.S0[e * P.lenL], &P.U[e * P.lenU * P.lenL],
+                           &P.Q[e * P.lenQ * P.lenL], &P.U0[e * P.lenU], &P.Q0[e * P.lenQ]});
+}
+
+static void condense_to(const Problem& P, int iEl, const Mat& A, const std::vector<double>& r, CondensedOut out) {
   int lenU = P.lenU, lenQ = P.lenQ, lenL = P.lenL;
   int sU = 0, sQ = lenU, sL = lenU + lenQ;
   Mat Sqq = block(A, sQ, sQ, lenQ, lenQ);
@@ -1006,12 +1020,32 @@ static void condense(Problem& P, int iEl, const Mat& A, const std::vector<double
     gemm(-1.0, block(A, sL, sU, lenL, lenU), sol, 1.0, S0);
     gemm(-1.0, block(A, sL, sQ, lenL, lenQ), flux, 1.0, S0);
   }
-  std::copy(S.a.begin(), S.a.end(), P.S.begin() + (size_t)iEl * lenL * lenL);
-  std::copy(S0.a.begin(), S0.a.end(), P.S0.begin() + (size_t)iEl * lenL);
-  std::copy(Ul.a.begin(), Ul.a.end(), P.U.begin() + (size_t)iEl * lenU * lenL);
-  std::copy(Qm.a.begin(), Qm.a.end(), P.Q.begin() + (size_t)iEl * lenQ * lenL);
-  std::copy(U0.a.begin(), U0.a.end(), P.U0.begin() + (size_t)iEl * lenU);
-  std::copy(Q0.a.begin(), Q0.a.end(), P.Q0.begin() + (size_t)iEl * lenQ);
+  std::copy(S.a.begin(), S.a.end(), out.S);
+  std::copy(S0.a.begin(), S0.a.end(), out.S0);
+  if (out.U) std::copy(Ul.a.begin(), Ul.a.end(), out.U);
+  if (out.Q) std::copy(Qm.a.begin(), Qm.a.end(), out.Q);
+  if (out.U0) std::copy(U0.a.begin(), U0.a.end(), out.U0);
+  if (out.Q0) std::copy(Q0.a.begin(), Q0.a.end(), out.Q0);
+}
+
+// The Dirichlet Set of apply_dirichlet on one element's S, S0 (its boundary faces).
+static void dirichlet_element(const Problem& P, int c, double* S, double* S0) {
+  int F = P.re->nFaces, Nf = P.re->face->nNodes, lenL = P.lenL;
+  for (int loc = 0; loc < F; ++loc) {
+    int f = P.mf.cell2face[(size_t)c * F + loc];
+    if (!std::binary_search(P.mf.boundary.begin(), P.mf.boundary.end(), f)) continue;
+    if (P.mf.face2cell[2 * f] != c) continue;
+    for (int i = 0; i < Nf; ++i) {
+      int row = loc * Nf + i;
+      for (int j = 0; j < lenL; ++j) S[row + (size_t)j * lenL] = 0.0;
+      S0[row] = 0.0;
+    }
+    for (int i = 0; i < Nf; ++i) {
+      int row = loc * Nf + i;
+      S[row + (size_t)row * lenL] += 1.0;
+      S0[row] += P.dirichlet[(size_t)f * Nf + i];
+    }
+  }
 }
 
 static double now() {
@@ -1960,6 +1994,118 @@ int orc_problem_local_matrix(void* h, int iEl, double* A, double* rhs, int* face
     std::copy(r.begin(), r.end(), rhs);
     if (face2cellmap) std::copy(f2c.begin(), f2c.end(), face2cellmap);
   })
+}
+
+// Condensed blocks of a list of elements only (compact outputs [count][...], the
+// Dirichlet Set applied to their boundary faces as the full assembly applies it):
+// element-block parity on meshes too large to condense whole.
+int orc_problem_sample(void* h, int nthreads, int count, const int* ids, double* S, double* S0, double* U,
+                       double* Q, double* U0, double* Q0) {
+  ORC_TRY({
+    Problem* P = (Problem*)h;
+    const size_t lU = P->lenU, lQ = P->lenQ, lL = P->lenL;
+    for (int k = 0; k < count; ++k)
+      if (ids[k] < 0 || ids[k] >= P->nCells) throw std::runtime_error("element id out of range");
+    parallel_for(count, nthreads, [&](int k) {
+      Mat A;
+      std::vector<double> r;
+      local_system(*P, ids[k], A, r);
+      const size_t e = (size_t)k;
+      condense_to(*P, ids[k], A, r,
+                  CondensedOut{S + e * lL * lL, S0 + e * lL, U ? U + e * lU * lL : nullptr,
+                               Q ? Q + e * lQ * lL : nullptr, U0 ? U0 + e * lU : nullptr, Q0 ? Q0 + e * lQ : nullptr});
+      dirichlet_element(*P, ids[k], S + e * lL * lL, S0 + e * lL);
+    });
+  })
+}
+
+// The trace-system rows of a list of faces (all Nf rows of each, in face order),
+// built as build_csr builds them but from the condensed blocks of the cells that
+// touch those faces only. Outputs: rowlen[nsel*Nf], then col/val of the rows back
+// to back (cap entries at most) and rhs[nsel*Nf]. Returns the entry count.
+long orc_problem_face_rows(void* h, int nthreads, int nsel, const int* faceIds, int* rowlen, int* col, double* val,
+                           double* rhs, long cap) {
+  try {
+    Problem* P = (Problem*)h;
+    const int F = P->re->nFaces, Nf = P->re->face->nNodes, N = P->re->nNodes, lenL = P->lenL;
+    std::vector<int> cellsOf;  // cells touching the selected faces, ascending (build_csr's order)
+    for (int k = 0; k < nsel; ++k) {
+      int f = faceIds[k];
+      if (f < 0 || f >= P->mf.nFaces) throw std::runtime_error("face id out of range");
+      for (int sd = 0; sd < 2; ++sd)
+        if (P->mf.face2cell[2 * f + sd] >= 0) cellsOf.push_back(P->mf.face2cell[2 * f + sd]);
+    }
+    std::sort(cellsOf.begin(), cellsOf.end());
+    cellsOf.erase(std::unique(cellsOf.begin(), cellsOf.end()), cellsOf.end());
+    const int nc = (int)cellsOf.size();
+    std::vector<double> S((size_t)nc * lenL * lenL), S0((size_t)nc * lenL);
+    parallel_for(nc, nthreads, [&](int k) {
+      Mat A;
+      std::vector<double> r;
+      local_system(*P, cellsOf[k], A, r);
+      condense_to(*P, cellsOf[k], A, r,
+                  CondensedOut{&S[(size_t)k * lenL * lenL], &S0[(size_t)k * lenL], nullptr, nullptr, nullptr, nullptr});
+      dirichlet_element(*P, cellsOf[k], &S[(size_t)k * lenL * lenL], &S0[(size_t)k * lenL]);
+    });
+    // row layout: the sorted set of faces of the cells touching f
+    std::vector<std::vector<int>> cols(nsel);
+    long total = 0;
+    std::map<int, int> selIndex;
+    for (int k = 0; k < nsel; ++k) {
+      int f = faceIds[k];
+      if (!selIndex.emplace(f, k).second) throw std::runtime_error("face listed twice");
+      std::set<int> nb;
+      for (int sd = 0; sd < 2; ++sd) {
+        int c = P->mf.face2cell[2 * f + sd];
+        if (c < 0) continue;
+        for (int i = 0; i < F; ++i) nb.insert(P->mf.cell2face[(size_t)c * F + i]);
+      }
+      for (int g : nb)
+        for (int b = 0; b < Nf; ++b) cols[k].push_back(g * Nf + b);
+      total += (long)cols[k].size() * Nf;
+    }
+    if (total > cap) return -total;
+    std::vector<long> start(nsel + 1, 0);
+    for (int k = 0; k < nsel; ++k) start[k + 1] = start[k] + (long)cols[k].size() * Nf;
+    for (int k = 0; k < nsel; ++k)
+      for (int a = 0; a < Nf; ++a) {
+        rowlen[k * Nf + a] = (int)cols[k].size();
+        std::copy(cols[k].begin(), cols[k].end(), col + start[k] + (long)a * cols[k].size());
+        std::fill(val + start[k] + (long)a * cols[k].size(), val + start[k] + (long)(a + 1) * cols[k].size(), 0.0);
+        rhs[k * Nf + a] = 0.0;
+      }
+    std::vector<int> rc(lenL);
+    for (int kc = 0; kc < nc; ++kc) {
+      int c = cellsOf[kc];
+      const int* cell = &P->cells[(size_t)c * N];
+      for (int i = 0; i < F; ++i) {
+        int f = P->mf.cell2face[(size_t)c * F + i];
+        const int* face = &P->mf.faces[(size_t)f * Nf];
+        for (int j = 0; j < Nf; ++j) {
+          int node = cell[P->re->faceNodes[i][j]], pos = 0;
+          while (face[pos] != node) ++pos;
+          rc[i * Nf + j] = f * Nf + pos;
+        }
+      }
+      const double* Se = &S[(size_t)kc * lenL * lenL];
+      for (int i = 0; i < lenL; ++i) {
+        auto it = selIndex.find(rc[i] / Nf);
+        if (it == selIndex.end()) continue;
+        int k = it->second, a = rc[i] % Nf;
+        const std::vector<int>& cb = cols[k];
+        long base = start[k] + (long)a * cb.size();
+        for (int j = 0; j < lenL; ++j) {
+          int pos = (int)(std::lower_bound(cb.begin(), cb.end(), rc[j]) - cb.begin());
+          val[base + pos] += Se[i + (size_t)j * lenL];
+        }
+        rhs[k * Nf + a] += S0[(size_t)kc * lenL + i];
+      }
+    }
+    return total;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return -1;
+  }
 }
 
 int orc_problem_condensed(void* h, double* S, double* S0, double* U, double* Q, double* U0, double* Q0) {

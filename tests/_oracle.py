@@ -46,6 +46,9 @@ def lib():
         L.orc_problem_assemble.argtypes = [vp, ip]
         L.orc_problem_local_matrix.argtypes = [vp, ip, vp, vp, vp]
         L.orc_problem_condensed.argtypes = [vp] * 7
+        L.orc_problem_sample.argtypes = [vp, ip, ip, vp] + [vp] * 6
+        L.orc_problem_face_rows.restype = ctypes.c_long
+        L.orc_problem_face_rows.argtypes = [vp, ip, ip, vp, vp, vp, vp, vp, ctypes.c_long]
         L.orc_problem_nnz.restype = ctypes.c_long
         L.orc_problem_nnz.argtypes = [vp]
         L.orc_problem_csr.argtypes = [vp] * 5
@@ -181,6 +184,33 @@ class Problem:
         Q0 = np.zeros((nC, Q))
         lib().orc_problem_condensed(self.h, _ptr(S), _ptr(S0), _ptr(Um), _ptr(Qm), _ptr(U0), _ptr(Q0))
         return dict(S=S, S0=S0, U=Um, Q=Qm, U0=U0, Q0=Q0)
+
+    def sample(self, ids, nthreads=1):
+        """Condensed blocks (Dirichlet Set applied) of the listed elements only."""
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        n, U, Q, L_ = len(ids), self.lenU, self.lenQ, self.lenL
+        out = dict(S=np.zeros((n, L_ * L_)), S0=np.zeros((n, L_)), U=np.zeros((n, U * L_)),
+                   Q=np.zeros((n, Q * L_)), U0=np.zeros((n, U)), Q0=np.zeros((n, Q)))
+        _check(lib().orc_problem_sample(self.h, nthreads, n, _ptr(ids), *[_ptr(out[k]) for k in
+                                                                           ("S", "S0", "U", "Q", "U0", "Q0")]))
+        return out
+
+    def face_rows(self, faces, nthreads=1):
+        """The trace-system rows (all nodes) of the listed faces, from their cells only:
+        (rowlen, col, val, rhs) with the rows back to back in face, node order."""
+        faces = np.ascontiguousarray(faces, dtype=np.int32)
+        Nf = self.re.nNodesFace
+        nr = len(faces) * Nf
+        cap = nr * (2 * self.re.nFaces) * Nf
+        rowlen = np.zeros(nr, np.int32)
+        col = np.zeros(cap, np.int32)
+        val = np.zeros(cap)
+        rhs = np.zeros(nr)
+        n = lib().orc_problem_face_rows(self.h, nthreads, len(faces), _ptr(faces), _ptr(rowlen), _ptr(col),
+                                        _ptr(val), _ptr(rhs), cap)
+        if n < 0:
+            raise RuntimeError("oracle face_rows: %s" % lib().orc_last_error().decode())
+        return rowlen, col[:n], val[:n], rhs
 
     def csr(self):
         nnz = lib().orc_problem_nnz(self.h)

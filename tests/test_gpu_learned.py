@@ -70,9 +70,12 @@ def test_learned_twolevel_solve_matches_direct_and_beats_block_jacobi(hfx_lib):
         assert np.linalg.norm(trace - x_ref) / np.linalg.norm(x_ref) < 1e-8
         _, bj = ctx.solve(precision=prec, rtol=1e-13, precond=capi.PC_BLOCK_JACOBI)
         assert tl.iterations < 0.7 * bj.iterations, (tl.iterations, bj.iterations)
-        # the default Chebyshev coarse solve needs a higher degree for the same outer work
+        # what the training gains: Chebyshev of the same degree needs more outer iterations
+        _, same = ctx.solve(precision=prec, rtol=1e-13, precond=capi.PC_TWOLEVEL, coarse_degree=4)
+        assert same.coarse_degree == 4 and same.coarse_learned == 0
+        assert tl.iterations < same.iterations, (tl.iterations, same.iterations)
+        # and the adaptive Chebyshev coarse solve takes a higher degree
         _, ch = ctx.solve(precision=prec, rtol=1e-13, precond=capi.PC_TWOLEVEL)
-        assert tl.iterations <= 1.15 * ch.iterations, (tl.iterations, ch.iterations)
         assert ch.coarse_degree > tl.coarse_degree
 
 

@@ -126,3 +126,26 @@ def test_twolevel_falls_back_to_block_jacobi(hfx_lib):
     rc = ctx.L.hfx_solve(ctx.h, ctypes.byref(o), None, ctypes.byref(info))
     assert rc == capi.HFX_ERR_NOT_CONVERGED
     assert info.fallback == 1
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_coarse_barrier_wait_runs_out_and_falls_back(hfx_lib, precision):
+    """The one-launch coarse solve's grid barrier waits a bounded time: with one block's
+    arrival withheld (test hook) the wait runs out (about a second), the kernel sets its
+    error flag and returns, the host discards the two-level iterates and block-Jacobi CG
+    finishes the solve (info.fallback = 1) with the right answer; the context stays
+    usable and later solves run the launch-per-step coarse solve."""
+    from hyperfox_gb300 import capi
+    P, ctx, _ = build_pair(hfx_lib, 3, 4, 2, tau2=False, kappa="cell")
+    P.assemble()
+    ctx.assemble()
+    x_ref = P.solve_direct()
+    trace, info = ctx.solve(precision=precision, precond=capi.PC_TWOLEVEL, rtol=1e-12)
+    assert info.status == 0 and info.fallback == 0
+    ctx._chk(ctx.L.hfx_test_coarse_barrier(ctx.h), "test_coarse_barrier")
+    trace, info = ctx.solve(precision=precision, precond=capi.PC_TWOLEVEL, rtol=1e-12)
+    assert info.status == 0 and info.fallback == 1
+    assert np.linalg.norm(trace - x_ref) / np.linalg.norm(x_ref) < 1e-8
+    trace, info = ctx.solve(precision=precision, precond=capi.PC_TWOLEVEL, rtol=1e-12)
+    assert info.status == 0 and info.fallback == 0
+    assert np.linalg.norm(trace - x_ref) / np.linalg.norm(x_ref) < 1e-8

@@ -133,3 +133,33 @@ def test_gmres_matches_direct():
     assert it > 0
     xd = P.solve_direct()
     assert np.linalg.norm(x - xd) / np.linalg.norm(xd) < 1e-9
+
+
+@pytest.mark.parametrize("dim,n,order", [(2, 4, 2), (3, 2, 3)])
+def test_sampled_blocks_and_face_rows_equal_full_assembly(dim, n, order):
+    """The oracle's element sample and face rows (parity on meshes too large to
+    condense whole) equal the full assembly's blocks and CSR rows."""
+    from helpers import manufactured, mesh
+    re, coords, cells = mesh(dim, n, order, jitter=0.1, seed=1)
+    P = O.Problem(dim, order, coords, cells)
+    P.set_fields(np.ones(P.ndofs), src_mode=2, dirichlet=manufactured(coords, P.faces).ravel())
+    P.assemble()
+    full = P.condensed()
+    ids = np.array([0, 3, 5, P.nCells - 1])
+    smp = P.sample(ids)
+    for k in smp:
+        assert np.array_equal(smp[k], full[k][ids]), k
+    rowptr, col, val, rhs = P.csr()
+    faces = np.unique([0, 7, P.nFaces - 1, int(P.boundary[0]), int(P.boundary[-1])])
+    rl, c2, v2, r2 = P.face_rows(faces)
+    Nf, pos = P.re.nNodesFace, 0
+    for k, f in enumerate(faces):
+        for a in range(Nf):
+            r, m = f * Nf + a, rl[k * Nf + a]
+            assert m == rowptr[r + 1] - rowptr[r]
+            assert np.array_equal(c2[pos:pos + m], col[rowptr[r]:rowptr[r + 1]])
+            assert np.array_equal(v2[pos:pos + m], val[rowptr[r]:rowptr[r + 1]])
+            assert r2[k * Nf + a] == rhs[r]
+            pos += m
+    with pytest.raises(RuntimeError):
+        P.face_rows(np.array([faces[0], faces[0]]))
