@@ -272,6 +272,8 @@ def run_ours(args, world, rank, local):
         ctx._chk(L.hfx_solve(ctx.h, capi.ctypes.byref(opts), capi._p(trace_h), capi.ctypes.byref(info)), "solve")
         ctx._chk(L.hfx_recover(ctx.h, capi._p(sol_h), capi._p(flux_h)), "recover")
 
+    if args.assembly_only:
+        return run_assembly_only(args, world, ctx, asm_prec, cfg), ctx
     # accuracy reference: plain FP64 CG to 1e-13 (untimed)
     ctx.assemble()
     # (a diffusion coefficient varying inside the cells makes the system non-symmetric: GMRES(100) to 1e-11)
@@ -518,6 +520,39 @@ def run_ours(args, world, rank, local):
     if plain:
         res["speedup_vs_plain_fp64"] = plain["time_to_solve_s"] / step_s
     return res, ctx
+
+
+def run_assembly_only(args, world, ctx, asm_prec, cfg):
+    """Element assembly + condensation + scatter alone (hfx_assemble_ex), K timed calls:
+    elements/s of the assembly and the per-kernel device times."""
+    from hyperfox_gb300 import capi
+    L = ctx.L
+    for _ in range(args.warmup):
+        ctx._chk(L.hfx_assemble_ex(ctx.h, asm_prec), "assemble")
+    barrier(world)
+    ctx._chk(L.hfx_synchronize(ctx.h), "sync")
+    ctx._chk(L.hfx_profile_enable(ctx.h, 1), "profile")
+    ctx._chk(L.hfx_mark(ctx.h, 0), "mark")
+    for _ in range(args.steps):
+        ctx._chk(L.hfx_assemble_ex(ctx.h, asm_prec), "assemble")
+    ctx._chk(L.hfx_mark(ctx.h, 1), "mark")
+    ms = capi.ctypes.c_double()
+    ctx._chk(L.hfx_elapsed_ms(ctx.h, 0, 1, capi.ctypes.byref(ms)), "elapsed")
+    dev_ms = barrier_max(world, ms.value)
+    kt = {}
+    for name, kid in (("local", 0), ("scatter", 1), ("residual", 7), ("tensor", 9)):
+        n_l, t_l = capi.ctypes.c_int(), capi.ctypes.c_double()
+        L.hfx_kernel_time(ctx.h, kid, capi.ctypes.byref(n_l), capi.ctypes.byref(t_l))
+        kt[name] = dict(launches=n_l.value, total_ms=round(t_l.value, 3))
+    ctx._chk(L.hfx_profile_enable(ctx.h, 0), "profile")
+    step_s = dev_ms / 1e3 / args.steps
+    return {"metric": "element assembly + condensation + scatter; elements/s", "value": ctx.nCells / step_s,
+            "unit": "elements/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if asm_prec == capi.PREC_FP64 else "tf32x3+f32+f64",
+            "data": "synthetic", "config": {"workload": cfg["desc"], "elements": ctx.nCells,
+                                            "precision": args.precision, "assembly_path": args.assembly_path},
+            "tensor_cores": ctx.mixed_assembly_info() if asm_prec != capi.PREC_FP64 else 0, "kernel_ms": kt}
 
 
 def burgers_initial(coords, cells, seed=0):
@@ -984,6 +1019,8 @@ def main():
     ap.add_argument("--assembly-path", type=int, default=0, choices=[0, 1],
                     help="element kernel choice (hfx_set_assembly_path): 0 automatic (affine kernel, or the "
                          "tensor-core contractions in the mixed assembly), 1 quadrature on the CUDA cores")
+    ap.add_argument("--assembly-only", action="store_true",
+                    help="time the element assembly (+ condensation + scatter) alone")
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

@@ -16,7 +16,7 @@ BUILD = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libhfx_gb300.so")
 
-SOURCES = ["hdg_local.cu", "hdg_burgers.cu", "hdg_trace.cu", "krylov.cu", "trace_gmres.cu", "la_gmres.cu", "noalloc_solve.cu", "hdg_residual.cu", "mixed_kernels.cu", "coarse.cu", "hdg_affine.cu", "tc_assembly.cu", "rk.cu", "capi.cpp", "refel.cpp", "mesh.cpp", "mesh_io.cpp", "h5io.cpp"]
+SOURCES = ["hdg_local.cu", "hdg_burgers.cu", "hdg_trace.cu", "krylov.cu", "trace_gmres.cu", "la_gmres.cu", "noalloc_solve.cu", "hdg_residual.cu", "mixed_kernels.cu", "coarse.cu", "hdg_affine.cu", "tc_assembly.cu", "cg_operators.cu", "rk.cu", "capi.cpp", "refel.cpp", "mesh.cpp", "mesh_io.cpp", "h5io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O3", "-I", CSRC, "-I", os.path.join(ROOT, "include")]
 

@@ -28,6 +28,7 @@ PC_NONE, PC_JACOBI, PC_BLOCK_JACOBI, PC_TWOLEVEL = 0, 1, 2, 3
 COARSE_CHEBYSHEV, COARSE_LEARNED = 0, 1
 IMPLICIT, WEXPLICIT, SEXPLICIT = 0, 1, 2
 PREC_FP64, PREC_MIXED = 0, 1
+OP_MASS, OP_DIFFUSION, OP_CONVECTION = 1, 2, 4
 SRC_NONE, SRC_VALUES, SRC_SINPROD = 0, 1, 2
 
 # Every symbol include/hfx_gb300.h declares.
@@ -40,7 +41,7 @@ EXPORTED = [
     "hfx_rk_butcher", "hfx_rk_set", "hfx_rk_set_type", "hfx_rk_begin_step", "hfx_rk_compute_stage",
     "hfx_rk_compute_solution", "hfx_set_trace", "hfx_get_state",
     "hfx_set_tau", "hfx_set_kappa", "hfx_set_source", "hfx_set_dirichlet", "hfx_set_time_scheme",
-    "hfx_ip_coords", "hfx_assemble", "hfx_assemble_ex", "hfx_set_solver_type", "hfx_set_state", "hfx_set_assembly_path", "hfx_assembly_info", "hfx_get_condensed", "hfx_get_csr", "hfx_get_condensed_sample", "hfx_get_csr_rows", "hfx_mixed_assembly_info", "hfx_get_tc_blocks", "hfx_test_coarse_barrier",
+    "hfx_ip_coords", "hfx_assemble", "hfx_assemble_ex", "hfx_set_solver_type", "hfx_set_state", "hfx_set_assembly_path", "hfx_assembly_info", "hfx_get_condensed", "hfx_get_csr", "hfx_get_condensed_sample", "hfx_get_csr_rows", "hfx_mixed_assembly_info", "hfx_get_tc_blocks", "hfx_test_coarse_barrier", "hfx_cg_operators",
     "hfx_solve_opts_default", "hfx_solve", "hfx_recover", "hfx_coarse_operator", "hfx_coarse_train",
     "hfx_coarse_loss_grad",
     "hfx_la_create", "hfx_la_destroy", "hfx_la_allocate", "hfx_la_set_values", "hfx_la_set_rhs",
@@ -134,6 +135,7 @@ def load(path=LIB_PATH):
         "hfx_get_condensed_sample": ([vp, ip, vp] + [vp] * 6, ip),
         "hfx_mixed_assembly_info": ([vp, vp], ip),
         "hfx_test_coarse_barrier": ([vp], ip),
+        "hfx_cg_operators": ([vp, ip, ip, vp, ip, vp], ip),
         "hfx_get_tc_blocks": ([vp, ip, vp, vp, vp], ip),
         "hfx_get_csr_rows": ([vp, ip, vp, vp, vp, vp, vp, ctypes.c_int64], ip),
         "hfx_solve_opts_default": ([ctypes.POINTER(SolveOpts)], None),
@@ -490,6 +492,15 @@ class Context:
                   "get_condensed")
         return out
 
+    def cg_operators(self, which=7, precision=0, velocity=None, vel_layout=1):
+        """CG element operators [nCells][3][N*N] (column-major per element): Mass, Diffusion
+        (this context's diffusion field), Convection (nodal velocity)."""
+        N = self.re["nNodes"]
+        out = np.zeros((self.nCells, 3, N * N))
+        v = None if velocity is None else np.ascontiguousarray(velocity, np.float64)
+        self._chk(self.L.hfx_cg_operators(self.h, which, precision, _p(v), vel_layout, _p(out)), "cg_operators")
+        return out
+
     def mixed_assembly_info(self):
         """1 when the last mixed assembly contracted the element blocks on the tensor cores."""
         v = ctypes.c_int()
@@ -774,6 +785,15 @@ class Burgers:
                    U0=np.zeros((E, U)), Q0=np.zeros((E, Q)))
         self.c._chk(self.c.L.hfx_burgers_get_condensed(self.c.h, *[_p(out[k]) for k in ("S", "S0", "U", "Q", "U0", "Q0")]),
                     "burgers_get_condensed")
+        return out
+
+    def cg_operators(self, which=7, precision=0, velocity=None, vel_layout=1):
+        """CG element operators [nCells][3][N*N] (column-major per element): Mass, Diffusion
+        (this context's diffusion field), Convection (nodal velocity)."""
+        N = self.re["nNodes"]
+        out = np.zeros((self.nCells, 3, N * N))
+        v = None if velocity is None else np.ascontiguousarray(velocity, np.float64)
+        self._chk(self.L.hfx_cg_operators(self.h, which, precision, _p(v), vel_layout, _p(out)), "cg_operators")
         return out
 
     def mixed_assembly_info(self):

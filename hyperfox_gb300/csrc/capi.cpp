@@ -17,6 +17,7 @@
 #include "hfx_device.h"
 #include "hdg_mixed.h"
 #include "hfx_host.h"
+#include "cg_operators.h"
 #include "krylov.h"
 #include "la_gmres.h"
 #include "tc_assembly.h"
@@ -117,6 +118,7 @@ struct hfx_ctx {
   std::vector<uint8_t> perm;
   DevMem meshMem;
   double* d_tab = nullptr;
+  float* d_tab32 = nullptr;
   int* d_itab = nullptr;
   double* d_phi = nullptr;
   double* d_coords = nullptr;
@@ -185,6 +187,11 @@ struct hfx_ctx {
   float* d_tctab = nullptr;
   float* d_tcb = nullptr;
   bool lastTensor = false;
+  // CG element operators (hfx_cg_operators): their tensor-core table, output and velocity buffers
+  DevMem cgMem;
+  float* d_cgtab = nullptr;
+  double *d_cgout = nullptr, *d_cgvel = nullptr;
+  size_t cgVelCap = 0;
   // two-level preconditioner: vertex coarse space (built on first use)
   std::vector<int> cellVerts;  // [nCells][dim+1]
   CoarseHost coarseHost;
@@ -260,6 +267,10 @@ void free_outputs(hfx_ctx* c) {
   c->d_S32 = c->d_S032 = c->d_U32 = c->d_Q32 = c->d_U032 = c->d_Q032 = c->d_dl32 = nullptr;
   c->d_tctab = c->d_tcb = nullptr;
   c->lastTensor = false;
+  c->cgMem.release();
+  c->d_cgtab = nullptr;
+  c->d_cgout = c->d_cgvel = nullptr;
+  c->cgVelCap = 0;
   c->d_ru = c->d_rq = c->d_rl = c->d_rtrace = c->d_part = nullptr;
   c->mixedMode = false;
   c->d_status = nullptr;
@@ -339,6 +350,7 @@ int hfx_ctx_destroy(hfx_ctx* c) {
   c->burgers.release();
   c->wsMem.release();
   c->mixMem.release();
+  c->cgMem.release();
   c->outMem.release();
   c->tau.release();
   c->kappa.release();
@@ -452,7 +464,11 @@ int hfx_mesh_upload(hfx_ctx* c, int dim, int order, int nNodes, const double* co
   itab.insert(itab.end(), c->re.faceOpposite.begin(), c->re.faceOpposite.end());
   std::vector<uint8_t> isBnd(c->topo.nFaces, 0);
   for (int f : c->topo.boundary) isBnd[f] = 1;
+  // whole 16-byte units for the element kernel's bulk copy (FP64 and FP32 copies)
+  tab.resize((tab.size() + 3) / 4 * 4, 0.0);
+  std::vector<float> tab32(tab.begin(), tab.end());
   HFX_CUDA(c, upload(m, &c->d_tab, tab.data(), tab.size(), s));
+  HFX_CUDA(c, upload(m, &c->d_tab32, tab32.data(), tab32.size(), s));
   HFX_CUDA(c, upload(m, &c->d_itab, itab.data(), itab.size(), s));
   HFX_CUDA(c, upload(m, &c->d_phi, c->re.phi.data(), c->re.phi.size(), s));
   HFX_CUDA(c, upload(m, &c->d_coords, coords, (size_t)nNodes * dim, s));
@@ -725,6 +741,7 @@ static int assemble_fp64(hfx_ctx* c) {
   p.dt = c->dt;
   p.uOld = c->uold.p;
   p.tab = c->d_tab;
+  p.tab32 = c->d_tab32;
   p.itab = c->d_itab;
   p.S = c->d_S;
   p.S0 = c->d_S0;
@@ -795,6 +812,7 @@ static int assemble_fp64(hfx_ctx* c) {
   int status = 0;
   HFX_CUDA(c, cudaMemcpyAsync(&status, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
   HFX_CUDA(c, cudaStreamSynchronize(s));
+  if (status == 2) return set_err(c, HFX_ERR_CUDA, "assemble: a bulk-copy or tensor-core wait ran out");
   if (status != 0) return set_err(c, HFX_ERR_SINGULAR, "assemble: singular element block in condensation");
   c->assembled = true;
   c->solved = false;
@@ -825,6 +843,7 @@ static LocalParams local_params(hfx_ctx* c) {
   p.dt = c->dt;
   p.uOld = c->uold.p;
   p.tab = c->d_tab;
+  p.tab32 = c->d_tab32;
   p.itab = c->d_itab;
   p.status = c->d_status;
   return p;
@@ -997,6 +1016,7 @@ static int assemble_mixed(hfx_ctx* c) {
   HFX_CUDA(c, cudaMemcpyAsync(&status, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
   HFX_CUDA(c, cudaStreamSynchronize(s));
   if (status == 2) return set_err(c, HFX_ERR_CUDA, "assemble: a tensor-core wait ran out");
+  if (status == 2) return set_err(c, HFX_ERR_CUDA, "assemble: a bulk-copy or tensor-core wait ran out");
   if (status != 0) return set_err(c, HFX_ERR_SINGULAR, "assemble: singular element block in condensation");
   c->assembled = true;
   c->solved = false;
@@ -1275,6 +1295,73 @@ int hfx_rk_compute_solution(hfx_ctx* c) {
 int hfx_assembly_info(hfx_ctx* c, int* affine) {
   if (!c || !affine) return HFX_ERR_ARG;
   *affine = c->lastAffine ? 1 : 0;
+  return HFX_OK;
+}
+
+int hfx_cg_operators(hfx_ctx* c, int which, int precision, const double* velocity, int velLayout, double* out) {
+  if (!c || !out || which <= 0 || which > 7) return HFX_ERR_ARG;
+  if (!c->haveMesh) return set_err(c, HFX_ERR_STATE, "cg_operators: upload a mesh first");
+  if (precision != HFX_PREC_FP64 && precision != HFX_PREC_MIXED)
+    return set_err(c, HFX_ERR_ARG, "cg_operators: precision is HFX_PREC_FP64 or HFX_PREC_MIXED");
+  if ((which & HFX_OP_CONVECTION) && (!velocity || (velLayout != 0 && velLayout != 1)))
+    return set_err(c, HFX_ERR_ARG, "cg_operators: convection needs a velocity (layout 0 or 1)");
+  if (!local_condense_supported(c->dim, c->order))
+    return set_err(c, HFX_ERR_UNSUPPORTED, "cg_operators: order not supported");
+  cudaSetDevice(c->device);
+  cudaStream_t s = c->stream;
+  const int N = c->re.nNodes;
+  const size_t outN = (size_t)c->nCells * 3 * N * N;
+  if (!c->d_cgout) HFX_CUDA(c, dalloc(c->cgMem, &c->d_cgout, outN));
+  const double* dvel = nullptr;
+  if (which & HFX_OP_CONVECTION) {
+    const size_t nv = (velLayout == 0 ? (size_t)c->nNodes : (size_t)c->nCells * N) * c->dim;
+    if (nv > c->cgVelCap) {
+      HFX_CUDA(c, dalloc(c->cgMem, &c->d_cgvel, nv));
+      c->cgVelCap = nv;
+    }
+    HFX_CUDA(c, cudaMemcpyAsync(c->d_cgvel, velocity, sizeof(double) * nv, cudaMemcpyHostToDevice, s));
+    dvel = c->d_cgvel;
+  }
+  CgOpParams p{};
+  p.nCells = c->nCells;
+  p.coords = c->d_coords;
+  p.cells = c->d_cells;
+  p.kappa = c->kappa.p;
+  p.kc = c->kc;
+  p.kappaLayout = c->kLayout;
+  p.vel = dvel;
+  p.velLayout = velLayout;
+  p.tab = c->d_tab;
+  p.which = which;
+  p.out = c->d_cgout;
+  p.status = c->d_status;
+  if (precision == HFX_PREC_MIXED) {
+    if (!c->d_cgtab) {
+      std::vector<double> tab;
+      tab.insert(tab.end(), c->re.phi.begin(), c->re.phi.end());
+      tab.insert(tab.end(), c->re.dphi.begin(), c->re.dphi.end());
+      tab.insert(tab.end(), c->re.ipW.begin(), c->re.ipW.end());
+      std::vector<float> t = tc_cg_table(c->dim, c->order, tab.data());
+      HFX_CUDA(c, upload(c->cgMem, &c->d_cgtab, t.data(), t.size(), s));
+    }
+    if (!c->d_status) HFX_CUDA(c, dalloc(c->outMem, &c->d_status, 1));
+    p.status = c->d_status;
+    p.tctab = c->d_cgtab;
+    HFX_CUDA(c, cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
+    c->timer.begin(K_TENSOR, s);
+    HFX_CUDA(c, launch_cg_operators_tc(c->dim, c->order, p, s));
+    c->timer.end(K_TENSOR, s);
+  } else {
+    c->timer.begin(K_LOCAL, s);
+    HFX_CUDA(c, launch_cg_operators_f64(c->dim, c->order, p, s));
+    c->timer.end(K_LOCAL, s);
+  }
+  HFX_CUDA(c, cudaMemcpyAsync(out, c->d_cgout, sizeof(double) * outN, cudaMemcpyDeviceToHost, s));
+  int status = 0;
+  if (precision == HFX_PREC_MIXED)
+    HFX_CUDA(c, cudaMemcpyAsync(&status, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  HFX_CUDA(c, cudaStreamSynchronize(s));
+  if (status == 2) return set_err(c, HFX_ERR_CUDA, "cg_operators: a tensor-core wait ran out");
   return HFX_OK;
 }
 

@@ -40,7 +40,7 @@ struct Layout {
   static constexpr int T_FPHI = T_W + NI;
   static constexpr int T_FDPHI = T_FPHI + NIF * NF;
   static constexpr int T_FW = T_FDPHI + NIF * NF * DM;
-  static constexpr int TAB = (T_FW + NIF + 1) & ~1;
+  static constexpr int TAB = (T_FW + NIF + 3) & ~3;  // whole 16-byte units for the bulk copy
   // per-group region (doubles)
   static constexpr int X = 0;                       // N*D coordinates
   static constexpr int KAPN = X + N * D;            // N*D*D nodal kappa tensor
@@ -86,16 +86,42 @@ __global__ void __launch_bounds__(TPE * EPC)
   __shared__ int sInt[EPC * L::IGROUP];
 
   const int nthr = TPE * EPC;
-  // ---- stage tables once per CTA
+  // ---- stage tables once per CTA: one bulk copy (the table in the kernel's precision,
+  // padded to whole 16-byte units), completion counted in bytes on an mbarrier
   {
-    constexpr int nTab = L::T_FW + NIF;
-    for (int i = threadIdx.x; i < nTab; i += nthr) smem[i] = (T)p.tab[i];
+    __shared__ __align__(8) uint64_t tabBar;
+    __shared__ int sTabFail;
+    const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&tabBar);
+    if (threadIdx.x == 0) sTabFail = 0;
+    const uint32_t bytes = (uint32_t)(((L::T_FW + NIF) * sizeof(T) + 15) / 16 * 16);
+    const void* src = sizeof(T) == 8 ? (const void*)p.tab : (const void*)p.tab32;
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                       (uint32_t)__cvta_generic_to_shared(smem)),
+                   "l"(src), "r"(bytes), "r"(bar)
+                   : "memory");
+    }
     for (int i = threadIdx.x; i < F * NF; i += nthr) sFaceNodes[i] = p.itab[i];
     for (int i = threadIdx.x; i < F; i += nthr) sOpp[i] = p.itab[F * NF + i];
     for (int i = threadIdx.x; i < F * N; i += nthr) sPos[i] = -1;
-    __syncthreads();
+    __syncthreads();  // also orders the barrier's initialisation before every thread's wait
     for (int i = threadIdx.x; i < F * NF; i += nthr) sPos[(i / NF) * N + sFaceNodes[i]] = i % NF;
+    // bounded wait for the table (phase 0); a wait that runs out reports status 2
+    uint32_t done = 0;
+    for (uint32_t it = 0; it < (1u << 26) && !done; ++it)
+      asm volatile("{ .reg .pred q; mbarrier.try_wait.parity.shared::cta.b64 q, [%1], 0; selp.u32 %0, 1, 0, q; }"
+                   : "=r"(done)
+                   : "r"(bar)
+                   : "memory");
+    if (!done) {
+      atomicCAS(p.status, 0, 2);
+      sTabFail = 1;
+    }
     __syncthreads();
+    if (sTabFail) return;  // the same value for every thread of the CTA
   }
   const T* phi = smem + L::T_PHI;
   const T* dphi = smem + L::T_DPHI;

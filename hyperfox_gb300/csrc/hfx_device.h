@@ -47,7 +47,8 @@ struct LocalParams {
   const double* dirichlet;     // [nFaces][NF]
   double dt;
   const double* uOld;          // [nCells][N]
-  const double* tab;           // phi, dphi, w, fphi, fdphi, fw
+  const double* tab;           // phi, dphi, w, fphi, fdphi, fw (padded to whole 16-byte units)
+  const float* tab32;          // the same table in FP32 (the FP32 element kernel's bulk copy)
   const int* itab;             // faceNodes[F*NF], faceOpposite[F]
   void *S, *S0, *U, *Q, *U0, *Q0;  // double (fp32 == 0) or float (fp32 == 1)
   int* status;                 // first error: 1 = singular block

@@ -39,6 +39,7 @@
 #include <cstring>
 #include <vector>
 
+#include "cg_operators.h"
 #include "hfx_device.h"
 #include "tc_assembly.h"
 
@@ -409,8 +410,11 @@ __global__ void __launch_bounds__(kThreads) tc_element_blocks(TcBlockParams p) {
     // ------------------------------- volume coefficient rows -> A (hi, lo)
     {
       constexpr int KC = T::NIP / 4;
-      for (int idx = tid; idx < T::TV * 128 * T::NIP; idx += kThreads) {
-        const int r = idx / T::NIP, q = idx % T::NIP;
+      // walk the tiles in shared-memory order (core matrices of 8 rows x 4 values), so that
+      // consecutive threads store to consecutive words
+      for (int o = tid; o < T::TV * 128 * T::NIP; o += kThreads) {
+        const int t = o / (128 * T::NIP), oo = o % (128 * T::NIP);
+        const int r = t * 128 + (oo / (KC * 32)) * 8 + (oo / 4) % 8, q = ((oo / 32) % KC) * 4 + (oo % 4);
         float v = 0.f;
         if (r < T::RV && q < NI) {
           if (r < 2 * D * N) {
@@ -422,7 +426,6 @@ __global__ void __launch_bounds__(kThreads) tc_element_blocks(TcBlockParams p) {
           }
         }
         const float hi = tf32_hi(v);
-        const int o = (r >> 7) * 128 * T::NIP + cm_index(r & 127, q, KC);
         aHi[o] = hi;
         aLo[o] = tf32_hi(v - hi);
       }
@@ -453,19 +456,21 @@ __global__ void __launch_bounds__(kThreads) tc_element_blocks(TcBlockParams p) {
       float v[32];
       tmem_ld<32>(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(t * T::NVB), v);
       const int r = 32 * warp + lane;
+      constexpr int SV = N | 1;  // odd row stride: the 32 rows of a warp hit 32 banks
 #pragma unroll
-      for (int j = 0; j < N; ++j) aHi[r * N + j] = v[j];
+      for (int j = 0; j < N; ++j) aHi[r * SV + j] = v[j];
       __syncthreads();
       const int rows = (T::RV - t * 128) < 128 ? (T::RV - t * 128) : 128;
       float* dst = out + (int64_t)t * 128 * N;
-      for (int i = tid; i < rows * N; i += kThreads) dst[i] = aHi[i];
+      for (int i = tid; i < rows * N; i += kThreads) dst[i] = aHi[(i / N) * SV + i % N];
       __syncthreads();
     }
     // ------------------------------------ face coefficient rows -> A (hi, lo)
     {
       constexpr int KC = T::NIFP / 4;
-      for (int idx = tid; idx < T::TF * 128 * T::NIFP; idx += kThreads) {
-        const int r = idx / T::NIFP, k = idx % T::NIFP;
+      for (int o = tid; o < T::TF * 128 * T::NIFP; o += kThreads) {
+        const int t = o / (128 * T::NIFP), oo = o % (128 * T::NIFP);
+        const int r = t * 128 + (oo / (KC * 32)) * 8 + (oo / 4) % 8, k = ((oo / 32) % KC) * 4 + (oo % 4);
         float v = 0.f;
         if (r < T::RF && k < NIF) {
           if (r < F * NF) {
@@ -479,7 +484,6 @@ __global__ void __launch_bounds__(kThreads) tc_element_blocks(TcBlockParams p) {
           }
         }
         const float hi = tf32_hi(v);
-        const int o = (r >> 7) * 128 * T::NIFP + cm_index(r & 127, k, KC);
         aHi[o] = hi;
         aLo[o] = tf32_hi(v - hi);
       }
@@ -503,12 +507,13 @@ __global__ void __launch_bounds__(kThreads) tc_element_blocks(TcBlockParams p) {
       float v[16];
       tmem_ld<16>(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(T::TV * T::NVB + t * T::NFB), v);
       const int r = 32 * warp + lane;
+      constexpr int SF = NF | 1;
 #pragma unroll
-      for (int j = 0; j < NF; ++j) aHi[r * NF + j] = v[j];
+      for (int j = 0; j < NF; ++j) aHi[r * SF + j] = v[j];
       __syncthreads();
       const int rows = (T::RF - t * 128) < 128 ? (T::RF - t * 128) : 128;
       float* dst = out + T::RV * N + (int64_t)t * 128 * NF;
-      for (int i = tid; i < rows * NF; i += kThreads) dst[i] = aHi[i];
+      for (int i = tid; i < rows * NF; i += kThreads) dst[i] = aHi[(i / NF) * SF + i % NF];
       __syncthreads();
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -519,6 +524,274 @@ __global__ void __launch_bounds__(kThreads) tc_element_blocks(TcBlockParams p) {
   __syncthreads();
   if (warp == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)T::TMEM_COLS));
+}
+
+// ------------------------------------------------ CG element operators
+// Mass (Mass.cpp:5-38), Diffusion (Diffusion.cpp:5-43) and Convection (Convection.cpp:21-46)
+// as the same contractions: mass rows a = dV phi_i against B = phi (K = the IPs); diffusion
+// rows a[(q, c)] = sum_r Gamma_q[c][r] d_r phi_i with Gamma_q = dV J^{-T} K_q J^{-1}, and
+// convection rows a[(q, c)] = phi_k beta_q[c] with beta_q = dV J^{-T} v_q, both against
+// B = the reference gradients (K = IPs x dimensions). Two MMA phases share the A buffer.
+template <int D, int P>
+struct CgTcDims {
+  using K = Dims<D, P>;
+  static constexpr int N = K::N, NI = K::NI;
+  static constexpr int NIP = (NI + 7) / 8 * 8;
+  static constexpr int KD = NI * D, KDP = (KD + 7) / 8 * 8;
+  static constexpr int NB = 32;  // MMA N (nodes, padded)
+  static constexpr int A_FLOATS = 128 * (KDP > NIP ? KDP : NIP);
+  static constexpr int TB_PHI_HI = 0, TB_PHI_LO = TB_PHI_HI + NB * NIP;
+  static constexpr int TB_DP_HI = TB_PHI_LO + NB * NIP, TB_DP_LO = TB_DP_HI + NB * KDP;
+  static constexpr int TB_PHI = TB_DP_LO + NB * KDP, TB_DPHI = TB_PHI + NI * N, TB_W = TB_DPHI + NI * N * D;
+  static constexpr int TB_FLOATS = (TB_W + NI + 3) / 4 * 4;
+  // per-element scratch: X, dV, Gamma [NI][D][D], beta [NI][D]
+  static constexpr int S_X = 0, S_DV = S_X + N * D, S_GAM = S_DV + NI, S_BETA = S_GAM + NI * D * D;
+  static constexpr int S_FLOATS = (S_BETA + NI * D + 3) / 4 * 4;
+  static constexpr size_t OFF_AHI = 0, OFF_ALO = (size_t)A_FLOATS * 4, OFF_TAB = OFF_ALO + (size_t)A_FLOATS * 4;
+  static constexpr size_t OFF_SCR = OFF_TAB + (size_t)TB_FLOATS * 4;
+  static constexpr size_t SMEM = OFF_SCR + (size_t)S_FLOATS * 4 + 1024;
+  static constexpr int TMEM_COLS = 64;
+};
+
+template <int D, int P>
+__global__ void __launch_bounds__(kThreads) tc_cg_operators(CgOpParams p) {
+  using T = CgTcDims<D, P>;
+  constexpr int N = T::N, NI = T::NI;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  float* aHi = (float*)(smem + T::OFF_AHI);
+  float* aLo = (float*)(smem + T::OFF_ALO);
+  float* tab = (float*)(smem + T::OFF_TAB);
+  float* scr = (float*)(smem + T::OFF_SCR);
+  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ uint32_t tmemBase;
+  __shared__ int sAbort;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[0])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[1])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    sAbort = 0;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmemBase)),
+                 "r"((uint32_t)T::TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmemBase;
+  if (tid == 0) {
+    const uint32_t bytes = (uint32_t)T::TB_FLOATS * 4u;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&bars[0])), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(tab)),
+                 "l"(p.tctab), "r"(bytes), "r"(smem_u32(&bars[0]))
+                 : "memory");
+  }
+  if (!mbar_wait(&bars[0], 0)) {
+    atomicCAS(p.status, 0, 2);
+    sAbort = 1;
+  }
+  __syncthreads();
+  const float* phi = tab + T::TB_PHI;
+  const float* dphi = tab + T::TB_DPHI;
+  const float* w = tab + T::TB_W;
+  float* X = scr + T::S_X;
+  float* dV = scr + T::S_DV;
+  float* Gam = scr + T::S_GAM;
+  float* beta = scr + T::S_BETA;
+  const uint32_t aHiS = smem_u32(aHi), aLoS = smem_u32(aLo), tabS = smem_u32(tab);
+  uint32_t phase = 0;
+  for (int64_t e = blockIdx.x; e < p.nCells && !sAbort; e += gridDim.x) {
+    const int* cell = p.cells + e * N;
+    for (int i = tid; i < N * D; i += kThreads) X[i] = (float)p.coords[(int64_t)cell[i / D] * D + (i % D)];
+    __syncthreads();
+    for (int q = tid; q < NI; q += kThreads) {
+      float J[D][D];
+      for (int r = 0; r < D; ++r)
+        for (int s = 0; s < D; ++s) {
+          float acc = 0.f;
+          for (int i = 0; i < N; ++i) acc += dphi[(q * N + i) * D + r] * X[i * D + s];
+          J[r][s] = acc;
+        }
+      float det, iv[D][D];
+      if (D == 2) {
+        det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+        const float id = 1.f / det;
+        iv[0][0] = J[1][1] * id;
+        iv[0][1] = -J[0][1] * id;
+        iv[1][0] = -J[1][0] * id;
+        iv[1][1] = J[0][0] * id;
+      } else {
+        const float c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        const float c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+        const float c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+        const float id = 1.f / det;
+        iv[0][0] = c00 * id;
+        iv[1][0] = c01 * id;
+        iv[2][0] = c02 * id;
+        iv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+        iv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+        iv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+        iv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+        iv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+        iv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+      }
+      const float dv = w[q] * det;
+      dV[q] = dv;
+      float K[D][D], v[D];
+      for (int a = 0; a < D; ++a) {
+        for (int b = 0; b < D; ++b) {
+          float acc = (p.kc == 0 && a == b) ? 1.f : 0.f;
+          if (p.kc > 0)
+            for (int j = 0; j < N; ++j) {
+              const int64_t bk = p.kappaLayout == 0 ? (int64_t)cell[j] * p.kc : (e * N + j) * p.kc;
+              const float kv = p.kc == 1 ? (a == b ? (float)p.kappa[bk] : 0.f) : (float)p.kappa[bk + a + b * D];
+              acc += phi[q * N + j] * kv;
+            }
+          K[a][b] = acc;
+        }
+        float acc = 0.f;
+        if (p.vel)
+          for (int j = 0; j < N; ++j) {
+            const int64_t bv = p.velLayout == 0 ? (int64_t)cell[j] * D : (e * N + j) * D;
+            acc += phi[q * N + j] * (float)p.vel[bv + a];
+          }
+        v[a] = acc;
+      }
+      // Gamma = dV J^{-T} K J^{-1} ([c][r]), beta = dV J^{-T} v
+      for (int c = 0; c < D; ++c) {
+        for (int r = 0; r < D; ++r) {
+          float acc = 0.f;
+          for (int a = 0; a < D; ++a)
+            for (int b = 0; b < D; ++b) acc += iv[a][c] * K[a][b] * iv[b][r];
+          Gam[(q * D + c) * D + r] = dv * acc;
+        }
+        float bb = 0.f;
+        for (int a = 0; a < D; ++a) bb += v[a] * iv[a][c];
+        beta[q * D + c] = dv * bb;
+      }
+    }
+    __syncthreads();
+    double* out = p.out + e * 3 * N * N;
+    // phase 1: mass rows against phi
+    {
+      constexpr int KC = T::NIP / 4;
+      for (int o = tid; o < 128 * T::NIP; o += kThreads) {  // shared-memory order
+        const int r = (o / (KC * 32)) * 8 + (o / 4) % 8, q = ((o / 32) % KC) * 4 + (o % 4);
+        const float val = (r < N && q < NI) ? dV[q] * phi[q * N + r] : 0.f;
+        const float hi = tf32_hi(val);
+        aHi[o] = hi;
+        aLo[o] = tf32_hi(val - hi);
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (tid == 0) {
+      issue_tiles(tmem, 1, T::NIP, T::NB, aHiS, aLoS, tabS + T::TB_PHI_HI * 4, tabS + T::TB_PHI_LO * 4);
+      mma_commit(&bars[1]);
+    }
+    if (!mbar_wait(&bars[1], phase)) {
+      atomicCAS(p.status, 0, 2);
+      sAbort = 1;
+    }
+    phase ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    {
+      float v[32];
+      tmem_ld<32>(tmem + ((uint32_t)(32 * warp) << 16), v);
+      const int r = 32 * warp + lane;
+      if ((p.which & 1) && r < N)
+#pragma unroll
+        for (int j = 0; j < N; ++j) out[j * N + r] = (double)v[j];
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // phase 2: diffusion rows then convection rows against the reference gradients
+    {
+      constexpr int KC = T::KDP / 4;
+      for (int o = tid; o < 128 * T::KDP; o += kThreads) {  // shared-memory order
+        const int r = (o / (KC * 32)) * 8 + (o / 4) % 8, k = ((o / 32) % KC) * 4 + (o % 4);
+        float val = 0.f;
+        if (k < T::KD && r < 2 * N) {
+          const int q = k / D, c = k % D;
+          if (r < N) {
+            for (int s = 0; s < D; ++s) val += Gam[(q * D + c) * D + s] * dphi[(q * N + r) * D + s];
+          } else {
+            val = phi[q * N + (r - N)] * beta[q * D + c];
+          }
+        }
+        const float hi = tf32_hi(val);
+        aHi[o] = hi;
+        aLo[o] = tf32_hi(val - hi);
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (tid == 0 && !sAbort) {
+      issue_tiles(tmem + 32u, 1, T::KDP, T::NB, aHiS, aLoS, tabS + T::TB_DP_HI * 4, tabS + T::TB_DP_LO * 4);
+      mma_commit(&bars[1]);
+    }
+    if (!sAbort && !mbar_wait(&bars[1], phase)) {
+      atomicCAS(p.status, 0, 2);
+      sAbort = 1;
+    }
+    phase ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    {
+      float v[32];
+      tmem_ld<32>(tmem + ((uint32_t)(32 * warp) << 16) + 32u, v);
+      const int r = 32 * warp + lane;
+      if (r < N && (p.which & 2))
+#pragma unroll
+        for (int j = 0; j < N; ++j) out[N * N + j * N + r] = (double)v[j];
+      if (r >= N && r < 2 * N && (p.which & 4))
+#pragma unroll
+        for (int j = 0; j < N; ++j) out[2 * N * N + j * N + (r - N)] = (double)v[j];
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)T::TMEM_COLS));
+}
+
+// Resident CTAs per SM for a kernel of `threads` threads and `smem` bytes of dynamic shared
+// memory: the occupancy API's answer, checked against the kernel's registers and shared
+// memory and the SM's 512 TMEM columns (tcols per CTA); the larger of the API's answer and
+// the resource count is used (extra CTAs only queue: the CTAs do not wait on one another).
+template <class K>
+int resident_ctas(K kern, int threads, size_t smem, int tcols) {
+  int dev = 0, perSM = 0;
+  cudaGetDevice(&dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, threads, smem) != cudaSuccess) perSM = 1;
+  cudaFuncAttributes a{};
+  int smemSM = 0, resv = 0, regsSM = 0;
+  if (cudaFuncGetAttributes(&a, kern) == cudaSuccess &&
+      cudaDeviceGetAttribute(&smemSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) == cudaSuccess &&
+      cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock, dev) == cudaSuccess &&
+      cudaDeviceGetAttribute(&regsSM, cudaDevAttrMaxRegistersPerMultiprocessor, dev) == cudaSuccess) {
+    const size_t perCta = smem + a.sharedSizeBytes + (size_t)resv;
+    const int bySmem = perCta > 0 ? (int)((size_t)smemSM / perCta) : 1;
+    const int regsCta = ((a.numRegs * 32 + 255) / 256 * 256) * ((threads + 31) / 32);
+    const int byRegs = regsCta > 0 ? regsSM / regsCta : 1;
+    const int calc = bySmem < byRegs ? bySmem : byRegs;
+    if (calc > perSM) perSM = calc;
+  }
+  if (perSM * tcols > 512) perSM = 512 / tcols;
+  return perSM < 1 ? 1 : perSM;
 }
 
 // ---------------------------------------------------------------- host side
@@ -565,19 +838,62 @@ std::vector<float> build_table(const double* tab64) {
 }
 
 template <int D, int P>
+std::vector<float> build_cg_table(const double* tab64) {
+  using T = CgTcDims<D, P>;
+  constexpr int N = T::N, NI = T::NI;
+  const double* phi = tab64;
+  const double* dphi = phi + NI * N;
+  const double* w = dphi + NI * N * D;
+  std::vector<float> t(T::TB_FLOATS, 0.f);
+  for (int j = 0; j < N; ++j) {
+    for (int q = 0; q < NI; ++q) {
+      const double x = phi[q * N + j], hi = tf32_round_host(x);
+      t[T::TB_PHI_HI + cm_index(j, q, T::NIP / 4)] = (float)hi;
+      t[T::TB_PHI_LO + cm_index(j, q, T::NIP / 4)] = (float)tf32_round_host(x - hi);
+      for (int c = 0; c < D; ++c) {
+        const double y = dphi[(q * N + j) * D + c], yh = tf32_round_host(y);
+        t[T::TB_DP_HI + cm_index(j, q * D + c, T::KDP / 4)] = (float)yh;
+        t[T::TB_DP_LO + cm_index(j, q * D + c, T::KDP / 4)] = (float)tf32_round_host(y - yh);
+      }
+    }
+  }
+  for (int i = 0; i < NI * N; ++i) t[T::TB_PHI + i] = (float)phi[i];
+  for (int i = 0; i < NI * N * D; ++i) t[T::TB_DPHI + i] = (float)dphi[i];
+  for (int i = 0; i < NI; ++i) t[T::TB_W + i] = (float)w[i];
+  return t;
+}
+
+template <int D, int P>
+cudaError_t launch_cg_t(const CgOpParams& p, cudaStream_t s) {
+  using T = CgTcDims<D, P>;
+  auto kern = tc_cg_operators<D, P>;
+  cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::SMEM);
+  if (err == cudaSuccess)
+    err = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+  if (err != cudaSuccess) return err;
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int perSM = resident_ctas(kern, kThreads, T::SMEM, T::TMEM_COLS);
+  int64_t grid = (int64_t)nsm * perSM;
+  if (grid > p.nCells) grid = p.nCells;
+  if (grid < 1) grid = 1;
+  kern<<<(unsigned)grid, kThreads, T::SMEM, s>>>(p);
+  return cudaGetLastError();
+}
+
+template <int D, int P>
 cudaError_t launch_t(const TcBlockParams& p, cudaStream_t s) {
   using T = TcDims<D, P>;
   auto kern = tc_element_blocks<D, P>;
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::SMEM);
+  if (err == cudaSuccess)
+    err = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
   if (err != cudaSuccess) return err;
-  int dev = 0, nsm = 0, perSM = 0;
+  int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, kThreads, T::SMEM);
-  if (err != cudaSuccess) return err;
-  if (perSM < 1) perSM = 1;
-  // resident CTAs share the SM's 512 TMEM columns
-  if (perSM * T::TMEM_COLS > 512) perSM = 512 / T::TMEM_COLS;
+  const int perSM = resident_ctas(kern, kThreads, T::SMEM, T::TMEM_COLS);
   int64_t grid = (int64_t)nsm * perSM;
   if (grid > p.nCells) grid = p.nCells;
   if (grid < 1) grid = 1;
@@ -620,6 +936,16 @@ std::vector<float> tc_table(int dim, int order, const double* tab64) {
 
 cudaError_t launch_tc_blocks(int dim, int order, const TcBlockParams& p, cudaStream_t s) {
   HFX_TC_DISPATCH(return launch_t<D, P>(p, s));
+  return cudaErrorInvalidValue;
+}
+
+std::vector<float> tc_cg_table(int dim, int order, const double* tab64) {
+  HFX_TC_DISPATCH(return build_cg_table<D, P>(tab64));
+  return {};
+}
+
+cudaError_t launch_cg_operators_tc(int dim, int order, const CgOpParams& p, cudaStream_t s) {
+  HFX_TC_DISPATCH(return launch_cg_t<D, P>(p, s));
   return cudaErrorInvalidValue;
 }
 

@@ -84,6 +84,22 @@ typedef struct {
                             coarse_rtol asks for */
 } hfx_solve_opts;
 
+/* ---- CG element operators (Mass.cpp:5-38, Diffusion.cpp:5-43, Convection.cpp:21-46) ----
+ * Per element, one DOF per node: Mass M(i,j) = sum dV phi_i phi_j; Diffusion D(i,j) = sum dV
+ * (K grad phi_i)^T grad phi_j with K the context's diffusion field (hfx_set_kappa: nodal scalar
+ * or d x d tensor interpolated to the IPs as Diffusion::setDiffTensor does; none: identity);
+ * Convection C(k,l) = sum dV phi_k (v . grad phi_l) with the nodal velocity v (layout 0
+ * [nNodes][dim], 1 [nCells][N][dim]; interpolated as Convection::setVelocity does). which: a
+ * sum of HFX_OP_*. out (host): [nCells][3][N*N], entry (i, j) of operator k at k*N*N + j*N + i
+ * (Eigen's column-major); operators not asked are left unspecified. precision HFX_PREC_FP64:
+ * FP64 quadrature on the CUDA cores (agrees with the reference's FP64 assembly to round-off);
+ * HFX_PREC_MIXED: the contractions on the tensor cores (TF32 hi/lo split, FP32 accumulation;
+ * within 2e-5 of each operator's largest entry). */
+#define HFX_OP_MASS 1
+#define HFX_OP_DIFFUSION 2
+#define HFX_OP_CONVECTION 4
+int hfx_cg_operators(hfx_ctx* ctx, int which, int precision, const double* velocity, int velLayout, double* out);
+
 /* Test hook of the failure path (no counterpart in the reference): in the next two-level
  * solve that runs the one-launch coarse solve, one block withholds its first grid-barrier
  * arrival, so the others' bounded wait (about a second) runs out; the solve must then report

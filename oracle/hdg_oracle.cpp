@@ -2108,6 +2108,81 @@ long orc_problem_face_rows(void* h, int nthreads, int nsel, const int* faceIds, 
   }
 }
 
+// CG element operators of one DOF per node, element by element, restated loop for loop:
+// Mass::assemble (Mass.cpp:5-38), Diffusion::assemble (Diffusion.cpp:5-43) with the nodal
+// diffusion field interpolated to the IPs as Diffusion::setDiffTensor does (Diffusion.cpp:59-69;
+// scalar kc = 1 times the identity, or a d x d tensor stored column-major, kc = d*d; none:
+// identity), Convection::assemble (Convection.cpp:21-46) with the nodal velocity interpolated
+// as Convection::setVelocity does (Convection.cpp:5-19). vel: [nCells][N][d] (may be null when
+// bit 2 is not asked). out: [nCells][3][N*N], op(i, j) at j*N + i; which: bit 0 mass, bit 1
+// diffusion, bit 2 convection (the others are left untouched).
+int orc_problem_cg_operators(void* h, int which, const double* vel, double* out) {
+  ORC_TRY({
+    Problem& P = *(Problem*)h;
+    const RefEl* re = P.re;
+    const int d = P.dim, N = re->nNodes, nI = re->nIP;
+    if ((which & 4) && !vel) throw std::runtime_error("convection needs a velocity");
+    for (int e = 0; e < P.nCells; ++e) {
+      const int* cell = &P.cells[(size_t)e * N];
+      double* oM = out + ((size_t)e * 3 + 0) * N * N;
+      double* oD = out + ((size_t)e * 3 + 1) * N * N;
+      double* oC = out + ((size_t)e * 3 + 2) * N * N;
+      for (int k = 0; k < 3; ++k)
+        if (which & (1 << k)) std::fill(out + ((size_t)e * 3 + k) * N * N, out + ((size_t)e * 3 + k + 1) * N * N, 0.0);
+      for (int q = 0; q < nI; ++q) {
+        Mat J(d, d);
+        for (int i = 0; i < N; ++i)
+          for (int r = 0; r < d; ++r)
+            for (int t = 0; t < d; ++t) J(r, t) += re->dphi[q][i][r] * P.coords[(size_t)cell[i] * d + t];
+        const double dv = re->ipW[q] * det_small(J);
+        const Mat iJ = inverse(J);
+        // gradShapes.col(i) = invJ * dphi_i
+        std::vector<std::vector<double>> g(N, std::vector<double>(d, 0.0));
+        for (int i = 0; i < N; ++i)
+          for (int a = 0; a < d; ++a)
+            for (int r = 0; r < d; ++r) g[i][a] += iJ(a, r) * re->dphi[q][i][r];
+        if (which & 1)
+          for (int j = 0; j < N; ++j)
+            for (int k = 0; k < N; ++k) oM[k * N + j] += re->phi[q][j] * re->phi[q][k] * dv;
+        if (which & 2) {
+          Mat K(d, d);
+          for (int a = 0; a < d; ++a) K(a, a) = P.kc == 0 ? 1.0 : 0.0;
+          if (P.kc > 0)
+            for (int j = 0; j < N; ++j) {
+              const double* kn = &P.kappa[((size_t)e * N + j) * P.kc];
+              for (int a = 0; a < d; ++a)
+                for (int b = 0; b < d; ++b)
+                  K(a, b) += re->phi[q][j] * (P.kc == 1 ? (a == b ? kn[0] : 0.0) : kn[a + b * d]);
+            }
+          for (int i = 0; i < N; ++i)
+            for (int j = 0; j < N; ++j) {
+              double v = 0.0;  // (K grad phi_i)^T grad phi_j
+              for (int a = 0; a < d; ++a) {
+                double kg = 0.0;
+                for (int b = 0; b < d; ++b) kg += K(a, b) * g[i][b];
+                v += kg * g[j][a];
+              }
+              oD[j * N + i] += v * dv;
+            }
+        }
+        if (which & 4) {
+          std::vector<double> vq(d, 0.0), meas(d, 0.0);
+          for (int j = 0; j < N; ++j)
+            for (int a = 0; a < d; ++a) vq[a] += vel[((size_t)e * N + j) * d + a] * re->phi[q][j];
+          for (int r = 0; r < d; ++r)
+            for (int a = 0; a < d; ++a) meas[r] += dv * vq[a] * iJ(a, r);  // dV (v^T invJ)^T
+          for (int k = 0; k < N; ++k)
+            for (int l = 0; l < N; ++l) {
+              double dot = 0.0;
+              for (int r = 0; r < d; ++r) dot += meas[r] * re->dphi[q][l][r];
+              oC[l * N + k] += dot * re->phi[q][k];
+            }
+        }
+      }
+    }
+  })
+}
+
 int orc_problem_condensed(void* h, double* S, double* S0, double* U, double* Q, double* U0, double* Q0) {
   Problem* P = (Problem*)h;
   std::copy(P->S.begin(), P->S.end(), S);

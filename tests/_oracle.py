@@ -47,6 +47,7 @@ def lib():
         L.orc_problem_local_matrix.argtypes = [vp, ip, vp, vp, vp]
         L.orc_problem_condensed.argtypes = [vp] * 7
         L.orc_problem_sample.argtypes = [vp, ip, ip, vp] + [vp] * 6
+        L.orc_problem_cg_operators.argtypes = [vp, ip, vp, vp]
         L.orc_problem_face_rows.restype = ctypes.c_long
         L.orc_problem_face_rows.argtypes = [vp, ip, ip, vp, vp, vp, vp, vp, ctypes.c_long]
         L.orc_problem_nnz.restype = ctypes.c_long
@@ -193,6 +194,14 @@ class Problem:
                    Q=np.zeros((n, Q * L_)), U0=np.zeros((n, U)), Q0=np.zeros((n, Q)))
         _check(lib().orc_problem_sample(self.h, nthreads, n, _ptr(ids), *[_ptr(out[k]) for k in
                                                                            ("S", "S0", "U", "Q", "U0", "Q0")]))
+        return out
+
+    def cg_operators(self, which=7, velocity=None):
+        """CG element operators [nCells][3][N*N] (column-major): Mass, Diffusion (the kappa field
+        set with set_fields), Convection (nodal velocity [nCells][N][d])."""
+        out = np.zeros((self.nCells, 3, self.lenU * self.lenU))
+        v = None if velocity is None else np.ascontiguousarray(velocity, dtype=np.float64)
+        _check(lib().orc_problem_cg_operators(self.h, which, _ptr(v), _ptr(out)))
         return out
 
     def face_rows(self, faces, nthreads=1):

@@ -99,3 +99,35 @@ def test_diffusion_blocks_on_reference_element(dim, p, kap):
                     Slq[f * Nf + k, re.faceNodes[f][l] * dim + d] -= fm[k, l] * REF_NORMALS[dim][f][d]
     assert np.abs(A[:lenU, lenU:sL] - kap * Suq).max() < 1e-12
     assert np.abs(A[sL:, lenU:sL] - kap * Slq).max() < 1e-12
+
+
+@pytest.mark.parametrize("dim,n,order", [(2, 3, 2), (2, 2, 4), (3, 2, 2), (3, 1, 3)])
+def test_cg_operators_identities(dim, n, order):
+    """Mass, Diffusion and Convection (Mass.cpp:5-38, Diffusion.cpp:5-43, Convection.cpp:21-46) on
+    jittered meshes: the mass equals HDGBase's Sqq block, the stiffness is symmetric, kills
+    constants and maps x to the row integrals of d phi_i / dx (HDGBase's C_0 times 1), and the
+    convection with v = e_0 kills constants and maps x to the mass row sums."""
+    from helpers import mesh
+    re, coords, cells = mesh(dim, n, order, jitter=0.1, seed=3)
+    P = O.Problem(dim, order, coords, cells)
+    P.set_fields(np.ones(P.ndofs), src_mode=0, dirichlet=np.zeros(P.ndofs))
+    N = P.lenU
+    vel = np.zeros((P.nCells, N, dim))
+    vel[..., 0] = 1.0
+    ops = P.cg_operators(7, vel)
+    x = coords[cells][..., 0]
+    for e in range(P.nCells):
+        M = ops[e, 0].reshape(N, N).T  # column-major
+        Dm = ops[e, 1].reshape(N, N).T
+        C = ops[e, 2].reshape(N, N).T
+        A, _, _ = P.local_matrix(e)
+        q0 = N
+        Sqq = A[q0::dim, q0::dim][:N, :N]
+        assert np.abs(M - Sqq).max() < 1e-14 * max(1.0, np.abs(Sqq).max())
+        scale = np.abs(Dm).max()
+        assert np.abs(Dm - Dm.T).max() < 1e-12 * scale
+        assert np.abs(Dm @ np.ones(N)).max() < 1e-12 * scale
+        C0 = A[q0::dim, :N][:N]  # Squ rows (i, 0): integral of d phi_i/dx phi_j
+        assert np.abs(Dm @ x[e] - C0 @ np.ones(N)).max() < 1e-12 * scale
+        assert np.abs(C @ np.ones(N)).max() < 1e-12 * np.abs(C).max()
+        assert np.abs(C @ x[e] - M @ np.ones(N)).max() < 1e-12 * np.abs(M).max()
