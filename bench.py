@@ -74,7 +74,8 @@ CONFIGS = {
     "cfg3": dict(dim=2, batch=dict(count=1024, seed=3, min_elements=200, max_elements=20000), cpu_budget=12000,
                  desc="1024 independent 2D HDG diffusion-source problems: unit-square meshes of 2n^2 triangles, "
                       "n = round(sqrt(c/2)), c log-uniform in [200, 20000]; interior vertices jittered "
-                      "U(+-0.2h); p uniform in 1..5 per problem; kappa = exp(g) at the nodes, g Gaussian "
+                      "U(+-0.2h); p uniform in 1..5 per problem; kappa = exp(g) at the cell centroids (constant per "
+                      "cell), g Gaussian "
                       "random field (sigma 1, corr 0.1); tau = 1; f = 2 pi^2 sin(pi x) sin(pi y), "
                       "Dirichlet u = sin(pi x) sin(pi y)"),
     "cfg3-small": dict(dim=2, batch=dict(count=64, seed=3, min_elements=200, max_elements=20000), cpu_budget=1500,
@@ -298,7 +299,6 @@ def run_ours(args, world, rank, local):
     ctx._chk(L.hfx_synchronize(ctx.h), "sync")
     clocks = ClockSampler(local)
     clocks.start()
-    ctx._chk(L.hfx_profile_enable(ctx.h, 1), "profile")
     ctx._chk(L.hfx_mark(ctx.h, 0), "mark")
     for _ in range(args.steps):
         step_device()
@@ -307,6 +307,12 @@ def run_ours(args, world, rank, local):
     ctx._chk(L.hfx_elapsed_ms(ctx.h, 0, 1, capi.ctypes.byref(ms)), "elapsed")
     clk = clocks.stop()
     dev_ms = barrier_max(world, ms.value)
+    # per-kernel device times from a second pass of the same steps with the event timer on
+    # (its events would otherwise add host work to the timed region)
+    ctx._chk(L.hfx_profile_enable(ctx.h, 1), "profile")
+    for _ in range(args.steps):
+        step_device()
+    ctx._chk(L.hfx_synchronize(ctx.h), "sync")
     kt = {}
     for name, kid in (("local", 0), ("scatter", 1), ("spmv64", 2), ("spmv32", 3), ("update", 4), ("recover", 5),
                       ("other", 6), ("residual", 7), ("coarse", 8), ("tensor", 9)):
@@ -353,7 +359,11 @@ def run_ours(args, world, rank, local):
         for name, kw in (("chebyshev_same_degree", dict(coarse_mode=capi.COARSE_CHEBYSHEV,
                                                         coarse_degree=args.coarse_degree)),
                          ("chebyshev_adaptive", dict(coarse_mode=capi.COARSE_CHEBYSHEV, coarse_degree=0)),
-                         ("learned", dict(coarse_mode=capi.COARSE_LEARNED, coarse_degree=0))):
+                         ("learned", dict(coarse_mode=capi.COARSE_LEARNED, coarse_degree=0)),
+                         # the trained coarse network also gives the initial guess: x0 = P q(A_c) P^T b'
+                         ("learned_initial_guess", dict(coarse_mode=capi.COARSE_LEARNED, coarse_degree=0,
+                                                        coarse_guess=1))):
+            kw.setdefault("coarse_guess", int(args.coarse_guess))
             o2 = capi.solve_opts(precision=prec, rtol=args.rtol, precond=pc, maxits=200000,
                                  inner_rtol=args.inner_rtol, coarse_rtol=args.coarse_rtol, **kw)
             i2 = capi.SolveInfo()
@@ -429,7 +439,9 @@ def run_ours(args, world, rank, local):
         launches = min(kt[key][0], iters * args.steps) if iters else kt[key][0]
         avg_ms = kt[key][1] / max(1, launches)
         achieved = alg / (avg_ms / 1e3) / 1e9
-        return dict(bound="hbm", kernel="cg_spmv_half_ell<float>" if sv == 4 else "cg_spmv<double>",
+        kname = ("cg_spmv_half_warp<float>" if ctx.tuning_info()[0] == 1 else "cg_spmv_half_ell<float>") \
+            if sv == 4 else "cg_spmv<double>"
+        return dict(bound="hbm", kernel=kname,
                     achieved=round(achieved, 1), peak=hbm, unit="GB/s", frac=round(achieved / hbm, 4),
                     traffic=(TRAFFIC_PER_NNZ[key] * nnz) if (dim, p) == (3, 3) else None, bytes_per_launch=int(alg),
                     avg_launch_ms=round(avg_ms, 4), peak_source=peak_kind)
@@ -505,6 +517,7 @@ def run_ours(args, world, rank, local):
         "rel_err_vs_oracle": oracle_check,
         "meets_1e-8_rel_err": bool(rel_err <= 1e-8),
         "coarse_solve_comparison": coarse_arms,
+        "spmv_tuner": dict(zip(("kernel", "ms_per_launch"), ctx.tuning_info())),
         "fp64_reference_iterations": ref_info.iterations,
         "plain_fp64": plain,
         "learned_coarse": learned,
@@ -757,8 +770,10 @@ def run_batch(args, world, rank, local):
     # for the single-problem workloads (the coarse solve Chebyshev: no per-group training)
     prec = capi.PREC_FP64 if args.precision == "fp64" else capi.PREC_MIXED
     pc = capi.PC_TWOLEVEL if args.precond == "twolevel" else capi.PC_BLOCK_JACOBI
+    # fixed Chebyshev degree (--coarse-degree; 0: the degree coarse_rtol asks for on the union's
+    # spectrum, which spans every problem of the group and runs to the cap)
     opts = dict(precision=prec, precond=pc, maxits=200000, inner_rtol=args.inner_rtol, coarse_rtol=args.coarse_rtol,
-                coarse_mode=capi.COARSE_CHEBYSHEV)
+                coarse_mode=capi.COARSE_CHEBYSHEV, coarse_degree=args.coarse_degree)
     pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
     bufs = B.host_buffers(alloc=pin)
     for g in B.groups.values():  # pinned copies of the per-step inputs
@@ -854,7 +869,9 @@ def run_batch(args, world, rank, local):
                    "elements_per_order": {str(k): v for k, v in sorted(per_order.items())},
                    "trace_dofs": int(sum(g.ctx.ndofs for g in B.groups.values())),
                    "precision": args.precision,
-                   "preconditioner": ("two-level: per-face block Jacobi + vertex coarse space (Chebyshev)"
+                   "preconditioner": (("two-level: per-face block Jacobi + vertex coarse space (Chebyshev, %s)"
+                                       % ("degree %d" % args.coarse_degree if args.coarse_degree > 0
+                                          else "adaptive degree"))
                                       if pc == capi.PC_TWOLEVEL else "block-Jacobi (per face)"),
                    "krylov": "CG (symmetric trace systems)",
                    "rtol": args.rtol, "rtol_per_problem": True,
@@ -1015,7 +1032,9 @@ def main():
     ap.add_argument("--coarse-rtol", type=float, default=0.3, help="Chebyshev coarse-solve reduction target")
     ap.add_argument("--coarse", default="learned", choices=["learned", "chebyshev"],
                     help="coarse solve of the two-level preconditioner: trained polynomial or Chebyshev")
-    ap.add_argument("--coarse-degree", type=int, default=8, help="degree of the learned coarse polynomial")
+    ap.add_argument("--coarse-degree", type=int, default=8,
+                    help="degree of the learned coarse polynomial (the batch workload: of its Chebyshev coarse "
+                         "solve, 0 = the degree --coarse-rtol asks for)")
     ap.add_argument("--assembly-path", type=int, default=0, choices=[0, 1],
                     help="element kernel choice (hfx_set_assembly_path): 0 automatic (affine kernel, or the "
                          "tensor-core contractions in the mixed assembly), 1 quadrature on the CUDA cores")

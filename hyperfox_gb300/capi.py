@@ -41,7 +41,7 @@ EXPORTED = [
     "hfx_rk_butcher", "hfx_rk_set", "hfx_rk_set_type", "hfx_rk_begin_step", "hfx_rk_compute_stage",
     "hfx_rk_compute_solution", "hfx_set_trace", "hfx_get_state",
     "hfx_set_tau", "hfx_set_kappa", "hfx_set_source", "hfx_set_dirichlet", "hfx_set_time_scheme",
-    "hfx_ip_coords", "hfx_assemble", "hfx_assemble_ex", "hfx_set_solver_type", "hfx_set_state", "hfx_set_assembly_path", "hfx_assembly_info", "hfx_get_condensed", "hfx_get_csr", "hfx_get_condensed_sample", "hfx_get_csr_rows", "hfx_mixed_assembly_info", "hfx_get_tc_blocks", "hfx_test_coarse_barrier", "hfx_cg_operators",
+    "hfx_ip_coords", "hfx_assemble", "hfx_assemble_ex", "hfx_set_solver_type", "hfx_set_state", "hfx_set_assembly_path", "hfx_assembly_info", "hfx_get_condensed", "hfx_get_csr", "hfx_get_condensed_sample", "hfx_get_csr_rows", "hfx_mixed_assembly_info", "hfx_get_tc_blocks", "hfx_test_coarse_barrier", "hfx_cg_operators", "hfx_tuning_info", "hfx_set_tuning",
     "hfx_solve_opts_default", "hfx_solve", "hfx_recover", "hfx_coarse_operator", "hfx_coarse_train",
     "hfx_coarse_loss_grad",
     "hfx_la_create", "hfx_la_destroy", "hfx_la_allocate", "hfx_la_set_values", "hfx_la_set_rhs",
@@ -136,6 +136,8 @@ def load(path=LIB_PATH):
         "hfx_mixed_assembly_info": ([vp, vp], ip),
         "hfx_test_coarse_barrier": ([vp], ip),
         "hfx_cg_operators": ([vp, ip, ip, vp, ip, vp], ip),
+        "hfx_tuning_info": ([vp, vp, vp], ip),
+        "hfx_set_tuning": ([vp, ip], ip),
         "hfx_get_tc_blocks": ([vp, ip, vp, vp, vp], ip),
         "hfx_get_csr_rows": ([vp, ip, vp, vp, vp, vp, vp, ctypes.c_int64], ip),
         "hfx_solve_opts_default": ([ctypes.POINTER(SolveOpts)], None),
@@ -501,6 +503,13 @@ class Context:
         self._chk(self.L.hfx_cg_operators(self.h, which, precision, _p(v), vel_layout, _p(out)), "cg_operators")
         return out
 
+    def tuning_info(self):
+        """(kernel chosen for the FP32 trace operator or -1, [ms row per lane, ms warp per face])."""
+        k = ctypes.c_int()
+        t = (ctypes.c_float * 2)()
+        self._chk(self.L.hfx_tuning_info(self.h, ctypes.byref(k), t), "tuning_info")
+        return k.value, [t[0], t[1]]
+
     def mixed_assembly_info(self):
         """1 when the last mixed assembly contracted the element blocks on the tensor cores."""
         v = ctypes.c_int()
@@ -795,6 +804,13 @@ class Burgers:
         v = None if velocity is None else np.ascontiguousarray(velocity, np.float64)
         self._chk(self.L.hfx_cg_operators(self.h, which, precision, _p(v), vel_layout, _p(out)), "cg_operators")
         return out
+
+    def tuning_info(self):
+        """(kernel chosen for the FP32 trace operator or -1, [ms row per lane, ms warp per face])."""
+        k = ctypes.c_int()
+        t = (ctypes.c_float * 2)()
+        self._chk(self.L.hfx_tuning_info(self.h, ctypes.byref(k), t), "tuning_info")
+        return k.value, [t[0], t[1]]
 
     def mixed_assembly_info(self):
         """1 when the last mixed assembly contracted the element blocks on the tensor cores."""

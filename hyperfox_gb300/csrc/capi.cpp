@@ -199,6 +199,12 @@ struct hfx_ctx {
   DevMem coarseMem;
   bool coarseBuilt = false;
   double coarseTarget = 0.0;
+  // launch tuner of the FP32 trace operator (mixed CG): -1 until the first mixed solve times both
+  int spmvChoice = -1;
+  // degree of the last coarse training; a learned solve without an accepted polynomial runs
+  // Chebyshev of that degree (0: no training yet, the reduction target decides)
+  int learnDegree = 0;
+  float spmvTimes[2] = {0.f, 0.f};
   int coarseMaxDeg = 64;      // degree cap of the Chebyshev coarse solve (a fixed degree when target ~ 0)
   // vector Burgers (hfx_burgers_*)
   BurgersState burgers;
@@ -267,6 +273,8 @@ void free_outputs(hfx_ctx* c) {
   c->d_S32 = c->d_S032 = c->d_U32 = c->d_Q32 = c->d_U032 = c->d_Q032 = c->d_dl32 = nullptr;
   c->d_tctab = c->d_tcb = nullptr;
   c->lastTensor = false;
+  c->spmvChoice = -1;
+  c->learnDegree = 0;
   c->cgMem.release();
   c->d_cgtab = nullptr;
   c->d_cgout = c->d_cgvel = nullptr;
@@ -1375,6 +1383,22 @@ int hfx_test_coarse_barrier(hfx_ctx* c) {
   return HFX_OK;
 }
 
+int hfx_set_tuning(hfx_ctx* c, int spmvKernel) {
+  if (!c || spmvKernel < -1 || spmvKernel > 1) return HFX_ERR_ARG;
+  c->spmvChoice = spmvKernel;
+  return HFX_OK;
+}
+
+int hfx_tuning_info(hfx_ctx* c, int* spmvKernel, float* spmvMs) {
+  if (!c) return HFX_ERR_ARG;
+  if (spmvKernel) *spmvKernel = c->spmvChoice;
+  if (spmvMs) {
+    spmvMs[0] = c->spmvTimes[0];
+    spmvMs[1] = c->spmvTimes[1];
+  }
+  return HFX_OK;
+}
+
 int hfx_mixed_assembly_info(hfx_ctx* c, int* tensorCores) {
   if (!c || !tensorCores) return HFX_ERR_ARG;
   *tensorCores = (c->mixedMode && c->lastTensor) ? 1 : 0;
@@ -1612,6 +1636,7 @@ static int ensure_coarse(hfx_ctx* c, double target, int maxDeg = 64) {
     HFX_CUDA(c, dalloc(m, &d.barrier, 2));
     HFX_CUDA(c, dalloc(m, &d.error, 1));
     HFX_CUDA(c, dalloc(m, &d.testHold, 1));
+    HFX_CUDA(c, dalloc(m, &d.lanczosOut, 2 * 30 + 2));
     HFX_CUDA(c, cudaMemsetAsync(d.barrier, 0, 2 * sizeof(unsigned), s));
     HFX_CUDA(c, cudaMemsetAsync(d.error, 0, sizeof(int), s));
     HFX_CUDA(c, cudaMemsetAsync(d.testHold, 0, sizeof(int), s));
@@ -1830,7 +1855,11 @@ int hfx_solve(hfx_ctx* c, const hfx_solve_opts* opts, double* trace, hfx_solve_i
   cudaEventCreate(&e1);
   cudaEventRecord(e0, c->stream);
   // a fixed Chebyshev degree K: the reduction target is out of reach, so the cap K decides
-  const int cdeg = o.coarse_degree > 0 ? std::min(o.coarse_degree, 64) : 0;
+  int cdeg = o.coarse_degree > 0 ? std::min(o.coarse_degree, 64) : 0;
+  // learned mode without an accepted polynomial: Chebyshev of the trained degree (the
+  // polynomial the training started from), not the reduction target's degree
+  if (!cdeg && o.precond == HFX_PC_TWOLEVEL && o.coarse_mode == HFX_COARSE_LEARNED && c->coarse.thetaHat.empty())
+    cdeg = c->learnDegree;
   const double ctarget = cdeg ? 1e-300 : (o.coarse_rtol > 0.0 && o.coarse_rtol < 1.0 ? o.coarse_rtol : 0.1);
   if (o.precond == HFX_PC_TWOLEVEL && (rc = ensure_coarse(c, ctarget, cdeg ? cdeg : 64))) {
     cudaEventDestroy(e0);
@@ -1863,6 +1892,8 @@ int hfx_solve(hfx_ctx* c, const hfx_solve_opts* opts, double* trace, hfx_solve_i
   a.restart = restart;
   a.coarse = o.precond == HFX_PC_TWOLEVEL ? &c->coarse : nullptr;
   a.coarse_guess = o.coarse_guess;
+  a.spmvChoice = &c->spmvChoice;
+  a.spmvTimes = c->spmvTimes;
   const bool learned = o.precond == HFX_PC_TWOLEVEL && o.coarse_mode == HFX_COARSE_LEARNED &&
                        !c->coarse.thetaHat.empty();
   c->coarse.useLearned = learned;
@@ -1952,6 +1983,7 @@ int hfx_coarse_train(hfx_ctx* c, int degree, int samples, int steps, hfx_train_i
   int rc = ensure_workspace(c, false, 0);
   if (rc) return rc;
   if ((rc = ensure_coarse(c, c->coarseTarget > 0.0 ? c->coarseTarget : 0.1, c->coarseMaxDeg))) return rc;
+  c->learnDegree = degree;
   const int64_t nV = c->coarse.dev.nV;
   float* buf = nullptr;
   HFX_CUDA(c, cudaMalloc(&buf, sizeof(float) * (size_t)samples * nV));

@@ -524,6 +524,100 @@ __global__ void __launch_bounds__(512) coarse_solve_coop(CoarseDev c, const T* _
   }
 }
 
+// The Lanczos steps of coarse_setup in one cooperative launch: the same passes with the
+// same arithmetic, the same block partition and the same block-ordered double sums as the
+// launch-per-step loop (so the same alpha, beta), but the scalars stay on the device and grid
+// barriers (bounded waits) replace the host round trips. Vectors written by other blocks are
+// read through L2 (__ldcg). out: alpha[m], beta[m], then the step count and the start norm.
+__device__ __forceinline__ double grid_sum(const double* partials, int slot) {
+  __shared__ double tot;
+  if (threadIdx.x == 0) {
+    double acc = 0.0;
+    for (unsigned b = 0; b < gridDim.x; ++b) acc += __ldcg(partials + (size_t)slot * gridDim.x + b);
+    tot = acc;
+  }
+  __syncthreads();
+  const double r = tot;
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(kT) lanczos_coop(CoarseDev c, int m, float* v, float* vprev, float* w,
+                                                   double* out) {
+  unsigned nb = 0;  // barriers passed in this launch
+  const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+  double ss = 0.0;
+  for (int64_t i = i0; i < c.nV; i += stride) {
+    uint32_t h = (uint32_t)i * 2654435761u + 12345u;
+    h ^= h >> 13;
+    h *= 0x5bd1e995u;
+    h ^= h >> 15;
+    const float x = c.dinv[i] > 0.f ? 0.5f + (float)(h & 0xffff) / 65536.f : 0.f;
+    v[i] = x;
+    vprev[i] = 0.f;
+    ss += (double)x * x;
+  }
+  block_partial(ss, c.partials, 0);
+  grid_barrier(c.barrier, ++nb * gridDim.x, c.error);
+  const double nrm = sqrt(grid_sum(c.partials, 0));
+  int steps = 0;
+  if (nrm > 0.0) {
+    const float sc = (float)(1.0 / nrm);
+    for (int64_t i = i0; i < c.nV; i += stride) v[i] *= sc;
+    grid_barrier(c.barrier, ++nb * gridDim.x, c.error);
+    double beta = 0.0;
+    for (int j = 0; j < m; ++j) {
+      double a = 0.0, ww = 0.0;
+      const float fb = (float)beta;
+      for (int64_t i = i0; i < c.nV; i += stride) {
+        float y = 0.f;
+        if (c.dinv[i] > 0.f) {
+          const float sv = sqrtf(c.dinv[i]);
+          for (int k = c.rowptr[i]; k < c.rowptr[i + 1]; ++k) {
+            const int col = c.col[k];
+            y = fmaf(c.val[k] * sqrtf(c.dinv[col]), __ldcg(v + col), y);
+          }
+          y *= sv;
+        }
+        y -= fb * __ldcg(vprev + i);
+        w[i] = y;
+        a += (double)y * __ldcg(v + i);
+        ww += (double)y * y;
+      }
+      block_partial(a, c.partials, 0);
+      block_partial(ww, c.partials, 1);
+      grid_barrier(c.barrier, ++nb * gridDim.x, c.error);
+      const double alpha = grid_sum(c.partials, 0), wsum = grid_sum(c.partials, 1);
+      if (blockIdx.x == 0 && threadIdx.x == 0) out[j] = alpha;
+      steps = j + 1;
+      beta = sqrt(fmax(wsum - alpha * alpha, 0.0));
+      // every block has read the partials before any block overwrites them in the next pass
+      grid_barrier(c.barrier, ++nb * gridDim.x, c.error);
+      if (j + 1 == m || beta < 1e-6 * sqrt(wsum)) break;
+      if (blockIdx.x == 0 && threadIdx.x == 0) out[m + j] = beta;
+      const float fa = (float)alpha, ib = (float)(1.0 / beta);
+      for (int64_t i = i0; i < c.nV; i += stride) w[i] = (__ldcg(w + i) - fa * __ldcg(v + i)) * ib;
+      grid_barrier(c.barrier, ++nb * gridDim.x, c.error);
+      float* t = vprev;
+      vprev = v;
+      v = w;
+      w = t;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    out[2 * m] = (double)steps;
+    out[2 * m + 1] = nrm;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned left = atomicAdd(c.barrier + 1, 1u) + 1u;
+    if (left == gridDim.x) {
+      atomicExch(c.barrier, 0u);
+      atomicExch(c.barrier + 1, 0u);
+    }
+  }
+}
+
 template <typename T>
 __global__ void coarse_prolong(CoarseDev c, T* __restrict__ x) {
   const int d = c.dim, NF = c.NF;
@@ -807,10 +901,55 @@ cudaError_t coarse_setup(CoarseSolver* cs, const T* S, int maxDegree, double tar
   coarse_fill_ell<<<blocks_for((int64_t)c->ellW * c->nV), kT, 0, s>>>(*c);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  // Lanczos, m steps, on D^{-1/2} A_c D^{-1/2}
-  const unsigned g = blocks_for(c->nV);
+  // Lanczos, m steps, on D^{-1/2} A_c D^{-1/2}; two partial sums per block fit the partials buffer
+  const unsigned g = std::min<unsigned>(blocks_for(c->nV), (152 * 32 + 64) / 2);
   std::vector<double> hp(2 * g);
   float *v = c->cd0, *vprev = c->cd1, *w = c->lz;
+  const int m = (int)std::min<int64_t>(30, c->nV);
+  std::vector<double> al, be;
+  {
+    // one cooperative launch when every block of the loop's partition fits at once
+    int dev = 0, coop = 0, nsm = 0, perSM = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (coop && c->barrier && c->lanczosOut &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, lanczos_coop, kT, 0) == cudaSuccess &&
+        (int64_t)perSM * nsm >= (int64_t)g) {
+      CoarseDev cv = *c;
+      int mm = m;
+      float *a0 = v, *a1 = vprev, *a2 = w;
+      double* o = c->lanczosOut;
+      void* args[] = {&cv, &mm, &a0, &a1, &a2, &o};
+      std::vector<double> ho(2 * m + 2);
+      int herr = 0;
+      const bool launched =
+          cudaLaunchCooperativeKernel((const void*)lanczos_coop, dim3(g), dim3(kT), args, 0, s) == cudaSuccess;
+      if (!launched) {
+        cudaGetLastError();  // not launched: the launch-per-step loop below does the steps
+      } else {
+        cudaMemcpyAsync(ho.data(), c->lanczosOut, sizeof(double) * (2 * m + 2), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(&herr, c->error, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+      }
+      if (launched && herr == 0) {
+        const int steps = (int)ho[2 * m];
+        if (!(ho[2 * m + 1] > 0)) {
+          cs->lmin = cs->lmax = 1.0;
+          cs->degree = 0;
+          cs->ready = true;
+          return cudaSuccess;
+        }
+        al.assign(ho.begin(), ho.begin() + steps);
+        be.assign(ho.begin() + m, ho.begin() + m + std::max(steps - 1, 0));
+      } else if (launched) {
+        // a barrier wait ran out: clear the flag and redo the steps one launch at a time
+        cudaMemsetAsync(c->error, 0, sizeof(int), s);
+        cudaMemsetAsync(c->barrier, 0, 2 * sizeof(unsigned), s);
+      }
+    }
+  }
+  if (al.empty()) {
   cudaMemsetAsync(vprev, 0, sizeof(float) * c->nV, s);
   lanczos_init<<<g, kT, 0, s>>>(*c, v, c->partials);
   cudaMemcpyAsync(hp.data(), c->partials, sizeof(double) * g, cudaMemcpyDeviceToHost, s);
@@ -823,8 +962,6 @@ cudaError_t coarse_setup(CoarseSolver* cs, const T* S, int maxDegree, double tar
     return cudaSuccess;
   }
   lanczos_scale<<<g, kT, 0, s>>>(c->nV, v, (float)(1.0 / nrm));
-  std::vector<double> al, be;
-  const int m = (int)std::min<int64_t>(30, c->nV);
   double beta = 0.0;
   for (int j = 0; j < m; ++j) {
     // one host round trip per step: alpha and |w|^2 from the same pass
@@ -844,6 +981,7 @@ cudaError_t coarse_setup(CoarseSolver* cs, const T* S, int maxDegree, double tar
     w = t;
   }
   be.resize(al.size() > 0 ? al.size() - 1 : 0);
+  }
   const double tmin = tridiag_eig(al, be, 0), tmax = tridiag_eig(al, be, (int)al.size() - 1);
   // upper bound must cover the spectrum (|p| <= 1 there keeps q(A_c) SPD);
   // the lower end may be above the true minimum: modes below it are damped less

@@ -65,6 +65,7 @@ struct CoarseDev {
   unsigned* barrier;    // [2] grid barrier of the one-launch coarse solve: count, generation
   int* error;           // set when a grid barrier wait ran out (the solve is then invalid)
   int* testHold;        // test hook, one shot: block 0 withholds its first barrier arrival
+  double* lanczosOut;   // [2*30+2] alpha, beta, step count and start norm of the one-launch Lanczos
 };
 
 // Coarse solver state: device view plus the polynomial schedule. Both coarse

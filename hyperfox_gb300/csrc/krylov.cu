@@ -277,6 +277,99 @@ __global__ void __launch_bounds__(kThreads, 6) cg_spmv_half_ell(TraceView A, con
   }
 }
 
+// The same K1 with one warp per face: CPL = 32 / NF lanes share each of the NF rows and
+// split the NF columns of every block between them (column c to lane group c % CPL), so a
+// lane's chain per block is about NF / CPL loads instead of NF and the warp streams each
+// block row by row (the lanes of one column group read NF consecutive values of a stored
+// block). The CPL partial sums of a row are joined by shuffles in a fixed order.
+template <int NF, int NBMAX>
+__global__ void __launch_bounds__(kThreads) cg_spmv_half_warp(TraceView A, const float* __restrict__ valh,
+                                                              const float* __restrict__ z,
+                                                              const float* __restrict__ pold,
+                                                              float* __restrict__ pnew, float* __restrict__ q,
+                                                              CgState* st, double* partials, int first) {
+  constexpr int CPL = 32 / NF;
+  __shared__ float xsh[kThreads / 32][NBMAX * NF];
+  if (st->done) return;
+  const float beta = first ? 0.f : (float)st->beta;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r = lane % NF, cg = lane / NF;
+  const bool used = cg < CPL;
+  float* xs = xsh[warp];
+  double pq = 0.0;
+  const int64_t warps = (int64_t)gridDim.x * (kThreads / 32);
+  for (int64_t f = (int64_t)blockIdx.x * (kThreads / 32) + warp; f < A.nFaces; f += warps) {
+    int2 e2 = make_int2(0, INT_MIN);
+    if (lane < NBMAX) e2 = __ldg(A.ell + f * NBMAX + lane);
+    int gk[NBMAX], hk[NBMAX];
+#pragma unroll
+    for (int k = 0; k < NBMAX; ++k) {
+      gk[k] = __shfl_sync(0xffffffffu, e2.x, k);
+      hk[k] = __shfl_sync(0xffffffffu, e2.y, k);
+    }
+    // p = z + beta p_old over the neighbour blocks' columns, staged per warp
+    for (int t = lane; t < NBMAX * NF; t += 32) {
+      const int k = t / NF, b = t - k * NF;
+      int g = 0, h = INT_MIN;
+#pragma unroll
+      for (int kk = 0; kk < NBMAX; ++kk)
+        if (kk == k) {
+          g = gk[kk];
+          h = hk[kk];
+        }
+      float xv = 0.f;
+      if (h != INT_MIN) {
+        const int64_t j = (int64_t)g * NF + b;
+        xv = fmaf(beta, pold[j], z[j]);
+      }
+      xs[t] = xv;
+    }
+    __syncwarp();
+    float acc = 0.f;
+    if (used) {
+#pragma unroll
+      for (int k = 0; k < NBMAX; ++k) {
+        const int h = hk[k];
+        if (h == INT_MIN) continue;
+        if (h >= 0) {
+          const float* blk = valh + (int64_t)h * NF * NF;  // entry (r, c) at r + c NF
+#pragma unroll
+          for (int c = cg; c < NF; c += CPL) acc = fmaf(__ldg(blk + r + c * NF), xs[k * NF + c], acc);
+        } else {
+          const float* blk = valh + (int64_t)(-h - 1) * NF * NF;  // transposed: (c, r) at c + r NF
+#pragma unroll
+          for (int c = cg; c < NF; c += CPL) acc = fmaf(__ldg(blk + c + r * NF), xs[k * NF + c], acc);
+        }
+      }
+    }
+    // row r's sum over its column groups, in group order
+    float y = acc;
+#pragma unroll
+    for (int j = 1; j < CPL; ++j) {
+      const float o = __shfl_sync(0xffffffffu, acc, (lane + j * NF) & 31);
+      if (cg == 0) y += o;
+    }
+    if (cg == 0) {
+      const int64_t i = f * NF + r;
+      const float pi = fmaf(beta, pold[i], z[i]);
+      pnew[i] = pi;
+      q[i] = y;
+      pq += (double)pi * (double)y;
+    }
+    __syncwarp();
+  }
+  double v[1] = {pq}, tot[1];
+  if (block_reduce_last<1>(v, partials, &st->ticket, tot) && threadIdx.x == 0) {
+    double pAp = tot[0];
+    if (!(pAp > 0.0) || !isfinite(pAp)) {
+      st->status = isfinite(pAp) ? 6 : 7;
+      st->done = 1;
+    } else {
+      st->alpha = st->rz / pAp;
+    }
+  }
+}
+
 // K1 of CG (see the file comment).
 template <typename T, int NF, int NBMAX, bool MASKED>
 __global__ void __launch_bounds__(kThreads) cg_spmv(TraceView A, const T* __restrict__ val,
@@ -872,13 +965,22 @@ struct Driver {
       return 3;
     };
     cudaError_t err;
-    const int gridF = grid_of(cg_spmv<double, NF, NBMAX, true>, kThreads);
-    const int gridF32 = grid_of(cg_spmv<float, NF, NBMAX, false>, kThreads);
-    const int gridE = grid_of(cg_spmv_half_ell<NF, NBMAX>, kThreads);
-    const int gridU = grid_of(cg_update<double, NF, 2>, kThreads);
-    const int gridS = grid_of(prepare_system<NF, NBMAX>, kThreads);
-    const int gridR1 = grid_of(cg_update_r<double, NF>, kThreads);
-    const int gridT = grid_of(tl_apply<double, NF>, kThreads);
+    // grids: the resident CTAs, but no more than the work needs (every kernel is a
+    // grid-stride loop; on small systems the extra CTAs would only add launch and
+    // reduction cost): face-slot kernels take 32 / NF faces per warp, vector kernels a
+    // trace value per thread
+    const int64_t slotThreads = ((int64_t)A.nFaces + RowCfg<NF, NBMAX>::FPW - 1) / RowCfg<NF, NBMAX>::FPW * 32;
+    auto cap = [](int g, int64_t threads) {
+      const int64_t need = (threads + kThreads - 1) / kThreads;
+      return (int)std::max<int64_t>(1, std::min<int64_t>(g, need));
+    };
+    const int gridF = cap(grid_of(cg_spmv<double, NF, NBMAX, true>, kThreads), slotThreads);
+    const int gridF32 = cap(grid_of(cg_spmv<float, NF, NBMAX, false>, kThreads), slotThreads);
+    const int gridE = cap(grid_of(cg_spmv_half_ell<NF, NBMAX>, kThreads), slotThreads);
+    const int gridU = cap(grid_of(cg_update<double, NF, 2>, kThreads), slotThreads);
+    const int gridS = cap(grid_of(prepare_system<NF, NBMAX>, kThreads), slotThreads);
+    const int gridR1 = cap(grid_of(cg_update_r<double, NF>, kThreads), n);
+    const int gridT = cap(grid_of(tl_apply<double, NF>, kThreads), slotThreads);
     double* partials = a.ws.partials;
     CgState* st = a.ws.state;
     CgState hst;
@@ -996,10 +1098,53 @@ struct Driver {
       // the iteration count stays close to FP64 CG's.
       float *r32 = a.ws.r32, *z32 = a.ws.z32, *p032 = a.ws.p032, *p132 = a.ws.p132, *q32 = a.ws.q32;
       float* y32 = a.ws.d32;
+      // launch tuner: the first mixed solve on a system layout times both FP32 operator
+      // kernels (three launches each, after one warm-up, on this system's own values; the
+      // state is cleared before each launch so that every launch runs in full) and keeps the
+      // faster one for this and later solves (*a.spmvChoice: 0 row per lane, 1 warp per face)
+      const bool ellOk = half && A.ell && A.ellWidth == NBMAX;
+      const int gridW = cap(grid_of(cg_spmv_half_warp<NF, NBMAX>, kThreads), (int64_t)A.nFaces * 32);
+      int variant = 0;
+      if (ellOk && a.spmvChoice) {
+        if (*a.spmvChoice < 0) {
+          cudaEvent_t e0, e1;
+          cudaEventCreate(&e0);
+          cudaEventCreate(&e1);
+          float best[2] = {0.f, 0.f};
+          for (int v = 0; v < 2; ++v) {
+            float tmin = 1e30f;
+            for (int rep = 0; rep < 4; ++rep) {
+              cudaMemsetAsync(st, 0, sizeof(CgState), s);
+              cudaEventRecord(e0, s);
+              if (v == 0)
+                cg_spmv_half_ell<NF, NBMAX><<<gridE, kThreads, 0, s>>>(A, a.ws.val32h, z32, p032, p132, q32, st,
+                                                                        partials, 1);
+              else
+                cg_spmv_half_warp<NF, NBMAX><<<gridW, kThreads, 0, s>>>(A, a.ws.val32h, z32, p032, p132, q32, st,
+                                                                         partials, 1);
+              cudaEventRecord(e1, s);
+              cudaEventSynchronize(e1);
+              float ms = 0.f;
+              cudaEventElapsedTime(&ms, e0, e1);
+              if (rep > 0) tmin = std::min(tmin, ms);
+            }
+            best[v] = tmin;
+          }
+          cudaEventDestroy(e0);
+          cudaEventDestroy(e1);
+          if ((err = cudaGetLastError()) != cudaSuccess) return fail(err);
+          *a.spmvChoice = best[1] < best[0] ? 1 : 0;
+          if (a.spmvTimes) {
+            a.spmvTimes[0] = best[0];
+            a.spmvTimes[1] = best[1];
+          }
+        }
+        variant = *a.spmvChoice;
+      }
       // replace the residual after every inner_rtol of FP32 reduction (two
       // decades by default); FP32 rounding bounds how far a stretch can go
       const double delta = std::min(0.5, std::max(1e-4, a.inner_rtol));
-      const int gridR = grid_of(cg_replace<NF, NBMAX, 2>, kThreads);
+      const int gridR = cap(grid_of(cg_replace<NF, NBMAX, 2>, kThreads), slotThreads);
       if (!a.use_initial_guess) set_dirichlet_start(A, a.ws.bS, x, s);
       cudaMemsetAsync(y32, 0, sizeof(float) * n, s);
       // true residual of x (and ||b||^2 of the reference rhs for the tolerance)
@@ -1057,7 +1202,10 @@ struct Driver {
             float* pold = (it & 1) ? p132 : p032;
             float* pnew = (it & 1) ? p032 : p132;
             tm->begin(K_SPMV32, s);
-            if (half && A.ell && A.ellWidth == NBMAX)
+            if (ellOk && variant == 1)
+              cg_spmv_half_warp<NF, NBMAX><<<gridW, kThreads, 0, s>>>(A, a.ws.val32h, z32, pold, pnew, q32, st,
+                                                                       partials, first ? 1 : 0);
+            else if (ellOk)
               cg_spmv_half_ell<NF, NBMAX><<<gridE, kThreads, 0, s>>>(A, a.ws.val32h, z32, pold, pnew, q32, st,
                                                                       partials, first ? 1 : 0);
             else if (half)

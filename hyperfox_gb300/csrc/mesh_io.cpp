@@ -172,6 +172,23 @@ int high_order(int dim, int order, int nLin, const double* lin, int nCells, cons
       std::array<int64_t, 3> key = {0, 0, 0};
       for (int c = 0; c < dim; ++c) key[c] = (int64_t)std::llround(x[c] / quantum);
       auto it = ids.find(key);
+      if (it == ids.end()) {
+        // the same node computed from another cell can round to a neighbouring key (its
+        // coordinates differ in the last bits and straddle a rounding boundary): look there
+        // for a node within one quantum before creating a new one
+        const int span = dim == 3 ? 27 : 9;
+        for (int o = 0; o < span && it == ids.end(); ++o) {
+          const int64_t d0 = o % 3 - 1, d1 = (o / 3) % 3 - 1, d2 = dim == 3 ? o / 9 - 1 : 0;
+          if (d0 == 0 && d1 == 0 && d2 == 0) continue;
+          const std::array<int64_t, 3> nk = {key[0] + d0, key[1] + d1, dim == 3 ? key[2] + d2 : 0};
+          auto jt = ids.find(nk);
+          if (jt == ids.end()) continue;
+          bool close = true;
+          for (int c = 0; c < dim; ++c)
+            if (std::fabs((*coords)[(size_t)jt->second * dim + c] - x[c]) > quantum) close = false;
+          if (close) it = jt;
+        }
+      }
       int id;
       if (it == ids.end()) {
         id = (int)(coords->size() / dim);

@@ -107,7 +107,8 @@ int hfx_cg_operators(hfx_ctx* ctx, int which, int precision, const double* veloc
 int hfx_test_coarse_barrier(hfx_ctx* ctx);
 
 /* Coarse solve of HFX_PC_TWOLEVEL. LEARNED applies the polynomial trained by
- * hfx_coarse_train (Chebyshev until one has been accepted). */
+ * hfx_coarse_train; until one has been accepted it applies Chebyshev of the trained degree
+ * (of the reduction target's degree when no training has run). */
 #define HFX_COARSE_CHEBYSHEV 0
 #define HFX_COARSE_LEARNED 1
 
@@ -259,6 +260,13 @@ int hfx_assembly_info(hfx_ctx* ctx, int* affine);
  * entry) for orders 1-5 (2D) / 1-3 (3D) under path 0; path 1 integrates them on the CUDA
  * cores. *tensorCores = 1 when the last mixed assembly used the tensor cores. */
 int hfx_mixed_assembly_info(hfx_ctx* ctx, int* tensorCores);
+/* Launch tuner (no counterpart in the reference): the first mixed-precision CG solve on a mesh
+ * times the two kernels of the FP32 trace operator on the system's own values (row per lane,
+ * warp per face) and keeps the faster one for that mesh. *spmvKernel: -1 not tuned yet, else
+ * the kernel chosen (0, 1); spmvMs[2]: their measured times per launch (ms). */
+int hfx_tuning_info(hfx_ctx* ctx, int* spmvKernel, float* spmvMs);
+/* Sets the choice instead: 0 or 1 fixes the kernel, -1 tunes again at the next mixed solve. */
+int hfx_set_tuning(hfx_ctx* ctx, int spmvKernel);
 /* Those FP32 blocks for a list of cells, [count][*stride]: volume rows [C_0..C_{d-1} | K_0..
  * K_{d-1} | M] of N values (row (k, i) = block k, node i), face rows [T | E | H] of Nf values
  * (T row (f, a); E, H rows (f, k, a)), then the source load f_u (N). */

@@ -95,7 +95,7 @@ def test_batch_arm_runs_on_a_stub_abi(monkeypatch):
                                                                       max_elements=400), cpu_budget=300,
                                                    desc="stub"))
     args = types.SimpleNamespace(config="stub", rtol=1e-8, precision="mixed", precond="twolevel", inner_rtol=1e-2,
-                                 coarse_rtol=0.3, warmup=1, steps=2)
+                                 coarse_rtol=0.3, coarse_degree=8, warmup=1, steps=2)
     res, B = bench.run_batch(args, 1, 0, 0)
     groups = len(B.groups)
     assert res["config"]["elements"] == B.nCells and res["config"]["problems"] == 12

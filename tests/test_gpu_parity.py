@@ -231,3 +231,25 @@ def test_mixed_assembly_refuses_fp64_exports(hfx_lib):
     ctx.assemble(precision=capi.PREC_MIXED)
     with pytest.raises(capi.HfxError):
         ctx.condensed()
+
+
+@pytest.mark.parametrize("kernel", [0, 1])
+def test_mixed_cg_both_fp32_operator_kernels(hfx_lib, kernel):
+    """Both kernels of the FP32 half-storage trace operator (row per lane, warp per face),
+    fixed through hfx_set_tuning, give the direct solution to 1e-8 with the two-level
+    mixed CG; the tuner, when left to choose, picks one of them and reports both times."""
+    from hyperfox_gb300 import capi
+    P, ctx, _ = build_pair(hfx_lib, 3, 3, 3, tau2=False, kappa="cell")
+    P.assemble()
+    ctx.assemble()
+    x_ref = P.solve_direct()
+    ctx._chk(ctx.L.hfx_set_tuning(ctx.h, kernel), "set_tuning")
+    for precond in (capi.PC_BLOCK_JACOBI, capi.PC_TWOLEVEL):
+        trace, info = ctx.solve(precision=capi.PREC_MIXED, rtol=1e-12, precond=precond)
+        assert info.status == 0
+        assert np.linalg.norm(trace - x_ref) / np.linalg.norm(x_ref) < 1e-8
+        assert ctx.tuning_info()[0] == kernel
+    ctx._chk(ctx.L.hfx_set_tuning(ctx.h, -1), "set_tuning")
+    ctx.solve(precision=capi.PREC_MIXED, rtol=1e-12, precond=capi.PC_TWOLEVEL)
+    k, ms = ctx.tuning_info()
+    assert k in (0, 1) and min(ms) > 0

@@ -87,3 +87,19 @@ def test_reference_regression_mesh_feeds_the_oracle():
     sol, _ = P.recover(x)
     exact = np.prod(np.sin(np.pi * hc[he]), axis=-1)
     assert np.abs(sol - exact).max() < 5e-3
+
+
+def test_high_order_merges_nodes_across_rounding_boundaries():
+    """Two problems of the 1024-problem batch (seed 3: problem 247, 47x47x2 triangles at p = 2,
+    and problem 68, 92x92x2 at p = 3, jittered vertices) have a shared edge node whose two
+    computations, from the two cells of the edge, round to neighbouring merge keys; the node
+    construction finds the node within one quantum there, so every cell's face nodes are the
+    face's nodes (the topology the element kernels need)."""
+    from hyperfox_gb300 import batch
+    for prob in batch.uneven_batch(count=1024, seed=3, select=[247, 68]):
+        c2f, _, faces, _ = prob.topology
+        fn = np.asarray(capi.refel(2, prob.order)["faceNodes"]).reshape(3, -1)
+        for i in range(3):
+            assert np.array_equal(np.sort(prob.cells[:, fn[i]], axis=1), np.sort(faces[c2f[:, i]], axis=1))
+        # merged means no two nodes closer than a small fraction of the mesh spacing
+        assert prob.coords.shape[0] == len(np.unique(np.round(prob.coords, 8), axis=0))
