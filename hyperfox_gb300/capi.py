@@ -504,11 +504,11 @@ class Context:
         return out
 
     def tuning_info(self):
-        """(kernel chosen for the FP32 trace operator or -1, [ms row per lane, ms warp per face])."""
+        """(kernel chosen for the FP32 trace operator or -1, [ms per launch of kernels 0..3])."""
         k = ctypes.c_int()
-        t = (ctypes.c_float * 2)()
+        t = (ctypes.c_float * 4)()
         self._chk(self.L.hfx_tuning_info(self.h, ctypes.byref(k), t), "tuning_info")
-        return k.value, [t[0], t[1]]
+        return k.value, [t[0], t[1], t[2], t[3]]
 
     def mixed_assembly_info(self):
         """1 when the last mixed assembly contracted the element blocks on the tensor cores."""
@@ -806,11 +806,11 @@ class Burgers:
         return out
 
     def tuning_info(self):
-        """(kernel chosen for the FP32 trace operator or -1, [ms row per lane, ms warp per face])."""
+        """(kernel chosen for the FP32 trace operator or -1, [ms per launch of kernels 0..3])."""
         k = ctypes.c_int()
-        t = (ctypes.c_float * 2)()
+        t = (ctypes.c_float * 4)()
         self._chk(self.L.hfx_tuning_info(self.h, ctypes.byref(k), t), "tuning_info")
-        return k.value, [t[0], t[1]]
+        return k.value, [t[0], t[1], t[2], t[3]]
 
     def mixed_assembly_info(self):
         """1 when the last mixed assembly contracted the element blocks on the tensor cores."""

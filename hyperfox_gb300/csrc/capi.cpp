@@ -204,7 +204,7 @@ struct hfx_ctx {
   // degree of the last coarse training; a learned solve without an accepted polynomial runs
   // Chebyshev of that degree (0: no training yet, the reduction target decides)
   int learnDegree = 0;
-  float spmvTimes[2] = {0.f, 0.f};
+  float spmvTimes[4] = {0.f, 0.f, 0.f, 0.f};
   int coarseMaxDeg = 64;      // degree cap of the Chebyshev coarse solve (a fixed degree when target ~ 0)
   // vector Burgers (hfx_burgers_*)
   BurgersState burgers;
@@ -1384,7 +1384,7 @@ int hfx_test_coarse_barrier(hfx_ctx* c) {
 }
 
 int hfx_set_tuning(hfx_ctx* c, int spmvKernel) {
-  if (!c || spmvKernel < -1 || spmvKernel > 1) return HFX_ERR_ARG;
+  if (!c || spmvKernel < -1 || spmvKernel > 3) return HFX_ERR_ARG;
   c->spmvChoice = spmvKernel;
   return HFX_OK;
 }
@@ -1392,10 +1392,8 @@ int hfx_set_tuning(hfx_ctx* c, int spmvKernel) {
 int hfx_tuning_info(hfx_ctx* c, int* spmvKernel, float* spmvMs) {
   if (!c) return HFX_ERR_ARG;
   if (spmvKernel) *spmvKernel = c->spmvChoice;
-  if (spmvMs) {
-    spmvMs[0] = c->spmvTimes[0];
-    spmvMs[1] = c->spmvTimes[1];
-  }
+  if (spmvMs)
+    for (int k = 0; k < 4; ++k) spmvMs[k] = c->spmvTimes[k];
   return HFX_OK;
 }
 

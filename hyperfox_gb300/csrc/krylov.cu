@@ -212,7 +212,15 @@ __global__ void __launch_bounds__(kThreads) cg_spmv_half(TraceView A, const floa
 // pointer has to arrive before the gather and the value loads can start; the
 // products are the same, in the same order. At most six 256-thread blocks per
 // SM keep the register count of the row-pointer version.
-template <int NF, int NBMAX>
+//
+// PAIRED: a block read transposed gives each lane NF consecutive values (its column of the
+// stored block), which are then loaded as NF/2 float2 pairs (the block's start is 16-byte
+// aligned and the column's 8-byte aligned): half the load instructions and half the L1
+// sector requests of the scalar loads, whose lanes touch one sector each.
+// WIDE (NF = 2 mod 4): the column starts 16-byte aligned for even a and 8-byte aligned for odd
+// a, so even lanes load float4 pairs then one float2 and odd lanes one float2 then float4s:
+// fewer sector requests again, at the cost of the two lane halves taking separate paths.
+template <int NF, int NBMAX, bool PAIRED = false, bool WIDE = false>
 __global__ void __launch_bounds__(kThreads, 6) cg_spmv_half_ell(TraceView A, const float* __restrict__ valh,
                                                                 const float* __restrict__ z,
                                                                 const float* __restrict__ pold,
@@ -251,8 +259,44 @@ __global__ void __launch_bounds__(kThreads, 6) cg_spmv_half_ell(TraceView A, con
           const float* blk = h >= 0 ? valh + (int64_t)h * NF * NF + a : valh + (int64_t)(-h - 1) * NF * NF + (int64_t)a * NF;
           const int sb = h >= 0 ? NF : 1;
           float v[NF];
+          if (WIDE && (NF % 4 == 2) && h < 0) {
+            if ((a & 1) == 0) {
 #pragma unroll
-          for (int b = 0; b < NF; ++b) v[b] = __ldg(blk + b * sb);
+              for (int b = 0; b + 4 <= NF - 2; b += 4) {
+                const float4 w = __ldg(reinterpret_cast<const float4*>(blk + b));
+                v[b] = w.x;
+                v[b + 1] = w.y;
+                v[b + 2] = w.z;
+                v[b + 3] = w.w;
+              }
+              const float2 w2 = __ldg(reinterpret_cast<const float2*>(blk + NF - 2));
+              v[NF - 2] = w2.x;
+              v[NF - 1] = w2.y;
+            } else {
+              const float2 w2 = __ldg(reinterpret_cast<const float2*>(blk));
+              v[0] = w2.x;
+              v[1] = w2.y;
+#pragma unroll
+              for (int b = 2; b + 4 <= NF; b += 4) {
+                const float4 w = __ldg(reinterpret_cast<const float4*>(blk + b));
+                v[b] = w.x;
+                v[b + 1] = w.y;
+                v[b + 2] = w.z;
+                v[b + 3] = w.w;
+              }
+            }
+          } else if (PAIRED && (NF % 2 == 0) && h < 0) {
+            const float2* b2 = reinterpret_cast<const float2*>(blk);
+#pragma unroll
+            for (int b = 0; b < NF / 2; ++b) {
+              const float2 w = __ldg(b2 + b);
+              v[2 * b] = w.x;
+              v[2 * b + 1] = w.y;
+            }
+          } else {
+#pragma unroll
+            for (int b = 0; b < NF; ++b) v[b] = __ldg(blk + b * sb);
+          }
 #pragma unroll
           for (int b = 0; b < NF; ++b) acc = fmaf(v[b], xs[k * NF + b], acc);
         }
@@ -1098,20 +1142,23 @@ struct Driver {
       // the iteration count stays close to FP64 CG's.
       float *r32 = a.ws.r32, *z32 = a.ws.z32, *p032 = a.ws.p032, *p132 = a.ws.p132, *q32 = a.ws.q32;
       float* y32 = a.ws.d32;
-      // launch tuner: the first mixed solve on a system layout times both FP32 operator
+      // launch tuner: the first mixed solve on a system layout times the FP32 operator
       // kernels (three launches each, after one warm-up, on this system's own values; the
       // state is cleared before each launch so that every launch runs in full) and keeps the
-      // faster one for this and later solves (*a.spmvChoice: 0 row per lane, 1 warp per face)
+      // fastest for this and later solves (*a.spmvChoice: 0 row per lane, 1 warp per face,
+      // 2 row per lane with paired loads of the transposed blocks, 3 the same with 16-byte loads
+      // where NF = 2 mod 4)
       const bool ellOk = half && A.ell && A.ellWidth == NBMAX;
       const int gridW = cap(grid_of(cg_spmv_half_warp<NF, NBMAX>, kThreads), (int64_t)A.nFaces * 32);
+      const int gridP = cap(grid_of(cg_spmv_half_ell<NF, NBMAX, true>, kThreads), slotThreads);
       int variant = 0;
       if (ellOk && a.spmvChoice) {
         if (*a.spmvChoice < 0) {
           cudaEvent_t e0, e1;
           cudaEventCreate(&e0);
           cudaEventCreate(&e1);
-          float best[2] = {0.f, 0.f};
-          for (int v = 0; v < 2; ++v) {
+          float best[4] = {0.f, 0.f, 0.f, 1e30f};
+          for (int v = 0; v < ((NF % 4 == 2) ? 4 : 3); ++v) {
             float tmin = 1e30f;
             for (int rep = 0; rep < 4; ++rep) {
               cudaMemsetAsync(st, 0, sizeof(CgState), s);
@@ -1119,9 +1166,15 @@ struct Driver {
               if (v == 0)
                 cg_spmv_half_ell<NF, NBMAX><<<gridE, kThreads, 0, s>>>(A, a.ws.val32h, z32, p032, p132, q32, st,
                                                                         partials, 1);
-              else
+              else if (v == 1)
                 cg_spmv_half_warp<NF, NBMAX><<<gridW, kThreads, 0, s>>>(A, a.ws.val32h, z32, p032, p132, q32, st,
                                                                          partials, 1);
+              else if (v == 2)
+                cg_spmv_half_ell<NF, NBMAX, true><<<gridP, kThreads, 0, s>>>(A, a.ws.val32h, z32, p032, p132, q32,
+                                                                              st, partials, 1);
+              else
+                cg_spmv_half_ell<NF, NBMAX, true, true><<<gridP, kThreads, 0, s>>>(A, a.ws.val32h, z32, p032, p132,
+                                                                                    q32, st, partials, 1);
               cudaEventRecord(e1, s);
               cudaEventSynchronize(e1);
               float ms = 0.f;
@@ -1133,11 +1186,12 @@ struct Driver {
           cudaEventDestroy(e0);
           cudaEventDestroy(e1);
           if ((err = cudaGetLastError()) != cudaSuccess) return fail(err);
-          *a.spmvChoice = best[1] < best[0] ? 1 : 0;
-          if (a.spmvTimes) {
-            a.spmvTimes[0] = best[0];
-            a.spmvTimes[1] = best[1];
-          }
+          int bestK = 0;
+          for (int v = 1; v < 4; ++v)
+            if (best[v] < best[bestK]) bestK = v;
+          *a.spmvChoice = bestK;
+          if (a.spmvTimes)
+            for (int v = 0; v < 4; ++v) a.spmvTimes[v] = best[v] < 1e29f ? best[v] : 0.f;
         }
         variant = *a.spmvChoice;
       }
@@ -1205,6 +1259,12 @@ struct Driver {
             if (ellOk && variant == 1)
               cg_spmv_half_warp<NF, NBMAX><<<gridW, kThreads, 0, s>>>(A, a.ws.val32h, z32, pold, pnew, q32, st,
                                                                        partials, first ? 1 : 0);
+            else if (ellOk && variant == 2)
+              cg_spmv_half_ell<NF, NBMAX, true><<<gridP, kThreads, 0, s>>>(A, a.ws.val32h, z32, pold, pnew, q32, st,
+                                                                            partials, first ? 1 : 0);
+            else if (ellOk && variant == 3)
+              cg_spmv_half_ell<NF, NBMAX, true, true><<<gridP, kThreads, 0, s>>>(A, a.ws.val32h, z32, pold, pnew, q32,
+                                                                                  st, partials, first ? 1 : 0);
             else if (ellOk)
               cg_spmv_half_ell<NF, NBMAX><<<gridE, kThreads, 0, s>>>(A, a.ws.val32h, z32, pold, pnew, q32, st,
                                                                       partials, first ? 1 : 0);
