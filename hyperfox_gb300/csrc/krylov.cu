@@ -126,6 +126,25 @@ __device__ __forceinline__ void gather_x(const TraceView& A, int64_t b0, int nb,
   }
 }
 
+// gather_x from the fixed-width rows: the (block column, block location) pairs of the face
+// come from one row of the ELL table, so the x loads need no row pointer first (the
+// residual replacement's value loads still take the row pointer, in parallel).
+template <typename T, int NF, int NBMAX>
+__device__ __forceinline__ void gather_x_ell(const TraceView& A, int64_t f, bool rowBnd, int a,
+                                             const T* __restrict__ x, T* xs) {
+  int2 e2[NBMAX];
+#pragma unroll
+  for (int k = 0; k < NBMAX; ++k) e2[k] = __ldg(A.ell + f * NBMAX + k);
+#pragma unroll
+  for (int k = 0; k < NBMAX; ++k) {
+    if (e2[k].y == INT_MIN) continue;
+    const int g = e2[k].x;
+    T v = x[(int64_t)g * NF + a];
+    if (rowBnd || A.isBnd[g]) v = T(0);
+    xs[k * NF + a] = v;
+  }
+}
+
 // One row of the face block-row: sum over the nb neighbour blocks.
 template <typename T, int NF>
 __device__ __forceinline__ T row_dot(const T* __restrict__ val, int64_t b0, int nb, int a, const T* xs) {
@@ -829,7 +848,10 @@ __global__ void __launch_bounds__(kThreads) cg_replace(TraceView A, const double
     const int nb = act ? (int)(A.browptr[f + 1] - b0) : 0;
     const bool rowBnd = act && A.isBnd[f];
     double* xs = laneUsed ? xsh[warp][slot] : nullptr;
-    if (act) gather_x<double, NF, NBMAX, true, false>(A, b0, nb, rowBnd, a, 0.0, x, x, xs);
+    if (act) {
+      if (A.ell && A.ellWidth == NBMAX) gather_x_ell<double, NF, NBMAX>(A, f, rowBnd, a, x, xs);
+      else gather_x<double, NF, NBMAX, true, false>(A, b0, nb, rowBnd, a, 0.0, x, x, xs);
+    }
     __syncwarp();
     float ra = 0.f;
     if (act) bb += bref[f * NF + a] * bref[f * NF + a];

@@ -63,7 +63,7 @@ constexpr int64_t kScratchDoubles = kOffCheck + 8;
 // symmetric to the rounding of its element matrices, about 1e-15)
 constexpr double kSymTol = 1e-10;
 
-__device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
+static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
 
 struct NoallocSys {
   int64_t nFaces;
