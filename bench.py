@@ -254,6 +254,8 @@ def run_ours(args, world, rank, local):
     L = ctx.L
     if args.assembly_path:
         ctx._chk(L.hfx_set_assembly_path(ctx.h, args.assembly_path), "assembly_path")
+    if args.spmv_kernel >= 0:
+        ctx._chk(L.hfx_set_tuning(ctx.h, args.spmv_kernel), "set_tuning")
     prec = capi.PREC_FP64 if args.precision == "fp64" else capi.PREC_MIXED
     pc = capi.PC_TWOLEVEL if args.precond == "twolevel" else capi.PC_BLOCK_JACOBI
     opts = capi.solve_opts(precision=prec, rtol=args.rtol, precond=pc, maxits=200000,
@@ -442,8 +444,8 @@ def run_ours(args, world, rank, local):
         launches = min(kt[key][0], iters * args.steps) if iters else kt[key][0]
         avg_ms = kt[key][1] / max(1, launches)
         achieved = alg / (avg_ms / 1e3) / 1e9
-        kname = {1: "cg_spmv_half_warp<float>", 2: "cg_spmv_half_ell<float, paired>",
-                 3: "cg_spmv_half_ell<float, wide>"}.get(
+        kname = {1: "cg_spmv_half_tma<float>", 2: "cg_spmv_half_ell<float, paired>",
+                 3: "cg_spmv_half_ell<float, paired, float4 x>"}.get(
             ctx.tuning_info()[0], "cg_spmv_half_ell<float>") if sv == 4 else "cg_spmv<double>"
         return dict(bound="hbm", kernel=kname,
                     achieved=round(achieved, 1), peak=hbm, unit="GB/s", frac=round(achieved / hbm, 4),
@@ -1047,6 +1049,10 @@ def main():
                          "tensor-core contractions in the mixed assembly), 1 quadrature on the CUDA cores")
     ap.add_argument("--assembly-only", action="store_true",
                     help="time the element assembly (+ condensation + scatter) alone")
+    ap.add_argument("--spmv-kernel", type=int, default=-1, choices=[-1, 0, 1, 2, 3],
+                    help="FP32 trace operator kernel (hfx_set_tuning): -1 timed per system by the launch "
+                         "tuner, else 0 row per lane, 1 blocks staged by bulk copies, 2 paired loads, "
+                         "3 paired loads and float4 reads of the gathered x")
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

@@ -236,16 +236,18 @@ __global__ void __launch_bounds__(kThreads) cg_spmv_half(TraceView A, const floa
 // stored block), which are then loaded as NF/2 float2 pairs (the block's start is 16-byte
 // aligned and the column's 8-byte aligned): half the load instructions and half the L1
 // sector requests of the scalar loads, whose lanes touch one sector each.
-// WIDE (NF = 2 mod 4): the column starts 16-byte aligned for even a and 8-byte aligned for odd
-// a, so even lanes load float4 pairs then one float2 and odd lanes one float2 then float4s:
-// fewer sector requests again, at the cost of the two lane halves taking separate paths.
-template <int NF, int NBMAX, bool PAIRED = false, bool WIDE = false>
+// XV: the gathered x of each block is stored with a row of NF rounded up to a multiple of
+// four and read back as float4s: a quarter of the shared-memory wavefronts of the scalar
+// reads (those wavefronts share the L1 data pipe with the value loads, which bound the
+// kernel). The products and their order do not change.
+template <int NF, int NBMAX, bool PAIRED = false, bool XV = false>
 __global__ void __launch_bounds__(kThreads, 6) cg_spmv_half_ell(TraceView A, const float* __restrict__ valh,
                                                                 const float* __restrict__ z,
                                                                 const float* __restrict__ pold,
                                                                 float* __restrict__ pnew, float* __restrict__ q,
                                                                 CgState* st, double* partials, int first) {
-  __shared__ float xsh[kThreads / 32][RowCfg<NF, NBMAX>::FPW][RowCfg<NF, NBMAX>::NPOS];
+  constexpr int XR = XV ? (NF + 3) / 4 * 4 : NF;  // stride of a block's gathered x
+  __shared__ __align__(16) float xsh[kThreads / 32][RowCfg<NF, NBMAX>::FPW][NBMAX * XR];
   if (st->done) return;
   const float beta = first ? 0.f : (float)st->beta;
   HFX_FACE_SLOTS(NF)
@@ -264,7 +266,7 @@ __global__ void __launch_bounds__(kThreads, 6) cg_spmv_half_ell(TraceView A, con
         hh[k] = e2.y;
         if (e2.y != INT_MIN) {
           const int64_t j = (int64_t)e2.x * NF + a;
-          xs[k * NF + a] = fmaf(beta, pold[j], z[j]);
+          xs[k * XR + a] = fmaf(beta, pold[j], z[j]);
         }
       }
     }
@@ -278,33 +280,7 @@ __global__ void __launch_bounds__(kThreads, 6) cg_spmv_half_ell(TraceView A, con
           const float* blk = h >= 0 ? valh + (int64_t)h * NF * NF + a : valh + (int64_t)(-h - 1) * NF * NF + (int64_t)a * NF;
           const int sb = h >= 0 ? NF : 1;
           float v[NF];
-          if (WIDE && (NF % 4 == 2) && h < 0) {
-            if ((a & 1) == 0) {
-#pragma unroll
-              for (int b = 0; b + 4 <= NF - 2; b += 4) {
-                const float4 w = __ldg(reinterpret_cast<const float4*>(blk + b));
-                v[b] = w.x;
-                v[b + 1] = w.y;
-                v[b + 2] = w.z;
-                v[b + 3] = w.w;
-              }
-              const float2 w2 = __ldg(reinterpret_cast<const float2*>(blk + NF - 2));
-              v[NF - 2] = w2.x;
-              v[NF - 1] = w2.y;
-            } else {
-              const float2 w2 = __ldg(reinterpret_cast<const float2*>(blk));
-              v[0] = w2.x;
-              v[1] = w2.y;
-#pragma unroll
-              for (int b = 2; b + 4 <= NF; b += 4) {
-                const float4 w = __ldg(reinterpret_cast<const float4*>(blk + b));
-                v[b] = w.x;
-                v[b + 1] = w.y;
-                v[b + 2] = w.z;
-                v[b + 3] = w.w;
-              }
-            }
-          } else if (PAIRED && (NF % 2 == 0) && h < 0) {
+          if (PAIRED && (NF % 2 == 0) && h < 0) {
             const float2* b2 = reinterpret_cast<const float2*>(blk);
 #pragma unroll
             for (int b = 0; b < NF / 2; ++b) {
@@ -316,8 +292,23 @@ __global__ void __launch_bounds__(kThreads, 6) cg_spmv_half_ell(TraceView A, con
 #pragma unroll
             for (int b = 0; b < NF; ++b) v[b] = __ldg(blk + b * sb);
           }
+          if (XV) {
+            float xv[XR];
+            const float4* x4 = reinterpret_cast<const float4*>(xs + k * XR);
 #pragma unroll
-          for (int b = 0; b < NF; ++b) acc = fmaf(v[b], xs[k * NF + b], acc);
+            for (int c = 0; c < XR / 4; ++c) {
+              const float4 w = x4[c];
+              xv[4 * c] = w.x;
+              xv[4 * c + 1] = w.y;
+              xv[4 * c + 2] = w.z;
+              xv[4 * c + 3] = w.w;
+            }
+#pragma unroll
+            for (int b = 0; b < NF; ++b) acc = fmaf(v[b], xv[b], acc);
+          } else {
+#pragma unroll
+            for (int b = 0; b < NF; ++b) acc = fmaf(v[b], xs[k * XR + b], acc);
+          }
         }
       }
       const int64_t i = f * NF + a;
@@ -340,97 +331,246 @@ __global__ void __launch_bounds__(kThreads, 6) cg_spmv_half_ell(TraceView A, con
   }
 }
 
-// The same K1 with one warp per face: CPL = 32 / NF lanes share each of the NF rows and
-// split the NF columns of every block between them (column c to lane group c % CPL), so a
-// lane's chain per block is about NF / CPL loads instead of NF and the warp streams each
-// block row by row (the lanes of one column group read NF consecutive values of a stored
-// block). The CPL partial sums of a row are joined by shuffles in a fixed order.
+// The same K1 with the blocks staged in shared memory by the copy engine. The values of a
+// face group (FPW faces, NBMAX blocks each, NF x NF floats per block) are fetched by
+// cp.async.bulk, one 16-byte-aligned copy per block, completing on a per-warp mbarrier.
+// STAGES = 2: each warp keeps two groups in flight (while it computes one group from
+// shared memory the next group's blocks are being copied), four warps per CTA; STAGES = 1:
+// one group per warp, eight warps per CTA, the other warps cover the copy latency (both
+// fit three CTAs per SM at NF = 10). The value stream then never goes
+// through the L1 tag stage (whose sector lookups, two to three per value byte for the
+// transposed reads, bound the load-based kernels), and the bytes in flight do not depend
+// on registers. The x gather, the products and their order are those of
+// cg_spmv_half_ell, so q is the same. Needs NF even (16-byte block size).
+// Every wait on an mbarrier is bounded: a wait that runs out waits (bounded) for the
+// warp's other copies, sets status HFX_ERR_CUDA and stops the solve.
+constexpr int kTmaStages = 1;
+constexpr uint32_t kTmaWait = 1u << 22;  // mbarrier polls before a wait is abandoned
+
+template <int NF, int NBMAX, int STAGES = kTmaStages>
+struct TmaCfg {
+  static constexpr int WARPS = STAGES == 2 ? 4 : 8;
+  static constexpr int THREADS = 32 * WARPS;
+  static constexpr int FPW = 32 / NF;
+  static constexpr int NBLK = FPW * NBMAX;     // blocks staged per face group
+  static constexpr int BLK = NF * NF;          // floats per block
+  static constexpr int NFP = (NF + 3) / 4 * 4;  // gathered x per block, padded for float4 reads
+  static constexpr int BUF = NBLK * BLK;       // floats per stage
+  static constexpr int XS = FPW * NBMAX * NFP;
+  static constexpr int NCH = (NBLK + 31) / 32;  // copy rounds of 32 lanes
+  static constexpr int WARP_BYTES = (STAGES * BUF + XS) * 4 + 16;
+  static constexpr int CTA_BYTES = WARP_BYTES * WARPS;
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// all lanes poll; the answer is made warp-uniform (a lane that gave up fails the warp)
+__device__ __forceinline__ bool tma_wait(uint32_t bar, uint32_t parity) {
+  uint32_t done = 0;
+  for (uint32_t it = 0; it < kTmaWait && !done; ++it)
+    asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                 : "=r"(done)
+                 : "r"(bar), "r"(parity)
+                 : "memory");
+  return __all_sync(0xffffffffu, done != 0);
+}
+
+// Copies of the blocks of face group g into buf: lane t takes block t (face t / NBMAX of the
+// group, slot t % NBMAX); the byte count is announced on the mbarrier before any copy starts.
 template <int NF, int NBMAX>
-__global__ void __launch_bounds__(kThreads) cg_spmv_half_warp(TraceView A, const float* __restrict__ valh,
-                                                              const float* __restrict__ z,
-                                                              const float* __restrict__ pold,
-                                                              float* __restrict__ pnew, float* __restrict__ q,
-                                                              CgState* st, double* partials, int first) {
-  constexpr int CPL = 32 / NF;
-  __shared__ float xsh[kThreads / 32][NBMAX * NF];
+__device__ __forceinline__ void tma_issue_group(const TraceView& A, const float* __restrict__ valh, int64_t g,
+                                                float* buf, uint32_t bar, int lane) {
+  using C = TmaCfg<NF, NBMAX>;
+  int hs[C::NCH];
+  uint32_t nblk = 0;
+#pragma unroll
+  for (int c = 0; c < C::NCH; ++c) {
+    const int t = c * 32 + lane;
+    int h = INT_MIN;
+    if (t < C::NBLK) {
+      const int64_t f = g * C::FPW + t / NBMAX;
+      if (f < A.nFaces) h = __ldg(A.ell + f * NBMAX + t % NBMAX).y;
+    }
+    hs[c] = h;
+    nblk += __popc(__ballot_sync(0xffffffffu, h != INT_MIN));
+  }
+  if (lane == 0)
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(nblk * C::BLK * 4u)
+                 : "memory");
+  __syncwarp();
+#pragma unroll
+  for (int c = 0; c < C::NCH; ++c) {
+    const int h = hs[c];
+    if (h != INT_MIN) {
+      const int t = c * 32 + lane;
+      const float* src = valh + (int64_t)(h >= 0 ? h : -h - 1) * C::BLK;
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                       smem_addr(buf + t * C::BLK)),
+                   "l"(src), "r"((uint32_t)(C::BLK * 4)), "r"(bar)
+                   : "memory");
+    }
+  }
+}
+
+template <int NF, int NBMAX, int STAGES = kTmaStages>
+__global__ void __launch_bounds__(TmaCfg<NF, NBMAX, STAGES>::THREADS)
+    cg_spmv_half_tma(TraceView A, const float* __restrict__ valh,
+                                                                const float* __restrict__ z,
+                                                                const float* __restrict__ pold,
+                                                                float* __restrict__ pnew, float* __restrict__ q,
+                                                                CgState* st, double* partials, int first) {
+  static_assert(NF % 2 == 0, "blocks of 16-byte multiples only");
+  using C = TmaCfg<NF, NBMAX, STAGES>;
+  constexpr int FPW = C::FPW, NFP = C::NFP;
+  extern __shared__ __align__(16) unsigned char tma_smem[];
   if (st->done) return;
-  const float beta = first ? 0.f : (float)st->beta;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int r = lane % NF, cg = lane / NF;
-  const bool used = cg < CPL;
-  float* xs = xsh[warp];
+  float* buf0 = reinterpret_cast<float*>(tma_smem + warp * C::WARP_BYTES);
+  float* buf1 = buf0 + (STAGES == 2 ? C::BUF : 0);
+  float* xsw = buf0 + STAGES * C::BUF;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(xsw + C::XS);
+  const uint32_t bar0 = smem_addr(&bars[0]), bar1 = smem_addr(&bars[1]);
+  if (lane == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar1));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncwarp();
+  const float beta = first ? 0.f : (float)st->beta;
+  const int slot = lane / NF, a = lane % NF;
+  const bool laneUsed = slot < FPW;
+  float* xs = xsw + (laneUsed ? slot : 0) * NBMAX * NFP;
+  const int64_t nGroups = ((int64_t)A.nFaces + FPW - 1) / FPW;
+  const int64_t warps = (int64_t)gridDim.x * C::WARPS;
+  int64_t g = (int64_t)blockIdx.x * C::WARPS + warp;
   double pq = 0.0;
-  const int64_t warps = (int64_t)gridDim.x * (kThreads / 32);
-  for (int64_t f = (int64_t)blockIdx.x * (kThreads / 32) + warp; f < A.nFaces; f += warps) {
-    int2 e2 = make_int2(0, INT_MIN);
-    if (lane < NBMAX) e2 = __ldg(A.ell + f * NBMAX + lane);
-    int gk[NBMAX], hk[NBMAX];
-#pragma unroll
-    for (int k = 0; k < NBMAX; ++k) {
-      gk[k] = __shfl_sync(0xffffffffu, e2.x, k);
-      hk[k] = __shfl_sync(0xffffffffu, e2.y, k);
+  bool bad = false;
+  uint32_t u = 0;
+  if (STAGES == 2 && g < nGroups) tma_issue_group<NF, NBMAX>(A, valh, g, buf0, bar0, lane);
+  for (; g < nGroups; g += warps, ++u) {
+    const int stg = STAGES == 2 ? (int)(u & 1) : 0;
+    const float* buf = stg ? buf1 : buf0;
+    const uint32_t bar = stg ? bar1 : bar0;
+    // the buffer about to be filled was last read by an earlier group (generic loads,
+    // finished at its __syncwarp): order those reads before the copy engine's writes
+    if (STAGES == 1) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      tma_issue_group<NF, NBMAX>(A, valh, g, buf0, bar0, lane);
+    } else if (g + warps < nGroups) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      tma_issue_group<NF, NBMAX>(A, valh, g + warps, stg ? buf0 : buf1, stg ? bar0 : bar1, lane);
     }
-    // p = z + beta p_old over the neighbour blocks' columns, staged per warp
-    for (int t = lane; t < NBMAX * NF; t += 32) {
-      const int k = t / NF, b = t - k * NF;
-      int g = 0, h = INT_MIN;
+    const int64_t f = g * FPW + slot;
+    const bool act = laneUsed && f < A.nFaces;
+    int hh[NBMAX];
 #pragma unroll
-      for (int kk = 0; kk < NBMAX; ++kk)
-        if (kk == k) {
-          g = gk[kk];
-          h = hk[kk];
-        }
-      float xv = 0.f;
-      if (h != INT_MIN) {
-        const int64_t j = (int64_t)g * NF + b;
-        xv = fmaf(beta, pold[j], z[j]);
-      }
-      xs[t] = xv;
-    }
-    __syncwarp();
-    float acc = 0.f;
-    if (used) {
+    for (int k = 0; k < NBMAX; ++k) hh[k] = INT_MIN;
+    if (act) {
+      const int2* row = A.ell + f * NBMAX;
 #pragma unroll
       for (int k = 0; k < NBMAX; ++k) {
-        const int h = hk[k];
-        if (h == INT_MIN) continue;
-        if (h >= 0) {
-          const float* blk = valh + (int64_t)h * NF * NF;  // entry (r, c) at r + c NF
-#pragma unroll
-          for (int c = cg; c < NF; c += CPL) acc = fmaf(__ldg(blk + r + c * NF), xs[k * NF + c], acc);
-        } else {
-          const float* blk = valh + (int64_t)(-h - 1) * NF * NF;  // transposed: (c, r) at c + r NF
-#pragma unroll
-          for (int c = cg; c < NF; c += CPL) acc = fmaf(__ldg(blk + c + r * NF), xs[k * NF + c], acc);
+        const int2 e2 = __ldg(row + k);
+        hh[k] = e2.y;
+        if (e2.y != INT_MIN) {
+          const int64_t j = (int64_t)e2.x * NF + a;
+          xs[k * NFP + a] = fmaf(beta, pold[j], z[j]);
         }
       }
     }
-    // row r's sum over its column groups, in group order
-    float y = acc;
-#pragma unroll
-    for (int j = 1; j < CPL; ++j) {
-      const float o = __shfl_sync(0xffffffffu, acc, (lane + j * NF) & 31);
-      if (cg == 0) y += o;
+    __syncwarp();
+    if (!tma_wait(bar, STAGES == 2 ? (u >> 1) & 1u : u & 1u)) {
+      bad = true;
+      if (STAGES == 2 && g + warps < nGroups) tma_wait(stg ? bar0 : bar1, ((u + 1) >> 1) & 1u);
+      break;
     }
-    if (cg == 0) {
-      const int64_t i = f * NF + r;
+    if (act) {
+      float acc = 0.f;
+#pragma unroll
+      for (int k = 0; k < NBMAX; ++k) {
+        const int h = hh[k];
+        if (h != INT_MIN) {
+          const float* blk = buf + (slot * NBMAX + k) * C::BLK;
+          float v[NF], xv[NFP];
+          if (h >= 0) {
+#pragma unroll
+            for (int b = 0; b < NF; ++b) v[b] = blk[b * NF + a];
+          } else {
+            const float2* b2 = reinterpret_cast<const float2*>(blk + a * NF);
+#pragma unroll
+            for (int b = 0; b < NF / 2; ++b) {
+              const float2 w = b2[b];
+              v[2 * b] = w.x;
+              v[2 * b + 1] = w.y;
+            }
+          }
+          const float4* x4 = reinterpret_cast<const float4*>(xs + k * NFP);
+#pragma unroll
+          for (int c = 0; c < NFP / 4; ++c) {
+            const float4 w = x4[c];
+            xv[4 * c] = w.x;
+            xv[4 * c + 1] = w.y;
+            xv[4 * c + 2] = w.z;
+            xv[4 * c + 3] = w.w;
+          }
+#pragma unroll
+          for (int b = 0; b < NF; ++b) acc = fmaf(v[b], xv[b], acc);
+        }
+      }
+      const int64_t i = f * NF + a;
       const float pi = fmaf(beta, pold[i], z[i]);
       pnew[i] = pi;
-      q[i] = y;
-      pq += (double)pi * (double)y;
+      q[i] = acc;
+      pq += (double)pi * (double)acc;
     }
     __syncwarp();
   }
+  // (done is set by the last block: a block that has not started yet must still take its ticket)
+  if (bad && lane == 0) st->status = 3;  // HFX_ERR_CUDA: a block copy did not arrive
   double v[1] = {pq}, tot[1];
   if (block_reduce_last<1>(v, partials, &st->ticket, tot) && threadIdx.x == 0) {
     double pAp = tot[0];
-    if (!(pAp > 0.0) || !isfinite(pAp)) {
+    if (st->status != 0) {
+      st->done = 1;
+    } else if (!(pAp > 0.0) || !isfinite(pAp)) {
       st->status = isfinite(pAp) ? 6 : 7;
       st->done = 1;
     } else {
       st->alpha = st->rz / pAp;
     }
   }
+}
+
+// Grid of cg_spmv_half_tma (every CTA resident, no more than the face groups need); 0 where
+// the kernel does not apply (NF odd) or cannot be resident.
+template <int NF, int NBMAX>
+int tma_grid(int64_t nFaces) {
+  if constexpr (NF % 2 != 0) {
+    return 0;
+  } else {
+    using C = TmaCfg<NF, NBMAX>;
+    int dev = 0, nsm = 0, perSM = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaFuncSetAttribute(cg_spmv_half_tma<NF, NBMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             C::CTA_BYTES) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, cg_spmv_half_tma<NF, NBMAX>, C::THREADS,
+                                                      C::CTA_BYTES) != cudaSuccess ||
+        perSM < 1) {
+      cudaGetLastError();
+      return 0;
+    }
+    const int64_t groups = (nFaces + C::FPW - 1) / C::FPW;
+    const int64_t need = (groups + C::WARPS - 1) / C::WARPS;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)nsm * perSM));
+  }
+}
+
+template <int NF, int NBMAX>
+void launch_spmv_tma(int grid, cudaStream_t s, const TraceView& A, const float* valh, const float* z,
+                     const float* pold, float* pnew, float* q, CgState* st, double* partials, int first) {
+  if constexpr (NF % 2 == 0)
+    cg_spmv_half_tma<NF, NBMAX><<<grid, TmaCfg<NF, NBMAX>::THREADS, TmaCfg<NF, NBMAX>::CTA_BYTES, s>>>(
+        A, valh, z, pold, pnew, q, st, partials, first);
 }
 
 // K1 of CG (see the file comment).
@@ -1167,11 +1307,11 @@ struct Driver {
       // launch tuner: the first mixed solve on a system layout times the FP32 operator
       // kernels (three launches each, after one warm-up, on this system's own values; the
       // state is cleared before each launch so that every launch runs in full) and keeps the
-      // fastest for this and later solves (*a.spmvChoice: 0 row per lane, 1 warp per face,
-      // 2 row per lane with paired loads of the transposed blocks, 3 the same with 16-byte loads
-      // where NF = 2 mod 4)
+      // fastest for this and later solves (*a.spmvChoice: 0 row per lane, 1 blocks staged in
+      // shared memory by bulk copies (NF even; elsewhere kernel 0 runs), 2 row per lane with
+      // paired loads of the transposed blocks, 3 the same with the gathered x read as float4s)
       const bool ellOk = half && A.ell && A.ellWidth == NBMAX;
-      const int gridW = cap(grid_of(cg_spmv_half_warp<NF, NBMAX>, kThreads), (int64_t)A.nFaces * 32);
+      const int gridTma = tma_grid<NF, NBMAX>(A.nFaces);
       const int gridP = cap(grid_of(cg_spmv_half_ell<NF, NBMAX, true>, kThreads), slotThreads);
       int variant = 0;
       if (ellOk && a.spmvChoice) {
@@ -1179,8 +1319,9 @@ struct Driver {
           cudaEvent_t e0, e1;
           cudaEventCreate(&e0);
           cudaEventCreate(&e1);
-          float best[4] = {0.f, 0.f, 0.f, 1e30f};
-          for (int v = 0; v < ((NF % 4 == 2) ? 4 : 3); ++v) {
+          float best[4] = {0.f, 1e30f, 0.f, 0.f};
+          for (int v = 0; v < 4; ++v) {
+            if (v == 1 && gridTma == 0) continue;
             float tmin = 1e30f;
             for (int rep = 0; rep < 4; ++rep) {
               cudaMemsetAsync(st, 0, sizeof(CgState), s);
@@ -1189,8 +1330,7 @@ struct Driver {
                 cg_spmv_half_ell<NF, NBMAX><<<gridE, kThreads, 0, s>>>(A, a.ws.val32h, z32, p032, p132, q32, st,
                                                                         partials, 1);
               else if (v == 1)
-                cg_spmv_half_warp<NF, NBMAX><<<gridW, kThreads, 0, s>>>(A, a.ws.val32h, z32, p032, p132, q32, st,
-                                                                         partials, 1);
+                launch_spmv_tma<NF, NBMAX>(gridTma, s, A, a.ws.val32h, z32, p032, p132, q32, st, partials, 1);
               else if (v == 2)
                 cg_spmv_half_ell<NF, NBMAX, true><<<gridP, kThreads, 0, s>>>(A, a.ws.val32h, z32, p032, p132, q32,
                                                                               st, partials, 1);
@@ -1278,9 +1418,8 @@ struct Driver {
             float* pold = (it & 1) ? p132 : p032;
             float* pnew = (it & 1) ? p032 : p132;
             tm->begin(K_SPMV32, s);
-            if (ellOk && variant == 1)
-              cg_spmv_half_warp<NF, NBMAX><<<gridW, kThreads, 0, s>>>(A, a.ws.val32h, z32, pold, pnew, q32, st,
-                                                                       partials, first ? 1 : 0);
+            if (ellOk && variant == 1 && gridTma > 0)
+              launch_spmv_tma<NF, NBMAX>(gridTma, s, A, a.ws.val32h, z32, pold, pnew, q32, st, partials, first ? 1 : 0);
             else if (ellOk && variant == 2)
               cg_spmv_half_ell<NF, NBMAX, true><<<gridP, kThreads, 0, s>>>(A, a.ws.val32h, z32, pold, pnew, q32, st,
                                                                             partials, first ? 1 : 0);

@@ -72,8 +72,9 @@ struct TraceSolveArgs {
   int* sampleCount;            // host counter
   int prepared;                // GMRES: b' and the preconditioner are already in ws (trace_prepare ran)
   // launch tuner of the FP32 half-storage operator (mixed CG): -1 not tuned yet, then the
-  // kernel chosen (0 row per lane, 1 warp per face, 2 row per lane with paired loads of transposed blocks) and their
-  // times (ms, three)
+  // kernel chosen (0 row per lane, 1 blocks staged by bulk copies, 2 row per lane with paired
+  // loads of transposed blocks, 3 the same with float4 reads of the gathered x) and their
+  // times (ms, four)
   int* spmvChoice;
   float* spmvTimes;
 };

@@ -262,13 +262,14 @@ int hfx_assembly_info(hfx_ctx* ctx, int* affine);
 int hfx_mixed_assembly_info(hfx_ctx* ctx, int* tensorCores);
 /* Launch tuner (no counterpart in the reference): the first mixed-precision CG solve on a mesh
  * times the kernels of the FP32 trace operator on the system's own values (0 row per lane,
- * 1 warp per face, 2 row per lane with paired (float2) loads of the blocks read transposed,
- * 3 the same with 16-byte loads, for Nf = 2 mod 4) and keeps the fastest for that mesh.
+ * 1 the blocks staged in shared memory by bulk copies (cp.async.bulk, for Nf even), 2 row
+ * per lane with paired (float2) loads of the blocks read transposed, 3 the same with the
+ * gathered x read back as float4s) and keeps the fastest for that mesh.
  * *spmvKernel: -1 not tuned yet, else the kernel chosen; spmvMs[4]: their measured times per
  * launch (ms; 0 for a kernel not tried). */
 int hfx_tuning_info(hfx_ctx* ctx, int* spmvKernel, float* spmvMs);
-/* Sets the choice instead: 0..3 fixes the kernel (3 only where Nf = 2 mod 4; elsewhere it runs
- * kernel 2), -1 tunes again at the next mixed solve. */
+/* Sets the choice instead: 0..3 fixes the kernel (1 only where Nf is even, elsewhere it runs
+ * kernel 0), -1 tunes again at the next mixed solve. */
 int hfx_set_tuning(hfx_ctx* ctx, int spmvKernel);
 /* Those FP32 blocks for a list of cells, [count][*stride]: volume rows [C_0..C_{d-1} | K_0..
  * K_{d-1} | M] of N values (row (k, i) = block k, node i), face rows [T | E | H] of Nf values

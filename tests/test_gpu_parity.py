@@ -234,13 +234,15 @@ def test_mixed_assembly_refuses_fp64_exports(hfx_lib):
 
 
 @pytest.mark.parametrize("kernel", [0, 1, 2, 3])
-def test_mixed_cg_both_fp32_operator_kernels(hfx_lib, kernel):
-    """Every kernel of the FP32 half-storage trace operator (row per lane, warp per face,
-    row per lane with paired loads, the same with 16-byte loads),
-    fixed through hfx_set_tuning, give the direct solution to 1e-8 with the two-level
-    mixed CG; the tuner, when left to choose, picks one of them and reports both times."""
+@pytest.mark.parametrize("dim,n,order", [(3, 3, 3), (3, 3, 2), (2, 8, 3)])
+def test_mixed_cg_both_fp32_operator_kernels(hfx_lib, kernel, dim, n, order):
+    """Every kernel of the FP32 half-storage trace operator (row per lane, blocks staged in
+    shared memory by bulk copies, row per lane with paired loads, the same with float4
+    reads of the gathered x), fixed through hfx_set_tuning, gives the direct solution to 1e-8 with the
+    two-level mixed CG at Nf = 10, 6 and 4; the tuner, when left to choose, picks one of
+    them and reports their times."""
     from hyperfox_gb300 import capi
-    P, ctx, _ = build_pair(hfx_lib, 3, 3, 3, tau2=False, kappa="cell")
+    P, ctx, _ = build_pair(hfx_lib, dim, n, order, tau2=False, kappa="cell")
     P.assemble()
     ctx.assemble()
     x_ref = P.solve_direct()
