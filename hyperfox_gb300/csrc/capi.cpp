@@ -205,6 +205,7 @@ struct hfx_ctx {
   // Chebyshev of that degree (0: no training yet, the reduction target decides)
   int learnDegree = 0;
   float spmvTimes[4] = {0.f, 0.f, 0.f, 0.f};
+  int stretchHint = 0;  // first-stretch length of the last mixed CG solve
   int coarseMaxDeg = 64;      // degree cap of the Chebyshev coarse solve (a fixed degree when target ~ 0)
   // vector Burgers (hfx_burgers_*)
   BurgersState burgers;
@@ -1892,6 +1893,7 @@ int hfx_solve(hfx_ctx* c, const hfx_solve_opts* opts, double* trace, hfx_solve_i
   a.coarse_guess = o.coarse_guess;
   a.spmvChoice = &c->spmvChoice;
   a.spmvTimes = c->spmvTimes;
+  a.stretchHint = &c->stretchHint;
   const bool learned = o.precond == HFX_PC_TWOLEVEL && o.coarse_mode == HFX_COARSE_LEARNED &&
                        !c->coarse.thetaHat.empty();
   c->coarse.useLearned = learned;

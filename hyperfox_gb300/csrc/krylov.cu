@@ -1411,8 +1411,12 @@ struct Driver {
         hst.ticket = 0;
         cudaMemcpyAsync(st, &hst, sizeof(CgState), cudaMemcpyHostToDevice, s);
         int it = totalIters;  // the ping-pong parity follows completed iterations
-        // iterations queued between host checks: about the length of the last stretch
-        const int batch = lastStretch > 0 ? std::max(3, std::min(a.check_every, lastStretch + 2)) : a.check_every;
+        // iterations queued before the host checks: one more than the last stretch took (the
+        // first stretch: one more than the first stretch of the previous solve on this system
+        // layout, else 8), then short batches. Iterations queued past the stretch's end return
+        // at entry, but each still costs its launches.
+        const int hint = a.stretchHint && *a.stretchHint > 0 ? *a.stretchHint + 1 : 8;
+        int batch = std::max(3, std::min(a.check_every, lastStretch > 0 ? lastStretch + 1 : hint));
         while (true) {
           for (int k = 0; k < batch; ++k, ++it) {
             float* pold = (it & 1) ? p132 : p032;
@@ -1452,7 +1456,9 @@ struct Driver {
           cudaMemcpyAsync(&hst, st, sizeof(CgState), cudaMemcpyDeviceToHost, s);
           cudaStreamSynchronize(s);
           if (hst.done) break;
+          batch = std::max(2, batch / 4);
         }
+        if (a.stretchHint && lastStretch == 0 && hst.iters > 0) *a.stretchHint = hst.iters;
         totalIters += hst.iters;
         lastStretch = hst.iters;
         if (hst.status != 0 && hst.status != 5) {

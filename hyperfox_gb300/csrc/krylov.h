@@ -77,6 +77,9 @@ struct TraceSolveArgs {
   // times (ms, four)
   int* spmvChoice;
   float* spmvTimes;
+  // mixed CG: iterations of the first stretch of the last solve on this context (host; 0
+  // unknown), used to size the first batch of queued iterations
+  int* stretchHint;
 };
 
 struct TraceSolveResult {
