@@ -18,8 +18,13 @@ trace right-hand side, r the true residual). With tol = rtol min_k |b_k| / |b| o
 the problems whose part b_k of b is non-zero, every problem's own relative residual is
 at most rtol: |r_k| <= |r| <= rtol min_j |b_j| <= rtol |b_k|. A problem with b_k = 0
 keeps an exactly zero trace, since every Krylov vector stays zero on its rows.
+
+The groups are independent: ``run(concurrent=True)`` drives each group from its own
+host thread on its own context (and stream), so their launches, reductions and host
+checks overlap on the GPU.
 """
 import ctypes
+import threading
 
 import numpy as np
 
@@ -133,7 +138,7 @@ class Batch:
     One context (one stream) per order present. Per step either the phases over all
     groups (``assemble()``, ``solve(rtol)``, ``recover()``, then ``results()`` for every
     problem's Trace, Solution and Flux) or ``run()``, which takes the groups one after
-    another and times each on its own stream."""
+    another, or all at once from one host thread each, and times each on its own stream."""
 
     def __init__(self, problems, device=0, src_mode=capi.SRC_NONE, src_param=0.0):
         if not problems:
@@ -204,32 +209,65 @@ class Batch:
         return {q: (alloc(g.ctx.ndofs), alloc((g.ctx.nCells, g.ctx.lenU)), alloc((g.ctx.nCells, g.ctx.lenQ)))
                 for q, g in self.groups.items()}
 
-    def run(self, rtol, bufs=None, **opts):
-        """One pass over the batch, group after group: assembly, Krylov solve and
-        recovery; with host buffers (``host_buffers()``) also the field uploads and the
-        downloads of Trace, Solution and Flux. Returns {order: device ms}, from events on
-        the group's stream around its work; a group starts after the previous one ended."""
+    def _run_group(self, q, g, rtol, bufs, opts):
         L = capi.load()
+        c = g.ctx
+        c._chk(L.hfx_mark(c.h, 0), "mark")
+        if bufs is not None:
+            g.upload()
+        c.assemble()
+        b = (None, None, None) if bufs is None else bufs[q]
+        self._solve(q, g, rtol, b[0], opts)
+        c._chk(L.hfx_recover(c.h, capi._p(b[1]), capi._p(b[2])), "recover")
+        c._chk(L.hfx_mark(c.h, 1), "mark")
+        c._chk(L.hfx_synchronize(c.h), "synchronize")
+
+    def run(self, rtol, bufs=None, concurrent=False, **opts):
+        """One pass over the batch: assembly, Krylov solve and recovery of every group;
+        with host buffers (``host_buffers()``) also the field uploads and the downloads of
+        Trace, Solution and Flux. Group after group, or with concurrent=True every group
+        from its own host thread at once. Returns {order: device ms}, from events on the
+        group's stream around its work; ``span_ms`` is then the device time from the first
+        group's start to the last group's end."""
+        L = capi.load()
+        if concurrent and len(self.groups) > 1:
+            errors = []
+
+            def work(q, g):
+                try:
+                    self._run_group(q, g, rtol, bufs, opts)
+                except Exception as e:  # reported by the calling thread
+                    errors.append(e)
+
+            threads = [threading.Thread(target=work, args=(q, g)) for q, g in self.groups.items()]
+            for t in threads:
+                t.start()
+            for t in threads:
+                t.join()
+            if errors:
+                raise errors[0]
+        else:
+            for q, g in self.groups.items():
+                self._run_group(q, g, rtol, bufs, opts)
         ms = {}
         for q, g in self.groups.items():
-            c = g.ctx
-            c._chk(L.hfx_mark(c.h, 0), "mark")
-            if bufs is not None:
-                g.upload()
-            c.assemble()
-            b = (None, None, None) if bufs is None else bufs[q]
-            self._solve(q, g, rtol, b[0], opts)
-            c._chk(L.hfx_recover(c.h, capi._p(b[1]), capi._p(b[2])), "recover")
-            c._chk(L.hfx_mark(c.h, 1), "mark")
-            c._chk(L.hfx_synchronize(c.h), "synchronize")
             t = ctypes.c_double()
-            c._chk(L.hfx_elapsed_ms(c.h, 0, 1, ctypes.byref(t)), "elapsed")
+            g.ctx._chk(L.hfx_elapsed_ms(g.ctx.h, 0, 1, ctypes.byref(t)), "elapsed")
             ms[q] = t.value
+        # span: earliest start to latest end, measured from the first group's start
+        first = next(iter(self.groups.values())).ctx
+        starts, ends = [], []
+        for g in self.groups.values():
+            for slot, out in ((0, starts), (1, ends)):
+                t = ctypes.c_double()
+                first._chk(L.hfx_elapsed_between(first.h, 0, g.ctx.h, slot, ctypes.byref(t)), "elapsed_between")
+                out.append(t.value)
+        self.span_ms = max(ends) - min(starts)
         return ms
 
-    def step(self, rtol, bufs, **opts):
+    def step(self, rtol, bufs, concurrent=False, **opts):
         """``run()`` through host buffers."""
-        return self.run(rtol, bufs, **opts)
+        return self.run(rtol, bufs, concurrent=concurrent, **opts)
 
     def results(self):
         """Per problem (in the batch's order): Trace [nFaces*Nf], Solution [nCells][N],

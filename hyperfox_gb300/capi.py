@@ -46,7 +46,7 @@ EXPORTED = [
     "hfx_coarse_loss_grad",
     "hfx_la_create", "hfx_la_destroy", "hfx_la_allocate", "hfx_la_set_values", "hfx_la_set_rhs",
     "hfx_la_zero_rows", "hfx_la_assemble", "hfx_la_clear", "hfx_la_solve", "hfx_la_nnz",
-    "hfx_profile_enable", "hfx_kernel_time", "hfx_mark", "hfx_elapsed_ms", "hfx_synchronize",
+    "hfx_profile_enable", "hfx_kernel_time", "hfx_mark", "hfx_elapsed_ms", "hfx_elapsed_between", "hfx_synchronize",
     "hfx_burgers_setup", "hfx_burgers_set_tau", "hfx_burgers_set_diffusion", "hfx_burgers_set_source",
     "hfx_burgers_set_dirichlet", "hfx_burgers_set_time_step", "hfx_burgers_set_state", "hfx_burgers_get_state",
     "hfx_burgers_begin_step", "hfx_burgers_assemble", "hfx_burgers_solve", "hfx_newton_opts_default",
@@ -179,6 +179,7 @@ def load(path=LIB_PATH):
         "hfx_kernel_time": ([vp, ip, vp, vp], ip),
         "hfx_mark": ([vp, ip], ip),
         "hfx_elapsed_ms": ([vp, ip, ip, vp], ip),
+        "hfx_elapsed_between": ([vp, ip, vp, ip, vp], ip),
         "hfx_synchronize": ([vp], ip),
         "hfx_burgers_setup": ([vp], ip),
         "hfx_burgers_set_tau": ([vp, vp, ip], ip),

@@ -2119,6 +2119,18 @@ int hfx_elapsed_ms(hfx_ctx* c, int slot0, int slot1, double* ms) {
   return HFX_OK;
 }
 
+int hfx_elapsed_between(hfx_ctx* c0, int slot0, hfx_ctx* c1, int slot1, double* ms) {
+  if (!c0 || !c1 || !ms || slot0 < 0 || slot0 >= 8 || slot1 < 0 || slot1 >= 8 || !c0->marks[slot0] ||
+      !c1->marks[slot1] || c0->device != c1->device)
+    return HFX_ERR_ARG;
+  HFX_CUDA(c0, cudaEventSynchronize(c0->marks[slot0]));
+  HFX_CUDA(c1, cudaEventSynchronize(c1->marks[slot1]));
+  float x = 0.f;
+  HFX_CUDA(c1, cudaEventElapsedTime(&x, c0->marks[slot0], c1->marks[slot1]));
+  *ms = x;
+  return HFX_OK;
+}
+
 int hfx_synchronize(hfx_ctx* c) {
   if (!c) return HFX_ERR_ARG;
   HFX_CUDA(c, cudaStreamSynchronize(c->stream));

@@ -384,6 +384,10 @@ int hfx_profile_enable(hfx_ctx* ctx, int on);
 int hfx_kernel_time(hfx_ctx* ctx, int kernel, int* launches, double* ms);
 int hfx_mark(hfx_ctx* ctx, int slot);
 int hfx_elapsed_ms(hfx_ctx* ctx, int slot0, int slot1, double* ms);
+/* Device time from mark slot0 of ctx0 to mark slot1 of ctx1 (contexts on one device; negative
+ * when the second event came first): the span of work that ran on several contexts' streams
+ * at once. */
+int hfx_elapsed_between(hfx_ctx* ctx0, int slot0, hfx_ctx* ctx1, int slot1, double* ms);
 int hfx_synchronize(hfx_ctx* ctx);
 
 /* ---- generic sparse system (LinAlgebraInterface, LinAlgebraInterface.h:23-162) ----

@@ -18,7 +18,9 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 class _StubLib:
     """Device entry points return 0; hfx_kernel_time reports 10 launches / 1.5 ms,
-    hfx_elapsed_ms 2 ms, hfx_solve 7 iterations. Host entry points are the library's."""
+    hfx_elapsed_ms 2 ms, hfx_elapsed_between 0 ms to a start mark and 2 ms to an end mark
+    (every group from 0 to 2 ms), hfx_solve 7 iterations. Host entry points are the
+    library's."""
 
     def __init__(self, real):
         self.real = real
@@ -32,6 +34,8 @@ class _StubLib:
                 a[2]._obj.value, a[3]._obj.value = 10, 1.5
             elif name == "hfx_elapsed_ms":
                 a[3]._obj.value = 2.0
+            elif name == "hfx_elapsed_between":
+                a[4]._obj.value = 2.0 if a[3] == 1 else 0.0
             elif name == "hfx_solve":
                 a[3]._obj.iterations = 7
             return 0
@@ -77,7 +81,8 @@ class _StubContext:
         pass
 
 
-def test_batch_arm_runs_on_a_stub_abi(monkeypatch):
+@pytest.mark.parametrize("serial", [False, True])
+def test_batch_arm_runs_on_a_stub_abi(monkeypatch, serial):
     import types
 
     import torch
@@ -95,17 +100,20 @@ def test_batch_arm_runs_on_a_stub_abi(monkeypatch):
                                                                       max_elements=400), cpu_budget=300,
                                                    desc="stub"))
     args = types.SimpleNamespace(config="stub", rtol=1e-8, precision="mixed", precond="twolevel", inner_rtol=1e-2,
-                                 coarse_rtol=0.3, coarse_degree=8, warmup=1, steps=2)
+                                 coarse_rtol=0.3, coarse_degree=8, warmup=1, steps=2, batch_serial=serial)
     res, B = bench.run_batch(args, 1, 0, 0)
     groups = len(B.groups)
+    assert groups > 1
     assert res["config"]["elements"] == B.nCells and res["config"]["problems"] == 12
-    # steps x groups x 2 ms of stub events per step
-    assert res["ms_per_step"] == pytest.approx(2.0 * groups)
-    assert res["value"] == pytest.approx(B.nCells / (2.0 * groups / 1e3))
+    # serial: the groups' 2 ms of stub events add up; concurrent: every group runs from 0 to
+    # 2 ms, so a step spans 2 ms
+    step = 2.0 * groups if serial else 2.0
+    assert res["ms_per_step"] == pytest.approx(step)
+    assert res["value"] == pytest.approx(B.nCells / (step / 1e3))
     for key in ("metric", "unit", "n_gpus", "steps", "warmup", "higher_is_better", "scaling", "dtype", "roofline",
                 "clocks", "e2e", "gpu_launches"):
         assert key in res, key
     assert res["roofline"]["bound"] == "hbm" and res["roofline"]["unit"] == "GB/s"
     assert res["e2e"]["h2d_bytes_per_step"] > 0 and res["e2e"]["d2h_bytes_per_step"] > 0
     assert res["gpu_launches"] == 9 * 10 * groups
-    assert set(res["group_ms"]) == {str(q) for q in B.groups}
+    assert set(res["group_ms_alone"]) == {str(q) for q in B.groups}

@@ -88,3 +88,20 @@ def test_batch_step_through_host_buffers(hfx_lib):
         assert np.array_equal(bufs[q][1][c0:c1], sol)
         assert np.array_equal(bufs[q][2][c0:c1], flux)
     B.close()
+
+
+def test_concurrent_groups_match_serial(hfx_lib):
+    """run(concurrent=True) drives every order group from its own host thread on its own
+    context and stream at once: each group computes exactly what it computes alone (the
+    same launches on its own data), so Trace, Solution and Flux are bit-identical to the
+    serial pass, and the step's span covers every group's own interval."""
+    probs, B = make(10, 11)
+    assert len(B.groups) >= 4
+    B.run(1e-10, maxits=20000)
+    serial = [tuple(a.copy() for a in r) for r in B.results()]
+    ms = B.run(1e-10, concurrent=True, maxits=20000)
+    for a, b in zip(serial, B.results()):
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
+    assert B.span_ms >= max(ms.values()) * (1 - 1e-6)
+    B.close()
