@@ -1379,6 +1379,7 @@ int hfx_test_coarse_barrier(hfx_ctx* c) {
   if (!c->coarseBuilt || !c->coarse.dev.testHold)
     return set_err(c, HFX_ERR_STATE, "test_coarse_barrier: no two-level solve has run yet");
   const int one = 1;
+  c->coarse.forceCoop = true;  // the next solve takes the cooperative kernel, whose barrier is tested
   HFX_CUDA(c, cudaMemcpyAsync(c->coarse.dev.testHold, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream));
   HFX_CUDA(c, cudaStreamSynchronize(c->stream));
   return HFX_OK;
@@ -1907,7 +1908,8 @@ int hfx_solve(hfx_ctx* c, const hfx_solve_opts* opts, double* trace, hfx_solve_i
     if (berr) {
       HFX_CUDA(c, cudaMemset(c->coarse.dev.error, 0, sizeof(int)));
       HFX_CUDA(c, cudaMemset(c->coarse.dev.barrier, 0, 2 * sizeof(unsigned)));
-      c->coarse.coopGrid = 0;  // launch-per-step coarse solve from now on
+      c->coarse.coopGrid = 0;  // one-cluster or launch-per-step coarse solve from now on
+      c->coarse.forceCoop = false;
       st = HFX_ERR_BREAKDOWN;
     }
   }

@@ -438,13 +438,23 @@ __device__ __forceinline__ void grid_barrier(unsigned* count, unsigned target, i
   __syncthreads();
 }
 
+// CLUSTER: the grid is one thread-block cluster (small coarse spaces: at most 8 CTAs of
+// 1024 threads) and the steps are separated by the hardware cluster barrier (release /
+// acquire at cluster scope, so the global writes of one step are visible to every CTA of
+// the cluster in the next; vectors written in the launch are read through L2, __ldcg).
+// Every thread reaches every barrier: the only early exit is the skip flag, which is the
+// same for all (set before the launch).
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
 // Four lanes per coarse row: the restriction splits the row's incident faces
 // and every step splits the ELL slots between them (a shuffle sum joins them),
 // which shortens each lane's chain of dependent L2 loads four-fold.
 constexpr int kCoarseLanes = 4;
-template <typename T>
-__global__ void __launch_bounds__(512) coarse_solve_coop(CoarseDev c, const T* __restrict__ r, const int* skip,
-                                                         ChebSchedule cs) {
+template <typename T, bool CLUSTER = false>
+__global__ void __launch_bounds__(CLUSTER ? 1024 : 512) coarse_solve_coop(CoarseDev c, const T* __restrict__ r,
+                                                                          const int* skip, ChebSchedule cs) {
   if (skip && *skip) return;  // the same value for every block: set before this launch
   // barrier[0] counts arrivals and starts every launch at 0: the last block to
   // leave (counted in barrier[1]) resets both, after every wait has finished
@@ -477,9 +487,12 @@ __global__ void __launch_bounds__(512) coarse_solve_coop(CoarseDev c, const T* _
   float* dk = c.cd0;
   float* dn = c.cd1;
   bool withhold = false;
-  if (c.testHold && blockIdx.x == 0 && threadIdx.x == 0) withhold = atomicExch(c.testHold, 0) != 0;
+  if (!CLUSTER && c.testHold && blockIdx.x == 0 && threadIdx.x == 0) withhold = atomicExch(c.testHold, 0) != 0;
   for (int k = 0; k < cs.degree; ++k) {
-    grid_barrier(c.barrier, (unsigned)(k + 1) * gridDim.x, c.error, k == 0 && withhold);
+    if (CLUSTER)
+      cluster_sync_all();
+    else
+      grid_barrier(c.barrier, (unsigned)(k + 1) * gridDim.x, c.error, k == 0 && withhold);
     const bool last = k + 1 == cs.degree;
     for (int64_t v = g0; v < nVr; v += groups) {
       float y = 0.f;
@@ -514,6 +527,7 @@ __global__ void __launch_bounds__(512) coarse_solve_coop(CoarseDev c, const T* _
     dk = dn;
     dn = t;
   }
+  if (CLUSTER) return;  // yc is complete at the end of the launch (kernel boundary)
   __syncthreads();
   if (threadIdx.x == 0) {
     const unsigned left = atomicAdd(c.barrier + 1, 1u) + 1u;
@@ -1016,6 +1030,15 @@ cudaError_t coarse_setup(CoarseSolver* cs, const T* S, int maxDegree, double tar
     int g = (int)std::min<int64_t>(want, (int64_t)nsm * std::min(perSM, 2));
     cs->coopGrid = std::max(g, 1);
   }
+  // small coarse spaces: one cluster of up to 8 CTAs of 1024 threads (256 rows each per pass,
+  // at most two passes per step), hardware cluster barriers between the steps
+  cs->clusterGrid = 0;
+  int clusterOk = 0;
+  cudaDeviceGetAttribute(&clusterOk, cudaDevAttrClusterLaunch, dev);
+  if (clusterOk && K <= kMaxDegree && c->nV <= 4096) {
+    const int g = (int)std::min<int64_t>(8, (c->nV + 255) / 256);
+    cs->clusterGrid = std::max(g, 1);
+  }
   cs->ready = true;
   return cudaGetLastError();
 }
@@ -1046,6 +1069,21 @@ template <typename T>
 cudaError_t coarse_apply(const CoarseSolver& cs, const T* r, const int* skip, cudaStream_t s) {
   const CoarseDev& c = cs.dev;
   const ChebSchedule sch = poly_schedule(cs);
+  if (cs.clusterGrid > 0 && !cs.forceCoop && sch.degree <= kMaxDegree) {
+    cudaLaunchConfig_t cfg{};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)cs.clusterGrid;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3((unsigned)cs.clusterGrid);
+    cfg.blockDim = dim3(1024);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, coarse_solve_coop<T, true>, c, r, skip, sch);
+  }
   if (cs.coopGrid > 0 && sch.degree <= kMaxDegree) {
     CoarseDev cv = c;
     const T* rr = r;

@@ -80,6 +80,8 @@ struct CoarseSolver {
   CoarseDev dev{};
   bool ready = false;   // operator and schedule match the assembled system
   int coopGrid = 0;     // >0: blocks of the cooperative one-launch coarse solve
+  int clusterGrid = 0;  // >0: CTAs of the one-cluster coarse solve (small coarse spaces)
+  bool forceCoop = false;  // test hook: the cooperative solve even where one cluster would do
   int degree = 0;
   double lmin = 0.0, lmax = 0.0;
   std::vector<float> c1, c2;  // Chebyshev schedule

@@ -100,9 +100,10 @@ typedef struct {
 #define HFX_OP_CONVECTION 4
 int hfx_cg_operators(hfx_ctx* ctx, int which, int precision, const double* velocity, int velLayout, double* out);
 
-/* Test hook of the failure path (no counterpart in the reference): in the next two-level
- * solve that runs the one-launch coarse solve, one block withholds its first grid-barrier
- * arrival, so the others' bounded wait (about a second) runs out; the solve must then report
+/* Test hook of the failure path (no counterpart in the reference): the next two-level solve
+ * runs the cooperative one-launch coarse solve (also where the coarse space is small enough
+ * for the one-cluster solve), one block withholds its first grid-barrier arrival, so the
+ * others' bounded wait (about a second) runs out; the solve must then report
  * info->fallback = 1 and finish with block-Jacobi CG. One shot. */
 int hfx_test_coarse_barrier(hfx_ctx* ctx);
 

@@ -134,7 +134,7 @@ def test_coarse_barrier_wait_runs_out_and_falls_back(hfx_lib, precision):
     arrival withheld (test hook) the wait runs out (about a second), the kernel sets its
     error flag and returns, the host discards the two-level iterates and block-Jacobi CG
     finishes the solve (info.fallback = 1) with the right answer; the context stays
-    usable and later solves run the launch-per-step coarse solve."""
+    usable and later solves run the one-cluster or launch-per-step coarse solve."""
     from hyperfox_gb300 import capi
     P, ctx, _ = build_pair(hfx_lib, 3, 4, 2, tau2=False, kappa="cell")
     P.assemble()
