@@ -445,6 +445,7 @@ __device__ __forceinline__ void grid_barrier(unsigned* count, unsigned target, i
 // Every thread reaches every barrier: the only early exit is the skip flag, which is the
 // same for all (set before the launch).
 __device__ __forceinline__ void cluster_sync_all() {
+  __syncwarp();  // the .aligned barrier wants the warp converged
   asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
