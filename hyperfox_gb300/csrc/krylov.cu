@@ -158,6 +158,73 @@ __device__ __forceinline__ T row_dot(const T* __restrict__ val, int64_t b0, int 
   return acc;
 }
 
+// Layout of one NF x NF block of the FP32 half storage. NF even and at least 8: 2 x 2 tiles
+// (rows 2i, 2i+1 by columns 2j, 2j+1, row-major inside the 16-byte tile), tiles in
+// column-major order; otherwise plain column-major. With tiles a lane's row of a block
+// (the stored orientation) is NF/2 8-byte pairs from NF/2 consecutive tiles, the lanes of
+// a face reading 8*NF contiguous bytes per instruction, and a lane's column (the mirrored
+// orientation) NF/2 tiles read whole, of which it keeps one column; column-major needs NF
+// scalar loads for a row and NF/2 pairs at a 4*NF-byte lane stride for a column. Measured
+// (launch tuner, 40^3x6 p=3, NF = 10): the bulk-copy kernel 0.294 ms per launch with tiles
+// against 0.318 ms column-major, the load-based kernels slower with tiles (0.355 against
+// 0.319 ms for paired loads); at NF = 6 (60^3x6 p=2) every kernel was slower with tiles
+// (best 0.58 against 0.495 ms), hence tiles only for NF >= 8. The element order of a
+// block's products does not change.
+template <int NF>
+__host__ __device__ constexpr bool tiled_blocks() {
+  return NF >= 8 && NF % 2 == 0;
+}
+template <int NF>
+__host__ __device__ __forceinline__ int hblk(int r, int c) {
+  if constexpr (tiled_blocks<NF>())
+    return 4 * ((r >> 1) + (NF / 2) * (c >> 1)) + 2 * (r & 1) + (c & 1);
+  else
+    return r + c * NF;
+}
+// v[b] = S(a, b): row a (GLOBAL: read-only global loads, else generic, e.g. shared memory)
+template <int NF, bool GLOBAL>
+__device__ __forceinline__ void blk_row(const float* blk, int a, float (&v)[NF]) {
+  if constexpr (tiled_blocks<NF>()) {
+#pragma unroll
+    for (int j = 0; j < NF / 2; ++j) {
+      const float2* p = reinterpret_cast<const float2*>(blk + 4 * ((a >> 1) + (NF / 2) * j) + 2 * (a & 1));
+      const float2 w = GLOBAL ? __ldg(p) : *p;
+      v[2 * j] = w.x;
+      v[2 * j + 1] = w.y;
+    }
+  } else {
+#pragma unroll
+    for (int b = 0; b < NF; ++b) v[b] = GLOBAL ? __ldg(blk + b * NF + a) : blk[b * NF + a];
+  }
+}
+// v[b] = S(b, a): column a
+template <int NF, bool GLOBAL>
+__device__ __forceinline__ void blk_col(const float* blk, int a, float (&v)[NF]) {
+  if constexpr (tiled_blocks<NF>()) {
+    const bool odd = a & 1;
+#pragma unroll
+    for (int i = 0; i < NF / 2; ++i) {
+      const float4* p = reinterpret_cast<const float4*>(blk + 4 * (i + (NF / 2) * (a >> 1)));
+      const float4 t = GLOBAL ? __ldg(p) : *p;
+      v[2 * i] = odd ? t.y : t.x;
+      v[2 * i + 1] = odd ? t.w : t.z;
+    }
+  } else if constexpr (NF % 2 == 0) {
+    // column-major: the lane's column is NF consecutive values, loaded as 8-byte pairs (the
+    // block starts 16-byte aligned, the column 8-byte aligned)
+#pragma unroll
+    for (int j = 0; j < NF / 2; ++j) {
+      const float2* p = reinterpret_cast<const float2*>(blk + a * NF + 2 * j);
+      const float2 w = GLOBAL ? __ldg(p) : *p;
+      v[2 * j] = w.x;
+      v[2 * j + 1] = w.y;
+    }
+  } else {
+#pragma unroll
+    for (int b = 0; b < NF; ++b) v[b] = GLOBAL ? __ldg(blk + a * NF + b) : blk[a * NF + b];
+  }
+}
+
 // Row of the face block-row from the symmetric half storage: stored blocks are
 // read by column (stride NF), mirrored ones by row (stride 1, the 400-byte block
 // comes through L1 once). All block indices are loaded first and every block's
@@ -173,11 +240,11 @@ __device__ __forceinline__ float row_dot_half(const float* __restrict__ valh, co
   for (int k = 0; k < NBMAX; ++k) {
     if (k < nb) {
       const int h = hh[k];
-      const float* blk = h >= 0 ? valh + (int64_t)h * NF * NF + a : valh + (int64_t)(-h - 1) * NF * NF + (int64_t)a * NF;
-      const int st = h >= 0 ? NF : 1;
       float v[NF];
-#pragma unroll
-      for (int b = 0; b < NF; ++b) v[b] = __ldg(blk + b * st);
+      if (h >= 0)
+        blk_row<NF, true>(valh + (int64_t)h * NF * NF, a, v);
+      else
+        blk_col<NF, true>(valh + (int64_t)(-h - 1) * NF * NF, a, v);
 #pragma unroll
       for (int b = 0; b < NF; ++b) acc = fmaf(v[b], xs[k * NF + b], acc);
     }
@@ -230,18 +297,18 @@ __global__ void __launch_bounds__(kThreads) cg_spmv_half(TraceView A, const floa
 // pairs of a face are one 8-byte load per slot at f * NBMAX + k, so no row
 // pointer has to arrive before the gather and the value loads can start; the
 // products are the same, in the same order. At most six 256-thread blocks per
-// SM keep the register count of the row-pointer version.
+// SM keep the register count of the row-pointer version (five with whole-tile loads,
+// whose values in flight need more registers).
 //
-// PAIRED: a block read transposed gives each lane NF consecutive values (its column of the
-// stored block), which are then loaded as NF/2 float2 pairs (the block's start is 16-byte
-// aligned and the column's 8-byte aligned): half the load instructions and half the L1
-// sector requests of the scalar loads, whose lanes touch one sector each.
+// PAIRED: the block values are loaded as whole pairs and tiles of the block layout (hblk:
+// with tiles NF/2 8-byte pairs for a row and NF/2 16-byte tiles for a column; column-major
+// with NF even, NF/2 pairs for a column); otherwise one scalar load per value.
 // XV: the gathered x of each block is stored with a row of NF rounded up to a multiple of
 // four and read back as float4s: a quarter of the shared-memory wavefronts of the scalar
 // reads (those wavefronts share the L1 data pipe with the value loads, which bound the
 // kernel). The products and their order do not change.
 template <int NF, int NBMAX, bool PAIRED = false, bool XV = false>
-__global__ void __launch_bounds__(kThreads, 6) cg_spmv_half_ell(TraceView A, const float* __restrict__ valh,
+__global__ void __launch_bounds__(kThreads, PAIRED && tiled_blocks<NF>() ? 5 : 6) cg_spmv_half_ell(TraceView A, const float* __restrict__ valh,
                                                                 const float* __restrict__ z,
                                                                 const float* __restrict__ pold,
                                                                 float* __restrict__ pnew, float* __restrict__ q,
@@ -277,20 +344,16 @@ __global__ void __launch_bounds__(kThreads, 6) cg_spmv_half_ell(TraceView A, con
       for (int k = 0; k < NBMAX; ++k) {
         const int h = hh[k];
         if (h != INT_MIN) {
-          const float* blk = h >= 0 ? valh + (int64_t)h * NF * NF + a : valh + (int64_t)(-h - 1) * NF * NF + (int64_t)a * NF;
-          const int sb = h >= 0 ? NF : 1;
+          const float* blk = valh + (int64_t)(h >= 0 ? h : -h - 1) * NF * NF;
           float v[NF];
-          if (PAIRED && (NF % 2 == 0) && h < 0) {
-            const float2* b2 = reinterpret_cast<const float2*>(blk);
-#pragma unroll
-            for (int b = 0; b < NF / 2; ++b) {
-              const float2 w = __ldg(b2 + b);
-              v[2 * b] = w.x;
-              v[2 * b + 1] = w.y;
-            }
+          if (PAIRED) {
+            if (h >= 0)
+              blk_row<NF, true>(blk, a, v);
+            else
+              blk_col<NF, true>(blk, a, v);
           } else {
 #pragma unroll
-            for (int b = 0; b < NF; ++b) v[b] = __ldg(blk + b * sb);
+            for (int b = 0; b < NF; ++b) v[b] = __ldg(blk + (h >= 0 ? hblk<NF>(a, b) : hblk<NF>(b, a)));
           }
           if (XV) {
             float xv[XR];
@@ -491,18 +554,10 @@ __global__ void __launch_bounds__(TmaCfg<NF, NBMAX, STAGES>::THREADS)
         if (h != INT_MIN) {
           const float* blk = buf + (slot * NBMAX + k) * C::BLK;
           float v[NF], xv[NFP];
-          if (h >= 0) {
-#pragma unroll
-            for (int b = 0; b < NF; ++b) v[b] = blk[b * NF + a];
-          } else {
-            const float2* b2 = reinterpret_cast<const float2*>(blk + a * NF);
-#pragma unroll
-            for (int b = 0; b < NF / 2; ++b) {
-              const float2 w = b2[b];
-              v[2 * b] = w.x;
-              v[2 * b + 1] = w.y;
-            }
-          }
+          if (h >= 0)
+            blk_row<NF, false>(blk, a, v);
+          else
+            blk_col<NF, false>(blk, a, v);
           const float4* x4 = reinterpret_cast<const float4*>(xs + k * NFP);
 #pragma unroll
           for (int c = 0; c < NFP / 4; ++c) {
@@ -881,7 +936,7 @@ __global__ void __launch_bounds__(kThreads) prepare_system(TraceView A, const do
           if (val32) val32[idx] = w;
           if (val32h) {
             const int h = A.hidx[b0 + k];
-            if (h >= 0) val32h[(int64_t)h * NF * NF + (int64_t)c * NF + a] = w;
+            if (h >= 0) val32h[(int64_t)h * NF * NF + hblk<NF>(a, c)] = w;
           }
         }
       }
