@@ -87,11 +87,15 @@ struct BurgersState {
   TraceWorkspace ws{};
   bool wsReady = false;
   int wsRestart = 0;
+  bool wsMixed = false;     // FP32 copies for the mixed-precision GMRES allocated
+  int wsRestart32 = 0;      // FP32 Krylov basis size
   void release() {
     wsMem.release();
     ws = TraceWorkspace{};
     wsReady = false;
     wsRestart = 0;
+    wsMixed = false;
+    wsRestart32 = 0;
     mem.release();
     tau.release();
     nu.release();
@@ -2483,8 +2487,8 @@ int hfx_burgers_assemble(hfx_ctx* c) {
 static int burgers_check_opts(hfx_ctx* c, const hfx_solve_opts& o) {
   if (o.method == HFX_KSP_CG)
     return set_err(c, HFX_ERR_ARG, "burgers_solve: the Burgers trace system is not symmetric (use GMRES)");
-  if (o.precision != HFX_PREC_FP64)
-    return set_err(c, HFX_ERR_UNSUPPORTED, "burgers_solve: FP64 GMRES only");
+  if (o.precision != HFX_PREC_FP64 && o.precision != HFX_PREC_MIXED)
+    return set_err(c, HFX_ERR_ARG, "burgers_solve: precision is HFX_PREC_FP64 or HFX_PREC_MIXED");
   if (o.precond < HFX_PC_NONE || o.precond > HFX_PC_BLOCK_JACOBI || o.rtol <= 0.0 || o.maxits <= 0)
     return set_err(c, HFX_ERR_ARG, "burgers_solve: precond none / Jacobi / block Jacobi, rtol > 0, maxits > 0");
   return HFX_OK;
@@ -2516,6 +2520,21 @@ static int burgers_solve_core(hfx_ctx* c, const hfx_solve_opts& o, TraceSolveRes
     HFX_CUDA(c, dalloc(m, &w.state, 1));
     B.wsReady = true;
   }
+  // mixed precision: FP32 GMRES on an FP32 copy of the system inside FP64 residual refinement
+  const bool mixed = o.precision == HFX_PREC_MIXED;
+  if (mixed && !B.wsMixed) {
+    HFX_CUDA(c, dalloc(m, &w.val32, (size_t)B.nnz));
+    HFX_CUDA(c, dalloc(m, &w.pc32, (size_t)c->topo.nFaces * B.NLF * B.NLF));
+    HFX_CUDA(c, dalloc(m, &w.rhs32, n));
+    HFX_CUDA(c, dalloc(m, &w.d32, n));
+    HFX_CUDA(c, dalloc(m, &w.q32, n));
+    HFX_CUDA(c, dalloc(m, &w.p032, n));
+    B.wsMixed = true;
+  }
+  if (mixed && restart > B.wsRestart32) {
+    HFX_CUDA(c, dalloc(m, &w.V32, n * (restart + 1)));
+    B.wsRestart32 = restart;
+  }
   TraceSolveArgs a{};
   a.dim = c->dim;
   a.A = TraceView{c->topo.nFaces, B.NLF, c->d_browptr, c->d_bcol, c->d_isBnd};
@@ -2523,11 +2542,13 @@ static int burgers_solve_core(hfx_ctx* c, const hfx_solve_opts& o, TraceSolveRes
   a.rhs = B.rhs;
   a.x = B.trace;
   a.precond = o.precond;
-  a.mixed = 0;
+  a.mixed = mixed ? 1 : 0;
   a.rtol = o.rtol;
-  a.inner_rtol = 1e-2;
+  // FP32 GMRES reduces the residual by inner_rtol (FP32 keeps about 1e-6 of it) between the
+  // FP64 residual replacements
+  a.inner_rtol = mixed ? std::min(std::max(o.inner_rtol, 1e-5), 0.5) : 1e-2;
   a.maxits = o.maxits;
-  a.max_refinements = 1;
+  a.max_refinements = mixed ? 100 : 1;
   a.check_every = 25;
   a.use_initial_guess = o.use_initial_guess;
   a.ws = B.ws;

@@ -566,10 +566,10 @@ int trace_gmres(const TraceSolveArgs& a, TraceSolveResult* out) {
       case 4: return drive<4, 5>(a, out);
       case 5: return drive<5, 5>(a, out);
       case 6: return drive<6, 5>(a, out);
-      // vector (Burgers) trace blocks, Nf * dim values per face: FP64 only
-      case 8: return a.mixed ? 9 : drive<8, 5>(a, out);
-      case 10: return a.mixed ? 9 : drive<10, 5>(a, out);
-      case 12: return a.mixed ? 9 : drive<12, 5>(a, out);
+      // vector (Burgers) trace blocks, Nf * dim values per face
+      case 8: return drive<8, 5>(a, out);
+      case 10: return drive<10, 5>(a, out);
+      case 12: return drive<12, 5>(a, out);
     }
   } else if (a.dim == 3) {
     switch (NF) {

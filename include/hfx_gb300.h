@@ -472,7 +472,9 @@ int hfx_burgers_begin_step(hfx_ctx* ctx);
  * (assembly + condensation + Dirichlet Set) and the scatter into the trace system. */
 int hfx_burgers_assemble(hfx_ctx* ctx);
 /* HDGSolver::solve (HDGSolver.cpp:677-779): GMRES on the trace system (PetscInterface::solve,
- * PetscInterface.cpp:222-247), Trace <- the solution, then the local recovery of Solution and Flux. */
+ * PetscInterface.cpp:222-247), Trace <- the solution, then the local recovery of Solution and Flux.
+ * opts->precision HFX_PREC_MIXED: FP32 GMRES on an FP32 copy of the system inside FP64 residual
+ * refinement (opts->inner_rtol per refinement, at least 1e-5), to the same FP64 rtol. */
 int hfx_burgers_solve(hfx_ctx* ctx, const hfx_solve_opts* opts, hfx_solve_info* info);
 /* NonLinearWrapper::solve (NonLinearWrapper.cpp:41-79) with the vanilla linearised solver and
  * residual (assemble + solve; ||Solution - BufferSolution|| / ||BufferSolution||), run on the

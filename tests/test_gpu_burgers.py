@@ -185,10 +185,12 @@ def test_newton_damped_and_capped_matches_oracle(hfx_lib):
     assert relerr(buf, P.buf) < 1e-8
 
 
-def test_time_steps_match_oracle(hfx_lib):
+@pytest.mark.parametrize("mixed", [False, True])
+def test_time_steps_match_oracle(hfx_lib, mixed):
     """Implicit Euler Burgers, nu = 1e-2, dt = 1e-3, tau = I (TestHDGBurgers.cpp:290-297),
     u0 = sin(2 pi x) sin(2 pi y) + seeded noise on both components, Dirichlet 0:
-    three steps, Newton to 1e-10 each, GPU vs oracle 1e-8 per step."""
+    three steps, Newton to 1e-10 each, GPU vs oracle 1e-8 per step; the linear solves in
+    FP64 GMRES, or (mixed) in FP32 GMRES inside FP64 residual refinement."""
     from hyperfox_gb300 import capi
     p, n = 3, 6
     re, coords, cells = mesh(2, n, p)
@@ -217,7 +219,8 @@ def test_time_steps_match_oracle(hfx_lib):
         u_next, _, its_o, _ = P.newton(res_tol=1e-10, max_iters=10)
         trace = P.trace
         B.begin_step()
-        info = B.newton(res_tol=1e-10, max_iters=10, lin_rtol=1e-13)
+        info = B.newton(res_tol=1e-10, max_iters=10, lin_rtol=1e-13,
+                        lin_precision=capi.PREC_MIXED if mixed else capi.PREC_FP64)
         assert info.status == 0 and info.iterations == its_o
         sol, _, tr_g, _ = B.get_state()
         assert relerr(sol, u_next) < 1e-8, step
