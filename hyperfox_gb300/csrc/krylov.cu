@@ -1092,15 +1092,6 @@ __global__ void accum_x(int64_t n, float* __restrict__ y, double* __restrict__ x
   }
 }
 
-// FP32 <-> FP64 vector helpers for the refinement loop.
-__global__ void scale_to_f32(int64_t n, const double* __restrict__ src, double scale, float* __restrict__ dst) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    dst[i] = (float)(src[i] * scale);
-}
-__global__ void axpy_f32_to_f64(int64_t n, double a, const float* __restrict__ d, double* __restrict__ x) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    x[i] += a * (double)d[i];
-}
 // Start of an inner FP32 CG from d = 0: r = rhs, z = M^{-1} r, r.z, r.r.
 template <int NF, int PC>
 __global__ void __launch_bounds__(kThreads) cg_start_zero_f32(int64_t nFaces, const float* __restrict__ rhs,
