@@ -2,7 +2,8 @@
 //
 // A CPU, FP64, single-file restatement of HyperFox's HDG element-local path and
 // the trace solve behind it. Only the tests, the smoke check and the bench's CPU
-// baseline load it, always as the checker; the CUDA library never links it.
+// baseline load it, always as the reference the CUDA path is compared with; the
+// CUDA library never links it.
 //
 // Every function names the HyperFox file:line it restates. The reference
 // cannot be built here (Eigen, Boost.Math, PETSc, MOAB are absent), so parity

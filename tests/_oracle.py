@@ -1,7 +1,7 @@
 """ctypes bindings of the CPU oracle (oracle/hdg_oracle.cpp).
 
-Test infrastructure only: the oracle is the checker for the CUDA path, never
-the thing measured or shipped.
+Test infrastructure only: the oracle is what the CUDA path is compared with,
+never the thing measured or shipped.
 """
 import ctypes
 import os

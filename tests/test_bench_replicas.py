@@ -68,7 +68,8 @@ def test_burgers_reference_arm_prints_its_metric():
 
 
 def test_anisotropic_lognormal_field():
-    """The configs[4] coefficient: exp(g) (I + 99 a a^T) per cell, g of standard deviation
+    """The anisotropic lognormal coefficient of the 60^3x6 p=2 workload: exp(g) (I + 99 a a^T)
+    per cell, g of standard deviation
     1.5, exactly symmetric and constant inside every cell (so the trace system is
     symmetric and the CG path applies)."""
     import numpy as np
