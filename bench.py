@@ -783,8 +783,8 @@ def run_batch(args, world, rank, local):
     # for the single-problem workloads (the coarse solve Chebyshev: no per-group training)
     prec = capi.PREC_FP64 if args.precision == "fp64" else capi.PREC_MIXED
     pc = capi.PC_TWOLEVEL if args.precond == "twolevel" else capi.PC_BLOCK_JACOBI
-    # fixed Chebyshev degree (--coarse-degree; 0: the degree coarse_rtol asks for on the union's
-    # spectrum, which spans every problem of the group and runs to the cap)
+    # fixed Chebyshev degree (--coarse-degree, default 32; 0: the degree coarse_rtol asks for on the
+    # union's spectrum: about as fast, but with fewer, costlier iterations)
     opts = dict(precision=prec, precond=pc, maxits=200000, inner_rtol=args.inner_rtol, coarse_rtol=args.coarse_rtol,
                 coarse_mode=capi.COARSE_CHEBYSHEV, coarse_degree=args.coarse_degree)
     pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
@@ -1058,9 +1058,9 @@ def main():
     ap.add_argument("--coarse-rtol", type=float, default=0.3, help="Chebyshev coarse-solve reduction target")
     ap.add_argument("--coarse", default="learned", choices=["learned", "chebyshev"],
                     help="coarse solve of the two-level preconditioner: trained polynomial or Chebyshev")
-    ap.add_argument("--coarse-degree", type=int, default=8,
-                    help="degree of the learned coarse polynomial (the batch workload: of its Chebyshev coarse "
-                         "solve, 0 = the degree --coarse-rtol asks for)")
+    ap.add_argument("--coarse-degree", type=int, default=None,
+                    help="degree of the learned coarse polynomial (default 8); the batch workload: of its "
+                         "Chebyshev coarse solve (default 32; 0 = the degree --coarse-rtol asks for)")
     ap.add_argument("--assembly-path", type=int, default=0, choices=[0, 1],
                     help="element kernel choice (hfx_set_assembly_path): 0 automatic (affine kernel, or the "
                          "tensor-core contractions in the mixed assembly), 1 quadrature on the CUDA cores")
@@ -1088,6 +1088,8 @@ def main():
     is_batch = "batch" in CONFIGS[args.config]
     if is_batch and not args.steps_given:
         args.steps = 3
+    if args.coarse_degree is None:
+        args.coarse_degree = 32 if is_batch else 8
     if is_batch and args.impl == "reference":
         if rank != 0:
             return

@@ -42,7 +42,8 @@ EXPORTED = [
     "hfx_rk_compute_solution", "hfx_set_trace", "hfx_get_state",
     "hfx_set_tau", "hfx_set_kappa", "hfx_set_source", "hfx_set_dirichlet", "hfx_set_time_scheme",
     "hfx_ip_coords", "hfx_assemble", "hfx_assemble_ex", "hfx_set_solver_type", "hfx_set_state", "hfx_set_assembly_path", "hfx_assembly_info", "hfx_get_condensed", "hfx_get_csr", "hfx_get_condensed_sample", "hfx_get_csr_rows", "hfx_mixed_assembly_info", "hfx_get_tc_blocks", "hfx_test_coarse_barrier", "hfx_cg_operators", "hfx_tuning_info", "hfx_set_tuning",
-    "hfx_solve_opts_default", "hfx_solve", "hfx_recover", "hfx_coarse_operator", "hfx_coarse_train",
+    "hfx_solve_opts_default", "hfx_solve", "hfx_recover", "hfx_coarse_operator", "hfx_coarse_bounds",
+    "hfx_coarse_train",
     "hfx_coarse_loss_grad",
     "hfx_la_create", "hfx_la_destroy", "hfx_la_allocate", "hfx_la_set_values", "hfx_la_set_rhs",
     "hfx_la_zero_rows", "hfx_la_assemble", "hfx_la_clear", "hfx_la_solve", "hfx_la_nnz",
@@ -144,6 +145,7 @@ def load(path=LIB_PATH):
         "hfx_solve": ([vp, ctypes.POINTER(SolveOpts), vp, ctypes.POINTER(SolveInfo)], ip),
         "hfx_recover": ([vp, vp, vp], ip),
         "hfx_coarse_operator": ([vp, vp, vp, vp, vp, vp, vp], ip),
+        "hfx_coarse_bounds": ([vp, vp], ip),
         "hfx_coarse_train": ([vp, ip, ip, ip, ctypes.POINTER(TrainInfo)], ip),
         "hfx_coarse_loss_grad": ([vp, ip, vp, ip, vp, vp, vp], ip),
         "hfx_set_assembly_path": ([vp, ip], ip),
@@ -580,6 +582,13 @@ class Context:
         self._chk(self.L.hfx_coarse_operator(self.h, ctypes.byref(nV), ctypes.byref(nnz), _p(rowptr), _p(col),
                                              _p(val), _p(vn)), "coarse_operator")
         return rowptr, col, val, vn
+
+    def coarse_bounds(self):
+        """Spectral bounds of D^-1 A_c: dict lmin, lmax (Chebyshev interval), ritz_min, ritz_max
+        (Lanczos), row_bound (infinity norm of D^-1/2 A_c D^-1/2)."""
+        out = (ctypes.c_double * 5)()
+        self._chk(self.L.hfx_coarse_bounds(self.h, out), "coarse_bounds")
+        return dict(zip(("lmin", "lmax", "ritz_min", "ritz_max", "row_bound"), list(out)))
 
     def assembly_info(self):
         """1 when the last FP64 assembly ran the affine element kernel, else 0."""

@@ -1640,7 +1640,7 @@ static int ensure_coarse(hfx_ctx* c, double target, int maxDeg = 64) {
     HFX_CUDA(c, dalloc(m, &d.barrier, 2));
     HFX_CUDA(c, dalloc(m, &d.error, 1));
     HFX_CUDA(c, dalloc(m, &d.testHold, 1));
-    HFX_CUDA(c, dalloc(m, &d.lanczosOut, 2 * 30 + 2));
+    HFX_CUDA(c, dalloc(m, &d.lanczosOut, 2 * 30 + 3));
     HFX_CUDA(c, cudaMemsetAsync(d.barrier, 0, 2 * sizeof(unsigned), s));
     HFX_CUDA(c, cudaMemsetAsync(d.error, 0, sizeof(int), s));
     HFX_CUDA(c, cudaMemsetAsync(d.testHold, 0, sizeof(int), s));
@@ -1973,6 +1973,22 @@ int hfx_coarse_operator(hfx_ctx* c, int* nV, int64_t* nnz, int* rowptr, int* col
   if (col) std::copy(h.col.begin(), h.col.end(), col);
   if (vertexNode) std::copy(h.vertexNode.begin(), h.vertexNode.end(), vertexNode);
   if (val) HFX_CUDA(c, cudaMemcpy(val, c->coarse.dev.val, sizeof(float) * h.col.size(), cudaMemcpyDeviceToHost));
+  return HFX_OK;
+}
+
+int hfx_coarse_bounds(hfx_ctx* c, double* out) {
+  if (!c || !out) return HFX_ERR_ARG;
+  if (!c->assembled || c->mixedMode)
+    return set_err(c, HFX_ERR_STATE, "coarse_bounds: needs a trace system assembled in FP64");
+  cudaSetDevice(c->device);
+  int rc = ensure_coarse(c, c->coarseTarget > 0.0 ? c->coarseTarget : 0.1, c->coarseMaxDeg);
+  if (rc) return rc;
+  const CoarseSolver& cs = c->coarse;
+  out[0] = cs.lmin;
+  out[1] = cs.lmax;
+  out[2] = cs.ritzMin;
+  out[3] = cs.ritzMax;
+  out[4] = cs.rowBound;
   return HFX_OK;
 }
 

@@ -333,25 +333,62 @@ __global__ void lanczos_scale(int64_t n, float* v, float s) {
     v[i] *= s;
 }
 
-// w = A v - beta v_prev; partials alpha = w . v and |w|^2 (|w - alpha v|^2 = |w|^2 - alpha^2)
+// w = A v - beta v_prev; partials alpha = w . v, |w|^2 and |v|^2. The next beta is
+// |w - alpha v| = sqrt(|w|^2 - alpha^2 (2 - |v|^2)), with the computed |v|^2: assuming
+// |v| = 1 instead multiplies the norm error of v by about (alpha / beta)^2 every step,
+// and within 15-30 steps the tridiagonal's eigenvalues leave the spectrum.
 __global__ void lanczos_apply(CoarseDev c, const float* v, const float* vprev, float beta, float* w,
                               double* partials) {
-  double a = 0.0, ww = 0.0;
+  double a = 0.0, ww = 0.0, vv = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < c.nV; i += (int64_t)gridDim.x * blockDim.x) {
     float y = c.dinv[i] > 0.f ? coarse_row_sym(c, i, v) : 0.f;
     y -= beta * vprev[i];
     w[i] = y;
-    a += (double)y * v[i];
+    const float vi = v[i];
+    a += (double)y * vi;
     ww += (double)y * y;
+    vv += (double)vi * vi;
   }
   block_partial(a, partials, 0);
   block_partial(ww, partials, 1);
+  block_partial(vv, partials, 2);
 }
 
 // v_next = (w - alpha v) / beta
 __global__ void lanczos_next(int64_t n, const float* v, float alpha, float ib, float* w) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     w[i] = (w[i] - alpha * v[i]) * ib;
+}
+
+// Absolute row sum of row v of D^{-1/2} A_c D^{-1/2} (0 for an inactive row). Its maximum
+// over the rows, the matrix's infinity norm, bounds the spectral radius from above.
+__device__ __forceinline__ double coarse_row_abs(const CoarseDev& c, int64_t v) {
+  const float dv = c.dinv[v];
+  if (!(dv > 0.f)) return 0.0;
+  double y = 0.0;
+  for (int k = c.rowptr[v]; k < c.rowptr[v + 1]; ++k) y += fabs((double)c.val[k]) * sqrt((double)c.dinv[c.col[k]]);
+  return y * sqrt((double)dv);
+}
+
+__device__ void block_max(double v, double* partials, int slot) {
+  __shared__ double red[kT / 32];
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s = fmax(s, red[w]);
+    partials[(size_t)slot * gridDim.x + blockIdx.x] = s;
+  }
+  __syncthreads();
+}
+
+// per-block maxima of the absolute row sums (slot 0)
+__global__ void coarse_row_bound(CoarseDev c, double* partials) {
+  double g = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < c.nV; i += (int64_t)gridDim.x * blockDim.x)
+    g = fmax(g, coarse_row_abs(c, i));
+  block_max(g, partials, 0);
 }
 
 
@@ -539,84 +576,169 @@ __global__ void __launch_bounds__(CLUSTER ? 1024 : 512) coarse_solve_coop(Coarse
   }
 }
 
-// The Lanczos steps of coarse_setup in one cooperative launch: the same passes with the
-// same arithmetic, the same block partition and the same block-ordered double sums as the
-// launch-per-step loop (so the same alpha, beta), but the scalars stay on the device and grid
-// barriers (bounded waits) replace the host round trips. Vectors written by other blocks are
-// read through L2 (__ldcg). out: alpha[m], beta[m], then the step count and the start norm.
-__device__ __forceinline__ double grid_sum(const double* partials, int slot) {
-  __shared__ double tot;
-  if (threadIdx.x == 0) {
-    double acc = 0.0;
-    for (unsigned b = 0; b < gridDim.x; ++b) acc += __ldcg(partials + (size_t)slot * gridDim.x + b);
-    tot = acc;
+// The Lanczos steps of coarse_setup in one cooperative launch, one grid barrier per step.
+// Step j reads w_{j-1} and v_{j-1} (written by every block in step j-1) and forms
+// v_j = (w_{j-1} - alpha_{j-1} v_{j-1}) / beta_{j-1} where it needs it, on the fly for
+// the neighbour columns of its rows; it writes its rows of v_j and
+// w_j = A v_j - beta_{j-1} v_{j-1} into the other pair of buffers, with the partial
+// sums of w_j . v_j, |w_j|^2 and |v_j|^2 (the next beta as in lanczos_apply). The partial
+// sums alternate between two sets by step parity, so a set is rewritten only after every
+// block has passed the next barrier, i.e. has read it. Vectors written by other blocks are
+// read through L2 (__ldcg). out: alpha[m], beta[m], the step count, the start norm and the
+// row-sum bound.
+
+// totals of three consecutive slots of block partials (gridDim.x values each), summed by
+// every thread of the block in the same order
+__device__ __forceinline__ void grid_sum3(const double* p, double* t0, double* t1, double* t2) {
+  __shared__ double red[3][kT / 32];
+  const unsigned g = gridDim.x;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  for (unsigned b = threadIdx.x; b < g; b += blockDim.x) {
+    a0 += __ldcg(p + b);
+    a1 += __ldcg(p + g + b);
+    a2 += __ldcg(p + 2 * g + b);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    a0 += __shfl_down_sync(0xffffffffu, a0, o);
+    a1 += __shfl_down_sync(0xffffffffu, a1, o);
+    a2 += __shfl_down_sync(0xffffffffu, a2, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = a0;
+    red[1][threadIdx.x >> 5] = a1;
+    red[2][threadIdx.x >> 5] = a2;
   }
   __syncthreads();
-  const double r = tot;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+    s0 += red[0][w];
+    s1 += red[1][w];
+    s2 += red[2][w];
+  }
+  __syncthreads();  // red is rewritten by the next call
+  *t0 = s0;
+  *t1 = s1;
+  *t2 = s2;
+}
+
+// maximum of one slot of block partials, by every thread of the block
+__device__ __forceinline__ double grid_max1(const double* p) {
+  __shared__ double red[kT / 32];
+  double a = 0.0;
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) a = fmax(a, __ldcg(p + b));
+  for (int o = 16; o > 0; o >>= 1) a = fmax(a, __shfl_down_sync(0xffffffffu, a, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = a;
+  __syncthreads();
+  double r = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmax(r, red[w]);
   __syncthreads();
   return r;
 }
 
-__global__ void __launch_bounds__(kT) lanczos_coop(CoarseDev c, int m, float* v, float* vprev, float* w,
+__device__ void block_partial3(double a, double b, double c, double* p) {
+  __shared__ double red[3][kT / 32];
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+    c += __shfl_down_sync(0xffffffffu, c, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = a;
+    red[1][threadIdx.x >> 5] = b;
+    red[2][threadIdx.x >> 5] = c;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      s0 += red[0][w];
+      s1 += red[1][w];
+      s2 += red[2][w];
+    }
+    p[blockIdx.x] = s0;
+    p[gridDim.x + blockIdx.x] = s1;
+    p[2 * gridDim.x + blockIdx.x] = s2;
+  }
+  __syncthreads();
+}
+
+// partials: 6 gridDim.x values (two sets of three slots)
+__global__ void __launch_bounds__(kT) lanczos_coop(CoarseDev c, int m, float* va, float* vb, float* wa, float* wb,
                                                    double* out) {
   unsigned nb = 0;  // barriers passed in this launch
   const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
-  double ss = 0.0;
+  double* const P0 = c.partials;
+  double* const P1 = c.partials + 3 * (size_t)gridDim.x;
+  // step -1: w = the start vector (wa), v = 0 (vb), alpha = 0, beta = its norm
+  double ss = 0.0, gmax = 0.0;
   for (int64_t i = i0; i < c.nV; i += stride) {
     uint32_t h = (uint32_t)i * 2654435761u + 12345u;
     h ^= h >> 13;
     h *= 0x5bd1e995u;
     h ^= h >> 15;
     const float x = c.dinv[i] > 0.f ? 0.5f + (float)(h & 0xffff) / 65536.f : 0.f;
-    v[i] = x;
-    vprev[i] = 0.f;
+    wa[i] = x;
+    vb[i] = 0.f;
     ss += (double)x * x;
+    gmax = fmax(gmax, coarse_row_abs(c, i));
   }
-  block_partial(ss, c.partials, 0);
+  // the start vector's sums in set 1: the first write to set 1 (step 1) follows the
+  // barrier of step 0, which every block reaches after reading them
+  block_partial(ss, P1, 0);
+  block_max(gmax, P1, 1);
   grid_barrier(c.barrier, ++nb * gridDim.x, c.error);
-  const double nrm = sqrt(grid_sum(c.partials, 0));
+  double nrm2, unused0, unused1;
+  grid_sum3(P1, &nrm2, &unused0, &unused1);  // slot 2 of set 1 is not read
+  const double nrm = sqrt(nrm2);
+  if (blockIdx.x == 0) {
+    const double g = grid_max1(P1 + gridDim.x);
+    if (threadIdx.x == 0) out[2 * m + 2] = g;
+  }
   int steps = 0;
   if (nrm > 0.0) {
-    const float sc = (float)(1.0 / nrm);
-    for (int64_t i = i0; i < c.nV; i += stride) v[i] *= sc;
-    grid_barrier(c.barrier, ++nb * gridDim.x, c.error);
-    double beta = 0.0;
+    double alpha = 0.0, beta = nrm;
+    const float *wr = wa, *vr = vb;  // w_{j-1}, v_{j-1}
+    float *wn = wb, *vn = va;        // w_j, v_j
     for (int j = 0; j < m; ++j) {
-      double a = 0.0, ww = 0.0;
-      const float fb = (float)beta;
+      const float fa = (float)alpha, ib = (float)(1.0 / beta), fb = (float)beta;
+      double a = 0.0, ww = 0.0, vv = 0.0;
       for (int64_t i = i0; i < c.nV; i += stride) {
-        float y = 0.f;
+        float y = 0.f, vi = 0.f;
         if (c.dinv[i] > 0.f) {
           const float sv = sqrtf(c.dinv[i]);
           for (int k = c.rowptr[i]; k < c.rowptr[i + 1]; ++k) {
             const int col = c.col[k];
-            y = fmaf(c.val[k] * sqrtf(c.dinv[col]), __ldcg(v + col), y);
+            const float vc = (__ldcg(wr + col) - fa * __ldcg(vr + col)) * ib;
+            y = fmaf(c.val[k] * sqrtf(c.dinv[col]), vc, y);
           }
           y *= sv;
+          vi = (__ldcg(wr + i) - fa * __ldcg(vr + i)) * ib;
         }
-        y -= fb * __ldcg(vprev + i);
-        w[i] = y;
-        a += (double)y * __ldcg(v + i);
+        y -= fb * __ldcg(vr + i);
+        wn[i] = y;
+        vn[i] = vi;
+        a += (double)y * vi;
         ww += (double)y * y;
+        vv += (double)vi * vi;
       }
-      block_partial(a, c.partials, 0);
-      block_partial(ww, c.partials, 1);
+      double* const P = (j & 1) ? P1 : P0;
+      block_partial3(a, ww, vv, P);
       grid_barrier(c.barrier, ++nb * gridDim.x, c.error);
-      const double alpha = grid_sum(c.partials, 0), wsum = grid_sum(c.partials, 1);
-      if (blockIdx.x == 0 && threadIdx.x == 0) out[j] = alpha;
+      double al, wsum, vsum;
+      grid_sum3(P, &al, &wsum, &vsum);
+      if (blockIdx.x == 0 && threadIdx.x == 0) out[j] = al;
       steps = j + 1;
-      beta = sqrt(fmax(wsum - alpha * alpha, 0.0));
-      // every block has read the partials before any block overwrites them in the next pass
-      grid_barrier(c.barrier, ++nb * gridDim.x, c.error);
-      if (j + 1 == m || beta < 1e-6 * sqrt(wsum)) break;
-      if (blockIdx.x == 0 && threadIdx.x == 0) out[m + j] = beta;
-      const float fa = (float)alpha, ib = (float)(1.0 / beta);
-      for (int64_t i = i0; i < c.nV; i += stride) w[i] = (__ldcg(w + i) - fa * __ldcg(v + i)) * ib;
-      grid_barrier(c.barrier, ++nb * gridDim.x, c.error);
-      float* t = vprev;
-      vprev = v;
-      v = w;
-      w = t;
+      // |w - alpha v| with the computed |v|^2 (lanczos_apply)
+      const double bn = sqrt(fmax(wsum - al * al * (2.0 - vsum), 0.0));
+      if (j + 1 == m || bn < 1e-6 * sqrt(wsum)) break;
+      if (blockIdx.x == 0 && threadIdx.x == 0) out[m + j] = bn;
+      alpha = al;
+      beta = bn;
+      const float *tw = wr, *tv = vr;
+      wr = wn;
+      vr = vn;
+      wn = const_cast<float*>(tw);
+      vn = const_cast<float*>(tv);
     }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -916,34 +1038,36 @@ cudaError_t coarse_setup(CoarseSolver* cs, const T* S, int maxDegree, double tar
   coarse_fill_ell<<<blocks_for((int64_t)c->ellW * c->nV), kT, 0, s>>>(*c);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  // Lanczos, m steps, on D^{-1/2} A_c D^{-1/2}; two partial sums per block fit the partials buffer
-  const unsigned g = std::min<unsigned>(blocks_for(c->nV), (152 * 32 + 64) / 2);
-  std::vector<double> hp(2 * g);
+  // Lanczos, m steps, on D^{-1/2} A_c D^{-1/2}; three partial sums per block fit the partials buffer
+  const unsigned g = std::min<unsigned>(blocks_for(c->nV), (152 * 32 + 64) / 3);
+  std::vector<double> hp(3 * g);
   float *v = c->cd0, *vprev = c->cd1, *w = c->lz;
   const int m = (int)std::min<int64_t>(30, c->nV);
   std::vector<double> al, be;
+  double rowBound = 0.0;  // infinity norm of D^{-1/2} A_c D^{-1/2}
   {
-    // one cooperative launch when every block of the loop's partition fits at once
+    // one cooperative launch (grid-stride over the rows; six partial sums per block fit the
+    // partials buffer) where the device has cooperative launches
     int dev = 0, coop = 0, nsm = 0, perSM = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (coop && c->barrier && c->lanczosOut &&
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, lanczos_coop, kT, 0) == cudaSuccess &&
-        (int64_t)perSM * nsm >= (int64_t)g) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, lanczos_coop, kT, 0) == cudaSuccess && perSM >= 1) {
+      const unsigned gc = (unsigned)std::min<int64_t>(std::min<int64_t>(g, (152 * 32 + 64) / 6), (int64_t)perSM * nsm);
       CoarseDev cv = *c;
       int mm = m;
-      float *a0 = v, *a1 = vprev, *a2 = w;
+      float *a0 = c->cd0, *a1 = c->cd1, *a2 = c->lz, *a3 = c->cr;  // cr: coarse-solve work, free here
       double* o = c->lanczosOut;
-      void* args[] = {&cv, &mm, &a0, &a1, &a2, &o};
-      std::vector<double> ho(2 * m + 2);
+      void* args[] = {&cv, &mm, &a0, &a1, &a2, &a3, &o};
+      std::vector<double> ho(2 * m + 3);
       int herr = 0;
       const bool launched =
-          cudaLaunchCooperativeKernel((const void*)lanczos_coop, dim3(g), dim3(kT), args, 0, s) == cudaSuccess;
+          cudaLaunchCooperativeKernel((const void*)lanczos_coop, dim3(gc), dim3(kT), args, 0, s) == cudaSuccess;
       if (!launched) {
         cudaGetLastError();  // not launched: the launch-per-step loop below does the steps
       } else {
-        cudaMemcpyAsync(ho.data(), c->lanczosOut, sizeof(double) * (2 * m + 2), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(ho.data(), c->lanczosOut, sizeof(double) * (2 * m + 3), cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(&herr, c->error, sizeof(int), cudaMemcpyDeviceToHost, s);
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
       }
@@ -957,6 +1081,7 @@ cudaError_t coarse_setup(CoarseSolver* cs, const T* S, int maxDegree, double tar
         }
         al.assign(ho.begin(), ho.begin() + steps);
         be.assign(ho.begin() + m, ho.begin() + m + std::max(steps - 1, 0));
+        rowBound = ho[2 * m + 2];
       } else if (launched) {
         // a barrier wait ran out: clear the flag and redo the steps one launch at a time
         cudaMemsetAsync(c->error, 0, sizeof(int), s);
@@ -965,6 +1090,11 @@ cudaError_t coarse_setup(CoarseSolver* cs, const T* S, int maxDegree, double tar
     }
   }
   if (al.empty()) {
+  coarse_row_bound<<<g, kT, 0, s>>>(*c, c->partials);
+  cudaMemcpyAsync(hp.data(), c->partials, sizeof(double) * g, cudaMemcpyDeviceToHost, s);
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+  rowBound = 0.0;
+  for (unsigned b = 0; b < g; ++b) rowBound = std::max(rowBound, hp[b]);
   cudaMemsetAsync(vprev, 0, sizeof(float) * c->nV, s);
   lanczos_init<<<g, kT, 0, s>>>(*c, v, c->partials);
   cudaMemcpyAsync(hp.data(), c->partials, sizeof(double) * g, cudaMemcpyDeviceToHost, s);
@@ -979,14 +1109,15 @@ cudaError_t coarse_setup(CoarseSolver* cs, const T* S, int maxDegree, double tar
   lanczos_scale<<<g, kT, 0, s>>>(c->nV, v, (float)(1.0 / nrm));
   double beta = 0.0;
   for (int j = 0; j < m; ++j) {
-    // one host round trip per step: alpha and |w|^2 from the same pass
+    // one host round trip per step: alpha, |w|^2 and |v|^2 from the same pass
     lanczos_apply<<<g, kT, 0, s>>>(*c, v, vprev, (float)beta, w, c->partials);
-    cudaMemcpyAsync(hp.data(), c->partials, sizeof(double) * 2 * g, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(hp.data(), c->partials, sizeof(double) * 3 * g, cudaMemcpyDeviceToHost, s);
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
     const double alpha = sum_partials(hp.data(), g);
     const double ww = sum_partials(hp.data() + g, g);
+    const double vv = sum_partials(hp.data() + 2 * g, g);
     al.push_back(alpha);
-    beta = std::sqrt(std::max(ww - alpha * alpha, 0.0));
+    beta = std::sqrt(std::max(ww - alpha * alpha * (2.0 - vv), 0.0));
     if (j + 1 == m || beta < 1e-6 * std::sqrt(ww)) break;
     be.push_back(beta);
     lanczos_next<<<g, kT, 0, s>>>(c->nV, v, (float)alpha, (float)(1.0 / beta), w);
@@ -998,9 +1129,14 @@ cudaError_t coarse_setup(CoarseSolver* cs, const T* S, int maxDegree, double tar
   be.resize(al.size() > 0 ? al.size() - 1 : 0);
   }
   const double tmin = tridiag_eig(al, be, 0), tmax = tridiag_eig(al, be, (int)al.size() - 1);
-  // upper bound must cover the spectrum (|p| <= 1 there keeps q(A_c) SPD);
-  // the lower end may be above the true minimum: modes below it are damped less
-  cs->lmax = 1.1 * tmax;
+  // upper bound must cover the spectrum (|p| <= 1 there keeps q(A_c) SPD): the largest
+  // Ritz value is below the spectral radius, the row-sum norm above it, so the margin on the
+  // Ritz value is capped by the norm; the lower end may be above the true minimum: modes
+  // below it are damped less
+  cs->ritzMin = tmin;
+  cs->ritzMax = tmax;
+  cs->rowBound = rowBound;
+  cs->lmax = rowBound > 0.0 ? std::min(1.1 * tmax, rowBound) : 1.1 * tmax;
   cs->lmin = std::max(tmin / 1.5, cs->lmax * 1e-6);
   const double th = 0.5 * (cs->lmax + cs->lmin), de = 0.5 * (cs->lmax - cs->lmin);
   const double sig = th / de;

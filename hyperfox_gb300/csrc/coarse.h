@@ -65,7 +65,7 @@ struct CoarseDev {
   unsigned* barrier;    // [2] grid barrier of the one-launch coarse solve: count, generation
   int* error;           // set when a grid barrier wait ran out (the solve is then invalid)
   int* testHold;        // test hook, one shot: block 0 withholds its first barrier arrival
-  double* lanczosOut;   // [2*30+2] alpha, beta, step count and start norm of the one-launch Lanczos
+  double* lanczosOut;   // [2*30+3] alpha, beta, step count, start norm and row-sum bound of the one-launch Lanczos
 };
 
 // Coarse solver state: device view plus the polynomial schedule. Both coarse
@@ -84,6 +84,9 @@ struct CoarseSolver {
   bool forceCoop = false;  // test hook: the cooperative solve even where one cluster would do
   int degree = 0;
   double lmin = 0.0, lmax = 0.0;
+  // of D^{-1/2} A_c D^{-1/2}: extreme Ritz values of the Lanczos steps (inside the spectrum)
+  // and the infinity norm (above the spectral radius)
+  double ritzMin = 0.0, ritzMax = 0.0, rowBound = 0.0;
   std::vector<float> c1, c2;  // Chebyshev schedule
   // learned polynomial: weights scaled by lmax (theta_k = thetaHat_k / lmax), so
   // that a trained schedule carries over to a re-assembled operator

@@ -346,6 +346,12 @@ int hfx_recover(hfx_ctx* ctx, double* solution, double* flux);
  * interior block of the trace system, in CSR (rowptr[nV+1], col/val[nnz],
  * FP32). Call with rowptr == NULL for the sizes. Needs an assembled system. */
 int hfx_coarse_operator(hfx_ctx* ctx, int* nV, int64_t* nnz, int* rowptr, int* col, float* val, int* vertexNode);
+/* Spectral bounds of D^{-1} A_c (D its diagonal) behind the Chebyshev coarse solve of
+ * HFX_PC_TWOLEVEL (no counterpart in the reference), set up like hfx_coarse_operator:
+ * out[5] = lmin, lmax (the Chebyshev interval), the smallest and largest Ritz values of
+ * the Lanczos steps (inside the spectrum) and the infinity norm of D^{-1/2} A_c D^{-1/2}
+ * (above the spectral radius); lmax = min(1.1 * largest Ritz value, that norm). */
+int hfx_coarse_bounds(hfx_ctx* ctx, double* out);
 
 /* Learned coarse correction (no counterpart in the reference). The coarse solve
  * of HFX_PC_TWOLEVEL becomes a degree-K polynomial in D^{-1} A_c, Richardson

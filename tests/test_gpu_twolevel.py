@@ -66,6 +66,74 @@ def test_coarse_operator_is_galerkin_product(hfx_lib, dim, n, order, tau2):
     assert np.abs(R[~mask]).max(initial=0.0) <= 1e-12 * np.abs(R).max()
 
 
+def scaled_coarse(ctx):
+    """D^-1/2 A_c D^-1/2 on the rows with a positive diagonal, FP64 from the exported FP32 values."""
+    rowptr, col, val, vn = ctx.coarse_operator()
+    nV = len(vn)
+    A = sp.csr_matrix((val.astype(np.float64), col, rowptr), shape=(nV, nV))
+    d = A.diagonal()
+    act = d > 0
+    s = np.zeros(nV)
+    s[act] = 1.0 / np.sqrt(d[act])
+    return (sp.diags(s) @ A @ sp.diags(s)).tocsr()[act][:, act]
+
+
+def bounds_case(hfx_lib, case):
+    from hyperfox_gb300 import batch, capi, meshgen
+    if case == "cube":
+        _, ctx, _ = build_pair(hfx_lib, 3, 6, 2, tau2=False, kappa="cell")
+        return ctx, None
+    if case == "union":
+        # one group of 24 small problems (one order, lognormal kappa per cell): a union of
+        # spectra, where the Lanczos bounds first went wrong
+        probs = batch.uneven_batch(count=24, seed=4, min_elements=200, max_elements=2000, orders=(2,))
+        B = batch.Batch(probs, 0, capi.SRC_SINPROD, 2 * np.pi ** 2)
+        return next(iter(B.groups.values())).ctx, B
+    # 720,000 triangles p = 1: several coarse rows per thread of the Lanczos launch
+    re = capi.refel(2, 1)
+    v, s = meshgen.square_simplices(600)
+    coords, cells = meshgen.high_order(v, s, re["nodes"])
+    ctx = capi.Context(0)
+    ctx.upload_mesh(2, 1, coords, cells)
+    _, _, faces, _ = ctx.topology()
+    ctx.set_source(capi.SRC_SINPROD, param=2 * np.pi ** 2)
+    ctx.set_dirichlet(np.prod(np.sin(np.pi * coords[faces]), axis=-1))
+    return ctx, None
+
+
+@pytest.mark.parametrize("case", ["cube", "union", "large"])
+def test_coarse_bounds_bracket_the_spectrum(hfx_lib, case):
+    """The Chebyshev interval of the coarse solve comes from 30 FP32 Lanczos steps on
+    D^-1/2 A_c D^-1/2. Its Ritz values must lie inside the operator's spectrum (scipy, FP64
+    on the exported operator), the largest within 10% of the spectral radius, and lmax must
+    cover the spectrum. (A Lanczos whose next beta assumed a unit Krylov vector let the
+    vector's norm error grow about four-fold per step: Ritz values of -0.68, and of 2.5
+    times the spectral radius, on such unions.)"""
+    import scipy.sparse.linalg as sla
+    ctx, keep = bounds_case(hfx_lib, case)
+    ctx.assemble()
+    b = ctx.coarse_bounds()
+    S = scaled_coarse(ctx)
+    lmax = sla.eigsh(S, k=1, which="LA", tol=1e-10, return_eigenvectors=False)[0]
+    assert b["ritz_max"] <= lmax * (1 + 1e-4), (b, lmax)
+    assert b["ritz_max"] >= 0.9 * lmax, (b, lmax)
+    assert b["row_bound"] >= lmax * (1 - 1e-5), (b, lmax)
+    assert b["lmax"] >= lmax * (1 - 1e-4), (b, lmax)
+    assert 0 < b["lmin"] < b["lmax"]
+    assert b["ritz_min"] > 0, b
+    if S.shape[0] <= 60000:
+        lmin = sla.eigsh(S.tocsc(), k=1, sigma=0, which="LM", return_eigenvectors=False)[0]
+        assert b["ritz_min"] >= lmin * (1 - 1e-3), (b, lmin)
+    # the two-level solve on these bounds converges
+    from hyperfox_gb300 import capi
+    _, info = ctx.solve(precision=1, rtol=1e-8, precond=capi.PC_TWOLEVEL, maxits=200000)
+    assert info.status == 0 and info.fallback == 0
+    if keep is not None:
+        keep.close()
+    else:
+        ctx.close()
+
+
 @pytest.mark.parametrize("dim,n,order", [(2, 8, 2), (2, 6, 3), (3, 3, 2), (3, 2, 3)])
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("coarse_guess", [0, 1])
