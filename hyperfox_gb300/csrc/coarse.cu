@@ -581,7 +581,9 @@ __global__ void __launch_bounds__(CLUSTER ? 1024 : 512) coarse_solve_coop(Coarse
 // v_j = (w_{j-1} - alpha_{j-1} v_{j-1}) / beta_{j-1} where it needs it, on the fly for
 // the neighbour columns of its rows; it writes its rows of v_j and
 // w_j = A v_j - beta_{j-1} v_{j-1} into the other pair of buffers, with the partial
-// sums of w_j . v_j, |w_j|^2 and |v_j|^2 (the next beta as in lanczos_apply). The partial
+// sums of w_j . v_j, |w_j|^2 and |v_j|^2 (the next beta as in lanczos_apply). The
+// vectors are stored times D^{-1/2} (A here is D^{-1/2} A_c D^{-1/2}), so a row gathers
+// its neighbours' stored values and multiplies the ELL row of A_c by them. The partial
 // sums alternate between two sets by step parity, so a set is rewritten only after every
 // block has passed the next barrier, i.e. has read it. Vectors written by other blocks are
 // read through L2 (__ldcg). out: alpha[m], beta[m], the step count, the start norm and the
@@ -677,7 +679,7 @@ __global__ void __launch_bounds__(kT) lanczos_coop(CoarseDev c, int m, float* va
     h *= 0x5bd1e995u;
     h ^= h >> 15;
     const float x = c.dinv[i] > 0.f ? 0.5f + (float)(h & 0xffff) / 65536.f : 0.f;
-    wa[i] = x;
+    wa[i] = x * sqrtf(c.dinv[i]);
     vb[i] = 0.f;
     ss += (double)x * x;
     gmax = fmax(gmax, coarse_row_abs(c, i));
@@ -703,20 +705,36 @@ __global__ void __launch_bounds__(kT) lanczos_coop(CoarseDev c, int m, float* va
       const float fa = (float)alpha, ib = (float)(1.0 / beta), fb = (float)beta;
       double a = 0.0, ww = 0.0, vv = 0.0;
       for (int64_t i = i0; i < c.nV; i += stride) {
-        float y = 0.f, vi = 0.f;
+        float y = 0.f, vi = 0.f, vti = 0.f, si = 0.f;
         if (c.dinv[i] > 0.f) {
-          const float sv = sqrtf(c.dinv[i]);
-          for (int k = c.rowptr[i]; k < c.rowptr[i + 1]; ++k) {
-            const int col = c.col[k];
-            const float vc = (__ldcg(wr + col) - fa * __ldcg(vr + col)) * ib;
-            y = fmaf(c.val[k] * sqrtf(c.dinv[col]), vc, y);
+          si = sqrtf(c.dinv[i]);
+          // the row from the ELL copy, eight neighbours' loads in flight at a time
+          const int W = c.ellW;
+          int k = 0;
+          for (; k + 8 <= W; k += 8) {
+            int cc[8];
+            float aa[8], xx[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              cc[u] = c.ellCol[(int64_t)(k + u) * c.nV + i];
+              aa[u] = c.ellVal[(int64_t)(k + u) * c.nV + i];
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) xx[u] = (__ldcg(wr + cc[u]) - fa * __ldcg(vr + cc[u])) * ib;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) y = fmaf(aa[u], xx[u], y);
           }
-          y *= sv;
-          vi = (__ldcg(wr + i) - fa * __ldcg(vr + i)) * ib;
+          for (; k < W; ++k) {
+            const int cc = c.ellCol[(int64_t)k * c.nV + i];
+            y = fmaf(c.ellVal[(int64_t)k * c.nV + i], (__ldcg(wr + cc) - fa * __ldcg(vr + cc)) * ib, y);
+          }
+          const float is = 1.f / si;
+          vti = (__ldcg(wr + i) - fa * __ldcg(vr + i)) * ib;
+          vi = vti * is;
+          y = y * si - fb * (__ldcg(vr + i) * is);
         }
-        y -= fb * __ldcg(vr + i);
-        wn[i] = y;
-        vn[i] = vi;
+        wn[i] = y * si;
+        vn[i] = vti;
         a += (double)y * vi;
         ww += (double)y * y;
         vv += (double)vi * vi;
