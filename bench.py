@@ -337,11 +337,20 @@ def run_ours(args, world, rank, local):
         step_e2e()
     barrier(world)
     ctx._chk(L.hfx_synchronize(ctx.h), "sync")
+    e2e_clocks = ClockSampler(local)
+    e2e_clocks.start()
     t0 = time.perf_counter()
+    ctx._chk(L.hfx_mark(ctx.h, 6), "mark")
     for _ in range(args.steps):
         step_e2e()
+    ctx._chk(L.hfx_mark(ctx.h, 7), "mark")
     ctx._chk(L.hfx_synchronize(ctx.h), "sync")
     e2e_s = barrier_max(world, time.perf_counter() - t0)
+    e2e_clk = e2e_clocks.stop()
+    # the same region on the device clock (events on the library's stream): the copies
+    # and the step's kernels, without the host time before the first and after the last
+    e2e_dev = capi.ctypes.c_double()
+    ctx._chk(L.hfx_elapsed_ms(ctx.h, 6, 7, capi.ctypes.byref(e2e_dev)), "elapsed")
     h2d = tau_h.nbytes + dir_h.nbytes
     d2h = trace_h.nbytes + sol_h.nbytes + flux_h.nbytes
     # plain FP64 GPU time-to-solve (same tolerance), for the learned+mixed vs plain comparison
@@ -534,6 +543,8 @@ def run_ours(args, world, rank, local):
         "roofline": roof,
         "roofline_hbm": roof_hbm,
         "clocks": clk,
+        "e2e_clocks": e2e_clk,
+        "e2e_device_ms_per_step": e2e_dev.value / args.steps,
         "e2e": {"value": E * args.steps / e2e_s, "unit": "elements/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(sum(v[0] for v in kt.values())),
