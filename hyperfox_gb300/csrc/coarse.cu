@@ -623,6 +623,20 @@ __device__ __forceinline__ void grid_sum3(const double* p, double* t0, double* t
   *t2 = s2;
 }
 
+// total of one slot of block partials, by every thread of the block
+__device__ __forceinline__ double grid_sum1(const double* p) {
+  __shared__ double red[kT / 32];
+  double a = 0.0;
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) a += __ldcg(p + b);
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = a;
+  __syncthreads();
+  double r = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r += red[w];
+  __syncthreads();
+  return r;
+}
+
 // maximum of one slot of block partials, by every thread of the block
 __device__ __forceinline__ double grid_max1(const double* p) {
   __shared__ double red[kT / 32];
@@ -689,9 +703,7 @@ __global__ void __launch_bounds__(kT) lanczos_coop(CoarseDev c, int m, float* va
   block_partial(ss, P1, 0);
   block_max(gmax, P1, 1);
   grid_barrier(c.barrier, ++nb * gridDim.x, c.error);
-  double nrm2, unused0, unused1;
-  grid_sum3(P1, &nrm2, &unused0, &unused1);  // slot 2 of set 1 is not read
-  const double nrm = sqrt(nrm2);
+  const double nrm = sqrt(grid_sum1(P1));
   if (blockIdx.x == 0) {
     const double g = grid_max1(P1 + gridDim.x);
     if (threadIdx.x == 0) out[2 * m + 2] = g;
